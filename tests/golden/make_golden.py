@@ -1,0 +1,134 @@
+"""Generate the golden fixtures in this directory.
+
+Runs the reference's own Python layer (``miepy`` from the reference tree,
+unmodified) on top of the CPU oracle registered as ``miepy.cpp``, and stores
+inputs and outputs of the sphere-cluster path as small ``.npz`` files.  The GPU
+parity tests compare the product against these fixtures without needing the
+reference tree at run time.
+
+Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle.refshim import import_reference  # noqa: E402
+
+nm = 1e-9
+
+
+def cluster_record(miepy, name, cluster, store_matrix=False, field_pts=None):
+    c = cluster
+    md = c.material_data
+    rec = dict(
+        position=c.position, radius=c.radius, wavelength=np.float64(c.wavelength), lmax=np.int64(c.lmax),
+        eps=np.asarray(md.eps, complex), mu=np.asarray(md.mu, complex), n=np.asarray(md.n, complex),
+        eps_b=np.complex128(md.eps_b), mu_b=np.complex128(md.mu_b), k_b=np.float64(np.real(md.k_b)),
+        mie_scat=c.mie_scat, mie_int=c.mie_int, p_src=c.p_src, p_inc=c.p_inc, p_scat=c.p_scat, p_int=c.p_int,
+    )
+    C = c.cross_sections()
+    rec["cross_sections"] = np.array([C.scattering, C.absorption, C.extinction], dtype=float)
+    per = np.array([[np.asarray(v) for v in c.cross_sections_per_multipole_of_particle(i)]
+                    for i in range(c.Nparticles)], dtype=float)   # [N, 3, 2, lmax]
+    rec["cross_sections_per_multipole"] = per
+    rec["force"] = c.force()
+    rec["torque"] = c.torque()
+    rec["force_nosource"] = c.force(source=False)
+    if store_matrix:
+        rec["agg_tmatrix"] = miepy.interactions.sphere_aggregate_tmatrix(c.position, c.mie_scat, md.k_b)
+    if field_pts is not None:
+        x, y, z = field_pts
+        rec["field_x"], rec["field_y"], rec["field_z"] = x, y, z
+        rec["E_total"] = c.E_field(x, y, z)
+        rec["E_scat_only"] = c.E_field(x, y, z, source=False, interior=False)
+        rec["H_total"] = c.H_field(x, y, z)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print("wrote", name, {k: np.shape(v) for k, v in rec.items() if np.ndim(v) > 1})
+
+
+def random_positions(rng, N, rmin, rmax, box):
+    pos, rad = [], []
+    tries = 0
+    while len(pos) < N:
+        tries += 1
+        if tries > 10**6:
+            raise RuntimeError("rejection sampling failed")
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(0, box, size=3)
+        if all(np.linalg.norm(c - p) > r + q for p, q in zip(pos, rad)):
+            pos.append(c)
+            rad.append(r)
+    return np.array(pos), np.array(rad)
+
+
+def main():
+    miepy = import_reference()
+    # dimer: radius 75 nm, n = 0.2+3.0i, centres (+-100 nm, 0, 0), water, x-polarised plane
+    # wave along +z, 600 nm, lmax 6
+    mat = miepy.constant_material(index=0.2 + 3.0j)
+    water = miepy.materials.water()
+    src_x = miepy.sources.plane_wave.from_string(polarization="x")
+    pts = (np.array([0.0, 0.0, 150 * nm, -60 * nm, 300 * nm, 100 * nm]),
+           np.array([0.0, 50 * nm, 0.0, 10 * nm, 200 * nm, 0.0]),
+           np.array([0.0, 0.0, 40 * nm, 20 * nm, -100 * nm, 10 * nm]))
+    kw = dict(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm, material=mat, source=src_x,
+              wavelength=600 * nm, lmax=6, medium=water)
+    cluster_record(miepy, "dimer_lmax6_exact", miepy.sphere_cluster(**kw, method=miepy.solver.exact),
+                   store_matrix=True, field_pts=pts)
+    cluster_record(miepy, "dimer_lmax6_bicgstab", miepy.sphere_cluster(**kw))
+
+    # five Ag spheres, rhc, lmax 2 (the reference's multi-particle BiCGSTAB case)
+    Ag = miepy.materials.Ag()
+    src_rhc = miepy.sources.plane_wave.from_string(polarization="rhc")
+    five = [[0, 0, 0], [250 * nm, 0, 0], [-250 * nm, 0, 0], [0, 250 * nm, 0], [0, -250 * nm, 0]]
+    for meth, tag in ((miepy.solver.exact, "exact"), (None, "bicgstab")):
+        cluster_record(miepy, f"ag5_lmax2_{tag}",
+                       miepy.sphere_cluster(position=five, radius=75 * nm, material=Ag, source=src_rhc,
+                                            wavelength=600 * nm, lmax=2, method=meth),
+                       store_matrix=(tag == "exact"))
+
+    # random cluster: 12 spheres, radii 50-100 nm in a 1 um cube, n = 1.5+0.01i, lmax 3, vacuum,
+    # y-polarised; and 6 spheres at lmax 8 (largest mode set)
+    rng = np.random.default_rng(7)
+    pos, rad = random_positions(rng, 12, 50 * nm, 100 * nm, 1000 * nm)
+    diel = miepy.constant_material(index=1.5 + 0.01j)
+    src_y = miepy.sources.plane_wave.from_string(polarization="y")
+    cluster_record(miepy, "rand12_lmax3_exact",
+                   miepy.sphere_cluster(position=pos, radius=rad, material=diel, source=src_y,
+                                        wavelength=600 * nm, lmax=3, method=miepy.solver.exact),
+                   field_pts=pts)
+    pos, rad = random_positions(rng, 4, 50 * nm, 100 * nm, 800 * nm)
+    cluster_record(miepy, "rand4_lmax8_exact",
+                   miepy.sphere_cluster(position=pos, radius=rad, material=diel, source=src_x,
+                                        wavelength=700 * nm, lmax=8, method=miepy.solver.exact))
+
+    # Drude sphere pair (the wavelength-sweep material): eps = 9 - wp^2/(w^2 + i g w),
+    # hbar wp = 9.0 eV, hbar g = 0.07 eV
+    def drude(wav):
+        w = 1239.84193e-9 / wav
+        return 9.0 - 9.0**2 / (w**2 + 1j * 0.07 * w)
+
+    dm = miepy.function_material(drude)
+    for wav in (450 * nm, 800 * nm):
+        cluster_record(miepy, f"drude2_lmax4_{int(round(wav / nm))}nm_exact",
+                       miepy.sphere_cluster(position=[[0, 0, -90 * nm], [30 * nm, 20 * nm, 90 * nm]],
+                                            radius=[60 * nm, 70 * nm], material=dm, source=src_x,
+                                            wavelength=wav, lmax=4, method=miepy.solver.exact))
+
+    # special-function tables for the device recurrences
+    from oracle import oracle as O
+    z = np.linspace(-0.999, 0.999, 23)
+    leg = np.array([O.associated_legendre_recursion(17, zz) for zz in z])
+    x = np.linspace(0.05, 40.0, 29)
+    hn = np.array([O.spherical_hn_recursion(17, xx) for xx in x])
+    np.savez_compressed(os.path.join(HERE, "special_tables.npz"), legendre_z=z, legendre=leg, hn_x=x, hn=hn)
+    print("wrote special_tables")
+
+
+if __name__ == "__main__":
+    main()
