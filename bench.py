@@ -1,0 +1,355 @@
+"""Benchmark: cluster solves per second on the random-cluster workload.
+
+Workload (the metric's configuration): N = 200 non-overlapping spheres, radii
+uniform in 50-100 nm, seeded rejection sampling (seed 2) in a 2 um cube,
+index 1.5+0.01i, vacuum, lambda = 600 nm, lmax = 4 (D = 9600), two right-hand
+sides (x- and y-polarised plane waves along +z).  A step is one complete cluster
+solve: assembly of the interaction matrix, BiCGSTAB for both polarisations to a
+relative residual of 1e-8, and the epilogue (p_scat, p_int, per-multipole
+cross-sections, force and torque of every particle).
+
+  value : mixed-precision solves/s with inputs resident in HBM
+  e2e   : the same solve through the public batch API from host buffers, with the
+          host->device copy of the inputs and the device->host copy of the results
+          inside the timed region
+The FP64 (plain complex128) path is timed in the same run (``fp64_solves_per_s``)
+and the C_ext error of the mixed path against it is reported.
+
+--impl reference times the CPU path of the reference (its C++ algorithm as
+restated by the oracle, OpenMP over all host cores) on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NM = 1e-9
+TOL = 1e-8
+WORKLOAD = "random cluster N=200 lmax=4 R=2 (D=9600), n=1.5+0.01i, vacuum, 600 nm, seed 2"
+
+
+# ---------------------------------------------------------------- workload --
+def random_cluster(seed=2, N=200, rmin=50 * NM, rmax=100 * NM, box=2000 * NM):
+    rng = np.random.default_rng(seed)
+    pos, rad = [], []
+    tries = 0
+    while len(pos) < N:
+        tries += 1
+        if tries > 10 ** 6:
+            raise RuntimeError("rejection sampling failed")
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(0, box, size=3)
+        if all(np.linalg.norm(c - p) > r + q for p, q in zip(pos, rad)):
+            pos.append(c)
+            rad.append(r)
+    return np.array(pos), np.array(rad)
+
+
+def workload_inputs():
+    import miepy_gb300 as gb
+    pos, rad = random_cluster()
+    mat = gb.constant_material(index=1.5 + 0.01j)
+    md = gb.material_struct([mat] * len(rad), gb.constant_material(eps=1.0, mu=1.0), wavelength=600 * NM)
+    lmax = 4
+    mie_scat, mie_int = gb.mie_coefficients(rad, md.eps, md.mu, md.eps_b, md.mu_b, md.k_b, lmax)
+    srcs = [gb.plane_wave.from_string("x"), gb.plane_wave.from_string("y")]
+    p_src = np.stack([s.structure(pos, md.k_b, lmax) for s in srcs], axis=-1)   # [N, 2, rmax, 2]
+    return dict(position=pos, radius=rad, mie_scat=mie_scat, mie_int=mie_int, k=float(np.real(md.k_b)),
+                p_src=np.ascontiguousarray(p_src), eps_b=float(np.real(md.eps_b)), lmax=lmax)
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm_, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm_)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- GPU arm --
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import miepy_gb300 as gb
+    from miepy_gb300.engine import ClusterBatch
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    W = workload_inputs()
+    spec = dict(position=W["position"], mie_scat=W["mie_scat"], mie_int=W["mie_int"], k=W["k"], p_src=W["p_src"])
+    N, lmax = W["position"].shape[0], W["lmax"]
+    R = 2
+    stream = torch.cuda.current_stream()
+
+    def one_solve(batch, precision):
+        batch.assemble()
+        batch.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8, precision=precision)
+        batch.epilogue(W["eps_b"])
+
+    # ---- resident inputs
+    batches = {p: ClusterBatch([spec], R=R, precision=p, device=dev) for p in ("mixed", "fp64")}
+    for p, b in batches.items():
+        for _ in range(args.warmup):
+            one_solve(b, p)
+    torch.cuda.synchronize()
+
+    def timed(precision, steps):
+        b = batches[precision]
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        evs[0].record(stream)
+        for s in range(steps):
+            one_solve(b, precision)
+            evs[s + 1].record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        per = np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(steps)])
+        return evs[0].elapsed_time(evs[-1]) / 1e3, per
+
+    clocks = ClockSampler(dev.index).start()
+    t_mixed, per_mixed = timed("mixed", args.steps)
+    clocks_info = clocks.stop()
+    t_fp64, per_fp64 = timed("fp64", max(3, args.steps // 2))
+
+    # accuracy of the mixed path against FP64, C_ext per polarisation
+    def cext(b):
+        xs = b.xs[: N * R * 6 * lmax].view(N, R, 3, 2, lmax).sum(dim=(0, 3, 4))
+        return xs[:, 2].cpu().numpy()
+
+    one_solve(batches["mixed"], "mixed")
+    one_solve(batches["fp64"], "fp64")
+    ce_m, ce_d = cext(batches["mixed"]), cext(batches["fp64"])
+    cext_err = float(np.max(np.abs(ce_m - ce_d) / np.abs(ce_d)))
+    iters_fp64 = batches["fp64"].iters.tolist()
+    iters_mixed = batches["mixed"].iters.tolist()
+
+    # ---- dominant kernel: one packed-operator product (c64, as in the mixed inner solve)
+    b = batches["mixed"]
+    x = torch.randn(b.totals["vec"], dtype=torch.complex128, device=dev)
+    for _ in range(3):
+        b.apply(x, "fp32")
+    torch.cuda.synchronize()
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.apply(x, "fp32")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_apply64 = e0.elapsed_time(e1) / 1e3 / reps
+    e0.record(stream)
+    for _ in range(reps):
+        b.apply(x, "fp64")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_apply128 = e0.elapsed_time(e1) / 1e3 / reps
+    P = N * (N - 1) // 2
+    B = 2 * lmax * (lmax + 2)
+    mat_bytes_64 = P * B * B * 8
+    mat_bytes_128 = P * B * B * 16
+    peak, peak_kind = peaks()
+
+    # ---- end to end from host buffers through the public batch API
+    host = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v) for k, v in spec.items()}
+
+    def e2e_step():
+        bb = ClusterBatch([host], R=R, precision="mixed", device=dev)
+        one_solve(bb, "mixed")
+        out = [bb.x.cpu(), bb.xs.cpu(), bb.F.cpu(), bb.T.cpu()]
+        return bb, out
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        bb, out = e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = e0.elapsed_time(e1) / 1e3
+    h2d = bb.h2d_bytes
+    d2h = sum(o.numel() * o.element_size() for o in out)
+
+    ts = np.array([t_mixed, t_fp64, t_e2e])
+    if world > 1:
+        tt = torch.tensor(ts, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ts = tt.cpu().numpy()
+    t_mixed, t_fp64, t_e2e = ts
+    res = dict(
+        value=world * args.steps / t_mixed,
+        ms_per_step=1e3 * t_mixed / args.steps,
+        p50_ms=float(np.percentile(per_mixed, 50)), p99_ms=float(np.percentile(per_mixed, 99)),
+        fp64_solves_per_s=world * max(3, args.steps // 2) / t_fp64,
+        fp64_p50_ms=float(np.percentile(per_fp64, 50)), fp64_p99_ms=float(np.percentile(per_fp64, 99)),
+        cext_rel_err_mixed_vs_fp64=cext_err, iterations_fp64=iters_fp64, refinement_passes_mixed=iters_mixed,
+        e2e=dict(value=world * e2e_steps / t_e2e, unit="solves/s", h2d_bytes_per_step=int(h2d),
+                 d2h_bytes_per_step=int(d2h)),
+        roofline=dict(bound="hbm", achieved=mat_bytes_64 / t_apply64 / 1e9, peak=peak, unit="GB/s",
+                      frac=mat_bytes_64 / t_apply64 / 1e9 / peak, traffic=None,
+                      kernel="packed c64 operator product (k_yprep + k_pgemv + k_reduce)",
+                      peak_source=peak_kind, ms_per_launch=1e3 * t_apply64),
+        fp64_operator=dict(achieved_gbs=mat_bytes_128 / t_apply128 / 1e9, ms_per_launch=1e3 * t_apply128),
+        clocks=clocks_info,
+    )
+    return res
+
+
+# ---------------------------------------------------------- CPU baseline --
+def run_cpu_sample(threads=None):
+    """One full cluster solve on the host cores with the oracle (OpenMP)."""
+    from oracle import oracle as O
+    W = workload_inputs()
+    if threads:
+        O.set_num_threads(threads)
+    n_thr = O.num_threads()
+    N, lmax = W["position"].shape[0], W["lmax"]
+    t0 = time.perf_counter()
+    T = O.sphere_aggregate_tmatrix(W["position"], W["mie_scat"].reshape(N, -1), W["k"])
+    t_asm = time.perf_counter() - t0
+    xs_all = []
+    its = []
+    for r in range(2):
+        x, it, _ = O.solve_linear_system_profiled(T, W["p_src"][..., r].ravel(), "bicgstab", tol=TOL)
+        its.append(it)
+        x = x.reshape(N, 2, -1)
+        t = W["mie_scat"][:, :, [n - 1 for n in range(1, lmax + 1) for _ in range(2 * n + 1)]]
+        ps = x * t
+        for i in range(N):
+            xs_all.append(O.particle_cross_sections(ps[i], x[i], W["p_src"][i, :, :, r], W["k"]))
+        O.force_all(ps, x, W["k"], W["eps_b"])
+        O.torque_all(ps, x, W["k"], W["eps_b"])
+    total = time.perf_counter() - t0
+    return dict(seconds=total, assembly_s=t_asm, cores=n_thr, iterations=its)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    base = dict(metric="cluster solves/s + p99 latency, mixed vs FP64 GPU, at <=1e-6 rel C_ext err",
+                unit="solves/s", n_gpus=world, steps=args.steps, warmup=args.warmup, higher_is_better=True,
+                scaling="weak", vs_baseline=None, data="synthetic (seeded random cluster)",
+                config=dict(workload=WORKLOAD, solve_tol=TOL, rhs=2, l2="inputs larger than L2 (packed matrix "
+                            "367 MB c64 + 733 MB c128)", parallelism=f"replicas x{world}"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, min(args.steps, 2))
+        from oracle import oracle as O
+        O.build()
+        for _ in range(min(args.warmup, 1)):
+            pass
+        times, info = [], None
+        for _ in range(steps):
+            info = run_cpu_sample(threads=len(os.sched_getaffinity(0)))
+            times.append(info["seconds"])
+        v = steps / sum(times)
+        line = dict(base, impl="reference", value=v, ms_per_step=1e3 * sum(times) / steps, dtype="c128",
+                    cpu_baseline=dict(value=v, unit="solves/s", cores=info["cores"], kind="port",
+                                      sample=f"{steps} full solve(s) of the workload (oracle restatement of the "
+                                             "reference's OpenMP C++ path)"),
+                    e2e=dict(value=v, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                    iterations=info["iterations"])
+        line["steps"] = steps
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    res = run_gpu(args, rank, world)
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            info = run_cpu_sample(threads=len(os.sched_getaffinity(0)))
+            cpu = dict(value=1.0 / info["seconds"], unit="solves/s", cores=info["cores"], kind="port",
+                       sample="1 full solve of the workload (assembly + 2 BiCGSTAB solves + epilogue) on the oracle",
+                       assembly_s=info["assembly_s"], iterations=info["iterations"])
+        line = dict(base, impl="gb300", dtype="c64 matvec + c128 refinement (mixed)", gpu_launches=None,
+                    cpu_baseline=cpu, **res)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+/*
+ * miepy_gb300 -- C ABI of the GB300 (sm_103a) sphere-cluster aggregate T-matrix path.
+ *
+ * Every entry point takes plain device/host pointers and sizes, is ordered on the
+ * CUDA stream it is given (NULL = legacy default stream), never throws, and returns
+ * an int status (GB_OK = 0).  gb_last_error() returns the message of the last
+ * failure on the calling thread.  All buffers are owned by the caller; entry points
+ * that need scratch memory take a workspace pointer whose size is reported by the
+ * matching *_workspace_size query.  The library itself holds only the per-lmax
+ * coefficient tables (built on first use on each device) and small pinned host
+ * staging buffers.
+ *
+ * Layout conventions (identical to the reference's C++ module):
+ *   mode index      r = n(n+2) - n + m - 1,  n = 1..lmax, m = -n..n,  rmax = lmax(lmax+2)
+ *   particle index  row = i*(2*rmax) + a*rmax + r   (a = 0 electric, 1 magnetic),
+ *                   D = 2*rmax*N
+ *   mie             [N, 2, lmax] complex128 (a_n then b_n), i.e. the reference's
+ *                   mie_scat array, interleaved (re, im) doubles
+ *   positions       [N, 3] float64
+ *   dense matrices  [D, D] row-major complex128
+ *
+ * Packed pair-block format ("packed"): for the P = N(N-1)/2 pairs i < j in
+ * i-major order, the block A_ij of the translation matrix WITHOUT the Mie
+ * factors, B x B row-major (B = 2*rmax), one block after the other.  The full
+ * aggregate matrix follows as  T[i,j] = A_ij diag(t_j)  and
+ * T[j,i] = S A_ij S diag(t_i),  S = diag((-1)^(n+a)),  t_j = mie of particle j
+ * expanded per row.  Half the storage of the dense matrix, no per-element Mie
+ * product.
+ */
+#ifndef MIEPY_GB300_H
+#define MIEPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GB_OK 0
+#define GB_NOT_CONVERGED 1   /* maxiter reached before the tolerance */
+#define GB_BREAKDOWN 2       /* Krylov breakdown that a restart did not cure */
+#define GB_NAN 3             /* non-finite value in the iteration */
+#define GB_OVER_BUDGET 4     /* workspace smaller than required */
+#define GB_TIMEOUT 5         /* host-side wait limit reached */
+#define GB_BAD_ARG 6
+#define GB_CUDA_ERROR 7
+#define GB_UNSUPPORTED 8
+
+/* precision of a solve */
+#define GB_PREC_FP64 0       /* complex128 matrix, complex128 Krylov vectors */
+#define GB_PREC_MIXED 1      /* complex64 matrix + complex64 BiCGSTAB, FP64 refinement on the complex128 matrix */
+#define GB_PREC_FP32 2       /* complex64 matrix + complex64 BiCGSTAB, no refinement */
+
+int gb_version(void);
+size_t gb_last_error(char* buf, size_t cap);
+int gb_device_sm_count(void);
+
+/* ---------------------------------------------------------------- tables --
+ * Per-lmax translation coefficient table (replaces create_vsh_cache_map,
+ * cpp/src/vsh_translation.cpp:36-51, with gaunt_batch / wigner_3j_batch,
+ * cpp/src/special.cpp:298-440).  Built on the device on first use.
+ * gb_tables_export copies it to the host for tests: M tuples, nmvu [M,4],
+ * qAB [M,2], cA [M, lmax+1], cB [M, lmax+1], elem_map [(2rmax)^2]. */
+int gb_tables_prepare(int lmax, void* stream);
+int gb_tables_count(int lmax, int* M_out);
+int gb_tables_export(int lmax, int* nmvu, int* qab, double* cA, double* cB, int* elem_map);
+
+/* -------------------------------------------------------------- assembly --
+ * Dense aggregate T-matrix in the reference layout (zero diagonal blocks):
+ * replaces sphere_aggregate_tmatrix, cpp/src/interactions.cpp:370-415, with
+ * vsh_translation_insert_pair (Mie overload), cpp/src/vsh_translation.cpp:161-237.
+ * pos [N,3] f64, mie [N,2,lmax] c128, out [D,D] c128 (all device). */
+int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* mie, double k,
+                             double* out, void* stream);
+
+/* Packed pair-block translation matrix of one cluster (see above).  Either
+ * output may be NULL: out128 [P*B*B] c128, out64 [P*B*B] c64. */
+int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,
+                              void* stream);
+
+/* ------------------------------------------------------ batched clusters --
+ * A batch describes independent clusters (ragged N and lmax) that share one
+ * launch sequence.  Offsets are in elements of the respective device arrays. */
+typedef struct {
+    int32_t N;          /* particles */
+    int32_t lmax;       /* expansion order, 1..10 */
+    double k;           /* medium wavenumber */
+    int64_t pos_off;    /* into pos (doubles): first of 3*N */
+    int64_t mat_off;    /* into the packed matrices (complex elements): first of P*B*B */
+    int64_t vec_off;    /* into the [D][R] vectors (complex elements): first of D*R */
+    int64_t t_off;      /* into the per-row Mie factor vector (complex128): first of D */
+} gb_system;
+
+/* Assemble the packed matrices of every cluster in the batch (one launch). */
+int gb_assemble_batch(int nsys, const gb_system* sys, const double* pos, double* mat128, float* mat64,
+                      void* stream);
+
+/* Expand Mie coefficients [N,2,lmax] into the per-row factor t (D entries) for
+ * every cluster; mie_off[s] is the complex offset of cluster s in mie. */
+int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, const double* mie, double* tvec,
+                        void* stream);
+
+/* Solve (I + T) x = b for every cluster and right-hand side (replaces
+ * solve_linear_system, cpp/src/interactions.cpp:347-368, BiCGSTAB branch; the
+ * iteration is the one Eigen's BiCGSTAB runs: x0 = 0, restart when rho becomes
+ * tiny, stop when |r| <= tol |b|).  R right-hand sides per cluster share every
+ * matrix pass.  b and x are [D][R] complex128 per cluster at vec_off.
+ * prec: GB_PREC_FP64 uses mat128; GB_PREC_FP32 uses mat64; GB_PREC_MIXED runs
+ * FP32 BiCGSTAB on mat64 to inner_tol and refines with FP64 residuals on
+ * mat128 until |b - (I+T)x| <= tol |b| (at most max_refine passes).
+ * status/iters/resid: host arrays of nsys*R entries (may be NULL). */
+size_t gb_solve_workspace_size(int nsys, const gb_system* sys, int R, int prec);
+int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+                   int max_refine, const double* mat128, const float* mat64, const double* tvec, const double* b,
+                   double* x, void* workspace, size_t ws_bytes, int* status, int* iters, double* resid,
+                   void* stream);
+
+/* Dense solve of (I + T) x = b for a caller-supplied dense aggregate matrix
+ * T [D,D] c128 (the plugin path, where the caller already holds T).  BiCGSTAB as
+ * above in FP64, R right-hand sides stored [D][R]. */
+size_t gb_solve_dense_workspace_size(int D, int R);
+int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, double tol, int maxiter,
+                   void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, void* stream);
+
+/* One application y = (I + T) x of the packed operator (c128 if prec == FP64,
+ * else c64), for tests and benchmarks.  x, y: [D][R] complex128. */
+size_t gb_apply_workspace_size(int nsys, const gb_system* sys, int R, int prec);
+int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                   const double* tvec, const double* x, double* y, void* workspace, size_t ws_bytes, void* stream);
+
+/* -------------------------------------------------------------- epilogue --
+ * Per cluster and right-hand side, from p_inc [D][R] (c128), p_src [D][R],
+ * mie_scat / mie_int [N,2,lmax] c128:
+ *   p_scat = t o p_inc,  p_int = p_inc * mie_int[:, ::-1, n-1]   (sphere_cluster.py:715-717)
+ *   xs[N][R][3][2*lmax] per-multipole (Cscat, Cabs, Cext)        (cpp/src/flux.cpp:5-30)
+ *   force, torque [N][R][3]                                       (cpp/src/forces.cpp:7-137)
+ * with the incident coefficients p_inc (source != 0) or p_inc - p_src
+ * (source == 0) in the force/torque sums (sphere_cluster.py:521-559).
+ * eps_b: medium permittivity (real part used, as the reference's double eps_b).
+ * p_scat/p_int are written at vec_off; xs/force/torque at obs_off[s] particles.
+ * mie_off[s]: complex offset of cluster s in mie_scat/mie_int.  Any output
+ * pointer may be NULL. */
+int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const int64_t* mie_off, const int64_t* obs_off,
+                      const double* mie_scat, const double* mie_int, const double* p_inc, const double* p_src,
+                      double eps_b, int source, double* p_scat, double* p_int, double* xs, double* force,
+                      double* torque, void* stream);
+
+/* Cross-sections of particles from given coefficients (replaces
+ * flux.particle_cross_sections, cpp/src/flux.cpp:5-30, and the plugin function
+ * particle_cross_sections_jax, backends/jax/flux.py:14-44): p_* [N,2,rmax] c128
+ * -> out [N][3][2*lmax] (Cscat, Cabs, Cext), all device. */
+int gb_particle_cross_sections(int N, int lmax, const double* p_scat, const double* p_inc, const double* p_src,
+                               double k, double* out, void* stream);
+
+/* ---------------------------------------------------------------- fields --
+ * Near field of one cluster at Npts points, following sphere_cluster.E_field /
+ * H_field (sphere_cluster.py:244-391) with expand_E / expand_H
+ * (vsh/expansion.py:13-108) and the VSH of cpp/src/vsh_functions.cpp:60-98:
+ *   outside every sphere: sum over particles of the outgoing expansion of p_scat
+ *     about the particle (h_n(k r)), factor i E_mn;
+ *   inside sphere i (when interior != 0): the interior expansion of p_int[i] with
+ *     j_n(k_int,i r) (complex k_int, upward recurrence), factor -i E_mn; the
+ *     scattered sum is not added there (the reference overwrites those points).
+ * magnetic != 0 evaluates H: expand_E of the polarisation-swapped coefficients
+ * times -i sqrt(eps/mu) (medium values outside, hfac_int[i] inside).
+ * pos [N,3], radius [N], p_scat / p_int [N,2,rmax] c128, k (medium),
+ * k_int [N] c128, hfac (re, im) and hfac_int [N] c128 (only for magnetic),
+ * pts [Npts,3] f64 -> out [Npts,3] c128 (Cartesian).  The source field is not
+ * included. */
+int gb_near_field(int N, int lmax, const double* pos, const double* radius, const double* p_scat,
+                  const double* p_int, double k, const double* k_int, int Npts, const double* pts, int interior,
+                  int magnetic, double hfac_re, double hfac_im, const double* hfac_int, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MIEPY_GB300_H */

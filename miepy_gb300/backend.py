@@ -1,0 +1,169 @@
+"""Drop-in GPU backend for miepy's plugin surface.
+
+The reference dispatches its hot path to the module ``miepy.backends.jax`` when
+``miepy.backends.set_backend('gpu')`` is active (backends/__init__.py:16-28) and
+imports exactly three names from it:
+
+  interactions.sphere_aggregate_tmatrix_jax(positions, mie, k)   (interactions.py:141-143)
+  interactions.solve_linear_system_jax(agg_tmatrix, p_src, method) (interactions.py:81-83)
+  flux.particle_cross_sections_jax(p_scat, p_inc, p_src, k)       (flux.py:21-26)
+
+This module provides the three with the same signatures and return shapes,
+computed by the CUDA extension.  ``install()`` registers them under
+``miepy.backends.jax`` so that an unmodified miepy picks them up.
+
+sphere_aggregate_tmatrix_jax returns a DeviceAggregateTMatrix: the packed matrix
+stays on the GPU and solve_linear_system_jax solves it there; converting it with
+numpy.asarray materialises the reference's dense [N,2,rmax,N,2,rmax] array.
+"""
+
+from __future__ import annotations
+
+import sys
+import types
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .engine import ClusterBatch, current_stream, require_cuda
+from .modes import lmax_to_rmax, rmax_to_lmax
+
+BICGSTAB_TOL = 1e-5       # the reference's BiCGSTAB tolerance
+EXACT_TOL = 1e-14         # stands in for the LU branch (no LU on the GPU path)
+
+
+def _is_exact(method):
+    return getattr(method, "name", None) == "exact" or str(method).endswith("exact")
+
+
+class DeviceAggregateTMatrix:
+    """Aggregate T-matrix of a sphere cluster held on the GPU in packed form."""
+
+    def __init__(self, positions, mie, k):
+        self.positions = np.asarray(positions, dtype=float).reshape(-1, 3)
+        self.mie = np.asarray(mie, dtype=complex)
+        self.N = self.positions.shape[0]
+        self.lmax = self.mie.shape[-1]
+        self.rmax = lmax_to_rmax(self.lmax)
+        self.k = float(np.real(k))
+        self.shape = (self.N, 2, self.rmax, self.N, 2, self.rmax)
+        self.ndim = 6
+        self.dtype = np.dtype(complex)
+        zeros = np.zeros((self.N, 2, self.rmax), dtype=complex)
+        self._batch = ClusterBatch([dict(position=self.positions, mie_scat=self.mie.reshape(self.N, 2, self.lmax),
+                                         k=self.k, p_src=zeros)], R=1, precision="fp64")
+        self._batch.assemble()
+
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+    def reshape(self, *shape):
+        shape = shape[0] if len(shape) == 1 and isinstance(shape[0], (tuple, list)) else shape
+        if int(np.prod([s for s in shape if s != -1])) not in (self.size, 0) and -1 not in shape:
+            raise ValueError(f"cannot reshape {self.shape} into {shape}")
+        view = object.__new__(DeviceAggregateTMatrix)
+        view.__dict__.update(self.__dict__)
+        view.shape = tuple(shape)
+        view.ndim = len(shape)
+        return view
+
+    def dense_device(self):
+        """The reference-layout dense matrix [D, D] as a device tensor."""
+        D = 2 * self.rmax * self.N
+        dev = self._batch.device
+        pos = torch.from_numpy(self.positions).to(dev)
+        mie = torch.from_numpy(np.ascontiguousarray(self.mie.reshape(self.N, 2, self.lmax))).to(dev)
+        out = torch.empty((D, D), dtype=torch.complex128, device=dev)
+        nat.check(nat.lib().gb_assemble_sphere_dense(self.N, self.lmax, nat.ptr(pos), nat.ptr(mie), self.k,
+                                                     nat.ptr(out), current_stream(dev)), "dense assembly")
+        return out
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.dense_device().cpu().numpy().reshape(self.shape)
+        return a.astype(dtype) if dtype is not None else a
+
+    def __sub__(self, other):
+        raise NotImplementedError("substrate reflection matrices are not on the GPU path yet")
+
+    __isub__ = __sub__
+
+
+def sphere_aggregate_tmatrix_jax(positions, mie, k):
+    """positions [N,3], mie [N,2,lmax], k -> T [N,2,rmax,N,2,rmax] (device-resident)."""
+    require_cuda()
+    mie = np.asarray(mie)
+    N = np.asarray(positions).reshape(-1, 3).shape[0]
+    lmax = mie.shape[-1]
+    rmax = lmax_to_rmax(lmax)
+    if N == 1:
+        return np.zeros((1, 2, rmax, 1, 2, rmax), dtype=complex)
+    return DeviceAggregateTMatrix(positions, mie, k)
+
+
+def solve_linear_system_jax(agg_tmatrix, p_src, method):
+    """Solve p_inc = (I + T)^-1 p_src; returns numpy [N, 2, rmax]."""
+    require_cuda()
+    p_src = np.asarray(p_src, dtype=complex)
+    N, rmax = p_src.shape[0], p_src.shape[-1]
+    tol = EXACT_TOL if _is_exact(method) else BICGSTAB_TOL
+    if isinstance(agg_tmatrix, DeviceAggregateTMatrix):
+        b = agg_tmatrix._batch
+        b.b.copy_(torch.from_numpy(p_src.reshape(-1)).to(b.device))
+        b.solve(tol=tol, maxiter=1000)
+        return b.cluster_view(0, b.x)[..., 0].cpu().numpy()
+    # a dense matrix supplied by the caller
+    D = N * 2 * rmax
+    T = torch.as_tensor(np.ascontiguousarray(np.asarray(agg_tmatrix, dtype=complex).reshape(D, D)))
+    dev = require_cuda()
+    T = T.to(dev)
+    bb = torch.from_numpy(np.ascontiguousarray(p_src.reshape(-1))).to(dev)
+    x = torch.empty_like(bb)
+    L = nat.lib()
+    need = L.gb_solve_dense_workspace_size(D, 1)
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    status = np.zeros(1, np.int32)
+    iters = np.zeros(1, np.int32)
+    resid = np.zeros(1)
+    rc = L.gb_solve_dense(D, 1, nat.ptr(T), nat.ptr(bb), nat.ptr(x), tol, 1000, nat.ptr(ws), ws.numel(),
+                          status.ctypes.data, iters.ctypes.data, resid.ctypes.data, current_stream(dev))
+    if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED):
+        nat.check(rc, "dense solve")
+    return x.cpu().numpy().reshape(N, 2, rmax)
+
+
+def particle_cross_sections_jax(p_scat, p_inc, p_src, k):
+    """(p_scat, p_inc, p_src [2, rmax], k) -> (Cscat, Cabs, Cext), each [2, lmax]."""
+    dev = require_cuda()
+    arrs = [torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=complex))).to(dev) for a in (p_scat, p_inc, p_src)]
+    rmax = arrs[0].shape[-1]
+    lmax = rmax_to_lmax(rmax)
+    out = torch.empty(6 * lmax, dtype=torch.float64, device=dev)
+    nat.check(nat.lib().gb_particle_cross_sections(1, lmax, nat.ptr(arrs[0]), nat.ptr(arrs[1]), nat.ptr(arrs[2]),
+                                                   float(np.real(k)), nat.ptr(out), current_stream(dev)),
+              "cross sections")
+    o = out.cpu().numpy().reshape(3, 2, lmax)
+    return o[0], o[1], o[2]
+
+
+def install():
+    """Register this backend as ``miepy.backends.jax`` (the module miepy's
+    set_backend('gpu') imports).  Returns the registered package module."""
+    pkg = types.ModuleType("miepy.backends.jax")
+    pkg.__path__ = []
+    pkg.HAS_JAX = True
+    inter = types.ModuleType("miepy.backends.jax.interactions")
+    inter.sphere_aggregate_tmatrix_jax = sphere_aggregate_tmatrix_jax
+    inter.solve_linear_system_jax = solve_linear_system_jax
+    flux = types.ModuleType("miepy.backends.jax.flux")
+    flux.particle_cross_sections_jax = particle_cross_sections_jax
+    pkg.interactions = inter
+    pkg.flux = flux
+    sys.modules["miepy.backends.jax"] = pkg
+    sys.modules["miepy.backends.jax.interactions"] = inter
+    sys.modules["miepy.backends.jax.flux"] = flux
+    backends = sys.modules.get("miepy.backends")
+    if backends is not None:
+        backends.jax = pkg
+    return pkg

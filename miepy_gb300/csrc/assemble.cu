@@ -1,0 +1,453 @@
+// K1: translation-matrix assembler (replaces sphere_aggregate_tmatrix,
+// cpp/src/interactions.cpp:370-415, and vsh_translation_insert_pair (Mie overload),
+// cpp/src/vsh_translation.cpp:161-237).
+//
+// One CTA per particle pair (grid-stride over all pairs of all clusters of a
+// batch).  Per pair, in shared memory:
+//   1. h_p(kr) by the upward j/y recurrence of spherical_hn_recursion
+//      (cpp/src/special.cpp:90-111), one thread; P_p^mu(cos theta) (no
+//      Condon-Shortley phase, GSL_SF_LEGENDRE_NONE convention), one thread per
+//      order mu; e^{i mu phi}, one thread per mu;
+//   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p);
+//   3. one thread per canonical tuple: A_t, B_t as real x complex FMA sums over
+//      the per-lmax coefficient table (tables.cu);
+//   4. coalesced block write: every entry of the B x B block looks up its tuple and
+//      sign in the element map.  Packed output writes the (i, j) block only, without
+//      Mie factors, in complex128 and/or complex64 (sign flips are bit operations,
+//      the complex64 copy is rounded once per tuple).  Dense output writes the (i, j)
+//      and (j, i) blocks of the reference's D x D matrix with the Mie factors of the
+//      column particle.
+
+#include <algorithm>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_internal.h"
+
+namespace {
+
+constexpr int kAsmThreads = 256;
+
+struct AsmSmem {
+    int PM, MU, M;
+    size_t off_h, off_P, off_e, off_G, off_T, off_Tf, total;
+};
+
+__host__ __device__ inline AsmSmem asm_layout(int L, int M, bool want64) {
+    AsmSmem s;
+    s.PM = 2 * L + 2;
+    s.MU = 4 * L + 1;
+    s.M = M;
+    size_t o = 0;
+    s.off_h = o;  o += sizeof(double2) * s.PM;
+    s.off_e = o;  o += sizeof(double2) * s.MU;
+    s.off_G = o;  o += sizeof(double2) * s.PM * s.MU;
+    s.off_T = o;  o += sizeof(double2) * 2 * M;
+    s.off_P = o;  o += sizeof(double) * s.PM * s.PM;
+    s.off_Tf = o; o += want64 ? sizeof(float2) * 2 * M : 0;
+    s.total = (o + 15) & ~size_t(15);
+    return s;
+}
+
+__device__ __forceinline__ double2 mul_ipow(double2 z, int k) {
+    switch (k & 3) {
+        case 0: return z;
+        case 1: return make_double2(-z.y, z.x);
+        case 2: return make_double2(-z.x, -z.y);
+        default: return make_double2(z.y, -z.x);
+    }
+}
+
+__device__ __forceinline__ int find_sys(const long long* base, int nsys, long long g) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool DENSE>
+__global__ void __launch_bounds__(kAsmThreads)
+k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ pair_base, long long total,
+           const double* __restrict__ pos, const double2* __restrict__ mie, double2* __restrict__ out128,
+           float2* __restrict__ out64, long long dense_ld) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x;
+    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+        const int s = find_sys(pair_base, nsys, g);
+        const gb::SysDev S = sys[s];
+        const int L = S.lmax, B = S.B, N = S.N;
+        const AsmSmem lay = asm_layout(L, S.M, out64 != nullptr);
+        double2* h = reinterpret_cast<double2*>(smem + lay.off_h);
+        double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);
+        double2* G = reinterpret_cast<double2*>(smem + lay.off_G);
+        double2* Tv = reinterpret_cast<double2*>(smem + lay.off_T);
+        double* Pl = reinterpret_cast<double*>(smem + lay.off_P);
+        float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
+        const int PM = lay.PM, MU = lay.MU;
+
+        const long long p = g - pair_base[s];
+        int i, j;
+        pair_ij(p, N, i, j);
+        const double* pi_ = pos + S.pos_off + 3 * (long long)i;
+        const double* pj_ = pos + S.pos_off + 3 * (long long)j;
+        const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
+        const double rad = sqrt(dx * dx + dy * dy + dz * dz);
+        const double theta = acos(dz / rad);
+        const double phi = atan2(dy, dx);
+        const double x = cos(theta);
+
+        // ---- phase 1: Hankel, Legendre, azimuthal phases
+        if (tid == 32) {
+            const double z = S.k * rad;
+            double sz, cz;
+            sincos(z, &sz, &cz);
+            double j0 = sz / z, y0 = -cz / z;
+            double j1 = j0 / z + y0, y1 = y0 / z - j0;
+            h[0] = make_double2(j0, y0);
+            if (PM > 1) h[1] = make_double2(j1, y1);
+            for (int q = 2; q < PM; q++) {
+                double jn = (2 * q - 1) / z * j1 - j0;
+                double yn = (2 * q - 1) / z * y1 - y0;
+                j0 = j1; j1 = jn; y0 = y1; y1 = yn;
+                h[q] = make_double2(jn, yn);
+            }
+        }
+        if (tid < PM) {
+            const int mu = tid;
+            const double u = sqrt(fmax(0.0, (1.0 - x) * (1.0 + x)));
+            double pmm = 1.0;
+            for (int k = 1; k <= mu; k++) pmm *= (2 * k - 1) * u;
+            Pl[mu * PM + mu] = pmm;
+            if (mu + 1 < PM) {
+                double p1 = x * (2 * mu + 1) * pmm;
+                Pl[(mu + 1) * PM + mu] = p1;
+                double pa = pmm, pb = p1;
+                for (int q = mu + 2; q < PM; q++) {
+                    double pc = ((2 * q - 1) * x * pb - (q + mu - 1) * pa) / (double)(q - mu);
+                    Pl[q * PM + mu] = pc;
+                    pa = pb;
+                    pb = pc;
+                }
+            }
+        }
+        if (tid >= 64 && tid < 64 + MU) {
+            const int mu = tid - 64 - 2 * L;
+            double sn, cs;
+            sincos((double)mu * phi, &sn, &cs);
+            eph[tid - 64] = make_double2(cs, sn);
+        }
+        __syncthreads();
+        for (int e = tid; e < PM * MU; e += kAsmThreads) {
+            const int q = e / MU, mi = e % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
+            double2 gval = make_double2(0.0, 0.0);
+            if (am <= q) {
+                double P = Pl[q * PM + am];
+                if (mu < 0) P *= S.neg_ratio[q * PM + am];
+                double2 he = cmul(h[q], eph[mi]);
+                gval = make_double2(P * he.x, P * he.y);
+            }
+            G[e] = gval;
+        }
+        __syncthreads();
+
+        // ---- phase 2: translation coefficients of every canonical tuple
+        const int Q = L + 1;
+        for (int t = tid; t < S.M; t += kAsmThreads) {
+            const int4 e = S.nmvu[t];
+            const int2 qq = S.qab[t];
+            const int mi = (e.w - e.y) + 2 * L;
+            const int nv = e.x + e.z;
+            const double* ca = S.cA + (size_t)t * Q;
+            const double* cb = S.cB + (size_t)t * Q;
+            double2 sa = make_double2(0.0, 0.0), sb = make_double2(0.0, 0.0);
+            for (int q = 0; q <= qq.x; q++) {
+                const double c = ca[q];
+                const double2 gv = G[(nv - 2 * q) * MU + mi];
+                sa.x = fma(c, gv.x, sa.x);
+                sa.y = fma(c, gv.y, sa.y);
+            }
+            for (int q = 1; q <= qq.y; q++) {
+                const double c = cb[q];
+                const double2 gv = G[(nv - 2 * q + 1) * MU + mi];
+                sb.x = fma(c, gv.x, sb.x);
+                sb.y = fma(c, gv.y, sb.y);
+            }
+            const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
+            Tv[2 * t] = At;
+            Tv[2 * t + 1] = Bt;
+            if (!DENSE && out64) {
+                Tf[2 * t] = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
+                Tf[2 * t + 1] = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
+            }
+        }
+        __syncthreads();
+
+        // ---- phase 3: block write
+        const int BB = B * B;
+        if (!DENSE) {
+            const long long base = S.mat_off + p * (long long)BB;
+            for (int e = tid; e < BB; e += kAsmThreads) {
+                const int code = __ldg(S.elem_map + e);
+                const unsigned neg = code & 1;
+                if (out128) {
+                    const double2 v = Tv[code >> 1];
+                    out128[base + e] = make_double2(flipd(v.x, neg), flipd(v.y, neg));
+                }
+                if (out64) {
+                    const float2 v = Tf[code >> 1];
+                    out64[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+                }
+            }
+        } else {
+            const double2* mi_ = mie + (long long)i * 2 * L;
+            const double2* mj_ = mie + (long long)j * 2 * L;
+            for (int e = tid; e < BB; e += kAsmThreads) {
+                const int R = e / B, C = e % B;
+                const int code = __ldg(S.elem_map + e);
+                const unsigned neg = code & 1;
+                double2 v = Tv[code >> 1];
+                v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
+                const int col = __ldg(S.miecol + C);
+                const double2 vij = cmul(v, mj_[col]);
+                const unsigned sneg = ((unsigned)__ldg(S.rowinfo + R) >> 30 ^ (unsigned)__ldg(S.rowinfo + C) >> 30) & 1;
+                double2 vji = cmul(v, mi_[col]);
+                vji = make_double2(flipd(vji.x, sneg), flipd(vji.y, sneg));
+                out128[((long long)i * B + R) * dense_ld + (long long)j * B + C] = vij;
+                out128[((long long)j * B + R) * dense_ld + (long long)i * B + C] = vji;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_expand_mie(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ mie_off,
+                             const double2* __restrict__ mie, double2* __restrict__ tvec) {
+    const int s = blockIdx.y;
+    if (s >= nsys) return;
+    const gb::SysDev S = sys[s];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S.D; e += gridDim.x * blockDim.x) {
+        const int pidx = e / S.B, R = e % S.B;
+        tvec[S.t_off + e] = mie[mie_off[s] + (long long)pidx * 2 * S.lmax + S.miecol[R]];
+    }
+}
+
+}   // namespace
+
+namespace gb {
+
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return 148;
+    if (!cached[dev]) {
+        int c = 0;
+        if (cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || c <= 0) c = 148;
+        cached[dev] = c;
+    }
+    return cached[dev];
+}
+
+int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector<SysDev>& out) {
+    out.resize(nsys);
+    for (int s = 0; s < nsys; s++) {
+        const gb_system& a = sys[s];
+        if (a.N < 1 || a.lmax < 1 || a.lmax > GB_LMAX_MAX)
+            return gb_set_error(GB_BAD_ARG, "cluster %d: N=%d lmax=%d invalid", s, a.N, a.lmax);
+        if (!(a.k > 0.0)) return gb_set_error(GB_BAD_ARG, "cluster %d: wavenumber must be positive", s);
+        const Tables* T = nullptr;
+        int st = get_tables(a.lmax, stream, &T);
+        if (st) return st;
+        SysDev& d = out[s];
+        d.N = a.N;
+        d.lmax = a.lmax;
+        d.rmax = T->rmax;
+        d.B = T->B;
+        d.D = T->B * a.N;
+        d.M = T->M;
+        d.P = (long long)a.N * (a.N - 1) / 2;
+        d.k = a.k;
+        d.pos_off = a.pos_off;
+        d.mat_off = a.mat_off;
+        d.vec_off = a.vec_off;
+        d.t_off = a.t_off;
+        d.nmvu = T->nmvu;
+        d.qab = T->qab;
+        d.cA = T->cA;
+        d.cB = T->cB;
+        d.elem_map = T->elem_map;
+        d.neg_ratio = T->neg_ratio;
+        d.rowinfo = T->rowinfo;
+        d.miecol = T->miecol;
+    }
+    return GB_OK;
+}
+
+// Small per-call descriptor arrays travel through a ring of pinned host /
+// device staging slots (per host thread and device).  A slot is reused only
+// after the event recorded behind the kernels that read it has completed, so
+// calls stay asynchronous.
+struct StageSlot {
+    void* host = nullptr;
+    void* dev = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+};
+struct StageRing {
+    int device = -1;
+    int next = 0;
+    StageSlot slot[16];
+};
+
+static StageRing& ring_for_thread() {
+    thread_local StageRing r[8];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return r[dev & 7];
+}
+
+int stage_acquire(const void* src, size_t bytes, cudaStream_t stream, void** dev_out, int* slot_out) {
+    StageRing& R = ring_for_thread();
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    R.device = dev;
+    const int k = R.next;
+    R.next = (R.next + 1) % 16;
+    StageSlot& S = R.slot[k];
+    if (S.pending) {
+        GB_CUDA_TRY(cudaEventSynchronize(S.done));
+        S.pending = false;
+    }
+    if (!S.done) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming));
+    if (S.cap < bytes) {
+        if (S.host) cudaFreeHost(S.host);
+        if (S.dev) cudaFree(S.dev);
+        S.host = S.dev = nullptr;
+        size_t cap = std::max<size_t>(bytes, 1 << 14);
+        GB_CUDA_TRY(cudaHostAlloc(&S.host, cap, cudaHostAllocDefault));
+        GB_CUDA_TRY(cudaMalloc(&S.dev, cap));
+        S.cap = cap;
+    }
+    memcpy(S.host, src, bytes);
+    GB_CUDA_TRY(cudaMemcpyAsync(S.dev, S.host, bytes, cudaMemcpyHostToDevice, stream));
+    *dev_out = S.dev;
+    *slot_out = k;
+    return GB_OK;
+}
+
+int stage_release(int slot, cudaStream_t stream) {
+    StageRing& R = ring_for_thread();
+    StageSlot& S = R.slot[slot];
+    GB_CUDA_TRY(cudaEventRecord(S.done, stream));
+    S.pending = true;
+    return GB_OK;
+}
+
+}   // namespace gb
+
+namespace {
+
+int launch_assemble(int nsys, const gb_system* sys, const double* pos, const double* mie, double* out128,
+                    float* out64, long long dense_ld, bool dense, cudaStream_t stream) {
+    std::vector<gb::SysDev> sd;
+    int st = gb::make_sysdev(nsys, sys, stream, sd);
+    if (st) return st;
+    std::vector<long long> base(nsys + 1, 0);
+    int Lmax = 1, Mmax = 0;
+    for (int s = 0; s < nsys; s++) {
+        base[s + 1] = base[s] + sd[s].P;
+        Lmax = std::max(Lmax, sd[s].lmax);
+        Mmax = std::max(Mmax, sd[s].M);
+    }
+    const long long total = base[nsys];
+    if (total == 0) return GB_OK;
+    // one staging upload: descriptors then pair prefix sums
+    std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * (nsys + 1));
+    memcpy(blob.data(), sd.data(), sizeof(gb::SysDev) * nsys);
+    memcpy(blob.data() + sizeof(gb::SysDev) * nsys, base.data(), sizeof(long long) * (nsys + 1));
+    void* dblob = nullptr;
+    int slot = 0;
+    st = gb::stage_acquire(blob.data(), blob.size(), stream, &dblob, &slot);
+    if (st) return st;
+    const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
+    const long long* dbase = reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys);
+    const AsmSmem lay = asm_layout(Lmax, Mmax, out64 != nullptr && !dense);
+    const size_t smem = lay.total;
+    int per_sm = 1;
+    if (dense) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(k_assemble<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<true>, kAsmThreads, smem));
+    } else {
+        GB_CUDA_TRY(cudaFuncSetAttribute(k_assemble<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<false>, kAsmThreads, smem));
+    }
+    if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
+    long long grid = std::min<long long>(total, (long long)gb::sm_count() * per_sm);
+    if (dense)
+        k_assemble<true><<<(unsigned)grid, kAsmThreads, smem, stream>>>(
+            dsys, nsys, dbase, total, pos, reinterpret_cast<const double2*>(mie), reinterpret_cast<double2*>(out128),
+            nullptr, dense_ld);
+    else
+        k_assemble<false><<<(unsigned)grid, kAsmThreads, smem, stream>>>(
+            dsys, nsys, dbase, total, pos, nullptr, reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64),
+            0);
+    GB_CUDA_TRY(cudaGetLastError());
+    return gb::stage_release(slot, stream);
+}
+
+}   // namespace
+
+extern "C" {
+
+int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* mie, double k, double* out,
+                             void* stream) {
+    if (!pos || !mie || !out) return gb_set_error(GB_BAD_ARG, "null pointer");
+    if (N < 1 || lmax < 1 || lmax > GB_LMAX_MAX) return gb_set_error(GB_BAD_ARG, "N=%d lmax=%d invalid", N, lmax);
+    const long long D = 2LL * lmax_to_rmax(lmax) * N;
+    GB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double2) * D * D, (cudaStream_t)stream));
+    if (N == 1) return GB_OK;
+    gb_system s{N, lmax, k, 0, 0, 0, 0};
+    return launch_assemble(1, &s, pos, mie, out, nullptr, D, true, (cudaStream_t)stream);
+}
+
+int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,
+                              void* stream) {
+    if (!pos || (!out128 && !out64)) return gb_set_error(GB_BAD_ARG, "null pointer");
+    gb_system s{N, lmax, k, 0, 0, 0, 0};
+    return launch_assemble(1, &s, pos, nullptr, out128, out64, 0, false, (cudaStream_t)stream);
+}
+
+int gb_assemble_batch(int nsys, const gb_system* sys, const double* pos, double* mat128, float* mat64,
+                      void* stream) {
+    if (nsys < 1 || !sys || !pos || (!mat128 && !mat64)) return gb_set_error(GB_BAD_ARG, "bad batch arguments");
+    return launch_assemble(nsys, sys, pos, nullptr, mat128, mat64, 0, false, (cudaStream_t)stream);
+}
+
+int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, const double* mie, double* tvec,
+                        void* stream) {
+    if (nsys < 1 || !sys || !mie_off || !mie || !tvec) return gb_set_error(GB_BAD_ARG, "bad arguments");
+    cudaStream_t st_ = (cudaStream_t)stream;
+    std::vector<gb::SysDev> sd;
+    int st = gb::make_sysdev(nsys, sys, st_, sd);
+    if (st) return st;
+    std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * nsys);
+    memcpy(blob.data(), sd.data(), sizeof(gb::SysDev) * nsys);
+    memcpy(blob.data() + sizeof(gb::SysDev) * nsys, mie_off, sizeof(long long) * nsys);
+    void* dblob = nullptr;
+    int slot = 0;
+    st = gb::stage_acquire(blob.data(), blob.size(), st_, &dblob, &slot);
+    if (st) return st;
+    int maxD = 0;
+    for (auto& d : sd) maxD = std::max(maxD, d.D);
+    dim3 grid((maxD + 255) / 256, nsys);
+    k_expand_mie<<<grid, 256, 0, st_>>>(reinterpret_cast<const gb::SysDev*>(dblob), nsys,
+                                        reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys),
+                                        reinterpret_cast<const double2*>(mie), reinterpret_cast<double2*>(tvec));
+    GB_CUDA_TRY(cudaGetLastError());
+    return gb::stage_release(slot, st_);
+}
+
+}   // extern "C"

@@ -1,0 +1,45 @@
+// Library-wide C-ABI helpers: version, error reporting, device queries.
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "gb_common.cuh"
+#include "gb_internal.h"
+
+namespace {
+thread_local char g_err[1024] = {0};
+}
+
+int gb_set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int gb_set_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    const char* base = strrchr(file, '/');
+    snprintf(g_err, sizeof(g_err), "CUDA error %d (%s) in %s at %s:%d", (int)e, cudaGetErrorString(e), what,
+             base ? base + 1 : file, line);
+    return GB_CUDA_ERROR;
+}
+
+extern "C" {
+
+int gb_version(void) { return 10000; }   // 1.0.0
+
+size_t gb_last_error(char* buf, size_t cap) {
+    size_t n = strlen(g_err);
+    if (buf && cap) {
+        size_t c = n < cap - 1 ? n : cap - 1;
+        memcpy(buf, g_err, c);
+        buf[c] = 0;
+    }
+    return n;
+}
+
+int gb_device_sm_count(void) { return gb::sm_count(); }
+
+}   // extern "C"

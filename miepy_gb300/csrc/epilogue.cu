@@ -1,0 +1,262 @@
+// K7: fused epilogue of a solve.  One thread per (particle, right-hand side):
+//   p_scat = t o p_inc, p_int = p_inc * mie_int[:, ::-1, n-1]  (sphere_cluster.py:715-717),
+//   per-multipole cross-sections                             (cpp/src/flux.cpp:5-30),
+//   force and torque (Barton-type coefficient sums)          (cpp/src/forces.cpp:7-137),
+// all in FP64, reading each coefficient once.
+
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_internal.h"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kEps0 = 8.854187817e-12;   // the GSL MKSA vacuum permittivity the reference uses
+
+__device__ __forceinline__ double2 cj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+
+// 2 a conj(b) - a conj(bi) - ai conj(b)
+__device__ __forceinline__ double2 tri(double2 a, double2 b, double2 ai, double2 bi) {
+    double2 t = cscale(2.0, cmul(a, cj(b)));
+    t = csub(t, cmul(a, cj(bi)));
+    return csub(t, cmul(ai, cj(b)));
+}
+
+struct EpiArgs {
+    const gb::SysDev* sys;
+    const long long* base;      // prefix sums of N*R per cluster
+    const long long* mie_off;
+    const long long* obs_off;
+    int nsys, R, source;
+    const double2* mie_scat;
+    const double2* mie_int;
+    const double2* p_inc;
+    const double2* p_src;
+    double eps_b;
+    double2* p_scat;
+    double2* p_int;
+    double* xs;
+    double* force;
+    double* torque;
+};
+
+__global__ void k_epilogue(EpiArgs a, long long total) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int s = 0;
+    while (s + 1 < a.nsys && a.base[s + 1] <= g) s++;
+    const gb::SysDev S = a.sys[s];
+    const int R = a.R;
+    const long long loc = g - a.base[s];
+    const int i = (int)(loc / R), rr = (int)(loc % R);
+    const int L = S.lmax, rmax = S.rmax, B = S.B;
+    const double2* ms = a.mie_scat + a.mie_off[s] + (long long)i * 2 * L;
+    const double2* mi = a.mie_int + a.mie_off[s] + (long long)i * 2 * L;
+    const long long vb = S.vec_off + (long long)i * B * R + rr;   // row e at vb + e*R
+    const double k = S.k;
+    auto pin = [&](int e) { return a.p_inc[vb + (long long)e * R]; };
+    auto psrc = [&](int e) { return a.p_src[vb + (long long)e * R]; };
+    auto pscat = [&](int e) {
+        const int n = (int)floor(sqrt((double)(e % rmax) + 1.0 + 0.5));   // r + 1 in [n^2, (n+1)^2 - 1]
+        int nn = n;
+        while (nn * nn > (e % rmax) + 1) nn--;
+        while ((nn + 1) * (nn + 1) <= (e % rmax) + 1) nn++;
+        const int aa = e / rmax;
+        return cmul(pin(e), ms[aa * L + nn - 1]);
+    };
+    // ---- p_scat, p_int, cross-sections
+    const double f = 4.0 * kPi / (k * k);
+    long long xo = 0;
+    if (a.xs) xo = ((a.obs_off[s] + i) * R + rr) * 3LL * 2 * L;
+    if (a.xs)
+        for (int c = 0; c < 6 * L; c++) a.xs[xo + c] = 0.0;
+    for (int aa = 0; aa < 2; aa++)
+        for (int n = 1; n <= L; n++) {
+            double cabs = 0.0, cext = 0.0;
+            for (int m = -n; m <= n; m++) {
+                const int e = aa * rmax + n * n + n + m - 1;
+                const double2 pi_ = pin(e);
+                const double2 ps = cmul(pi_, ms[aa * L + n - 1]);
+                if (a.p_scat) a.p_scat[vb + (long long)e * R] = ps;
+                if (a.p_int) a.p_int[vb + (long long)e * R] = cmul(pi_, mi[(1 - aa) * L + n - 1]);
+                if (a.xs) {
+                    const double2 pr = psrc(e);
+                    cabs += f * ((pi_.x * ps.x + pi_.y * ps.y) - (ps.x * ps.x + ps.y * ps.y));
+                    cext += f * (pr.x * ps.x + pr.y * ps.y);
+                }
+            }
+            if (a.xs) {
+                const int idx = aa * L + n - 1;
+                a.xs[xo + 0 * 2 * L + idx] = cext - cabs;   // scattering
+                a.xs[xo + 1 * 2 * L + idx] = cabs;          // absorption
+                a.xs[xo + 2 * 2 * L + idx] = cext;          // extinction
+            }
+        }
+    if (!a.force && !a.torque) return;
+    // ---- force / torque: p, q = scattered electric / magnetic; pi, qi = incident
+    auto P = [&](int r) { return pscat(r); };
+    auto Qs = [&](int r) { return pscat(rmax + r); };
+    auto PI = [&](int r) { return a.source ? pin(r) : csub(pin(r), psrc(r)); };
+    auto QI = [&](int r) { return a.source ? pin(rmax + r) : csub(pin(rmax + r), psrc(rmax + r)); };
+    const double eb = a.eps_b;
+    if (a.force) {
+        double2 Fxy = make_double2(0, 0), Fz = make_double2(0, 0);
+        const double Axy = kPi / (k * k) * kEps0 * eb;
+        const double Az = -2 * Axy;
+        for (int n = 1; n <= L; n++)
+            for (int m = -n; m <= n; m++) {
+                const int r = n * n + n + m - 1;
+                const double2 p = P(r), q = Qs(r), pi_ = PI(r), qi = QI(r);
+                if (m != n) {
+                    const double fc = Axy * sqrt((double)((n + m + 1) * (n - m))) / (double)(n * (n + 1));
+                    const int r1 = r + 1;
+                    const double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
+                    double2 t = cadd(tri(p, q1, pi_, qi1), tri(q, p1, qi, pi1));
+                    // p conj(q1) form: 2 p q1* - p qi1* - pi q1*  +  2 q p1* - q pi1* - qi p1*
+                    Fxy = cadd(Fxy, cscale(fc, t));
+                }
+                const double fz = Az * m / (double)(n * (n + 1));
+                Fz = cadd(Fz, cscale(fz, tri(p, q, pi_, qi)));
+                if (n < L) {
+                    double fc = -Axy * sqrt((double)((n + m + 2) * (n + m + 1) * n * (n + 2)) /
+                                            (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
+                    int r1 = (n + 1) * (n + 1) + (n + 1) + m;
+                    double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
+                    Fxy = cadd(Fxy, cscale(fc, cadd(tri(p, p1, pi_, pi1), tri(q, q1, qi, qi1))));
+                    fc = Axy * sqrt((double)((n - m + 1) * (n - m + 2) * n * (n + 2)) /
+                                    (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
+                    r1 = (n + 1) * (n + 1) + (n + 1) + m - 2;
+                    p1 = P(r1); q1 = Qs(r1); pi1 = PI(r1); qi1 = QI(r1);
+                    Fxy = cadd(Fxy, cscale(fc, cadd(tri(p1, p, pi1, pi_), tri(q1, q, qi1, qi))));
+                    fc = Az * sqrt((double)((n - m + 1) * (n + m + 1) * n * (n + 2)) /
+                                   (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
+                    r1 = (n + 1) * (n + 1) + (n + 1) + m - 1;
+                    p1 = P(r1); q1 = Qs(r1); pi1 = PI(r1); qi1 = QI(r1);
+                    Fz = cadd(Fz, cscale(fc, cadd(tri(p1, p, pi1, pi_), tri(q1, q, qi1, qi))));
+                }
+            }
+        const long long fo = ((a.obs_off[s] + i) * R + rr) * 3LL;
+        a.force[fo + 0] = Fxy.x;
+        a.force[fo + 1] = Fxy.y;
+        a.force[fo + 2] = Fz.x;
+    }
+    if (a.torque) {
+        const double A = -2 * kPi / (k * k * k) * kEps0 * eb;
+        double T0 = 0, T1 = 0, T2 = 0;
+        for (int n = 1; n <= L; n++)
+            for (int m = -n; m <= n; m++) {
+                const int r = n * n + n + m - 1;
+                const double2 p = P(r), q = Qs(r), pi_ = PI(r), qi = QI(r);
+                if (m != n) {
+                    const double fc = -A * sqrt((double)((n - m) * (n + m + 1)));
+                    const int r1 = r + 1;
+                    const double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
+                    const double2 base = cadd(cmul(p, cj(p1)), cmul(q, cj(q1)));
+                    const double2 sx = cadd(cadd(cmul(p1, cj(pi_)), cmul(p, cj(pi1))), cadd(cmul(q1, cj(qi)), cmul(q, cj(qi1))));
+                    const double2 sy = cadd(csub(cmul(p1, cj(pi_)), cmul(p, cj(pi1))), csub(cmul(q1, cj(qi)), cmul(q, cj(qi1))));
+                    T0 += fc * (base.x - 0.5 * sx.x);
+                    T1 += fc * (base.y + 0.5 * sy.y);
+                }
+                const double fz = A * m;
+                const double2 c = cadd(cmul(p, cj(pi_)), cmul(q, cj(qi)));
+                T2 += fz * ((p.x * p.x + p.y * p.y) + (q.x * q.x + q.y * q.y) - c.x);
+            }
+        const long long fo = ((a.obs_off[s] + i) * R + rr) * 3LL;
+        a.torque[fo + 0] = T0;
+        a.torque[fo + 1] = T1;
+        a.torque[fo + 2] = T2;
+    }
+}
+
+}   // namespace
+
+extern "C" int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const int64_t* mie_off,
+                                 const int64_t* obs_off, const double* mie_scat, const double* mie_int,
+                                 const double* p_inc, const double* p_src, double eps_b, int source, double* p_scat,
+                                 double* p_int, double* xs, double* force, double* torque, void* stream) {
+    if (nsys < 1 || !sys || !mie_off || !obs_off || !mie_scat || !p_inc || R < 1)
+        return gb_set_error(GB_BAD_ARG, "bad epilogue arguments");
+    if ((xs || !source) && !p_src) return gb_set_error(GB_BAD_ARG, "p_src required");
+    if (p_int && !mie_int) return gb_set_error(GB_BAD_ARG, "mie_int required for p_int");
+    cudaStream_t st_ = (cudaStream_t)stream;
+    std::vector<gb::SysDev> sd;
+    int st = gb::make_sysdev(nsys, sys, st_, sd);
+    if (st) return st;
+    std::vector<long long> base(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) base[s + 1] = base[s] + (long long)sd[s].N * R;
+    std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * (3 * nsys + 1));
+    unsigned char* w = blob.data();
+    memcpy(w, sd.data(), sizeof(gb::SysDev) * nsys);
+    w += sizeof(gb::SysDev) * nsys;
+    memcpy(w, base.data(), sizeof(long long) * (nsys + 1));
+    w += sizeof(long long) * (nsys + 1);
+    memcpy(w, mie_off, sizeof(long long) * nsys);
+    w += sizeof(long long) * nsys;
+    memcpy(w, obs_off, sizeof(long long) * nsys);
+    void* dblob = nullptr;
+    int slot = 0;
+    st = gb::stage_acquire(blob.data(), blob.size(), st_, &dblob, &slot);
+    if (st) return st;
+    unsigned char* d = static_cast<unsigned char*>(dblob);
+    EpiArgs a;
+    a.sys = reinterpret_cast<const gb::SysDev*>(d);
+    a.base = reinterpret_cast<const long long*>(d + sizeof(gb::SysDev) * nsys);
+    a.mie_off = a.base + (nsys + 1);
+    a.obs_off = a.mie_off + nsys;
+    a.nsys = nsys;
+    a.R = R;
+    a.source = source;
+    a.mie_scat = reinterpret_cast<const double2*>(mie_scat);
+    a.mie_int = reinterpret_cast<const double2*>(mie_int);
+    a.p_inc = reinterpret_cast<const double2*>(p_inc);
+    a.p_src = reinterpret_cast<const double2*>(p_src);
+    a.eps_b = eps_b;
+    a.p_scat = reinterpret_cast<double2*>(p_scat);
+    a.p_int = reinterpret_cast<double2*>(p_int);
+    a.xs = xs;
+    a.force = force;
+    a.torque = torque;
+    const long long total = base[nsys];
+    k_epilogue<<<(unsigned)((total + 127) / 128), 128, 0, st_>>>(a, total);
+    GB_CUDA_TRY(cudaGetLastError());
+    return gb::stage_release(slot, st_);
+}
+
+// Per-particle cross-sections from given coefficients (flux.particle_cross_sections,
+// cpp/src/flux.cpp:5-30): one thread per (particle, a, n).
+namespace {
+__global__ void k_particle_xs(int N, int lmax, const double2* __restrict__ ps, const double2* __restrict__ pi,
+                              const double2* __restrict__ pr, double k, double* __restrict__ out) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= N * 2 * lmax) return;
+    const int i = g / (2 * lmax), idx = g % (2 * lmax), a = idx / lmax, n = idx % lmax + 1;
+    const int rmax = lmax * (lmax + 2);
+    const double f = 4.0 * 3.14159265358979323846 / (k * k);
+    double cabs = 0.0, cext = 0.0;
+    for (int m = -n; m <= n; m++) {
+        const long long e = (long long)i * 2 * rmax + a * rmax + n * n + n + m - 1;
+        const double2 s = ps[e], c = pi[e], r = pr[e];
+        cabs += f * ((c.x * s.x + c.y * s.y) - (s.x * s.x + s.y * s.y));
+        cext += f * (r.x * s.x + r.y * s.y);
+    }
+    double* o = out + (long long)i * 6 * lmax;
+    o[idx] = cext - cabs;
+    o[2 * lmax + idx] = cabs;
+    o[4 * lmax + idx] = cext;
+}
+}   // namespace
+
+extern "C" int gb_particle_cross_sections(int N, int lmax, const double* p_scat, const double* p_inc,
+                                          const double* p_src, double k, double* out, void* stream) {
+    if (N < 1 || lmax < 1 || !p_scat || !p_inc || !p_src || !out) return gb_set_error(GB_BAD_ARG, "bad arguments");
+    const int total = N * 2 * lmax;
+    k_particle_xs<<<(total + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+        N, lmax, reinterpret_cast<const double2*>(p_scat), reinterpret_cast<const double2*>(p_inc),
+        reinterpret_cast<const double2*>(p_src), k, out);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}

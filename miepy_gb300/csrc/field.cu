@@ -1,0 +1,273 @@
+// K8: near field of a cluster on a set of points.
+//
+// Follows sphere_cluster.E_field / H_field (sphere_cluster.py:244-391): outside
+// the spheres the outgoing expansions of p_scat about every particle are summed
+// (expand_E, vsh/expansion.py:13-42, VSH N/M of vsh/vsh_functions.py:40-78 /
+// cpp/src/vsh_functions.cpp:60-98, converted with vec_sph_to_cart); a point
+// inside sphere i instead takes the interior expansion of p_int[i] with
+// j_n(k_int r) (complex argument, the upward recurrence of
+// cpp/src/special.cpp:20-45).  H fields use expand_H: the polarisation-swapped
+// coefficients times -i sqrt(eps/mu).
+//
+// One thread per point; particles are streamed through shared memory in tiles of
+// 16 with their coefficients; E_mn and the negative-order Legendre factors are
+// tabulated once per CTA.
+
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_internal.h"
+
+namespace {
+
+constexpr int kFieldThreads = 128;
+
+__device__ __forceinline__ double2 cdivd(double2 a, double2 b) {
+    const double den = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+__device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csin(double2 z) {
+    double s, c;
+    sincos(z.x, &s, &c);
+    return make_double2(s * cosh(z.y), c * sinh(z.y));
+}
+__device__ __forceinline__ double2 ccos(double2 z) {
+    double s, c;
+    sincos(z.x, &s, &c);
+    return make_double2(c * cosh(z.y), -s * sinh(z.y));
+}
+
+// E_mn = i^n sqrt((2n+1)(n-m)!/(n(n+1)(n+m)!))  (cpp/src/vsh_functions.cpp:56-58)
+__device__ double2 Emn(int m, int n) {
+    double mag = sqrt((2.0 * n + 1) * tgamma((double)(n - m) + 1.0) / ((double)n * (n + 1) * tgamma((double)(n + m) + 1.0)));
+    switch (n & 3) {
+        case 0: return make_double2(mag, 0);
+        case 1: return make_double2(0, mag);
+        case 2: return make_double2(-mag, 0);
+        default: return make_double2(0, -mag);
+    }
+}
+
+// Adds the expansion of coefficients c [2][rmax] about a particle to E (spherical
+// components, then Cartesian).  outgoing: h_n of real kr, factor i;
+// otherwise j_n of complex kr, factor -i.
+constexpr int kLF = 8;   // largest expansion order of the field kernel
+
+__device__ void add_expansion(int L, const double2* __restrict__ c, int rmax, bool outgoing, double2 k, double rad,
+                              double theta, double phi, bool swap, double2 pref, const double2* __restrict__ emn,
+                              const double* __restrict__ negf_tab, double2 E[3]) {
+    const int NP = L + 2;
+    // radial functions z_n and derivatives for n = 0..L (the reference's recurrences)
+    double2 z[kLF + 2], zp[kLF + 2];
+    const double2 kr = make_double2(k.x * rad, k.y * rad);
+    if (outgoing) {
+        const double x = kr.x;
+        double s, co;
+        sincos(x, &s, &co);
+        double j0 = s / x, y0 = -co / x;
+        z[0] = make_double2(j0, y0);
+        double j1 = j0 / x - co / x, y1 = y0 / x - j0;
+        if (NP > 1) z[1] = make_double2(j1, y1);
+        double ja = j0, jb = j1, ya = y0, yb = y1;
+#pragma unroll 1
+        for (int n = 2; n < NP; n++) {
+            double jn = (2 * n - 1) / x * jb - ja, yn = (2 * n - 1) / x * yb - ya;
+            ja = jb; jb = jn; ya = yb; yb = yn;
+            z[n] = make_double2(jn, yn);
+        }
+    } else {
+        const double2 sz = csin(kr), cz = ccos(kr);
+        z[0] = cdivd(sz, kr);
+        if (NP > 1) {
+            double2 t = cdivd(z[0], kr);
+            double2 u = cdivd(cz, kr);
+            z[1] = make_double2(t.x - u.x, t.y - u.y);
+        }
+#pragma unroll 1
+        for (int n = 2; n < NP; n++) {
+            double2 f = cdivd(make_double2(2.0 * n - 1, 0), kr);
+            double2 a = cmul(f, z[n - 1]);
+            z[n] = make_double2(a.x - z[n - 2].x, a.y - z[n - 2].y);
+        }
+    }
+    // derivative z_n' = z_{n-1} - (n+1)/kr z_n, n >= 1
+#pragma unroll 1
+    for (int n = 1; n <= L; n++) {
+        double2 f = cdivd(make_double2((double)(n + 1), 0), kr);
+        double2 a = cmul(f, z[n]);
+        zp[n] = make_double2(z[n - 1].x - a.x, z[n - 1].y - a.y);
+    }
+    // Legendre P_n^m (m >= 0, no Condon-Shortley phase) for n <= L+1
+    const double x = cos(theta);
+    const double u = sqrt(fmax(0.0, (1.0 - x) * (1.0 + x)));
+    double P[kLF + 2][kLF + 3];
+#pragma unroll 1
+    for (int a = 0; a < L + 2; a++)
+#pragma unroll 1
+        for (int b = 0; b < L + 3; b++) P[a][b] = 0.0;
+    P[0][0] = 1.0;
+#pragma unroll 1
+    for (int m = 1; m <= L + 1; m++) P[m][m] = (2 * m - 1) * u * P[m - 1][m - 1];
+#pragma unroll 1
+    for (int m = 0; m <= L; m++) P[m + 1][m] = x * (2 * m + 1) * P[m][m];
+#pragma unroll 1
+    for (int m = 0; m <= L + 1; m++)
+#pragma unroll 1
+        for (int n = m + 2; n <= L + 1; n++)
+            P[n][m] = ((2 * n - 1) * x * P[n - 1][m] - (n + m - 1) * P[n - 2][m]) / (double)(n - m);
+    const bool at0 = (theta == 0.0), atpi = (theta == 3.14159265358979323846);
+    const double st = sin(theta), ct = x;
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    const double2 fac = outgoing ? make_double2(0, 1) : make_double2(0, -1);
+    double2 Es[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+#pragma unroll 1
+    for (int n = 1; n <= L; n++) {
+#pragma unroll 1
+        for (int m = -n; m <= n; m++) {
+            const int am = m < 0 ? -m : m;
+            const int r = n * n + n + m - 1;
+            const double negf = negf_tab[r];
+            const double Pnm = negf * P[n][am];
+            double pi_v, tau_v;
+            if (at0 || atpi) {
+                const double sgn = atpi ? (((n + 1) & 1) ? -1.0 : 1.0) : 1.0;    // (-1)^(n+1) at pi
+                const double sgt = atpi ? ((n & 1) ? -1.0 : 1.0) : 1.0;          // (-1)^n at pi
+                if (m == 1) { pi_v = sgn * n * (n + 1) / 2.0; tau_v = sgt * n * (n + 1) / 2.0; }
+                else if (m == -1) { pi_v = sgn * 0.5; tau_v = -sgt * 0.5; }
+                else { pi_v = 0.0; tau_v = 0.0; }
+            } else {
+                pi_v = m / st * Pnm;
+                const double pm1 = (am >= 1) ? P[n][am - 1] : -P[n][1] / (double)(n * (n + 1));
+                const double pp1 = (am + 1 <= n) ? P[n][am + 1] : 0.0;
+                tau_v = negf * 0.5 * ((n + am) * (n - am + 1) * pm1 - pp1);
+            }
+            double sm, cm;
+            sincos((double)m * phi, &sm, &cm);
+            const double2 eph = make_double2(cm, sm);
+            const double2 H = z[n], Hp = zp[n];
+            // N: (n(n+1) P H/kr e, (H + kr H') e/kr tau, i (H + kr H') e/kr pi)
+            const double2 hk = cdivd(cmul(H, eph), kr);
+            const double2 g = cdivd(cmul(make_double2(H.x + (kr.x * Hp.x - kr.y * Hp.y), H.y + (kr.x * Hp.y + kr.y * Hp.x)), eph), kr);
+            const double2 N0 = make_double2(n * (n + 1) * Pnm * hk.x, n * (n + 1) * Pnm * hk.y);
+            const double2 N1 = make_double2(g.x * tau_v, g.y * tau_v);
+            const double2 N2 = make_double2(-g.y * pi_v, g.x * pi_v);
+            // M: (0, i pi H e, -tau H e)
+            const double2 he = cmul(H, eph);
+            const double2 M1 = make_double2(-he.y * pi_v, he.x * pi_v);
+            const double2 M2 = make_double2(-he.x * tau_v, -he.y * tau_v);
+            const double2 c0 = swap ? c[rmax + r] : c[r];
+            const double2 c1 = swap ? c[r] : c[rmax + r];
+            const double2 w = cmul(fac, emn[r]);
+            const double2 w0 = cmul(w, c0), w1 = cmul(w, c1);
+            double2 t;
+            t = cmul(w0, N0); Es[0].x += t.x; Es[0].y += t.y;
+            t = cadd2(cmul(w0, N1), cmul(w1, M1)); Es[1].x += t.x; Es[1].y += t.y;
+            t = cadd2(cmul(w0, N2), cmul(w1, M2)); Es[2].x += t.x; Es[2].y += t.y;
+        }
+    }
+    // spherical -> Cartesian (vec_sph_to_cart), times the prefactor
+    const double rh[3] = {st * cp, st * sp, ct}, th[3] = {ct * cp, ct * sp, -st}, ph[3] = {-sp, cp, 0.0};
+    for (int d = 0; d < 3; d++) {
+        double2 v = make_double2(Es[0].x * rh[d] + Es[1].x * th[d] + Es[2].x * ph[d],
+                                 Es[0].y * rh[d] + Es[1].y * th[d] + Es[2].y * ph[d]);
+        v = cmul(pref, v);
+        E[d].x += v.x;
+        E[d].y += v.y;
+    }
+}
+
+__global__ void __launch_bounds__(kFieldThreads)
+k_field(int L, int N, const double* __restrict__ pos, const double* __restrict__ radius, const double2* __restrict__ p_scat,
+        const double2* __restrict__ p_int, double k, const double2* __restrict__ k_int, int Npts,
+        const double* __restrict__ pts, int interior, int magnetic, double2 hfac, const double2* __restrict__ hfac_int,
+        double2* __restrict__ out) {
+    const int rmax = L * (L + 2);
+    constexpr int kTile = 16;
+    __shared__ double sp_pos[kTile][3];
+    __shared__ double2 sp_c[kTile * 2 * kLF * (kLF + 2)];
+    __shared__ double2 emn[kLF * (kLF + 2)];
+    __shared__ double negf_tab[kLF * (kLF + 2)];
+    for (int r = threadIdx.x; r < rmax; r += blockDim.x) {
+        int n = (int)floor(sqrt((double)r + 1.0));
+        while (n * n > r + 1) n--;
+        while ((n + 1) * (n + 1) <= r + 1) n++;
+        const int m = r + 1 - n * n - n;
+        emn[r] = Emn(m, n);
+        const int am = m < 0 ? -m : m;
+        negf_tab[r] = (m < 0) ? (((am & 1) ? -1.0 : 1.0) * tgamma((double)(n - am) + 1.0) / tgamma((double)(n + am) + 1.0)) : 1.0;
+    }
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = pt < Npts;
+    double X = 0, Y = 0, Z = 0;
+    if (valid) {
+        X = pts[3LL * pt];
+        Y = pts[3LL * pt + 1];
+        Z = pts[3LL * pt + 2];
+    }
+    // interior test first (the reference overwrites interior points)
+    int inside = -1;
+    if (interior && valid) {
+        for (int i = 0; i < N; i++) {
+            const double dx = X - pos[3 * i], dy = Y - pos[3 * i + 1], dz = Z - pos[3 * i + 2];
+            if (dx * dx + dy * dy + dz * dz < radius[i] * radius[i]) inside = i;   // last match wins, as in the reference loop
+        }
+    }
+    double2 E[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+    const double2 pref_out = magnetic ? hfac : make_double2(1, 0);
+    for (int t0 = 0; t0 < N; t0 += kTile) {
+        const int cnt = min(kTile, N - t0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt * 3; e += blockDim.x) sp_pos[e / 3][e % 3] = pos[3LL * t0 + e];
+        for (int e = threadIdx.x; e < cnt * 2 * rmax; e += blockDim.x)
+            sp_c[e] = p_scat[(long long)t0 * 2 * rmax + e];
+        __syncthreads();
+        if (!valid || inside >= 0) continue;
+        for (int q = 0; q < cnt; q++) {
+            const double dx = X - sp_pos[q][0], dy = Y - sp_pos[q][1], dz = Z - sp_pos[q][2];
+            const double rad = sqrt(dx * dx + dy * dy + dz * dz);
+            const double theta = acos(dz / rad);
+            const double phi = atan2(dy, dx);
+            add_expansion(L, sp_c + q * 2 * rmax, rmax, true, make_double2(k, 0), rad, theta, phi, magnetic != 0,
+                          pref_out, emn, negf_tab, E);
+        }
+    }
+    if (!valid) return;
+    if (inside >= 0) {
+        const int i = inside;
+        const double dx = X - pos[3 * i], dy = Y - pos[3 * i + 1], dz = Z - pos[3 * i + 2];
+        const double rad = sqrt(dx * dx + dy * dy + dz * dz);
+        const double theta = acos(dz / rad);
+        const double phi = atan2(dy, dx);
+        const double2 pref = magnetic ? hfac_int[i] : make_double2(1, 0);
+        add_expansion(L, p_int + (long long)i * 2 * rmax, rmax, false, k_int[i], rad, theta, phi, magnetic != 0, pref,
+                      emn, negf_tab, E);
+    }
+    for (int d = 0; d < 3; d++) out[3LL * pt + d] = E[d];
+}
+
+}   // namespace
+
+extern "C" int gb_near_field(int N, int lmax, const double* pos, const double* radius, const double* p_scat,
+                             const double* p_int, double k, const double* k_int, int Npts, const double* pts,
+                             int interior, int magnetic, double hfac_re, double hfac_im, const double* hfac_int,
+                             double* out, void* stream) {
+    if (N < 1 || Npts < 0 || !pos || !p_scat || !pts || !out) return gb_set_error(GB_BAD_ARG, "bad field arguments");
+    if (interior && (!radius || !p_int || !k_int)) return gb_set_error(GB_BAD_ARG, "interior fields need radius, p_int, k_int");
+    if (magnetic && interior && !hfac_int) return gb_set_error(GB_BAD_ARG, "interior H fields need hfac_int");
+    if (Npts == 0) return GB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned grid = (unsigned)((Npts + kFieldThreads - 1) / kFieldThreads);
+    const double2 hf = make_double2(hfac_re, hfac_im);
+    const double2* pi2 = reinterpret_cast<const double2*>(p_int);
+    const double2* ps2 = reinterpret_cast<const double2*>(p_scat);
+    const double2* ki2 = reinterpret_cast<const double2*>(k_int);
+    const double2* hi2 = reinterpret_cast<const double2*>(hfac_int);
+    double2* o2 = reinterpret_cast<double2*>(out);
+    if (lmax < 1 || lmax > kLF) return gb_set_error(GB_UNSUPPORTED, "near field supports lmax 1..%d (got %d)", kLF, lmax);
+    k_field<<<grid, kFieldThreads, 0, s>>>(lmax, N, pos, radius, ps2, pi2, k, ki2, Npts, pts, interior, magnetic, hf,
+                                           hi2, o2);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}

@@ -1,0 +1,54 @@
+// Internal host-side declarations shared by the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <vector>
+
+#include "../../include/miepy_gb300.h"
+
+namespace gb {
+
+// Per-lmax device tables (see tables.cu).
+struct Tables {
+    int lmax = 0, M = 0, rmax = 0, B = 0;
+    int4* nmvu = nullptr;      // [M] canonical tuples (n, m, v, u)
+    int2* qab = nullptr;       // [M] (qmax_A, qmax_B)
+    double* cA = nullptr;      // [M][lmax+1]
+    double* cB = nullptr;      // [M][lmax+1]
+    int* elem_map = nullptr;   // [B*B] (tuple << 2) | (is_B << 1) | negate
+    double* neg_ratio = nullptr;   // [(2L+2)^2] (-1)^mu (p-mu)!/(p+mu)!
+    int* rowinfo = nullptr;    // [B] rho(row) | eps_neg << 29 | sig_neg << 30
+    int* miecol = nullptr;     // [B] a*lmax + n - 1
+};
+
+int get_tables(int lmax, cudaStream_t stream, const Tables** out);
+int host_tuples(int L, std::vector<int4>& nmvu);
+
+int sm_count();
+
+// Device-side description of one cluster of a batch (expanded from gb_system).
+struct SysDev {
+    int N, lmax, rmax, B, D;
+    int M;                  // tuples of this lmax
+    long long P;            // pairs
+    double k;
+    long long pos_off, mat_off, vec_off, t_off;
+    // table pointers for this lmax
+    const int4* nmvu;
+    const int2* qab;
+    const double* cA;
+    const double* cB;
+    const int* elem_map;
+    const double* neg_ratio;
+    const int* rowinfo;
+    const int* miecol;
+};
+
+// Pinned staging ring for per-call descriptor uploads (assemble.cu).
+int stage_acquire(const void* src, size_t bytes, cudaStream_t stream, void** dev_out, int* slot_out);
+int stage_release(int slot, cudaStream_t stream);
+
+int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector<SysDev>& out);
+
+}   // namespace gb

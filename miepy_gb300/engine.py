@@ -1,0 +1,222 @@
+"""Device-resident batches of sphere clusters.
+
+A ClusterBatch owns, on one GPU, everything a set of independent cluster solves
+needs: positions, Mie coefficients, the packed translation matrices (complex128
+and/or complex64), right-hand sides, solutions, workspace and observables.  The
+single-cluster solver, the wavelength sweep and the solve server all drive this
+one class; every step is a call into the CUDA extension.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .modes import lmax_to_rmax
+
+PRECISIONS = {"fp64": nat.PREC_FP64, "mixed": nat.PREC_MIXED, "fp32": nat.PREC_FP32}
+
+
+def current_stream(device=None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("miepy_gb300 needs a CUDA device (GB300); no CPU fallback exists")
+    nat.lib()
+    return torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+
+
+def matrix_elements(N, lmax):
+    B = 2 * lmax_to_rmax(lmax)
+    return N * (N - 1) // 2 * B * B
+
+
+def footprint_bytes(N, lmax, R=1, precision="fp64"):
+    """HBM bytes a cluster needs inside a batch (matrices + vectors + solver scratch), for admission."""
+    el = matrix_elements(N, lmax)
+    D = 2 * lmax_to_rmax(lmax) * N
+    mat = (16 * el if precision in ("fp64", "mixed") else 0) + (8 * el if precision in ("mixed", "fp32") else 0)
+    P = N * (N - 1) // 2
+    B = 2 * lmax_to_rmax(lmax)
+    partials = 16 * (P * B * R + (P + N) * B * R)
+    vec = 16 * D * R * 16
+    return mat + partials + vec + 4096
+
+
+class ClusterBatch:
+    """Independent clusters sharing launch sequences.
+
+    specs: list of dicts with
+        position [N,3] float, mie_scat [N,2,lmax] complex, k float (medium wavenumber),
+        p_src [N,2,rmax,R] complex (or [N,2,rmax] when R == 1),
+        optional mie_int [N,2,lmax], eps_b float.
+    """
+
+    def __init__(self, specs, R=1, precision="fp64", device=None):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {list(PRECISIONS)}")
+        self.device = require_cuda(device)
+        self.R = int(R)
+        self.precision = precision
+        self.specs = specs
+        self.nsys = len(specs)
+        descs, mie_off, obs_off = [], [], []
+        pos_off = mat_off = vec_off = t_off = m_off = o_off = 0
+        self.layout = []
+        for s in specs:
+            pos = np.asarray(s["position"], float).reshape(-1, 3)
+            N = pos.shape[0]
+            lmax = int(np.asarray(s["mie_scat"]).shape[-1])
+            rmax = lmax_to_rmax(lmax)
+            D = 2 * rmax * N
+            el = matrix_elements(N, lmax)
+            descs.append((N, lmax, float(np.real(s["k"])), pos_off, mat_off, vec_off, t_off))
+            mie_off.append(m_off)
+            obs_off.append(o_off)
+            self.layout.append(dict(N=N, lmax=lmax, rmax=rmax, D=D, pos_off=pos_off, mat_off=mat_off, vec_off=vec_off,
+                                    t_off=t_off, mie_off=m_off, obs_off=o_off))
+            pos_off += 3 * N
+            mat_off += el
+            vec_off += D * self.R
+            t_off += D
+            m_off += N * 2 * lmax
+            o_off += N
+        self.totals = dict(pos=pos_off, mat=mat_off, vec=vec_off, t=t_off, mie=m_off, obs=o_off)
+        self.sys = nat.systems_array(descs)
+        self.mie_off = np.asarray(mie_off, dtype=np.int64)
+        self.obs_off = np.asarray(obs_off, dtype=np.int64)
+        dev = self.device
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        self.pos = torch.empty(max(pos_off, 1), dtype=torch.float64, device=dev)
+        self.mie_scat = torch.empty(max(m_off, 1), dtype=torch.complex128, device=dev)
+        self.mie_int = torch.empty(max(m_off, 1), dtype=torch.complex128, device=dev)
+        self.b = torch.empty(max(vec_off, 1), dtype=torch.complex128, device=dev)
+        hpos = np.concatenate([np.asarray(s["position"], float).reshape(-1) for s in specs])
+        hmie = np.concatenate([np.asarray(s["mie_scat"], complex).reshape(-1) for s in specs])
+        hint = np.concatenate([np.asarray(s.get("mie_int", np.zeros_like(s["mie_scat"])), complex).reshape(-1)
+                               for s in specs])
+        hb = np.concatenate([np.asarray(s["p_src"], complex).reshape(-1) for s in specs])
+        self.pos.copy_(pin(hpos), non_blocking=True)
+        self.mie_scat.copy_(pin(hmie), non_blocking=True)
+        self.mie_int.copy_(pin(hint), non_blocking=True)
+        self.b.copy_(pin(hb), non_blocking=True)
+        self.h2d_bytes = hpos.nbytes + hmie.nbytes + hint.nbytes + hb.nbytes
+        self.tvec = torch.empty(max(t_off, 1), dtype=torch.complex128, device=dev)
+        self.x = torch.zeros(max(vec_off, 1), dtype=torch.complex128, device=dev)
+        need128 = precision in ("fp64", "mixed")
+        need64 = precision in ("mixed", "fp32")
+        self.mat128 = torch.empty(max(mat_off, 1), dtype=torch.complex128, device=dev) if need128 else None
+        self.mat64 = torch.empty(max(mat_off, 1), dtype=torch.complex64, device=dev) if need64 else None
+        self._ws = None
+        self.status = self.iters = self.resid = None
+        self.assembled = False
+
+    # ---------------------------------------------------------------- steps --
+    def assemble(self):
+        L = nat.lib()
+        st = current_stream(self.device)
+        nat.check(L.gb_expand_mie_batch(self.nsys, self.sys, self.mie_off.ctypes.data, nat.ptr(self.mie_scat),
+                                        nat.ptr(self.tvec), st), "expand mie")
+        if self.totals["mat"] > 0:
+            nat.check(L.gb_assemble_batch(self.nsys, self.sys, nat.ptr(self.pos), nat.ptr(self.mat128),
+                                          nat.ptr(self.mat64), st), "assemble")
+        self.assembled = True
+        return self
+
+    def workspace(self, prec_code):
+        L = nat.lib()
+        need = L.gb_solve_workspace_size(self.nsys, self.sys, self.R, prec_code)
+        if need == 0:
+            raise nat.GBError(nat.GB_BAD_ARG, "workspace query failed: " + nat.last_error())
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def solve(self, tol=1e-5, maxiter=1000, inner_tol=1e-6, max_refine=6, precision=None, raise_on_fail=False):
+        if not self.assembled:
+            self.assemble()
+        precision = precision or self.precision
+        code = PRECISIONS[precision]
+        L = nat.lib()
+        ws = self.workspace(code)
+        n = self.nsys * self.R
+        status = np.zeros(n, dtype=np.int32)
+        iters = np.zeros(n, dtype=np.int32)
+        resid = np.zeros(n, dtype=np.float64)
+        rc = L.gb_solve_batch(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
+                              int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64), nat.ptr(self.tvec),
+                              nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data,
+                              iters.ctypes.data, resid.ctypes.data, current_stream(self.device))
+        if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN) or (raise_on_fail and rc):
+            nat.check(rc, "solve")
+        self.status, self.iters, self.resid = status, iters, resid
+        return status
+
+    def apply(self, x, precision="fp64"):
+        """y = (I + T) x on the packed matrices (x: device complex128 [total_vec])."""
+        L = nat.lib()
+        code = PRECISIONS[precision]
+        need = L.gb_apply_workspace_size(self.nsys, self.sys, self.R, code)
+        ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        y = torch.empty_like(x)
+        nat.check(L.gb_apply_batch(self.nsys, self.sys, self.R, code, nat.ptr(self.mat128), nat.ptr(self.mat64),
+                                   nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y), nat.ptr(ws), ws.numel(),
+                                   current_stream(self.device)), "apply")
+        return y
+
+    def epilogue(self, eps_b, source=True, want_fields=True):
+        """p_scat, p_int (device, [total_vec]) and per particle xs [N,R,3,2lmax], force/torque [N,R,3]."""
+        L = nat.lib()
+        dev = self.device
+        n_obs = self.totals["obs"]
+        lmaxes = [l["lmax"] for l in self.layout]
+        if len(set(lmaxes)) != 1:
+            xs_len = sum(l["N"] * self.R * 6 * l["lmax"] for l in self.layout)
+        else:
+            xs_len = n_obs * self.R * 6 * lmaxes[0]
+        self.p_scat = torch.empty_like(self.x) if want_fields else None
+        self.p_int = torch.empty_like(self.x) if want_fields else None
+        # xs offsets assume a common lmax per batch; ragged batches get per-cluster calls
+        out = []
+        if len(set(lmaxes)) == 1:
+            xs = torch.empty(max(xs_len, 1), dtype=torch.float64, device=dev)
+            F = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
+            T = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
+            nat.check(L.gb_epilogue_batch(self.nsys, self.sys, self.R, self.mie_off.ctypes.data,
+                                          self.obs_off.ctypes.data, nat.ptr(self.mie_scat), nat.ptr(self.mie_int),
+                                          nat.ptr(self.x), nat.ptr(self.b), float(np.real(eps_b)), int(bool(source)),
+                                          nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
+                                          nat.ptr(T), current_stream(dev)), "epilogue")
+            self.xs, self.F, self.T = xs, F, T
+            return self
+        # ragged lmax: obs offsets in units of particles of each cluster's own lmax
+        xs_parts, F_parts, T_parts = [], [], []
+        for s, l in enumerate(self.layout):
+            sub = nat.systems_array([tuple(getattr(self.sys[s], f) for f, _ in nat.gb_system._fields_)])
+            xs = torch.empty(l["N"] * self.R * 6 * l["lmax"], dtype=torch.float64, device=dev)
+            F = torch.empty(l["N"] * self.R * 3, dtype=torch.float64, device=dev)
+            T = torch.empty(l["N"] * self.R * 3, dtype=torch.float64, device=dev)
+            mo = np.asarray([l["mie_off"]], dtype=np.int64)
+            oo = np.zeros(1, dtype=np.int64)
+            nat.check(L.gb_epilogue_batch(1, sub, self.R, mo.ctypes.data, oo.ctypes.data, nat.ptr(self.mie_scat),
+                                          nat.ptr(self.mie_int), nat.ptr(self.x), nat.ptr(self.b),
+                                          float(np.real(eps_b[s] if np.ndim(eps_b) else eps_b)), int(bool(source)),
+                                          nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
+                                          nat.ptr(T), current_stream(dev)), "epilogue")
+            xs_parts.append(xs)
+            F_parts.append(F)
+            T_parts.append(T)
+            out.append(xs)
+        self.xs = torch.cat(xs_parts)
+        self.F = torch.cat(F_parts)
+        self.T = torch.cat(T_parts)
+        return self
+
+    # ------------------------------------------------------------- accessors --
+    def cluster_view(self, s, t):
+        """Slice of a [total_vec] device vector for cluster s as [N, 2, rmax, R]."""
+        l = self.layout[s]
+        return t[l["vec_off"]: l["vec_off"] + l["D"] * self.R].view(l["N"], 2, l["rmax"], self.R)

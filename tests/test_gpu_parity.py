@@ -1,0 +1,286 @@
+"""GPU parity tests: the CUDA path against the oracle and the golden fixtures.
+
+Tolerances (stated per assertion): translation tables and assembled matrices
+1e-12 relative to the largest entry; FP64 solves against the exact solution
+1e-10 (p coefficients) and 1e-9 (cross-sections, forces, torques); BiCGSTAB at
+the reference's tolerance against the reference's own BiCGSTAB result 1e-4 (the
+reference's own GPU-vs-CPU bar); complex64 products 2e-6; mixed precision
+C_ext within 1e-6 of FP64.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import miepy_gb300 as gb
+from miepy_gb300 import _native as nat
+from miepy_gb300.engine import ClusterBatch, current_stream
+from oracle import oracle as O
+from tests import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+nm = 1e-9
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(np.asarray(b))), 1e-300))
+
+
+def batch_from_golden(g, precision="fp64", R=1):
+    return ClusterBatch([dict(position=g["position"], mie_scat=g["mie_scat"], mie_int=g["mie_int"], k=float(g["k_b"]),
+                              p_src=g["p_src"])], R=R, precision=precision)
+
+
+def random_cluster(rng, N, rmin, rmax_, box):
+    pos, rad = [], []
+    while len(pos) < N:
+        r = rng.uniform(rmin, rmax_)
+        c = rng.uniform(0, box, size=3)
+        if all(np.linalg.norm(c - p) > r + q for p, q in zip(pos, rad)):
+            pos.append(c)
+            rad.append(r)
+    return np.array(pos), np.array(rad)
+
+
+# ------------------------------------------------------------------ tables --
+@pytest.mark.parametrize("lmax", [1, 2, 4, 6, 8])
+def test_translation_tables_match_oracle_cache(lmax):
+    L = nat.lib()
+    M = ctypes.c_int(0)
+    assert L.gb_tables_count(lmax, ctypes.byref(M)) == 0
+    M = M.value
+    Q = lmax + 1
+    nmvu = np.zeros((M, 4), np.int32)
+    qab = np.zeros((M, 2), np.int32)
+    cA = np.zeros((M, Q))
+    cB = np.zeros((M, Q))
+    nat.check(L.gb_tables_export(lmax, nmvu.ctypes.data, qab.ctypes.data, cA.ctypes.data, cB.ctypes.data, None))
+    worst = 0.0
+    for t in range(M):
+        n, m, v, u = nmvu[t]
+        factor, qa, qb, A, B = O.vsh_cache_entry(n, -m, v, u)
+        assert (qa, qb) == tuple(qab[t])
+        ia = (1j) ** (n + v)
+        expA = np.real(factor * A / ia)
+        expB = np.real(-factor * B[1:] / (ia * 1j))
+        scale = max(np.max(np.abs(expA)), 1e-300)
+        worst = max(worst, np.max(np.abs(cA[t, : qa + 1] - expA)) / scale)
+        if qb >= 1:
+            worst = max(worst, np.max(np.abs(cB[t, 1: qb + 1] - expB)) / max(np.max(np.abs(expB)), 1e-300))
+    assert worst < 1e-12, worst
+
+
+# --------------------------------------------------------------- assembly --
+def dense_on_device(pos, mie, k, lmax):
+    dev = torch.device("cuda")
+    N = pos.shape[0]
+    D = 2 * lmax * (lmax + 2) * N
+    P = torch.from_numpy(np.ascontiguousarray(pos)).to(dev)
+    Mi = torch.from_numpy(np.ascontiguousarray(mie)).to(dev)
+    out = torch.empty((D, D), dtype=torch.complex128, device=dev)
+    nat.check(nat.lib().gb_assemble_sphere_dense(N, lmax, nat.ptr(P), nat.ptr(Mi), float(k), nat.ptr(out),
+                                                 current_stream()))
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["dimer_lmax6_exact", "ag5_lmax2_exact"])
+def test_dense_assembly_matches_reference(name):
+    g = G.load(name)
+    T = dense_on_device(g["position"], g["mie_scat"], g["k_b"], int(g["lmax"]))
+    ref = g["agg_tmatrix"].reshape(T.shape)
+    assert rel(T, ref) < 1e-12
+
+
+@pytest.mark.parametrize("N,lmax,seed", [(7, 3, 1), (4, 8, 2), (12, 1, 3), (9, 5, 4)])
+def test_dense_assembly_matches_oracle_random(N, lmax, seed):
+    rng = np.random.default_rng(seed)
+    pos, _ = random_cluster(rng, N, 50 * nm, 90 * nm, 1200 * nm)
+    mie = rng.normal(size=(N, 2, lmax)) + 1j * rng.normal(size=(N, 2, lmax))
+    k = 2 * np.pi / (600 * nm)
+    T = dense_on_device(pos, mie, k, lmax)
+    ref = O.sphere_aggregate_tmatrix(pos, mie.reshape(N, -1), k)
+    assert rel(T, ref) < 1e-12
+
+
+@pytest.mark.parametrize("N,lmax,R", [(6, 3, 1), (5, 4, 2), (3, 8, 2), (25, 2, 1), (40, 3, 2)])
+def test_packed_operator_matches_oracle_matvec(N, lmax, R):
+    rng = np.random.default_rng(N * 10 + lmax)
+    pos, _ = random_cluster(rng, N, 40 * nm, 80 * nm, 1500 * nm)
+    mie = (rng.normal(size=(N, 2, lmax)) + 1j * rng.normal(size=(N, 2, lmax))) * 0.3
+    k = 2 * np.pi / (650 * nm)
+    rmax = lmax * (lmax + 2)
+    x = rng.normal(size=(N, 2, rmax, R)) + 1j * rng.normal(size=(N, 2, rmax, R))
+    T = O.sphere_aggregate_tmatrix(pos, mie.reshape(N, -1), k)
+    D = T.shape[0]
+    ref = np.stack([O.gemv(T, x.reshape(D, R)[:, r]) + x.reshape(D, R)[:, r] for r in range(R)], axis=1)
+    b = ClusterBatch([dict(position=pos, mie_scat=mie, k=k, p_src=x)], R=R, precision="mixed").assemble()
+    xd = torch.from_numpy(x.reshape(-1)).to(b.device)
+    y128 = b.apply(xd, "fp64").cpu().numpy().reshape(D, R)
+    y64 = b.apply(xd, "fp32").cpu().numpy().reshape(D, R)
+    assert rel(y128, ref) < 1e-12
+    assert rel(y64, ref) < 2e-6
+
+
+# ------------------------------------------------------------------ solves --
+@pytest.mark.parametrize("name", G.EXACT_CASES)
+def test_fp64_solve_matches_exact_reference(name):
+    g = G.load(name)
+    b = batch_from_golden(g).assemble()
+    b.solve(tol=1e-14, maxiter=2000)
+    assert b.status[0] == 0
+    N = g["position"].shape[0]
+    x = b.cluster_view(0, b.x)[..., 0].cpu().numpy()
+    scale = np.max(np.abs(g["p_inc"]))
+    np.testing.assert_allclose(x, g["p_inc"], rtol=1e-10, atol=1e-14 * scale)
+    b.epilogue(np.real(g["eps_b"]))
+    L = int(g["lmax"])
+    ps = b.cluster_view(0, b.p_scat)[..., 0].cpu().numpy()
+    pi_ = b.cluster_view(0, b.p_int)[..., 0].cpu().numpy()
+    np.testing.assert_allclose(ps, g["p_scat"], rtol=1e-10, atol=1e-14 * np.max(np.abs(g["p_scat"])))
+    np.testing.assert_allclose(pi_, g["p_int"], rtol=1e-10, atol=1e-14 * np.max(np.abs(g["p_int"])))
+    xs = b.xs[: N * 6 * L].view(N, 3, 2, L).cpu().numpy()
+    tot = xs.sum(axis=(0, 2, 3))
+    np.testing.assert_allclose(tot, g["cross_sections"], rtol=1e-9)
+    ref_per = g["cross_sections_per_multipole"]
+    assert rel(xs, ref_per) < 1e-9
+    F = b.F[: N * 3].view(N, 3).cpu().numpy()
+    T = b.T[: N * 3].view(N, 3).cpu().numpy()
+    assert rel(F, g["force"]) < 1e-9
+    assert rel(T, g["torque"]) < 1e-9
+    b.epilogue(np.real(g["eps_b"]), source=False, want_fields=False)
+    assert rel(b.F[: N * 3].view(N, 3).cpu().numpy(), g["force_nosource"]) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["dimer_lmax6_bicgstab", "ag5_lmax2_bicgstab"])
+def test_bicgstab_reference_tolerance_matches_reference_run(name):
+    g = G.load(name)
+    b = batch_from_golden(g).assemble()
+    b.solve(tol=1e-5, maxiter=1000)
+    x = b.cluster_view(0, b.x)[..., 0].cpu().numpy()
+    np.testing.assert_allclose(x, g["p_inc"], rtol=1e-4, atol=1e-14 * np.max(np.abs(g["p_inc"])))
+    # same algorithm, same start: the iterates agree far below the tolerance
+    assert rel(x, g["p_inc"]) < 1e-8
+
+
+def test_mixed_precision_meets_fp64_within_1e6():
+    rng = np.random.default_rng(11)
+    N, lmax = 40, 4
+    pos, rad = random_cluster(rng, N, 50 * nm, 100 * nm, 1200 * nm)
+    mat = gb.constant_material(index=1.5 + 0.01j)
+    specs = []
+    for pol in ("x", "y"):
+        pass
+    c64 = gb.sphere_cluster(position=pos, radius=rad, material=mat, source=gb.plane_wave.from_string("x"),
+                            wavelength=600 * nm, lmax=lmax, precision="mixed", tol=1e-10)
+    c128 = gb.sphere_cluster(position=pos, radius=rad, material=mat, source=gb.plane_wave.from_string("x"),
+                             wavelength=600 * nm, lmax=lmax, precision="fp64", tol=1e-12)
+    e64 = c64.cross_sections().extinction
+    e128 = c128.cross_sections().extinction
+    assert abs(e64 - e128) / abs(e128) < 1e-6
+    assert rel(c64.p_inc, c128.p_inc) < 1e-8
+    c32 = gb.sphere_cluster(position=pos, radius=rad, material=mat, source=gb.plane_wave.from_string("x"),
+                            wavelength=600 * nm, lmax=lmax, precision="fp32", tol=1e-6)
+    assert abs(c32.cross_sections().extinction - e128) / abs(e128) < 1e-4
+
+
+def test_ragged_batch_equals_individual_solves():
+    rng = np.random.default_rng(5)
+    specs = []
+    for N, lmax in ((3, 2), (8, 4), (5, 3), (2, 6)):
+        pos, _ = random_cluster(rng, N, 40 * nm, 80 * nm, 900 * nm)
+        mie = (rng.normal(size=(N, 2, lmax)) + 1j * rng.normal(size=(N, 2, lmax))) * 0.2
+        p = rng.normal(size=(N, 2, lmax * (lmax + 2), 2)) + 0j
+        specs.append(dict(position=pos, mie_scat=mie, mie_int=mie, k=2 * np.pi / (600 * nm), p_src=p))
+    for prec in ("fp64", "mixed"):
+        bb = ClusterBatch(specs, R=2, precision=prec).assemble()
+        bb.solve(tol=1e-12)
+        for s, spec in enumerate(specs):
+            one = ClusterBatch([spec], R=2, precision=prec).assemble()
+            one.solve(tol=1e-12)
+            a = bb.cluster_view(s, bb.x).cpu().numpy()
+            c = one.cluster_view(0, one.x).cpu().numpy()
+            assert rel(a, c) < 1e-10, (prec, s)
+            # and against the oracle's exact solution, per right-hand side
+            T = O.sphere_aggregate_tmatrix(spec["position"], spec["mie_scat"].reshape(spec["position"].shape[0], -1),
+                                           spec["k"])
+            for r in range(2):
+                ex = O.solve_linear_system(T, spec["p_src"][..., r].ravel(), "exact")
+                assert rel(a[..., r].ravel(), ex) < 1e-9
+
+
+def test_public_cluster_api_dimer():
+    g = G.load("dimer_lmax6_exact")
+    c = gb.sphere_cluster(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm,
+                          material=gb.constant_material(index=0.2 + 3.0j), source=gb.plane_wave.from_string("x"),
+                          wavelength=600 * nm, lmax=6, medium=gb.materials.water(), method=gb.solver.exact)
+    np.testing.assert_allclose(c.p_inc, g["p_inc"], rtol=1e-10, atol=1e-14 * np.max(np.abs(g["p_inc"])))
+    C = c.cross_sections()
+    np.testing.assert_allclose([C.scattering, C.absorption, C.extinction], g["cross_sections"], rtol=1e-9)
+    assert rel(c.force(), g["force"]) < 1e-9
+    assert rel(c.torque(), g["torque"]) < 1e-9
+    for i in range(2):
+        Fi = c.force_on_particle(i)
+        assert rel(Fi, g["force"][i]) < 1e-9
+
+
+def test_near_fields_match_reference():
+    for name in ("dimer_lmax6_exact", "rand12_lmax3_exact"):
+        g = G.load(name)
+        pos, rad = g["position"], g["radius"]
+        lmax = int(g["lmax"])
+        N = pos.shape[0]
+        dev = torch.device("cuda")
+        d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+        x, y, z = g["field_x"], g["field_y"], g["field_z"]
+        pts = d(np.stack([x, y, z], 1), torch.float64)
+        k_int = d(2 * np.pi * g["n"] / g["wavelength"], torch.complex128)
+        out = torch.empty((len(x), 3), dtype=torch.complex128, device=dev)
+        nat.check(nat.lib().gb_near_field(N, lmax, nat.ptr(d(pos, torch.float64)), nat.ptr(d(rad, torch.float64)),
+                                          nat.ptr(d(g["p_scat"], torch.complex128)),
+                                          nat.ptr(d(g["p_int"], torch.complex128)), float(g["k_b"]), nat.ptr(k_int),
+                                          len(x), nat.ptr(pts), 0, 0, 1.0, 0.0, None, nat.ptr(out), current_stream()))
+        E = out.cpu().numpy().T
+        assert rel(E, g["E_scat_only"]) < 1e-9, name
+
+
+def test_cluster_fields_match_reference():
+    g = G.load("dimer_lmax6_exact")
+    c = gb.sphere_cluster(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm,
+                          material=gb.constant_material(index=0.2 + 3.0j), source=gb.plane_wave.from_string("x"),
+                          wavelength=600 * nm, lmax=6, medium=gb.materials.water(), method=gb.solver.exact)
+    x, y, z = g["field_x"], g["field_y"], g["field_z"]
+    assert rel(c.E_field(x, y, z), g["E_total"]) < 1e-8
+    assert rel(c.H_field(x, y, z), g["H_total"]) < 1e-8
+
+
+def test_plugin_backend_functions():
+    g = G.load("ag5_lmax2_exact")
+    from miepy_gb300 import backend
+    T = backend.sphere_aggregate_tmatrix_jax(g["position"], g["mie_scat"], g["k_b"])
+    assert rel(np.asarray(T), g["agg_tmatrix"]) < 1e-12
+    p = backend.solve_linear_system_jax(T, g["p_src"], gb.solver.exact)
+    np.testing.assert_allclose(p, g["p_inc"], rtol=1e-10, atol=1e-14 * np.max(np.abs(g["p_inc"])))
+    p2 = backend.solve_linear_system_jax(np.asarray(T), g["p_src"], gb.solver.exact)
+    np.testing.assert_allclose(p2, g["p_inc"], rtol=1e-10, atol=1e-14 * np.max(np.abs(g["p_inc"])))
+    Cs, Ca, Ce = backend.particle_cross_sections_jax(g["p_scat"][0], g["p_inc"][0], g["p_src"][0], g["k_b"])
+    ref = g["cross_sections_per_multipole"][0]
+    assert rel(np.array([Cs, Ca, Ce]), ref) < 1e-12
+    one = backend.sphere_aggregate_tmatrix_jax(g["position"][:1], g["mie_scat"][:1], g["k_b"])
+    assert np.all(np.asarray(one) == 0)
+
+
+def test_full_size_random_cluster_residual():
+    """N = 200, lmax = 4 (D = 9600), two polarisations: the FP64 solution satisfies
+    the oracle's own matrix equation (a size-independent check)."""
+    rng = np.random.default_rng(2)
+    pos, rad = random_cluster(rng, 200, 50 * nm, 100 * nm, 2000 * nm)
+    mat = gb.constant_material(index=1.5 + 0.01j)
+    c = gb.sphere_cluster(position=pos, radius=rad, material=mat, source=gb.plane_wave.from_string("x"),
+                          wavelength=600 * nm, lmax=4, tol=1e-12)
+    assert c.solver_status == 0
+    T = O.sphere_aggregate_tmatrix(pos, c.mie_scat.reshape(200, -1), c.material_data.k_b)
+    r = O.gemv(T, c.p_inc.ravel()) + c.p_inc.ravel() - c.p_src.ravel()
+    assert np.linalg.norm(r) / np.linalg.norm(c.p_src) < 1e-11
