@@ -49,13 +49,18 @@ extern "C" {
 #define GB_UNSUPPORTED 8
 
 /* precision of a solve */
-#define GB_PREC_FP64 0       /* complex128 matrix, complex128 Krylov vectors */
-#define GB_PREC_MIXED 1      /* complex64 matrix + complex64 BiCGSTAB, FP64 refinement on the complex128 matrix */
-#define GB_PREC_FP32 2       /* complex64 matrix + complex64 BiCGSTAB, no refinement */
+#define GB_PREC_FP64 0           /* complex128 matrix, complex128 Krylov vectors, FP64 arithmetic */
+#define GB_PREC_MIXED 1          /* complex64 BiCGSTAB on the hi matrix; refinement residuals with the
+                                    double-float (hi + lo) matrix, ~1e-14 relative accuracy, FP32 pipes */
+#define GB_PREC_FP32 2           /* complex64 matrix + complex64 BiCGSTAB, no refinement */
+#define GB_PREC_MIXED_FP64RES 3  /* as MIXED, refinement residuals in FP64 arithmetic on the complex128 matrix */
 
 int gb_version(void);
 size_t gb_last_error(char* buf, size_t cap);
 int gb_device_sm_count(void);
+/* Number of kernels this library has launched in the process so far (graph
+ * replays count every kernel node they run). */
+long long gb_launch_count(void);
 
 /* ---------------------------------------------------------------- tables --
  * Per-lmax translation coefficient table (replaces create_vsh_cache_map,
@@ -75,10 +80,11 @@ int gb_tables_export(int lmax, int* nmvu, int* qab, double* cA, double* cB, int*
 int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* mie, double k,
                              double* out, void* stream);
 
-/* Packed pair-block translation matrix of one cluster (see above).  Either
- * output may be NULL: out128 [P*B*B] c128, out64 [P*B*B] c64. */
+/* Packed pair-block translation matrix of one cluster (see above).  Any
+ * output may be NULL: out128 [P*B*B] c128; out64 [P*B*B] c64 = fl32(a);
+ * out64lo [P*B*B] c64 = fl32(a - fl32(a)) (hi + lo carries ~48 bits). */
 int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,
-                              void* stream);
+                              float* out64lo, void* stream);
 
 /* ------------------------------------------------------ batched clusters --
  * A batch describes independent clusters (ragged N and lmax) that share one
@@ -93,9 +99,10 @@ typedef struct {
     int64_t t_off;      /* into the per-row Mie factor vector (complex128): first of D */
 } gb_system;
 
-/* Assemble the packed matrices of every cluster in the batch (one launch). */
+/* Assemble the packed matrices of every cluster in the batch (one launch);
+ * outputs as for gb_assemble_sphere_packed, any may be NULL. */
 int gb_assemble_batch(int nsys, const gb_system* sys, const double* pos, double* mat128, float* mat64,
-                      void* stream);
+                      float* mat64lo, void* stream);
 
 /* Expand Mie coefficients [N,2,lmax] into the per-row factor t (D entries) for
  * every cluster; mie_off[s] is the complex offset of cluster s in mie. */
@@ -108,14 +115,16 @@ int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, 
  * tiny, stop when |r| <= tol |b|).  R right-hand sides per cluster share every
  * matrix pass.  b and x are [D][R] complex128 per cluster at vec_off.
  * prec: GB_PREC_FP64 uses mat128; GB_PREC_FP32 uses mat64; GB_PREC_MIXED runs
- * FP32 BiCGSTAB on mat64 to inner_tol and refines with FP64 residuals on
- * mat128 until |b - (I+T)x| <= tol |b| (at most max_refine passes).
- * status/iters/resid: host arrays of nsys*R entries (may be NULL). */
+ * FP32 BiCGSTAB on mat64 to inner_tol and refines x with residuals computed
+ * from mat64 + mat64lo until |b - (I+T)x| <= tol |b| (at most max_refine
+ * refinement passes); GB_PREC_MIXED_FP64RES takes its residuals from mat128.
+ * status/iters/resid: host arrays of nsys*R entries (may be NULL); iters are
+ * BiCGSTAB iterations (FP64/FP32) or refinement passes (mixed). */
 size_t gb_solve_workspace_size(int nsys, const gb_system* sys, int R, int prec);
 int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
-                   int max_refine, const double* mat128, const float* mat64, const double* tvec, const double* b,
-                   double* x, void* workspace, size_t ws_bytes, int* status, int* iters, double* resid,
-                   void* stream);
+                   int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
+                   const double* tvec, const double* b, double* x, void* workspace, size_t ws_bytes, int* status,
+                   int* iters, double* resid, void* stream);
 
 /* Dense solve of (I + T) x = b for a caller-supplied dense aggregate matrix
  * T [D,D] c128 (the plugin path, where the caller already holds T).  BiCGSTAB as
@@ -124,11 +133,14 @@ size_t gb_solve_dense_workspace_size(int D, int R);
 int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, double tol, int maxiter,
                    void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, void* stream);
 
-/* One application y = (I + T) x of the packed operator (c128 if prec == FP64,
- * else c64), for tests and benchmarks.  x, y: [D][R] complex128. */
+/* One application y = (I + T) x of the packed operator, for tests and
+ * benchmarks: FP64 arithmetic on mat128 (GB_PREC_FP64), FP32 on mat64
+ * (GB_PREC_FP32) or double-float on mat64 + mat64lo (GB_PREC_MIXED).
+ * x, y: [D][R] complex128. */
 size_t gb_apply_workspace_size(int nsys, const gb_system* sys, int R, int prec);
 int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
-                   const double* tvec, const double* x, double* y, void* workspace, size_t ws_bytes, void* stream);
+                   const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
+                   size_t ws_bytes, void* stream);
 
 /* -------------------------------------------------------------- epilogue --
  * Per cluster and right-hand side, from p_inc [D][R] (c128), p_src [D][R],

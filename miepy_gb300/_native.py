@@ -20,7 +20,7 @@ c_int, c_double, c_size_t, c_void_p, c_int64 = ctypes.c_int, ctypes.c_double, ct
 _P = c_void_p
 
 GB_OK, GB_NOT_CONVERGED, GB_BREAKDOWN, GB_NAN, GB_OVER_BUDGET, GB_TIMEOUT, GB_BAD_ARG, GB_CUDA_ERROR, GB_UNSUPPORTED = range(9)
-PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_FP32, PREC_MIXED_FP64RES = 0, 1, 2, 3
 STATUS_NAMES = {0: "ok", 1: "not converged", 2: "breakdown", 3: "nan", 4: "over budget", 5: "timeout",
                 6: "bad argument", 7: "cuda error", 8: "unsupported", -1: "running"}
 
@@ -40,20 +40,21 @@ SIGNATURES = {
     "gb_version": (c_int, []),
     "gb_last_error": (c_size_t, [ctypes.c_char_p, c_size_t]),
     "gb_device_sm_count": (c_int, []),
+    "gb_launch_count": (ctypes.c_longlong, []),
     "gb_tables_prepare": (c_int, [c_int, _P]),
     "gb_tables_count": (c_int, [c_int, ctypes.POINTER(c_int)]),
     "gb_tables_export": (c_int, [c_int, _P, _P, _P, _P, _P]),
     "gb_assemble_sphere_dense": (c_int, [c_int, c_int, _P, _P, c_double, _P, _P]),
-    "gb_assemble_sphere_packed": (c_int, [c_int, c_int, _P, c_double, _P, _P, _P]),
-    "gb_assemble_batch": (c_int, [c_int, _P, _P, _P, _P, _P]),
+    "gb_assemble_sphere_packed": (c_int, [c_int, c_int, _P, c_double, _P, _P, _P, _P]),
+    "gb_assemble_batch": (c_int, [c_int, _P, _P, _P, _P, _P, _P]),
     "gb_expand_mie_batch": (c_int, [c_int, _P, _P, _P, _P, _P]),
     "gb_solve_workspace_size": (c_size_t, [c_int, _P, c_int, c_int]),
     "gb_solve_batch": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P, _P,
-                               c_size_t, _P, _P, _P, _P]),
+                               _P, c_size_t, _P, _P, _P, _P]),
     "gb_solve_dense_workspace_size": (c_size_t, [c_int, c_int]),
     "gb_solve_dense": (c_int, [c_int, c_int, _P, _P, _P, c_double, c_int, _P, c_size_t, _P, _P, _P, _P]),
     "gb_apply_workspace_size": (c_size_t, [c_int, _P, c_int, c_int]),
-    "gb_apply_batch": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, c_size_t, _P]),
+    "gb_apply_batch": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_size_t, _P]),
     "gb_epilogue_batch": (c_int, [c_int, _P, c_int, _P, _P, _P, _P, _P, _P, c_double, c_int, _P, _P, _P, _P, _P,
                                   _P]),
     "gb_particle_cross_sections": (c_int, [c_int, c_int, _P, _P, _P, c_double, _P, _P]),

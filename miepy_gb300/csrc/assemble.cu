@@ -30,7 +30,7 @@ constexpr int kAsmThreads = 256;
 
 struct AsmSmem {
     int PM, MU, M;
-    size_t off_h, off_P, off_e, off_G, off_T, off_Tf, total;
+    size_t off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
 };
 
 __host__ __device__ inline AsmSmem asm_layout(int L, int M, bool want64) {
@@ -45,6 +45,7 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, bool want64) {
     s.off_T = o;  o += sizeof(double2) * 2 * M;
     s.off_P = o;  o += sizeof(double) * s.PM * s.PM;
     s.off_Tf = o; o += want64 ? sizeof(float2) * 2 * M : 0;
+    s.off_Tl = o; o += want64 ? sizeof(float2) * 2 * M : 0;
     s.total = (o + 15) & ~size_t(15);
     return s;
 }
@@ -72,20 +73,21 @@ template <bool DENSE>
 __global__ void __launch_bounds__(kAsmThreads)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ pair_base, long long total,
            const double* __restrict__ pos, const double2* __restrict__ mie, double2* __restrict__ out128,
-           float2* __restrict__ out64, long long dense_ld) {
+           float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     for (long long g = blockIdx.x; g < total; g += gridDim.x) {
         const int s = find_sys(pair_base, nsys, g);
         const gb::SysDev S = sys[s];
         const int L = S.lmax, B = S.B, N = S.N;
-        const AsmSmem lay = asm_layout(L, S.M, out64 != nullptr);
+        const AsmSmem lay = asm_layout(L, S.M, out64 != nullptr || out64lo != nullptr);
         double2* h = reinterpret_cast<double2*>(smem + lay.off_h);
         double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);
         double2* G = reinterpret_cast<double2*>(smem + lay.off_G);
         double2* Tv = reinterpret_cast<double2*>(smem + lay.off_T);
         double* Pl = reinterpret_cast<double*>(smem + lay.off_P);
         float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
+        float2* Tl = reinterpret_cast<float2*>(smem + lay.off_Tl);
         const int PM = lay.PM, MU = lay.MU;
 
         const long long p = g - pair_base[s];
@@ -178,9 +180,13 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
             Tv[2 * t] = At;
             Tv[2 * t + 1] = Bt;
-            if (!DENSE && out64) {
-                Tf[2 * t] = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
-                Tf[2 * t + 1] = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
+            if (!DENSE && (out64 || out64lo)) {
+                const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
+                const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
+                Tf[2 * t] = ah;
+                Tf[2 * t + 1] = bh;
+                Tl[2 * t] = make_float2(__double2float_rn(At.x - (double)ah.x), __double2float_rn(At.y - (double)ah.y));
+                Tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
             }
         }
         __syncthreads();
@@ -199,6 +205,10 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 if (out64) {
                     const float2 v = Tf[code >> 1];
                     out64[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+                }
+                if (out64lo) {
+                    const float2 v = Tl[code >> 1];
+                    out64lo[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
                 }
             }
         } else {
@@ -351,7 +361,7 @@ int stage_release(int slot, cudaStream_t stream) {
 namespace {
 
 int launch_assemble(int nsys, const gb_system* sys, const double* pos, const double* mie, double* out128,
-                    float* out64, long long dense_ld, bool dense, cudaStream_t stream) {
+                    float* out64, float* out64lo, long long dense_ld, bool dense, cudaStream_t stream) {
     std::vector<gb::SysDev> sd;
     int st = gb::make_sysdev(nsys, sys, stream, sd);
     if (st) return st;
@@ -374,7 +384,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     if (st) return st;
     const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
     const long long* dbase = reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys);
-    const AsmSmem lay = asm_layout(Lmax, Mmax, out64 != nullptr && !dense);
+    const AsmSmem lay = asm_layout(Lmax, Mmax, (out64 != nullptr || out64lo != nullptr) && !dense);
     const size_t smem = lay.total;
     int per_sm = 1;
     if (dense) {
@@ -386,14 +396,17 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     }
     if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
     long long grid = std::min<long long>(total, (long long)gb::sm_count() * per_sm);
-    if (dense)
+    if (dense) {
+        gb::note_launch();
         k_assemble<true><<<(unsigned)grid, kAsmThreads, smem, stream>>>(
             dsys, nsys, dbase, total, pos, reinterpret_cast<const double2*>(mie), reinterpret_cast<double2*>(out128),
-            nullptr, dense_ld);
-    else
+            nullptr, nullptr, dense_ld);
+    } else {
+        gb::note_launch();
         k_assemble<false><<<(unsigned)grid, kAsmThreads, smem, stream>>>(
             dsys, nsys, dbase, total, pos, nullptr, reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64),
-            0);
+            reinterpret_cast<float2*>(out64lo), 0);
+    }
     GB_CUDA_TRY(cudaGetLastError());
     return gb::stage_release(slot, stream);
 }
@@ -410,20 +423,21 @@ int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* m
     GB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double2) * D * D, (cudaStream_t)stream));
     if (N == 1) return GB_OK;
     gb_system s{N, lmax, k, 0, 0, 0, 0};
-    return launch_assemble(1, &s, pos, mie, out, nullptr, D, true, (cudaStream_t)stream);
+    return launch_assemble(1, &s, pos, mie, out, nullptr, nullptr, D, true, (cudaStream_t)stream);
 }
 
 int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,
-                              void* stream) {
-    if (!pos || (!out128 && !out64)) return gb_set_error(GB_BAD_ARG, "null pointer");
+                              float* out64lo, void* stream) {
+    if (!pos || (!out128 && !out64 && !out64lo)) return gb_set_error(GB_BAD_ARG, "null pointer");
     gb_system s{N, lmax, k, 0, 0, 0, 0};
-    return launch_assemble(1, &s, pos, nullptr, out128, out64, 0, false, (cudaStream_t)stream);
+    return launch_assemble(1, &s, pos, nullptr, out128, out64, out64lo, 0, false, (cudaStream_t)stream);
 }
 
 int gb_assemble_batch(int nsys, const gb_system* sys, const double* pos, double* mat128, float* mat64,
-                      void* stream) {
-    if (nsys < 1 || !sys || !pos || (!mat128 && !mat64)) return gb_set_error(GB_BAD_ARG, "bad batch arguments");
-    return launch_assemble(nsys, sys, pos, nullptr, mat128, mat64, 0, false, (cudaStream_t)stream);
+                      float* mat64lo, void* stream) {
+    if (nsys < 1 || !sys || !pos || (!mat128 && !mat64 && !mat64lo))
+        return gb_set_error(GB_BAD_ARG, "bad batch arguments");
+    return launch_assemble(nsys, sys, pos, nullptr, mat128, mat64, mat64lo, 0, false, (cudaStream_t)stream);
 }
 
 int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, const double* mie, double* tvec,
@@ -443,6 +457,7 @@ int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, 
     int maxD = 0;
     for (auto& d : sd) maxD = std::max(maxD, d.D);
     dim3 grid((maxD + 255) / 256, nsys);
+    gb::note_launch();
     k_expand_mie<<<grid, 256, 0, st_>>>(reinterpret_cast<const gb::SysDev*>(dblob), nsys,
                                         reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys),
                                         reinterpret_cast<const double2*>(mie), reinterpret_cast<double2*>(tvec));

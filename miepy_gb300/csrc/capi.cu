@@ -1,5 +1,6 @@
 // Library-wide C-ABI helpers: version, error reporting, device queries.
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -9,7 +10,20 @@
 
 namespace {
 thread_local char g_err[1024] = {0};
+std::atomic<long long> g_launches{0};
+thread_local int g_capturing = 0;
+thread_local long long g_captured = 0;
 }
+
+namespace gb {
+void note_launch() {
+    if (g_capturing) g_captured++;
+    else g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void capture_begin() { g_capturing = 1; g_captured = 0; }
+long long capture_end() { g_capturing = 0; return g_captured; }
+}   // namespace gb
 
 int gb_set_error(int code, const char* fmt, ...) {
     va_list ap;
@@ -41,5 +55,7 @@ size_t gb_last_error(char* buf, size_t cap) {
 }
 
 int gb_device_sm_count(void) { return gb::sm_count(); }
+
+long long gb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 }   // extern "C"

@@ -221,6 +221,7 @@ extern "C" int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const in
     a.force = force;
     a.torque = torque;
     const long long total = base[nsys];
+    gb::note_launch();
     k_epilogue<<<(unsigned)((total + 127) / 128), 128, 0, st_>>>(a, total);
     GB_CUDA_TRY(cudaGetLastError());
     return gb::stage_release(slot, st_);
@@ -254,6 +255,7 @@ extern "C" int gb_particle_cross_sections(int N, int lmax, const double* p_scat,
                                           const double* p_src, double k, double* out, void* stream) {
     if (N < 1 || lmax < 1 || !p_scat || !p_inc || !p_src || !out) return gb_set_error(GB_BAD_ARG, "bad arguments");
     const int total = N * 2 * lmax;
+    gb::note_launch();
     k_particle_xs<<<(total + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
         N, lmax, reinterpret_cast<const double2*>(p_scat), reinterpret_cast<const double2*>(p_inc),
         reinterpret_cast<const double2*>(p_src), k, out);

@@ -266,6 +266,7 @@ extern "C" int gb_near_field(int N, int lmax, const double* pos, const double* r
     const double2* hi2 = reinterpret_cast<const double2*>(hfac_int);
     double2* o2 = reinterpret_cast<double2*>(out);
     if (lmax < 1 || lmax > kLF) return gb_set_error(GB_UNSUPPORTED, "near field supports lmax 1..%d (got %d)", kLF, lmax);
+    gb::note_launch();
     k_field<<<grid, kFieldThreads, 0, s>>>(lmax, N, pos, radius, ps2, pi2, k, ki2, Npts, pts, interior, magnetic, hf,
                                            hi2, o2);
     GB_CUDA_TRY(cudaGetLastError());

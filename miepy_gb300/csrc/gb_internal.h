@@ -27,6 +27,13 @@ int host_tuples(int L, std::vector<int4>& nmvu);
 
 int sm_count();
 
+// Kernel-launch accounting (gb_launch_count): direct launches call note_launch;
+// launches recorded into a CUDA graph are counted once per graph replay.
+void note_launch();
+void note_launches(long long n);
+void capture_begin();
+long long capture_end();
+
 // Device-side description of one cluster of a batch (expanded from gb_system).
 struct SysDev {
     int N, lmax, rmax, B, D;

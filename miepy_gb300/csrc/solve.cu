@@ -14,17 +14,29 @@
 //   y_w[r] = eps(r) sig(r) t_i[rho(r)] x_i[rho(r)]      (for block row j)
 // and (A_ij z_j)[r] = eps(r) c_u[rho(r)],  (S A_ij S z_i)[r] = sig(r) eps(r) c_w[rho(r)].
 // Column sums let a warp stream a block row by row with every lane owning fixed
-// columns: 128-bit coalesced loads, per-lane accumulators, no cross-lane traffic.
+// columns: 128-bit coalesced loads, per-lane accumulators, no per-row cross-lane
+// reduction.  A lane owns NS "slots" (row offset, column group) so that RPS rows
+// are covered per step by all 32 lanes; slot sums of one column are combined in
+// shared memory once per block.
+//
+// Three arithmetic policies share the kernel:
+//   Pol64  complex128 matrix, FP64 FMAs (the plain method);
+//   Pol32  complex64 matrix, FP32 FMAs (inner solves of the mixed method);
+//   PolDF  double-float: the complex128 matrix stored as complex64 hi + lo
+//          (hi = fl32(a), lo = fl32(a - hi)), x split the same way, every hi*hi
+//          product formed exactly (FMA two-product) and accumulated with TwoSum;
+//          the residual of the mixed method at about 1e-14 relative accuracy,
+//          on the FP32 pipes (GB300's FP64 rate is 1/58 of its FP32 rate).
 //
 // K3a (k_pgemv): warp per strip of consecutive blocks (i, j0..j0+J-1) of one block
-//   row.  c_u accumulates across the strip (written once per strip), c_w is
-//   written per block.  Deterministic: no atomics.
-// K3b (k_reduce): thread per row; sums the strip / block partials in a fixed order,
+//   row; c_u accumulates across the strip, c_w is written per block.
+// K3b (k_reduce): 8 warps x 32 rows; warps split the partial terms of a row, a
+//   fixed-order shared-memory sum combines them (deterministic, no atomics),
 //   adds the identity term and emits per-item partial dot products.
 // K4: BiCGSTAB vector updates fused with the dot-product partials, and one-thread-
-//   per-(cluster, rhs) scalar kernels; all scalars stay on the device.  The host
-//   launches fixed chunks of iterations and reads back one flag array per chunk;
-//   kernels of finished clusters return immediately.
+//   per-(cluster, rhs) scalar kernels; all scalars stay on the device.  Chunks of
+//   iterations are captured once into a CUDA graph and replayed; the host reads one
+//   flag array per chunk and finished clusters' kernels return immediately.
 //
 // The iteration is Eigen's: x0 = 0, r0 = r = b, rho = alpha = omega = 1, restart
 // with r = b - A x when |rho| < eps^2 |r0|^2, stop when |r|^2 <= tol^2 |b|^2.
@@ -32,6 +44,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -39,15 +54,15 @@
 
 namespace {
 
-constexpr int kItemRows = 128;      // rows per vector/reduce work item (= threads per CTA)
-constexpr int kGemvThreads = 256;   // 8 warps
-constexpr int kChunk = 4;           // iterations per host check
+constexpr int kVRows = 128;        // rows per vector work item (= threads per CTA)
+constexpr int kRRows = 32;         // rows per reduce work item
+constexpr int kRWarps = 8;         // warps per reduce CTA
+constexpr int kGemvThreads = 256;  // 8 warps
+constexpr int kGemvWarps = kGemvThreads / 32;
+constexpr int kChunk = 4;          // iterations per host check
+constexpr int kMaxRestarts = 8;
 
 // ------------------------------------------------------------ type helpers --
-template <typename T> struct Cplx;
-template <> struct Cplx<double> { using t = double2; };
-template <> struct Cplx<float> { using t = float2; };
-
 __device__ __forceinline__ double2 to_d2(double2 v) { return v; }
 __device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(v.x, v.y); }
 template <typename VT> __device__ __forceinline__ VT from_d2(double2 v);
@@ -56,23 +71,21 @@ template <> __device__ __forceinline__ float2 from_d2<float2>(double2 v) {
     return make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
 }
 
-__device__ __forceinline__ void acc_fma(double2& a, double2 m, double2 y) { cfma(a, m, y); }
-__device__ __forceinline__ void acc_fma(float2& a, float2 m, float2 y) { cfmaf(a, m, y); }
-
 // ----------------------------------------------------------- plan structs --
 struct Strip {          // GEMV work: blocks (i, j0 .. j0+nb-1) of cluster sys
     int sys, i, nb, pad;
     long long p0;       // first pair index (cluster-local)
 };
-struct Item {           // vector / reduce work: rows [r0, r0+nr) of cluster sys
+struct Item {           // rows [r0, r0+nr) of cluster sys
     int sys, r0, nr, pad;
 };
-struct SysPlan {        // per-cluster plan data (device)
+struct SysPlan {
     long long strip_row_base;   // index into row_strip (first block row of this cluster)
     long long strip_base;       // global index of the first strip of this cluster
     long long cw_off;           // element offset of this cluster's per-pair column partials
     long long cu_off;           // element offset of this cluster's per-strip row partials
-    int item_begin, item_end;
+    int vbeg, vend;             // vector items
+    int rbeg, rend;             // reduce items
 };
 
 struct KState {         // per (cluster, rhs) BiCGSTAB scalars
@@ -84,174 +97,290 @@ struct KState {         // per (cluster, rhs) BiCGSTAB scalars
 
 enum { ST_RUNNING = -1 };
 
+// mask_mode: -1 all, 0 running clusters, 1 restarting clusters
+template <int R>
+__device__ __forceinline__ bool active_rhs(const KState* st, int sys, int rr, int mask_mode) {
+    if (mask_mode < 0) return true;
+    const KState& k = st[sys * R + rr];
+    return (mask_mode == 0) ? (!k.done && !k.need_restart) : (k.need_restart != 0);
+}
+template <int R>
+__device__ __forceinline__ bool any_active(const KState* st, int sys, int mask_mode) {
+    bool a = false;
+#pragma unroll
+    for (int rr = 0; rr < R; rr++) a |= active_rhs<R>(st, sys, rr, mask_mode);
+    return a;
+}
+
+// --------------------------------------------------------------- policies --
+struct DFAcc {          // double-float complex accumulator + FP32 correction terms
+    float hr, lr, hi, li, sr, si;
+};
+
+__device__ __forceinline__ void two_sum_acc(float& h, float& l, float p, float e) {
+    // (h, l) += p + e: p added exactly (TwoSum), its error and e into the low part
+    const float s = h + p;
+    const float bb = s - h;
+    const float err = (h - (s - bb)) + (p - bb);
+    h = s;
+    l += err + e;
+}
+
+struct Pol64 {
+    static constexpr int CPG = 1;
+    using YT = double2;
+    using Acc = double2;
+    using OutT = double2;
+    using Mat = double2;
+    __device__ static void zero(Acc& a) { a = make_double2(0, 0); }
+    __device__ static void fma(Acc& a, const Mat& m, const YT& y) { cfma(a, m, y); }
+    __device__ static OutT out(const Acc& a) { return a; }
+};
+
+struct Pol32 {
+    static constexpr int CPG = 2;
+    using YT = float2;
+    using Acc = float2;
+    using OutT = float2;
+    using Mat = float2;
+    __device__ static void zero(Acc& a) { a = make_float2(0, 0); }
+    __device__ static void fma(Acc& a, const Mat& m, const YT& y) { cfmaf(a, m, y); }
+    __device__ static OutT out(const Acc& a) { return a; }
+};
+
+struct PolDF {
+    static constexpr int CPG = 2;
+    using YT = float4;     // (hi.re, hi.im, lo.re, lo.im)
+    using Acc = DFAcc;
+    using OutT = double2;
+    struct Mat { float2 h, l; };
+    __device__ static void zero(Acc& a) { a = DFAcc{0, 0, 0, 0, 0, 0}; }
+    __device__ static void fma(Acc& a, const Mat& m, const YT& y) {
+        // main term m.h * y.h: every real product exact as p + e
+        float p, e;
+        p = m.h.x * y.x; e = fmaf(m.h.x, y.x, -p); two_sum_acc(a.hr, a.lr, p, e);
+        p = m.h.y * y.y; e = fmaf(m.h.y, y.y, -p); two_sum_acc(a.hr, a.lr, -p, -e);
+        p = m.h.x * y.y; e = fmaf(m.h.x, y.y, -p); two_sum_acc(a.hi, a.li, p, e);
+        p = m.h.y * y.x; e = fmaf(m.h.y, y.x, -p); two_sum_acc(a.hi, a.li, p, e);
+        // corrections m.h * y.l + m.l * y.h (relative size 2^-24)
+        a.sr = fmaf(m.h.x, y.z, a.sr); a.sr = fmaf(-m.h.y, y.w, a.sr);
+        a.si = fmaf(m.h.x, y.w, a.si); a.si = fmaf(m.h.y, y.z, a.si);
+        a.sr = fmaf(m.l.x, y.x, a.sr); a.sr = fmaf(-m.l.y, y.y, a.sr);
+        a.si = fmaf(m.l.x, y.y, a.si); a.si = fmaf(m.l.y, y.x, a.si);
+    }
+    __device__ static OutT out(const Acc& a) {
+        return make_double2((double)a.hr + ((double)a.lr + (double)a.sr), (double)a.hi + ((double)a.li + (double)a.si));
+    }
+};
+
+template <class Pol> struct Load;
+template <> struct Load<Pol64> {
+    __device__ static void get(const void* hi, const void*, long long idx, Pol64::Mat* m) {
+        m[0] = __ldg(reinterpret_cast<const double2*>(hi) + idx);
+    }
+};
+template <> struct Load<Pol32> {
+    __device__ static void get(const void* hi, const void*, long long idx, Pol32::Mat* m) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(hi) + idx));
+        m[0] = make_float2(q.x, q.y);
+        m[1] = make_float2(q.z, q.w);
+    }
+};
+template <> struct Load<PolDF> {
+    __device__ static void get(const void* hi, const void* lo, long long idx, PolDF::Mat* m) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(hi) + idx));
+        const float4 r = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(lo) + idx));
+        m[0].h = make_float2(q.x, q.y);
+        m[1].h = make_float2(q.z, q.w);
+        m[0].l = make_float2(r.x, r.y);
+        m[1].l = make_float2(r.z, r.w);
+    }
+};
+
 // ------------------------------------------------------------ y vectors --
-// Yu[k][r][rr] = eps(r) t_k[rho(r)] x_k[rho(r)][rr],  Yw = sig(r) Yu, for all
-// particles k of all clusters (thread per row).
-template <typename VT, int R>
-__global__ void k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
-                        const KState* __restrict__ st, int mask_mode, const double2* __restrict__ tvec,
-                        const VT* __restrict__ x, VT* __restrict__ Yu, VT* __restrict__ Yw) {
+// For every row (particle k, local row r) of every cluster:
+//   z = eps(r) t_k[rho(r)] x_k[rho(r)],   Yu = z,  Yw = sig(r) z
+// stored as double2 (YK 0), float2 (YK 1) or the float4 hi/lo split (YK 2).
+template <int YK> struct YType;
+template <> struct YType<0> { using t = double2; };
+template <> struct YType<1> { using t = float2; };
+template <> struct YType<2> { using t = float4; };
+
+template <int YK> __device__ __forceinline__ typename YType<YK>::t make_y(double2 z);
+template <> __device__ __forceinline__ double2 make_y<0>(double2 z) { return z; }
+template <> __device__ __forceinline__ float2 make_y<1>(double2 z) {
+    return make_float2(__double2float_rn(z.x), __double2float_rn(z.y));
+}
+template <> __device__ __forceinline__ float4 make_y<2>(double2 z) {
+    const float hx = __double2float_rn(z.x), hy = __double2float_rn(z.y);
+    return make_float4(hx, hy, __double2float_rn(z.x - (double)hx), __double2float_rn(z.y - (double)hy));
+}
+
+template <int YK, typename VT, int R>
+__global__ void __launch_bounds__(kVRows)
+k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
+        int mask_mode, const double2* __restrict__ tvec, const VT* __restrict__ x, typename YType<YK>::t* __restrict__ Yu,
+        typename YType<YK>::t* __restrict__ Yw) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
+    if (!any_active<R>(st, I.sys, mask_mode)) return;
     const gb::SysDev S = sys[I.sys];
-    if (mask_mode >= 0) {   // skip clusters whose every rhs is finished (or not restarting)
-        bool any = false;
-        for (int rr = 0; rr < R; rr++) {
-            const KState& k = st[I.sys * R + rr];
-            any |= (mask_mode == 0) ? (!k.done && !k.need_restart) : (k.need_restart != 0);
-        }
-        if (!any) return;
-    }
     const int lr = threadIdx.x;
     if (lr >= I.nr) return;
     const int row = I.r0 + lr;
-    const int part = row / S.B, R_ = row % S.B;
-    const int info = __ldg(S.rowinfo + R_);
+    const int part = row / S.B, Rr = row % S.B;
+    const int info = __ldg(S.rowinfo + Rr);
     const int rho = info & ((1 << 29) - 1);
     const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
     const long long src = (long long)part * S.B + rho;
     const double2 t = tvec[S.t_off + src];
+#pragma unroll
     for (int rr = 0; rr < R; rr++) {
-        double2 xv = to_d2(x[(S.vec_off + src * R) + rr]);
-        double2 z = cmul(t, xv);
-        double2 yu = make_double2(flipd(z.x, eneg), flipd(z.y, eneg));
-        double2 yw = make_double2(flipd(yu.x, sneg), flipd(yu.y, sneg));
-        Yu[(S.vec_off + (long long)row * R) + rr] = from_d2<VT>(yu);
-        Yw[(S.vec_off + (long long)row * R) + rr] = from_d2<VT>(yw);
+        const double2 z = cmul(t, to_d2(x[S.vec_off + src * R + rr]));
+        const double2 yu = make_double2(flipd(z.x, eneg), flipd(z.y, eneg));
+        const double2 yw = make_double2(flipd(yu.x, sneg), flipd(yu.y, sneg));
+        Yu[S.vec_off + (long long)row * R + rr] = make_y<YK>(yu);
+        Yw[S.vec_off + (long long)row * R + rr] = make_y<YK>(yw);
     }
 }
 
 // --------------------------------------------------------------- K3a GEMV --
-// MT: matrix element (double2 | float2), AT: accumulator scalar (double | float).
-// CPG: complex elements per 16-byte load (1 for c128, 2 for c64). NG: column
-// groups per lane.
-template <typename MT, typename AT, int R, int NG>
+// RR: right-hand sides handled per launch (all R for Pol64/Pol32, one for PolDF,
+// the one at rr0); RT: stride of the [D][RT] vectors and partials.
+template <class Pol, int RR, int RT, int RPS, int NS>
 __global__ void __launch_bounds__(kGemvThreads)
 k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long nstrips,
-        const KState* __restrict__ st, int mask_mode, const MT* __restrict__ mat,
-        const typename Cplx<AT>::t* __restrict__ Yu, const typename Cplx<AT>::t* __restrict__ Yw,
-        typename Cplx<AT>::t* __restrict__ CU, typename Cplx<AT>::t* __restrict__ CW,
-        const SysPlan* __restrict__ plan) {
-    using AC = typename Cplx<AT>::t;
-    constexpr int CPG = 16 / sizeof(MT);
-    const int lane = threadIdx.x & 31;
+        const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
+        const typename Pol::YT* __restrict__ Yu, const typename Pol::YT* __restrict__ Yw,
+        typename Pol::OutT* __restrict__ CU, typename Pol::OutT* __restrict__ CW, const SysPlan* __restrict__ plan,
+        int rr0, int Bmax) {
+    using Acc = typename Pol::Acc;
+    using OutT = typename Pol::OutT;
+    using YT = typename Pol::YT;
+    constexpr int CPG = Pol::CPG;
+    extern __shared__ __align__(16) unsigned char gemv_smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    OutT* comb = reinterpret_cast<OutT*>(gemv_smem) + (size_t)wid * RPS * Bmax * RR;
     const long long warp = ((long long)blockIdx.x * kGemvThreads + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     for (long long w = warp; w < nstrips; w += nwarps) {
         const Strip sp = strips[w];
-        const gb::SysDev S = sys[sp.sys];
-        if (mask_mode >= 0) {
-            bool any = false;
-            for (int rr = 0; rr < R; rr++) {
-                const KState& k = st[sp.sys * R + rr];
-                any |= (mask_mode == 0) ? (!k.done && !k.need_restart) : (k.need_restart != 0);
-            }
-            if (!any) continue;
-        }
-        const int B = S.B;
-        const int ncg = B / CPG;     // column groups in a row
-        AC cu[NG][CPG][R];
+        bool act = false;
 #pragma unroll
-        for (int g = 0; g < NG; g++)
+        for (int q = 0; q < RR; q++) act |= active_rhs<RT>(st, sp.sys, rr0 + q, mask_mode);
+        if (!act) continue;
+        const gb::SysDev S = sys[sp.sys];
+        const SysPlan pl = plan[sp.sys];
+        const int B = S.B;
+        const int ncg = B / CPG;
+        int sro[NS], sg[NS];
+        bool sval[NS];
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+            const int f = lane + 32 * k;
+            sval[k] = f < RPS * ncg;
+            sro[k] = sval[k] ? f / ncg : 0;
+            sg[k] = sval[k] ? f % ncg : 0;
+        }
+        Acc cu[NS][CPG][RR];
+#pragma unroll
+        for (int k = 0; k < NS; k++)
 #pragma unroll
             for (int c = 0; c < CPG; c++)
 #pragma unroll
-                for (int rr = 0; rr < R; rr++) cu[g][c][rr] = AC{0, 0};
-        const AC* yw_i = Yw + S.vec_off + (long long)sp.i * B * R;
+                for (int q = 0; q < RR; q++) Pol::zero(cu[k][c][q]);
+        const YT* yw_i = Yw + S.vec_off + (long long)sp.i * B * RT;
         for (int b = 0; b < sp.nb; b++) {
             const long long p = sp.p0 + b;
             const int j = sp.i + 1 + (int)(p - pair_start(sp.i, S.N));
-            const AC* yu_j = Yu + S.vec_off + (long long)j * B * R;
-            const MT* blk = mat + S.mat_off + p * (long long)B * B;
-            AC cw[NG][CPG][R];
+            const YT* yu_j = Yu + S.vec_off + (long long)j * B * RT;
+            const long long blk = S.mat_off + p * (long long)B * B;
+            Acc cw[NS][CPG][RR];
 #pragma unroll
-            for (int g = 0; g < NG; g++)
+            for (int k = 0; k < NS; k++)
 #pragma unroll
                 for (int c = 0; c < CPG; c++)
 #pragma unroll
-                    for (int rr = 0; rr < R; rr++) cw[g][c][rr] = AC{0, 0};
-            constexpr int RU = 4;   // rows in flight per lane
-            int r = 0;
-            for (; r + RU <= B; r += RU) {
-                uint4 q[RU][NG];
+                    for (int q = 0; q < RR; q++) Pol::zero(cw[k][c][q]);
+            constexpr int RU = 2;   // row steps in flight
+            for (int r = 0; r < B; r += RPS * RU) {
+                typename Pol::Mat m[RU][NS][CPG];
 #pragma unroll
                 for (int u = 0; u < RU; u++)
 #pragma unroll
-                    for (int g = 0; g < NG; g++) {
-                        const int cg = lane + 32 * g;
-                        q[u][g] = (cg < ncg) ? __ldg(reinterpret_cast<const uint4*>(blk + (long long)(r + u) * B) + cg)
-                                             : make_uint4(0, 0, 0, 0);
+                    for (int k = 0; k < NS; k++) {
+                        const int row = r + u * RPS + sro[k];
+                        if (sval[k] && row < B) {
+                            Load<Pol>::get(mat_hi, mat_lo, blk + (long long)row * B + sg[k] * CPG, m[u][k]);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < CPG; c++) m[u][k][c] = typename Pol::Mat{};
+                        }
                     }
 #pragma unroll
-                for (int u = 0; u < RU; u++) {
-                    AC yu[R], yw[R];
+                for (int u = 0; u < RU; u++)
 #pragma unroll
-                    for (int rr = 0; rr < R; rr++) {
-                        yu[rr] = yu_j[(r + u) * R + rr];
-                        yw[rr] = yw_i[(r + u) * R + rr];
-                    }
+                    for (int k = 0; k < NS; k++) {
+                        const int row = r + u * RPS + sro[k];
+                        if (!(sval[k] && row < B)) continue;
+                        YT yu[RR], yw[RR];
 #pragma unroll
-                    for (int g = 0; g < NG; g++) {
-                        const MT* m = reinterpret_cast<const MT*>(&q[u][g]);
+                        for (int q = 0; q < RR; q++) {
+                            yu[q] = yu_j[row * RT + rr0 + q];
+                            yw[q] = yw_i[row * RT + rr0 + q];
+                        }
 #pragma unroll
-                        for (int c = 0; c < CPG; c++) {
-                            AC mv = AC{(AT)m[c].x, (AT)m[c].y};
+                        for (int c = 0; c < CPG; c++)
 #pragma unroll
-                            for (int rr = 0; rr < R; rr++) {
-                                acc_fma(cu[g][c][rr], mv, yu[rr]);
-                                acc_fma(cw[g][c][rr], mv, yw[rr]);
+                            for (int q = 0; q < RR; q++) {
+                                Pol::fma(cu[k][c][q], m[u][k][c], yu[q]);
+                                Pol::fma(cw[k][c][q], m[u][k][c], yw[q]);
                             }
-                        }
                     }
-                }
             }
-            for (; r < B; r++) {
-                AC yu[R], yw[R];
+            // column partial of this block for block row j: slots of one column summed in a fixed order
 #pragma unroll
-                for (int rr = 0; rr < R; rr++) {
-                    yu[rr] = yu_j[r * R + rr];
-                    yw[rr] = yw_i[r * R + rr];
+            for (int k = 0; k < NS; k++)
+                if (sval[k])
+#pragma unroll
+                    for (int c = 0; c < CPG; c++)
+#pragma unroll
+                        for (int q = 0; q < RR; q++)
+                            comb[((size_t)sro[k] * B + sg[k] * CPG + c) * RR + q] = Pol::out(cw[k][c][q]);
+            __syncwarp();
+            OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
+            for (int e = lane; e < B * RR; e += 32) {
+                OutT s = comb[e];
+                for (int ro = 1; ro < RPS; ro++) {
+                    const OutT v = comb[(size_t)ro * B * RR + e];
+                    s.x += v.x;
+                    s.y += v.y;
                 }
-#pragma unroll
-                for (int g = 0; g < NG; g++) {
-                    const int cg = lane + 32 * g;
-                    if (cg >= ncg) continue;
-                    uint4 qq = __ldg(reinterpret_cast<const uint4*>(blk + (long long)r * B) + cg);
-                    const MT* m = reinterpret_cast<const MT*>(&qq);
-#pragma unroll
-                    for (int c = 0; c < CPG; c++) {
-                        AC mv = AC{(AT)m[c].x, (AT)m[c].y};
-#pragma unroll
-                        for (int rr = 0; rr < R; rr++) {
-                            acc_fma(cu[g][c][rr], mv, yu[rr]);
-                            acc_fma(cw[g][c][rr], mv, yw[rr]);
-                        }
-                    }
-                }
+                cwp[(e / RR) * RT + rr0 + (e % RR)] = s;
             }
-            // column partial of this block for block row j: CW[pair][col][rr]
-            AC* cwp = CW + plan[sp.sys].cw_off + p * (long long)B * R;
+            __syncwarp();
+        }
 #pragma unroll
-            for (int g = 0; g < NG; g++) {
-                const int cg = lane + 32 * g;
-                if (cg >= ncg) continue;
+        for (int k = 0; k < NS; k++)
+            if (sval[k])
 #pragma unroll
                 for (int c = 0; c < CPG; c++)
 #pragma unroll
-                    for (int rr = 0; rr < R; rr++) cwp[(cg * CPG + c) * R + rr] = cw[g][c][rr];
+                    for (int q = 0; q < RR; q++)
+                        comb[((size_t)sro[k] * B + sg[k] * CPG + c) * RR + q] = Pol::out(cu[k][c][q]);
+        __syncwarp();
+        OutT* cup = CU + pl.cu_off + (w - pl.strip_base) * (long long)B * RT;
+        for (int e = lane; e < B * RR; e += 32) {
+            OutT s = comb[e];
+            for (int ro = 1; ro < RPS; ro++) {
+                const OutT v = comb[(size_t)ro * B * RR + e];
+                s.x += v.x;
+                s.y += v.y;
             }
+            cup[(e / RR) * RT + rr0 + (e % RR)] = s;
         }
-        AC* cup = CU + plan[sp.sys].cu_off + (w - plan[sp.sys].strip_base) * (long long)B * R;
-#pragma unroll
-        for (int g = 0; g < NG; g++) {
-            const int cg = lane + 32 * g;
-            if (cg >= ncg) continue;
-#pragma unroll
-            for (int c = 0; c < CPG; c++)
-#pragma unroll
-                for (int rr = 0; rr < R; rr++) cup[(cg * CPG + c) * R + rr] = cu[g][c][rr];
-        }
+        __syncwarp();
     }
 }
 
@@ -259,11 +388,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
 // Tx = T x for a caller-supplied dense D x D complex128 matrix; warp per row.
 template <int R>
 __global__ void __launch_bounds__(256)
-k_dense_gemv(int D, const double2* __restrict__ T, const double2* __restrict__ x, double2* __restrict__ Tx,
-             const KState* __restrict__ st) {
-    bool any = false;
-    for (int rr = 0; rr < R; rr++) any |= (!st[rr].done && !st[rr].need_restart) || st[rr].need_restart;
-    if (!any) return;
+k_dense_gemv(int D, const double2* __restrict__ T, const double2* __restrict__ x, double2* __restrict__ Tx) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -289,98 +414,118 @@ k_dense_gemv(int D, const double2* __restrict__ T, const double2* __restrict__ x
 }
 
 // --------------------------------------------------------------- K3b reduce --
-// y = x + T x (row-wise from the partials, or from a dense Tx), plus per-item dot
-// partials: mode 1 -> d0 = <r0, y>;  mode 2 -> d0 = |y|^2, d1 = <y, s>;
-// mode 3 -> d0 = |b - y|^2 with y := b - y (restart residual).
-template <typename AT, typename VT, int R, bool DENSE>
-__global__ void __launch_bounds__(kItemRows)
+// y = x + T x (from the partials, or from a dense Tx), and per-item partial dots:
+//   mode 1: d0 = <r0, y>;  mode 2: d0 = |y|^2, d1 = <y, s>;
+//   mode 3: y := b - (x + T x), d0 = |y|^2  (residual).
+template <typename OutT, typename VT, int R, bool DENSE>
+__global__ void __launch_bounds__(kRWarps * 32)
 k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
-         const SysPlan* __restrict__ plan, const long long* __restrict__ row_strip,
-         const KState* __restrict__ st, int mask_mode,
-         const typename Cplx<AT>::t* __restrict__ CU, const typename Cplx<AT>::t* __restrict__ CW,
-         const double2* __restrict__ Tx_dense, const VT* __restrict__ x, VT* __restrict__ y, int mode,
-         const VT* __restrict__ aux, const double2* __restrict__ b128, double2* __restrict__ dots) {
-    using AC = typename Cplx<AT>::t;
+         const SysPlan* __restrict__ plan, const long long* __restrict__ row_strip, const KState* __restrict__ st,
+         int mask_mode, const OutT* __restrict__ CU, const OutT* __restrict__ CW, const double2* __restrict__ Tx_dense,
+         const VT* __restrict__ x, VT* __restrict__ y, int mode, const VT* __restrict__ aux,
+         const double2* __restrict__ b128, double2* __restrict__ dots) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
+    if (!any_active<R>(st, I.sys, mask_mode)) return;
     const gb::SysDev S = sys[I.sys];
-    bool act[R];
-    bool any = false;
-    for (int rr = 0; rr < R; rr++) {
-        const KState& k = st[I.sys * R + rr];
-        act[rr] = (mask_mode == 0) ? (!k.done && !k.need_restart) : (k.need_restart != 0);
-        if (mask_mode < 0) act[rr] = true;
-        any |= act[rr];
-    }
-    if (!any) return;
-    __shared__ double2 red[kItemRows / 32][R][2];
-    const int lr = threadIdx.x;
-    double2 d0[R], d1[R];
-    for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = make_double2(0, 0);
-    if (lr < I.nr) {
-        const int row = I.r0 + lr;
-        const int B = S.B;
-        const int k = row / B, R_ = row % B;
-        double2 tx[R];
-        if (DENSE) {
-            for (int rr = 0; rr < R; rr++) tx[rr] = Tx_dense[(long long)row * R + rr];
-        } else {
-            const int info = __ldg(S.rowinfo + R_);
+    __shared__ double2 pu[kRWarps][kRRows][R];
+    __shared__ double2 pw[kRWarps][kRRows][R];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool valid = lane < I.nr;
+    const int row = I.r0 + lane;
+    const int B = S.B;
+    if (!DENSE) {
+        double2 su[R], sw[R];
+#pragma unroll
+        for (int rr = 0; rr < R; rr++) su[rr] = sw[rr] = make_double2(0, 0);
+        if (valid) {
+            const int k = row / B, Rr = row % B;
+            const int info = __ldg(S.rowinfo + Rr);
             const int rho = info & ((1 << 29) - 1);
-            const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
-            AC su[R], sw[R];
-            for (int rr = 0; rr < R; rr++) su[rr] = sw[rr] = AC{0, 0};
             const SysPlan pl = plan[I.sys];
             const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
-            for (long long q = s0; q < s1; q++)
-                for (int rr = 0; rr < R; rr++) {
-                    AC v = CU[pl.cu_off + ((q - pl.strip_base) * B + rho) * R + rr];
-                    su[rr].x += v.x;
-                    su[rr].y += v.y;
-                }
-            for (int i = 0; i < k; i++) {
-                const long long pr = pair_start(i, S.N) + (k - i - 1);
-                for (int rr = 0; rr < R; rr++) {
-                    AC v = CW[pl.cw_off + (pr * B + rho) * R + rr];
-                    sw[rr].x += v.x;
-                    sw[rr].y += v.y;
+            const long long nterm = (s1 - s0) + k;
+            for (long long t = wid; t < nterm; t += kRWarps) {
+                if (t < s1 - s0) {
+                    const OutT* src = CU + pl.cu_off + ((t + s0 - pl.strip_base) * B + rho) * R;
+#pragma unroll
+                    for (int rr = 0; rr < R; rr++) {
+                        const OutT v = src[rr];
+                        su[rr].x += (double)v.x;
+                        su[rr].y += (double)v.y;
+                    }
+                } else {
+                    const int i = (int)(t - (s1 - s0));
+                    const long long pr = pair_start(i, S.N) + (k - i - 1);
+                    const OutT* src = CW + pl.cw_off + (pr * B + rho) * R;
+#pragma unroll
+                    for (int rr = 0; rr < R; rr++) {
+                        const OutT v = src[rr];
+                        sw[rr].x += (double)v.x;
+                        sw[rr].y += (double)v.y;
+                    }
                 }
             }
+        }
+#pragma unroll
+        for (int rr = 0; rr < R; rr++) {
+            pu[wid][lane][rr] = su[rr];
+            pw[wid][lane][rr] = sw[rr];
+        }
+        __syncthreads();
+    }
+    if (wid != 0) return;
+    double2 d0[R], d1[R];
+#pragma unroll
+    for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = make_double2(0, 0);
+    if (valid) {
+        double2 tx[R];
+        if (DENSE) {
+#pragma unroll
+            for (int rr = 0; rr < R; rr++) tx[rr] = Tx_dense[(long long)row * R + rr];
+        } else {
+            const int info = __ldg(S.rowinfo + row % B);
+            const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
+#pragma unroll
             for (int rr = 0; rr < R; rr++) {
-                double2 a = make_double2((double)su[rr].x, (double)su[rr].y);
-                double2 c = make_double2((double)sw[rr].x, (double)sw[rr].y);
+                double2 a = make_double2(0, 0), c = make_double2(0, 0);
+                for (int w = 0; w < kRWarps; w++) {
+                    a.x += pu[w][lane][rr].x;
+                    a.y += pu[w][lane][rr].y;
+                    c.x += pw[w][lane][rr].x;
+                    c.y += pw[w][lane][rr].y;
+                }
                 a = make_double2(flipd(a.x, eneg), flipd(a.y, eneg));
                 c = make_double2(flipd(c.x, eneg ^ sneg), flipd(c.y, eneg ^ sneg));
                 tx[rr] = make_double2(a.x + c.x, a.y + c.y);
             }
         }
         const long long vo = S.vec_off + (long long)row * R;
+#pragma unroll
         for (int rr = 0; rr < R; rr++) {
-            if (!act[rr]) continue;
+            if (!active_rhs<R>(st, I.sys, rr, mask_mode)) continue;
             const double2 xv = to_d2(x[vo + rr]);
             double2 yv = make_double2(xv.x + tx[rr].x, xv.y + tx[rr].y);
             if (mode == 3) {
                 const double2 bv = b128 ? b128[vo + rr] : to_d2(aux[vo + rr]);
                 yv = make_double2(bv.x - yv.x, bv.y - yv.y);
-                d0[rr].x += yv.x * yv.x + yv.y * yv.y;
             }
             const VT yo = from_d2<VT>(yv);
             y[vo + rr] = yo;
             const double2 yq = to_d2(yo);   // dots of the stored (rounded) vector
             if (mode == 1) {
-                const double2 r0 = to_d2(aux[vo + rr]);
-                cfma_conj(d0[rr], r0, yq);
+                cfma_conj(d0[rr], to_d2(aux[vo + rr]), yq);
             } else if (mode == 2) {
-                const double2 sv = to_d2(aux[vo + rr]);
                 d0[rr].x += yq.x * yq.x + yq.y * yq.y;
-                cfma_conj(d1[rr], yq, sv);
+                cfma_conj(d1[rr], yq, to_d2(aux[vo + rr]));
+            } else if (mode == 3) {
+                d0[rr].x += yq.x * yq.x + yq.y * yq.y;
             }
         }
     }
     if (mode == 0) return;
-    // block reduction in a fixed order
-    const int lane = lr & 31, wid = lr >> 5;
+#pragma unroll
     for (int rr = 0; rr < R; rr++) {
         for (int o = 16; o > 0; o >>= 1) {
             d0[rr].x += __shfl_xor_sync(0xffffffffu, d0[rr].x, o);
@@ -389,19 +534,9 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
             d1[rr].y += __shfl_xor_sync(0xffffffffu, d1[rr].y, o);
         }
         if (lane == 0) {
-            red[wid][rr][0] = d0[rr];
-            red[wid][rr][1] = d1[rr];
+            dots[((long long)it * R + rr) * 2 + 0] = d0[rr];
+            dots[((long long)it * R + rr) * 2 + 1] = d1[rr];
         }
-    }
-    __syncthreads();
-    if (lr < R * 2) {
-        const int rr = lr >> 1, which = lr & 1;
-        double2 s = make_double2(0, 0);
-        for (int w = 0; w < kItemRows / 32; w++) {
-            s.x += red[w][rr][which].x;
-            s.y += red[w][rr][which].y;
-        }
-        dots[((long long)it * R + rr) * 2 + which] = s;
     }
 }
 
@@ -410,9 +545,9 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
 // kind 1: p-update  p = r + beta (p - omega v)
 // kind 2: s-update  s = r - alpha v
 // kind 3: x/r       x += alpha p + omega s; r = s - omega t;  dots: |r|^2, <r0, r>
-// kind 4: restart   r0 = r (r already b - A x);  dots: none (|r|^2 from reduce)
+// kind 4: restart   r0 = r (r already b - A x)
 template <typename VT, int R>
-__global__ void __launch_bounds__(kItemRows)
+__global__ void __launch_bounds__(kVRows)
 k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
       int kind, const double2* __restrict__ b, VT* __restrict__ bx, VT* __restrict__ x, VT* __restrict__ r,
       VT* __restrict__ r0, VT* __restrict__ p, VT* __restrict__ v, VT* __restrict__ s, const VT* __restrict__ t,
@@ -420,23 +555,19 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
+    const int mask = (kind == 0) ? -1 : (kind == 4 ? 1 : 0);
+    if (!any_active<R>(st, I.sys, mask)) return;
     const gb::SysDev S = sys[I.sys];
-    bool act[R];
-    bool any = false;
-    for (int rr = 0; rr < R; rr++) {
-        const KState& k = st[I.sys * R + rr];
-        act[rr] = (kind == 0) ? true : (kind == 4 ? (k.need_restart != 0) : (!k.done && !k.need_restart));
-        any |= act[rr];
-    }
-    if (!any) return;
-    __shared__ double2 red[kItemRows / 32][R][2];
+    __shared__ double2 red[kVRows / 32][R][2];
     const int lr = threadIdx.x;
     double2 d0[R], d1[R];
+#pragma unroll
     for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = make_double2(0, 0);
     if (lr < I.nr) {
         const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
+#pragma unroll
         for (int rr = 0; rr < R; rr++) {
-            if (!act[rr]) continue;
+            if (!active_rhs<R>(st, I.sys, rr, mask)) continue;
             const long long e = vo + rr;
             const KState& k = st[I.sys * R + rr];
             if (kind == 0) {
@@ -450,9 +581,8 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
                 d0[rr].x += bd.x * bd.x + bd.y * bd.y;
             } else if (kind == 1) {
                 const double2 rv = to_d2(r[e]), pv = to_d2(p[e]), vv = to_d2(v[e]);
-                const double2 tmp = make_double2(pv.x - (k.omega.x * vv.x - k.omega.y * vv.y),
-                                                 pv.y - (k.omega.x * vv.y + k.omega.y * vv.x));
-                const double2 bt = cmul(k.beta, tmp);
+                const double2 ov = cmul(k.omega, vv);
+                const double2 bt = cmul(k.beta, make_double2(pv.x - ov.x, pv.y - ov.y));
                 p[e] = from_d2<VT>(make_double2(rv.x + bt.x, rv.y + bt.y));
             } else if (kind == 2) {
                 const double2 rv = to_d2(r[e]), vv = to_d2(v[e]);
@@ -474,6 +604,7 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     }
     if (kind == 1 || kind == 2 || kind == 4) return;
     const int lane = lr & 31, wid = lr >> 5;
+#pragma unroll
     for (int rr = 0; rr < R; rr++) {
         for (int o = 16; o > 0; o >>= 1) {
             d0[rr].x += __shfl_xor_sync(0xffffffffu, d0[rr].x, o);
@@ -490,7 +621,7 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     if (lr < R * 2) {
         const int rr = lr >> 1, which = lr & 1;
         double2 sm = make_double2(0, 0);
-        for (int w = 0; w < kItemRows / 32; w++) {
+        for (int w = 0; w < kVRows / 32; w++) {
             sm.x += red[w][rr][which].x;
             sm.y += red[w][rr][which].y;
         }
@@ -505,9 +636,9 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 }
 __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
-// phase 0: init (bsq from dots d0; tol); 1: alpha = rho/<r0,v>; 2: omega = <t,s>/|t|^2;
-// 3: end of iteration (convergence, restart test, beta); 4: restart finished
-// (dots d0 = |r|^2 of the new residual).
+// Phases: 0 init (vector dots: |b|^2); 1 alpha = rho/<r0,v> (reduce dots);
+// 2 omega = <t,s>/|t|^2 (reduce dots); 3 end of iteration (vector dots |r|^2,
+// <r0,r>: convergence, restart test, beta); 4 restart done (reduce dots |r|^2).
 template <int R>
 __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ st, int phase,
                          const double2* __restrict__ dots, double tol, int maxiter) {
@@ -515,9 +646,13 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
     if (id >= nsys * R) return;
     const int sidx = id / R, rr = id % R;
     KState& k = st[id];
+    if (phase != 0 && phase != 4 && (k.done || k.need_restart)) return;
+    if (phase == 4 && !k.need_restart) return;
     const SysPlan pl = plan[sidx];
+    const bool vec = (phase == 0 || phase == 3);
+    const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
     double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
-    for (int it = pl.item_begin; it < pl.item_end; it++) {
+    for (int it = b0; it < b1; it++) {
         const double2 a = dots[((long long)it * R + rr) * 2 + 0];
         const double2 c = dots[((long long)it * R + rr) * 2 + 1];
         d0.x += a.x; d0.y += a.y;
@@ -525,14 +660,10 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
     }
     const double eps = 2.220446049250313e-16;
     if (phase == 0) {
-        k.bsq = d0.x;
-        k.r0sq = d0.x;
-        k.rsq = d0.x;
+        k.bsq = k.r0sq = k.rsq = d0.x;
         k.tol2 = tol * tol * d0.x;
         k.rho = k.alpha = k.omega = make_double2(1, 0);
-        k.iters = 0;
-        k.restarts = 0;
-        k.need_restart = 0;
+        k.iters = k.restarts = k.need_restart = 0;
         k.maxiter = maxiter;
         if (d0.x == 0.0 || !(k.rsq > k.tol2) || maxiter <= 0) {
             k.done = 1;
@@ -540,32 +671,23 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
         } else {
             k.done = 0;
             k.status = ST_RUNNING;
-            // loop top of the first iteration: rho = <r0, r> = |b|^2
-            const double2 rho_old = k.rho;
-            k.rho = make_double2(d0.x, 0.0);
+            const double2 rho_old = k.rho;          // loop top of the first iteration
+            k.rho = make_double2(d0.x, 0.0);        // <r0, r> = |b|^2
             k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
         }
         return;
     }
-    if (phase == 4) {
-        if (!k.need_restart) return;
-        // Eigen: r = b - A x; r0 = r; rho = r0_sqnorm = |r|^2; first restart resets i
+    if (phase == 4) {   // Eigen: r = b - A x; r0 = r; rho = r0_sqnorm = |r|^2; the first restart resets i
         k.need_restart = 0;
-        k.rsq = d0.x;
-        k.r0sq = d0.x;
+        k.rsq = k.r0sq = d0.x;
         const double2 rho_old = k.rho;
         k.rho = make_double2(d0.x, 0.0);
         if (k.restarts++ == 0) k.iters = 0;
-        if (!(k.rsq > k.tol2)) {   // converged exactly at the restart point
-            k.done = 1;
-            k.status = GB_OK;
-            return;
-        }
+        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
         k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
         if (!finite2(k.beta)) { k.done = 1; k.status = GB_BREAKDOWN; }
         return;
     }
-    if (k.done || k.need_restart) return;
     if (phase == 1) {
         k.alpha = cdiv(k.rho, d0);
         if (!finite2(k.alpha)) { k.done = 1; k.status = (d0.x == 0 && d0.y == 0) ? GB_BREAKDOWN : GB_NAN; }
@@ -582,7 +704,7 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
         const double2 rho_old = k.rho;
         k.rho = d1;   // <r0, r>
         if (sqrt(k.rho.x * k.rho.x + k.rho.y * k.rho.y) < eps * eps * k.r0sq) {
-            if (k.restarts > 8) { k.done = 1; k.status = GB_BREAKDOWN; return; }
+            if (k.restarts >= kMaxRestarts) { k.done = 1; k.status = GB_BREAKDOWN; return; }
             k.rho = rho_old;   // phase 4 recomputes rho from the fresh residual
             k.need_restart = 1;
             return;
@@ -593,7 +715,6 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
 }
 
 // ------------------------------------------------------ refinement helpers --
-// x128 += d (FP32 correction); r32 = rounded FP64 residual
 template <int R>
 __global__ void k_refine_axpy(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
                               const KState* __restrict__ ost, double2* __restrict__ x128, const float2* __restrict__ d) {
@@ -614,7 +735,7 @@ __global__ void k_refine_axpy(const gb::SysDev* __restrict__ sys, const Item* __
     }
 }
 
-// outer (refinement) state update from |r|^2 partials: done when |r|^2 <= tol^2 |b|^2
+// outer (refinement) state from the residual's |r|^2 (reduce dots)
 template <int R>
 __global__ void k_refine_check(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ ost,
                                const double2* __restrict__ dots, int pass, int max_refine) {
@@ -625,7 +746,7 @@ __global__ void k_refine_check(const SysPlan* __restrict__ plan, int nsys, KStat
     if (k.done) return;
     const SysPlan pl = plan[sidx];
     double s = 0;
-    for (int it = pl.item_begin; it < pl.item_end; it++) s += dots[((long long)it * R + rr) * 2].x;
+    for (int it = pl.rbeg; it < pl.rend; it++) s += dots[((long long)it * R + rr) * 2].x;
     k.rsq = s;
     k.iters = pass;
     if (!isfinite(s)) { k.done = 1; k.status = GB_NAN; return; }
@@ -633,7 +754,7 @@ __global__ void k_refine_check(const SysPlan* __restrict__ plan, int nsys, KStat
     if (pass > max_refine) { k.done = 1; k.status = GB_NOT_CONVERGED; }
 }
 
-// |b|^2 per (cluster, rhs) for the outer state
+// outer state init from |b|^2 (vector dots of k_outer_start)
 template <int R>
 __global__ void k_outer_init(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ ost,
                              const double2* __restrict__ dots, double tol) {
@@ -642,7 +763,7 @@ __global__ void k_outer_init(const SysPlan* __restrict__ plan, int nsys, KState*
     const int sidx = id / R, rr = id % R;
     const SysPlan pl = plan[sidx];
     double s = 0;
-    for (int it = pl.item_begin; it < pl.item_end; it++) s += dots[((long long)it * R + rr) * 2].x;
+    for (int it = pl.vbeg; it < pl.vend; it++) s += dots[((long long)it * R + rr) * 2].x;
     KState& k = ost[id];
     memset(&k, 0, sizeof(KState));
     k.bsq = s;
@@ -652,15 +773,16 @@ __global__ void k_outer_init(const SysPlan* __restrict__ plan, int nsys, KState*
     k.status = k.done ? GB_OK : ST_RUNNING;
 }
 
-// r (FP64) = b;  x (FP64) = 0;  |b|^2 partials
+// x (FP64) = 0 and |b|^2 partials (vector items)
 template <int R>
-__global__ void k_outer_start(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
-                              const double2* __restrict__ b, double2* __restrict__ x, double2* __restrict__ dots) {
+__global__ void __launch_bounds__(kVRows)
+k_outer_start(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
+              const double2* __restrict__ b, double2* __restrict__ x, double2* __restrict__ dots) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
     const gb::SysDev S = sys[I.sys];
-    __shared__ double red[kItemRows / 32][R];
+    __shared__ double red[kVRows / 32][R];
     const int lr = threadIdx.x;
     double d[R];
     for (int rr = 0; rr < R; rr++) d[rr] = 0;
@@ -680,24 +802,58 @@ __global__ void k_outer_start(const gb::SysDev* __restrict__ sys, const Item* __
     __syncthreads();
     if (lr < R) {
         double s = 0;
-        for (int w = 0; w < kItemRows / 32; w++) s += red[w][lr];
+        for (int w = 0; w < kVRows / 32; w++) s += red[w][lr];
         dots[((long long)it * R + lr) * 2] = make_double2(s, 0);
         dots[((long long)it * R + lr) * 2 + 1] = make_double2(0, 0);
     }
 }
 
+template <typename VT>
+__global__ void k_copy_out(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, int R,
+                           const VT* __restrict__ src, double2* __restrict__ dst) {
+    const int it = blockIdx.x;
+    if (it >= nitems) return;
+    const Item I = items[it];
+    const gb::SysDev S = sys[I.sys];
+    const int lr = threadIdx.x;
+    if (lr >= I.nr) return;
+    const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
+    for (int rr = 0; rr < R; rr++) dst[vo + rr] = to_d2(src[vo + rr]);
+}
+
+// dst (FP32) = src (FP64), zero for clusters the mask marks done
+__global__ void k_cast_f(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, int R,
+                         const double2* __restrict__ src, float2* __restrict__ dst, const KState* __restrict__ mask) {
+    const int it = blockIdx.x;
+    if (it >= nitems) return;
+    const Item I = items[it];
+    const gb::SysDev S = sys[I.sys];
+    const int lr = threadIdx.x;
+    if (lr >= I.nr) return;
+    const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
+    for (int rr = 0; rr < R; rr++) {
+        const double2 v = src[vo + rr];
+        const bool off = mask && mask[I.sys * R + rr].done;
+        dst[vo + rr] = off ? make_float2(0.f, 0.f) : make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+    }
+}
+
 // ================================================================== host ==
 struct Plan {
-    int nsys = 0, R = 1, nitems = 0;
-    long long nstrips = 0, total_pairs = 0, total_rows = 0, total_vec = 0, max_B = 0;
-    long long cw_elems = 0, cu_elems = 0;
+    int nsys = 0, R = 1, nv = 0, nr = 0;
+    long long nstrips = 0, total_pairs = 0, total_vec = 0, max_B = 0, cw_elems = 0, cu_elems = 0;
     std::vector<gb::SysDev> sd;
     std::vector<Strip> strips;
-    std::vector<Item> items;
+    std::vector<Item> vitems, ritems;
     std::vector<SysPlan> sp;
     std::vector<long long> row_strip;
-    int ng128 = 1, ng64 = 1;
 };
+
+void add_items(std::vector<Item>& v, int s, int D, int rows, int& beg, int& end) {
+    beg = (int)v.size();
+    for (int r0 = 0; r0 < D; r0 += rows) v.push_back(Item{s, r0, std::min(rows, D - r0), 0});
+    end = (int)v.size();
+}
 
 int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan& P) {
     P.nsys = nsys;
@@ -708,7 +864,7 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
     for (auto& d : P.sd) pairs += d.P;
     P.total_pairs = pairs;
     const long long warps = (long long)gb::sm_count() * 32;
-    const long long J = std::max<long long>(1, std::min<long long>(16, pairs / std::max<long long>(1, 4 * warps)));
+    const long long J = std::max<long long>(1, std::min<long long>(8, pairs / std::max<long long>(1, 2 * warps)));
     P.sp.resize(nsys);
     long long cw_off = 0, cu_off = 0;
     for (int s = 0; s < nsys; s++) {
@@ -735,26 +891,41 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
         P.row_strip.push_back((long long)P.strips.size());
         cw_off += d.P * d.B * R;
         cu_off += ((long long)P.strips.size() - pl.strip_base) * d.B * R;
-        pl.item_begin = (int)P.items.size();
-        for (int r0 = 0; r0 < d.D; r0 += kItemRows) P.items.push_back(Item{s, r0, std::min(kItemRows, d.D - r0), 0});
-        pl.item_end = (int)P.items.size();
-        P.total_rows += d.D;
+        add_items(P.vitems, s, d.D, kVRows, pl.vbeg, pl.vend);
+        add_items(P.ritems, s, d.D, kRRows, pl.rbeg, pl.rend);
         P.total_vec = std::max<long long>(P.total_vec, d.vec_off + (long long)d.D * R);
         P.max_B = std::max<long long>(P.max_B, d.B);
     }
     P.nstrips = (long long)P.strips.size();
-    P.nitems = (int)P.items.size();
+    P.nv = (int)P.vitems.size();
+    P.nr = (int)P.ritems.size();
     P.cw_elems = cw_off;
     P.cu_elems = cu_off;
-    P.ng128 = (int)((P.max_B + 31) / 32);
-    P.ng64 = (int)((P.max_B / 2 + 31) / 32);
     return GB_OK;
 }
 
-// workspace layout
+// dense pseudo-cluster (plugin path): one cluster of D rows, no strips
+void dense_plan(int D, int R, Plan& P) {
+    P.nsys = 1;
+    P.R = R;
+    gb::SysDev sd{};
+    sd.D = D;
+    sd.B = D;
+    sd.N = 1;
+    P.sd.push_back(sd);
+    SysPlan sp{};
+    add_items(P.vitems, 0, D, kVRows, sp.vbeg, sp.vend);
+    add_items(P.ritems, 0, D, kRRows, sp.rbeg, sp.rend);
+    P.sp.push_back(sp);
+    P.row_strip = {0, 0};
+    P.nv = (int)P.vitems.size();
+    P.nr = (int)P.ritems.size();
+    P.total_vec = (long long)D * R;
+    P.max_B = 0;
+}
+
 struct WS {
-    size_t off_state, off_ostate, off_dots, off_cu, off_cw, off_yu, off_yw, off_vec, off_tx, off_x128r, off_blob, total;
-    int nvec;
+    size_t off_state, off_ostate, off_dots, off_cu, off_cw, off_yu, off_yw, off_vec, off_tx, off_r128, off_blob, total;
 };
 
 WS ws_layout(const Plan& P, int prec, bool dense) {
@@ -765,27 +936,21 @@ WS ws_layout(const Plan& P, int prec, bool dense) {
     auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 255) & ~size_t(255); return r; };
     w.off_state = take(sizeof(KState) * P.nsys * R);
     w.off_ostate = take(sizeof(KState) * P.nsys * R);
-    w.off_dots = take(sizeof(double2) * 2 * (size_t)std::max(P.nitems, 1) * R);
+    w.off_dots = take(sizeof(double2) * 2 * (size_t)std::max(std::max(P.nv, P.nr), 1) * R);
     if (!dense) {
-        // partials in the accumulator type of the matrix pass (FP64 refinement passes need double)
-        const size_t asz = sizeof(double2);
-        w.off_cu = take(asz * (size_t)std::max<long long>(P.cu_elems, 1));
-        w.off_cw = take(asz * (size_t)std::max<long long>(P.cw_elems, 1));
-        w.off_yu = take(sizeof(double2) * (size_t)P.total_vec);
-        w.off_yw = take(sizeof(double2) * (size_t)P.total_vec);
+        w.off_cu = take(sizeof(double2) * (size_t)std::max<long long>(P.cu_elems, 1));
+        w.off_cw = take(sizeof(double2) * (size_t)std::max<long long>(P.cw_elems, 1));
+        w.off_yu = take(16 * (size_t)P.total_vec);
+        w.off_yw = take(16 * (size_t)P.total_vec);
         w.off_tx = take(0);
     } else {
         w.off_cu = w.off_cw = w.off_yu = w.off_yw = take(0);
         w.off_tx = take(sizeof(double2) * (size_t)P.total_vec);
     }
-    // Krylov vectors: r, r0, p, v, s, t (+ x, b copies in reduced precision)
-    w.nvec = 8;
-    w.off_vec = take(vsz * (size_t)P.total_vec * w.nvec);
-    // FP64 residual for refinement
-    w.off_x128r = take(prec == GB_PREC_MIXED ? sizeof(double2) * (size_t)P.total_vec : 0);
-    // device copies of the plan
-    w.off_blob = take(sizeof(gb::SysDev) * P.nsys + sizeof(Strip) * P.nstrips + sizeof(Item) * P.nitems +
-                      sizeof(SysPlan) * P.nsys + sizeof(long long) * P.row_strip.size() + 64);
+    w.off_vec = take(vsz * (size_t)P.total_vec * 8);   // x r r0 p v s t b
+    w.off_r128 = take((prec == GB_PREC_MIXED || prec == GB_PREC_MIXED_FP64RES) ? sizeof(double2) * (size_t)P.total_vec : 0);
+    w.off_blob = take(sizeof(gb::SysDev) * P.nsys + sizeof(Strip) * P.nstrips + sizeof(Item) * (P.nv + P.nr) +
+                      sizeof(SysPlan) * P.nsys + sizeof(long long) * P.row_strip.size() + 256);
     w.total = o;
     return w;
 }
@@ -793,7 +958,8 @@ WS ws_layout(const Plan& P, int prec, bool dense) {
 struct DevPlan {
     const gb::SysDev* sys;
     const Strip* strips;
-    const Item* items;
+    const Item* vitems;
+    const Item* ritems;
     const SysPlan* sp;
     const long long* row_strip;
 };
@@ -808,72 +974,173 @@ int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t st
     };
     size_t o_sys = put(P.sd.data(), sizeof(gb::SysDev) * P.nsys);
     size_t o_str = put(P.strips.data(), sizeof(Strip) * P.nstrips);
-    size_t o_it = put(P.items.data(), sizeof(Item) * P.nitems);
+    size_t o_vi = put(P.vitems.data(), sizeof(Item) * P.nv);
+    size_t o_ri = put(P.ritems.data(), sizeof(Item) * P.nr);
     size_t o_sp = put(P.sp.data(), sizeof(SysPlan) * P.nsys);
     size_t o_rs = put(P.row_strip.data(), sizeof(long long) * P.row_strip.size());
     unsigned char* dst = base + w.off_blob;
-    GB_CUDA_TRY(cudaMemcpyAsync(dst, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
-    // the host blob dies at return: wait for the (pageable) copy
-    GB_CUDA_TRY(cudaStreamSynchronize(stream));
+    void* dblob = nullptr;
+    int slot = 0;
+    int e = gb::stage_acquire(blob.data(), blob.size(), stream, &dblob, &slot);
+    if (e) return e;
+    GB_CUDA_TRY(cudaMemcpyAsync(dst, dblob, blob.size(), cudaMemcpyDeviceToDevice, stream));
+    e = gb::stage_release(slot, stream);
+    if (e) return e;
     D.sys = reinterpret_cast<const gb::SysDev*>(dst + o_sys);
     D.strips = reinterpret_cast<const Strip*>(dst + o_str);
-    D.items = reinterpret_cast<const Item*>(dst + o_it);
+    D.vitems = reinterpret_cast<const Item*>(dst + o_vi);
+    D.ritems = reinterpret_cast<const Item*>(dst + o_ri);
     D.sp = reinterpret_cast<const SysPlan*>(dst + o_sp);
     D.row_strip = reinterpret_cast<const long long*>(dst + o_rs);
     return GB_OK;
 }
 
-// launch the packed product partials + reduce for vector xin -> yout
-template <typename MT, typename AT, typename VT, int R>
-int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, const KState* st, int mask_mode,
-                 const MT* mat, const double2* tvec, const VT* xin, VT* yout, int mode, const VT* aux,
-                 const double2* b128, double2* dots, cudaStream_t stream) {
-    using AC = typename Cplx<AT>::t;
-    AC* Yu = reinterpret_cast<AC*>(base + w.off_yu);
-    AC* Yw = reinterpret_cast<AC*>(base + w.off_yw);
-    AC* CU = reinterpret_cast<AC*>(base + w.off_cu);
-    AC* CW = reinterpret_cast<AC*>(base + w.off_cw);
-    k_yprep<AC, R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, st, mask_mode, tvec,
-                                                       reinterpret_cast<const AC*>(xin), Yu, Yw);
-    // Yu/Yw must be in the accumulator type: when VT differs (FP32 vectors with a c128
-    // pass do not occur), xin is already AC.
-    if (P.nstrips > 0) {
-        constexpr int CPG = 16 / sizeof(MT);
-        const int ng = (int)((P.max_B / CPG + 31) / 32);
-        const long long warps_needed = P.nstrips;
-        int per_sm = 2;
-        long long grid = std::min<long long>((warps_needed * 32 + kGemvThreads - 1) / kGemvThreads,
-                                             (long long)gb::sm_count() * 8);
-        (void)per_sm;
-        if (grid < 1) grid = 1;
-        switch (ng) {
-#define GB_NG_CASE(NGV)                                                                                         \
-    case NGV:                                                                                                   \
-        k_pgemv<MT, AT, R, NGV><<<(unsigned)grid, kGemvThreads, 0, stream>>>(D.sys, D.strips, P.nstrips, st,   \
-                                                                              mask_mode, mat, Yu, Yw, CU, CW, D.sp); \
-        break;
-            GB_NG_CASE(1) GB_NG_CASE(2) GB_NG_CASE(3) GB_NG_CASE(4) GB_NG_CASE(5) GB_NG_CASE(6) GB_NG_CASE(7)
-            GB_NG_CASE(8)
-#undef GB_NG_CASE
-            default: return gb_set_error(GB_UNSUPPORTED, "block size %lld too large", P.max_B);
-        }
-        GB_CUDA_TRY(cudaGetLastError());
+// --------------------------------------------------- GEMV launch selection --
+struct Shape { int rps, ns; };
+
+// Rows per step and slots per lane: all 32 lanes busy where possible, within a
+// register budget per policy (slots <= nsmax).
+Shape pick_shape(int Bmax, int cpg, int nsmax) {
+    const int ncg = Bmax / cpg;
+    Shape best{1, (ncg + 31) / 32};
+    double beff = -1;
+    for (int rps : {1, 2, 4}) {
+        const int ns = (rps * ncg + 31) / 32;
+        if (ns > nsmax) continue;
+        const double eff = double(rps * ncg) / (32.0 * ns);
+        if (eff > beff + 1e-9) { beff = eff; best = Shape{rps, ns}; }
     }
-    k_reduce<AT, VT, R, false><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, D.sp, D.row_strip, st,
-                                                                   mask_mode, CU, CW, nullptr, xin, yout, mode, aux,
-                                                                   b128, dots);
+    return best;
+}
+
+template <class Pol, int RR, int RT>
+int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* mat_hi, const void* mat_lo,
+                 const void* Yu, const void* Yw, void* CU, void* CW, int rr0, cudaStream_t stream) {
+    using YT = typename Pol::YT;
+    using OutT = typename Pol::OutT;
+    constexpr int nsmax = std::is_same<Pol, Pol64>::value ? 8 : (std::is_same<Pol, Pol32>::value ? 5 : 4);
+    const Shape sh = pick_shape((int)P.max_B, Pol::CPG, nsmax);
+    const int Bmax = (int)P.max_B;
+    const size_t smem = (size_t)kGemvWarps * sh.rps * Bmax * RR * sizeof(OutT);
+    const long long grid = std::max<long long>(1, std::min<long long>((P.nstrips * 32 + kGemvThreads - 1) / kGemvThreads,
+                                                                      (long long)gb::sm_count() * 8));
+#define GB_PG(RPSV, NSV)                                                                                         \
+    if (sh.rps == RPSV && sh.ns == NSV) {                                                                        \
+        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV>;                                                              \
+        if (smem > 48 * 1024)                                                                                    \
+            GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
+        gb::note_launch();                                                                                         \
+        kfn<<<(unsigned)grid, kGemvThreads, smem, stream>>>(D.sys, D.strips, P.nstrips, st, mask, mat_hi, mat_lo,  \
+                                                            reinterpret_cast<const YT*>(Yu),                     \
+                                                            reinterpret_cast<const YT*>(Yw),                     \
+                                                            reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), \
+                                                            D.sp, rr0, Bmax);                                   \
+        GB_CUDA_TRY(cudaGetLastError());                                                                         \
+        return GB_OK;                                                                                            \
+    }
+    if constexpr (std::is_same<Pol, Pol64>::value) {
+        GB_PG(4, 1) GB_PG(2, 1) GB_PG(1, 1) GB_PG(2, 3) GB_PG(2, 5) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 5) GB_PG(1, 7)
+        GB_PG(1, 8) GB_PG(1, 2) GB_PG(1, 6)
+    } else if constexpr (std::is_same<Pol, Pol32>::value) {
+        GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(4, 5) GB_PG(2, 3) GB_PG(1, 2) GB_PG(2, 5) GB_PG(1, 4) GB_PG(1, 1)
+        GB_PG(1, 3) GB_PG(1, 5)
+    } else {
+        GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(2, 3) GB_PG(1, 2) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 1)
+    }
+#undef GB_PG
+    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d (rps %d, ns %d)", Bmax, sh.rps, sh.ns);
+}
+
+// One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
+// packed matrices with arithmetic policy pol: 0 Pol64, 1 Pol32, 2 PolDF.
+template <typename VT, int R>
+int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, const KState* st, int mask,
+                 int pol, const void* mat_hi, const void* mat_lo, const double2* tvec, const VT* xin, VT* yout,
+                 int mode, const VT* aux, const double2* b128, double2* dots, cudaStream_t stream) {
+    void* Yu = base + w.off_yu;
+    void* Yw = base + w.off_yw;
+    void* CU = base + w.off_cu;
+    void* CW = base + w.off_cw;
+    const unsigned vb = (unsigned)P.nv;
+    int e = GB_OK;
+    if (pol == 0) {
+        gb::note_launch();
+        k_yprep<0, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
+                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw));
+        if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, stream);
+        if (e) return e;
+        gb::note_launch();
+        k_reduce<double2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
+            reinterpret_cast<const double2*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+    } else if (pol == 1) {
+        gb::note_launch();
+        k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
+                                                     reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw));
+        if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, stream);
+        if (e) return e;
+        gb::note_launch();
+        k_reduce<float2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
+            reinterpret_cast<const float2*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+    } else {
+        gb::note_launch();
+        k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
+                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
+        for (int rr = 0; rr < R && P.nstrips; rr++) {
+            e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, rr, stream);
+            if (e) return e;
+        }
+        gb::note_launch();
+        k_reduce<double2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
+            reinterpret_cast<const double2*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+    }
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
 
+// ----------------------------------------------------------- graph cache --
+struct GraphKey {
+    const void* a[12];
+    long long n[8];
+    bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof(GraphKey)) == 0; }
+};
+struct GraphKeyHash {
+    size_t operator()(const GraphKey& k) const {
+        const unsigned char* p = reinterpret_cast<const unsigned char*>(&k);
+        size_t h = 1469598103934665603ull;
+        for (size_t i = 0; i < sizeof(GraphKey); i++) h = (h ^ p[i]) * 1099511628211ull;
+        return h;
+    }
+};
+struct GraphEntry {
+    cudaGraphExec_t exec;
+    long long kernels;   // kernel nodes per replay
+};
+struct GraphCache {
+    std::mutex mu;
+    std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> map;
+    cudaStream_t cap[64] = {nullptr};
+};
+GraphCache g_graphs;
+
+cudaStream_t capture_stream() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_graphs.mu);
+    if (!g_graphs.cap[dev & 63]) cudaStreamCreateWithFlags(&g_graphs.cap[dev & 63], cudaStreamNonBlocking);
+    return g_graphs.cap[dev & 63];
+}
+
 // ------------------------------------------------------------- BiCGSTAB run --
-// Runs BiCGSTAB on vectors of type VT with the packed matrix of type MT until
-// every (cluster, rhs) is done.  bsrc: right-hand side (FP64, or VT when b128 is
-// null and bvt given).  The solution lands in the x vector of the workspace.
-template <typename MT, typename AT, typename VT, int R, bool DENSE>
-int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, const MT* mat,
-                 const double2* tvec, const double2* b128, VT* bvt, double tol, int maxiter, KState* st,
-                 int dense_D, cudaStream_t stream, int* host_status_buf) {
+// Runs BiCGSTAB on vectors of type VT (double2 with pol 0 or dense, float2 with
+// pol 1) until every (cluster, rhs) is done.  The right-hand side is b128 (FP64) or,
+// when null, bvt.  The solution stays in the x vector of the workspace.
+template <typename VT, int R, bool DENSE>
+int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, int pol, const void* mat,
+                 const double2* tvec, const double2* b128, VT* bvt, double tol, int maxiter, KState* st, int dense_D,
+                 cudaStream_t stream, bool use_graph) {
     const size_t TV = (size_t)P.total_vec;
     VT* V = reinterpret_cast<VT*>(base + w.off_vec);
     VT *x = V, *r = V + TV, *r0 = V + 2 * TV, *p = V + 3 * TV, *v = V + 4 * TV, *s = V + 5 * TV, *t = V + 6 * TV,
@@ -881,109 +1148,143 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
     double2* Tx = reinterpret_cast<double2*>(base + w.off_tx);
     const int nsr = P.nsys * R;
-    const int sblocks = (nsr + 127) / 128;
+    const unsigned sblocks = (unsigned)((nsr + 127) / 128);
+    const unsigned vb = (unsigned)P.nv;
 
-    auto apply = [&](const VT* xin, VT* yout, int mode, const VT* aux, int mask, const double2* bb) -> int {
+    auto apply = [&](const VT* xin, VT* yout, int mode, const VT* aux, int mask, const double2* bb,
+                     cudaStream_t sm) -> int {
         if (DENSE) {
             const long long grid = std::min<long long>(((long long)dense_D * 32 + 255) / 256, (long long)gb::sm_count() * 8);
-            k_dense_gemv<R><<<(unsigned)std::max<long long>(grid, 1), 256, 0, stream>>>(
-                dense_D, reinterpret_cast<const double2*>(mat), reinterpret_cast<const double2*>(xin), Tx, st);
+            gb::note_launch();
+            k_dense_gemv<R><<<(unsigned)std::max<long long>(grid, 1), 256, 0, sm>>>(
+                dense_D, reinterpret_cast<const double2*>(mat), reinterpret_cast<const double2*>(xin), Tx);
             GB_CUDA_TRY(cudaGetLastError());
-            k_reduce<double, VT, R, true><<<P.nitems, kItemRows, 0, stream>>>(
-                D.sys, D.items, P.nitems, D.sp, D.row_strip, st, mask, nullptr, nullptr, Tx, xin, yout, mode, aux, bb,
+            gb::note_launch();
+            k_reduce<double2, VT, R, true><<<(unsigned)P.nr, kRWarps * 32, 0, sm>>>(
+                D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, nullptr, nullptr, Tx, xin, yout, mode, aux, bb,
                 dots);
             GB_CUDA_TRY(cudaGetLastError());
             return GB_OK;
         }
-        return launch_apply<MT, AT, VT, R>(P, D, w, base, st, mask, mat, tvec, xin, yout, mode, aux, bb, dots, stream);
+        return launch_apply<VT, R>(P, D, w, base, st, mask, pol, mat, nullptr, tvec, xin, yout, mode, aux, bb, dots, sm);
+    };
+    auto iteration = [&](cudaStream_t sm) -> int {
+        gb::note_launch();
+        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 1, nullptr, nullptr, x, r, r0, p, v, s, t, dots);
+        int e = apply(p, v, 1, r0, 0, nullptr, sm);
+        if (e) return e;
+        gb::note_launch();
+        k_scalar<R><<<sblocks, 128, 0, sm>>>(D.sp, P.nsys, st, 1, dots, tol, maxiter);
+        gb::note_launch();
+        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 2, nullptr, nullptr, x, r, r0, p, v, s, t, dots);
+        e = apply(s, t, 2, s, 0, nullptr, sm);
+        if (e) return e;
+        gb::note_launch();
+        k_scalar<R><<<sblocks, 128, 0, sm>>>(D.sp, P.nsys, st, 2, dots, tol, maxiter);
+        gb::note_launch();
+        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 3, nullptr, nullptr, x, r, r0, p, v, s, t, dots);
+        gb::note_launch();
+        k_scalar<R><<<sblocks, 128, 0, sm>>>(D.sp, P.nsys, st, 3, dots, tol, maxiter);
+        GB_CUDA_TRY(cudaGetLastError());
+        return GB_OK;
     };
 
-    // init
-    k_vec<VT, R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, st, 0, b128, bvt ? bvt : bx, x, r, r0,
-                                                     p, v, s, t, dots);
+    // init: x = 0, r = r0 = b, scalars
+    gb::note_launch();
+    k_vec<VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, 0, b128, bvt ? bvt : bx, x, r, r0, p, v, s, t,
+                                            dots);
     GB_CUDA_TRY(cudaGetLastError());
+    gb::note_launch();
     k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 0, dots, tol, maxiter);
     GB_CUDA_TRY(cudaGetLastError());
     const VT* bsrc_vt = bvt ? bvt : bx;
 
-    KState* hst = nullptr;
-    std::vector<KState> hbuf(nsr);
-    (void)host_status_buf;
-    const int max_chunks = maxiter / kChunk + 64;
-    for (int chunk = 0; chunk < max_chunks; chunk++) {
-        for (int itn = 0; itn < kChunk; itn++) {
-            k_vec<VT, R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, st, 1, nullptr, nullptr, x, r,
-                                                             r0, p, v, s, t, dots);
-            int e = apply(p, v, 1, r0, 0, nullptr);
-            if (e) return e;
-            k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 1, dots, tol, maxiter);
-            k_vec<VT, R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, st, 2, nullptr, nullptr, x, r,
-                                                             r0, p, v, s, t, dots);
-            e = apply(s, t, 2, s, 0, nullptr);
-            if (e) return e;
-            k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 2, dots, tol, maxiter);
-            k_vec<VT, R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, st, 3, nullptr, nullptr, x, r,
-                                                             r0, p, v, s, t, dots);
-            k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 3, dots, tol, maxiter);
-            GB_CUDA_TRY(cudaGetLastError());
+    // a chunk of iterations, captured once per argument set and replayed
+    cudaGraphExec_t exec = nullptr;
+    long long exec_kernels = 0;
+    if (use_graph) {
+        GraphKey key{};
+        const void* a[12] = {base, mat, tvec, D.sys, D.strips, D.vitems, D.ritems, D.sp, st, nullptr, nullptr, nullptr};
+        memcpy(key.a, a, sizeof(a));
+        key.n[0] = P.nsys;
+        key.n[1] = R | (pol << 8) | ((DENSE ? 1 : 0) << 16) | ((long long)sizeof(VT) << 24);
+        key.n[2] = P.nstrips;
+        key.n[3] = P.nv | ((long long)P.nr << 32);
+        memcpy(&key.n[4], &tol, sizeof(double));
+        key.n[5] = maxiter | ((long long)dense_D << 32);
+        key.n[6] = P.max_B;
+        key.n[7] = P.total_vec;
+        {
+            std::lock_guard<std::mutex> lk(g_graphs.mu);
+            auto f = g_graphs.map.find(key);
+            if (f != g_graphs.map.end()) {
+                exec = f->second.exec;
+                exec_kernels = f->second.kernels;
+            }
         }
-        GB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), st, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
+        if (!exec) {
+            cudaStream_t cs = capture_stream();
+            GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            gb::capture_begin();
+            int e = GB_OK;
+            for (int itn = 0; itn < kChunk && e == GB_OK; itn++) e = iteration(cs);
+            exec_kernels = gb::capture_end();
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(cs, &g);
+            if (e) {
+                if (g) cudaGraphDestroy(g);
+                return e;
+            }
+            if (ce != cudaSuccess) return gb_set_cuda_error(ce, "capture of BiCGSTAB chunk", __FILE__, __LINE__);
+            ce = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) return gb_set_cuda_error(ce, "instantiate BiCGSTAB graph", __FILE__, __LINE__);
+            std::lock_guard<std::mutex> lk(g_graphs.mu);
+            if (g_graphs.map.size() > 256) {   // bounded cache
+                for (auto& kv : g_graphs.map) cudaGraphExecDestroy(kv.second.exec);
+                g_graphs.map.clear();
+            }
+            g_graphs.map[key] = GraphEntry{exec, exec_kernels};
+        }
+    }
+
+    std::vector<KState> hst(nsr);
+    // every restart may reset the count once; bound the chunks accordingly
+    const long long max_chunks = ((long long)maxiter / kChunk + 2) * (kMaxRestarts + 2) + 16;
+    for (long long chunk = 0; chunk < max_chunks; chunk++) {
+        if (exec) {
+            GB_CUDA_TRY(cudaGraphLaunch(exec, stream));
+            gb::note_launches(exec_kernels);
+        } else {
+            for (int itn = 0; itn < kChunk; itn++) {
+                int e = iteration(stream);
+                if (e) return e;
+            }
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
         GB_CUDA_TRY(cudaStreamSynchronize(stream));
         bool all_done = true, restart = false;
         for (int q = 0; q < nsr; q++) {
-            if (!hbuf[q].done) all_done = false;
-            if (hbuf[q].need_restart) restart = true;
+            if (!hst[q].done) all_done = false;
+            if (hst[q].need_restart) restart = true;
         }
-        if (restart) {
-            // r = b - A x for the restarting clusters, r0 = r, rho = |r|^2
-            int e = apply(x, r, 3, bsrc_vt, 1, b128);
+        if (restart) {   // r = b - A x for the restarting clusters, r0 = r, rho = |r|^2
+            int e = apply(x, r, 3, bsrc_vt, 1, b128, stream);
             if (e) return e;
-            k_vec<VT, R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, st, 4, nullptr, nullptr, x, r,
-                                                             r0, p, v, s, t, dots);
+            gb::note_launch();
+            k_vec<VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, 4, nullptr, nullptr, x, r, r0, p, v, s,
+                                                    t, dots);
+            gb::note_launch();
             k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 4, dots, tol, maxiter);
             GB_CUDA_TRY(cudaGetLastError());
             continue;
         }
         if (all_done) return GB_OK;
     }
-    (void)hst;
-    return gb_set_error(GB_TIMEOUT, "BiCGSTAB driver exceeded its chunk limit");
+    return gb_set_error(GB_TIMEOUT, "BiCGSTAB driver exceeded its iteration bound");
 }
 
-template <typename VT>
-__global__ void k_copy_out(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, int R,
-                           const VT* __restrict__ src, double2* __restrict__ dst) {
-    const int it = blockIdx.x;
-    if (it >= nitems) return;
-    const Item I = items[it];
-    const gb::SysDev S = sys[I.sys];
-    const int lr = threadIdx.x;
-    if (lr >= I.nr) return;
-    const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
-    for (int rr = 0; rr < R; rr++) dst[vo + rr] = to_d2(src[vo + rr]);
-}
-
-__global__ void k_cast_f(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, int R,
-                         const double2* __restrict__ src, float2* __restrict__ dst, const KState* __restrict__ mask) {
-    const int it = blockIdx.x;
-    if (it >= nitems) return;
-    const Item I = items[it];
-    const gb::SysDev S = sys[I.sys];
-    const int lr = threadIdx.x;
-    if (lr >= I.nr) return;
-    const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
-    for (int rr = 0; rr < R; rr++) {
-        const double2 v = src[vo + rr];
-        const bool off = mask && mask[I.sys * R + rr].done;   // finished clusters get b = 0
-        dst[vo + rr] = off ? make_float2(0.f, 0.f) : make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
-    }
-}
-
-int finish_status(const Plan& P, KState* st_dev, int* status, int* iters, double* resid, cudaStream_t stream) {
-    const int nsr = P.nsys * P.R;
-    std::vector<KState> h(nsr);
-    GB_CUDA_TRY(cudaMemcpyAsync(h.data(), st_dev, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
-    GB_CUDA_TRY(cudaStreamSynchronize(stream));
+int finish_status(const KState* h, int nsr, int* status, int* iters, double* resid) {
     int worst = GB_OK;
     for (int q = 0; q < nsr; q++) {
         if (status) status[q] = h[q].status;
@@ -994,10 +1295,18 @@ int finish_status(const Plan& P, KState* st_dev, int* status, int* iters, double
     return worst;
 }
 
+int read_state(const KState* dev, int nsr, std::vector<KState>& h, cudaStream_t stream) {
+    h.resize(nsr);
+    GB_CUDA_TRY(cudaMemcpyAsync(h.data(), dev, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(stream));
+    return GB_OK;
+}
+
 template <int R>
 int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_tol, int max_refine,
-               const double* mat128, const float* mat64, const double* tvec, const double* b, double* x,
-               unsigned char* base, const WS& w, int* status, int* iters, double* resid, cudaStream_t stream) {
+               const double* mat128, const float* mat64, const float* mat64lo, const double* tvec, const double* b,
+               double* x, unsigned char* base, const WS& w, int* status, int* iters, double* resid,
+               cudaStream_t stream) {
     DevPlan D;
     int e = upload_plan(P, base, w, stream, D);
     if (e) return e;
@@ -1007,67 +1316,79 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
     const double2* b2 = reinterpret_cast<const double2*>(b);
     double2* x2 = reinterpret_cast<double2*>(x);
     const size_t TV = (size_t)P.total_vec;
+    const int nsr = P.nsys * R;
+    const unsigned vb = (unsigned)P.nv;
+    std::vector<KState> h;
     if (prec == GB_PREC_FP64) {
-        e = run_bicgstab<double2, double, double2, R, false>(P, D, w, base, reinterpret_cast<const double2*>(mat128),
-                                                             t2, b2, nullptr, tol, maxiter, st, 0, stream, nullptr);
+        e = run_bicgstab<double2, R, false>(P, D, w, base, 0, mat128, t2, b2, nullptr, tol, maxiter, st, 0, stream, true);
         if (e) return e;
-        double2* xv = reinterpret_cast<double2*>(base + w.off_vec);
-        k_copy_out<double2><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, R, xv, x2);
+        gb::note_launch();
+        k_copy_out<double2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R,
+                                                       reinterpret_cast<double2*>(base + w.off_vec), x2);
         GB_CUDA_TRY(cudaGetLastError());
-        return finish_status(P, st, status, iters, resid, stream);
+        e = read_state(st, nsr, h, stream);
+        if (e) return e;
+        return finish_status(h.data(), nsr, status, iters, resid);
     }
     float2* V = reinterpret_cast<float2*>(base + w.off_vec);
     float2* bx = V + 7 * TV;
     if (prec == GB_PREC_FP32) {
-        e = run_bicgstab<float2, float, float2, R, false>(P, D, w, base, reinterpret_cast<const float2*>(mat64), t2, b2,
-                                                          nullptr, tol, maxiter, st, 0, stream, nullptr);
+        e = run_bicgstab<float2, R, false>(P, D, w, base, 1, mat64, t2, b2, nullptr, tol, maxiter, st, 0, stream, true);
         if (e) return e;
-        k_copy_out<float2><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, R, V, x2);
+        gb::note_launch();
+        k_copy_out<float2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, V, x2);
         GB_CUDA_TRY(cudaGetLastError());
-        return finish_status(P, st, status, iters, resid, stream);
+        e = read_state(st, nsr, h, stream);
+        if (e) return e;
+        return finish_status(h.data(), nsr, status, iters, resid);
     }
-    // mixed: x = 0, r = b (FP64); repeat { FP32 BiCGSTAB on (I+T) d = r; x += d; r = b - (I+T) x (FP64) }
-    double2* r128 = reinterpret_cast<double2*>(base + w.off_x128r);
+    // mixed: x = 0, r = b (FP64); repeat { FP32 BiCGSTAB on (I + T) d = r; x += d;
+    // r = b - (I + T) x in double-float (or FP64) }
+    double2* r128 = reinterpret_cast<double2*>(base + w.off_r128);
     double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
-    const int nsr = P.nsys * R;
-    k_outer_start<R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, b2, x2, dots);
+    gb::note_launch();
+    k_outer_start<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, b2, x2, dots);
+    gb::note_launch();
     k_outer_init<R><<<(nsr + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, tol);
     GB_CUDA_TRY(cudaGetLastError());
     GB_CUDA_TRY(cudaMemcpyAsync(r128, b2, sizeof(double2) * TV, cudaMemcpyDeviceToDevice, stream));
-    int total_inner = 0;
-    std::vector<KState> hst(nsr), hin(nsr);
     for (int pass = 1; pass <= max_refine + 1; pass++) {
-        // inner FP32 solve of the current residual (clusters already done are masked by ost)
-        k_cast_f<<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, R, r128, bx, ost);
+        gb::note_launch();
+        k_cast_f<<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, r128, bx, ost);
         GB_CUDA_TRY(cudaGetLastError());
-        e = run_bicgstab<float2, float, float2, R, false>(P, D, w, base, reinterpret_cast<const float2*>(mat64), t2,
-                                                          nullptr, bx, inner_tol, maxiter, st, 0, stream, nullptr);
+        e = run_bicgstab<float2, R, false>(P, D, w, base, 1, mat64, t2, nullptr, bx, inner_tol, maxiter, st, 0, stream,
+                                           true);
         if (e) return e;
-        GB_CUDA_TRY(cudaMemcpyAsync(hin.data(), st, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
-        k_refine_axpy<R><<<P.nitems, kItemRows, 0, stream>>>(D.sys, D.items, P.nitems, ost, x2, V);
+        gb::note_launch();
+        k_refine_axpy<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, ost, x2, V);
         GB_CUDA_TRY(cudaGetLastError());
-        // FP64 residual r = b - (I + T) x on the complex128 matrix
-        e = launch_apply<double2, double, double2, R>(P, D, w, base, ost, -1, reinterpret_cast<const double2*>(mat128),
-                                                      t2, x2, r128, 3, nullptr, b2, dots, stream);
+        if (prec == GB_PREC_MIXED)
+            e = launch_apply<double2, R>(P, D, w, base, ost, -1, 2, mat64, mat64lo, t2, x2, r128, 3, nullptr, b2, dots,
+                                         stream);
+        else
+            e = launch_apply<double2, R>(P, D, w, base, ost, -1, 0, mat128, nullptr, t2, x2, r128, 3, nullptr, b2,
+                                         dots, stream);
         if (e) return e;
+        gb::note_launch();
         k_refine_check<R><<<(nsr + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, pass, max_refine);
         GB_CUDA_TRY(cudaGetLastError());
-        GB_CUDA_TRY(cudaMemcpyAsync(hst.data(), ost, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
-        GB_CUDA_TRY(cudaStreamSynchronize(stream));
-        for (int q = 0; q < nsr; q++) total_inner = std::max(total_inner, hin[q].iters);
+        e = read_state(ost, nsr, h, stream);
+        if (e) return e;
         bool all = true;
-        for (int q = 0; q < nsr; q++) all &= (hst[q].done != 0);
+        for (int q = 0; q < nsr; q++) all &= (h[q].done != 0);
         if (all) break;
     }
-    int worst = GB_OK;
-    for (int q = 0; q < nsr; q++) {
-        if (status) status[q] = hst[q].status;
-        if (iters) iters[q] = hst[q].iters;   // refinement passes
-        if (resid) resid[q] = hst[q].bsq > 0 ? std::sqrt(hst[q].rsq / hst[q].bsq) : 0.0;
-        if (hst[q].status != GB_OK && worst == GB_OK) worst = hst[q].status;
+    return finish_status(h.data(), nsr, status, iters, resid);
+}
+
+bool prec_ok(int prec, const double* m128, const float* m64, const float* m64lo) {
+    switch (prec) {
+        case GB_PREC_FP64: return m128 != nullptr;
+        case GB_PREC_FP32: return m64 != nullptr;
+        case GB_PREC_MIXED: return m64 && m64lo;
+        case GB_PREC_MIXED_FP64RES: return m64 && m128;
+        default: return false;
     }
-    (void)total_inner;
-    return worst;
 }
 
 }   // namespace
@@ -1081,14 +1402,13 @@ size_t gb_solve_workspace_size(int nsys, const gb_system* sys, int R, int prec) 
 }
 
 int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
-                   int max_refine, const double* mat128, const float* mat64, const double* tvec, const double* b,
-                   double* x, void* workspace, size_t ws_bytes, int* status, int* iters, double* resid,
-                   void* stream) {
+                   int max_refine, const double* mat128, const float* mat64, const float* mat64lo, const double* tvec,
+                   const double* b, double* x, void* workspace, size_t ws_bytes, int* status, int* iters,
+                   double* resid, void* stream) {
     if (nsys < 1 || !sys || !tvec || !b || !x || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
     if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
-    if (prec == GB_PREC_FP64 && !mat128) return gb_set_error(GB_BAD_ARG, "FP64 solve needs the complex128 matrix");
-    if (prec == GB_PREC_FP32 && !mat64) return gb_set_error(GB_BAD_ARG, "FP32 solve needs the complex64 matrix");
-    if (prec == GB_PREC_MIXED && (!mat64 || !mat128)) return gb_set_error(GB_BAD_ARG, "mixed solve needs both matrices");
+    if (!prec_ok(prec, mat128, mat64, mat64lo))
+        return gb_set_error(GB_BAD_ARG, "precision %d is missing one of its matrices", prec);
     if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
     cudaStream_t s = (cudaStream_t)stream;
     Plan P;
@@ -1099,26 +1419,27 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
     unsigned char* base = static_cast<unsigned char*>(workspace);
     if (inner_tol <= 0) inner_tol = 1e-6;
     if (R == 1)
-        return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, tvec, b, x, base, w, status,
-                             iters, resid, s);
-    return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, tvec, b, x, base, w, status,
-                         iters, resid, s);
+        return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                             status, iters, resid, s);
+    return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                         status, iters, resid, s);
 }
 
 size_t gb_apply_workspace_size(int nsys, const gb_system* sys, int R, int prec) {
-    return gb_solve_workspace_size(nsys, sys, R, prec == GB_PREC_FP64 ? GB_PREC_FP64 : GB_PREC_FP32);
+    return gb_solve_workspace_size(nsys, sys, R, prec);
 }
 
 int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
-                   const double* tvec, const double* x, double* y, void* workspace, size_t ws_bytes, void* stream) {
+                   const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
+                   size_t ws_bytes, void* stream) {
     if (nsys < 1 || !sys || !tvec || !x || !y || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
     if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
+    if (!prec_ok(prec, mat128, mat64, mat64lo)) return gb_set_error(GB_BAD_ARG, "matrix missing for precision %d", prec);
     cudaStream_t s = (cudaStream_t)stream;
     Plan P;
     int e = build_plan(nsys, sys, R, s, P);
     if (e) return e;
-    const int pw = (prec == GB_PREC_FP64) ? GB_PREC_FP64 : GB_PREC_FP32;
-    WS w = ws_layout(P, pw, false);
+    WS w = ws_layout(P, prec, false);
     if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
     unsigned char* base = static_cast<unsigned char*>(workspace);
     DevPlan D;
@@ -1129,50 +1450,35 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
     double2* y2 = reinterpret_cast<double2*>(y);
     double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
     const double2* t2 = reinterpret_cast<const double2*>(tvec);
-    if (prec == GB_PREC_FP64) {
-        if (!mat128) return gb_set_error(GB_BAD_ARG, "complex128 matrix missing");
-        if (R == 1)
-            return launch_apply<double2, double, double2, 1>(P, D, w, base, st, -1, reinterpret_cast<const double2*>(mat128),
-                                                             t2, x2, y2, 0, nullptr, nullptr, dots, s);
-        return launch_apply<double2, double, double2, 2>(P, D, w, base, st, -1, reinterpret_cast<const double2*>(mat128),
-                                                         t2, x2, y2, 0, nullptr, nullptr, dots, s);
-    }
-    if (!mat64) return gb_set_error(GB_BAD_ARG, "complex64 matrix missing");
-    // FP32 product on a rounded copy of x, result widened to FP64
+    const unsigned vb = (unsigned)P.nv;
+    auto ap = [&](int pol, const void* hi, const void* lo) {
+        return R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr,
+                                                 dots, s)
+                      : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr,
+                                                 dots, s);
+    };
+    if (prec == GB_PREC_FP64) return ap(0, mat128, nullptr);
+    if (prec == GB_PREC_MIXED) return ap(2, mat64, mat64lo);
+    // FP32 product on a rounded copy of x, widened to FP64
     const size_t TV = (size_t)P.total_vec;
     float2* V = reinterpret_cast<float2*>(base + w.off_vec);
     float2 *xf = V, *yf = V + TV;
-    k_cast_f<<<P.nitems, kItemRows, 0, s>>>(D.sys, D.items, P.nitems, R, x2, xf, nullptr);
+    gb::note_launch();
+    k_cast_f<<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, x2, xf, nullptr);
     if (R == 1)
-        e = launch_apply<float2, float, float2, 1>(P, D, w, base, st, -1, reinterpret_cast<const float2*>(mat64), t2, xf,
-                                                   yf, 0, nullptr, nullptr, dots, s);
+        e = launch_apply<float2, 1>(P, D, w, base, st, -1, 1, mat64, nullptr, t2, xf, yf, 0, nullptr, nullptr, dots, s);
     else
-        e = launch_apply<float2, float, float2, 2>(P, D, w, base, st, -1, reinterpret_cast<const float2*>(mat64), t2, xf,
-                                                   yf, 0, nullptr, nullptr, dots, s);
+        e = launch_apply<float2, 2>(P, D, w, base, st, -1, 1, mat64, nullptr, t2, xf, yf, 0, nullptr, nullptr, dots, s);
     if (e) return e;
-    k_copy_out<float2><<<P.nitems, kItemRows, 0, s>>>(D.sys, D.items, P.nitems, R, yf, y2);
+    gb::note_launch();
+    k_copy_out<float2><<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, yf, y2);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
 
 size_t gb_solve_dense_workspace_size(int D, int R) {
-    // one pseudo-cluster of D rows (B = D handled by items only)
     Plan P;
-    P.nsys = 1;
-    P.R = R;
-    gb::SysDev sd{};
-    sd.D = D;
-    sd.B = D;
-    sd.N = 1;
-    P.sd.push_back(sd);
-    SysPlan sp{};
-    sp.item_begin = 0;
-    for (int r0 = 0; r0 < D; r0 += kItemRows) P.items.push_back(Item{0, r0, std::min(kItemRows, D - r0), 0});
-    sp.item_end = (int)P.items.size();
-    P.sp.push_back(sp);
-    P.row_strip = {0, 0};
-    P.nitems = (int)P.items.size();
-    P.total_vec = (long long)D * R;
+    dense_plan(D, R, P);
     return ws_layout(P, GB_PREC_FP64, true).total;
 }
 
@@ -1183,22 +1489,7 @@ int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, do
     if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
     cudaStream_t s = (cudaStream_t)stream;
     Plan P;
-    P.nsys = 1;
-    P.R = R;
-    gb::SysDev sd{};
-    sd.D = D;
-    sd.B = D;
-    sd.N = 1;
-    sd.vec_off = 0;
-    P.sd.push_back(sd);
-    SysPlan sp{};
-    sp.item_begin = 0;
-    for (int r0 = 0; r0 < D; r0 += kItemRows) P.items.push_back(Item{0, r0, std::min(kItemRows, D - r0), 0});
-    sp.item_end = (int)P.items.size();
-    P.sp.push_back(sp);
-    P.row_strip = {0, 0};
-    P.nitems = (int)P.items.size();
-    P.total_vec = (long long)D * R;
+    dense_plan(D, R, P);
     WS w = ws_layout(P, GB_PREC_FP64, true);
     if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
     unsigned char* base = static_cast<unsigned char*>(workspace);
@@ -1207,18 +1498,21 @@ int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, do
     if (e) return e;
     KState* st = reinterpret_cast<KState*>(base + w.off_state);
     if (R == 1)
-        e = run_bicgstab<double2, double, double2, 1, true>(P, Dp, w, base, reinterpret_cast<const double2*>(T), nullptr,
-                                                            reinterpret_cast<const double2*>(b), nullptr, tol, maxiter,
-                                                            st, D, s, nullptr);
+        e = run_bicgstab<double2, 1, true>(P, Dp, w, base, 0, T, nullptr, reinterpret_cast<const double2*>(b), nullptr,
+                                           tol, maxiter, st, D, s, false);
     else
-        e = run_bicgstab<double2, double, double2, 2, true>(P, Dp, w, base, reinterpret_cast<const double2*>(T), nullptr,
-                                                            reinterpret_cast<const double2*>(b), nullptr, tol, maxiter,
-                                                            st, D, s, nullptr);
+        e = run_bicgstab<double2, 2, true>(P, Dp, w, base, 0, T, nullptr, reinterpret_cast<const double2*>(b), nullptr,
+                                           tol, maxiter, st, D, s, false);
     if (e) return e;
-    double2* xv = reinterpret_cast<double2*>(base + w.off_vec);
-    k_copy_out<double2><<<P.nitems, kItemRows, 0, s>>>(Dp.sys, Dp.items, P.nitems, R, xv, reinterpret_cast<double2*>(x));
+    gb::note_launch();
+    k_copy_out<double2><<<(unsigned)P.nv, kVRows, 0, s>>>(Dp.sys, Dp.vitems, P.nv, R,
+                                                          reinterpret_cast<double2*>(base + w.off_vec),
+                                                          reinterpret_cast<double2*>(x));
     GB_CUDA_TRY(cudaGetLastError());
-    return finish_status(P, st, status, iters, resid, s);
+    std::vector<KState> h;
+    e = read_state(st, P.nsys * R, h, s);
+    if (e) return e;
+    return finish_status(h.data(), P.nsys * R, status, iters, resid);
 }
 
 }   // extern "C"

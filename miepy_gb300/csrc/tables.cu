@@ -231,6 +231,7 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->rowinfo, rowinfo.data(), sizeof(int) * B, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->miecol, miecol.data(), sizeof(int) * B, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) {
+        gb::note_launch();
         k_tuple_table<<<(M + 127) / 128, 128, 0, stream>>>(L, M, T->nmvu, T->qab, T->cA, T->cB);
         e = cudaGetLastError();
     }

@@ -15,7 +15,9 @@ import torch
 from . import _native as nat
 from .modes import lmax_to_rmax
 
-PRECISIONS = {"fp64": nat.PREC_FP64, "mixed": nat.PREC_MIXED, "fp32": nat.PREC_FP32}
+PRECISIONS = {"fp64": nat.PREC_FP64, "mixed": nat.PREC_MIXED, "fp32": nat.PREC_FP32,
+              "mixed_fp64res": nat.PREC_MIXED_FP64RES}
+NEEDS = {"fp64": ("c128",), "mixed": ("hi", "lo"), "fp32": ("hi",), "mixed_fp64res": ("hi", "c128")}
 
 
 def current_stream(device=None) -> int:
@@ -38,7 +40,7 @@ def footprint_bytes(N, lmax, R=1, precision="fp64"):
     """HBM bytes a cluster needs inside a batch (matrices + vectors + solver scratch), for admission."""
     el = matrix_elements(N, lmax)
     D = 2 * lmax_to_rmax(lmax) * N
-    mat = (16 * el if precision in ("fp64", "mixed") else 0) + (8 * el if precision in ("mixed", "fp32") else 0)
+    mat = sum({"c128": 16, "hi": 8, "lo": 8}[m] for m in NEEDS[precision]) * el
     P = N * (N - 1) // 2
     B = 2 * lmax_to_rmax(lmax)
     partials = 16 * (P * B * R + (P + N) * B * R)
@@ -106,10 +108,10 @@ class ClusterBatch:
         self.h2d_bytes = hpos.nbytes + hmie.nbytes + hint.nbytes + hb.nbytes
         self.tvec = torch.empty(max(t_off, 1), dtype=torch.complex128, device=dev)
         self.x = torch.zeros(max(vec_off, 1), dtype=torch.complex128, device=dev)
-        need128 = precision in ("fp64", "mixed")
-        need64 = precision in ("mixed", "fp32")
-        self.mat128 = torch.empty(max(mat_off, 1), dtype=torch.complex128, device=dev) if need128 else None
-        self.mat64 = torch.empty(max(mat_off, 1), dtype=torch.complex64, device=dev) if need64 else None
+        need = NEEDS[precision]
+        self.mat128 = torch.empty(max(mat_off, 1), dtype=torch.complex128, device=dev) if "c128" in need else None
+        self.mat64 = torch.empty(max(mat_off, 1), dtype=torch.complex64, device=dev) if "hi" in need else None
+        self.mat64lo = torch.empty(max(mat_off, 1), dtype=torch.complex64, device=dev) if "lo" in need else None
         self._ws = None
         self.status = self.iters = self.resid = None
         self.assembled = False
@@ -122,7 +124,7 @@ class ClusterBatch:
                                         nat.ptr(self.tvec), st), "expand mie")
         if self.totals["mat"] > 0:
             nat.check(L.gb_assemble_batch(self.nsys, self.sys, nat.ptr(self.pos), nat.ptr(self.mat128),
-                                          nat.ptr(self.mat64), st), "assemble")
+                                          nat.ptr(self.mat64), nat.ptr(self.mat64lo), st), "assemble")
         self.assembled = True
         return self
 
@@ -147,7 +149,8 @@ class ClusterBatch:
         iters = np.zeros(n, dtype=np.int32)
         resid = np.zeros(n, dtype=np.float64)
         rc = L.gb_solve_batch(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
-                              int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64), nat.ptr(self.tvec),
+                              int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64), nat.ptr(self.mat64lo),
+                              nat.ptr(self.tvec),
                               nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data,
                               iters.ctypes.data, resid.ctypes.data, current_stream(self.device))
         if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN) or (raise_on_fail and rc):
@@ -156,15 +159,17 @@ class ClusterBatch:
         return status
 
     def apply(self, x, precision="fp64"):
-        """y = (I + T) x on the packed matrices (x: device complex128 [total_vec])."""
+        """y = (I + T) x on the packed matrices (x: device complex128 [total_vec]);
+        precision "fp64" (complex128 matrix), "fp32" (complex64) or "mixed"
+        (double-float hi + lo)."""
         L = nat.lib()
         code = PRECISIONS[precision]
         need = L.gb_apply_workspace_size(self.nsys, self.sys, self.R, code)
         ws = torch.empty(need, dtype=torch.uint8, device=self.device)
         y = torch.empty_like(x)
         nat.check(L.gb_apply_batch(self.nsys, self.sys, self.R, code, nat.ptr(self.mat128), nat.ptr(self.mat64),
-                                   nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y), nat.ptr(ws), ws.numel(),
-                                   current_stream(self.device)), "apply")
+                                   nat.ptr(self.mat64lo), nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y), nat.ptr(ws),
+                                   ws.numel(), current_stream(self.device)), "apply")
         return y
 
     def epilogue(self, eps_b, source=True, want_fields=True):

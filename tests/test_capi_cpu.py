@@ -96,8 +96,9 @@ def test_materials_drude_and_struct():
 def test_footprint_grows_with_size():
     a = gb.footprint_bytes(10, 3, 1, "fp64")
     b = gb.footprint_bytes(20, 3, 1, "fp64")
-    c = gb.footprint_bytes(20, 3, 1, "mixed")
-    assert b > a and c > b
+    c = gb.footprint_bytes(20, 3, 1, "mixed_fp64res")
+    d = gb.footprint_bytes(20, 3, 1, "fp32")
+    assert b > a and c > b > d
 
 
 def test_no_cpu_fallback_when_cuda_missing():
