@@ -142,6 +142,14 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
                    const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
                    size_t ws_bytes, void* stream);
 
+/* The operator product of gb_apply_batch launched reps times back to back on
+ * one prepared plan (no host work between launches), for kernel timing with
+ * events on the stream.  gemv_only != 0 repeats only the matrix pass (the
+ * partial-sum kernel) after the first full product. */
+int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                    const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
+                    size_t ws_bytes, int reps, int gemv_only, void* stream);
+
 /* -------------------------------------------------------------- epilogue --
  * Per cluster and right-hand side, from p_inc [D][R] (c128), p_src [D][R],
  * mie_scat / mie_int [N,2,lmax] c128:

@@ -7,7 +7,9 @@
 //   1. h_p(kr) by the upward j/y recurrence of spherical_hn_recursion
 //      (cpp/src/special.cpp:90-111), one thread; P_p^mu(cos theta) (no
 //      Condon-Shortley phase, GSL_SF_LEGENDRE_NONE convention), one thread per
-//      order mu; e^{i mu phi}, one thread per mu;
+//      order mu; e^{i mu phi} by powering e^{i phi}, one thread per mu.  The angles
+//      enter only through cos/sin of theta and phi, taken directly from the
+//      separation vector: no acos/atan2/sincos of angles on the (slow) FP64 pipe;
 //   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p);
 //   3. one thread per canonical tuple: A_t, B_t as real x complex FMA sums over
 //      the per-lmax coefficient table (tables.cu);
@@ -27,6 +29,12 @@
 namespace {
 
 constexpr int kAsmThreads = 256;
+
+// 1/k for the Legendre recurrence (k = q - mu <= 2*lmax + 1)
+__constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
+    0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8, 1.0 / 9, 1.0 / 10, 1.0 / 11,
+    1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20, 1.0 / 21,
+    1.0 / 22, 1.0 / 23};
 
 struct AsmSmem {
     int PM, MU, M;
@@ -96,39 +104,49 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         const double* pi_ = pos + S.pos_off + 3 * (long long)i;
         const double* pj_ = pos + S.pos_off + 3 * (long long)j;
         const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
-        const double rad = sqrt(dx * dx + dy * dy + dz * dz);
-        const double theta = acos(dz / rad);
-        const double phi = atan2(dy, dx);
-        const double x = cos(theta);
+        // direction cosines straight from the separation vector (the reference goes
+        // through acos/atan2 and back; the values agree to rounding)
+        const double rho2 = dx * dx + dy * dy;
+        const double rad = sqrt(rho2 + dz * dz);
+        const double inv_r = 1.0 / rad;
+        const double x = dz * inv_r;                       // cos(theta)
+        const double u = sqrt(rho2) * inv_r;               // sin(theta) >= 0
+        double cphi = 1.0, sphi = 0.0;                     // phi = atan2(dy, dx) = 0 on the z axis
+        if (rho2 > 0.0) {
+            const double inv_rho = 1.0 / sqrt(rho2);
+            cphi = dx * inv_rho;
+            sphi = dy * inv_rho;
+        }
 
         // ---- phase 1: Hankel, Legendre, azimuthal phases
         if (tid == 32) {
             const double z = S.k * rad;
+            const double inv_z = 1.0 / z;
             double sz, cz;
             sincos(z, &sz, &cz);
-            double j0 = sz / z, y0 = -cz / z;
-            double j1 = j0 / z + y0, y1 = y0 / z - j0;
+            double j0 = sz * inv_z, y0 = -cz * inv_z;
+            double j1 = j0 * inv_z + y0, y1 = y0 * inv_z - j0;
             h[0] = make_double2(j0, y0);
             if (PM > 1) h[1] = make_double2(j1, y1);
             for (int q = 2; q < PM; q++) {
-                double jn = (2 * q - 1) / z * j1 - j0;
-                double yn = (2 * q - 1) / z * y1 - y0;
+                const double f = (2 * q - 1) * inv_z;
+                const double jn = f * j1 - j0;
+                const double yn = f * y1 - y0;
                 j0 = j1; j1 = jn; y0 = y1; y1 = yn;
                 h[q] = make_double2(jn, yn);
             }
         }
         if (tid < PM) {
             const int mu = tid;
-            const double u = sqrt(fmax(0.0, (1.0 - x) * (1.0 + x)));
             double pmm = 1.0;
-            for (int k = 1; k <= mu; k++) pmm *= (2 * k - 1) * u;
+            for (int kk = 1; kk <= mu; kk++) pmm *= (2 * kk - 1) * u;
             Pl[mu * PM + mu] = pmm;
             if (mu + 1 < PM) {
                 double p1 = x * (2 * mu + 1) * pmm;
                 Pl[(mu + 1) * PM + mu] = p1;
                 double pa = pmm, pb = p1;
                 for (int q = mu + 2; q < PM; q++) {
-                    double pc = ((2 * q - 1) * x * pb - (q + mu - 1) * pa) / (double)(q - mu);
+                    const double pc = ((2 * q - 1) * x * pb - (q + mu - 1) * pa) * c_inv_int[q - mu];
                     Pl[q * PM + mu] = pc;
                     pa = pb;
                     pb = pc;
@@ -136,10 +154,16 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             }
         }
         if (tid >= 64 && tid < 64 + MU) {
+            // e^{i mu phi} = (cos phi + i sin phi)^mu by binary powering
             const int mu = tid - 64 - 2 * L;
-            double sn, cs;
-            sincos((double)mu * phi, &sn, &cs);
-            eph[tid - 64] = make_double2(cs, sn);
+            int e = mu < 0 ? -mu : mu;
+            double2 acc = make_double2(1.0, 0.0), base = make_double2(cphi, sphi);
+            while (e) {
+                if (e & 1) acc = cmul(acc, base);
+                base = cmul(base, base);
+                e >>= 1;
+            }
+            eph[tid - 64] = mu < 0 ? make_double2(acc.x, -acc.y) : acc;
         }
         __syncthreads();
         for (int e = tid; e < PM * MU; e += kAsmThreads) {
@@ -148,7 +172,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             if (am <= q) {
                 double P = Pl[q * PM + am];
                 if (mu < 0) P *= S.neg_ratio[q * PM + am];
-                double2 he = cmul(h[q], eph[mi]);
+                const double2 he = cmul(h[q], eph[mi]);
                 gval = make_double2(P * he.x, P * he.y);
             }
             G[e] = gval;

@@ -1,4 +1,4 @@
-// K7: fused epilogue of a solve.  One thread per (particle, right-hand side):
+// K7: fused epilogue of a solve.  One warp per (particle, right-hand side):
 //   p_scat = t o p_inc, p_int = p_inc * mie_int[:, ::-1, n-1]  (sphere_cluster.py:715-717),
 //   per-multipole cross-sections                             (cpp/src/flux.cpp:5-30),
 //   force and torque (Barton-type coefficient sums)          (cpp/src/forces.cpp:7-137),
@@ -44,8 +44,13 @@ struct EpiArgs {
     double* torque;
 };
 
-__global__ void k_epilogue(EpiArgs a, long long total) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per (particle, rhs).  Lanes stride over the rows for p_scat / p_int,
+// over the (a, n) multipoles for the cross-sections, and over the modes r for
+// the force / torque sums; butterfly shuffles combine lane partials in a fixed
+// order, so results do not depend on scheduling.
+__global__ void __launch_bounds__(128) k_epilogue(EpiArgs a, long long total) {
+    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (g >= total) return;
     int s = 0;
     while (s + 1 < a.nsys && a.base[s + 1] <= g) s++;
@@ -60,42 +65,36 @@ __global__ void k_epilogue(EpiArgs a, long long total) {
     const double k = S.k;
     auto pin = [&](int e) { return a.p_inc[vb + (long long)e * R]; };
     auto psrc = [&](int e) { return a.p_src[vb + (long long)e * R]; };
-    auto pscat = [&](int e) {
-        const int n = (int)floor(sqrt((double)(e % rmax) + 1.0 + 0.5));   // r + 1 in [n^2, (n+1)^2 - 1]
-        int nn = n;
-        while (nn * nn > (e % rmax) + 1) nn--;
-        while ((nn + 1) * (nn + 1) <= (e % rmax) + 1) nn++;
-        const int aa = e / rmax;
-        return cmul(pin(e), ms[aa * L + nn - 1]);
-    };
-    // ---- p_scat, p_int, cross-sections
-    const double f = 4.0 * kPi / (k * k);
-    long long xo = 0;
-    if (a.xs) xo = ((a.obs_off[s] + i) * R + rr) * 3LL * 2 * L;
-    if (a.xs)
-        for (int c = 0; c < 6 * L; c++) a.xs[xo + c] = 0.0;
-    for (int aa = 0; aa < 2; aa++)
-        for (int n = 1; n <= L; n++) {
+    auto pscat = [&](int e) { return cmul(pin(e), ms[__ldg(S.miecol + e)]); };
+    // ---- p_scat, p_int (polarisation-swapped interior coefficients)
+    for (int e = lane; e < B; e += 32) {
+        const double2 pi_ = pin(e);
+        const int col = __ldg(S.miecol + e);   // a*L + n - 1
+        if (a.p_scat) a.p_scat[vb + (long long)e * R] = cmul(pi_, ms[col]);
+        if (a.p_int) {
+            const int aa = col / L, n1 = col % L;
+            a.p_int[vb + (long long)e * R] = cmul(pi_, mi[(1 - aa) * L + n1]);
+        }
+    }
+    // ---- per-multipole cross-sections: lane per (a, n)
+    if (a.xs) {
+        const double f = 4.0 * kPi / (k * k);
+        const long long xo = ((a.obs_off[s] + i) * R + rr) * 3LL * 2 * L;
+        for (int idx = lane; idx < 2 * L; idx += 32) {
+            const int aa = idx / L, n = idx % L + 1;
             double cabs = 0.0, cext = 0.0;
             for (int m = -n; m <= n; m++) {
                 const int e = aa * rmax + n * n + n + m - 1;
-                const double2 pi_ = pin(e);
+                const double2 pi_ = pin(e), pr = psrc(e);
                 const double2 ps = cmul(pi_, ms[aa * L + n - 1]);
-                if (a.p_scat) a.p_scat[vb + (long long)e * R] = ps;
-                if (a.p_int) a.p_int[vb + (long long)e * R] = cmul(pi_, mi[(1 - aa) * L + n - 1]);
-                if (a.xs) {
-                    const double2 pr = psrc(e);
-                    cabs += f * ((pi_.x * ps.x + pi_.y * ps.y) - (ps.x * ps.x + ps.y * ps.y));
-                    cext += f * (pr.x * ps.x + pr.y * ps.y);
-                }
+                cabs += f * ((pi_.x * ps.x + pi_.y * ps.y) - (ps.x * ps.x + ps.y * ps.y));
+                cext += f * (pr.x * ps.x + pr.y * ps.y);
             }
-            if (a.xs) {
-                const int idx = aa * L + n - 1;
-                a.xs[xo + 0 * 2 * L + idx] = cext - cabs;   // scattering
-                a.xs[xo + 1 * 2 * L + idx] = cabs;          // absorption
-                a.xs[xo + 2 * 2 * L + idx] = cext;          // extinction
-            }
+            a.xs[xo + 0 * 2 * L + idx] = cext - cabs;   // scattering
+            a.xs[xo + 1 * 2 * L + idx] = cabs;          // absorption
+            a.xs[xo + 2 * 2 * L + idx] = cext;          // extinction
         }
+    }
     if (!a.force && !a.torque) return;
     // ---- force / torque: p, q = scattered electric / magnetic; pi, qi = incident
     auto P = [&](int r) { return pscat(r); };
@@ -103,72 +102,79 @@ __global__ void k_epilogue(EpiArgs a, long long total) {
     auto PI = [&](int r) { return a.source ? pin(r) : csub(pin(r), psrc(r)); };
     auto QI = [&](int r) { return a.source ? pin(rmax + r) : csub(pin(rmax + r), psrc(rmax + r)); };
     const double eb = a.eps_b;
-    if (a.force) {
-        double2 Fxy = make_double2(0, 0), Fz = make_double2(0, 0);
-        const double Axy = kPi / (k * k) * kEps0 * eb;
-        const double Az = -2 * Axy;
-        for (int n = 1; n <= L; n++)
-            for (int m = -n; m <= n; m++) {
-                const int r = n * n + n + m - 1;
-                const double2 p = P(r), q = Qs(r), pi_ = PI(r), qi = QI(r);
-                if (m != n) {
-                    const double fc = Axy * sqrt((double)((n + m + 1) * (n - m))) / (double)(n * (n + 1));
-                    const int r1 = r + 1;
-                    const double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
-                    double2 t = cadd(tri(p, q1, pi_, qi1), tri(q, p1, qi, pi1));
-                    // p conj(q1) form: 2 p q1* - p qi1* - pi q1*  +  2 q p1* - q pi1* - qi p1*
-                    Fxy = cadd(Fxy, cscale(fc, t));
-                }
-                const double fz = Az * m / (double)(n * (n + 1));
-                Fz = cadd(Fz, cscale(fz, tri(p, q, pi_, qi)));
-                if (n < L) {
-                    double fc = -Axy * sqrt((double)((n + m + 2) * (n + m + 1) * n * (n + 2)) /
-                                            (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
-                    int r1 = (n + 1) * (n + 1) + (n + 1) + m;
-                    double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
-                    Fxy = cadd(Fxy, cscale(fc, cadd(tri(p, p1, pi_, pi1), tri(q, q1, qi, qi1))));
-                    fc = Axy * sqrt((double)((n - m + 1) * (n - m + 2) * n * (n + 2)) /
-                                    (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
-                    r1 = (n + 1) * (n + 1) + (n + 1) + m - 2;
-                    p1 = P(r1); q1 = Qs(r1); pi1 = PI(r1); qi1 = QI(r1);
-                    Fxy = cadd(Fxy, cscale(fc, cadd(tri(p1, p, pi1, pi_), tri(q1, q, qi1, qi))));
-                    fc = Az * sqrt((double)((n - m + 1) * (n + m + 1) * n * (n + 2)) /
-                                   (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
-                    r1 = (n + 1) * (n + 1) + (n + 1) + m - 1;
-                    p1 = P(r1); q1 = Qs(r1); pi1 = PI(r1); qi1 = QI(r1);
-                    Fz = cadd(Fz, cscale(fc, cadd(tri(p1, p, pi1, pi_), tri(q1, q, qi1, qi))));
-                }
+    const double Axy = kPi / (k * k) * kEps0 * eb;
+    const double Az = -2 * Axy;
+    const double At = -2 * kPi / (k * k * k) * kEps0 * eb;
+    double2 Fxy = make_double2(0, 0), Fz = make_double2(0, 0);
+    double T0 = 0, T1 = 0, T2 = 0;
+    for (int r = lane; r < rmax; r += 32) {
+        int n = (int)sqrt((double)(r + 1));
+        while (n * n > r + 1) n--;
+        while ((n + 1) * (n + 1) <= r + 1) n++;
+        const int m = r + 1 - n * n - n;
+        const double2 p = P(r), q = Qs(r), pi_ = PI(r), qi = QI(r);
+        if (a.force) {
+            if (m != n) {
+                const double fc = Axy * sqrt((double)((n + m + 1) * (n - m))) / (double)(n * (n + 1));
+                const int r1 = r + 1;
+                const double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
+                Fxy = cadd(Fxy, cscale(fc, cadd(tri(p, q1, pi_, qi1), tri(q, p1, qi, pi1))));
             }
-        const long long fo = ((a.obs_off[s] + i) * R + rr) * 3LL;
-        a.force[fo + 0] = Fxy.x;
-        a.force[fo + 1] = Fxy.y;
-        a.force[fo + 2] = Fz.x;
+            const double fz = Az * m / (double)(n * (n + 1));
+            Fz = cadd(Fz, cscale(fz, tri(p, q, pi_, qi)));
+            if (n < L) {
+                double fc = -Axy * sqrt((double)((n + m + 2) * (n + m + 1) * n * (n + 2)) /
+                                        (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
+                int r1 = (n + 1) * (n + 1) + (n + 1) + m;
+                double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
+                Fxy = cadd(Fxy, cscale(fc, cadd(tri(p, p1, pi_, pi1), tri(q, q1, qi, qi1))));
+                fc = Axy * sqrt((double)((n - m + 1) * (n - m + 2) * n * (n + 2)) /
+                                (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
+                r1 = (n + 1) * (n + 1) + (n + 1) + m - 2;
+                p1 = P(r1); q1 = Qs(r1); pi1 = PI(r1); qi1 = QI(r1);
+                Fxy = cadd(Fxy, cscale(fc, cadd(tri(p1, p, pi1, pi_), tri(q1, q, qi1, qi))));
+                fc = Az * sqrt((double)((n - m + 1) * (n + m + 1) * n * (n + 2)) /
+                               (double)((2 * n + 3) * (2 * n + 1))) / (n + 1);
+                r1 = (n + 1) * (n + 1) + (n + 1) + m - 1;
+                p1 = P(r1); q1 = Qs(r1); pi1 = PI(r1); qi1 = QI(r1);
+                Fz = cadd(Fz, cscale(fc, cadd(tri(p1, p, pi1, pi_), tri(q1, q, qi1, qi))));
+            }
+        }
+        if (a.torque) {
+            if (m != n) {
+                const double fc = -At * sqrt((double)((n - m) * (n + m + 1)));
+                const int r1 = r + 1;
+                const double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
+                const double2 base = cadd(cmul(p, cj(p1)), cmul(q, cj(q1)));
+                const double2 sx = cadd(cadd(cmul(p1, cj(pi_)), cmul(p, cj(pi1))), cadd(cmul(q1, cj(qi)), cmul(q, cj(qi1))));
+                const double2 sy = cadd(csub(cmul(p1, cj(pi_)), cmul(p, cj(pi1))), csub(cmul(q1, cj(qi)), cmul(q, cj(qi1))));
+                T0 += fc * (base.x - 0.5 * sx.x);
+                T1 += fc * (base.y + 0.5 * sy.y);
+            }
+            const double2 c = cadd(cmul(p, cj(pi_)), cmul(q, cj(qi)));
+            T2 += At * m * ((p.x * p.x + p.y * p.y) + (q.x * q.x + q.y * q.y) - c.x);
+        }
     }
-    if (a.torque) {
-        const double A = -2 * kPi / (k * k * k) * kEps0 * eb;
-        double T0 = 0, T1 = 0, T2 = 0;
-        for (int n = 1; n <= L; n++)
-            for (int m = -n; m <= n; m++) {
-                const int r = n * n + n + m - 1;
-                const double2 p = P(r), q = Qs(r), pi_ = PI(r), qi = QI(r);
-                if (m != n) {
-                    const double fc = -A * sqrt((double)((n - m) * (n + m + 1)));
-                    const int r1 = r + 1;
-                    const double2 p1 = P(r1), q1 = Qs(r1), pi1 = PI(r1), qi1 = QI(r1);
-                    const double2 base = cadd(cmul(p, cj(p1)), cmul(q, cj(q1)));
-                    const double2 sx = cadd(cadd(cmul(p1, cj(pi_)), cmul(p, cj(pi1))), cadd(cmul(q1, cj(qi)), cmul(q, cj(qi1))));
-                    const double2 sy = cadd(csub(cmul(p1, cj(pi_)), cmul(p, cj(pi1))), csub(cmul(q1, cj(qi)), cmul(q, cj(qi1))));
-                    T0 += fc * (base.x - 0.5 * sx.x);
-                    T1 += fc * (base.y + 0.5 * sy.y);
-                }
-                const double fz = A * m;
-                const double2 c = cadd(cmul(p, cj(pi_)), cmul(q, cj(qi)));
-                T2 += fz * ((p.x * p.x + p.y * p.y) + (q.x * q.x + q.y * q.y) - c.x);
-            }
+    for (int o = 16; o > 0; o >>= 1) {
+        Fxy.x += __shfl_xor_sync(0xffffffffu, Fxy.x, o);
+        Fxy.y += __shfl_xor_sync(0xffffffffu, Fxy.y, o);
+        Fz.x += __shfl_xor_sync(0xffffffffu, Fz.x, o);
+        T0 += __shfl_xor_sync(0xffffffffu, T0, o);
+        T1 += __shfl_xor_sync(0xffffffffu, T1, o);
+        T2 += __shfl_xor_sync(0xffffffffu, T2, o);
+    }
+    if (lane == 0) {
         const long long fo = ((a.obs_off[s] + i) * R + rr) * 3LL;
-        a.torque[fo + 0] = T0;
-        a.torque[fo + 1] = T1;
-        a.torque[fo + 2] = T2;
+        if (a.force) {
+            a.force[fo + 0] = Fxy.x;
+            a.force[fo + 1] = Fxy.y;
+            a.force[fo + 2] = Fz.x;
+        }
+        if (a.torque) {
+            a.torque[fo + 0] = T0;
+            a.torque[fo + 1] = T1;
+            a.torque[fo + 2] = T2;
+        }
     }
 }
 
@@ -222,7 +228,7 @@ extern "C" int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const in
     a.torque = torque;
     const long long total = base[nsys];
     gb::note_launch();
-    k_epilogue<<<(unsigned)((total + 127) / 128), 128, 0, st_>>>(a, total);
+    k_epilogue<<<(unsigned)((total * 32 + 127) / 128), 128, 0, st_>>>(a, total);
     GB_CUDA_TRY(cudaGetLastError());
     return gb::stage_release(slot, st_);
 }

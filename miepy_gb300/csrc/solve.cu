@@ -57,7 +57,7 @@ namespace {
 constexpr int kVRows = 128;        // rows per vector work item (= threads per CTA)
 constexpr int kRRows = 32;         // rows per reduce work item
 constexpr int kRWarps = 8;         // warps per reduce CTA
-constexpr int kGemvThreads = 256;  // 8 warps
+constexpr int kGemvThreads = 128;  // 4 warps
 constexpr int kGemvWarps = kGemvThreads / 32;
 constexpr int kChunk = 4;          // iterations per host check
 constexpr int kMaxRestarts = 8;
@@ -247,8 +247,10 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
 
 // --------------------------------------------------------------- K3a GEMV --
 // RR: right-hand sides handled per launch (all R for Pol64/Pol32, one for PolDF,
-// the one at rr0); RT: stride of the [D][RT] vectors and partials.
-template <class Pol, int RR, int RT, int RPS, int NS>
+// the one at rr0); RT: stride of the [D][RT] vectors and partials.  The y vectors
+// of the current block pair live in per-warp shared memory, so the inner loop
+// only waits on the matrix stream; RU row steps of matrix loads are in flight.
+template <class Pol, int RR, int RT, int RPS, int NS, int RU>
 __global__ void __launch_bounds__(kGemvThreads)
 k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long nstrips,
         const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
@@ -261,7 +263,12 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     constexpr int CPG = Pol::CPG;
     extern __shared__ __align__(16) unsigned char gemv_smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    OutT* comb = reinterpret_cast<OutT*>(gemv_smem) + (size_t)wid * RPS * Bmax * RR;
+    // per warp: comb [RPS][Bmax][RR] OutT, then yu [Bmax][RR] YT, yw [Bmax][RR] YT
+    const size_t per_warp = (size_t)RPS * Bmax * RR * sizeof(OutT) + 2 * (size_t)Bmax * RR * sizeof(YT);
+    unsigned char* wbase = gemv_smem + (size_t)wid * ((per_warp + 15) & ~size_t(15));
+    OutT* comb = reinterpret_cast<OutT*>(wbase);
+    YT* syu = reinterpret_cast<YT*>(wbase + (size_t)RPS * Bmax * RR * sizeof(OutT));
+    YT* syw = syu + (size_t)Bmax * RR;
     const long long warp = ((long long)blockIdx.x * kGemvThreads + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     for (long long w = warp; w < nstrips; w += nwarps) {
@@ -290,11 +297,18 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             for (int c = 0; c < CPG; c++)
 #pragma unroll
                 for (int q = 0; q < RR; q++) Pol::zero(cu[k][c][q]);
-        const YT* yw_i = Yw + S.vec_off + (long long)sp.i * B * RT;
+        {   // y_w of particle i: the same for every block of the strip
+            const YT* src = Yw + S.vec_off + (long long)sp.i * B * RT;
+            for (int e = lane; e < B * RR; e += 32) syw[e] = src[(e / RR) * RT + rr0 + (e % RR)];
+        }
         for (int b = 0; b < sp.nb; b++) {
             const long long p = sp.p0 + b;
             const int j = sp.i + 1 + (int)(p - pair_start(sp.i, S.N));
-            const YT* yu_j = Yu + S.vec_off + (long long)j * B * RT;
+            {
+                const YT* src = Yu + S.vec_off + (long long)j * B * RT;
+                for (int e = lane; e < B * RR; e += 32) syu[e] = src[(e / RR) * RT + rr0 + (e % RR)];
+            }
+            __syncwarp();
             const long long blk = S.mat_off + p * (long long)B * B;
             Acc cw[NS][CPG][RR];
 #pragma unroll
@@ -303,7 +317,6 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
                 for (int c = 0; c < CPG; c++)
 #pragma unroll
                     for (int q = 0; q < RR; q++) Pol::zero(cw[k][c][q]);
-            constexpr int RU = 2;   // row steps in flight
             for (int r = 0; r < B; r += RPS * RU) {
                 typename Pol::Mat m[RU][NS][CPG];
 #pragma unroll
@@ -322,13 +335,12 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
                 for (int u = 0; u < RU; u++)
 #pragma unroll
                     for (int k = 0; k < NS; k++) {
-                        const int row = r + u * RPS + sro[k];
-                        if (!(sval[k] && row < B)) continue;
+                        const int row = min(r + u * RPS + sro[k], B - 1);   // padded rows carry zero matrix entries
                         YT yu[RR], yw[RR];
 #pragma unroll
                         for (int q = 0; q < RR; q++) {
-                            yu[q] = yu_j[row * RT + rr0 + q];
-                            yw[q] = yw_i[row * RT + rr0 + q];
+                            yu[q] = syu[row * RR + q];
+                            yw[q] = syw[row * RR + q];
                         }
 #pragma unroll
                         for (int c = 0; c < CPG; c++)
@@ -639,10 +651,13 @@ __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isf
 // Phases: 0 init (vector dots: |b|^2); 1 alpha = rho/<r0,v> (reduce dots);
 // 2 omega = <t,s>/|t|^2 (reduce dots); 3 end of iteration (vector dots |r|^2,
 // <r0,r>: convergence, restart test, beta); 4 restart done (reduce dots |r|^2).
+// One warp per (cluster, rhs): lanes stride over the item partials, a fixed
+// butterfly combines them (deterministic), lane 0 updates the scalars.
 template <int R>
 __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ st, int phase,
                          const double2* __restrict__ dots, double tol, int maxiter) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (id >= nsys * R) return;
     const int sidx = id / R, rr = id % R;
     KState& k = st[id];
@@ -652,12 +667,19 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
     const bool vec = (phase == 0 || phase == 3);
     const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
     double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
-    for (int it = b0; it < b1; it++) {
+    for (int it = b0 + lane; it < b1; it += 32) {
         const double2 a = dots[((long long)it * R + rr) * 2 + 0];
         const double2 c = dots[((long long)it * R + rr) * 2 + 1];
         d0.x += a.x; d0.y += a.y;
         d1.x += c.x; d1.y += c.y;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
+        d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
+        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
+        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
+    }
+    if (lane != 0) return;
     const double eps = 2.220446049250313e-16;
     if (phase == 0) {
         k.bsq = k.r0sq = k.rsq = d0.x;
@@ -739,14 +761,17 @@ __global__ void k_refine_axpy(const gb::SysDev* __restrict__ sys, const Item* __
 template <int R>
 __global__ void k_refine_check(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ ost,
                                const double2* __restrict__ dots, int pass, int max_refine) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (id >= nsys * R) return;
     const int sidx = id / R, rr = id % R;
     KState& k = ost[id];
     if (k.done) return;
     const SysPlan pl = plan[sidx];
     double s = 0;
-    for (int it = pl.rbeg; it < pl.rend; it++) s += dots[((long long)it * R + rr) * 2].x;
+    for (int it = pl.rbeg + lane; it < pl.rend; it += 32) s += dots[((long long)it * R + rr) * 2].x;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane != 0) return;
     k.rsq = s;
     k.iters = pass;
     if (!isfinite(s)) { k.done = 1; k.status = GB_NAN; return; }
@@ -758,12 +783,15 @@ __global__ void k_refine_check(const SysPlan* __restrict__ plan, int nsys, KStat
 template <int R>
 __global__ void k_outer_init(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ ost,
                              const double2* __restrict__ dots, double tol) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (id >= nsys * R) return;
     const int sidx = id / R, rr = id % R;
     const SysPlan pl = plan[sidx];
     double s = 0;
-    for (int it = pl.vbeg; it < pl.vend; it++) s += dots[((long long)it * R + rr) * 2].x;
+    for (int it = pl.vbeg + lane; it < pl.vend; it += 32) s += dots[((long long)it * R + rr) * 2].x;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane != 0) return;
     KState& k = ost[id];
     memset(&k, 0, sizeof(KState));
     k.bsq = s;
@@ -1019,14 +1047,16 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
     using YT = typename Pol::YT;
     using OutT = typename Pol::OutT;
     constexpr int nsmax = std::is_same<Pol, Pol64>::value ? 8 : (std::is_same<Pol, Pol32>::value ? 5 : 4);
+    constexpr int RU = std::is_same<Pol, Pol32>::value ? 4 : 2;
     const Shape sh = pick_shape((int)P.max_B, Pol::CPG, nsmax);
     const int Bmax = (int)P.max_B;
-    const size_t smem = (size_t)kGemvWarps * sh.rps * Bmax * RR * sizeof(OutT);
+    const size_t per_warp = (size_t)sh.rps * Bmax * RR * sizeof(OutT) + 2 * (size_t)Bmax * RR * sizeof(YT);
+    const size_t smem = (size_t)kGemvWarps * ((per_warp + 15) & ~size_t(15));
     const long long grid = std::max<long long>(1, std::min<long long>((P.nstrips * 32 + kGemvThreads - 1) / kGemvThreads,
                                                                       (long long)gb::sm_count() * 8));
 #define GB_PG(RPSV, NSV)                                                                                         \
     if (sh.rps == RPSV && sh.ns == NSV) {                                                                        \
-        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV>;                                                              \
+        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV, RU>;                                                              \
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
         gb::note_launch();                                                                                         \
@@ -1148,7 +1178,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
     double2* Tx = reinterpret_cast<double2*>(base + w.off_tx);
     const int nsr = P.nsys * R;
-    const unsigned sblocks = (unsigned)((nsr + 127) / 128);
+    const unsigned sblocks = (unsigned)((nsr * 32 + 127) / 128);
     const unsigned vb = (unsigned)P.nv;
 
     auto apply = [&](const VT* xin, VT* yout, int mode, const VT* aux, int mask, const double2* bb,
@@ -1349,7 +1379,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
     gb::note_launch();
     k_outer_start<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, b2, x2, dots);
     gb::note_launch();
-    k_outer_init<R><<<(nsr + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, tol);
+    k_outer_init<R><<<(nsr * 32 + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, tol);
     GB_CUDA_TRY(cudaGetLastError());
     GB_CUDA_TRY(cudaMemcpyAsync(r128, b2, sizeof(double2) * TV, cudaMemcpyDeviceToDevice, stream));
     for (int pass = 1; pass <= max_refine + 1; pass++) {
@@ -1370,7 +1400,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
                                          dots, stream);
         if (e) return e;
         gb::note_launch();
-        k_refine_check<R><<<(nsr + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, pass, max_refine);
+        k_refine_check<R><<<(nsr * 32 + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, pass, max_refine);
         GB_CUDA_TRY(cudaGetLastError());
         e = read_state(ost, nsr, h, stream);
         if (e) return e;
@@ -1473,6 +1503,59 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
     gb::note_launch();
     k_copy_out<float2><<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, yf, y2);
     GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                    const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
+                    size_t ws_bytes, int reps, int gemv_only, void* stream) {
+    if (nsys < 1 || !sys || !tvec || !x || !y || !workspace || reps < 1) return gb_set_error(GB_BAD_ARG, "bad argument");
+    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
+    if (!prec_ok(prec, mat128, mat64, mat64lo)) return gb_set_error(GB_BAD_ARG, "matrix missing for precision %d", prec);
+    if (prec == GB_PREC_MIXED_FP64RES) prec = GB_PREC_FP64;
+    cudaStream_t s = (cudaStream_t)stream;
+    Plan P;
+    int e = build_plan(nsys, sys, R, s, P);
+    if (e) return e;
+    WS w = ws_layout(P, prec, false);
+    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
+    unsigned char* base = static_cast<unsigned char*>(workspace);
+    DevPlan D;
+    e = upload_plan(P, base, w, s, D);
+    if (e) return e;
+    KState* st = reinterpret_cast<KState*>(base + w.off_state);
+    const double2* x2 = reinterpret_cast<const double2*>(x);
+    double2* y2 = reinterpret_cast<double2*>(y);
+    double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
+    const double2* t2 = reinterpret_cast<const double2*>(tvec);
+    const int pol = prec == GB_PREC_FP64 ? 0 : (prec == GB_PREC_MIXED ? 2 : 1);
+    const void* hi = pol == 0 ? (const void*)mat128 : (const void*)mat64;
+    const void* lo = pol == 2 ? (const void*)mat64lo : nullptr;
+    // the first product prepares the y vectors; gemv_only repeats the matrix pass alone
+    e = R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s)
+               : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s);
+    if (e) return e;
+    void* Yu = base + w.off_yu;
+    void* Yw = base + w.off_yw;
+    void* CU = base + w.off_cu;
+    void* CW = base + w.off_cw;
+    for (int k = 1; k < reps; k++) {
+        if (!gemv_only) {
+            e = R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s)
+                       : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s);
+        } else if (pol == 0) {
+            e = R == 1 ? launch_pgemv<Pol64, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s)
+                       : launch_pgemv<Pol64, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s);
+        } else if (pol == 1) {
+            e = R == 1 ? launch_pgemv<Pol32, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s)
+                       : launch_pgemv<Pol32, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s);
+        } else {
+            for (int rr = 0; rr < R && !e; rr++)
+                e = R == 1 ? launch_pgemv<PolDF, 1, 1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, s)
+                           : launch_pgemv<PolDF, 1, 2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, s);
+        }
+        if (e) return e;
+    }
     return GB_OK;
 }
 

@@ -172,6 +172,20 @@ class ClusterBatch:
                                    ws.numel(), current_stream(self.device)), "apply")
         return y
 
+    def apply_repeat(self, x, precision="fp32", reps=10, gemv_only=False):
+        """Launch the operator product reps times back to back (kernel timing)."""
+        L = nat.lib()
+        code = PRECISIONS[precision]
+        need = L.gb_apply_workspace_size(self.nsys, self.sys, self.R, code)
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        y = torch.empty_like(x)
+        nat.check(L.gb_apply_repeat(self.nsys, self.sys, self.R, code, nat.ptr(self.mat128), nat.ptr(self.mat64),
+                                    nat.ptr(self.mat64lo), nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y),
+                                    nat.ptr(self._ws), self._ws.numel(), int(reps), int(bool(gemv_only)),
+                                    current_stream(self.device)), "apply_repeat")
+        return y
+
     def epilogue(self, eps_b, source=True, want_fields=True):
         """p_scat, p_int (device, [total_vec]) and per particle xs [N,R,3,2lmax], force/torque [N,R,3]."""
         L = nat.lib()
