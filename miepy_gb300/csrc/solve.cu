@@ -216,11 +216,13 @@ template <> __device__ __forceinline__ float4 make_y<2>(double2 z) {
     return make_float4(hx, hy, __double2float_rn(z.x - (double)hx), __double2float_rn(z.y - (double)hy));
 }
 
+// Layout: [D][R] interleaved for YK 0/1; for YK 2 one plane per right-hand side,
+// element (rr, row) at rr*TR + vec_off/R + row (TR = rows of all clusters).
 template <int YK, typename VT, int R>
 __global__ void __launch_bounds__(kVRows)
 k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
         int mask_mode, const double2* __restrict__ tvec, const VT* __restrict__ x, typename YType<YK>::t* __restrict__ Yu,
-        typename YType<YK>::t* __restrict__ Yw) {
+        typename YType<YK>::t* __restrict__ Yw, long long TR) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
@@ -240,35 +242,76 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
         const double2 z = cmul(t, to_d2(x[S.vec_off + src * R + rr]));
         const double2 yu = make_double2(flipd(z.x, eneg), flipd(z.y, eneg));
         const double2 yw = make_double2(flipd(yu.x, sneg), flipd(yu.y, sneg));
-        Yu[S.vec_off + (long long)row * R + rr] = make_y<YK>(yu);
-        Yw[S.vec_off + (long long)row * R + rr] = make_y<YK>(yw);
+        const long long o = (YK == 2) ? rr * TR + S.vec_off / R + row : S.vec_off + (long long)row * R + rr;
+        Yu[o] = make_y<YK>(yu);
+        Yw[o] = make_y<YK>(yw);
     }
 }
 
 // --------------------------------------------------------------- K3a GEMV --
-// RR: right-hand sides handled per launch (all R for Pol64/Pol32, one for PolDF,
-// the one at rr0); RT: stride of the [D][RT] vectors and partials.  The y vectors
-// of the current block pair live in per-warp shared memory, so the inner loop
-// only waits on the matrix stream; RU row steps of matrix loads are in flight.
-template <class Pol, int RR, int RT, int RPS, int NS, int RU>
+// cp.async (16-byte, L1-bypassing) copies feed a per-warp ring of S stages in
+// shared memory; each stage holds the RPS rows one step consumes.  Every lane
+// copies exactly the 16-byte pieces it later reads (its slots), so a lane only
+// waits on its own copy groups (cp.async.wait_group) and no cross-lane barrier
+// sits in the inner loop.  The y vector of the next block is fetched the same
+// way, a few steps ahead, into a small ring (visibility across lanes through
+// __syncwarp at the block boundary).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <class Pol> struct MatBytes { static constexpr int v = 16 / Pol::CPG; };
+template <class Pol> struct IsDF { static constexpr bool v = false; };
+template <> struct IsDF<PolDF> { static constexpr bool v = true; };
+
+constexpr int kYRing = 4;   // y-vector buffers per warp (next blocks prefetched)
+
+struct GemvLayout {
+    int stage_bytes, comb_bytes, y_bytes, warp_bytes;
+};
+__host__ __device__ inline GemvLayout gemv_layout(int Bmax, int RPS, int RR, int S, int mat_bytes, bool df,
+                                                  int out_bytes, int y_bytes) {
+    GemvLayout g;
+    g.stage_bytes = RPS * Bmax * mat_bytes * (df ? 2 : 1);
+    g.comb_bytes = RPS * Bmax * RR * out_bytes;
+    g.y_bytes = Bmax * RR * y_bytes;
+    g.warp_bytes = ((g.comb_bytes + 15) & ~15) + (kYRing + 1) * ((g.y_bytes + 15) & ~15) + S * g.stage_bytes;
+    g.warp_bytes = (g.warp_bytes + 127) & ~127;
+    return g;
+}
+
+// RR: right-hand sides per launch (all R for Pol64/Pol32; one, rr0, for PolDF);
+// RT: stride of the [D][RT] partials.  Y vectors: [D][RT] (Pol64/Pol32) or one
+// contiguous [rows] plane per right-hand side (PolDF, plane rr0 at Yu + rr0*TR).
+template <class Pol, int RR, int RT, int RPS, int NS, int S>
 __global__ void __launch_bounds__(kGemvThreads)
 k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long nstrips,
         const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
         const typename Pol::YT* __restrict__ Yu, const typename Pol::YT* __restrict__ Yw,
         typename Pol::OutT* __restrict__ CU, typename Pol::OutT* __restrict__ CW, const SysPlan* __restrict__ plan,
-        int rr0, int Bmax) {
+        int rr0, int Bmax, long long TR) {
     using Acc = typename Pol::Acc;
     using OutT = typename Pol::OutT;
     using YT = typename Pol::YT;
     constexpr int CPG = Pol::CPG;
-    extern __shared__ __align__(16) unsigned char gemv_smem[];
+    constexpr int MB = MatBytes<Pol>::v;
+    constexpr bool DF = IsDF<Pol>::v;
+    extern __shared__ __align__(128) unsigned char gemv_smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    // per warp: comb [RPS][Bmax][RR] OutT, then yu [Bmax][RR] YT, yw [Bmax][RR] YT
-    const size_t per_warp = (size_t)RPS * Bmax * RR * sizeof(OutT) + 2 * (size_t)Bmax * RR * sizeof(YT);
-    unsigned char* wbase = gemv_smem + (size_t)wid * ((per_warp + 15) & ~size_t(15));
+    const GemvLayout lay = gemv_layout(Bmax, RPS, RR, S, MB, DF, sizeof(OutT), sizeof(YT));
+    unsigned char* wbase = gemv_smem + (size_t)wid * lay.warp_bytes;
     OutT* comb = reinterpret_cast<OutT*>(wbase);
-    YT* syu = reinterpret_cast<YT*>(wbase + (size_t)RPS * Bmax * RR * sizeof(OutT));
-    YT* syw = syu + (size_t)Bmax * RR;
+    unsigned char* ybase = wbase + ((lay.comb_bytes + 15) & ~15);
+    const int ystride = (lay.y_bytes + 15) & ~15;
+    YT* syw = reinterpret_cast<YT*>(ybase + kYRing * ystride);
+    unsigned char* ring = ybase + (kYRing + 1) * ystride;
+    const unsigned char* mh = reinterpret_cast<const unsigned char*>(mat_hi);
+    const unsigned char* ml = reinterpret_cast<const unsigned char*>(mat_lo);
     const long long warp = ((long long)blockIdx.x * kGemvThreads + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     for (long long w = warp; w < nstrips; w += nwarps) {
@@ -277,10 +320,12 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
 #pragma unroll
         for (int q = 0; q < RR; q++) act |= active_rhs<RT>(st, sp.sys, rr0 + q, mask_mode);
         if (!act) continue;
-        const gb::SysDev S = sys[sp.sys];
+        const gb::SysDev S_ = sys[sp.sys];
         const SysPlan pl = plan[sp.sys];
-        const int B = S.B;
+        const int B = S_.B;
         const int ncg = B / CPG;
+        const int spb = (B + RPS - 1) / RPS;           // steps per block
+        const int total = sp.nb * spb;
         int sro[NS], sg[NS];
         bool sval[NS];
 #pragma unroll
@@ -290,89 +335,128 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             sro[k] = sval[k] ? f / ncg : 0;
             sg[k] = sval[k] ? f % ncg : 0;
         }
-        Acc cu[NS][CPG][RR];
+        const int yrow_bytes = RR * (int)sizeof(YT);
+        auto ysrc = [&](int part) -> const YT* {
+            if (DF) return Yu + (long long)rr0 * TR + S_.vec_off / RT + (long long)part * B;
+            return Yu + S_.vec_off + (long long)part * B * RT;
+        };
+        // step t: copy this lane's pieces of rows (t % spb)*RPS + sro of block t / spb,
+        // and at the first step of a block the block's y vector
+        auto issue = [&](int t) {
+            const int b = t / spb, r0 = (t % spb) * RPS;
+            const long long p = sp.p0 + b;
+            const long long blk = S_.mat_off + p * (long long)B * B;
+            unsigned char* stg = ring + (size_t)(t % S) * lay.stage_bytes;
+#pragma unroll
+            for (int k = 0; k < NS; k++) {
+                const int row = r0 + sro[k];
+                if (sval[k] && row < B) {
+                    const long long eidx = blk + (long long)row * B + sg[k] * CPG;
+                    const size_t soff = ((size_t)sro[k] * B + sg[k] * CPG) * MB;
+                    cp_async16(stg + soff, mh + eidx * MB);
+                    if (DF) cp_async16(stg + (size_t)RPS * Bmax * MB + soff, ml + eidx * MB);
+                }
+            }
+            if (r0 == 0) {
+                const int j = sp.i + 1 + (int)(p - pair_start(sp.i, S_.N));
+                const unsigned char* src = reinterpret_cast<const unsigned char*>(ysrc(j));
+                unsigned char* dst = ybase + (size_t)(b % kYRing) * ystride;
+                for (int e = lane * 16; e < B * yrow_bytes; e += 32 * 16) cp_async16(dst + e, src + e);
+            }
+            cp_async_commit();
+        };
+        {   // y_w of particle i: the same for every block of the strip
+            const YT* src = DF ? Yw + (long long)rr0 * TR + S_.vec_off / RT + (long long)sp.i * B
+                               : Yw + S_.vec_off + (long long)sp.i * B * RT;
+            for (int e = lane; e < B * RR; e += 32) syw[e] = src[e];
+        }
+        Acc cu[NS][CPG][RR], cw[NS][CPG][RR];
 #pragma unroll
         for (int k = 0; k < NS; k++)
 #pragma unroll
             for (int c = 0; c < CPG; c++)
 #pragma unroll
                 for (int q = 0; q < RR; q++) Pol::zero(cu[k][c][q]);
-        {   // y_w of particle i: the same for every block of the strip
-            const YT* src = Yw + S.vec_off + (long long)sp.i * B * RT;
-            for (int e = lane; e < B * RR; e += 32) syw[e] = src[(e / RR) * RT + rr0 + (e % RR)];
+#pragma unroll
+        for (int t = 0; t < S - 1; t++) {
+            if (t < total) issue(t);
+            else cp_async_commit();
         }
-        for (int b = 0; b < sp.nb; b++) {
-            const long long p = sp.p0 + b;
-            const int j = sp.i + 1 + (int)(p - pair_start(sp.i, S.N));
-            {
-                const YT* src = Yu + S.vec_off + (long long)j * B * RT;
-                for (int e = lane; e < B * RR; e += 32) syu[e] = src[(e / RR) * RT + rr0 + (e % RR)];
-            }
-            __syncwarp();
-            const long long blk = S.mat_off + p * (long long)B * B;
-            Acc cw[NS][CPG][RR];
+        for (int t = 0; t < total; t++) {
+            if (t + S - 1 < total) issue(t + S - 1);
+            else cp_async_commit();
+            cp_async_wait<S - 1>();
+            const int b = t / spb, rs = t % spb;
+            if (rs == 0) {
+                __syncwarp();   // this block's y copies of all lanes have landed
 #pragma unroll
-            for (int k = 0; k < NS; k++)
-#pragma unroll
-                for (int c = 0; c < CPG; c++)
-#pragma unroll
-                    for (int q = 0; q < RR; q++) Pol::zero(cw[k][c][q]);
-            for (int r = 0; r < B; r += RPS * RU) {
-                typename Pol::Mat m[RU][NS][CPG];
-#pragma unroll
-                for (int u = 0; u < RU; u++)
-#pragma unroll
-                    for (int k = 0; k < NS; k++) {
-                        const int row = r + u * RPS + sro[k];
-                        if (sval[k] && row < B) {
-                            Load<Pol>::get(mat_hi, mat_lo, blk + (long long)row * B + sg[k] * CPG, m[u][k]);
-                        } else {
-#pragma unroll
-                            for (int c = 0; c < CPG; c++) m[u][k][c] = typename Pol::Mat{};
-                        }
-                    }
-#pragma unroll
-                for (int u = 0; u < RU; u++)
-#pragma unroll
-                    for (int k = 0; k < NS; k++) {
-                        const int row = min(r + u * RPS + sro[k], B - 1);   // padded rows carry zero matrix entries
-                        YT yu[RR], yw[RR];
-#pragma unroll
-                        for (int q = 0; q < RR; q++) {
-                            yu[q] = syu[row * RR + q];
-                            yw[q] = syw[row * RR + q];
-                        }
-#pragma unroll
-                        for (int c = 0; c < CPG; c++)
-#pragma unroll
-                            for (int q = 0; q < RR; q++) {
-                                Pol::fma(cu[k][c][q], m[u][k][c], yu[q]);
-                                Pol::fma(cw[k][c][q], m[u][k][c], yw[q]);
-                            }
-                    }
-            }
-            // column partial of this block for block row j: slots of one column summed in a fixed order
-#pragma unroll
-            for (int k = 0; k < NS; k++)
-                if (sval[k])
+                for (int k = 0; k < NS; k++)
 #pragma unroll
                     for (int c = 0; c < CPG; c++)
 #pragma unroll
-                        for (int q = 0; q < RR; q++)
-                            comb[((size_t)sro[k] * B + sg[k] * CPG + c) * RR + q] = Pol::out(cw[k][c][q]);
-            __syncwarp();
-            OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
-            for (int e = lane; e < B * RR; e += 32) {
-                OutT s = comb[e];
-                for (int ro = 1; ro < RPS; ro++) {
-                    const OutT v = comb[(size_t)ro * B * RR + e];
-                    s.x += v.x;
-                    s.y += v.y;
-                }
-                cwp[(e / RR) * RT + rr0 + (e % RR)] = s;
+                        for (int q = 0; q < RR; q++) Pol::zero(cw[k][c][q]);
             }
-            __syncwarp();
+            const YT* syu = reinterpret_cast<const YT*>(ybase + (size_t)(b % kYRing) * ystride);
+            const unsigned char* stg = ring + (size_t)(t % S) * lay.stage_bytes;
+#pragma unroll
+            for (int k = 0; k < NS; k++) {
+                const int row = rs * RPS + sro[k];
+                if (!(sval[k] && row < B)) continue;
+                const size_t soff = ((size_t)sro[k] * B + sg[k] * CPG) * MB;
+                typename Pol::Mat m[CPG];
+                if constexpr (DF) {
+                    const float4 qh = *reinterpret_cast<const float4*>(stg + soff);
+                    const float4 ql = *reinterpret_cast<const float4*>(stg + (size_t)RPS * Bmax * MB + soff);
+                    m[0].h = make_float2(qh.x, qh.y);
+                    m[1].h = make_float2(qh.z, qh.w);
+                    m[0].l = make_float2(ql.x, ql.y);
+                    m[1].l = make_float2(ql.z, ql.w);
+                } else if constexpr (CPG == 2) {
+                    const float4 qh = *reinterpret_cast<const float4*>(stg + soff);
+                    m[0] = typename Pol::Mat{qh.x, qh.y};
+                    m[1] = typename Pol::Mat{qh.z, qh.w};
+                } else {
+                    m[0] = *reinterpret_cast<const typename Pol::Mat*>(stg + soff);
+                }
+                YT yu[RR], yw[RR];
+#pragma unroll
+                for (int q = 0; q < RR; q++) {
+                    yu[q] = syu[row * RR + q];
+                    yw[q] = syw[row * RR + q];
+                }
+#pragma unroll
+                for (int c = 0; c < CPG; c++)
+#pragma unroll
+                    for (int q = 0; q < RR; q++) {
+                        Pol::fma(cu[k][c][q], m[c], yu[q]);
+                        Pol::fma(cw[k][c][q], m[c], yw[q]);
+                    }
+            }
+            if (rs == spb - 1) {   // block done: column partial for block row j, slots combined in a fixed order
+                const long long p = sp.p0 + b;
+#pragma unroll
+                for (int k = 0; k < NS; k++)
+                    if (sval[k])
+#pragma unroll
+                        for (int c = 0; c < CPG; c++)
+#pragma unroll
+                            for (int q = 0; q < RR; q++)
+                                comb[((size_t)sro[k] * B + sg[k] * CPG + c) * RR + q] = Pol::out(cw[k][c][q]);
+                __syncwarp();
+                OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
+                for (int e = lane; e < B * RR; e += 32) {
+                    OutT sm = comb[e];
+                    for (int ro = 1; ro < RPS; ro++) {
+                        const OutT v = comb[(size_t)ro * B * RR + e];
+                        sm.x += v.x;
+                        sm.y += v.y;
+                    }
+                    cwp[(e / RR) * RT + rr0 + (e % RR)] = sm;
+                }
+                __syncwarp();
+            }
         }
+        cp_async_wait<0>();
 #pragma unroll
         for (int k = 0; k < NS; k++)
             if (sval[k])
@@ -384,13 +468,13 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
         __syncwarp();
         OutT* cup = CU + pl.cu_off + (w - pl.strip_base) * (long long)B * RT;
         for (int e = lane; e < B * RR; e += 32) {
-            OutT s = comb[e];
+            OutT sm = comb[e];
             for (int ro = 1; ro < RPS; ro++) {
                 const OutT v = comb[(size_t)ro * B * RR + e];
-                s.x += v.x;
-                s.y += v.y;
+                sm.x += v.x;
+                sm.y += v.y;
             }
-            cup[(e / RR) * RT + rr0 + (e % RR)] = s;
+            cup[(e / RR) * RT + rr0 + (e % RR)] = sm;
         }
         __syncwarp();
     }
@@ -1046,28 +1130,43 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
                  const void* Yu, const void* Yw, void* CU, void* CW, int rr0, cudaStream_t stream) {
     using YT = typename Pol::YT;
     using OutT = typename Pol::OutT;
-    constexpr int nsmax = std::is_same<Pol, Pol64>::value ? 8 : (std::is_same<Pol, Pol32>::value ? 5 : 4);
-    constexpr int RU = std::is_same<Pol, Pol32>::value ? 4 : 2;
+    constexpr int nsmax = std::is_same<Pol, Pol64>::value ? 8 : 5;
+    constexpr bool DF = IsDF<Pol>::v;
     const Shape sh = pick_shape((int)P.max_B, Pol::CPG, nsmax);
     const int Bmax = (int)P.max_B;
-    const size_t per_warp = (size_t)sh.rps * Bmax * RR * sizeof(OutT) + 2 * (size_t)Bmax * RR * sizeof(YT);
-    const size_t smem = (size_t)kGemvWarps * ((per_warp + 15) & ~size_t(15));
+    // stages: up to 6, per-warp shared memory about 24 KB, and no more lookahead than
+    // the y ring covers (S - 1 <= kYRing - 1 block boundaries ahead is guaranteed
+    // when S - 1 <= (kYRing - 2) * steps-per-block)
+    int minB = (int)P.max_B;
+    for (const auto& d : P.sd) minB = std::min(minB, d.B);
+    const int spb_min = std::max(1, (minB + sh.rps - 1) / sh.rps);
+    int Sst = 6;   // stage counts 6, 4 or 2
+    while (Sst > 2) {
+        const GemvLayout g = gemv_layout(Bmax, sh.rps, RR, Sst, MatBytes<Pol>::v, DF, sizeof(OutT), sizeof(YT));
+        if (g.warp_bytes <= 26 * 1024 && Sst - 1 <= (kYRing - 2) * spb_min) break;
+        Sst -= 2;
+    }
+    const GemvLayout g = gemv_layout(Bmax, sh.rps, RR, Sst, MatBytes<Pol>::v, DF, sizeof(OutT), sizeof(YT));
+    const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
+    if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
+    const long long TR = P.total_vec / P.R;
     const long long grid = std::max<long long>(1, std::min<long long>((P.nstrips * 32 + kGemvThreads - 1) / kGemvThreads,
                                                                       (long long)gb::sm_count() * 8));
-#define GB_PG(RPSV, NSV)                                                                                         \
-    if (sh.rps == RPSV && sh.ns == NSV) {                                                                        \
-        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV, RU>;                                                              \
+#define GB_PG_S(RPSV, NSV, SV)                                                                                   \
+    if (sh.rps == RPSV && sh.ns == NSV && Sst == SV) {                                                           \
+        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV, SV>;                                                          \
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
-        gb::note_launch();                                                                                         \
+        gb::note_launch();                                                                                       \
         kfn<<<(unsigned)grid, kGemvThreads, smem, stream>>>(D.sys, D.strips, P.nstrips, st, mask, mat_hi, mat_lo,  \
                                                             reinterpret_cast<const YT*>(Yu),                     \
                                                             reinterpret_cast<const YT*>(Yw),                     \
                                                             reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), \
-                                                            D.sp, rr0, Bmax);                                   \
+                                                            D.sp, rr0, Bmax, TR);                               \
         GB_CUDA_TRY(cudaGetLastError());                                                                         \
         return GB_OK;                                                                                            \
     }
+#define GB_PG(RPSV, NSV) GB_PG_S(RPSV, NSV, 6) GB_PG_S(RPSV, NSV, 4) GB_PG_S(RPSV, NSV, 2)
     if constexpr (std::is_same<Pol, Pol64>::value) {
         GB_PG(4, 1) GB_PG(2, 1) GB_PG(1, 1) GB_PG(2, 3) GB_PG(2, 5) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 5) GB_PG(1, 7)
         GB_PG(1, 8) GB_PG(1, 2) GB_PG(1, 6)
@@ -1075,10 +1174,13 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
         GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(4, 5) GB_PG(2, 3) GB_PG(1, 2) GB_PG(2, 5) GB_PG(1, 4) GB_PG(1, 1)
         GB_PG(1, 3) GB_PG(1, 5)
     } else {
-        GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(2, 3) GB_PG(1, 2) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 1)
+        GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(2, 3) GB_PG(1, 2) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 1) GB_PG(4, 5)
+        GB_PG(2, 5) GB_PG(1, 5)
     }
 #undef GB_PG
-    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d (rps %d, ns %d)", Bmax, sh.rps, sh.ns);
+#undef GB_PG_S
+    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d (rps %d, ns %d, stages %d)", Bmax, sh.rps,
+                        sh.ns, Sst);
 }
 
 // One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
@@ -1096,7 +1198,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     if (pol == 0) {
         gb::note_launch();
         k_yprep<0, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw));
+                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), 0);
         if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, stream);
         if (e) return e;
         gb::note_launch();
@@ -1106,7 +1208,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     } else if (pol == 1) {
         gb::note_launch();
         k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw));
+                                                     reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw), 0);
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, stream);
         if (e) return e;
         gb::note_launch();
@@ -1116,7 +1218,8 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     } else {
         gb::note_launch();
         k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
+                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw),
+                                                     P.total_vec / R);
         for (int rr = 0; rr < R && P.nstrips; rr++) {
             e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, rr, stream);
             if (e) return e;
