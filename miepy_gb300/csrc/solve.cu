@@ -173,30 +173,6 @@ struct PolDF {
     }
 };
 
-template <class Pol> struct Load;
-template <> struct Load<Pol64> {
-    __device__ static void get(const void* hi, const void*, long long idx, Pol64::Mat* m) {
-        m[0] = __ldg(reinterpret_cast<const double2*>(hi) + idx);
-    }
-};
-template <> struct Load<Pol32> {
-    __device__ static void get(const void* hi, const void*, long long idx, Pol32::Mat* m) {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(hi) + idx));
-        m[0] = make_float2(q.x, q.y);
-        m[1] = make_float2(q.z, q.w);
-    }
-};
-template <> struct Load<PolDF> {
-    __device__ static void get(const void* hi, const void* lo, long long idx, PolDF::Mat* m) {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(hi) + idx));
-        const float4 r = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(lo) + idx));
-        m[0].h = make_float2(q.x, q.y);
-        m[1].h = make_float2(q.z, q.w);
-        m[0].l = make_float2(r.x, r.y);
-        m[1].l = make_float2(r.z, r.w);
-    }
-};
-
 // ------------------------------------------------------------ y vectors --
 // For every row (particle k, local row r) of every cluster:
 //   z = eps(r) t_k[rho(r)] x_k[rho(r)],   Yu = z,  Yw = sig(r) z
@@ -249,38 +225,60 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
 }
 
 // --------------------------------------------------------------- K3a GEMV --
-// cp.async (16-byte, L1-bypassing) copies feed a per-warp ring of S stages in
-// shared memory; each stage holds the RPS rows one step consumes.  Every lane
-// copies exactly the 16-byte pieces it later reads (its slots), so a lane only
-// waits on its own copy groups (cp.async.wait_group) and no cross-lane barrier
-// sits in the inner loop.  The y vector of the next block is fetched the same
-// way, a few steps ahead, into a small ring (visibility across lanes through
-// __syncwarp at the block boundary).
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+// The matrix stream is moved by TMA bulk copies (cp.async.bulk, 1-D): a strip of
+// blocks is contiguous in memory, so lane 0 of a warp copies whole chunks of rows
+// (and, with the first chunk of each block, the block's y vector) into a ring of S
+// shared-memory stages, each completed through its own mbarrier.  The other lanes
+// only wait on the mbarrier and read their slots from shared memory.  Every wait is
+// bounded in time; a wait that expires sets the error flag and the warp stops.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_1d(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: about 0.2 s of clock at most
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > 400000000LL) return false;
+    return true;
 }
 
 template <class Pol> struct MatBytes { static constexpr int v = 16 / Pol::CPG; };
 template <class Pol> struct IsDF { static constexpr bool v = false; };
 template <> struct IsDF<PolDF> { static constexpr bool v = true; };
 
-constexpr int kYRing = 4;   // y-vector buffers per warp (next blocks prefetched)
+constexpr int kYRing = 4;   // y-vector buffers per warp
 
 struct GemvLayout {
-    int stage_bytes, comb_bytes, y_bytes, warp_bytes;
+    int chunk_cap, comb_bytes, y_bytes, warp_bytes;
 };
-__host__ __device__ inline GemvLayout gemv_layout(int Bmax, int RPS, int RR, int S, int mat_bytes, bool df,
+// per warp: S mbarriers | comb [RPS][Bmax][RR] OutT | syw | y ring [kYRing] | S stages
+__host__ __device__ inline GemvLayout gemv_layout(int Bmax, int RPS, int G, int RR, int S, int mat_bytes, bool df,
                                                   int out_bytes, int y_bytes) {
     GemvLayout g;
-    g.stage_bytes = RPS * Bmax * mat_bytes * (df ? 2 : 1);
-    g.comb_bytes = RPS * Bmax * RR * out_bytes;
-    g.y_bytes = Bmax * RR * y_bytes;
-    g.warp_bytes = ((g.comb_bytes + 15) & ~15) + (kYRing + 1) * ((g.y_bytes + 15) & ~15) + S * g.stage_bytes;
+    g.chunk_cap = G * RPS * Bmax * mat_bytes;               // bytes of one matrix chunk (hi; lo follows for DF)
+    g.comb_bytes = (RPS * Bmax * RR * out_bytes + 127) & ~127;
+    g.y_bytes = (Bmax * RR * y_bytes + 127) & ~127;
+    g.warp_bytes = 128 + g.comb_bytes + (kYRing + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1);
     g.warp_bytes = (g.warp_bytes + 127) & ~127;
     return g;
 }
@@ -294,7 +292,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
         const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
         const typename Pol::YT* __restrict__ Yu, const typename Pol::YT* __restrict__ Yw,
         typename Pol::OutT* __restrict__ CU, typename Pol::OutT* __restrict__ CW, const SysPlan* __restrict__ plan,
-        int rr0, int Bmax, long long TR) {
+        int rr0, int Bmax, int G, long long TR, int* __restrict__ err) {
     using Acc = typename Pol::Acc;
     using OutT = typename Pol::OutT;
     using YT = typename Pol::YT;
@@ -303,71 +301,77 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     constexpr bool DF = IsDF<Pol>::v;
     extern __shared__ __align__(128) unsigned char gemv_smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const GemvLayout lay = gemv_layout(Bmax, RPS, RR, S, MB, DF, sizeof(OutT), sizeof(YT));
+    const GemvLayout lay = gemv_layout(Bmax, RPS, G, RR, S, MB, DF, sizeof(OutT), sizeof(YT));
     unsigned char* wbase = gemv_smem + (size_t)wid * lay.warp_bytes;
-    OutT* comb = reinterpret_cast<OutT*>(wbase);
-    unsigned char* ybase = wbase + ((lay.comb_bytes + 15) & ~15);
-    const int ystride = (lay.y_bytes + 15) & ~15;
-    YT* syw = reinterpret_cast<YT*>(ybase + kYRing * ystride);
-    unsigned char* ring = ybase + (kYRing + 1) * ystride;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(wbase);
+    OutT* comb = reinterpret_cast<OutT*>(wbase + 128);
+    unsigned char* yring = wbase + 128 + lay.comb_bytes;
+    YT* syw = reinterpret_cast<YT*>(yring + kYRing * lay.y_bytes);
+    unsigned char* stages = yring + (kYRing + 1) * lay.y_bytes;
+    const unsigned stage_stride = lay.chunk_cap * (DF ? 2 : 1);
     const unsigned char* mh = reinterpret_cast<const unsigned char*>(mat_hi);
     const unsigned char* ml = reinterpret_cast<const unsigned char*>(mat_lo);
+    if (lane == 0)
+        for (int k = 0; k < S; k++) mbar_init(bars + k, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    __syncwarp();
+    unsigned long long gchunk = 0;   // chunks consumed by this warp (stage = % S, parity = / S)
     const long long warp = ((long long)blockIdx.x * kGemvThreads + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
-    for (long long w = warp; w < nstrips; w += nwarps) {
+    bool failed = false;
+    unsigned long long fail_lo = 0, fail_hi = 0;   // chunks possibly in flight when a wait expired
+    for (long long w = warp; w < nstrips && !failed; w += nwarps) {
         const Strip sp = strips[w];
         bool act = false;
 #pragma unroll
         for (int q = 0; q < RR; q++) act |= active_rhs<RT>(st, sp.sys, rr0 + q, mask_mode);
         if (!act) continue;
-        const gb::SysDev S_ = sys[sp.sys];
-        const SysPlan pl = plan[sp.sys];
-        const int B = S_.B;
+        const gb::SysDev& S_ = sys[sp.sys];
+        const int B = S_.B, N = S_.N;
+        const long long mat_off = S_.mat_off, vec_off = S_.vec_off;
+        const SysPlan& pl = plan[sp.sys];
         const int ncg = B / CPG;
         const int spb = (B + RPS - 1) / RPS;           // steps per block
-        const int total = sp.nb * spb;
-        int sro[NS], sg[NS];
+        const int cpb = (spb + G - 1) / G;             // chunks per block
+        const int total = sp.nb * cpb;
+        int soff[NS], sro[NS];
         bool sval[NS];
 #pragma unroll
         for (int k = 0; k < NS; k++) {
             const int f = lane + 32 * k;
             sval[k] = f < RPS * ncg;
             sro[k] = sval[k] ? f / ncg : 0;
-            sg[k] = sval[k] ? f % ncg : 0;
+            soff[k] = sval[k] ? (sro[k] * B + (f % ncg) * CPG) * MB : 0;
         }
-        const int yrow_bytes = RR * (int)sizeof(YT);
+        const unsigned ybytes = (unsigned)(B * RR * sizeof(YT));
         auto ysrc = [&](int part) -> const YT* {
-            if (DF) return Yu + (long long)rr0 * TR + S_.vec_off / RT + (long long)part * B;
-            return Yu + S_.vec_off + (long long)part * B * RT;
+            if (DF) return Yu + (long long)rr0 * TR + vec_off / RT + (long long)part * B;
+            return Yu + vec_off + (long long)part * B * RT;
         };
-        // step t: copy this lane's pieces of rows (t % spb)*RPS + sro of block t / spb,
-        // and at the first step of a block the block's y vector
+        // chunk t of the strip: rows [c*G*RPS, ...) of block b (contiguous), plus the
+        // block's y vector with its first chunk; issued by lane 0
         auto issue = [&](int t) {
-            const int b = t / spb, r0 = (t % spb) * RPS;
+            const int b = t / cpb, c = t % cpb;
             const long long p = sp.p0 + b;
-            const long long blk = S_.mat_off + p * (long long)B * B;
-            unsigned char* stg = ring + (size_t)(t % S) * lay.stage_bytes;
-#pragma unroll
-            for (int k = 0; k < NS; k++) {
-                const int row = r0 + sro[k];
-                if (sval[k] && row < B) {
-                    const long long eidx = blk + (long long)row * B + sg[k] * CPG;
-                    const size_t soff = ((size_t)sro[k] * B + sg[k] * CPG) * MB;
-                    cp_async16(stg + soff, mh + eidx * MB);
-                    if (DF) cp_async16(stg + (size_t)RPS * Bmax * MB + soff, ml + eidx * MB);
-                }
+            const int r0 = c * G * RPS;
+            const int nrows = min(G * RPS, B - r0);
+            const unsigned bytes = (unsigned)(nrows * B * MB);
+            const unsigned long long gc = gchunk + (unsigned long long)t;
+            uint64_t* bar = bars + (gc % S);
+            unsigned char* dst = stages + (size_t)(gc % S) * stage_stride;
+            const long long src = (mat_off + p * (long long)B * B + (long long)r0 * B) * MB;
+            unsigned tx = bytes * (DF ? 2u : 1u) + (c == 0 ? ybytes : 0u);
+            mbar_expect_tx(bar, tx);
+            tma_1d(dst, mh + src, bytes, bar);
+            if (DF) tma_1d(dst + lay.chunk_cap, ml + src, bytes, bar);
+            if (c == 0) {
+                const int j = sp.i + 1 + (int)(p - pair_start(sp.i, N));
+                tma_1d(yring + (size_t)(b % kYRing) * lay.y_bytes, ysrc(j), ybytes, bar);
             }
-            if (r0 == 0) {
-                const int j = sp.i + 1 + (int)(p - pair_start(sp.i, S_.N));
-                const unsigned char* src = reinterpret_cast<const unsigned char*>(ysrc(j));
-                unsigned char* dst = ybase + (size_t)(b % kYRing) * ystride;
-                for (int e = lane * 16; e < B * yrow_bytes; e += 32 * 16) cp_async16(dst + e, src + e);
-            }
-            cp_async_commit();
         };
         {   // y_w of particle i: the same for every block of the strip
-            const YT* src = DF ? Yw + (long long)rr0 * TR + S_.vec_off / RT + (long long)sp.i * B
-                               : Yw + S_.vec_off + (long long)sp.i * B * RT;
+            const YT* src = DF ? Yw + (long long)rr0 * TR + vec_off / RT + (long long)sp.i * B
+                               : Yw + vec_off + (long long)sp.i * B * RT;
             for (int e = lane; e < B * RR; e += 32) syw[e] = src[e];
         }
         Acc cu[NS][CPG][RR], cw[NS][CPG][RR];
@@ -377,71 +381,86 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             for (int c = 0; c < CPG; c++)
 #pragma unroll
                 for (int q = 0; q < RR; q++) Pol::zero(cu[k][c][q]);
-#pragma unroll
-        for (int t = 0; t < S - 1; t++) {
-            if (t < total) issue(t);
-            else cp_async_commit();
+        // every lane has finished reading the stages it may overwrite (previous strip)
+        __syncwarp();
+        if (lane == 0) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            for (int t = 0; t < S - 1 && t < total; t++) issue(t);
         }
         for (int t = 0; t < total; t++) {
-            if (t + S - 1 < total) issue(t + S - 1);
-            else cp_async_commit();
-            cp_async_wait<S - 1>();
-            const int b = t / spb, rs = t % spb;
-            if (rs == 0) {
-                __syncwarp();   // this block's y copies of all lanes have landed
+            const unsigned long long gc = gchunk + (unsigned long long)t;
+            const bool ok = mbar_wait_bounded(bars + (gc % S), (unsigned)((gc / S) & 1));
+            if (!__all_sync(0xffffffffu, ok)) {   // warp-uniform decision
+                if (lane == 0) atomicExch(err, 1);
+                failed = true;
+                fail_lo = gc;
+                fail_hi = gchunk + (unsigned long long)min(t + S - 1, total);
+                break;
+            }
+            const int b = t / cpb, c = t % cpb;
+            if (c == 0) {
 #pragma unroll
                 for (int k = 0; k < NS; k++)
 #pragma unroll
-                    for (int c = 0; c < CPG; c++)
+                    for (int cc = 0; cc < CPG; cc++)
 #pragma unroll
-                        for (int q = 0; q < RR; q++) Pol::zero(cw[k][c][q]);
+                        for (int q = 0; q < RR; q++) Pol::zero(cw[k][cc][q]);
             }
-            const YT* syu = reinterpret_cast<const YT*>(ybase + (size_t)(b % kYRing) * ystride);
-            const unsigned char* stg = ring + (size_t)(t % S) * lay.stage_bytes;
+            const YT* syu = reinterpret_cast<const YT*>(yring + (size_t)(b % kYRing) * lay.y_bytes);
+            const unsigned char* stg = stages + (size_t)(gc % S) * stage_stride;
+            const int r0 = c * G * RPS;
+            const int nsteps = min(G, spb - c * G);
+            for (int g = 0; g < nsteps; g++) {
 #pragma unroll
-            for (int k = 0; k < NS; k++) {
-                const int row = rs * RPS + sro[k];
-                if (!(sval[k] && row < B)) continue;
-                const size_t soff = ((size_t)sro[k] * B + sg[k] * CPG) * MB;
-                typename Pol::Mat m[CPG];
-                if constexpr (DF) {
-                    const float4 qh = *reinterpret_cast<const float4*>(stg + soff);
-                    const float4 ql = *reinterpret_cast<const float4*>(stg + (size_t)RPS * Bmax * MB + soff);
-                    m[0].h = make_float2(qh.x, qh.y);
-                    m[1].h = make_float2(qh.z, qh.w);
-                    m[0].l = make_float2(ql.x, ql.y);
-                    m[1].l = make_float2(ql.z, ql.w);
-                } else if constexpr (CPG == 2) {
-                    const float4 qh = *reinterpret_cast<const float4*>(stg + soff);
-                    m[0] = typename Pol::Mat{qh.x, qh.y};
-                    m[1] = typename Pol::Mat{qh.z, qh.w};
-                } else {
-                    m[0] = *reinterpret_cast<const typename Pol::Mat*>(stg + soff);
-                }
-                YT yu[RR], yw[RR];
-#pragma unroll
-                for (int q = 0; q < RR; q++) {
-                    yu[q] = syu[row * RR + q];
-                    yw[q] = syw[row * RR + q];
-                }
-#pragma unroll
-                for (int c = 0; c < CPG; c++)
+                for (int k = 0; k < NS; k++) {
+                    const int row = r0 + g * RPS + sro[k];
+                    if (!(sval[k] && row < B)) continue;
+                    const size_t so = (size_t)g * RPS * B * MB + soff[k];
+                    typename Pol::Mat m[CPG];
+                    if constexpr (DF) {
+                        const float4 qh = *reinterpret_cast<const float4*>(stg + so);
+                        const float4 ql = *reinterpret_cast<const float4*>(stg + lay.chunk_cap + so);
+                        m[0].h = make_float2(qh.x, qh.y);
+                        m[1].h = make_float2(qh.z, qh.w);
+                        m[0].l = make_float2(ql.x, ql.y);
+                        m[1].l = make_float2(ql.z, ql.w);
+                    } else if constexpr (CPG == 2) {
+                        const float4 qh = *reinterpret_cast<const float4*>(stg + so);
+                        m[0] = typename Pol::Mat{qh.x, qh.y};
+                        m[1] = typename Pol::Mat{qh.z, qh.w};
+                    } else {
+                        m[0] = *reinterpret_cast<const typename Pol::Mat*>(stg + so);
+                    }
+                    YT yu[RR], yw[RR];
 #pragma unroll
                     for (int q = 0; q < RR; q++) {
-                        Pol::fma(cu[k][c][q], m[c], yu[q]);
-                        Pol::fma(cw[k][c][q], m[c], yw[q]);
+                        yu[q] = syu[row * RR + q];
+                        yw[q] = syw[row * RR + q];
                     }
+#pragma unroll
+                    for (int cc = 0; cc < CPG; cc++)
+#pragma unroll
+                        for (int q = 0; q < RR; q++) {
+                            Pol::fma(cu[k][cc][q], m[cc], yu[q]);
+                            Pol::fma(cw[k][cc][q], m[cc], yw[q]);
+                        }
+                }
             }
-            if (rs == spb - 1) {   // block done: column partial for block row j, slots combined in a fixed order
+            __syncwarp();   // all lanes are done with this stage
+            if (lane == 0 && t + S - 1 < total) {
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                issue(t + S - 1);
+            }
+            if (c == cpb - 1) {   // block done: column partial for block row j, slots combined in a fixed order
                 const long long p = sp.p0 + b;
 #pragma unroll
                 for (int k = 0; k < NS; k++)
                     if (sval[k])
 #pragma unroll
-                        for (int c = 0; c < CPG; c++)
+                        for (int cc = 0; cc < CPG; cc++)
 #pragma unroll
                             for (int q = 0; q < RR; q++)
-                                comb[((size_t)sro[k] * B + sg[k] * CPG + c) * RR + q] = Pol::out(cw[k][c][q]);
+                                comb[(soff[k] / MB + cc) * RR + q] = Pol::out(cw[k][cc][q]);
                 __syncwarp();
                 OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
                 for (int e = lane; e < B * RR; e += 32) {
@@ -456,15 +475,15 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
                 __syncwarp();
             }
         }
-        cp_async_wait<0>();
+        if (failed) break;
+        gchunk += (unsigned long long)total;
 #pragma unroll
         for (int k = 0; k < NS; k++)
             if (sval[k])
 #pragma unroll
-                for (int c = 0; c < CPG; c++)
+                for (int cc = 0; cc < CPG; cc++)
 #pragma unroll
-                    for (int q = 0; q < RR; q++)
-                        comb[((size_t)sro[k] * B + sg[k] * CPG + c) * RR + q] = Pol::out(cu[k][c][q]);
+                    for (int q = 0; q < RR; q++) comb[(soff[k] / MB + cc) * RR + q] = Pol::out(cu[k][cc][q]);
         __syncwarp();
         OutT* cup = CU + pl.cu_off + (w - pl.strip_base) * (long long)B * RT;
         for (int e = lane; e < B * RR; e += 32) {
@@ -477,6 +496,10 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             cup[(e / RR) * RT + rr0 + (e % RR)] = sm;
         }
         __syncwarp();
+    }
+    if (failed) {   // drain: wait (bounded) for every copy this warp may still have in flight
+        for (unsigned long long gc = fail_lo; gc < fail_hi; gc++)
+            (void)mbar_wait_bounded(bars + (gc % S), (unsigned)((gc / S) & 1));
     }
 }
 
@@ -532,9 +555,13 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
     const int row = I.r0 + lane;
     const int B = S.B;
     if (!DENSE) {
-        double2 su[R], sw[R];
+        // partial sums kept in the partials' own precision (FP32 for the FP32 policy)
+        OutT su[R], sw[R];
 #pragma unroll
-        for (int rr = 0; rr < R; rr++) su[rr] = sw[rr] = make_double2(0, 0);
+        for (int rr = 0; rr < R; rr++) {
+            su[rr].x = su[rr].y = 0;
+            sw[rr].x = sw[rr].y = 0;
+        }
         if (valid) {
             const int k = row / B, Rr = row % B;
             const int info = __ldg(S.rowinfo + Rr);
@@ -548,8 +575,8 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
 #pragma unroll
                     for (int rr = 0; rr < R; rr++) {
                         const OutT v = src[rr];
-                        su[rr].x += (double)v.x;
-                        su[rr].y += (double)v.y;
+                        su[rr].x += v.x;
+                        su[rr].y += v.y;
                     }
                 } else {
                     const int i = (int)(t - (s1 - s0));
@@ -558,16 +585,16 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
 #pragma unroll
                     for (int rr = 0; rr < R; rr++) {
                         const OutT v = src[rr];
-                        sw[rr].x += (double)v.x;
-                        sw[rr].y += (double)v.y;
+                        sw[rr].x += v.x;
+                        sw[rr].y += v.y;
                     }
                 }
             }
         }
 #pragma unroll
         for (int rr = 0; rr < R; rr++) {
-            pu[wid][lane][rr] = su[rr];
-            pw[wid][lane][rr] = sw[rr];
+            pu[wid][lane][rr] = make_double2((double)su[rr].x, (double)su[rr].y);
+            pw[wid][lane][rr] = make_double2((double)sw[rr].x, (double)sw[rr].y);
         }
         __syncthreads();
     }
@@ -1074,6 +1101,7 @@ struct DevPlan {
     const Item* ritems;
     const SysPlan* sp;
     const long long* row_strip;
+    int* err;   // set by a GEMV whose bounded wait on a copy expired
 };
 
 int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t stream, DevPlan& D) {
@@ -1090,6 +1118,8 @@ int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t st
     size_t o_ri = put(P.ritems.data(), sizeof(Item) * P.nr);
     size_t o_sp = put(P.sp.data(), sizeof(SysPlan) * P.nsys);
     size_t o_rs = put(P.row_strip.data(), sizeof(long long) * P.row_strip.size());
+    const int zeros[4] = {0, 0, 0, 0};
+    size_t o_err = put(zeros, sizeof(zeros));
     unsigned char* dst = base + w.off_blob;
     void* dblob = nullptr;
     int slot = 0;
@@ -1104,6 +1134,16 @@ int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t st
     D.ritems = reinterpret_cast<const Item*>(dst + o_ri);
     D.sp = reinterpret_cast<const SysPlan*>(dst + o_sp);
     D.row_strip = reinterpret_cast<const long long*>(dst + o_rs);
+    D.err = reinterpret_cast<int*>(dst + o_err);
+    return GB_OK;
+}
+
+// Reads the GEMV error flag back (synchronises the stream).
+int check_device_error(const DevPlan& D, cudaStream_t stream) {
+    int h = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&h, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (h) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
     return GB_OK;
 }
 
@@ -1127,34 +1167,31 @@ Shape pick_shape(int Bmax, int cpg, int nsmax) {
 
 template <class Pol, int RR, int RT>
 int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* mat_hi, const void* mat_lo,
-                 const void* Yu, const void* Yw, void* CU, void* CW, int rr0, cudaStream_t stream) {
+                 const void* Yu, const void* Yw, void* CU, void* CW, int rr0, int* err, cudaStream_t stream) {
     using YT = typename Pol::YT;
     using OutT = typename Pol::OutT;
     constexpr int nsmax = std::is_same<Pol, Pol64>::value ? 8 : 5;
     constexpr bool DF = IsDF<Pol>::v;
+    constexpr int MB = MatBytes<Pol>::v;
+    constexpr int S = 3;   // chunks in the ring: one being read, two in flight
     const Shape sh = pick_shape((int)P.max_B, Pol::CPG, nsmax);
     const int Bmax = (int)P.max_B;
-    // stages: up to 6, per-warp shared memory about 24 KB, and no more lookahead than
-    // the y ring covers (S - 1 <= kYRing - 1 block boundaries ahead is guaranteed
-    // when S - 1 <= (kYRing - 2) * steps-per-block)
-    int minB = (int)P.max_B;
-    for (const auto& d : P.sd) minB = std::min(minB, d.B);
-    const int spb_min = std::max(1, (minB + sh.rps - 1) / sh.rps);
-    int Sst = 6;   // stage counts 6, 4 or 2
-    while (Sst > 2) {
-        const GemvLayout g = gemv_layout(Bmax, sh.rps, RR, Sst, MatBytes<Pol>::v, DF, sizeof(OutT), sizeof(YT));
-        if (g.warp_bytes <= 26 * 1024 && Sst - 1 <= (kYRing - 2) * spb_min) break;
-        Sst -= 2;
-    }
-    const GemvLayout g = gemv_layout(Bmax, sh.rps, RR, Sst, MatBytes<Pol>::v, DF, sizeof(OutT), sizeof(YT));
+    // steps per chunk: about 6 KB of matrix per chunk (12 KB hi + lo)
+    int G = std::max(1, (6 * 1024) / (sh.rps * Bmax * MB));
+    G = std::min(G, (Bmax + sh.rps - 1) / sh.rps);
+    const GemvLayout g = gemv_layout(Bmax, sh.rps, G, RR, S, MB, DF, sizeof(OutT), sizeof(YT));
+    // bulk copies need 16-byte aligned sources (block sizes are even, so offsets keep it)
+    if ((reinterpret_cast<uintptr_t>(mat_hi) | reinterpret_cast<uintptr_t>(mat_lo) | reinterpret_cast<uintptr_t>(Yu) |
+         reinterpret_cast<uintptr_t>(Yw)) & 15)
+        return gb_set_error(GB_BAD_ARG, "matrix and workspace pointers must be 16-byte aligned");
     const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
     if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
     const long long TR = P.total_vec / P.R;
     const long long grid = std::max<long long>(1, std::min<long long>((P.nstrips * 32 + kGemvThreads - 1) / kGemvThreads,
                                                                       (long long)gb::sm_count() * 8));
-#define GB_PG_S(RPSV, NSV, SV)                                                                                   \
-    if (sh.rps == RPSV && sh.ns == NSV && Sst == SV) {                                                           \
-        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV, SV>;                                                          \
+#define GB_PG(RPSV, NSV)                                                                                         \
+    if (sh.rps == RPSV && sh.ns == NSV) {                                                                        \
+        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV, S>;                                                           \
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
         gb::note_launch();                                                                                       \
@@ -1162,11 +1199,10 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
                                                             reinterpret_cast<const YT*>(Yu),                     \
                                                             reinterpret_cast<const YT*>(Yw),                     \
                                                             reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), \
-                                                            D.sp, rr0, Bmax, TR);                               \
+                                                            D.sp, rr0, Bmax, G, TR, err);                        \
         GB_CUDA_TRY(cudaGetLastError());                                                                         \
         return GB_OK;                                                                                            \
     }
-#define GB_PG(RPSV, NSV) GB_PG_S(RPSV, NSV, 6) GB_PG_S(RPSV, NSV, 4) GB_PG_S(RPSV, NSV, 2)
     if constexpr (std::is_same<Pol, Pol64>::value) {
         GB_PG(4, 1) GB_PG(2, 1) GB_PG(1, 1) GB_PG(2, 3) GB_PG(2, 5) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 5) GB_PG(1, 7)
         GB_PG(1, 8) GB_PG(1, 2) GB_PG(1, 6)
@@ -1178,9 +1214,7 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
         GB_PG(2, 5) GB_PG(1, 5)
     }
 #undef GB_PG
-#undef GB_PG_S
-    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d (rps %d, ns %d, stages %d)", Bmax, sh.rps,
-                        sh.ns, Sst);
+    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d (rps %d, ns %d)", Bmax, sh.rps, sh.ns);
 }
 
 // One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
@@ -1199,7 +1233,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         gb::note_launch();
         k_yprep<0, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
                                                      reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), 0);
-        if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, stream);
+        if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
         k_reduce<double2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
@@ -1209,7 +1243,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         gb::note_launch();
         k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
                                                      reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw), 0);
-        if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, stream);
+        if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
         k_reduce<float2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
@@ -1221,7 +1255,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
                                                      reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw),
                                                      P.total_vec / R);
         for (int rr = 0; rr < R && P.nstrips; rr++) {
-            e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, rr, stream);
+            e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, rr, D.err, stream);
             if (e) return e;
         }
         gb::note_launch();
@@ -1394,8 +1428,11 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
                 if (e) return e;
             }
         }
+        int herr = 0;
         GB_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
+        GB_CUDA_TRY(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
         GB_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (herr) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
         bool all_done = true, restart = false;
         for (int q = 0; q < nsr; q++) {
             if (!hst[q].done) all_done = false;
@@ -1428,10 +1465,13 @@ int finish_status(const KState* h, int nsr, int* status, int* iters, double* res
     return worst;
 }
 
-int read_state(const KState* dev, int nsr, std::vector<KState>& h, cudaStream_t stream) {
+int read_state(const DevPlan& D, const KState* dev, int nsr, std::vector<KState>& h, cudaStream_t stream) {
     h.resize(nsr);
+    int herr = 0;
     GB_CUDA_TRY(cudaMemcpyAsync(h.data(), dev, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GB_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (herr) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
     return GB_OK;
 }
 
@@ -1459,7 +1499,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         k_copy_out<double2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R,
                                                        reinterpret_cast<double2*>(base + w.off_vec), x2);
         GB_CUDA_TRY(cudaGetLastError());
-        e = read_state(st, nsr, h, stream);
+        e = read_state(D, st, nsr, h, stream);
         if (e) return e;
         return finish_status(h.data(), nsr, status, iters, resid);
     }
@@ -1471,7 +1511,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         gb::note_launch();
         k_copy_out<float2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, V, x2);
         GB_CUDA_TRY(cudaGetLastError());
-        e = read_state(st, nsr, h, stream);
+        e = read_state(D, st, nsr, h, stream);
         if (e) return e;
         return finish_status(h.data(), nsr, status, iters, resid);
     }
@@ -1505,7 +1545,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         gb::note_launch();
         k_refine_check<R><<<(nsr * 32 + 127) / 128, 128, 0, stream>>>(D.sp, P.nsys, ost, dots, pass, max_refine);
         GB_CUDA_TRY(cudaGetLastError());
-        e = read_state(ost, nsr, h, stream);
+        e = read_state(D, ost, nsr, h, stream);
         if (e) return e;
         bool all = true;
         for (int q = 0; q < nsr; q++) all &= (h[q].done != 0);
@@ -1590,8 +1630,11 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
                       : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr,
                                                  dots, s);
     };
-    if (prec == GB_PREC_FP64) return ap(0, mat128, nullptr);
-    if (prec == GB_PREC_MIXED) return ap(2, mat64, mat64lo);
+    if (prec == GB_PREC_FP64 || prec == GB_PREC_MIXED) {
+        e = prec == GB_PREC_FP64 ? ap(0, mat128, nullptr) : ap(2, mat64, mat64lo);
+        if (e) return e;
+        return check_device_error(D, s);
+    }
     // FP32 product on a rounded copy of x, widened to FP64
     const size_t TV = (size_t)P.total_vec;
     float2* V = reinterpret_cast<float2*>(base + w.off_vec);
@@ -1606,7 +1649,7 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
     gb::note_launch();
     k_copy_out<float2><<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, yf, y2);
     GB_CUDA_TRY(cudaGetLastError());
-    return GB_OK;
+    return check_device_error(D, s);
 }
 
 int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
@@ -1647,19 +1690,19 @@ int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const doubl
             e = R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s)
                        : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s);
         } else if (pol == 0) {
-            e = R == 1 ? launch_pgemv<Pol64, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s)
-                       : launch_pgemv<Pol64, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s);
+            e = R == 1 ? launch_pgemv<Pol64, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s)
+                       : launch_pgemv<Pol64, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s);
         } else if (pol == 1) {
-            e = R == 1 ? launch_pgemv<Pol32, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s)
-                       : launch_pgemv<Pol32, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, s);
+            e = R == 1 ? launch_pgemv<Pol32, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s)
+                       : launch_pgemv<Pol32, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s);
         } else {
             for (int rr = 0; rr < R && !e; rr++)
-                e = R == 1 ? launch_pgemv<PolDF, 1, 1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, s)
-                           : launch_pgemv<PolDF, 1, 2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, s);
+                e = R == 1 ? launch_pgemv<PolDF, 1, 1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, D.err, s)
+                           : launch_pgemv<PolDF, 1, 2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, D.err, s);
         }
         if (e) return e;
     }
-    return GB_OK;
+    return check_device_error(D, s);
 }
 
 size_t gb_solve_dense_workspace_size(int D, int R) {
@@ -1696,7 +1739,7 @@ int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, do
                                                           reinterpret_cast<double2*>(x));
     GB_CUDA_TRY(cudaGetLastError());
     std::vector<KState> h;
-    e = read_state(st, P.nsys * R, h, s);
+    e = read_state(Dp, st, P.nsys * R, h, s);
     if (e) return e;
     return finish_status(h.data(), P.nsys * R, status, iters, resid);
 }
