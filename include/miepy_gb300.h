@@ -133,6 +133,19 @@ size_t gb_solve_dense_workspace_size(int D, int R);
 int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, double tol, int maxiter,
                    void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, void* stream);
 
+/* gb_solve_dense without any allocation, for callers that cannot allocate device
+ * memory: a server whose HBM is reserved up front, or a loop in which cudaMalloc /
+ * cudaFree would synchronise the device.  It has no counterpart in the reference.
+ * The solve (same arguments and results as gb_solve_dense) runs in a fixed scratch
+ * array of 1.25 MiB that the library carries in device memory; D * R may be at most
+ * 8192, larger sizes return GB_OVER_BUDGET.  No cudaMalloc, cudaFree or pinned host
+ * buffer is used.  The first call on each device looks up the array's address on
+ * that device (make it before any stream capture begins).  All calls on a device
+ * share the one array and it keeps the previous call's contents: calls whose work
+ * overlaps on the GPU (other streams, other host threads) race on it. */
+int gb_solve_dense_noalloc(int D, int R, const double* T, const double* b, double* x, double tol, int maxiter,
+                           int* status, int* iters, double* resid, void* stream);
+
 /* One application y = (I + T) x of the packed operator, for tests and
  * benchmarks: FP64 arithmetic on mat128 (GB_PREC_FP64), FP32 on mat64
  * (GB_PREC_FP32) or double-float on mat64 + mat64lo (GB_PREC_MIXED).

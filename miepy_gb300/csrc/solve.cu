@@ -1564,6 +1564,73 @@ bool prec_ok(int prec, const double* m128, const float* m64, const float* m64lo)
     }
 }
 
+// ------------------------------------------- dense solve without allocation --
+// Scratch of gb_solve_dense_noalloc: a fixed device array that the library's module
+// brings with it, so that callers that must not allocate device memory (a server
+// whose HBM is fully reserved up front, a real-time loop where cudaMalloc/cudaFree
+// would synchronise the device) can still solve.  Enough for D * R <= 8192.
+constexpr size_t kNoAllocScratchBytes = 1280u * 1024u;
+constexpr long long kNoAllocMaxDR = 8192;
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices];
+
+}   // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+// Device address of the scratch array on the current device, looked up once per
+// device (the lookup may load the library's module onto that device).
+int noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return gb_set_error(GB_UNSUPPORTED, "device %d is beyond the %d devices the scratch table covers", dev,
+                            kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    return GB_OK;
+}
+
+// Plan upload for the scratch array: the same blob as upload_plan, copied straight
+// from ordinary host memory (no pinned staging buffer, which would be allocated on
+// first use).  The blob carries the zeroed GEMV error flag.
+int upload_plan_pageable(const Plan& P, unsigned char* base, const WS& w, cudaStream_t stream, DevPlan& D) {
+    std::vector<unsigned char> blob;
+    auto put = [&](const void* src, size_t bytes) {
+        size_t off = blob.size();
+        blob.resize(off + ((bytes + 15) & ~size_t(15)));
+        if (bytes) memcpy(blob.data() + off, src, bytes);
+        return off;
+    };
+    size_t o_sys = put(P.sd.data(), sizeof(gb::SysDev) * P.nsys);
+    size_t o_str = put(P.strips.data(), sizeof(Strip) * P.nstrips);
+    size_t o_vi = put(P.vitems.data(), sizeof(Item) * P.nv);
+    size_t o_ri = put(P.ritems.data(), sizeof(Item) * P.nr);
+    size_t o_sp = put(P.sp.data(), sizeof(SysPlan) * P.nsys);
+    size_t o_rs = put(P.row_strip.data(), sizeof(long long) * P.row_strip.size());
+    const int zeros[4] = {0, 0, 0, 0};
+    size_t o_err = put(zeros, sizeof(zeros));
+    unsigned char* dst = base + w.off_blob;
+    // from pageable memory: returns once the blob has been taken, so it may go out of scope
+    GB_CUDA_TRY(cudaMemcpyAsync(dst, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
+    D.sys = reinterpret_cast<const gb::SysDev*>(dst + o_sys);
+    D.strips = reinterpret_cast<const Strip*>(dst + o_str);
+    D.vitems = reinterpret_cast<const Item*>(dst + o_vi);
+    D.ritems = reinterpret_cast<const Item*>(dst + o_ri);
+    D.sp = reinterpret_cast<const SysPlan*>(dst + o_sp);
+    D.row_strip = reinterpret_cast<const long long*>(dst + o_rs);
+    D.err = reinterpret_cast<int*>(dst + o_err);
+    return GB_OK;
+}
+
 }   // namespace
 
 extern "C" {
@@ -1725,6 +1792,48 @@ int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, do
     DevPlan Dp;
     int e = upload_plan(P, base, w, s, Dp);
     if (e) return e;
+    KState* st = reinterpret_cast<KState*>(base + w.off_state);
+    if (R == 1)
+        e = run_bicgstab<double2, 1, true>(P, Dp, w, base, 0, T, nullptr, reinterpret_cast<const double2*>(b), nullptr,
+                                           tol, maxiter, st, D, s, false);
+    else
+        e = run_bicgstab<double2, 2, true>(P, Dp, w, base, 0, T, nullptr, reinterpret_cast<const double2*>(b), nullptr,
+                                           tol, maxiter, st, D, s, false);
+    if (e) return e;
+    gb::note_launch();
+    k_copy_out<double2><<<(unsigned)P.nv, kVRows, 0, s>>>(Dp.sys, Dp.vitems, P.nv, R,
+                                                          reinterpret_cast<double2*>(base + w.off_vec),
+                                                          reinterpret_cast<double2*>(x));
+    GB_CUDA_TRY(cudaGetLastError());
+    std::vector<KState> h;
+    e = read_state(Dp, st, P.nsys * R, h, s);
+    if (e) return e;
+    return finish_status(h.data(), P.nsys * R, status, iters, resid);
+}
+
+int gb_solve_dense_noalloc(int D, int R, const double* T, const double* b, double* x, double tol, int maxiter,
+                           int* status, int* iters, double* resid, void* stream) {
+    if (D < 1 || !T || !b || !x) return gb_set_error(GB_BAD_ARG, "null argument");
+    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
+    if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
+    if ((long long)D * R > kNoAllocMaxDR)
+        return gb_set_error(GB_OVER_BUDGET, "D * R = %lld exceeds the no-allocation solve's limit of %lld",
+                            (long long)D * R, kNoAllocMaxDR);
+    cudaStream_t s = (cudaStream_t)stream;
+    Plan P;
+    dense_plan(D, R, P);
+    WS w = ws_layout(P, GB_PREC_FP64, true);
+    if (w.total > kNoAllocScratchBytes)
+        return gb_set_error(GB_OVER_BUDGET, "D = %d, R = %d needs %zu B of scratch; the fixed array holds %zu B", D, R,
+                            w.total, kNoAllocScratchBytes);
+    unsigned char* base = nullptr;
+    int e = noalloc_scratch(&base);
+    if (e) return e;
+    DevPlan Dp;
+    e = upload_plan_pageable(P, base, w, s, Dp);
+    if (e) return e;
+    // every other scratch region is written before it is read (x0 = 0, r = b and
+    // the iteration scalars are set by the first kernels of the solve)
     KState* st = reinterpret_cast<KState*>(base + w.off_state);
     if (R == 1)
         e = run_bicgstab<double2, 1, true>(P, Dp, w, base, 0, T, nullptr, reinterpret_cast<const double2*>(b), nullptr,
