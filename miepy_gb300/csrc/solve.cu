@@ -113,63 +113,126 @@ __device__ __forceinline__ bool any_active(const KState* st, int sys, int mask_m
 }
 
 // --------------------------------------------------------------- policies --
-struct DFAcc {          // double-float complex accumulator + FP32 correction terms
-    float hr, lr, hi, li, sr, si;
-};
+// Arithmetic of the GEMV.  A lane multiplies one matrix element m by the y
+// values of its row; complex products use packed f32x2 FMAs where the policy is
+// FP32-based: with m = (re, im) as loaded,
+//   a += m * y.re,  b += m * y.im,  and m y = (a.x - b.y, a.y + b.x),
+// so no shuffling of m is needed and each complex multiply-add is two FFMA2.
+__device__ __forceinline__ float2 bc(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
 
-__device__ __forceinline__ void two_sum_acc(float& h, float& l, float p, float e) {
-    // (h, l) += p + e: p added exactly (TwoSum), its error and e into the low part
-    const float s = h + p;
-    const float bb = s - h;
-    const float err = (h - (s - bb)) + (p - bb);
+// (h, l) += p exactly (TwoSum on both components), error into l
+__device__ __forceinline__ void two_sum2(float2& h, float2& l, float2 p) {
+    const float2 s = __fadd2_rn(h, p);
+    const float2 bb = __fadd2_rn(s, neg2(h));
+    const float2 err = __fadd2_rn(__fadd2_rn(h, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(p, neg2(bb)));
     h = s;
-    l += err + e;
+    l = __fadd2_rn(l, err);
+}
+// scalar double-float helpers: (h, l) normalised sum of two double-floats
+__device__ __forceinline__ void df_add(float& h, float& l, float h2, float l2) {
+    const float s = h + h2;
+    const float bb = s - h;
+    const float err = (h - (s - bb)) + (h2 - bb);
+    const float t = err + l + l2;
+    h = s + t;
+    l = t - (h - s);
 }
 
-struct Pol64 {
-    static constexpr int CPG = 1;
+struct Pol64 {                 // complex128 matrix, FP64 FMAs
+    static constexpr int MB = 16;
+    static constexpr bool DF = false;
     using YT = double2;
+    using OutT = double2;
     using Acc = double2;
-    using OutT = double2;
-    using Mat = double2;
-    __device__ static void zero(Acc& a) { a = make_double2(0, 0); }
-    __device__ static void fma(Acc& a, const Mat& m, const YT& y) { cfma(a, m, y); }
-    __device__ static OutT out(const Acc& a) { return a; }
-};
-
-struct Pol32 {
-    static constexpr int CPG = 2;
-    using YT = float2;
-    using Acc = float2;
-    using OutT = float2;
-    using Mat = float2;
-    __device__ static void zero(Acc& a) { a = make_float2(0, 0); }
-    __device__ static void fma(Acc& a, const Mat& m, const YT& y) { cfmaf(a, m, y); }
-    __device__ static OutT out(const Acc& a) { return a; }
-};
-
-struct PolDF {
-    static constexpr int CPG = 2;
-    using YT = float4;     // (hi.re, hi.im, lo.re, lo.im)
-    using Acc = DFAcc;
-    using OutT = double2;
-    struct Mat { float2 h, l; };
-    __device__ static void zero(Acc& a) { a = DFAcc{0, 0, 0, 0, 0, 0}; }
-    __device__ static void fma(Acc& a, const Mat& m, const YT& y) {
-        // main term m.h * y.h: every real product exact as p + e
-        float p, e;
-        p = m.h.x * y.x; e = fmaf(m.h.x, y.x, -p); two_sum_acc(a.hr, a.lr, p, e);
-        p = m.h.y * y.y; e = fmaf(m.h.y, y.y, -p); two_sum_acc(a.hr, a.lr, -p, -e);
-        p = m.h.x * y.y; e = fmaf(m.h.x, y.y, -p); two_sum_acc(a.hi, a.li, p, e);
-        p = m.h.y * y.x; e = fmaf(m.h.y, y.x, -p); two_sum_acc(a.hi, a.li, p, e);
-        // corrections m.h * y.l + m.l * y.h (relative size 2^-24)
-        a.sr = fmaf(m.h.x, y.z, a.sr); a.sr = fmaf(-m.h.y, y.w, a.sr);
-        a.si = fmaf(m.h.x, y.w, a.si); a.si = fmaf(m.h.y, y.z, a.si);
-        a.sr = fmaf(m.l.x, y.x, a.sr); a.sr = fmaf(-m.l.y, y.y, a.sr);
-        a.si = fmaf(m.l.x, y.y, a.si); a.si = fmaf(m.l.y, y.x, a.si);
+    struct M { double2 h; };
+    __device__ static M load(const unsigned char* hi, const unsigned char*, unsigned off) {
+        return M{*reinterpret_cast<const double2*>(hi + off)};
     }
-    __device__ static OutT out(const Acc& a) {
-        return make_double2((double)a.hr + ((double)a.lr + (double)a.sr), (double)a.hi + ((double)a.li + (double)a.si));
+    __device__ static void zero(Acc& a) { a = make_double2(0, 0); }
+    __device__ static void prep(M&) {}
+    __device__ static void mac(Acc& a, const M& m, const YT& y) { cfma(a, m.h, y); }
+    __device__ static OutT out(const Acc& a) { return a; }
+    __device__ static OutT add(OutT u, OutT v) { return make_double2(u.x + v.x, u.y + v.y); }
+    __device__ static OutT shfl(OutT v, int off) {
+        return make_double2(__shfl_xor_sync(0xffffffffu, v.x, off), __shfl_xor_sync(0xffffffffu, v.y, off));
+    }
+};
+
+struct Pol32 {                 // complex64 matrix, packed FP32 FMAs
+    static constexpr int MB = 8;
+    static constexpr bool DF = false;
+    using YT = float2;
+    using OutT = float2;
+    struct Acc { float2 a, b; };
+    struct M { float2 h; };
+    __device__ static M load(const unsigned char* hi, const unsigned char*, unsigned off) {
+        return M{*reinterpret_cast<const float2*>(hi + off)};
+    }
+    __device__ static void zero(Acc& s) { s.a = s.b = make_float2(0, 0); }
+    __device__ static void prep(M&) {}
+    __device__ static void mac(Acc& s, const M& m, const YT& y) {
+        s.a = __ffma2_rn(m.h, bc(y.x), s.a);
+        s.b = __ffma2_rn(m.h, bc(y.y), s.b);
+    }
+    __device__ static OutT out(const Acc& s) { return make_float2(s.a.x - s.b.y, s.a.y + s.b.x); }
+    __device__ static OutT add(OutT u, OutT v) { return make_float2(u.x + v.x, u.y + v.y); }
+    __device__ static OutT shfl(OutT v, int off) {
+        return make_float2(__shfl_xor_sync(0xffffffffu, v.x, off), __shfl_xor_sync(0xffffffffu, v.y, off));
+    }
+};
+
+// Double-float: the complex128 matrix as complex64 hi + lo, y as (hi.re, hi.im,
+// lo.re, lo.im).  Every hi*hi real product is formed exactly (p = fl(m y),
+// e = fma(m, y, -p)) and summed with TwoSum; e, the TwoSum errors and the
+// hi*lo + lo*hi corrections accumulate in the low word.  Partial results leave as
+// a double-float complex float4 (re.h, im.h, re.l, im.l), about 1e-14 relative.
+struct DFAcc { float2 ha, la, hb, lb; };
+struct PolDF {
+    static constexpr int MB = 8;
+    static constexpr bool DF = true;
+    using YT = float4;
+    using OutT = float4;
+    using Acc = DFAcc;
+    struct M { float2 h, l, nh; };
+    __device__ static M load(const unsigned char* hi, const unsigned char* lo, unsigned off) {
+        M m;
+        m.h = *reinterpret_cast<const float2*>(hi + off);
+        m.l = *reinterpret_cast<const float2*>(lo + off);
+        return m;
+    }
+    __device__ static void zero(Acc& s) { s.ha = s.la = s.hb = s.lb = make_float2(0, 0); }
+    __device__ static void prep(M& m) { m.nh = neg2(m.h); }
+    __device__ static void mac(Acc& s, const M& m, const YT& y) {
+        const float2 yr = bc(y.x), yi = bc(y.y);
+        float2 p = __fmul2_rn(m.h, yr);
+        float2 en = __ffma2_rn(m.nh, yr, p);                 // p - m y = -(rounding error)
+        two_sum2(s.ha, s.la, p);
+        s.la = __fadd2_rn(s.la, neg2(en));
+        s.la = __ffma2_rn(m.l, yr, s.la);
+        s.la = __ffma2_rn(m.h, bc(y.z), s.la);
+        p = __fmul2_rn(m.h, yi);
+        en = __ffma2_rn(m.nh, yi, p);
+        two_sum2(s.hb, s.lb, p);
+        s.lb = __fadd2_rn(s.lb, neg2(en));
+        s.lb = __ffma2_rn(m.l, yi, s.lb);
+        s.lb = __ffma2_rn(m.h, bc(y.w), s.lb);
+    }
+    __device__ static OutT out(const Acc& s) {
+        // re = a.x - b.y, im = a.y + b.x, each as a normalised double-float
+        float rh = s.ha.x, rl = s.la.x, ih = s.ha.y, il = s.la.y;
+        df_add(rh, rl, -s.hb.y, -s.lb.y);
+        df_add(ih, il, s.hb.x, s.lb.x);
+        return make_float4(rh, ih, rl, il);
+    }
+    __device__ static OutT add(OutT u, OutT v) {
+        df_add(u.x, u.z, v.x, v.z);
+        df_add(u.y, u.w, v.y, v.w);
+        return u;
+    }
+    __device__ static OutT shfl(OutT v, int off) {
+        return make_float4(__shfl_xor_sync(0xffffffffu, v.x, off), __shfl_xor_sync(0xffffffffu, v.y, off),
+                           __shfl_xor_sync(0xffffffffu, v.z, off), __shfl_xor_sync(0xffffffffu, v.w, off));
     }
 };
 
@@ -192,13 +255,12 @@ template <> __device__ __forceinline__ float4 make_y<2>(double2 z) {
     return make_float4(hx, hy, __double2float_rn(z.x - (double)hx), __double2float_rn(z.y - (double)hy));
 }
 
-// Layout: [D][R] interleaved for YK 0/1; for YK 2 one plane per right-hand side,
-// element (rr, row) at rr*TR + vec_off/R + row (TR = rows of all clusters).
+// Layout: [D][R] interleaved (element (row, rr) at vec_off + row*R + rr).
 template <int YK, typename VT, int R>
 __global__ void __launch_bounds__(kVRows)
 k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
         int mask_mode, const double2* __restrict__ tvec, const VT* __restrict__ x, typename YType<YK>::t* __restrict__ Yu,
-        typename YType<YK>::t* __restrict__ Yw, long long TR) {
+        typename YType<YK>::t* __restrict__ Yw) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
@@ -218,7 +280,7 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
         const double2 z = cmul(t, to_d2(x[S.vec_off + src * R + rr]));
         const double2 yu = make_double2(flipd(z.x, eneg), flipd(z.y, eneg));
         const double2 yw = make_double2(flipd(yu.x, sneg), flipd(yu.y, sneg));
-        const long long o = (YK == 2) ? rr * TR + S.vec_off / R + row : S.vec_off + (long long)row * R + rr;
+        const long long o = S.vec_off + (long long)row * R + rr;
         Yu[o] = make_y<YK>(yu);
         Yw[o] = make_y<YK>(yw);
     }
@@ -262,52 +324,49 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
     return true;
 }
 
-template <class Pol> struct MatBytes { static constexpr int v = 16 / Pol::CPG; };
-template <class Pol> struct IsDF { static constexpr bool v = false; };
-template <> struct IsDF<PolDF> { static constexpr bool v = true; };
-
-constexpr int kYRing = 4;   // y-vector buffers per warp
-
 struct GemvLayout {
-    int chunk_cap, comb_bytes, y_bytes, warp_bytes;
+    int chunk_cap, y_bytes, warp_bytes;
 };
-// per warp: S mbarriers | comb [RPS][Bmax][RR] OutT | syw | y ring [kYRing] | S stages
-__host__ __device__ inline GemvLayout gemv_layout(int Bmax, int RPS, int G, int RR, int S, int mat_bytes, bool df,
-                                                  int out_bytes, int y_bytes) {
+// Per warp: S mbarriers | S y-vector slots (y_u of the blocks in flight) | y_w of
+// the strip's particle | S matrix stages (hi, then lo for double-float).
+__host__ __device__ inline GemvLayout gemv_layout(int Bmax, int rows_per_chunk, int RT, int S, int mat_bytes, bool df,
+                                                  int y_bytes) {
     GemvLayout g;
-    g.chunk_cap = G * RPS * Bmax * mat_bytes;               // bytes of one matrix chunk (hi; lo follows for DF)
-    g.comb_bytes = (RPS * Bmax * RR * out_bytes + 127) & ~127;
-    g.y_bytes = (Bmax * RR * y_bytes + 127) & ~127;
-    g.warp_bytes = 128 + g.comb_bytes + (kYRing + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1);
-    g.warp_bytes = (g.warp_bytes + 127) & ~127;
+    g.chunk_cap = ((rows_per_chunk * Bmax * mat_bytes) + 127) & ~127;
+    g.y_bytes = (Bmax * RT * y_bytes + 127) & ~127;
+    g.warp_bytes = 128 + (S + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1);
     return g;
 }
 
-// RR: right-hand sides per launch (all R for Pol64/Pol32; one, rr0, for PolDF);
-// RT: stride of the [D][RT] partials.  Y vectors: [D][RT] (Pol64/Pol32) or one
-// contiguous [rows] plane per right-hand side (PolDF, plane rr0 at Yu + rr0*TR).
-template <class Pol, int RR, int RT, int RPS, int NS, int S>
+// Row-lane mapping: LPR lanes share a matrix row, RPW = 32/LPR rows per step;
+// lane (ro, cl) owns the columns cl + LPR*k (k < CPL) of its row, so one y load
+// serves CPL elements and the smem reads of a row are contiguous across lanes.
+// Column sums of the RPW rows are combined by shuffles once per block.
+// RR right-hand sides per launch (rr0 .. rr0+RR-1), RT the row stride of y and
+// of the partials.
+template <class Pol, int RR, int RT, int LPR, int CPL, int S>
 __global__ void __launch_bounds__(kGemvThreads)
 k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long nstrips,
         const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
         const typename Pol::YT* __restrict__ Yu, const typename Pol::YT* __restrict__ Yw,
         typename Pol::OutT* __restrict__ CU, typename Pol::OutT* __restrict__ CW, const SysPlan* __restrict__ plan,
-        int rr0, int Bmax, int G, long long TR, int* __restrict__ err) {
+        int rr0, int Bmax, int G, int* __restrict__ err) {
     using Acc = typename Pol::Acc;
     using OutT = typename Pol::OutT;
     using YT = typename Pol::YT;
-    constexpr int CPG = Pol::CPG;
-    constexpr int MB = MatBytes<Pol>::v;
-    constexpr bool DF = IsDF<Pol>::v;
+    constexpr int MB = Pol::MB;
+    constexpr bool DF = Pol::DF;
+    constexpr int RPW = 32 / LPR;
     extern __shared__ __align__(128) unsigned char gemv_smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const GemvLayout lay = gemv_layout(Bmax, RPS, G, RR, S, MB, DF, sizeof(OutT), sizeof(YT));
+    const int ro = lane / LPR, cl = lane % LPR;
+    const int RC = G * RPW;   // rows per chunk
+    const GemvLayout lay = gemv_layout(Bmax, RC, RT, S, MB, DF, sizeof(YT));
     unsigned char* wbase = gemv_smem + (size_t)wid * lay.warp_bytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(wbase);
-    OutT* comb = reinterpret_cast<OutT*>(wbase + 128);
-    unsigned char* yring = wbase + 128 + lay.comb_bytes;
-    YT* syw = reinterpret_cast<YT*>(yring + kYRing * lay.y_bytes);
-    unsigned char* stages = yring + (kYRing + 1) * lay.y_bytes;
+    unsigned char* yring = wbase + 128;
+    YT* syw = reinterpret_cast<YT*>(yring + S * lay.y_bytes);
+    unsigned char* stages = yring + (S + 1) * lay.y_bytes;
     const unsigned stage_stride = lay.chunk_cap * (DF ? 2 : 1);
     const unsigned char* mh = reinterpret_cast<const unsigned char*>(mat_hi);
     const unsigned char* ml = reinterpret_cast<const unsigned char*>(mat_lo);
@@ -326,176 +385,121 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
 #pragma unroll
         for (int q = 0; q < RR; q++) act |= active_rhs<RT>(st, sp.sys, rr0 + q, mask_mode);
         if (!act) continue;
-        const gb::SysDev& S_ = sys[sp.sys];
-        const int B = S_.B, N = S_.N;
-        const long long mat_off = S_.mat_off, vec_off = S_.vec_off;
+        const gb::SysDev& Sd = sys[sp.sys];
+        const int B = Sd.B, N = Sd.N;
+        const long long mat_off = Sd.mat_off, vec_off = Sd.vec_off;
         const SysPlan& pl = plan[sp.sys];
-        const int ncg = B / CPG;
-        const int spb = (B + RPS - 1) / RPS;           // steps per block
-        const int cpb = (spb + G - 1) / G;             // chunks per block
+        const int cpb = (B + RC - 1) / RC;            // chunks per block
         const int total = sp.nb * cpb;
-        int soff[NS], sro[NS];
-        bool sval[NS];
-#pragma unroll
-        for (int k = 0; k < NS; k++) {
-            const int f = lane + 32 * k;
-            sval[k] = f < RPS * ncg;
-            sro[k] = sval[k] ? f / ncg : 0;
-            soff[k] = sval[k] ? (sro[k] * B + (f % ncg) * CPG) * MB : 0;
-        }
-        const unsigned ybytes = (unsigned)(B * RR * sizeof(YT));
-        auto ysrc = [&](int part) -> const YT* {
-            if (DF) return Yu + (long long)rr0 * TR + vec_off / RT + (long long)part * B;
-            return Yu + vec_off + (long long)part * B * RT;
-        };
-        // chunk t of the strip: rows [c*G*RPS, ...) of block b (contiguous), plus the
-        // block's y vector with its first chunk; issued by lane 0
-        auto issue = [&](int t) {
+        const unsigned ybytes = (unsigned)(B * RT * sizeof(YT));
+        auto issue = [&](int t) {   // lane 0: chunk t of the strip (+ the block's y_u with its first chunk)
             const int b = t / cpb, c = t % cpb;
             const long long p = sp.p0 + b;
-            const int r0 = c * G * RPS;
-            const int nrows = min(G * RPS, B - r0);
+            const int r0 = c * RC;
+            const int nrows = min(RC, B - r0);
             const unsigned bytes = (unsigned)(nrows * B * MB);
             const unsigned long long gc = gchunk + (unsigned long long)t;
             uint64_t* bar = bars + (gc % S);
             unsigned char* dst = stages + (size_t)(gc % S) * stage_stride;
             const long long src = (mat_off + p * (long long)B * B + (long long)r0 * B) * MB;
-            unsigned tx = bytes * (DF ? 2u : 1u) + (c == 0 ? ybytes : 0u);
+            const unsigned tx = bytes * (DF ? 2u : 1u) + (c == 0 ? ybytes : 0u);
             mbar_expect_tx(bar, tx);
             tma_1d(dst, mh + src, bytes, bar);
             if (DF) tma_1d(dst + lay.chunk_cap, ml + src, bytes, bar);
             if (c == 0) {
                 const int j = sp.i + 1 + (int)(p - pair_start(sp.i, N));
-                tma_1d(yring + (size_t)(b % kYRing) * lay.y_bytes, ysrc(j), ybytes, bar);
+                tma_1d(yring + (size_t)(b % S) * lay.y_bytes, Yu + vec_off + (long long)j * B * RT, ybytes, bar);
             }
         };
         {   // y_w of particle i: the same for every block of the strip
-            const YT* src = DF ? Yw + (long long)rr0 * TR + vec_off / RT + (long long)sp.i * B
-                               : Yw + vec_off + (long long)sp.i * B * RT;
-            for (int e = lane; e < B * RR; e += 32) syw[e] = src[e];
+            const YT* src = Yw + vec_off + (long long)sp.i * B * RT;
+            for (int e = lane; e < B * RT; e += 32) syw[e] = src[e];
         }
-        Acc cu[NS][CPG][RR], cw[NS][CPG][RR];
+        Acc cu[CPL][RR], cw[CPL][RR];
 #pragma unroll
-        for (int k = 0; k < NS; k++)
+        for (int k = 0; k < CPL; k++)
 #pragma unroll
-            for (int c = 0; c < CPG; c++)
-#pragma unroll
-                for (int q = 0; q < RR; q++) Pol::zero(cu[k][c][q]);
-        // every lane has finished reading the stages it may overwrite (previous strip)
-        __syncwarp();
+            for (int q = 0; q < RR; q++) Pol::zero(cu[k][q]);
+        __syncwarp();   // syw written; every stage of the previous strip consumed
         if (lane == 0) {
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             for (int t = 0; t < S - 1 && t < total; t++) issue(t);
         }
         for (int t = 0; t < total; t++) {
             const unsigned long long gc = gchunk + (unsigned long long)t;
+            if (lane == 0 && t + S - 1 < total) issue(t + S - 1);   // into the stage freed by chunk t-1
             const bool ok = mbar_wait_bounded(bars + (gc % S), (unsigned)((gc / S) & 1));
             if (!__all_sync(0xffffffffu, ok)) {   // warp-uniform decision
                 if (lane == 0) atomicExch(err, 1);
                 failed = true;
                 fail_lo = gc;
-                fail_hi = gchunk + (unsigned long long)min(t + S - 1, total);
+                fail_hi = gchunk + (unsigned long long)min(t + S, total);
                 break;
             }
             const int b = t / cpb, c = t % cpb;
             if (c == 0) {
 #pragma unroll
-                for (int k = 0; k < NS; k++)
+                for (int k = 0; k < CPL; k++)
 #pragma unroll
-                    for (int cc = 0; cc < CPG; cc++)
-#pragma unroll
-                        for (int q = 0; q < RR; q++) Pol::zero(cw[k][cc][q]);
+                    for (int q = 0; q < RR; q++) Pol::zero(cw[k][q]);
             }
-            const YT* syu = reinterpret_cast<const YT*>(yring + (size_t)(b % kYRing) * lay.y_bytes);
+            const YT* syu = reinterpret_cast<const YT*>(yring + (size_t)(b % S) * lay.y_bytes);
             const unsigned char* stg = stages + (size_t)(gc % S) * stage_stride;
-            const int r0 = c * G * RPS;
-            const int nsteps = min(G, spb - c * G);
-            for (int g = 0; g < nsteps; g++) {
+            const int nrows = min(RC, B - c * RC);
+            const int row0 = c * RC;
+            for (int lr = ro; lr < nrows; lr += RPW) {
+                const int row = row0 + lr;
+                YT yu[RR], yw[RR];
 #pragma unroll
-                for (int k = 0; k < NS; k++) {
-                    const int row = r0 + g * RPS + sro[k];
-                    if (!(sval[k] && row < B)) continue;
-                    const size_t so = (size_t)g * RPS * B * MB + soff[k];
-                    typename Pol::Mat m[CPG];
-                    if constexpr (DF) {
-                        const float4 qh = *reinterpret_cast<const float4*>(stg + so);
-                        const float4 ql = *reinterpret_cast<const float4*>(stg + lay.chunk_cap + so);
-                        m[0].h = make_float2(qh.x, qh.y);
-                        m[1].h = make_float2(qh.z, qh.w);
-                        m[0].l = make_float2(ql.x, ql.y);
-                        m[1].l = make_float2(ql.z, ql.w);
-                    } else if constexpr (CPG == 2) {
-                        const float4 qh = *reinterpret_cast<const float4*>(stg + so);
-                        m[0] = typename Pol::Mat{qh.x, qh.y};
-                        m[1] = typename Pol::Mat{qh.z, qh.w};
-                    } else {
-                        m[0] = *reinterpret_cast<const typename Pol::Mat*>(stg + so);
-                    }
-                    YT yu[RR], yw[RR];
+                for (int q = 0; q < RR; q++) {
+                    yu[q] = syu[row * RT + rr0 + q];
+                    yw[q] = syw[row * RT + rr0 + q];
+                }
+                const unsigned rbase = (unsigned)(lr * B) * MB;
 #pragma unroll
-                    for (int q = 0; q < RR; q++) {
-                        yu[q] = syu[row * RR + q];
-                        yw[q] = syw[row * RR + q];
-                    }
-#pragma unroll
-                    for (int cc = 0; cc < CPG; cc++)
+                for (int k = 0; k < CPL; k++) {
+                    const int col = cl + LPR * k;
+                    if (col < B) {
+                        typename Pol::M m = Pol::load(stg, stg + lay.chunk_cap, rbase + (unsigned)col * MB);
+                        Pol::prep(m);
 #pragma unroll
                         for (int q = 0; q < RR; q++) {
-                            Pol::fma(cu[k][cc][q], m[cc], yu[q]);
-                            Pol::fma(cw[k][cc][q], m[cc], yw[q]);
+                            Pol::mac(cu[k][q], m, yu[q]);
+                            Pol::mac(cw[k][q], m, yw[q]);
                         }
-                }
-            }
-            __syncwarp();   // all lanes are done with this stage
-            if (lane == 0 && t + S - 1 < total) {
-                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                issue(t + S - 1);
-            }
-            if (c == cpb - 1) {   // block done: column partial for block row j, slots combined in a fixed order
-                const long long p = sp.p0 + b;
-#pragma unroll
-                for (int k = 0; k < NS; k++)
-                    if (sval[k])
-#pragma unroll
-                        for (int cc = 0; cc < CPG; cc++)
-#pragma unroll
-                            for (int q = 0; q < RR; q++)
-                                comb[(soff[k] / MB + cc) * RR + q] = Pol::out(cw[k][cc][q]);
-                __syncwarp();
-                OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
-                for (int e = lane; e < B * RR; e += 32) {
-                    OutT sm = comb[e];
-                    for (int ro = 1; ro < RPS; ro++) {
-                        const OutT v = comb[(size_t)ro * B * RR + e];
-                        sm.x += v.x;
-                        sm.y += v.y;
                     }
-                    cwp[(e / RR) * RT + rr0 + (e % RR)] = sm;
                 }
-                __syncwarp();
+            }
+            __syncwarp();   // every lane is done with this stage and y slot
+            if (lane == 0) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            if (c == cpb - 1) {   // block done: column partial of block row j
+                const long long p = sp.p0 + b;
+                OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
+#pragma unroll
+                for (int k = 0; k < CPL; k++)
+#pragma unroll
+                    for (int q = 0; q < RR; q++) {
+                        OutT v = Pol::out(cw[k][q]);
+#pragma unroll
+                        for (int off = LPR; off < 32; off <<= 1) v = Pol::add(v, Pol::shfl(v, off));
+                        const int col = cl + LPR * k;
+                        if (ro == 0 && col < B) cwp[col * RT + rr0 + q] = v;
+                    }
             }
         }
         if (failed) break;
         gchunk += (unsigned long long)total;
-#pragma unroll
-        for (int k = 0; k < NS; k++)
-            if (sval[k])
-#pragma unroll
-                for (int cc = 0; cc < CPG; cc++)
-#pragma unroll
-                    for (int q = 0; q < RR; q++) comb[(soff[k] / MB + cc) * RR + q] = Pol::out(cu[k][cc][q]);
-        __syncwarp();
         OutT* cup = CU + pl.cu_off + (w - pl.strip_base) * (long long)B * RT;
-        for (int e = lane; e < B * RR; e += 32) {
-            OutT sm = comb[e];
-            for (int ro = 1; ro < RPS; ro++) {
-                const OutT v = comb[(size_t)ro * B * RR + e];
-                sm.x += v.x;
-                sm.y += v.y;
+#pragma unroll
+        for (int k = 0; k < CPL; k++)
+#pragma unroll
+            for (int q = 0; q < RR; q++) {
+                OutT v = Pol::out(cu[k][q]);
+#pragma unroll
+                for (int off = LPR; off < 32; off <<= 1) v = Pol::add(v, Pol::shfl(v, off));
+                const int col = cl + LPR * k;
+                if (ro == 0 && col < B) cup[col * RT + rr0 + q] = v;
             }
-            cup[(e / RR) * RT + rr0 + (e % RR)] = sm;
-        }
-        __syncwarp();
     }
     if (failed) {   // drain: wait (bounded) for every copy this warp may still have in flight
         for (unsigned long long gc = fail_lo; gc < fail_hi; gc++)
@@ -533,6 +537,24 @@ k_dense_gemv(int D, const double2* __restrict__ T, const double2* __restrict__ x
 }
 
 // --------------------------------------------------------------- K3b reduce --
+// Per-lane sum of partials: plain sums for float2 / double2 partials, a
+// double-float sum for the double-float complex partials (re.h, im.h, re.l, im.l).
+template <typename OutT> struct RAcc {
+    OutT s;
+    __device__ void zero() { s.x = s.y = 0; }
+    __device__ void add(const OutT& v) { s.x += v.x; s.y += v.y; }
+    __device__ double2 get() const { return make_double2((double)s.x, (double)s.y); }
+};
+template <> struct RAcc<float4> {
+    float rh, ih, rl, il;
+    __device__ void zero() { rh = ih = rl = il = 0.f; }
+    __device__ void add(const float4& v) {
+        df_add(rh, rl, v.x, v.z);
+        df_add(ih, il, v.y, v.w);
+    }
+    __device__ double2 get() const { return make_double2((double)rh + (double)rl, (double)ih + (double)il); }
+};
+
 // y = x + T x (from the partials, or from a dense Tx), and per-item partial dots:
 //   mode 1: d0 = <r0, y>;  mode 2: d0 = |y|^2, d1 = <y, s>;
 //   mode 3: y := b - (x + T x), d0 = |y|^2  (residual).
@@ -555,12 +577,13 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
     const int row = I.r0 + lane;
     const int B = S.B;
     if (!DENSE) {
-        // partial sums kept in the partials' own precision (FP32 for the FP32 policy)
-        OutT su[R], sw[R];
+        // partial sums kept in the partials' own precision (FP32 for the FP32 policy,
+        // double-float for the double-float one)
+        RAcc<OutT> su[R], sw[R];
 #pragma unroll
         for (int rr = 0; rr < R; rr++) {
-            su[rr].x = su[rr].y = 0;
-            sw[rr].x = sw[rr].y = 0;
+            su[rr].zero();
+            sw[rr].zero();
         }
         if (valid) {
             const int k = row / B, Rr = row % B;
@@ -574,9 +597,7 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
                     const OutT* src = CU + pl.cu_off + ((t + s0 - pl.strip_base) * B + rho) * R;
 #pragma unroll
                     for (int rr = 0; rr < R; rr++) {
-                        const OutT v = src[rr];
-                        su[rr].x += v.x;
-                        su[rr].y += v.y;
+                        su[rr].add(src[rr]);
                     }
                 } else {
                     const int i = (int)(t - (s1 - s0));
@@ -584,17 +605,15 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
                     const OutT* src = CW + pl.cw_off + (pr * B + rho) * R;
 #pragma unroll
                     for (int rr = 0; rr < R; rr++) {
-                        const OutT v = src[rr];
-                        sw[rr].x += v.x;
-                        sw[rr].y += v.y;
+                        sw[rr].add(src[rr]);
                     }
                 }
             }
         }
 #pragma unroll
         for (int rr = 0; rr < R; rr++) {
-            pu[wid][lane][rr] = make_double2((double)su[rr].x, (double)su[rr].y);
-            pw[wid][lane][rr] = make_double2((double)sw[rr].x, (double)sw[rr].y);
+            pu[wid][lane][rr] = su[rr].get();
+            pw[wid][lane][rr] = sw[rr].get();
         }
         __syncthreads();
     }
@@ -1148,19 +1167,18 @@ int check_device_error(const DevPlan& D, cudaStream_t stream) {
 }
 
 // --------------------------------------------------- GEMV launch selection --
-struct Shape { int rps, ns; };
+struct Shape { int lpr, cpl; };
 
-// Rows per step and slots per lane: all 32 lanes busy where possible, within a
-// register budget per policy (slots <= nsmax).
-Shape pick_shape(int Bmax, int cpg, int nsmax) {
-    const int ncg = Bmax / cpg;
-    Shape best{1, (ncg + 31) / 32};
+// Lanes per row and columns per lane for a block size: the fewest idle lanes
+// (LPR*CPL >= Bmax), ties to more columns per lane.
+Shape pick_shape(int Bmax) {
+    static const Shape cands[] = {{8, 1}, {8, 2}, {8, 4}, {16, 3}, {16, 5}, {32, 3}, {32, 4}, {32, 5}};
+    Shape best{0, 0};
     double beff = -1;
-    for (int rps : {1, 2, 4}) {
-        const int ns = (rps * ncg + 31) / 32;
-        if (ns > nsmax) continue;
-        const double eff = double(rps * ncg) / (32.0 * ns);
-        if (eff > beff + 1e-9) { beff = eff; best = Shape{rps, ns}; }
+    for (const Shape& c : cands) {
+        if (c.lpr * c.cpl < Bmax) continue;
+        const double eff = double(Bmax) / (c.lpr * c.cpl);
+        if (eff > beff + 1e-9 || (std::fabs(eff - beff) < 1e-9 && c.cpl > best.cpl)) { beff = eff; best = c; }
     }
     return best;
 }
@@ -1170,28 +1188,27 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
                  const void* Yu, const void* Yw, void* CU, void* CW, int rr0, int* err, cudaStream_t stream) {
     using YT = typename Pol::YT;
     using OutT = typename Pol::OutT;
-    constexpr int nsmax = std::is_same<Pol, Pol64>::value ? 8 : 5;
-    constexpr bool DF = IsDF<Pol>::v;
-    constexpr int MB = MatBytes<Pol>::v;
-    constexpr int S = 3;   // chunks in the ring: one being read, two in flight
-    const Shape sh = pick_shape((int)P.max_B, Pol::CPG, nsmax);
+    constexpr int S = 3;   // stages per warp: one being read, two in flight
     const int Bmax = (int)P.max_B;
-    // steps per chunk: about 6 KB of matrix per chunk (12 KB hi + lo)
-    int G = std::max(1, (6 * 1024) / (sh.rps * Bmax * MB));
-    G = std::min(G, (Bmax + sh.rps - 1) / sh.rps);
-    const GemvLayout g = gemv_layout(Bmax, sh.rps, G, RR, S, MB, DF, sizeof(OutT), sizeof(YT));
+    const Shape sh = pick_shape(Bmax);
+    if (sh.lpr == 0) return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
+    const int rpw = 32 / sh.lpr;
+    // rows per chunk: about 4 KB of matrix (3 KB of hi + 3 KB of lo for double-float)
+    const int target = Pol::DF ? 3072 : 4096;
+    int G = std::max(1, target / (rpw * Bmax * Pol::MB));
+    G = std::min(G, (Bmax + rpw - 1) / rpw);
+    const GemvLayout g = gemv_layout(Bmax, G * rpw, RT, S, Pol::MB, Pol::DF, sizeof(YT));
+    const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
+    if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
     // bulk copies need 16-byte aligned sources (block sizes are even, so offsets keep it)
     if ((reinterpret_cast<uintptr_t>(mat_hi) | reinterpret_cast<uintptr_t>(mat_lo) | reinterpret_cast<uintptr_t>(Yu) |
          reinterpret_cast<uintptr_t>(Yw)) & 15)
         return gb_set_error(GB_BAD_ARG, "matrix and workspace pointers must be 16-byte aligned");
-    const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
-    if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
-    const long long TR = P.total_vec / P.R;
     const long long grid = std::max<long long>(1, std::min<long long>((P.nstrips * 32 + kGemvThreads - 1) / kGemvThreads,
                                                                       (long long)gb::sm_count() * 8));
-#define GB_PG(RPSV, NSV)                                                                                         \
-    if (sh.rps == RPSV && sh.ns == NSV) {                                                                        \
-        auto kfn = k_pgemv<Pol, RR, RT, RPSV, NSV, S>;                                                           \
+#define GB_PG(LPRV, CPLV)                                                                                        \
+    if (sh.lpr == LPRV && sh.cpl == CPLV) {                                                                      \
+        auto kfn = k_pgemv<Pol, RR, RT, LPRV, CPLV, S>;                                                          \
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
         gb::note_launch();                                                                                       \
@@ -1199,22 +1216,13 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
                                                             reinterpret_cast<const YT*>(Yu),                     \
                                                             reinterpret_cast<const YT*>(Yw),                     \
                                                             reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), \
-                                                            D.sp, rr0, Bmax, G, TR, err);                        \
+                                                            D.sp, rr0, Bmax, G, err);                            \
         GB_CUDA_TRY(cudaGetLastError());                                                                         \
         return GB_OK;                                                                                            \
     }
-    if constexpr (std::is_same<Pol, Pol64>::value) {
-        GB_PG(4, 1) GB_PG(2, 1) GB_PG(1, 1) GB_PG(2, 3) GB_PG(2, 5) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 5) GB_PG(1, 7)
-        GB_PG(1, 8) GB_PG(1, 2) GB_PG(1, 6)
-    } else if constexpr (std::is_same<Pol, Pol32>::value) {
-        GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(4, 5) GB_PG(2, 3) GB_PG(1, 2) GB_PG(2, 5) GB_PG(1, 4) GB_PG(1, 1)
-        GB_PG(1, 3) GB_PG(1, 5)
-    } else {
-        GB_PG(4, 1) GB_PG(2, 1) GB_PG(4, 3) GB_PG(2, 3) GB_PG(1, 2) GB_PG(1, 3) GB_PG(1, 4) GB_PG(1, 1) GB_PG(4, 5)
-        GB_PG(2, 5) GB_PG(1, 5)
-    }
+    GB_PG(8, 1) GB_PG(8, 2) GB_PG(8, 4) GB_PG(16, 3) GB_PG(16, 5) GB_PG(32, 3) GB_PG(32, 4) GB_PG(32, 5)
 #undef GB_PG
-    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d (rps %d, ns %d)", Bmax, sh.rps, sh.ns);
+    return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
 }
 
 // One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
@@ -1232,7 +1240,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     if (pol == 0) {
         gb::note_launch();
         k_yprep<0, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), 0);
+                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw));
         if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
@@ -1242,7 +1250,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     } else if (pol == 1) {
         gb::note_launch();
         k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw), 0);
+                                                     reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw));
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
@@ -1252,16 +1260,13 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     } else {
         gb::note_launch();
         k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw),
-                                                     P.total_vec / R);
-        for (int rr = 0; rr < R && P.nstrips; rr++) {
-            e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, rr, D.err, stream);
-            if (e) return e;
-        }
+                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
+        if (P.nstrips) e = launch_pgemv<PolDF, R, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, 0, D.err, stream);
+        if (e) return e;
         gb::note_launch();
-        k_reduce<double2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
-            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
-            reinterpret_cast<const double2*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+        k_reduce<float4, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float4*>(CU),
+            reinterpret_cast<const float4*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
     }
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
@@ -1763,9 +1768,8 @@ int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const doubl
             e = R == 1 ? launch_pgemv<Pol32, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s)
                        : launch_pgemv<Pol32, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s);
         } else {
-            for (int rr = 0; rr < R && !e; rr++)
-                e = R == 1 ? launch_pgemv<PolDF, 1, 1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, D.err, s)
-                           : launch_pgemv<PolDF, 1, 2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, rr, D.err, s);
+            e = R == 1 ? launch_pgemv<PolDF, 1, 1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, 0, D.err, s)
+                       : launch_pgemv<PolDF, 2, 2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, 0, D.err, s);
         }
         if (e) return e;
     }
