@@ -162,7 +162,7 @@ struct Pol64 {                 // complex128 matrix, FP64 FMAs
 struct Pol32 {                 // complex64 matrix, packed FP32 FMAs
     static constexpr int MB = 8;
     static constexpr bool DF = false;
-    using YT = float2;
+    using YT = float4;         // (re, re, im, im)
     using OutT = float2;
     struct Acc { float2 a, b; };
     struct M { float2 h; };
@@ -172,8 +172,8 @@ struct Pol32 {                 // complex64 matrix, packed FP32 FMAs
     __device__ static void zero(Acc& s) { s.a = s.b = make_float2(0, 0); }
     __device__ static void prep(M&) {}
     __device__ static void mac(Acc& s, const M& m, const YT& y) {
-        s.a = __ffma2_rn(m.h, bc(y.x), s.a);
-        s.b = __ffma2_rn(m.h, bc(y.y), s.b);
+        s.a = __ffma2_rn(m.h, make_float2(y.x, y.y), s.a);
+        s.b = __ffma2_rn(m.h, make_float2(y.z, y.w), s.b);
     }
     __device__ static OutT out(const Acc& s) { return make_float2(s.a.x - s.b.y, s.a.y + s.b.x); }
     __device__ static OutT add(OutT u, OutT v) { return make_float2(u.x + v.x, u.y + v.y); }
@@ -239,16 +239,18 @@ struct PolDF {
 // ------------------------------------------------------------ y vectors --
 // For every row (particle k, local row r) of every cluster:
 //   z = eps(r) t_k[rho(r)] x_k[rho(r)],   Yu = z,  Yw = sig(r) z
-// stored as double2 (YK 0), float2 (YK 1) or the float4 hi/lo split (YK 2).
+// stored as double2 (YK 0), float4 (re, re, im, im) (YK 1) or the float4 hi/lo
+// split (YK 2).
 template <int YK> struct YType;
 template <> struct YType<0> { using t = double2; };
-template <> struct YType<1> { using t = float2; };
+template <> struct YType<1> { using t = float4; };   // (re, re, im, im): broadcast pairs for f32x2 FMAs
 template <> struct YType<2> { using t = float4; };
 
 template <int YK> __device__ __forceinline__ typename YType<YK>::t make_y(double2 z);
 template <> __device__ __forceinline__ double2 make_y<0>(double2 z) { return z; }
-template <> __device__ __forceinline__ float2 make_y<1>(double2 z) {
-    return make_float2(__double2float_rn(z.x), __double2float_rn(z.y));
+template <> __device__ __forceinline__ float4 make_y<1>(double2 z) {
+    const float re = __double2float_rn(z.x), im = __double2float_rn(z.y);
+    return make_float4(re, re, im, im);
 }
 template <> __device__ __forceinline__ float4 make_y<2>(double2 z) {
     const float hx = __double2float_rn(z.x), hy = __double2float_rn(z.y);
@@ -334,33 +336,37 @@ __host__ __device__ inline GemvLayout gemv_layout(int Bmax, int rows_per_chunk, 
     GemvLayout g;
     g.chunk_cap = ((rows_per_chunk * Bmax * mat_bytes) + 127) & ~127;
     g.y_bytes = (Bmax * RT * y_bytes + 127) & ~127;
-    g.warp_bytes = 128 + (S + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1);
+    // + 256 B of padding: lanes whose columns lie past the block's end read (and
+    // discard) up to LPR-1 elements beyond the last stage
+    g.warp_bytes = 128 + (S + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1) + 256;
     return g;
 }
 
 // Row-lane mapping: LPR lanes share a matrix row, RPW = 32/LPR rows per step;
 // lane (ro, cl) owns the columns cl + LPR*k (k < CPL) of its row, so one y load
 // serves CPL elements and the smem reads of a row are contiguous across lanes.
-// Column sums of the RPW rows are combined by shuffles once per block.
+// Column sums of the RPW rows are combined by shuffles once per block.  A chunk
+// is G steps (G*RPW rows, the last chunk of a block may be shorter).
 // RR right-hand sides per launch (rr0 .. rr0+RR-1), RT the row stride of y and
 // of the partials.
-template <class Pol, int RR, int RT, int LPR, int CPL, int S>
+template <class Pol, int RR, int RT, int LPR, int CPL, int G, int S>
 __global__ void __launch_bounds__(kGemvThreads)
 k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long nstrips,
         const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
         const typename Pol::YT* __restrict__ Yu, const typename Pol::YT* __restrict__ Yw,
         typename Pol::OutT* __restrict__ CU, typename Pol::OutT* __restrict__ CW, const SysPlan* __restrict__ plan,
-        int rr0, int Bmax, int G, int* __restrict__ err) {
+        int rr0_rt, int Bmax, int* __restrict__ err) {
     using Acc = typename Pol::Acc;
     using OutT = typename Pol::OutT;
     using YT = typename Pol::YT;
     constexpr int MB = Pol::MB;
     constexpr bool DF = Pol::DF;
     constexpr int RPW = 32 / LPR;
+    constexpr int RC = G * RPW;   // rows per full chunk
+    const int rr0 = (RR == RT) ? 0 : rr0_rt;
     extern __shared__ __align__(128) unsigned char gemv_smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int ro = lane / LPR, cl = lane % LPR;
-    const int RC = G * RPW;   // rows per chunk
     const GemvLayout lay = gemv_layout(Bmax, RC, RT, S, MB, DF, sizeof(YT));
     unsigned char* wbase = gemv_smem + (size_t)wid * lay.warp_bytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(wbase);
@@ -374,11 +380,13 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
         for (int k = 0; k < S; k++) mbar_init(bars + k, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     __syncwarp();
-    unsigned long long gchunk = 0;   // chunks consumed by this warp (stage = % S, parity = / S)
+    // ring position: chunk number gc of this warp lives in stage gc % S, phase gc / S
+    unsigned cstage = 0, cphase = 0;      // consumer
+    unsigned pstage = 0;                  // producer (lane 0)
     const long long warp = ((long long)blockIdx.x * kGemvThreads + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     bool failed = false;
-    unsigned long long fail_lo = 0, fail_hi = 0;   // chunks possibly in flight when a wait expired
+    int in_flight = 0;                    // chunks issued and not yet consumed
     for (long long w = warp; w < nstrips && !failed; w += nwarps) {
         const Strip sp = strips[w];
         bool act = false;
@@ -386,30 +394,33 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
         for (int q = 0; q < RR; q++) act |= active_rhs<RT>(st, sp.sys, rr0 + q, mask_mode);
         if (!act) continue;
         const gb::SysDev& Sd = sys[sp.sys];
-        const int B = Sd.B, N = Sd.N;
-        const long long mat_off = Sd.mat_off, vec_off = Sd.vec_off;
+        const int B = Sd.B;
+        const long long vec_off = Sd.vec_off;
         const SysPlan& pl = plan[sp.sys];
         const int cpb = (B + RC - 1) / RC;            // chunks per block
         const int total = sp.nb * cpb;
         const unsigned ybytes = (unsigned)(B * RT * sizeof(YT));
-        auto issue = [&](int t) {   // lane 0: chunk t of the strip (+ the block's y_u with its first chunk)
-            const int b = t / cpb, c = t % cpb;
-            const long long p = sp.p0 + b;
-            const int r0 = c * RC;
+        const unsigned row_bytes = (unsigned)(B * MB);
+        // first block of the strip: pair p0 = (i, j0), j0 = i + 1 + (p0 - pair_start(i))
+        const int j0 = sp.i + 1 + (int)(sp.p0 - pair_start(sp.i, Sd.N));
+        const unsigned char* mstrip_h = mh + (Sd.mat_off + sp.p0 * (long long)B * B) * MB;
+        const unsigned char* mstrip_l = DF ? ml + (Sd.mat_off + sp.p0 * (long long)B * B) * MB : nullptr;
+        int pb = 0, pc = 0;                           // producer cursor: block, chunk within block
+        auto issue = [&]() {                          // lane 0: next chunk (+ its block's y_u with the first)
+            const int r0 = pc * RC;
             const int nrows = min(RC, B - r0);
-            const unsigned bytes = (unsigned)(nrows * B * MB);
-            const unsigned long long gc = gchunk + (unsigned long long)t;
-            uint64_t* bar = bars + (gc % S);
-            unsigned char* dst = stages + (size_t)(gc % S) * stage_stride;
-            const long long src = (mat_off + p * (long long)B * B + (long long)r0 * B) * MB;
-            const unsigned tx = bytes * (DF ? 2u : 1u) + (c == 0 ? ybytes : 0u);
-            mbar_expect_tx(bar, tx);
-            tma_1d(dst, mh + src, bytes, bar);
-            if (DF) tma_1d(dst + lay.chunk_cap, ml + src, bytes, bar);
-            if (c == 0) {
-                const int j = sp.i + 1 + (int)(p - pair_start(sp.i, N));
-                tma_1d(yring + (size_t)(b % S) * lay.y_bytes, Yu + vec_off + (long long)j * B * RT, ybytes, bar);
-            }
+            const unsigned bytes = (unsigned)nrows * row_bytes;
+            uint64_t* bar = bars + pstage;
+            unsigned char* dst = stages + (size_t)pstage * stage_stride;
+            const long long src = (long long)pb * B * row_bytes + (long long)r0 * row_bytes;
+            mbar_expect_tx(bar, bytes * (DF ? 2u : 1u) + (pc == 0 ? ybytes : 0u));
+            tma_1d(dst, mstrip_h + src, bytes, bar);
+            if (DF) tma_1d(dst + lay.chunk_cap, mstrip_l + src, bytes, bar);
+            if (pc == 0)
+                tma_1d(yring + (size_t)(pb % S) * lay.y_bytes, Yu + vec_off + (long long)(j0 + pb) * B * RT, ybytes,
+                       bar);
+            pstage = (pstage + 1 == S) ? 0 : pstage + 1;
+            if (++pc == cpb) { pc = 0; ++pb; }
         };
         {   // y_w of particle i: the same for every block of the strip
             const YT* src = Yw + vec_off + (long long)sp.i * B * RT;
@@ -421,46 +432,48 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
 #pragma unroll
             for (int q = 0; q < RR; q++) Pol::zero(cu[k][q]);
         __syncwarp();   // syw written; every stage of the previous strip consumed
-        if (lane == 0) {
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            for (int t = 0; t < S - 1 && t < total; t++) issue(t);
-        }
-        for (int t = 0; t < total; t++) {
-            const unsigned long long gc = gchunk + (unsigned long long)t;
-            if (lane == 0 && t + S - 1 < total) issue(t + S - 1);   // into the stage freed by chunk t-1
-            const bool ok = mbar_wait_bounded(bars + (gc % S), (unsigned)((gc / S) & 1));
-            if (!__all_sync(0xffffffffu, ok)) {   // warp-uniform decision
-                if (lane == 0) atomicExch(err, 1);
-                failed = true;
-                fail_lo = gc;
-                fail_hi = gchunk + (unsigned long long)min(t + S, total);
-                break;
-            }
-            const int b = t / cpb, c = t % cpb;
-            if (c == 0) {
+        if (lane == 0) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        int npre = min(S - 1, total);
+        if (lane == 0)
+            for (int t = 0; t < npre; t++) issue();
+        in_flight = npre;
+        int issued = npre;
+        for (int b = 0; b < sp.nb && !failed; b++) {
 #pragma unroll
-                for (int k = 0; k < CPL; k++)
+            for (int k = 0; k < CPL; k++)
 #pragma unroll
-                    for (int q = 0; q < RR; q++) Pol::zero(cw[k][q]);
-            }
+                for (int q = 0; q < RR; q++) Pol::zero(cw[k][q]);
             const YT* syu = reinterpret_cast<const YT*>(yring + (size_t)(b % S) * lay.y_bytes);
-            const unsigned char* stg = stages + (size_t)(gc % S) * stage_stride;
-            const int nrows = min(RC, B - c * RC);
-            const int row0 = c * RC;
-            for (int lr = ro; lr < nrows; lr += RPW) {
-                const int row = row0 + lr;
-                YT yu[RR], yw[RR];
-#pragma unroll
-                for (int q = 0; q < RR; q++) {
-                    yu[q] = syu[row * RT + rr0 + q];
-                    yw[q] = syw[row * RT + rr0 + q];
+            for (int c = 0; c < cpb; c++) {
+                if (issued < total) {   // into the stage freed by the previous chunk
+                    if (lane == 0) issue();
+                    issued++;
+                    in_flight++;
                 }
-                const unsigned rbase = (unsigned)(lr * B) * MB;
+                const bool ok = mbar_wait_bounded(bars + cstage, cphase);
+                if (!__all_sync(0xffffffffu, ok)) {   // warp-uniform decision
+                    if (lane == 0) atomicExch(err, 1);
+                    failed = true;
+                    break;
+                }
+                const unsigned char* stg = stages + (size_t)cstage * stage_stride;
+                const int row0 = c * RC;
+                const int nrows = min(RC, B - row0);
+                // One step: rows lr of the chunk.  Columns cl + LPR*k >= B (when LPR*CPL
+                // exceeds the block size) accumulate whatever follows the row in shared
+                // memory; those sums are never stored.
+                auto step = [&](int lr) {
+                    const int row = row0 + lr;
+                    YT yu[RR], yw[RR];
 #pragma unroll
-                for (int k = 0; k < CPL; k++) {
-                    const int col = cl + LPR * k;
-                    if (col < B) {
-                        typename Pol::M m = Pol::load(stg, stg + lay.chunk_cap, rbase + (unsigned)col * MB);
+                    for (int q = 0; q < RR; q++) {
+                        yu[q] = syu[row * RT + rr0 + q];
+                        yw[q] = syw[row * RT + rr0 + q];
+                    }
+                    const unsigned rbase = (unsigned)lr * row_bytes + (unsigned)cl * MB;
+#pragma unroll
+                    for (int k = 0; k < CPL; k++) {
+                        typename Pol::M m = Pol::load(stg, stg + lay.chunk_cap, rbase + LPR * k * MB);
                         Pol::prep(m);
 #pragma unroll
                         for (int q = 0; q < RR; q++) {
@@ -468,27 +481,36 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
                             Pol::mac(cw[k][q], m, yw[q]);
                         }
                     }
+                };
+                if (nrows == RC) {   // full chunk: every lane has a row in every step
+#pragma unroll
+                    for (int g = 0; g < G; g++) step(g * RPW + ro);
+                } else {
+#pragma unroll
+                    for (int g = 0; g < G; g++)
+                        if (g * RPW + ro < nrows) step(g * RPW + ro);
                 }
+                __syncwarp();   // every lane is done with this stage (and, at the block's end, its y slot)
+                if (lane == 0) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                in_flight--;
+                cstage = (cstage + 1 == S) ? 0 : cstage + 1;
+                if (cstage == 0) cphase ^= 1u;
             }
-            __syncwarp();   // every lane is done with this stage and y slot
-            if (lane == 0) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            if (c == cpb - 1) {   // block done: column partial of block row j
-                const long long p = sp.p0 + b;
-                OutT* cwp = CW + pl.cw_off + p * (long long)B * RT;
+            if (failed) break;
+            // block done: column partial of block row j
+            OutT* cwp = CW + pl.cw_off + (sp.p0 + b) * (long long)B * RT;
 #pragma unroll
-                for (int k = 0; k < CPL; k++)
+            for (int k = 0; k < CPL; k++)
 #pragma unroll
-                    for (int q = 0; q < RR; q++) {
-                        OutT v = Pol::out(cw[k][q]);
+                for (int q = 0; q < RR; q++) {
+                    OutT v = Pol::out(cw[k][q]);
 #pragma unroll
-                        for (int off = LPR; off < 32; off <<= 1) v = Pol::add(v, Pol::shfl(v, off));
-                        const int col = cl + LPR * k;
-                        if (ro == 0 && col < B) cwp[col * RT + rr0 + q] = v;
-                    }
-            }
+                    for (int off = LPR; off < 32; off <<= 1) v = Pol::add(v, Pol::shfl(v, off));
+                    const int col = cl + LPR * k;
+                    if (ro == 0 && col < B) cwp[col * RT + rr0 + q] = v;
+                }
         }
         if (failed) break;
-        gchunk += (unsigned long long)total;
         OutT* cup = CU + pl.cu_off + (w - pl.strip_base) * (long long)B * RT;
 #pragma unroll
         for (int k = 0; k < CPL; k++)
@@ -501,9 +523,12 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
                 if (ro == 0 && col < B) cup[col * RT + rr0 + q] = v;
             }
     }
-    if (failed) {   // drain: wait (bounded) for every copy this warp may still have in flight
-        for (unsigned long long gc = fail_lo; gc < fail_hi; gc++)
-            (void)mbar_wait_bounded(bars + (gc % S), (unsigned)((gc / S) & 1));
+    if (failed) {   // drain: wait (bounded) for every copy this warp still has in flight
+        for (int k = 0; k < in_flight; k++) {
+            (void)mbar_wait_bounded(bars + cstage, cphase);
+            cstage = (cstage + 1 == S) ? 0 : cstage + 1;
+            if (cstage == 0) cphase ^= 1u;
+        }
     }
 }
 
@@ -1183,6 +1208,15 @@ Shape pick_shape(int Bmax) {
     return best;
 }
 
+// Steps per chunk for a shape: chunks of about 3 KB of matrix for the block size
+// the shape is made for (LPR*CPL columns), so that three stages and four y slots
+// per warp leave room for three 4-warp CTAs per SM.
+constexpr int gemv_steps(int lpr, int cpl, int elem_bytes) {
+    return (3072 / ((32 / lpr) * lpr * cpl * elem_bytes)) < 1 ? 1
+           : (3072 / ((32 / lpr) * lpr * cpl * elem_bytes)) > 4 ? 4
+                                                                : 3072 / ((32 / lpr) * lpr * cpl * elem_bytes);
+}
+
 template <class Pol, int RR, int RT>
 int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* mat_hi, const void* mat_lo,
                  const void* Yu, const void* Yw, void* CU, void* CW, int rr0, int* err, cudaStream_t stream) {
@@ -1193,10 +1227,9 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
     const Shape sh = pick_shape(Bmax);
     if (sh.lpr == 0) return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
     const int rpw = 32 / sh.lpr;
-    // rows per chunk: about 4 KB of matrix (3 KB of hi + 3 KB of lo for double-float)
-    const int target = Pol::DF ? 3072 : 4096;
-    int G = std::max(1, target / (rpw * Bmax * Pol::MB));
-    G = std::min(G, (Bmax + rpw - 1) / rpw);
+    // steps per chunk, per shape: chunks of about 4-6 KB of matrix (half as many
+    // rows for the 16-byte formats)
+    const int G = gemv_steps(sh.lpr, sh.cpl, Pol::MB * (Pol::DF ? 2 : 1));
     const GemvLayout g = gemv_layout(Bmax, G * rpw, RT, S, Pol::MB, Pol::DF, sizeof(YT));
     const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
     if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
@@ -1208,7 +1241,8 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
                                                                       (long long)gb::sm_count() * 8));
 #define GB_PG(LPRV, CPLV)                                                                                        \
     if (sh.lpr == LPRV && sh.cpl == CPLV) {                                                                      \
-        auto kfn = k_pgemv<Pol, RR, RT, LPRV, CPLV, S>;                                                          \
+        constexpr int GV = gemv_steps(LPRV, CPLV, Pol::MB * (Pol::DF ? 2 : 1));                                                      \
+        auto kfn = k_pgemv<Pol, RR, RT, LPRV, CPLV, GV, S>;                                                      \
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
         gb::note_launch();                                                                                       \
@@ -1216,13 +1250,28 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
                                                             reinterpret_cast<const YT*>(Yu),                     \
                                                             reinterpret_cast<const YT*>(Yw),                     \
                                                             reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), \
-                                                            D.sp, rr0, Bmax, G, err);                            \
+                                                            D.sp, rr0, Bmax, err);                               \
         GB_CUDA_TRY(cudaGetLastError());                                                                         \
         return GB_OK;                                                                                            \
     }
     GB_PG(8, 1) GB_PG(8, 2) GB_PG(8, 4) GB_PG(16, 3) GB_PG(16, 5) GB_PG(32, 3) GB_PG(32, 4) GB_PG(32, 5)
 #undef GB_PG
     return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
+}
+
+// Double-float pass for R right-hand sides: one launch for both, or one per
+// right-hand side where the wide shapes (5 columns per lane) would not keep two
+// sets of double-float accumulators in registers.
+template <int R>
+int launch_df(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* hi, const void* lo,
+              const void* Yu, const void* Yw, void* CU, void* CW, cudaStream_t stream) {
+    if (R == 1 || pick_shape((int)P.max_B).cpl < 5)
+        return launch_pgemv<PolDF, R, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
+    for (int rr = 0; rr < R; rr++) {
+        const int e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
+        if (e) return e;
+    }
+    return GB_OK;
 }
 
 // One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
@@ -1250,7 +1299,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     } else if (pol == 1) {
         gb::note_launch();
         k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw));
+                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
@@ -1261,7 +1310,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         gb::note_launch();
         k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
                                                      reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
-        if (P.nstrips) e = launch_pgemv<PolDF, R, R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, 0, D.err, stream);
+        if (P.nstrips) e = launch_df<R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
         k_reduce<float4, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
@@ -1768,8 +1817,8 @@ int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const doubl
             e = R == 1 ? launch_pgemv<Pol32, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s)
                        : launch_pgemv<Pol32, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s);
         } else {
-            e = R == 1 ? launch_pgemv<PolDF, 1, 1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, 0, D.err, s)
-                       : launch_pgemv<PolDF, 2, 2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, 0, D.err, s);
+            e = R == 1 ? launch_df<1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, s)
+                       : launch_df<2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, s);
         }
         if (e) return e;
     }
