@@ -37,6 +37,11 @@ sys.path.insert(0, ROOT)
 NM = 1e-9
 TOL = 1e-8
 WORKLOAD = "random cluster N=200 lmax=4 R=2 (D=9600), n=1.5+0.01i, vacuum, 600 nm, seed 2"
+# DRAM bytes (read + write) of one k_pgemv<Pol32> launch on this workload, from one
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); summary and command in
+# profiles/k_pgemv_pol32_cluster_n200_lmax4.txt
+GEMV_TRAFFIC_BYTES = 387_552_512
+GEMV_TRAFFIC_SOURCE = "ncu: dram__bytes_read.sum 367.82 MB + dram__bytes_write.sum 19.74 MB per launch"
 
 
 # ---------------------------------------------------------------- workload --
@@ -85,7 +90,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -181,11 +186,11 @@ def run_gpu(args, rank, world):
         return evs[0].elapsed_time(evs[-1]) / 1e3, per
 
     L = nat_lib()
+    # clocks are sampled across all timed regions (mixed, FP64 and end-to-end)
     clocks = ClockSampler(dev.index).start()
     n0 = L.gb_launch_count()
     t_mixed, per_mixed = timed("mixed", args.steps)
     launches = L.gb_launch_count() - n0
-    clocks_info = clocks.stop()
     t_fp64, per_fp64 = timed("fp64", max(3, args.steps // 2))
 
     # accuracy of the mixed path against FP64, C_ext per polarisation
@@ -246,6 +251,7 @@ def run_gpu(args, rank, world):
     e1.record(stream)
     torch.cuda.synchronize()
     t_e2e = e0.elapsed_time(e1) / 1e3
+    clocks_info = clocks.stop()
     h2d = bb.h2d_bytes
     d2h = sum(o.numel() * o.element_size() for o in out)
 
@@ -265,7 +271,8 @@ def run_gpu(args, rank, world):
         e2e=dict(value=world * e2e_steps / t_e2e, unit="solves/s", h2d_bytes_per_step=int(h2d),
                  d2h_bytes_per_step=int(d2h)),
         roofline=dict(bound="hbm", achieved=mat_bytes_64 / t_gemv64 / 1e9, peak=peak, unit="GB/s",
-                      frac=mat_bytes_64 / t_gemv64 / 1e9 / peak, traffic=None,
+                      frac=mat_bytes_64 / t_gemv64 / 1e9 / peak, traffic=GEMV_TRAFFIC_BYTES,
+                      traffic_source=GEMV_TRAFFIC_SOURCE,
                       kernel="k_pgemv<Pol32> (packed complex64 matrix pass of the inner BiCGSTAB)",
                       algorithmic_bytes_per_launch=int(mat_bytes_64),
                       peak_source=peak_kind + " (MEASURED_PEAKS.json hbm_gbs, copy burst)",
