@@ -167,7 +167,9 @@ int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const doubl
  * Per cluster and right-hand side, from p_inc [D][R] (c128), p_src [D][R],
  * mie_scat / mie_int [N,2,lmax] c128:
  *   p_scat = t o p_inc,  p_int = p_inc * mie_int[:, ::-1, n-1]   (sphere_cluster.py:715-717)
- *   xs[N][R][3][2*lmax] per-multipole (Cscat, Cabs, Cext)        (cpp/src/flux.cpp:5-30)
+ *   xs[N][R][3][2*Lx] per-multipole (Cscat, Cabs, Cext)          (cpp/src/flux.cpp:5-30)
+ *      with Lx the largest lmax of the batch (a cluster of smaller lmax fills
+ *      the first 2*lmax entries of each row and leaves the rest untouched)
  *   force, torque [N][R][3]                                       (cpp/src/forces.cpp:7-137)
  * with the incident coefficients p_inc (source != 0) or p_inc - p_src
  * (source == 0) in the force/torque sums (sphere_cluster.py:521-559).

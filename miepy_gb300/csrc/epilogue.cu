@@ -4,6 +4,7 @@
 //   force and torque (Barton-type coefficient sums)          (cpp/src/forces.cpp:7-137),
 // all in FP64, reading each coefficient once.
 
+#include <algorithm>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -32,6 +33,7 @@ struct EpiArgs {
     const long long* mie_off;
     const long long* obs_off;
     int nsys, R, source;
+    int xs_L;                   // lmax stride of the xs rows (largest lmax of the batch)
     const double2* mie_scat;
     const double2* mie_int;
     const double2* p_inc;
@@ -52,8 +54,12 @@ __global__ void __launch_bounds__(128) k_epilogue(EpiArgs a, long long total) {
     const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (g >= total) return;
-    int s = 0;
-    while (s + 1 < a.nsys && a.base[s + 1] <= g) s++;
+    int s = 0, hi = a.nsys - 1;   // last cluster whose base is <= g
+    while (s < hi) {
+        const int mid = (s + hi + 1) >> 1;
+        if (a.base[mid] <= g) s = mid;
+        else hi = mid - 1;
+    }
     const gb::SysDev S = a.sys[s];
     const int R = a.R;
     const long long loc = g - a.base[s];
@@ -79,7 +85,8 @@ __global__ void __launch_bounds__(128) k_epilogue(EpiArgs a, long long total) {
     // ---- per-multipole cross-sections: lane per (a, n)
     if (a.xs) {
         const double f = 4.0 * kPi / (k * k);
-        const long long xo = ((a.obs_off[s] + i) * R + rr) * 3LL * 2 * L;
+        const int XL = a.xs_L;
+        const long long xo = ((a.obs_off[s] + i) * R + rr) * 3LL * 2 * XL;
         for (int idx = lane; idx < 2 * L; idx += 32) {
             const int aa = idx / L, n = idx % L + 1;
             double cabs = 0.0, cext = 0.0;
@@ -90,9 +97,9 @@ __global__ void __launch_bounds__(128) k_epilogue(EpiArgs a, long long total) {
                 cabs += f * ((pi_.x * ps.x + pi_.y * ps.y) - (ps.x * ps.x + ps.y * ps.y));
                 cext += f * (pr.x * ps.x + pr.y * ps.y);
             }
-            a.xs[xo + 0 * 2 * L + idx] = cext - cabs;   // scattering
-            a.xs[xo + 1 * 2 * L + idx] = cabs;          // absorption
-            a.xs[xo + 2 * 2 * L + idx] = cext;          // extinction
+            a.xs[xo + 0 * 2 * XL + idx] = cext - cabs;   // scattering
+            a.xs[xo + 1 * 2 * XL + idx] = cabs;          // absorption
+            a.xs[xo + 2 * 2 * XL + idx] = cext;          // extinction
         }
     }
     if (!a.force && !a.torque) return;
@@ -216,6 +223,8 @@ extern "C" int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const in
     a.nsys = nsys;
     a.R = R;
     a.source = source;
+    a.xs_L = 0;
+    for (int s = 0; s < nsys; s++) a.xs_L = std::max(a.xs_L, sd[s].lmax);
     a.mie_scat = reinterpret_cast<const double2*>(mie_scat);
     a.mie_int = reinterpret_cast<const double2*>(mie_int);
     a.p_inc = reinterpret_cast<const double2*>(p_inc);

@@ -351,7 +351,7 @@ __host__ __device__ inline GemvLayout gemv_layout(int Bmax, int rows_per_chunk, 
 // of the partials.
 template <class Pol, int RR, int RT, int LPR, int CPL, int G, int S>
 __global__ void __launch_bounds__(kGemvThreads)
-k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long nstrips,
+k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, long long sbeg, long long send,
         const KState* __restrict__ st, int mask_mode, const void* __restrict__ mat_hi, const void* __restrict__ mat_lo,
         const typename Pol::YT* __restrict__ Yu, const typename Pol::YT* __restrict__ Yw,
         typename Pol::OutT* __restrict__ CU, typename Pol::OutT* __restrict__ CW, const SysPlan* __restrict__ plan,
@@ -387,7 +387,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     bool failed = false;
     int in_flight = 0;                    // chunks issued and not yet consumed
-    for (long long w = warp; w < nstrips && !failed; w += nwarps) {
+    for (long long w = sbeg + warp; w < send && !failed; w += nwarps) {
         const Strip sp = strips[w];
         bool act = false;
 #pragma unroll
@@ -1022,9 +1022,15 @@ __global__ void k_cast_f(const gb::SysDev* __restrict__ sys, const Item* __restr
 }
 
 // ================================================================== host ==
+struct StripGroup {     // strips [beg, end) of clusters with block size B (one GEMV launch each)
+    int B;
+    long long beg, end;
+};
+
 struct Plan {
     int nsys = 0, R = 1, nv = 0, nr = 0;
     long long nstrips = 0, total_pairs = 0, total_vec = 0, max_B = 0, cw_elems = 0, cu_elems = 0;
+    std::vector<StripGroup> groups;
     std::vector<gb::SysDev> sd;
     std::vector<Strip> strips;
     std::vector<Item> vitems, ritems;
@@ -1050,8 +1056,15 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
     const long long J = std::max<long long>(1, std::min<long long>(8, pairs / std::max<long long>(1, 2 * warps)));
     P.sp.resize(nsys);
     long long cw_off = 0, cu_off = 0;
-    for (int s = 0; s < nsys; s++) {
+    // clusters in order of block size, so that the strips of one block size are
+    // contiguous and each size gets a GEMV launch with its own lane shape
+    std::vector<int> order(nsys);
+    for (int s = 0; s < nsys; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return P.sd[a].B < P.sd[b].B; });
+    for (int s : order) {
         const gb::SysDev& d = P.sd[s];
+        if (P.groups.empty() || P.groups.back().B != d.B)
+            P.groups.push_back(StripGroup{d.B, (long long)P.strips.size(), (long long)P.strips.size()});
         SysPlan& pl = P.sp[s];
         pl.strip_row_base = (long long)P.row_strip.size();
         pl.strip_base = (long long)P.strips.size();
@@ -1072,6 +1085,7 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
             }
         }
         P.row_strip.push_back((long long)P.strips.size());
+        P.groups.back().end = (long long)P.strips.size();
         cw_off += d.P * d.B * R;
         cu_off += ((long long)P.strips.size() - pl.strip_base) * d.B * R;
         add_items(P.vitems, s, d.D, kVRows, pl.vbeg, pl.vend);
@@ -1218,39 +1232,34 @@ constexpr int gemv_steps(int lpr, int cpl, int elem_bytes) {
 }
 
 template <class Pol, int RR, int RT>
-int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* mat_hi, const void* mat_lo,
-                 const void* Yu, const void* Yw, void* CU, void* CW, int rr0, int* err, cudaStream_t stream) {
+int launch_pgemv_group(const Plan& P, const DevPlan& D, const StripGroup& grp, const KState* st, int mask,
+                       const void* mat_hi, const void* mat_lo, const void* Yu, const void* Yw, void* CU, void* CW,
+                       int rr0, int* err, cudaStream_t stream) {
     using YT = typename Pol::YT;
     using OutT = typename Pol::OutT;
     constexpr int S = 3;   // stages per warp: one being read, two in flight
-    const int Bmax = (int)P.max_B;
+    const int Bmax = grp.B;
     const Shape sh = pick_shape(Bmax);
     if (sh.lpr == 0) return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
     const int rpw = 32 / sh.lpr;
-    // steps per chunk, per shape: chunks of about 4-6 KB of matrix (half as many
-    // rows for the 16-byte formats)
     const int G = gemv_steps(sh.lpr, sh.cpl, Pol::MB * (Pol::DF ? 2 : 1));
     const GemvLayout g = gemv_layout(Bmax, G * rpw, RT, S, Pol::MB, Pol::DF, sizeof(YT));
     const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
     if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
-    // bulk copies need 16-byte aligned sources (block sizes are even, so offsets keep it)
-    if ((reinterpret_cast<uintptr_t>(mat_hi) | reinterpret_cast<uintptr_t>(mat_lo) | reinterpret_cast<uintptr_t>(Yu) |
-         reinterpret_cast<uintptr_t>(Yw)) & 15)
-        return gb_set_error(GB_BAD_ARG, "matrix and workspace pointers must be 16-byte aligned");
-    const long long grid = std::max<long long>(1, std::min<long long>((P.nstrips * 32 + kGemvThreads - 1) / kGemvThreads,
+    const long long n = grp.end - grp.beg;
+    const long long grid = std::max<long long>(1, std::min<long long>((n * 32 + kGemvThreads - 1) / kGemvThreads,
                                                                       (long long)gb::sm_count() * 8));
 #define GB_PG(LPRV, CPLV)                                                                                        \
     if (sh.lpr == LPRV && sh.cpl == CPLV) {                                                                      \
-        constexpr int GV = gemv_steps(LPRV, CPLV, Pol::MB * (Pol::DF ? 2 : 1));                                                      \
+        constexpr int GV = gemv_steps(LPRV, CPLV, Pol::MB * (Pol::DF ? 2 : 1));                                  \
         auto kfn = k_pgemv<Pol, RR, RT, LPRV, CPLV, GV, S>;                                                      \
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
         gb::note_launch();                                                                                       \
-        kfn<<<(unsigned)grid, kGemvThreads, smem, stream>>>(D.sys, D.strips, P.nstrips, st, mask, mat_hi, mat_lo,  \
-                                                            reinterpret_cast<const YT*>(Yu),                     \
-                                                            reinterpret_cast<const YT*>(Yw),                     \
-                                                            reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), \
-                                                            D.sp, rr0, Bmax, err);                               \
+        kfn<<<(unsigned)grid, kGemvThreads, smem, stream>>>(                                                     \
+            D.sys, D.strips, grp.beg, grp.end, st, mask, mat_hi, mat_lo, reinterpret_cast<const YT*>(Yu),         \
+            reinterpret_cast<const YT*>(Yw), reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), D.sp, rr0, \
+            Bmax, err);                                                                                          \
         GB_CUDA_TRY(cudaGetLastError());                                                                         \
         return GB_OK;                                                                                            \
     }
@@ -1259,13 +1268,33 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
     return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
 }
 
+// The matrix pass: one launch per block-size group of the batch, each with the
+// lane shape of its block size.
+template <class Pol, int RR, int RT>
+int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* mat_hi, const void* mat_lo,
+                 const void* Yu, const void* Yw, void* CU, void* CW, int rr0, int* err, cudaStream_t stream) {
+    // bulk copies need 16-byte aligned sources (block sizes are even, so offsets keep it)
+    if ((reinterpret_cast<uintptr_t>(mat_hi) | reinterpret_cast<uintptr_t>(mat_lo) | reinterpret_cast<uintptr_t>(Yu) |
+         reinterpret_cast<uintptr_t>(Yw)) & 15)
+        return gb_set_error(GB_BAD_ARG, "matrix and workspace pointers must be 16-byte aligned");
+    for (const StripGroup& grp : P.groups) {
+        if (grp.end == grp.beg) continue;
+        const int e = launch_pgemv_group<Pol, RR, RT>(P, D, grp, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, rr0, err,
+                                                      stream);
+        if (e) return e;
+    }
+    return GB_OK;
+}
+
 // Double-float pass for R right-hand sides: one launch for both, or one per
 // right-hand side where the wide shapes (5 columns per lane) would not keep two
 // sets of double-float accumulators in registers.
 template <int R>
 int launch_df(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* hi, const void* lo,
               const void* Yu, const void* Yw, void* CU, void* CW, cudaStream_t stream) {
-    if (R == 1 || pick_shape((int)P.max_B).cpl < 5)
+    bool wide = false;
+    for (const StripGroup& grp : P.groups) wide |= pick_shape(grp.B).cpl >= 5;
+    if (R == 1 || !wide)
         return launch_pgemv<PolDF, R, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
     for (int rr = 0; rr < R; rr++) {
         const int e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);

@@ -187,52 +187,33 @@ class ClusterBatch:
         return y
 
     def epilogue(self, eps_b, source=True, want_fields=True):
-        """p_scat, p_int (device, [total_vec]) and per particle xs [N,R,3,2lmax], force/torque [N,R,3]."""
+        """p_scat, p_int (device, [total_vec]) and per particle xs [N,R,3,2*Lx]
+        (Lx: the batch's largest lmax; a cluster of smaller lmax fills the first
+        2*lmax entries, the rest stay zero), force/torque [N,R,3]."""
         L = nat.lib()
         dev = self.device
         n_obs = self.totals["obs"]
-        lmaxes = [l["lmax"] for l in self.layout]
-        if len(set(lmaxes)) != 1:
-            xs_len = sum(l["N"] * self.R * 6 * l["lmax"] for l in self.layout)
-        else:
-            xs_len = n_obs * self.R * 6 * lmaxes[0]
+        self.xs_L = max(l["lmax"] for l in self.layout)
+        ragged = any(l["lmax"] != self.xs_L for l in self.layout)
         self.p_scat = torch.empty_like(self.x) if want_fields else None
         self.p_int = torch.empty_like(self.x) if want_fields else None
-        # xs offsets assume a common lmax per batch; ragged batches get per-cluster calls
-        out = []
-        if len(set(lmaxes)) == 1:
-            xs = torch.empty(max(xs_len, 1), dtype=torch.float64, device=dev)
-            F = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
-            T = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
-            nat.check(L.gb_epilogue_batch(self.nsys, self.sys, self.R, self.mie_off.ctypes.data,
-                                          self.obs_off.ctypes.data, nat.ptr(self.mie_scat), nat.ptr(self.mie_int),
-                                          nat.ptr(self.x), nat.ptr(self.b), float(np.real(eps_b)), int(bool(source)),
-                                          nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
-                                          nat.ptr(T), current_stream(dev)), "epilogue")
-            self.xs, self.F, self.T = xs, F, T
-            return self
-        # ragged lmax: obs offsets in units of particles of each cluster's own lmax
-        xs_parts, F_parts, T_parts = [], [], []
-        for s, l in enumerate(self.layout):
-            sub = nat.systems_array([tuple(getattr(self.sys[s], f) for f, _ in nat.gb_system._fields_)])
-            xs = torch.empty(l["N"] * self.R * 6 * l["lmax"], dtype=torch.float64, device=dev)
-            F = torch.empty(l["N"] * self.R * 3, dtype=torch.float64, device=dev)
-            T = torch.empty(l["N"] * self.R * 3, dtype=torch.float64, device=dev)
-            mo = np.asarray([l["mie_off"]], dtype=np.int64)
-            oo = np.zeros(1, dtype=np.int64)
-            nat.check(L.gb_epilogue_batch(1, sub, self.R, mo.ctypes.data, oo.ctypes.data, nat.ptr(self.mie_scat),
-                                          nat.ptr(self.mie_int), nat.ptr(self.x), nat.ptr(self.b),
-                                          float(np.real(eps_b[s] if np.ndim(eps_b) else eps_b)), int(bool(source)),
-                                          nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
-                                          nat.ptr(T), current_stream(dev)), "epilogue")
-            xs_parts.append(xs)
-            F_parts.append(F)
-            T_parts.append(T)
-            out.append(xs)
-        self.xs = torch.cat(xs_parts)
-        self.F = torch.cat(F_parts)
-        self.T = torch.cat(T_parts)
+        alloc = torch.zeros if ragged else torch.empty
+        xs = alloc(max(n_obs * self.R * 6 * self.xs_L, 1), dtype=torch.float64, device=dev)
+        F = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
+        T = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
+        nat.check(L.gb_epilogue_batch(self.nsys, self.sys, self.R, self.mie_off.ctypes.data,
+                                      self.obs_off.ctypes.data, nat.ptr(self.mie_scat), nat.ptr(self.mie_int),
+                                      nat.ptr(self.x), nat.ptr(self.b), float(np.real(eps_b)), int(bool(source)),
+                                      nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
+                                      nat.ptr(T), current_stream(dev)), "epilogue")
+        self.xs, self.F, self.T = xs, F, T
         return self
+
+    def cross_sections(self, s):
+        """Total (C_sca, C_abs, C_ext) of cluster s per right-hand side: [R, 3] (device)."""
+        l = self.layout[s]
+        xs = self.xs[: self.totals["obs"] * self.R * 6 * self.xs_L].view(-1, self.R, 3, 2 * self.xs_L)
+        return xs[l["obs_off"]: l["obs_off"] + l["N"], :, :, : 2 * l["lmax"]].sum(dim=(0, 3))
 
     # ------------------------------------------------------------- accessors --
     def cluster_view(self, s, t):
