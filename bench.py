@@ -349,8 +349,17 @@ def run_sweep(args):
             evs[k + 1].record(stream)
         torch.cuda.synchronize()
         per = np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(steps)])
+        # phase split of one more step (events between the phases)
+        ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ph[0].record(stream); b.assemble(); ph[1].record(stream)
+        b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); ph[2].record(stream)
+        b.epilogue(1.0); ph[3].record(stream)
+        torch.cuda.synchronize()
+        phases = dict(assemble_ms=ph[0].elapsed_time(ph[1]), solve_ms=ph[1].elapsed_time(ph[2]),
+                      epilogue_ms=ph[2].elapsed_time(ph[3]))
         cext = np.array([b.cross_sections(s)[0, 2].item() for s in range(len(specs))])
         out = dict(t=evs[0].elapsed_time(evs[-1]) / 1e3, per=per, launches=L.gb_launch_count() - n0, cext=cext,
+                   phases=phases,
                    status=b.status.copy(), iters=b.iters.copy(), mat_bytes=sum(
                        (t.numel() * t.element_size()) for t in (b.mat128, b.mat64, b.mat64lo) if t is not None))
         del b
@@ -369,13 +378,90 @@ def run_sweep(args):
                 fp64_solves_per_s=W / d["t"], cext_rel_err_mixed_vs_fp64=err,
                 all_converged=bool(np.all(m["status"] == 0) and np.all(d["status"] == 0)),
                 lmax_histogram={int(l): int(np.sum(lm == l)) for l in np.unique(lm)},
-                resident_matrix_gb=m["mat_bytes"] / 1e9, gpu_launches=int(m["launches"]), clocks=clocks_info)
+                resident_matrix_gb=m["mat_bytes"] / 1e9, gpu_launches=int(m["launches"]),
+                phases_mixed=m["phases"], phases_fp64=d["phases"], clocks=clocks_info)
+
+
+# --------------------------------------------------------- serving stream --
+SERVE_WORKLOAD = ("serving stream: seeded requests (seed 4), N log-uniform 2-500, lmax uniform 2-8, index "
+                  "U[1.3,2.5]+iU[0,0.1], radii 50-100 nm at constant density, 600 nm, vacuum, plane wave or "
+                  "Gaussian beam (waist 1 um) 50/50; Poisson arrivals")
+
+
+def run_serve(args):
+    """Throughput at saturation (all requests queued at once) and latency at a
+    Poisson arrival rate of half that throughput, mixed precision; FP64 throughput
+    on the same requests."""
+    import torch
+    from miepy_gb300 import server as SV
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(4)
+    nreq = max(8, args.requests)
+    reqs = [SV.random_request(rng, rid=i) for i in range(nreq)]
+    L = nat_lib()
+
+    def saturate(precision, rs):
+        with SV.SolveServer(precision=precision, tol=TOL, max_waves=3, max_wave_requests=16) as srv:
+            t0 = time.perf_counter()
+            futs = [srv.submit(r) for r in rs]
+            out = [f.result() for f in futs]
+            t = time.perf_counter() - t0
+            stats = dict(srv.stats)
+        return t, out, stats
+
+    # warm-up: tables of every lmax and the kernels (one small request per lmax)
+    warm = [SV.random_request(np.random.default_rng(100 + l), rid=-1, n_range=(4, 6), lmax_range=(l, l))
+            for l in range(2, 9)]
+    for p in ("mixed", "fp64"):
+        saturate(p, warm)
+    clocks = ClockSampler(dev.index).start()
+    n0 = L.gb_launch_count()
+    t_sat, res_sat, st_sat = saturate("mixed", reqs)
+    launches = L.gb_launch_count() - n0
+    rate = 0.5 * nreq / t_sat
+    arr = np.cumsum(np.random.default_rng(44).exponential(1.0 / rate, size=nreq))
+    with SV.SolveServer(precision="mixed", tol=TOL, max_waves=3, max_wave_requests=16) as srv:
+        t0 = time.perf_counter()
+        futs = []
+        for r, ta in zip(reqs, arr):
+            dt = t0 + ta - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            futs.append(srv.submit(r))
+        res_poi = [f.result() for f in futs]
+        t_poi = time.perf_counter() - t0
+        st_poi = dict(srv.stats)
+    n64 = min(nreq, max(8, args.requests // 2))
+    t_64, res_64, _ = saturate("fp64", reqs[:n64])
+    t_m64, res_m64, _ = saturate("mixed", reqs[:n64])
+    clocks_info = clocks.stop()
+    lat = np.array([r.latency for r in res_poi]) * 1e3
+    lat_sat = np.array([r.latency for r in res_sat]) * 1e3
+    err = max(abs(a.C_ext - b.C_ext) / abs(b.C_ext) for a, b in zip(res_m64, res_64))
+    sizes = [(len(np.asarray(r.radius)), r.lmax) for r in reqs]
+    return dict(value=nreq / t_sat, ms_per_step=1e3 * t_sat / nreq,
+                p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
+                poisson=dict(rate_per_s=rate, achieved_solves_per_s=nreq / t_poi, p50_ms=float(np.percentile(lat, 50)),
+                             p99_ms=float(np.percentile(lat, 99)), waves=st_poi["waves"],
+                             max_concurrent_waves=st_poi["max_concurrent_waves"]),
+                saturation=dict(solves_per_s=nreq / t_sat, p50_ms=float(np.percentile(lat_sat, 50)),
+                                p99_ms=float(np.percentile(lat_sat, 99)), waves=st_sat["waves"],
+                                max_concurrent_waves=st_sat["max_concurrent_waves"],
+                                peak_hbm_gb=st_sat["peak_bytes"] / 1e9),
+                fp64_solves_per_s=n64 / t_64, mixed_solves_per_s_same_subset=n64 / t_m64,
+                cext_rel_err_mixed_vs_fp64=float(err),
+                all_converged=bool(all(r.status == 0 for r in res_sat + res_poi + res_64)),
+                requests=nreq, largest_request=dict(N=int(max(sizes)[0]), lmax=int(max(s[1] for s in sizes))),
+                gpu_launches=int(launches), clocks=clocks_info)
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="cluster", choices=["cluster", "sweep"],
-                    help="cluster: the headline N=200 cluster; sweep: the 256-wavelength Drude sweep")
+    ap.add_argument("--config", default="cluster", choices=["cluster", "sweep", "serve"],
+                    help="cluster: the headline N=200 cluster; sweep: the 256-wavelength Drude sweep; "
+                         "serve: the request stream through the solve server")
+    ap.add_argument("--requests", type=int, default=48, help="requests in the serving stream")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -414,6 +500,17 @@ def main():
         return
 
     import torch
+    if args.config == "serve":
+        if rank == 0:
+            res = run_serve(args)
+            line = dict(base, metric="cluster solves/s + p99 latency, mixed vs FP64 GPU, serving stream",
+                        unit="solves/s", impl="gb300", dtype="c64 BiCGSTAB + double-float refinement residual",
+                        data="synthetic (seeded request stream)", cpu_baseline=None,
+                        config=dict(workload=SERVE_WORKLOAD, solve_tol=TOL, rhs=1,
+                                    batching="continuous (waves admitted by HBM budget, 3 concurrent streams)"),
+                        **res)
+            print(json.dumps(line))
+        return
     if args.config == "sweep":
         if rank == 0:
             res = run_sweep(args)

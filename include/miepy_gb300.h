@@ -208,6 +208,17 @@ int gb_near_field(int N, int lmax, const double* pos, const double* radius, cons
                   const double* p_int, double k, const double* k_int, int Npts, const double* pts, int interior,
                   int magnetic, double hfac_re, double hfac_im, const double* hfac_int, double* out, void* stream);
 
+/* ------------------------------------------------------------ beam source --
+ * Beam expansion coefficients at N particles from the beam's far-field
+ * projection: replaces integrate_phase, cpp/src/decomposition.cpp:29-66, as
+ * applied per particle by beam.structure, sources/beams.py:168-200.
+ *   pos [N,3] f64 (positions relative to the beam centre), rhat [G,3] f64 far-field
+ *   directions, w [G][ncol] c128 the projected angular spectrum times the
+ *   trapezoid weights of the (theta, phi) grid, ncol = 2*rmax columns (a*rmax + r);
+ *   out[(i*ncol + c) * out_stride] = sum_g w[g][c] exp(-i k rhat_g . pos_i)  (c128). */
+int gb_beam_project(int N, int ncol, int G, const double* pos, const double* rhat, const double* w, double k,
+                    double* out, int out_stride, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

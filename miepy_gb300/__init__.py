@@ -7,7 +7,8 @@ The compute path is the CUDA extension in csrc/, reached through the C ABI of
 include/miepy_gb300.h.
 """
 
-from . import backend, materials as _materials_mod, sources
+from . import backend, beams, materials as _materials_mod, sources, sweep
+from .beams import gaussian_beam
 from .cluster import cross_sections, solver, sphere_cluster
 from .engine import ClusterBatch, footprint_bytes
 from .materials import (constant_material, dielectric, drude_material, function_material, material_struct,
@@ -15,6 +16,8 @@ from .materials import (constant_material, dielectric, drude_material, function_
 from .mie import mie_coefficients
 from .modes import lmax_to_rmax, mode_indices, reduced_index, rmax_to_lmax
 from .sources import plane_wave
+
+sources.gaussian_beam = gaussian_beam
 
 __version__ = "1.0.0"
 

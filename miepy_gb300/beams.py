@@ -1,0 +1,155 @@
+"""Beam sources: Gaussian beams and their expansion coefficients at the particles.
+
+The decomposition follows the reference's far-field integral method:
+
+* theta_cutoff / E0 / scalar_angular_spectrum of gaussian_beam
+  (sources/common.py:10-52) and the polarised angular spectrum
+  (sources/sources.py:188-195);
+* integral_project_source_far (vsh/decomposition.py:284-325): on a 20 x 40
+  (theta, phi) far-field grid over [pi - theta_c, pi] x [0, 2 pi], project the
+  angular spectrum onto the ingoing far-field VSHs N_mn, M_mn (vsh/vsh_functions.py:
+  81-109) to get p0[a, r, theta, phi];
+* integrate_phase (cpp/src/decomposition.cpp:29-66) per particle: the 2-D
+  trapezoid integral of p0 times exp(-i k rhat . x_i).
+
+The per-(k, lmax) projection p0 is a small host computation (numpy, cached on the
+beam as in the reference); the per-particle integrals, which dominate for many
+particles, run on the GPU in one launch (gb_beam_project).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+from scipy.constants import physical_constants
+from scipy.special import erfc
+
+from . import _native as nat
+from .modes import lmax_to_rmax, mode_indices
+from .special import Emn, pi_func, tau_func
+from .sources import sph_basis_vectors
+
+Z0 = physical_constants["characteristic impedance of vacuum"][0]
+
+
+def _trapz_weights(x):
+    """Weights of the composite trapezoid rule on the nodes x."""
+    x = np.asarray(x, float)
+    w = np.zeros_like(x)
+    d = np.diff(x)
+    w[:-1] += d / 2
+    w[1:] += d / 2
+    return w
+
+
+class gaussian_beam:
+    """Gaussian beam (sources/common.py:10-52) propagating along +z."""
+
+    def __init__(self, width, polarization, power=1, theta_max=np.pi / 2, phase=0, center=None, theta=0, phi=0,
+                 standing=False):
+        if theta != 0 or phi != 0:
+            raise NotImplementedError("rotated beams are not on the GPU path (propagation along +z only)")
+        if standing:
+            raise NotImplementedError("standing beams are not on the sphere-cluster path")
+        self.width = width
+        self.polarization = np.asarray(polarization, dtype=complex)
+        self.polarization = self.polarization / np.linalg.norm(self.polarization)
+        self.power = power
+        self.theta_max = theta_max
+        self.phase = phase
+        self.center = np.zeros(3) if center is None else np.asarray(center, float)
+        self.theta = theta
+        self.phi = phi
+        self.amplitude = 1
+        self._cache = {}
+
+    def __repr__(self):
+        return (f"gaussian_beam(width={self.width}, polarization={self.polarization}, power={self.power}, "
+                f"center={self.center}, theta={self.theta}, phi={self.phi})")
+
+    # ---------------------------------------------------- angular spectrum --
+    def E0(self, k):
+        c = 0.5 * (k * self.width) ** 2
+        if c < 700:
+            U0 = np.sqrt(Z0 * self.power / (np.pi * (1 - np.sqrt(np.pi * c) * np.exp(c) * erfc(np.sqrt(c)))))
+        else:
+            U0 = np.sqrt(Z0 * self.power / (np.pi * (1 / (2 * c) - 3 / (4 * c ** 2) + 15 / (8 * c ** 3))))
+        return U0
+
+    def scalar_angular_spectrum(self, theta, phi, k):
+        return np.exp(-((k * self.width * np.tan(theta) / 2) ** 2))
+
+    def angular_spectrum(self, theta, phi, k):
+        U = self.scalar_angular_spectrum(theta, phi, k)
+        Ex = U * self.polarization[0]
+        Ey = U * self.polarization[1]
+        return np.array([-Ex * np.cos(phi) - Ey * np.sin(phi), -Ex * np.sin(phi) + Ey * np.cos(phi)], dtype=complex)
+
+    def theta_cutoff(self, k, cutoff=1e-6, tol=None):
+        arg = np.sqrt(-2 * np.log(cutoff)) / (k * self.width)
+        theta_c = np.pi / 2 if arg >= 1 else np.arctan(arg)
+        return min(self.theta_max, theta_c, np.pi / 2 - 1e-5)
+
+    # ------------------------------------------------------- decomposition --
+    def far_projection(self, k, lmax, sampling=20):
+        """(rhat [G,3], w [G, 2*rmax] c128): the ingoing-VSH projection p0 of the
+        angular spectrum on the far-field grid, times the trapezoid weights."""
+        key = (float(k), int(lmax), int(sampling))
+        if key in self._cache:
+            return self._cache[key]
+        theta_0 = np.pi - self.theta_cutoff(k)
+        theta = np.linspace(theta_0, np.pi, sampling)
+        phi = np.linspace(0, 2 * np.pi, 2 * sampling)
+        THETA, PHI = np.meshgrid(theta, phi, indexing="ij")
+        rad = 1
+        rhat = sph_basis_vectors(THETA, PHI)[0]
+        Esrc = self.angular_spectrum(THETA, PHI, k) * np.exp(-1j * k) / rad
+        E0 = self.E0(k) * np.exp(1j * self.phase)
+        rmax = lmax_to_rmax(lmax)
+        p0 = np.zeros((2, rmax) + THETA.shape, dtype=complex)
+        z = k * rad
+        sin_t = np.sin(THETA)
+        for r, n, m in mode_indices(lmax):
+            factor = E0 * k ** 2 * 1j ** (2 - n) * np.abs(Emn(m, n)) / (4 * np.pi)
+            zn = np.exp(-1j * (z - (n + 1) * np.pi / 2)) / z      # ingoing far-field radial factor
+            tau = tau_func(n, m, THETA)
+            pi_ = pi_func(n, m, THETA)
+            eph = np.exp(1j * m * PHI)
+            fN = -zn * eph                                        # ingoing N carries a minus sign
+            N = np.array([1j * tau * fN, -pi_ * fN])
+            fM = zn * eph
+            M = np.array([1j * pi_ * fM, -tau * fM])
+            p0[0, r] = 2 * factor * np.sum(Esrc * np.conjugate(N), axis=0) * sin_t * rad ** 2
+            p0[1, r] = 2 * factor * np.sum(Esrc * np.conjugate(M), axis=0) * sin_t * rad ** 2
+        wgt = _trapz_weights(theta)[:, None] * _trapz_weights(phi)[None, :]          # [T, P]
+        w = (p0 * wgt).reshape(2 * rmax, -1).T                                      # [G, 2*rmax]
+        out = (np.ascontiguousarray(rhat.reshape(3, -1).T), np.ascontiguousarray(w))
+        self._cache[key] = out
+        return out
+
+    def structure_device(self, position, k, lmax, out=None, out_stride=1, device=None):
+        """p_src [N, 2, rmax] computed on the GPU into ``out`` (a device complex128
+        tensor; element (i, c) at (i*2*rmax + c) * out_stride) or a new tensor."""
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        pos = np.asarray(position, float).reshape(-1, 3) - self.center
+        N = pos.shape[0]
+        rmax = lmax_to_rmax(lmax)
+        rhat, w = self.far_projection(k, lmax)
+        d_pos = torch.from_numpy(np.ascontiguousarray(pos)).to(dev)
+        d_rhat = torch.from_numpy(rhat).to(dev)
+        d_w = torch.from_numpy(w).to(dev)
+        if out is None:
+            out = torch.empty(N * 2 * rmax, dtype=torch.complex128, device=dev)
+            out_stride = 1
+        nat.check(nat.lib().gb_beam_project(N, 2 * rmax, rhat.shape[0], nat.ptr(d_pos), nat.ptr(d_rhat),
+                                            nat.ptr(d_w), float(k), nat.ptr(out), int(out_stride),
+                                            torch.cuda.current_stream(dev).cuda_stream), "beam projection")
+        # keep the inputs alive until the kernel has run
+        out._beam_inputs = (d_pos, d_rhat, d_w)
+        return out
+
+    def structure(self, position, k, lmax):
+        """p_src [N, 2, rmax] (host numpy), computed on the GPU."""
+        N = np.asarray(position, float).reshape(-1, 3).shape[0]
+        out = self.structure_device(position, k, lmax)
+        return out.cpu().numpy().reshape(N, 2, lmax_to_rmax(lmax))

@@ -38,7 +38,7 @@ __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
 
 struct AsmSmem {
     int PM, MU, M;
-    size_t off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
+    size_t off_geo, off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
 };
 
 __host__ __device__ inline AsmSmem asm_layout(int L, int M, bool want64) {
@@ -47,6 +47,7 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, bool want64) {
     s.MU = 4 * L + 1;
     s.M = M;
     size_t o = 0;
+    s.off_geo = o; o += sizeof(double) * 8;
     s.off_h = o;  o += sizeof(double2) * s.PM;
     s.off_e = o;  o += sizeof(double2) * s.MU;
     s.off_G = o;  o += sizeof(double2) * s.PM * s.MU;
@@ -101,22 +102,33 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         const long long p = g - pair_base[s];
         int i, j;
         pair_ij(p, N, i, j);
-        const double* pi_ = pos + S.pos_off + 3 * (long long)i;
-        const double* pj_ = pos + S.pos_off + 3 * (long long)j;
-        const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
-        // direction cosines straight from the separation vector (the reference goes
-        // through acos/atan2 and back; the values agree to rounding)
-        const double rho2 = dx * dx + dy * dy;
-        const double rad = sqrt(rho2 + dz * dz);
-        const double inv_r = 1.0 / rad;
-        const double x = dz * inv_r;                       // cos(theta)
-        const double u = sqrt(rho2) * inv_r;               // sin(theta) >= 0
-        double cphi = 1.0, sphi = 0.0;                     // phi = atan2(dy, dx) = 0 on the z axis
-        if (rho2 > 0.0) {
-            const double inv_rho = 1.0 / sqrt(rho2);
-            cphi = dx * inv_rho;
-            sphi = dy * inv_rho;
+        // geometry once per pair (one thread; FP64 sqrt/division are slow on this
+        // part's FP64 pipe): r, cos/sin theta, cos/sin phi straight from the
+        // separation vector (the reference goes through acos/atan2 and back; the
+        // values agree to rounding)
+        double* geo = reinterpret_cast<double*>(smem + lay.off_geo);
+        if (tid == 0) {
+            const double* pi_ = pos + S.pos_off + 3 * (long long)i;
+            const double* pj_ = pos + S.pos_off + 3 * (long long)j;
+            const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
+            const double rho2 = dx * dx + dy * dy;
+            const double rad = sqrt(rho2 + dz * dz);
+            const double inv_r = 1.0 / rad;
+            double cphi = 1.0, sphi = 0.0;                 // phi = atan2(dy, dx) = 0 on the z axis
+            const double rho = sqrt(rho2);
+            if (rho2 > 0.0) {
+                const double inv_rho = 1.0 / rho;
+                cphi = dx * inv_rho;
+                sphi = dy * inv_rho;
+            }
+            geo[0] = rad;
+            geo[1] = dz * inv_r;                           // cos(theta)
+            geo[2] = rho * inv_r;                          // sin(theta) >= 0
+            geo[3] = cphi;
+            geo[4] = sphi;
         }
+        __syncthreads();
+        const double rad = geo[0], x = geo[1], u = geo[2], cphi = geo[3], sphi = geo[4];
 
         // ---- phase 1: Hankel, Legendre, azimuthal phases
         if (tid == 32) {
@@ -412,10 +424,10 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     const size_t smem = lay.total;
     int per_sm = 1;
     if (dense) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(k_assemble<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(k_assemble<true>), smem));
         GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<true>, kAsmThreads, smem));
     } else {
-        GB_CUDA_TRY(cudaFuncSetAttribute(k_assemble<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(k_assemble<false>), smem));
         GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<false>, kAsmThreads, smem));
     }
     if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);

@@ -2,6 +2,9 @@
 
 #include <atomic>
 #include <cstdarg>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <cstdio>
 #include <cstring>
 
@@ -23,6 +26,23 @@ void note_launch() {
 void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 void capture_begin() { g_capturing = 1; g_captured = 0; }
 long long capture_end() { g_capturing = 0; return g_captured; }
+
+// The dynamic shared-memory limit is an attribute of the kernel, shared by every
+// host thread: raise it, never lower it, so that a launch on one thread cannot find
+// the limit lowered by another thread's smaller launch.
+cudaError_t ensure_dynamic_smem(const void* func, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> set;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = set[{dev, func}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
 }   // namespace gb
 
 int gb_set_error(int code, const char* fmt, ...) {

@@ -29,6 +29,9 @@ int sm_count();
 
 // Kernel-launch accounting (gb_launch_count): direct launches call note_launch;
 // launches recorded into a CUDA graph are counted once per graph replay.
+// Raises (never lowers) a kernel's dynamic shared-memory limit, thread-safely.
+cudaError_t ensure_dynamic_smem(const void* func, size_t bytes);
+
 void note_launch();
 void note_launches(long long n);
 void capture_begin();

@@ -1254,7 +1254,7 @@ int launch_pgemv_group(const Plan& P, const DevPlan& D, const StripGroup& grp, c
         constexpr int GV = gemv_steps(LPRV, CPLV, Pol::MB * (Pol::DF ? 2 : 1));                                  \
         auto kfn = k_pgemv<Pol, RR, RT, LPRV, CPLV, GV, S>;                                                      \
         if (smem > 48 * 1024)                                                                                    \
-            GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));      \
+            GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));      \
         gb::note_launch();                                                                                       \
         kfn<<<(unsigned)grid, kGemvThreads, smem, stream>>>(                                                     \
             D.sys, D.strips, grp.beg, grp.end, st, mask, mat_hi, mat_lo, reinterpret_cast<const YT*>(Yu),         \
@@ -1353,7 +1353,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
 // ----------------------------------------------------------- graph cache --
 struct GraphKey {
     const void* a[12];
-    long long n[8];
+    long long n[10];
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
 struct GraphKeyHash {
@@ -1366,21 +1366,59 @@ struct GraphKeyHash {
 };
 struct GraphEntry {
     cudaGraphExec_t exec;
-    long long kernels;   // kernel nodes per replay
+    long long kernels;        // kernel nodes per replay
+    int inuse;                // solves replaying it right now (other host threads included)
+    unsigned long long last;  // use stamp, for eviction of the least recently used
 };
 struct GraphCache {
     std::mutex mu;
     std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> map;
-    cudaStream_t cap[64] = {nullptr};
+    unsigned long long clock = 0;
+    // drop least recently used graphs that no solve is replaying, down to keep entries
+    void evict(size_t keep) {
+        while (map.size() > keep) {
+            auto victim = map.end();
+            for (auto it = map.begin(); it != map.end(); ++it)
+                if (it->second.inuse == 0 && (victim == map.end() || it->second.last < victim->second.last)) victim = it;
+            if (victim == map.end()) return;
+            cudaGraphExecDestroy(victim->second.exec);
+            map.erase(victim);
+        }
+    }
 };
 GraphCache g_graphs;
 
+// Marks a cached graph in use for the lifetime of one solve.
+struct GraphUse {
+    GraphKey key{};
+    bool held = false;
+    ~GraphUse() {
+        if (!held) return;
+        std::lock_guard<std::mutex> lk(g_graphs.mu);
+        auto f = g_graphs.map.find(key);
+        if (f != g_graphs.map.end()) f->second.inuse--;
+    }
+};
+
+// FNV-1a over the block-size groups of a plan (each group is one GEMV launch in a graph)
+long long groups_hash(const Plan& P) {
+    unsigned long long h = 1469598103934665603ull;
+    for (const StripGroup& g : P.groups) {
+        const long long v[3] = {g.B, g.beg, g.end};
+        const unsigned char* b = reinterpret_cast<const unsigned char*>(v);
+        for (size_t i = 0; i < sizeof(v); i++) h = (h ^ b[i]) * 1099511628211ull;
+    }
+    return (long long)h;
+}
+
+// Capture stream of the calling host thread on the current device: concurrent
+// solves on different host threads capture on different streams.
 cudaStream_t capture_stream() {
+    thread_local cudaStream_t cap[64] = {nullptr};
     int dev = 0;
     cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lk(g_graphs.mu);
-    if (!g_graphs.cap[dev & 63]) cudaStreamCreateWithFlags(&g_graphs.cap[dev & 63], cudaStreamNonBlocking);
-    return g_graphs.cap[dev & 63];
+    if (!cap[dev & 63]) cudaStreamCreateWithFlags(&cap[dev & 63], cudaStreamNonBlocking);
+    return cap[dev & 63];
 }
 
 // ------------------------------------------------------------- BiCGSTAB run --
@@ -1452,6 +1490,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     // a chunk of iterations, captured once per argument set and replayed
     cudaGraphExec_t exec = nullptr;
     long long exec_kernels = 0;
+    GraphUse use;
     if (use_graph) {
         GraphKey key{};
         const void* a[12] = {base, mat, tvec, D.sys, D.strips, D.vitems, D.ritems, D.sp, st, nullptr, nullptr, nullptr};
@@ -1464,12 +1503,17 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         key.n[5] = maxiter | ((long long)dense_D << 32);
         key.n[6] = P.max_B;
         key.n[7] = P.total_vec;
+        key.n[8] = groups_hash(P);
+        use.key = key;
         {
             std::lock_guard<std::mutex> lk(g_graphs.mu);
             auto f = g_graphs.map.find(key);
             if (f != g_graphs.map.end()) {
                 exec = f->second.exec;
                 exec_kernels = f->second.kernels;
+                f->second.inuse++;
+                f->second.last = ++g_graphs.clock;
+                use.held = true;
             }
         }
         if (!exec) {
@@ -1490,11 +1534,18 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             cudaGraphDestroy(g);
             if (ce != cudaSuccess) return gb_set_cuda_error(ce, "instantiate BiCGSTAB graph", __FILE__, __LINE__);
             std::lock_guard<std::mutex> lk(g_graphs.mu);
-            if (g_graphs.map.size() > 256) {   // bounded cache
-                for (auto& kv : g_graphs.map) cudaGraphExecDestroy(kv.second.exec);
-                g_graphs.map.clear();
+            g_graphs.evict(255);   // bounded cache
+            auto f = g_graphs.map.find(key);
+            if (f != g_graphs.map.end()) {   // another thread built the same graph meanwhile
+                cudaGraphExecDestroy(exec);
+                exec = f->second.exec;
+                exec_kernels = f->second.kernels;
+                f->second.inuse++;
+                f->second.last = ++g_graphs.clock;
+            } else {
+                g_graphs.map[key] = GraphEntry{exec, exec_kernels, 1, ++g_graphs.clock};
             }
-            g_graphs.map[key] = GraphEntry{exec, exec_kernels};
+            use.held = true;
         }
     }
 

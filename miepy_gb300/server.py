@@ -1,0 +1,285 @@
+"""Continuous-batching solve server for sphere-cluster requests on one GPU.
+
+Requests (a cluster, a wavelength, an lmax and a source) arrive at any time.  A
+dispatcher thread admits waiting requests in arrival order against an HBM budget
+(the footprint of each request's matrices, vectors and solver scratch) and a number
+of wave slots.  Everything admitted together forms a wave: one ragged ClusterBatch
+that is assembled, solved (all clusters advance through the same masked kernels;
+finished ones drop out) and reduced to observables in one sequence of launches on
+the wave's own CUDA stream.  Up to ``max_waves`` waves are on the GPU at once, so
+requests that arrive while others are being solved are admitted as soon as memory
+and a slot free up, and their work overlaps on the device with the waves already
+running.  Each request's result is that of its own cluster: clusters in a batch
+share launches, never arithmetic.
+
+The reference has no server; a user would loop over ``sphere_cluster`` objects
+(sphere_cluster.py:27-125), one solve at a time.
+"""
+
+from __future__ import annotations
+
+import collections
+import concurrent.futures as cf
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .engine import ClusterBatch, footprint_bytes, require_cuda
+from .materials import constant_material, material_struct
+from .mie import mie_coefficients
+from .modes import lmax_to_rmax
+from .sources import plane_wave
+
+
+@dataclass
+class ClusterRequest:
+    position: np.ndarray                 # [N, 3] m
+    radius: object                       # [N] or scalar, m
+    index: object                        # particle refractive index (complex, [N] or scalar)
+    wavelength: float                    # m
+    lmax: int
+    source: object = None                # plane_wave / gaussian_beam (default: x-polarised plane wave)
+    medium_index: float = 1.0            # non-absorbing medium
+    rid: int = -1
+
+
+@dataclass
+class ClusterResult:
+    rid: int
+    status: int
+    passes: int                          # refinement passes (mixed) or BiCGSTAB iterations (fp64)
+    C_sca: float
+    C_abs: float
+    C_ext: float
+    p_inc: np.ndarray                    # [N, 2, rmax]
+    force: np.ndarray                    # [N, 3]
+    torque: np.ndarray                   # [N, 3]
+    t_submit: float = 0.0
+    t_admit: float = 0.0
+    t_done: float = 0.0
+    wave: int = -1
+    wave_size: int = 0
+
+    @property
+    def latency(self):
+        return self.t_done - self.t_submit
+
+
+class OverBudget(RuntimeError):
+    """A request larger than the whole HBM budget."""
+
+
+def request_spec(req: ClusterRequest):
+    """Host inputs of one request: Mie coefficients, wavenumber and p_src."""
+    pos = np.asarray(np.atleast_2d(req.position), float)
+    N = pos.shape[0]
+    radius = np.broadcast_to(np.asarray(req.radius, float), (N,))
+    mat = [constant_material(index=complex(i)) for i in np.broadcast_to(np.asarray(req.index, complex), (N,))]
+    medium = constant_material(index=float(req.medium_index))
+    md = material_struct(np.asarray(mat, dtype=object), medium, wavelength=req.wavelength)
+    ms, mi = mie_coefficients(radius, md.eps, md.mu, md.eps_b, md.mu_b, md.k_b, int(req.lmax))
+    k = float(np.real(md.k_b))
+    src = req.source if req.source is not None else plane_wave.from_string("x")
+    p_src = src.structure(pos, k, int(req.lmax))
+    return dict(position=pos, mie_scat=ms, mie_int=mi, k=k, p_src=p_src, eps_b=float(np.real(md.eps_b)))
+
+
+def request_footprint(req: ClusterRequest, precision):
+    N = np.asarray(np.atleast_2d(req.position)).shape[0]
+    return footprint_bytes(N, int(req.lmax), 1, precision)
+
+
+class SolveServer:
+    """Admits, batches and solves cluster requests; ``submit`` returns a Future of
+    a ClusterResult."""
+
+    def __init__(self, hbm_budget=None, max_waves=3, max_wave_requests=64, precision="mixed", tol=1e-8,
+                 inner_tol=1e-5, maxiter=1000, device=None):
+        self.device = require_cuda(device)
+        if hbm_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            hbm_budget = int(0.8 * free)
+        self.budget = int(hbm_budget)
+        self.max_waves = int(max_waves)
+        self.max_wave_requests = int(max_wave_requests)
+        self.precision = precision
+        self.tol, self.inner_tol, self.maxiter = float(tol), float(inner_tol), int(maxiter)
+        self._pending = collections.deque()
+        self._cv = threading.Condition()
+        self._in_use = 0
+        self._waves_running = 0
+        self._wave_counter = 0
+        self._closing = False
+        self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.max_waves)]
+        self._free_streams = list(range(self.max_waves))
+        # persistent workers: the native library keeps per-thread staging buffers
+        # and capture streams, reused wave after wave
+        self._pool = cf.ThreadPoolExecutor(max_workers=self.max_waves, thread_name_prefix="miepy-gb300-wave")
+        self.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0)
+        self._dispatcher = threading.Thread(target=self._dispatch, name="miepy-gb300-dispatch", daemon=True)
+        self._dispatcher.start()
+
+    # --------------------------------------------------------------- client --
+    def submit(self, req: ClusterRequest) -> cf.Future:
+        fut = cf.Future()
+        with self._cv:
+            if self._closing:
+                raise RuntimeError("server is closed")
+            self._pending.append((req, fut, time.perf_counter()))
+            self._cv.notify_all()
+        return fut
+
+    def close(self, wait=True):
+        with self._cv:
+            self._closing = True
+            self._cv.notify_all()
+        if wait:
+            self._dispatcher.join()
+        self._pool.shutdown(wait=wait)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------ dispatch --
+    def _take_wave(self):
+        """Requests for the next wave (arrival order, within the free budget and
+        the same medium); caller holds the lock."""
+        wave, used = [], 0
+        free = self.budget - self._in_use
+        while self._pending and len(wave) < self.max_wave_requests:
+            req, fut, t0 = self._pending[0]
+            need = request_footprint(req, self.precision)
+            if need > self.budget:
+                self._pending.popleft()
+                self.stats["rejected"] += 1
+                fut.set_exception(OverBudget(f"request {req.rid} needs {need} B, budget {self.budget} B"))
+                continue
+            if wave and req.medium_index != wave[0][0].medium_index:
+                break
+            if used + need > free:
+                break
+            self._pending.popleft()
+            wave.append((req, fut, t0, need))
+            used += need
+        return wave, used
+
+    def _dispatch(self):
+        while True:
+            with self._cv:
+                while True:
+                    if self._closing and not self._pending:
+                        return
+                    if self._pending and self._free_streams:
+                        wave, used = self._take_wave()
+                        if wave:
+                            break
+                    self._cv.wait(timeout=0.5)
+                self._in_use += used
+                self._waves_running += 1
+                self.stats["peak_bytes"] = max(self.stats["peak_bytes"], self._in_use)
+                self.stats["max_concurrent_waves"] = max(self.stats["max_concurrent_waves"], self._waves_running)
+                self.stats["admitted"] += len(wave)
+                self.stats["waves"] += 1
+                sidx = self._free_streams.pop()
+                wid = self._wave_counter
+                self._wave_counter += 1
+            self._pool.submit(self._run_wave, wave, used, sidx, wid)
+
+    def _run_wave(self, wave, used, sidx, wid):
+        t_admit = time.perf_counter()
+        stream = self._streams[sidx]
+        try:
+            with torch.cuda.device(self.device), torch.cuda.stream(stream):
+                specs = [request_spec(req) for req, _, _, _ in wave]
+                b = ClusterBatch(specs, R=1, precision=self.precision, device=self.device)
+                b.assemble()
+                b.solve(tol=self.tol, maxiter=self.maxiter, inner_tol=self.inner_tol, max_refine=8)
+                b.epilogue(specs[0]["eps_b"])
+                xs = b.xs[: b.totals["obs"] * 6 * b.xs_L].view(-1, 3, 2 * b.xs_L).cpu().numpy()
+                F = b.F[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
+                T = b.T[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
+                x = b.x.cpu().numpy()
+                status, iters = b.status.copy(), b.iters.copy()
+                del b
+            t_done = time.perf_counter()
+            for s, (req, fut, t0, _) in enumerate(wave):
+                l = _layout(specs, s)
+                o, N, L = l["obs_off"], l["N"], l["lmax"]
+                C = xs[o: o + N, :, : 2 * L].sum(axis=(0, 2))
+                res = ClusterResult(rid=req.rid, status=int(status[s]), passes=int(iters[s]), C_sca=float(C[0]),
+                                    C_abs=float(C[1]), C_ext=float(C[2]),
+                                    p_inc=x[l["vec_off"]: l["vec_off"] + l["D"]].reshape(N, 2, l["rmax"]),
+                                    force=F[o: o + N].copy(), torque=T[o: o + N].copy(), t_submit=t0,
+                                    t_admit=t_admit, t_done=t_done, wave=wid, wave_size=len(wave))
+                fut.set_result(res)
+        except Exception as exc:   # every request of a failed wave learns why
+            for _, fut, _, _ in wave:
+                if not fut.done():
+                    fut.set_exception(exc)
+        finally:
+            with self._cv:
+                self._in_use -= used
+                self._waves_running -= 1
+                self._free_streams.append(sidx)
+                self.stats["completed"] += len(wave)
+                self._cv.notify_all()
+
+
+def _layout(specs, s):
+    """Offsets of cluster s in a ClusterBatch built from specs with R = 1."""
+    obs = vec = 0
+    for i, sp in enumerate(specs):
+        N = np.asarray(sp["position"]).reshape(-1, 3).shape[0]
+        L = int(np.asarray(sp["mie_scat"]).shape[-1])
+        rmax = lmax_to_rmax(L)
+        if i == s:
+            return dict(obs_off=obs, vec_off=vec, N=N, lmax=L, rmax=rmax, D=2 * rmax * N)
+        obs += N
+        vec += 2 * rmax * N
+    raise IndexError(s)
+
+
+# ------------------------------------------------------------ request stream --
+_BEAMS = {}                       # one beam object per waist: its far-field projection is cached
+_BEAMS_LOCK = threading.Lock()
+
+def random_request(rng, rid=-1, n_range=(2, 500), lmax_range=(2, 8), wavelength=600e-9, beam_width=1e-6,
+                   rmin=50e-9, rmax=100e-9, cell=0.5e-6, max_tries=1_000_000):
+    """One request of the serving workload: N log-uniform in n_range, lmax uniform,
+    index U[1.3, 2.5] + i U[0, 0.1], radii U[rmin, rmax], centres in a cube of side
+    (N cell^3)^(1/3) by rejection sampling; plane wave or Gaussian beam with equal
+    probability."""
+    from .beams import gaussian_beam
+    N = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+    L = int(rng.integers(lmax_range[0], lmax_range[1] + 1))
+    index = rng.uniform(1.3, 2.5) + 1j * rng.uniform(0.0, 0.1)
+    side = (N * cell ** 3) ** (1 / 3)
+    pos = np.zeros((N, 3))
+    rad = np.zeros(N)
+    n = tries = 0
+    while n < N:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("rejection sampling did not place all spheres")
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(0, side, 3)
+        if n == 0 or np.all(np.linalg.norm(pos[:n] - c, axis=1) > r + rad[:n]):
+            pos[n], rad[n] = c, r
+            n += 1
+    pos = pos - side / 2
+    if rng.uniform() < 0.5:
+        key = float(beam_width)
+        with _BEAMS_LOCK:
+            if key not in _BEAMS:
+                _BEAMS[key] = gaussian_beam(width=beam_width, polarization=[1, 0])
+            source = _BEAMS[key]
+    else:
+        source = plane_wave.from_string("x")
+    return ClusterRequest(position=pos, radius=np.array(rad), index=index, wavelength=wavelength, lmax=L,
+                          source=source, rid=rid)

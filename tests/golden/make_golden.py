@@ -120,6 +120,24 @@ def main():
                                             radius=[60 * nm, 70 * nm], material=dm, source=src_x,
                                             wavelength=wav, lmax=4, method=miepy.solver.exact))
 
+    # Gaussian beam (waist 1 um, x-polarised, vacuum, 600 nm): p_src at scattered
+    # points (sources/beams.py:168-200) and a 3-sphere cluster driven by it
+    beam = miepy.sources.gaussian_beam(width=1000 * nm, polarization=[1, 0])
+    rng_b = np.random.default_rng(11)
+    bpos = rng_b.uniform(-600 * nm, 600 * nm, size=(7, 3))
+    k_v = 2 * np.pi / (600 * nm)
+    rec = dict(position=bpos, k=np.float64(k_v), lmax=np.int64(5), width=np.float64(1000 * nm),
+               polarization=np.array([1.0, 0.0]), p_src=beam.structure(bpos, k_v, 5),
+               E0=np.float64(beam.E0(k_v)), theta_c=np.float64(beam.theta_cutoff(k_v)))
+    np.savez_compressed(os.path.join(HERE, "gauss_beam_lmax5.npz"), **rec)
+    print("wrote gauss_beam_lmax5")
+    cluster_record(miepy, "gauss3_lmax3_exact",
+                   miepy.sphere_cluster(position=[[0, 0, 0], [200 * nm, 50 * nm, 0], [-150 * nm, 100 * nm, 80 * nm]],
+                                        radius=[70 * nm, 60 * nm, 80 * nm], material=diel,
+                                        source=miepy.sources.gaussian_beam(width=1000 * nm, polarization=[1, 0]),
+                                        wavelength=600 * nm, lmax=3, method=miepy.solver.exact),
+                   store_matrix=True)
+
     # special-function tables for the device recurrences
     from oracle import oracle as O
     z = np.linspace(-0.999, 0.999, 23)

@@ -1,0 +1,130 @@
+"""Continuous-batching solve server.
+
+CPU: admission in arrival order within the HBM budget, over-budget rejection, one
+medium per wave, and the request generator of the serving workload.
+GPU: every result is the same alone and in the mix (tolerance: C_ext within 1e-8
+relative, p_inc within 1e-8 of its largest coefficient, at solve tolerance 1e-10),
+with waves overlapping on the device; Gaussian-beam and plane-wave requests mixed.
+"""
+
+import collections
+import concurrent.futures as cf
+import threading
+
+import numpy as np
+import pytest
+
+from miepy_gb300 import server as SV
+
+
+def _bare_server(budget, max_wave_requests=8, precision="mixed"):
+    s = object.__new__(SV.SolveServer)
+    s.budget = budget
+    s.max_wave_requests = max_wave_requests
+    s.precision = precision
+    s._pending = collections.deque()
+    s._in_use = 0
+    s.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0)
+    return s
+
+
+def _req(N, L, rid, medium=1.0):
+    return SV.ClusterRequest(position=np.arange(3 * N, dtype=float).reshape(N, 3) * 1e-6, radius=50e-9,
+                             index=1.5, wavelength=600e-9, lmax=L, medium_index=medium, rid=rid)
+
+
+def test_admission_fifo_budget_and_rejection():
+    reqs = [_req(20, 3, 0), _req(30, 4, 1), _req(400, 8, 2), _req(10, 2, 3)]
+    need = [SV.request_footprint(r, "mixed") for r in reqs]
+    s = _bare_server(budget=need[0] + need[1] + need[3])
+    futs = []
+    for r in reqs:
+        f = cf.Future()
+        futs.append(f)
+        s._pending.append((r, f, 0.0))
+    wave, used = s._take_wave()
+    assert [w[0].rid for w in wave] == [0, 1, 3]       # request 2 exceeds the whole budget ...
+    assert used == need[0] + need[1] + need[3]
+    assert isinstance(futs[2].exception(timeout=0), SV.OverBudget)  # ... and is rejected
+    assert s.stats["rejected"] == 1
+    assert not s._pending
+    s2 = _bare_server(budget=need[0] + need[1])
+    for r in (reqs[0], reqs[1], reqs[3]):
+        s2._pending.append((r, cf.Future(), 0.0))
+    wave, used = s2._take_wave()
+    assert [w[0].rid for w in wave] == [0, 1]          # request 3 waits: the budget is used up
+    s2._in_use = used - need[0]                         # request 0's wave finished
+    wave, used = s2._take_wave()
+    assert [w[0].rid for w in wave] == [3]
+
+
+def test_admission_waits_for_memory_and_splits_media():
+    a, b = _req(40, 5, 0), _req(40, 5, 1)
+    na = SV.request_footprint(a, "mixed")
+    s = _bare_server(budget=int(1.5 * na))
+    for r in (a, b):
+        s._pending.append((r, cf.Future(), 0.0))
+    wave, used = s._take_wave()
+    assert [w[0].rid for w in wave] == [0]
+    s._in_use = used
+    wave, _ = s._take_wave()
+    assert wave == []                                   # request 1 waits for request 0's memory
+    s2 = _bare_server(budget=10 * na)
+    for r in (_req(10, 3, 0, 1.0), _req(10, 3, 1, 1.33), _req(10, 3, 2, 1.0)):
+        s2._pending.append((r, cf.Future(), 0.0))
+    wave, _ = s2._take_wave()
+    assert [w[0].rid for w in wave] == [0]              # one medium per wave
+
+
+def test_request_generator():
+    rng = np.random.default_rng(4)
+    Ns, Ls, beams = [], [], 0
+    for i in range(60):
+        r = SV.random_request(rng, rid=i, n_range=(2, 60))
+        pos, rad = np.asarray(r.position), np.asarray(r.radius)
+        d = np.linalg.norm(pos[:, None] - pos[None], axis=-1)
+        np.fill_diagonal(d, np.inf)
+        assert np.all(d > rad[:, None] + rad[None])
+        assert 1.3 <= np.real(r.index) <= 2.5 and 0 <= np.imag(r.index) <= 0.1
+        Ns.append(len(rad))
+        Ls.append(r.lmax)
+        beams += type(r.source).__name__ == "gaussian_beam"
+    assert min(Ns) >= 2 and max(Ns) <= 60 and set(Ls) <= set(range(2, 9))
+    assert 10 < beams < 50
+
+
+@pytest.mark.gpu
+def test_results_same_alone_and_in_the_mix():
+    rng = np.random.default_rng(4)
+    reqs = [SV.random_request(rng, rid=i, n_range=(2, 40), lmax_range=(2, 5)) for i in range(12)]
+    kw = dict(precision="mixed", tol=1e-10, inner_tol=1e-6)
+    with SV.SolveServer(max_waves=3, max_wave_requests=3, **kw) as srv:
+        futs = [srv.submit(r) for r in reqs]
+        mix = [f.result(timeout=600) for f in futs]
+        stats = dict(srv.stats)
+    assert stats["admitted"] == stats["completed"] == 12
+    assert stats["waves"] >= 4
+    alone = []
+    with SV.SolveServer(max_waves=1, max_wave_requests=1, **kw) as srv:
+        for r in reqs:
+            alone.append(srv.submit(r).result(timeout=600))
+    for a, m in zip(alone, mix):
+        assert a.status == 0 and m.status == 0
+        assert abs(a.C_ext - m.C_ext) <= 1e-8 * abs(a.C_ext)
+        assert np.max(np.abs(a.p_inc - m.p_inc)) <= 1e-8 * np.max(np.abs(a.p_inc))
+        np.testing.assert_allclose(m.force, a.force, rtol=1e-6, atol=1e-6 * np.max(np.abs(a.force)))
+
+
+@pytest.mark.gpu
+def test_server_against_fp64_single_cluster():
+    """A served request equals the sphere_cluster FP64 solve of the same cluster."""
+    import miepy_gb300 as gb
+    rng = np.random.default_rng(5)
+    r = SV.random_request(rng, rid=0, n_range=(8, 12), lmax_range=(3, 3))
+    with SV.SolveServer(precision="mixed", tol=1e-10) as srv:
+        res = srv.submit(r).result(timeout=600)
+    c = gb.sphere_cluster(position=r.position, radius=r.radius, material=gb.constant_material(index=r.index),
+                          source=r.source, wavelength=r.wavelength, lmax=r.lmax, method=gb.solver.exact)
+    C = c.cross_sections()
+    assert abs(res.C_ext - C.extinction) <= 1e-8 * abs(C.extinction)
+    assert np.max(np.abs(res.p_inc - c.p_inc)) <= 1e-8 * np.max(np.abs(c.p_inc))
