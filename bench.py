@@ -456,9 +456,88 @@ def run_serve(args):
                 gpu_launches=int(launches), clocks=clocks_info)
 
 
+# ------------------------------------------------------------ large system --
+LARGE_WORKLOAD = ("large system: N=2000 spheres on a jittered hexagonal lattice (pitch 300 nm, jitter +-30 nm, "
+                  "seed 5), radius 80 nm, n=2.0, lmax 3 (D=60000), vacuum, 600 nm, x-polarised plane wave; "
+                  "E on a 512x512 plane at z=0 over the lattice + 500 nm")
+
+
+def run_large(args):
+    """One step = assembly + mixed solve + epilogue of the 2000-sphere lattice; the
+    512 x 512 field map (FP32 exterior sums) is timed separately; the FP64 solve once."""
+    import torch
+    from miepy_gb300 import large as LG
+    from miepy_gb300.engine import ClusterBatch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    pos = LG.hex_lattice()
+    spec, md, rad = LG.lattice_spec(pos)
+    eps_b = float(np.real(md.eps_b))
+    stream = torch.cuda.current_stream()
+    L = nat_lib()
+
+    def step(b):
+        b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); b.epilogue(eps_b)
+
+    clocks = ClockSampler(dev.index).start()
+    b = ClusterBatch([spec], R=1, precision="mixed", device=dev)
+    for _ in range(args.warmup):
+        step(b)
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    n0 = L.gb_launch_count()
+    ev[0].record(stream)
+    for i in range(steps):
+        step(b)
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    launches = L.gb_launch_count() - n0
+    per = np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)])
+    t = ev[0].elapsed_time(ev[-1]) / 1e3
+    ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ph[0].record(stream); b.assemble(); ph[1].record(stream)
+    b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); ph[2].record(stream)
+    b.epilogue(eps_b); ph[3].record(stream)
+    torch.cuda.synchronize()
+    phases = dict(assemble_ms=ph[0].elapsed_time(ph[1]), solve_ms=ph[1].elapsed_time(ph[2]),
+                  epilogue_ms=ph[2].elapsed_time(ph[3]))
+    Cm = b.cross_sections(0)[0].cpu().numpy()
+    pts = torch.from_numpy(LG.plane_grid(pos, n=512)).to(dev)
+    LG.near_field(b, 0, md, rad, pts[:4096], precision="fp32")
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    E = LG.near_field(b, 0, md, rad, pts, precision="fp32")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_field = f0.elapsed_time(f1) / 1e3
+    mat_gb = sum(x.numel() * x.element_size() for x in (b.mat64, b.mat64lo) if x is not None) / 1e9
+    del b, E
+    torch.cuda.empty_cache()
+    b = ClusterBatch([spec], R=1, precision="fp64", device=dev)
+    d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    d0.record(stream)
+    step(b)
+    d1.record(stream)
+    torch.cuda.synchronize()
+    t64 = d0.elapsed_time(d1) / 1e3
+    Cd = b.cross_sections(0)[0].cpu().numpy()
+    clocks_info = clocks.stop()
+    Npts, N, rmax = 512 * 512, 2000, 15
+    return dict(value=steps / t, ms_per_step=1e3 * t / steps, p50_ms=float(np.percentile(per, 50)),
+                p99_ms=float(np.percentile(per, 99)), phases_mixed=phases, fp64_solves_per_s=1.0 / t64,
+                cext_rel_err_mixed_vs_fp64=float(abs(Cm[2] - Cd[2]) / abs(Cd[2])),
+                resident_matrix_gb=mat_gb,
+                field=dict(points=Npts, ms=1e3 * t_field, point_particle_terms_per_s=Npts * N / t_field,
+                           tflops_by_40_P_N_rmax=40.0 * Npts * N * rmax / t_field / 1e12,
+                           precision="FP32 exterior sums, FP64 interior expansions"),
+                gpu_launches=int(launches), clocks=clocks_info)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="cluster", choices=["cluster", "sweep", "serve"],
+    ap.add_argument("--config", default="cluster", choices=["cluster", "sweep", "serve", "large"],
                     help="cluster: the headline N=200 cluster; sweep: the 256-wavelength Drude sweep; "
                          "serve: the request stream through the solve server")
     ap.add_argument("--requests", type=int, default=48, help="requests in the serving stream")
@@ -500,6 +579,15 @@ def main():
         return
 
     import torch
+    if args.config == "large":
+        if rank == 0:
+            res = run_large(args)
+            line = dict(base, metric="large-system solves/s (assembly + mixed solve + epilogue), 512^2 near field",
+                        unit="solves/s", impl="gb300", dtype="c64 BiCGSTAB + double-float refinement residual",
+                        data="synthetic (seeded jittered lattice)", cpu_baseline=None,
+                        config=dict(workload=LARGE_WORKLOAD, solve_tol=TOL, rhs=1), **res)
+            print(json.dumps(line))
+        return
     if args.config == "serve":
         if rank == 0:
             res = run_serve(args)

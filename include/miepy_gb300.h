@@ -208,6 +208,15 @@ int gb_near_field(int N, int lmax, const double* pos, const double* radius, cons
                   const double* p_int, double k, const double* k_int, int Npts, const double* pts, int interior,
                   int magnetic, double hfac_re, double hfac_im, const double* hfac_int, double* out, void* stream);
 
+/* gb_near_field with the exterior sums (outgoing expansions of p_scat about every
+ * particle) in FP32, for large maps; points inside a sphere take the FP64 interior
+ * expansion.  Same arguments and output layout.  About 1e-6 relative accuracy
+ * against gb_near_field (no counterpart in the reference, whose field evaluation
+ * is the Python of sphere_cluster.py:244-391). */
+int gb_near_field32(int N, int lmax, const double* pos, const double* radius, const double* p_scat,
+                    const double* p_int, double k, const double* k_int, int Npts, const double* pts, int interior,
+                    int magnetic, double hfac_re, double hfac_im, const double* hfac_int, double* out, void* stream);
+
 /* ------------------------------------------------------------ beam source --
  * Beam expansion coefficients at N particles from the beam's far-field
  * projection: replaces integrate_phase, cpp/src/decomposition.cpp:29-66, as

@@ -63,6 +63,8 @@ SIGNATURES = {
     "gb_particle_cross_sections": (c_int, [c_int, c_int, _P, _P, _P, c_double, _P, _P]),
     "gb_near_field": (c_int, [c_int, c_int, _P, _P, _P, _P, c_double, _P, c_int, _P, c_int, c_int, c_double, c_double,
                               _P, _P, _P]),
+    "gb_near_field32": (c_int, [c_int, c_int, _P, _P, _P, _P, c_double, _P, c_int, _P, c_int, c_int, c_double,
+                                c_double, _P, _P, _P]),
 }
 
 

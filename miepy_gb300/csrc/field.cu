@@ -247,6 +247,202 @@ k_field(int L, int N, const double* __restrict__ pos, const double* __restrict__
     for (int d = 0; d < 3; d++) out[3LL * pt + d] = E[d];
 }
 
+// ------------------------------------------------------------ FP32 field --
+// The same exterior sum in FP32 for large maps (a 512 x 512 plane around
+// thousands of spheres is ~1e9 point-particle terms): no trigonometry per term
+// beyond one sincosf of k r; angles enter through r-hat components, e^{i m phi}
+// by powering (x + i y)/rho.  Coefficients are pre-multiplied by i E_mn in shared
+// memory (tiles of 32 particles); separations are formed in FP64.  Points inside a
+// sphere take the FP64 interior expansion, as in k_field.
+constexpr int kTile32 = 32;
+
+template <int LT>
+__global__ void __launch_bounds__(kFieldThreads)
+k_field32(int Lrun, int N, const double* __restrict__ pos, const double* __restrict__ radius,
+          const double2* __restrict__ p_scat, const double2* __restrict__ p_int, double k,
+          const double2* __restrict__ k_int, int Npts, const double* __restrict__ pts, int interior, int magnetic,
+          double2 hfac, const double2* __restrict__ hfac_int, double2* __restrict__ out) {
+    // LT > 0: lmax known at compile time, every per-term loop unrolled (arrays in
+    // registers); LT == 0: any lmax up to kLF
+    const int L = LT > 0 ? LT : Lrun;
+    const int rmax = L * (L + 2);
+    __shared__ double sp_pos[kTile32][3];
+    __shared__ float2 sw0[kTile32 * kLF * (kLF + 2)];
+    __shared__ float2 sw1[kTile32 * kLF * (kLF + 2)];
+    __shared__ double2 emn[kLF * (kLF + 2)];
+    __shared__ double negf_tab[kLF * (kLF + 2)];
+    __shared__ float negf32[kLF * (kLF + 2)];
+    for (int r = threadIdx.x; r < rmax; r += blockDim.x) {
+        int n = (int)floor(sqrt((double)r + 1.0));
+        while (n * n > r + 1) n--;
+        while ((n + 1) * (n + 1) <= r + 1) n++;
+        const int m = r + 1 - n * n - n;
+        emn[r] = Emn(m, n);
+        const int am = m < 0 ? -m : m;
+        negf_tab[r] = (m < 0) ? (((am & 1) ? -1.0 : 1.0) * tgamma((double)(n - am) + 1.0) / tgamma((double)(n + am) + 1.0)) : 1.0;
+        negf32[r] = (float)negf_tab[r];
+    }
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = pt < Npts;
+    double X = 0, Y = 0, Z = 0;
+    if (valid) {
+        X = pts[3LL * pt];
+        Y = pts[3LL * pt + 1];
+        Z = pts[3LL * pt + 2];
+    }
+    int inside = -1;
+    if (interior && valid) {
+        for (int i = 0; i < N; i++) {
+            const double dx = X - pos[3 * i], dy = Y - pos[3 * i + 1], dz = Z - pos[3 * i + 2];
+            if (dx * dx + dy * dy + dz * dz < radius[i] * radius[i]) inside = i;
+        }
+    }
+    const float kf = (float)k;
+    float Ex[2] = {0.f, 0.f}, Ey[2] = {0.f, 0.f}, Ez[2] = {0.f, 0.f};
+    for (int t0 = 0; t0 < N; t0 += kTile32) {
+        const int cnt = min(kTile32, N - t0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt * 3; e += blockDim.x) sp_pos[e / 3][e % 3] = pos[3LL * t0 + e];
+        for (int e = threadIdx.x; e < cnt * rmax; e += blockDim.x) {
+            const int q = e / rmax, r = e % rmax;
+            const double2* c = p_scat + (long long)(t0 + q) * 2 * rmax;
+            const double2 c0 = magnetic ? c[rmax + r] : c[r];
+            const double2 c1 = magnetic ? c[r] : c[rmax + r];
+            const double2 w = cmul(make_double2(0, 1), emn[r]);   // outgoing: factor i
+            const double2 a = cmul(w, c0), b = cmul(w, c1);
+            sw0[e] = make_float2((float)a.x, (float)a.y);
+            sw1[e] = make_float2((float)b.x, (float)b.y);
+        }
+        __syncthreads();
+        if (!valid || inside >= 0) continue;
+        for (int q = 0; q < cnt; q++) {
+            const float dx = (float)(X - sp_pos[q][0]), dy = (float)(Y - sp_pos[q][1]), dz = (float)(Z - sp_pos[q][2]);
+            const float rho2 = dx * dx + dy * dy;
+            const float r = sqrtf(rho2 + dz * dz);
+            const float inv_r = 1.f / r;
+            const float rho = sqrtf(rho2);
+            const float ct = dz * inv_r, st = rho * inv_r;
+            float cphi = 1.f, sphi = 0.f;
+            if (rho > 0.f) {
+                const float ir = 1.f / rho;
+                cphi = dx * ir;
+                sphi = dy * ir;
+            }
+            // h_n(x) = j_n + i y_n, n = 0..L, by the upward recurrences
+            const float x = kf * r, ix = 1.f / x;
+            float sx, cx;
+            sincosf(x, &sx, &cx);
+            float hr[kLF + 1], hi[kLF + 1];
+            hr[0] = sx * ix;
+            hi[0] = -cx * ix;
+            hr[1] = hr[0] * ix - cx * ix;
+            hi[1] = hi[0] * ix - hr[0];
+#pragma unroll
+            for (int n = 2; n <= L; n++) {
+                const float f = (2 * n - 1) * ix;
+                hr[n] = f * hr[n - 1] - hr[n - 2];
+                hi[n] = f * hi[n - 1] - hi[n - 2];
+            }
+            // Legendre P_n^m(ct), m >= 0, no Condon-Shortley phase
+            float P[kLF + 1][kLF + 2];
+            P[0][0] = 1.f;
+#pragma unroll
+            for (int m = 1; m <= L; m++) P[m][m] = (2 * m - 1) * st * P[m - 1][m - 1];
+#pragma unroll
+            for (int m = 0; m < L; m++) P[m + 1][m] = ct * (2 * m + 1) * P[m][m];
+#pragma unroll
+            for (int m = 0; m <= L; m++)
+#pragma unroll
+                for (int n = m + 2; n <= L; n++)
+                    P[n][m] = ((2 * n - 1) * ct * P[n - 1][m] - (n + m - 1) * P[n - 2][m]) / (float)(n - m);
+            const bool axis = !(st > 0.f);
+            const float2* w0 = sw0 + q * rmax;
+            const float2* w1 = sw1 + q * rmax;
+            float Er[2] = {0.f, 0.f}, Et[2] = {0.f, 0.f}, Ep[2] = {0.f, 0.f};
+#pragma unroll
+            for (int n = 1; n <= L; n++) {
+                // radial parts: h_n / x and (x h_n)'/x = h_{n-1} - n h_n / x
+                const float hx_r = hr[n] * ix, hx_i = hi[n] * ix;
+                const float dr = hr[n - 1] - n * hx_r, di = hi[n - 1] - n * hx_i;
+                // e^{i m phi} for m = -n: conj((cphi + i sphi)^n)
+                float er = 1.f, ei = 0.f;
+                #pragma unroll
+                for (int s = 0; s < n; s++) {
+                    const float t = er * cphi + ei * sphi;   // multiply by e^{-i phi}
+                    ei = ei * cphi - er * sphi;
+                    er = t;
+                }
+#pragma unroll
+                for (int m = -n; m <= n; m++) {
+                    const int am = m < 0 ? -m : m;
+                    const int rr = n * n + n + m - 1;
+                    const float nf = negf32[rr];
+                    const float Pnm = nf * P[n][am];
+                    float pi_v, tau_v;
+                    if (axis) {
+                        const bool atpi = ct < 0.f;
+                        const float sgn = atpi ? (((n + 1) & 1) ? -1.f : 1.f) : 1.f;
+                        const float sgt = atpi ? ((n & 1) ? -1.f : 1.f) : 1.f;
+                        if (m == 1) { pi_v = sgn * n * (n + 1) * 0.5f; tau_v = sgt * n * (n + 1) * 0.5f; }
+                        else if (m == -1) { pi_v = sgn * 0.5f; tau_v = -sgt * 0.5f; }
+                        else { pi_v = 0.f; tau_v = 0.f; }
+                    } else {
+                        pi_v = m / st * Pnm;
+                        const float pm1 = (am >= 1) ? P[n][am - 1] : -P[n][1] / (float)(n * (n + 1));
+                        const float pp1 = (am + 1 <= n) ? P[n][am + 1] : 0.f;
+                        tau_v = nf * 0.5f * ((n + am) * (n - am + 1) * pm1 - pp1);
+                    }
+                    const float2 a = w0[rr], b = w1[rr];
+                    // u = a e, v = b e
+                    const float ur = a.x * er - a.y * ei, ui = a.x * ei + a.y * er;
+                    const float vr = b.x * er - b.y * ei, vi = b.x * ei + b.y * er;
+                    // N = (n(n+1) P h/x, d tau, i d pi) e ;  M = (0, i pi h, -tau h) e
+                    const float c0 = n * (n + 1) * Pnm;
+                    Er[0] += c0 * (ur * hx_r - ui * hx_i);
+                    Er[1] += c0 * (ur * hx_i + ui * hx_r);
+                    const float udr = ur * dr - ui * di, udi = ur * di + ui * dr;   // u d
+                    const float vhr = vr * hr[n] - vi * hi[n], vhi = vr * hi[n] + vi * hr[n];   // v h
+                    Et[0] += tau_v * udr - pi_v * vhi;
+                    Et[1] += tau_v * udi + pi_v * vhr;
+                    Ep[0] += -pi_v * udi - tau_v * vhr;
+                    Ep[1] += pi_v * udr - tau_v * vhi;
+                    const float t = er * cphi - ei * sphi;   // e <- e e^{i phi}
+                    ei = er * sphi + ei * cphi;
+                    er = t;
+                }
+            }
+            // spherical -> Cartesian
+            const float rh0 = st * cphi, rh1 = st * sphi, rh2 = ct;
+            const float th0 = ct * cphi, th1 = ct * sphi, th2 = -st;
+            const float ph0 = -sphi, ph1 = cphi;
+            for (int c = 0; c < 2; c++) {
+                Ex[c] += Er[c] * rh0 + Et[c] * th0 + Ep[c] * ph0;
+                Ey[c] += Er[c] * rh1 + Et[c] * th1 + Ep[c] * ph1;
+                Ez[c] += Er[c] * rh2 + Et[c] * th2;
+            }
+        }
+    }
+    if (!valid) return;
+    double2 E[3];
+    if (inside >= 0) {
+        E[0] = E[1] = E[2] = make_double2(0, 0);
+        const int i = inside;
+        const double dx = X - pos[3 * i], dy = Y - pos[3 * i + 1], dz = Z - pos[3 * i + 2];
+        const double rad = sqrt(dx * dx + dy * dy + dz * dz);
+        const double theta = acos(dz / rad);
+        const double phi = atan2(dy, dx);
+        const double2 pref = magnetic ? hfac_int[i] : make_double2(1, 0);
+        add_expansion(L, p_int + (long long)i * 2 * rmax, rmax, false, k_int[i], rad, theta, phi, magnetic != 0, pref,
+                      emn, negf_tab, E);
+    } else {
+        const double2 pref = magnetic ? hfac : make_double2(1, 0);
+        E[0] = cmul(pref, make_double2(Ex[0], Ex[1]));
+        E[1] = cmul(pref, make_double2(Ey[0], Ey[1]));
+        E[2] = cmul(pref, make_double2(Ez[0], Ez[1]));
+    }
+    for (int d = 0; d < 3; d++) out[3LL * pt + d] = E[d];
+}
+
 }   // namespace
 
 extern "C" int gb_near_field(int N, int lmax, const double* pos, const double* radius, const double* p_scat,
@@ -269,6 +465,28 @@ extern "C" int gb_near_field(int N, int lmax, const double* pos, const double* r
     gb::note_launch();
     k_field<<<grid, kFieldThreads, 0, s>>>(lmax, N, pos, radius, ps2, pi2, k, ki2, Npts, pts, interior, magnetic, hf,
                                            hi2, o2);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+// Same arguments and result as gb_near_field, with the exterior sums in FP32.
+extern "C" int gb_near_field32(int N, int lmax, const double* pos, const double* radius, const double* p_scat,
+                               const double* p_int, double k, const double* k_int, int Npts, const double* pts,
+                               int interior, int magnetic, double hfac_re, double hfac_im, const double* hfac_int,
+                               double* out, void* stream) {
+    if (N < 1 || Npts < 0 || !pos || !p_scat || !pts || !out) return gb_set_error(GB_BAD_ARG, "bad field arguments");
+    if (interior && (!radius || !p_int || !k_int)) return gb_set_error(GB_BAD_ARG, "interior fields need radius, p_int, k_int");
+    if (magnetic && interior && !hfac_int) return gb_set_error(GB_BAD_ARG, "interior H fields need hfac_int");
+    if (Npts == 0) return GB_OK;
+    if (lmax < 1 || lmax > kLF) return gb_set_error(GB_UNSUPPORTED, "near field supports lmax 1..%d (got %d)", kLF, lmax);
+    const unsigned grid = (unsigned)((Npts + kFieldThreads - 1) / kFieldThreads);
+    auto kfn = lmax == 1 ? k_field32<1> : lmax == 2 ? k_field32<2> : lmax == 3 ? k_field32<3>
+             : lmax == 4 ? k_field32<4> : k_field32<0>;
+    gb::note_launch();
+    kfn<<<grid, kFieldThreads, 0, (cudaStream_t)stream>>>(
+        lmax, N, pos, radius, reinterpret_cast<const double2*>(p_scat), reinterpret_cast<const double2*>(p_int), k,
+        reinterpret_cast<const double2*>(k_int), Npts, pts, interior, magnetic, make_double2(hfac_re, hfac_im),
+        reinterpret_cast<const double2*>(hfac_int), reinterpret_cast<double2*>(out));
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
