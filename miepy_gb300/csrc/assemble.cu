@@ -36,26 +36,31 @@ __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
     1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20, 1.0 / 21,
     1.0 / 22, 1.0 / 23};
 
+// Shared-memory layout of one CTA: the special functions of a group of PB pairs
+// (launch-wide strides PM = 2 Lmax + 2 orders, MU = 4 Lmax + 1 azimuthal orders),
+// then the tuple values of the pair being written.
 struct AsmSmem {
-    int PM, MU, M;
+    int PM, MU, M, PB;
     size_t off_geo, off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
 };
 
-__host__ __device__ inline AsmSmem asm_layout(int L, int M, bool want64) {
+__host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_sums, bool want64) {
     AsmSmem s;
     s.PM = 2 * L + 2;
     s.MU = 4 * L + 1;
     s.M = M;
+    s.PB = PB;
     size_t o = 0;
-    s.off_geo = o; o += sizeof(double) * 8;
-    s.off_h = o;  o += sizeof(double2) * s.PM;
-    s.off_e = o;  o += sizeof(double2) * s.MU;
-    s.off_G = o;  o += sizeof(double2) * s.PM * s.MU;
-    s.off_T = o;  o += sizeof(double2) * 2 * M;
-    s.off_P = o;  o += sizeof(double) * s.PM * s.PM;
-    s.off_Tf = o; o += want64 ? sizeof(float2) * 2 * M : 0;
-    s.off_Tl = o; o += want64 ? sizeof(float2) * 2 * M : 0;
-    s.total = (o + 15) & ~size_t(15);
+    auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 15) & ~size_t(15); return r; };
+    s.off_geo = take(sizeof(double) * 8 * PB);
+    s.off_h = take(sizeof(double2) * s.PM * PB);
+    s.off_e = take(sizeof(double2) * s.MU * PB);
+    s.off_P = take(sizeof(double) * s.PM * s.PM * PB);
+    s.off_G = take(16 * (size_t)s.PM * s.MU * PB);          // double2 (FP64 sums) or float4 (double-float)
+    s.off_T = take(fp64_sums ? sizeof(double2) * 2 * M : 0);
+    s.off_Tf = take(want64 ? sizeof(float2) * 2 * M : 0);
+    s.off_Tl = take(want64 ? sizeof(float2) * 2 * M : 0);
+    s.total = o;
     return s;
 }
 
@@ -66,6 +71,33 @@ __device__ __forceinline__ double2 mul_ipow(double2 z, int k) {
         case 2: return make_double2(-z.x, -z.y);
         default: return make_double2(z.y, -z.x);
     }
+}
+__device__ __forceinline__ float2 mul_ipowf(float2 z, int k) {
+    switch (k & 3) {
+        case 0: return z;
+        case 1: return make_float2(-z.y, z.x);
+        case 2: return make_float2(-z.x, -z.y);
+        default: return make_float2(z.y, -z.x);
+    }
+}
+__device__ __forceinline__ float2 bcf(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 negf2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// (sh, sl) += (c.x + c.y) * (g.hi + g.lo): double-float real x complex
+// multiply-add on the FP32 pipes (packed f32x2): the hi*hi product is exact
+// (FMA error term), cross terms and the TwoSum error go to the low word.
+__device__ __forceinline__ void df_rc_fma(float2& sh, float2& sl, float2 c, float4 g) {
+    const float2 ah = bcf(c.x), al = bcf(c.y);
+    const float2 gh = make_float2(g.x, g.y), gl = make_float2(g.z, g.w);
+    const float2 p = __fmul2_rn(ah, gh);
+    float2 e = __ffma2_rn(ah, gh, negf2(p));
+    e = __ffma2_rn(ah, gl, e);
+    e = __ffma2_rn(al, gh, e);
+    const float2 t = __fadd2_rn(sh, p);
+    const float2 bb = __fadd2_rn(t, negf2(sh));
+    const float2 err = __fadd2_rn(__fadd2_rn(sh, negf2(__fadd2_rn(t, negf2(bb)))), __fadd2_rn(p, negf2(bb)));
+    sh = t;
+    sl = __fadd2_rn(sl, __fadd2_rn(err, e));
 }
 
 __device__ __forceinline__ int find_sys(const long long* base, int nsys, long long g) {
@@ -78,68 +110,69 @@ __device__ __forceinline__ int find_sys(const long long* base, int nsys, long lo
     return lo;
 }
 
-template <bool DENSE>
+// FP64_SUMS: tuple sums in FP64 (complex128 or dense output); otherwise in
+// double-float on the FP32 pipes, straight to the complex64 hi / lo outputs.
+template <bool DENSE, bool FP64_SUMS>
 __global__ void __launch_bounds__(kAsmThreads)
-k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ pair_base, long long total,
-           const double* __restrict__ pos, const double2* __restrict__ mie, double2* __restrict__ out128,
-           float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld) {
+k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
+           int Lmax, int Mmax, int PB, const double* __restrict__ pos, const double2* __restrict__ mie,
+           double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
-    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
-        const int s = find_sys(pair_base, nsys, g);
+    const bool want64 = out64 != nullptr || out64lo != nullptr;
+    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE);
+    double* geo = reinterpret_cast<double*>(smem + lay.off_geo);        // [PB][8]
+    double2* hh = reinterpret_cast<double2*>(smem + lay.off_h);         // [PB][PM]
+    double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);        // [PB][MU]
+    double* Pl = reinterpret_cast<double*>(smem + lay.off_P);           // [PB][PM][PM]
+    double2* G64 = reinterpret_cast<double2*>(smem + lay.off_G);        // [PB][PM][MU]
+    float4* G32 = reinterpret_cast<float4*>(smem + lay.off_G);
+    double2* Tv = reinterpret_cast<double2*>(smem + lay.off_T);
+    float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
+    float2* Tl = reinterpret_cast<float2*>(smem + lay.off_Tl);
+    const int PMs = lay.PM, MUs = lay.MU;   // launch-wide strides
+    for (long long g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const int s = find_sys(grp_base, nsys, g);
         const gb::SysDev S = sys[s];
         const int L = S.lmax, B = S.B, N = S.N;
-        const AsmSmem lay = asm_layout(L, S.M, out64 != nullptr || out64lo != nullptr);
-        double2* h = reinterpret_cast<double2*>(smem + lay.off_h);
-        double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);
-        double2* G = reinterpret_cast<double2*>(smem + lay.off_G);
-        double2* Tv = reinterpret_cast<double2*>(smem + lay.off_T);
-        double* Pl = reinterpret_cast<double*>(smem + lay.off_P);
-        float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
-        float2* Tl = reinterpret_cast<float2*>(smem + lay.off_Tl);
-        const int PM = lay.PM, MU = lay.MU;
+        const int PM = 2 * L + 2, MU = 4 * L + 1;
+        const long long p_first = (g - grp_base[s]) * (long long)PB;
+        const int np = (int)min((long long)PB, S.P - p_first);
 
-        const long long p = g - pair_base[s];
-        int i, j;
-        pair_ij(p, N, i, j);
-        // geometry once per pair (one thread; FP64 sqrt/division are slow on this
-        // part's FP64 pipe): r, cos/sin theta, cos/sin phi straight from the
-        // separation vector (the reference goes through acos/atan2 and back; the
-        // values agree to rounding)
-        double* geo = reinterpret_cast<double*>(smem + lay.off_geo);
-        if (tid == 0) {
+        // ---- phase 1a: one thread per pair: geometry, then h_p(kr) by the upward
+        // j/y recurrence of spherical_hn_recursion (cpp/src/special.cpp:90-111).  The
+        // angles enter only through cos/sin of theta and phi, straight from the
+        // separation vector (the reference goes through acos/atan2 and back).
+        if (tid < np) {
+            int i, j;
+            pair_ij(p_first + tid, N, i, j);
             const double* pi_ = pos + S.pos_off + 3 * (long long)i;
             const double* pj_ = pos + S.pos_off + 3 * (long long)j;
             const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
             const double rho2 = dx * dx + dy * dy;
             const double rad = sqrt(rho2 + dz * dz);
             const double inv_r = 1.0 / rad;
-            double cphi = 1.0, sphi = 0.0;                 // phi = atan2(dy, dx) = 0 on the z axis
             const double rho = sqrt(rho2);
+            double cphi = 1.0, sphi = 0.0;                  // phi = atan2(dy, dx) = 0 on the z axis
             if (rho2 > 0.0) {
                 const double inv_rho = 1.0 / rho;
                 cphi = dx * inv_rho;
                 sphi = dy * inv_rho;
             }
-            geo[0] = rad;
-            geo[1] = dz * inv_r;                           // cos(theta)
-            geo[2] = rho * inv_r;                          // sin(theta) >= 0
-            geo[3] = cphi;
-            geo[4] = sphi;
-        }
-        __syncthreads();
-        const double rad = geo[0], x = geo[1], u = geo[2], cphi = geo[3], sphi = geo[4];
-
-        // ---- phase 1: Hankel, Legendre, azimuthal phases
-        if (tid == 32) {
+            double* ge = geo + 8 * tid;
+            ge[0] = dz * inv_r;                             // cos(theta)
+            ge[1] = rho * inv_r;                            // sin(theta) >= 0
+            ge[2] = cphi;
+            ge[3] = sphi;
             const double z = S.k * rad;
             const double inv_z = 1.0 / z;
             double sz, cz;
             sincos(z, &sz, &cz);
             double j0 = sz * inv_z, y0 = -cz * inv_z;
             double j1 = j0 * inv_z + y0, y1 = y0 * inv_z - j0;
+            double2* h = hh + PMs * tid;
             h[0] = make_double2(j0, y0);
-            if (PM > 1) h[1] = make_double2(j1, y1);
+            h[1] = make_double2(j1, y1);
             for (int q = 2; q < PM; q++) {
                 const double f = (2 * q - 1) * inv_z;
                 const double jn = f * j1 - j0;
@@ -148,124 +181,162 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 h[q] = make_double2(jn, yn);
             }
         }
-        if (tid < PM) {
-            const int mu = tid;
+        __syncthreads();
+        // ---- phase 1b: P_q^mu(cos theta) (no Condon-Shortley phase), one thread per
+        // (pair, mu); e^{i mu phi} by binary powering, one thread per (pair, mu >= 0)
+        for (int it = tid; it < np * PM; it += kAsmThreads) {
+            const int pp = it / PM, mu = it % PM;
+            const double x = geo[8 * pp], u = geo[8 * pp + 1];
+            double* P = Pl + (size_t)PMs * PMs * pp;
             double pmm = 1.0;
             for (int kk = 1; kk <= mu; kk++) pmm *= (2 * kk - 1) * u;
-            Pl[mu * PM + mu] = pmm;
+            P[mu * PMs + mu] = pmm;
             if (mu + 1 < PM) {
-                double p1 = x * (2 * mu + 1) * pmm;
-                Pl[(mu + 1) * PM + mu] = p1;
-                double pa = pmm, pb = p1;
+                double pa = pmm, pb = x * (2 * mu + 1) * pmm;
+                P[(mu + 1) * PMs + mu] = pb;
                 for (int q = mu + 2; q < PM; q++) {
                     const double pc = ((2 * q - 1) * x * pb - (q + mu - 1) * pa) * c_inv_int[q - mu];
-                    Pl[q * PM + mu] = pc;
+                    P[q * PMs + mu] = pc;
                     pa = pb;
                     pb = pc;
                 }
             }
         }
-        if (tid >= 64 && tid < 64 + MU) {
-            // e^{i mu phi} = (cos phi + i sin phi)^mu by binary powering
-            const int mu = tid - 64 - 2 * L;
-            int e = mu < 0 ? -mu : mu;
-            double2 acc = make_double2(1.0, 0.0), base = make_double2(cphi, sphi);
+        for (int it = tid; it < np * (2 * L + 1); it += kAsmThreads) {
+            const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
+            int e = mu;
+            double2 acc = make_double2(1.0, 0.0), base = make_double2(geo[8 * pp + 2], geo[8 * pp + 3]);
             while (e) {
                 if (e & 1) acc = cmul(acc, base);
                 base = cmul(base, base);
                 e >>= 1;
             }
-            eph[tid - 64] = mu < 0 ? make_double2(acc.x, -acc.y) : acc;
+            eph[MUs * pp + 2 * L + mu] = acc;
+            eph[MUs * pp + 2 * L - mu] = make_double2(acc.x, -acc.y);
         }
         __syncthreads();
-        for (int e = tid; e < PM * MU; e += kAsmThreads) {
-            const int q = e / MU, mi = e % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
+        // ---- phase 1c: G[p][mu] = P_p^mu h_p e^{i mu phi} (negative mu through the
+        // (-1)^mu (p-mu)!/(p+mu)! ratio), FP64 or split into double-float
+        for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
+            const int pp = it / (PM * MU), rem = it % (PM * MU);
+            const int q = rem / MU, mi = rem % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
             double2 gval = make_double2(0.0, 0.0);
             if (am <= q) {
-                double P = Pl[q * PM + am];
+                double P = Pl[(size_t)PMs * PMs * pp + q * PMs + am];
                 if (mu < 0) P *= S.neg_ratio[q * PM + am];
-                const double2 he = cmul(h[q], eph[mi]);
+                const double2 he = cmul(hh[PMs * pp + q], eph[MUs * pp + mi]);
                 gval = make_double2(P * he.x, P * he.y);
             }
-            G[e] = gval;
-        }
-        __syncthreads();
-
-        // ---- phase 2: translation coefficients of every canonical tuple
-        const int Q = L + 1;
-        for (int t = tid; t < S.M; t += kAsmThreads) {
-            const int4 e = S.nmvu[t];
-            const int2 qq = S.qab[t];
-            const int mi = (e.w - e.y) + 2 * L;
-            const int nv = e.x + e.z;
-            const double* ca = S.cA + (size_t)t * Q;
-            const double* cb = S.cB + (size_t)t * Q;
-            double2 sa = make_double2(0.0, 0.0), sb = make_double2(0.0, 0.0);
-            for (int q = 0; q <= qq.x; q++) {
-                const double c = ca[q];
-                const double2 gv = G[(nv - 2 * q) * MU + mi];
-                sa.x = fma(c, gv.x, sa.x);
-                sa.y = fma(c, gv.y, sa.y);
-            }
-            for (int q = 1; q <= qq.y; q++) {
-                const double c = cb[q];
-                const double2 gv = G[(nv - 2 * q + 1) * MU + mi];
-                sb.x = fma(c, gv.x, sb.x);
-                sb.y = fma(c, gv.y, sb.y);
-            }
-            const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
-            Tv[2 * t] = At;
-            Tv[2 * t + 1] = Bt;
-            if (!DENSE && (out64 || out64lo)) {
-                const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
-                const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
-                Tf[2 * t] = ah;
-                Tf[2 * t + 1] = bh;
-                Tl[2 * t] = make_float2(__double2float_rn(At.x - (double)ah.x), __double2float_rn(At.y - (double)ah.y));
-                Tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
+            const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
+            if (FP64_SUMS) {
+                G64[gi] = gval;
+            } else {
+                const float hx = __double2float_rn(gval.x), hy = __double2float_rn(gval.y);
+                G32[gi] = make_float4(hx, hy, __double2float_rn(gval.x - (double)hx),
+                                      __double2float_rn(gval.y - (double)hy));
             }
         }
         __syncthreads();
 
-        // ---- phase 3: block write
-        const int BB = B * B;
-        if (!DENSE) {
-            const long long base = S.mat_off + p * (long long)BB;
-            for (int e = tid; e < BB; e += kAsmThreads) {
-                const int code = __ldg(S.elem_map + e);
-                const unsigned neg = code & 1;
-                if (out128) {
-                    const double2 v = Tv[code >> 1];
-                    out128[base + e] = make_double2(flipd(v.x, neg), flipd(v.y, neg));
-                }
-                if (out64) {
-                    const float2 v = Tf[code >> 1];
-                    out64[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
-                }
-                if (out64lo) {
-                    const float2 v = Tl[code >> 1];
-                    out64lo[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+        for (int pp = 0; pp < np; pp++) {
+            const long long p = p_first + pp;
+            const size_t gbase = (size_t)PMs * MUs * pp;
+            // ---- phase 2: translation coefficients of every canonical tuple
+            const int Q = L + 1;
+            for (int t = tid; t < S.M; t += kAsmThreads) {
+                const int4 e = S.nmvu[t];
+                const int2 qq = S.qab[t];
+                const int mi = (e.w - e.y) + 2 * L;
+                const int nv = e.x + e.z;
+                if (FP64_SUMS) {
+                    const double* ca = S.cA + (size_t)t * Q;
+                    const double* cb = S.cB + (size_t)t * Q;
+                    double2 sa = make_double2(0.0, 0.0), sb = make_double2(0.0, 0.0);
+                    for (int q = 0; q <= qq.x; q++) {
+                        const double c = ca[q];
+                        const double2 gv = G64[gbase + (size_t)(nv - 2 * q) * MUs + mi];
+                        sa.x = fma(c, gv.x, sa.x);
+                        sa.y = fma(c, gv.y, sa.y);
+                    }
+                    for (int q = 1; q <= qq.y; q++) {
+                        const double c = cb[q];
+                        const double2 gv = G64[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi];
+                        sb.x = fma(c, gv.x, sb.x);
+                        sb.y = fma(c, gv.y, sb.y);
+                    }
+                    const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
+                    Tv[2 * t] = At;
+                    Tv[2 * t + 1] = Bt;
+                    if (!DENSE && want64) {
+                        const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
+                        const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
+                        Tf[2 * t] = ah;
+                        Tf[2 * t + 1] = bh;
+                        Tl[2 * t] = make_float2(__double2float_rn(At.x - (double)ah.x), __double2float_rn(At.y - (double)ah.y));
+                        Tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
+                    }
+                } else {
+                    const float2* ca = S.cA2 + (size_t)t * Q;
+                    const float2* cb = S.cB2 + (size_t)t * Q;
+                    float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
+                    for (int q = 0; q <= qq.x; q++)
+                        df_rc_fma(ah, al, ca[q], G32[gbase + (size_t)(nv - 2 * q) * MUs + mi]);
+                    for (int q = 1; q <= qq.y; q++)
+                        df_rc_fma(bh, bl, cb[q], G32[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi]);
+                    // normalise (Fast2Sum): hi = fl(h + l), lo = l - (hi - h)
+                    const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
+                    const float2 a2 = __fadd2_rn(al, negf2(__fadd2_rn(a1, negf2(ah))));
+                    const float2 b2 = __fadd2_rn(bl, negf2(__fadd2_rn(b1, negf2(bh))));
+                    Tf[2 * t] = mul_ipowf(a1, nv);
+                    Tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
+                    Tl[2 * t] = mul_ipowf(a2, nv);
+                    Tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
                 }
             }
-        } else {
-            const double2* mi_ = mie + (long long)i * 2 * L;
-            const double2* mj_ = mie + (long long)j * 2 * L;
-            for (int e = tid; e < BB; e += kAsmThreads) {
-                const int R = e / B, C = e % B;
-                const int code = __ldg(S.elem_map + e);
-                const unsigned neg = code & 1;
-                double2 v = Tv[code >> 1];
-                v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
-                const int col = __ldg(S.miecol + C);
-                const double2 vij = cmul(v, mj_[col]);
-                const unsigned sneg = ((unsigned)__ldg(S.rowinfo + R) >> 30 ^ (unsigned)__ldg(S.rowinfo + C) >> 30) & 1;
-                double2 vji = cmul(v, mi_[col]);
-                vji = make_double2(flipd(vji.x, sneg), flipd(vji.y, sneg));
-                out128[((long long)i * B + R) * dense_ld + (long long)j * B + C] = vij;
-                out128[((long long)j * B + R) * dense_ld + (long long)i * B + C] = vji;
+            __syncthreads();
+
+            // ---- phase 3: block write
+            const int BB = B * B;
+            if (!DENSE) {
+                const long long base = S.mat_off + p * (long long)BB;
+                for (int e = tid; e < BB; e += kAsmThreads) {
+                    const int code = __ldg(S.elem_map + e);
+                    const unsigned neg = code & 1;
+                    if (FP64_SUMS && out128) {
+                        const double2 v = Tv[code >> 1];
+                        out128[base + e] = make_double2(flipd(v.x, neg), flipd(v.y, neg));
+                    }
+                    if (out64) {
+                        const float2 v = Tf[code >> 1];
+                        out64[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+                    }
+                    if (out64lo) {
+                        const float2 v = Tl[code >> 1];
+                        out64lo[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+                    }
+                }
+            } else {
+                int i, j;
+                pair_ij(p, N, i, j);
+                const double2* mi_ = mie + (long long)i * 2 * L;
+                const double2* mj_ = mie + (long long)j * 2 * L;
+                for (int e = tid; e < BB; e += kAsmThreads) {
+                    const int R = e / B, C = e % B;
+                    const int code = __ldg(S.elem_map + e);
+                    const unsigned neg = code & 1;
+                    double2 v = Tv[code >> 1];
+                    v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
+                    const int col = __ldg(S.miecol + C);
+                    const double2 vij = cmul(v, mj_[col]);
+                    const unsigned sneg = ((unsigned)__ldg(S.rowinfo + R) >> 30 ^ (unsigned)__ldg(S.rowinfo + C) >> 30) & 1;
+                    double2 vji = cmul(v, mi_[col]);
+                    vji = make_double2(flipd(vji.x, sneg), flipd(vji.y, sneg));
+                    out128[((long long)i * B + R) * dense_ld + (long long)j * B + C] = vij;
+                    out128[((long long)j * B + R) * dense_ld + (long long)i * B + C] = vji;
+                }
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -323,6 +394,8 @@ int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector
         d.qab = T->qab;
         d.cA = T->cA;
         d.cB = T->cB;
+        d.cA2 = T->cA2;
+        d.cB2 = T->cB2;
         d.elem_map = T->elem_map;
         d.neg_ratio = T->neg_ratio;
         d.rowinfo = T->rowinfo;
@@ -401,48 +474,47 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     std::vector<gb::SysDev> sd;
     int st = gb::make_sysdev(nsys, sys, stream, sd);
     if (st) return st;
-    std::vector<long long> base(nsys + 1, 0);
     int Lmax = 1, Mmax = 0;
+    long long total_pairs = 0;
     for (int s = 0; s < nsys; s++) {
-        base[s + 1] = base[s] + sd[s].P;
         Lmax = std::max(Lmax, sd[s].lmax);
         Mmax = std::max(Mmax, sd[s].M);
+        total_pairs += sd[s].P;
     }
-    const long long total = base[nsys];
-    if (total == 0) return GB_OK;
-    // one staging upload: descriptors then pair prefix sums
+    if (total_pairs == 0) return GB_OK;
+    const bool fp64_sums = dense || out128 != nullptr;
+    const bool want64 = (out64 != nullptr || out64lo != nullptr) && !dense;
+    // pairs per group: the largest power of two up to 32 whose special-function
+    // tables keep the CTA within ~100 KB of shared memory (at least one pair)
+    int PB = 32;
+    while (PB > 1 && asm_layout(Lmax, Mmax, PB, fp64_sums, want64).total > 100 * 1024) PB >>= 1;
+    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, fp64_sums, want64);
+    const size_t smem = lay.total;
+    if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
+    std::vector<long long> gbase(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) gbase[s + 1] = gbase[s] + (sd[s].P + PB - 1) / PB;
+    const long long ngroups = gbase[nsys];
+    // one staging upload: descriptors then group prefix sums
     std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * (nsys + 1));
     memcpy(blob.data(), sd.data(), sizeof(gb::SysDev) * nsys);
-    memcpy(blob.data() + sizeof(gb::SysDev) * nsys, base.data(), sizeof(long long) * (nsys + 1));
+    memcpy(blob.data() + sizeof(gb::SysDev) * nsys, gbase.data(), sizeof(long long) * (nsys + 1));
     void* dblob = nullptr;
     int slot = 0;
     st = gb::stage_acquire(blob.data(), blob.size(), stream, &dblob, &slot);
     if (st) return st;
     const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
     const long long* dbase = reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys);
-    const AsmSmem lay = asm_layout(Lmax, Mmax, (out64 != nullptr || out64lo != nullptr) && !dense);
-    const size_t smem = lay.total;
+    auto kfn = dense ? k_assemble<true, true> : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>);
+    GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
     int per_sm = 1;
-    if (dense) {
-        GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(k_assemble<true>), smem));
-        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<true>, kAsmThreads, smem));
-    } else {
-        GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(k_assemble<false>), smem));
-        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assemble<false>, kAsmThreads, smem));
-    }
+    GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
     if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
-    long long grid = std::min<long long>(total, (long long)gb::sm_count() * per_sm);
-    if (dense) {
-        gb::note_launch();
-        k_assemble<true><<<(unsigned)grid, kAsmThreads, smem, stream>>>(
-            dsys, nsys, dbase, total, pos, reinterpret_cast<const double2*>(mie), reinterpret_cast<double2*>(out128),
-            nullptr, nullptr, dense_ld);
-    } else {
-        gb::note_launch();
-        k_assemble<false><<<(unsigned)grid, kAsmThreads, smem, stream>>>(
-            dsys, nsys, dbase, total, pos, nullptr, reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64),
-            reinterpret_cast<float2*>(out64lo), 0);
-    }
+    const long long grid = std::min<long long>(ngroups, (long long)gb::sm_count() * per_sm);
+    gb::note_launch();
+    kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
+        dsys, nsys, dbase, ngroups, Lmax, Mmax, PB, pos, reinterpret_cast<const double2*>(mie),
+        reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
+        dense_ld);
     GB_CUDA_TRY(cudaGetLastError());
     return gb::stage_release(slot, stream);
 }

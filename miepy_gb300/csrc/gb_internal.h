@@ -16,6 +16,8 @@ struct Tables {
     int2* qab = nullptr;       // [M] (qmax_A, qmax_B)
     double* cA = nullptr;      // [M][lmax+1]
     double* cB = nullptr;      // [M][lmax+1]
+    float2* cA2 = nullptr;     // [M][lmax+1] (hi, lo) split of cA
+    float2* cB2 = nullptr;     // [M][lmax+1] (hi, lo) split of cB
     int* elem_map = nullptr;   // [B*B] (tuple << 2) | (is_B << 1) | negate
     double* neg_ratio = nullptr;   // [(2L+2)^2] (-1)^mu (p-mu)!/(p+mu)!
     int* rowinfo = nullptr;    // [B] rho(row) | eps_neg << 29 | sig_neg << 30
@@ -49,6 +51,8 @@ struct SysDev {
     const int2* qab;
     const double* cA;
     const double* cB;
+    const float2* cA2;
+    const float2* cB2;
     const int* elem_map;
     const double* neg_ratio;
     const int* rowinfo;

@@ -138,6 +138,17 @@ struct TableCache {
 };
 TableCache g_cache;
 
+// Double-float split of the coefficient tables: c = hi + lo, hi = fl32(c),
+// lo = fl32(c - hi), for the FP32-pipe tuple sums of the assembler.
+__global__ void k_split_coeffs(int n, const double* __restrict__ cA, const double* __restrict__ cB,
+                               float2* __restrict__ cA2, float2* __restrict__ cB2) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float ah = __double2float_rn(cA[e]), bh = __double2float_rn(cB[e]);
+    cA2[e] = make_float2(ah, __double2float_rn(cA[e] - (double)ah));
+    cB2[e] = make_float2(bh, __double2float_rn(cB[e] - (double)bh));
+}
+
 }   // namespace
 
 namespace gb {
@@ -221,6 +232,8 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     if (e == cudaSuccess) e = cudaMalloc(&T->qab, sizeof(int2) * M);
     if (e == cudaSuccess) e = cudaMalloc(&T->cA, sizeof(double) * M * Q);
     if (e == cudaSuccess) e = cudaMalloc(&T->cB, sizeof(double) * M * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&T->cA2, sizeof(float2) * M * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&T->cB2, sizeof(float2) * M * Q);
     if (e == cudaSuccess) e = cudaMalloc(&T->elem_map, sizeof(int) * B * B);
     if (e == cudaSuccess) e = cudaMalloc(&T->neg_ratio, sizeof(double) * PM * PM);
     if (e == cudaSuccess) e = cudaMalloc(&T->rowinfo, sizeof(int) * B);
@@ -235,10 +248,15 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
         k_tuple_table<<<(M + 127) / 128, 128, 0, stream>>>(L, M, T->nmvu, T->qab, T->cA, T->cB);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess) {
+        gb::note_launch();
+        k_split_coeffs<<<(M * Q + 255) / 256, 256, 0, stream>>>(M * Q, T->cA, T->cB, T->cA2, T->cB2);
+        e = cudaGetLastError();
+    }
     // the host vectors above go out of scope: make the copies complete first
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
-        cudaFree(T->nmvu); cudaFree(T->qab); cudaFree(T->cA); cudaFree(T->cB);
+        cudaFree(T->nmvu); cudaFree(T->qab); cudaFree(T->cA); cudaFree(T->cB); cudaFree(T->cA2); cudaFree(T->cB2);
         cudaFree(T->elem_map); cudaFree(T->neg_ratio); cudaFree(T->rowinfo); cudaFree(T->miecol);
         delete T;
         return gb_set_cuda_error(e, "building translation tables", __FILE__, __LINE__);
