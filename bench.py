@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 NM = 1e-9
 TOL = 1e-8
+INNER_TOL = 1e-4   # relative residual of each FP32 inner solve of the mixed method
 WORKLOAD = "random cluster N=200 lmax=4 R=2 (D=9600), n=1.5+0.01i, vacuum, 600 nm, seed 2"
 # DRAM bytes (read + write) of one k_pgemv<Pol32> launch on this workload, from one
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); summary and command in
@@ -159,7 +160,7 @@ def run_gpu(args, rank, world):
 
     def one_solve(batch, precision):
         batch.assemble()
-        batch.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8, precision=precision)
+        batch.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8, precision=precision)
         batch.epilogue(W["eps_b"])
 
     # ---- resident inputs
@@ -339,20 +340,20 @@ def run_sweep(args):
     def timed(precision, steps, warmup):
         b = ClusterBatch(specs, R=1, precision=precision, device=dev)
         for _ in range(warmup):
-            b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); b.epilogue(1.0)
+            b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8); b.epilogue(1.0)
         torch.cuda.synchronize()
         evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
         n0 = L.gb_launch_count()
         evs[0].record(stream)
         for k in range(steps):
-            b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); b.epilogue(1.0)
+            b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8); b.epilogue(1.0)
             evs[k + 1].record(stream)
         torch.cuda.synchronize()
         per = np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(steps)])
         # phase split of one more step (events between the phases)
         ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         ph[0].record(stream); b.assemble(); ph[1].record(stream)
-        b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); ph[2].record(stream)
+        b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8); ph[2].record(stream)
         b.epilogue(1.0); ph[3].record(stream)
         torch.cuda.synchronize()
         phases = dict(assemble_ms=ph[0].elapsed_time(ph[1]), solve_ms=ph[1].elapsed_time(ph[2]),
@@ -477,7 +478,7 @@ def run_large(args):
     L = nat_lib()
 
     def step(b):
-        b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); b.epilogue(eps_b)
+        b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8); b.epilogue(eps_b)
 
     clocks = ClockSampler(dev.index).start()
     b = ClusterBatch([spec], R=1, precision="mixed", device=dev)
@@ -497,7 +498,7 @@ def run_large(args):
     t = ev[0].elapsed_time(ev[-1]) / 1e3
     ph = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ph[0].record(stream); b.assemble(); ph[1].record(stream)
-    b.solve(tol=TOL, maxiter=1000, inner_tol=1e-5, max_refine=8); ph[2].record(stream)
+    b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8); ph[2].record(stream)
     b.epilogue(eps_b); ph[3].record(stream)
     torch.cuda.synchronize()
     phases = dict(assemble_ms=ph[0].elapsed_time(ph[1]), solve_ms=ph[1].elapsed_time(ph[2]),

@@ -137,7 +137,7 @@ class ClusterBatch:
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
         return self._ws
 
-    def solve(self, tol=1e-5, maxiter=1000, inner_tol=1e-6, max_refine=6, precision=None, raise_on_fail=False):
+    def solve(self, tol=1e-5, maxiter=1000, inner_tol=1e-4, max_refine=8, precision=None, raise_on_fail=False):
         if not self.assembled:
             self.assemble()
         precision = precision or self.precision

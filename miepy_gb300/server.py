@@ -97,7 +97,7 @@ class SolveServer:
     a ClusterResult."""
 
     def __init__(self, hbm_budget=None, max_waves=3, max_wave_requests=64, precision="mixed", tol=1e-8,
-                 inner_tol=1e-5, maxiter=1000, device=None):
+                 inner_tol=1e-4, maxiter=1000, device=None):
         self.device = require_cuda(device)
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info(self.device)

@@ -88,7 +88,7 @@ def _batches(specs, R, precision, max_batch_bytes):
 
 
 def wavelength_sweep(position, radius, material, wavelengths, lmax=adaptive_lmax, medium=None, sources=None,
-                     precision="mixed", tol=1e-8, inner_tol=1e-5, max_refine=8, maxiter=1000, device=None,
+                     precision="mixed", tol=1e-8, inner_tol=1e-4, max_refine=8, maxiter=1000, device=None,
                      max_batch_bytes=None, per_particle=False, specs=None):
     """Spectra of a sphere cluster over many wavelengths, solved as ragged batches.
 
