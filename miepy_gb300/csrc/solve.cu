@@ -842,6 +842,11 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
         k.rho = k.alpha = k.omega = make_double2(1, 0);
         k.iters = k.restarts = k.need_restart = 0;
         k.maxiter = maxiter;
+        if (!isfinite(d0.x)) {   // a non-finite right-hand side: no comparison below may call it converged
+            k.done = 1;
+            k.status = GB_NAN;
+            return;
+        }
         if (d0.x == 0.0 || !(k.rsq > k.tol2) || maxiter <= 0) {
             k.done = 1;
             k.status = GB_OK;
@@ -860,6 +865,7 @@ __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __r
         const double2 rho_old = k.rho;
         k.rho = make_double2(d0.x, 0.0);
         if (k.restarts++ == 0) k.iters = 0;
+        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
         if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
         k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
         if (!finite2(k.beta)) { k.done = 1; k.status = GB_BREAKDOWN; }
@@ -952,6 +958,11 @@ __global__ void k_outer_init(const SysPlan* __restrict__ plan, int nsys, KState*
     k.bsq = s;
     k.tol2 = tol * tol * s;
     k.rsq = s;
+    if (!isfinite(s)) {   // non-finite right-hand side
+        k.done = 1;
+        k.status = GB_NAN;
+        return;
+    }
     k.done = (s == 0.0) ? 1 : 0;
     k.status = k.done ? GB_OK : ST_RUNNING;
 }

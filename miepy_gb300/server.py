@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import collections
 import concurrent.futures as cf
+import json
 import threading
 import time
 from dataclasses import dataclass, field
@@ -72,6 +73,23 @@ class OverBudget(RuntimeError):
     """A request larger than the whole HBM budget."""
 
 
+def validate_request(req: ClusterRequest):
+    """Rejects requests that the solver could only answer with NaN: non-finite
+    positions, radii, indices or wavelength, non-positive sizes, lmax out of 1..8."""
+    pos = np.asarray(np.atleast_2d(req.position), float)
+    if pos.ndim != 2 or pos.shape[1] != 3 or pos.shape[0] < 1:
+        raise ValueError(f"request {req.rid}: position must be [N, 3]")
+    arrays = dict(position=pos, radius=np.asarray(req.radius, float), index=np.asarray(req.index, complex),
+                  wavelength=np.asarray(req.wavelength, float), medium_index=np.asarray(req.medium_index, float))
+    for name, a in arrays.items():
+        if not np.all(np.isfinite(a)):
+            raise ValueError(f"request {req.rid}: non-finite {name}")
+    if np.any(arrays["radius"] <= 0) or req.wavelength <= 0 or req.medium_index <= 0:
+        raise ValueError(f"request {req.rid}: radius, wavelength and medium index must be positive")
+    if not (1 <= int(req.lmax) <= 8):
+        raise ValueError(f"request {req.rid}: lmax must be in 1..8")
+
+
 def request_spec(req: ClusterRequest):
     """Host inputs of one request: Mie coefficients, wavenumber and p_src."""
     pos = np.asarray(np.atleast_2d(req.position), float)
@@ -97,11 +115,17 @@ class SolveServer:
     a ClusterResult."""
 
     def __init__(self, hbm_budget=None, max_waves=3, max_wave_requests=64, precision="mixed", tol=1e-8,
-                 inner_tol=1e-4, maxiter=1000, device=None):
-        self.device = require_cuda(device)
-        if hbm_budget is None:
-            free, _ = torch.cuda.mem_get_info(self.device)
-            hbm_budget = int(0.8 * free)
+                 inner_tol=1e-4, maxiter=1000, device=None, max_retries=2, fault_hook=None, metrics_path=None):
+        """max_retries: times a request whose wave failed (an exception on the host,
+        e.g. an allocation failure) is re-admitted before its Future gets the error.
+        fault_hook(wave_id, requests): called at the start of every wave; an exception
+        it raises fails that wave (fault injection for tests).  metrics_path: JSONL
+        file receiving one line per finished request."""
+        self.max_retries = int(max_retries)
+        self.fault_hook = fault_hook
+        self.metrics_path = metrics_path
+        self._metrics_lock = threading.Lock()
+        hbm_budget = self._setup_device(device, hbm_budget)
         self.budget = int(hbm_budget)
         self.max_waves = int(max_waves)
         self.max_wave_requests = int(max_wave_requests)
@@ -113,22 +137,37 @@ class SolveServer:
         self._waves_running = 0
         self._wave_counter = 0
         self._closing = False
-        self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.max_waves)]
         self._free_streams = list(range(self.max_waves))
+        self._streams = self._make_streams()
         # persistent workers: the native library keeps per-thread staging buffers
         # and capture streams, reused wave after wave
         self._pool = cf.ThreadPoolExecutor(max_workers=self.max_waves, thread_name_prefix="miepy-gb300-wave")
-        self.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0)
+        self.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0,
+                          failed_waves=0, readmitted=0, cancelled=0)
         self._dispatcher = threading.Thread(target=self._dispatch, name="miepy-gb300-dispatch", daemon=True)
         self._dispatcher.start()
 
+    def _setup_device(self, device, hbm_budget):
+        self.device = require_cuda(device)
+        if hbm_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            hbm_budget = int(0.8 * free)
+        return hbm_budget
+
+    def _make_streams(self):
+        return [torch.cuda.Stream(device=self.device) for _ in range(self.max_waves)]
+
     # --------------------------------------------------------------- client --
     def submit(self, req: ClusterRequest) -> cf.Future:
+        """Queues a request; raises ValueError for inputs that cannot be solved
+        (see validate_request).  Cancelling the Future before its wave starts drops
+        the request."""
+        validate_request(req)
         fut = cf.Future()
         with self._cv:
             if self._closing:
                 raise RuntimeError("server is closed")
-            self._pending.append((req, fut, time.perf_counter()))
+            self._pending.append((req, fut, time.perf_counter(), 0))
             self._cv.notify_all()
         return fut
 
@@ -153,7 +192,11 @@ class SolveServer:
         wave, used = [], 0
         free = self.budget - self._in_use
         while self._pending and len(wave) < self.max_wave_requests:
-            req, fut, t0 = self._pending[0]
+            req, fut, t0, tries = self._pending[0]
+            if fut.cancelled():
+                self._pending.popleft()
+                self.stats["cancelled"] += 1
+                continue
             need = request_footprint(req, self.precision)
             if need > self.budget:
                 self._pending.popleft()
@@ -165,7 +208,10 @@ class SolveServer:
             if used + need > free:
                 break
             self._pending.popleft()
-            wave.append((req, fut, t0, need))
+            if not fut.running() and not fut.set_running_or_notify_cancel():   # cancelled meanwhile
+                self.stats["cancelled"] += 1
+                continue
+            wave.append((req, fut, t0, need, tries))
             used += need
         return wave, used
 
@@ -193,42 +239,76 @@ class SolveServer:
 
     def _run_wave(self, wave, used, sidx, wid):
         t_admit = time.perf_counter()
-        stream = self._streams[sidx]
+        requeue = []
         try:
-            with torch.cuda.device(self.device), torch.cuda.stream(stream):
-                specs = [request_spec(req) for req, _, _, _ in wave]
-                b = ClusterBatch(specs, R=1, precision=self.precision, device=self.device)
-                b.assemble()
-                b.solve(tol=self.tol, maxiter=self.maxiter, inner_tol=self.inner_tol, max_refine=8)
-                b.epilogue(specs[0]["eps_b"])
-                xs = b.xs[: b.totals["obs"] * 6 * b.xs_L].view(-1, 3, 2 * b.xs_L).cpu().numpy()
-                F = b.F[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
-                T = b.T[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
-                x = b.x.cpu().numpy()
-                status, iters = b.status.copy(), b.iters.copy()
-                del b
+            if self.fault_hook is not None:
+                self.fault_hook(wid, [w[0] for w in wave])
+            results = self._execute(wave, sidx)
             t_done = time.perf_counter()
-            for s, (req, fut, t0, _) in enumerate(wave):
-                l = _layout(specs, s)
-                o, N, L = l["obs_off"], l["N"], l["lmax"]
-                C = xs[o: o + N, :, : 2 * L].sum(axis=(0, 2))
-                res = ClusterResult(rid=req.rid, status=int(status[s]), passes=int(iters[s]), C_sca=float(C[0]),
-                                    C_abs=float(C[1]), C_ext=float(C[2]),
-                                    p_inc=x[l["vec_off"]: l["vec_off"] + l["D"]].reshape(N, 2, l["rmax"]),
-                                    force=F[o: o + N].copy(), torque=T[o: o + N].copy(), t_submit=t0,
-                                    t_admit=t_admit, t_done=t_done, wave=wid, wave_size=len(wave))
+            for (req, fut, t0, _, _), res in zip(wave, results):
+                res.t_submit, res.t_admit, res.t_done = t0, t_admit, t_done
+                res.wave, res.wave_size = wid, len(wave)
+                self._record(req, res)
                 fut.set_result(res)
-        except Exception as exc:   # every request of a failed wave learns why
-            for _, fut, _, _ in wave:
-                if not fut.done():
+        except Exception as exc:
+            # the wave failed on the host (allocation, a library error): its requests
+            # are admitted again, up to max_retries times each, then fail with exc
+            for req, fut, t0, _, tries in wave:
+                if fut.done():
+                    continue
+                if tries < self.max_retries:
+                    requeue.append((req, fut, t0, tries + 1))
+                else:
                     fut.set_exception(exc)
         finally:
             with self._cv:
                 self._in_use -= used
                 self._waves_running -= 1
                 self._free_streams.append(sidx)
-                self.stats["completed"] += len(wave)
+                if requeue:
+                    self.stats["failed_waves"] += 1
+                    self.stats["readmitted"] += len(requeue)
+                    self._pending.extendleft(reversed(requeue))   # keep arrival order at the head
+                self.stats["completed"] += len(wave) - len(requeue)
                 self._cv.notify_all()
+
+    def _execute(self, wave, sidx):
+        """Solves one wave on its stream: one ragged ClusterBatch, assembled,
+        solved and reduced; returns one ClusterResult per request."""
+        stream = self._streams[sidx]
+        with torch.cuda.device(self.device), torch.cuda.stream(stream):
+            specs = [request_spec(w[0]) for w in wave]
+            b = ClusterBatch(specs, R=1, precision=self.precision, device=self.device)
+            b.assemble()
+            b.solve(tol=self.tol, maxiter=self.maxiter, inner_tol=self.inner_tol, max_refine=8)
+            b.epilogue(specs[0]["eps_b"])
+            xs = b.xs[: b.totals["obs"] * 6 * b.xs_L].view(-1, 3, 2 * b.xs_L).cpu().numpy()
+            F = b.F[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
+            T = b.T[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
+            x = b.x.cpu().numpy()
+            status, iters = b.status.copy(), b.iters.copy()
+            del b
+        out = []
+        for s, w in enumerate(wave):
+            req = w[0]
+            l = _layout(specs, s)
+            o, N, L = l["obs_off"], l["N"], l["lmax"]
+            C = xs[o: o + N, :, : 2 * L].sum(axis=(0, 2))
+            out.append(ClusterResult(rid=req.rid, status=int(status[s]), passes=int(iters[s]), C_sca=float(C[0]),
+                                     C_abs=float(C[1]), C_ext=float(C[2]),
+                                     p_inc=x[l["vec_off"]: l["vec_off"] + l["D"]].reshape(N, 2, l["rmax"]),
+                                     force=F[o: o + N].copy(), torque=T[o: o + N].copy()))
+        return out
+
+    def _record(self, req, res):
+        if not self.metrics_path:
+            return
+        N = np.asarray(np.atleast_2d(req.position)).shape[0]
+        line = dict(rid=req.rid, N=int(N), lmax=int(req.lmax), status=res.status, passes=res.passes,
+                    latency_ms=1e3 * res.latency, wait_ms=1e3 * (res.t_admit - res.t_submit), wave=res.wave,
+                    wave_size=res.wave_size, footprint_bytes=int(request_footprint(req, self.precision)))
+        with self._metrics_lock, open(self.metrics_path, "a") as f:
+            f.write(json.dumps(line) + "\n")
 
 
 def _layout(specs, s):

@@ -1,7 +1,10 @@
 """Continuous-batching solve server.
 
 CPU: admission in arrival order within the HBM budget, over-budget rejection, one
-medium per wave, and the request generator of the serving workload.
+medium per wave, the request generator of the serving workload, and host-side fault
+injection through a server whose wave execution is replaced by a fake: a failing
+wave re-admits its requests, persistent failure reaches the caller, cancelled
+requests are dropped, non-finite inputs are rejected, metrics are streamed.
 GPU: every result is the same alone and in the mix (tolerance: C_ext within 1e-8
 relative, p_inc within 1e-8 of its largest coefficient, at solve tolerance 1e-10),
 with waves overlapping on the device; Gaussian-beam and plane-wave requests mixed.
@@ -9,7 +12,9 @@ with waves overlapping on the device; Gaussian-beam and plane-wave requests mixe
 
 import collections
 import concurrent.futures as cf
+import json
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -24,7 +29,8 @@ def _bare_server(budget, max_wave_requests=8, precision="mixed"):
     s.precision = precision
     s._pending = collections.deque()
     s._in_use = 0
-    s.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0)
+    s.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0,
+                   failed_waves=0, readmitted=0, cancelled=0)
     return s
 
 
@@ -41,7 +47,7 @@ def test_admission_fifo_budget_and_rejection():
     for r in reqs:
         f = cf.Future()
         futs.append(f)
-        s._pending.append((r, f, 0.0))
+        s._pending.append((r, f, 0.0, 0))
     wave, used = s._take_wave()
     assert [w[0].rid for w in wave] == [0, 1, 3]       # request 2 exceeds the whole budget ...
     assert used == need[0] + need[1] + need[3]
@@ -50,7 +56,7 @@ def test_admission_fifo_budget_and_rejection():
     assert not s._pending
     s2 = _bare_server(budget=need[0] + need[1])
     for r in (reqs[0], reqs[1], reqs[3]):
-        s2._pending.append((r, cf.Future(), 0.0))
+        s2._pending.append((r, cf.Future(), 0.0, 0))
     wave, used = s2._take_wave()
     assert [w[0].rid for w in wave] == [0, 1]          # request 3 waits: the budget is used up
     s2._in_use = used - need[0]                         # request 0's wave finished
@@ -63,7 +69,7 @@ def test_admission_waits_for_memory_and_splits_media():
     na = SV.request_footprint(a, "mixed")
     s = _bare_server(budget=int(1.5 * na))
     for r in (a, b):
-        s._pending.append((r, cf.Future(), 0.0))
+        s._pending.append((r, cf.Future(), 0.0, 0))
     wave, used = s._take_wave()
     assert [w[0].rid for w in wave] == [0]
     s._in_use = used
@@ -71,7 +77,7 @@ def test_admission_waits_for_memory_and_splits_media():
     assert wave == []                                   # request 1 waits for request 0's memory
     s2 = _bare_server(budget=10 * na)
     for r in (_req(10, 3, 0, 1.0), _req(10, 3, 1, 1.33), _req(10, 3, 2, 1.0)):
-        s2._pending.append((r, cf.Future(), 0.0))
+        s2._pending.append((r, cf.Future(), 0.0, 0))
     wave, _ = s2._take_wave()
     assert [w[0].rid for w in wave] == [0]              # one medium per wave
 
@@ -91,6 +97,90 @@ def test_request_generator():
         beams += type(r.source).__name__ == "gaussian_beam"
     assert min(Ns) >= 2 and max(Ns) <= 60 and set(Ls) <= set(range(2, 9))
     assert 10 < beams < 50
+
+
+class FakeServer(SV.SolveServer):
+    """The dispatcher, admission and fault handling of SolveServer with the GPU
+    work replaced by a fake that answers after a short delay."""
+
+    delay = 0.02
+
+    def _setup_device(self, device, hbm_budget):
+        self.device = None
+        return hbm_budget
+
+    def _make_streams(self):
+        return [None] * self.max_waves
+
+    def _execute(self, wave, sidx):
+        time.sleep(self.delay)
+        return [SV.ClusterResult(rid=w[0].rid, status=0, passes=1, C_sca=1.0, C_abs=0.0, C_ext=1.0 + w[0].rid,
+                                 p_inc=np.zeros((1, 2, 3)), force=np.zeros((1, 3)), torque=np.zeros((1, 3)))
+                for w in wave]
+
+
+def test_failed_wave_readmits_its_requests(tmp_path):
+    calls = []
+
+    def hook(wid, reqs):
+        calls.append(wid)
+        if wid == 0:
+            raise MemoryError("injected allocation failure")
+
+    metrics = tmp_path / "metrics.jsonl"
+    with FakeServer(hbm_budget=10 ** 12, max_waves=1, max_wave_requests=4, fault_hook=hook,
+                    metrics_path=str(metrics)) as srv:
+        futs = [srv.submit(_req(5, 2, i)) for i in range(6)]
+        res = [f.result(timeout=30) for f in futs]
+        stats = dict(srv.stats)
+    assert [r.rid for r in res] == list(range(6))
+    assert [r.C_ext for r in res] == [1.0 + i for i in range(6)]
+    assert stats["failed_waves"] == 1 and stats["readmitted"] >= 1
+    assert stats["completed"] == 6 and srv._in_use == 0
+    lines = [json.loads(l) for l in metrics.read_text().splitlines()]
+    assert sorted(l["rid"] for l in lines) == list(range(6))
+    assert all(l["latency_ms"] >= l["wait_ms"] >= 0 for l in lines)
+
+
+def test_persistent_failure_reaches_the_caller():
+    def hook(wid, reqs):
+        raise RuntimeError("injected")
+
+    with FakeServer(hbm_budget=10 ** 12, max_waves=2, max_retries=2, fault_hook=hook) as srv:
+        f = srv.submit(_req(5, 2, 0))
+        with pytest.raises(RuntimeError, match="injected"):
+            f.result(timeout=30)
+        assert srv.stats["readmitted"] == 2          # two re-admissions, then the error
+    assert srv._in_use == 0
+
+
+def test_cancelled_requests_are_dropped():
+    class Slow(FakeServer):
+        delay = 0.3
+
+    with Slow(hbm_budget=10 ** 12, max_waves=1, max_wave_requests=1) as srv:
+        first = srv.submit(_req(5, 2, 0))
+        time.sleep(0.05)                             # request 0 is on the (fake) GPU
+        queued = [srv.submit(_req(5, 2, i)) for i in (1, 2)]
+        assert queued[0].cancel()
+        assert first.result(timeout=30).rid == 0
+        assert queued[1].result(timeout=30).rid == 2
+        assert queued[0].cancelled()
+        assert srv.stats["cancelled"] == 1
+
+
+def test_non_finite_inputs_rejected_at_submit():
+    with FakeServer(hbm_budget=10 ** 12) as srv:
+        bad = _req(4, 2, 0)
+        bad.position[1, 2] = np.nan
+        with pytest.raises(ValueError, match="non-finite position"):
+            srv.submit(bad)
+        with pytest.raises(ValueError, match="lmax"):
+            srv.submit(_req(4, 9, 1))
+        r = _req(4, 2, 2)
+        r.index = complex(np.inf, 0)
+        with pytest.raises(ValueError, match="non-finite index"):
+            srv.submit(r)
 
 
 @pytest.mark.gpu
@@ -128,3 +218,22 @@ def test_server_against_fp64_single_cluster():
     C = c.cross_sections()
     assert abs(res.C_ext - C.extinction) <= 1e-8 * abs(C.extinction)
     assert np.max(np.abs(res.p_inc - c.p_inc)) <= 1e-8 * np.max(np.abs(c.p_inc))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_nan_right_hand_side_reported_per_cluster(precision):
+    """A NaN in one cluster's source is reported as that cluster's status (GB_NAN),
+    without an error for the call, and its batch-mate still converges."""
+    from miepy_gb300 import _native as nat
+    from miepy_gb300.engine import ClusterBatch
+    rng = np.random.default_rng(6)
+    s1 = SV.request_spec(SV.random_request(rng, rid=0, n_range=(6, 8), lmax_range=(3, 3)))
+    s2 = SV.request_spec(SV.random_request(rng, rid=1, n_range=(6, 8), lmax_range=(3, 3)))
+    s2["p_src"] = np.array(s2["p_src"])
+    s2["p_src"][0, 0, 0] = np.nan
+    b = ClusterBatch([s1, s2], R=1, precision=precision)
+    b.assemble()
+    b.solve(tol=1e-8)
+    assert b.status[0] == nat.GB_OK
+    assert b.status[1] == nat.GB_NAN
