@@ -236,6 +236,15 @@ struct PolDF {
     }
 };
 
+// Optional BiCGSTAB vector update folded into the y-vector preparation of the
+// next product (kind 1: p-update into out = p; kind 2: s-update into out = s).
+template <typename VT> struct YUpd {
+    int kind = 0;
+    const VT* r = nullptr;
+    const VT* v = nullptr;
+    VT* out = nullptr;
+};
+
 // ------------------------------------------------------------ y vectors --
 // For every row (particle k, local row r) of every cluster:
 //   z = eps(r) t_k[rho(r)] x_k[rho(r)],   Yu = z,  Yw = sig(r) z
@@ -262,7 +271,7 @@ template <int YK, typename VT, int R>
 __global__ void __launch_bounds__(kVRows)
 k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
         int mask_mode, const double2* __restrict__ tvec, const VT* __restrict__ x, typename YType<YK>::t* __restrict__ Yu,
-        typename YType<YK>::t* __restrict__ Yw) {
+        typename YType<YK>::t* __restrict__ Yw, YUpd<VT> up) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
@@ -279,7 +288,30 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
     const double2 t = tvec[S.t_off + src];
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
-        const double2 z = cmul(t, to_d2(x[S.vec_off + src * R + rr]));
+        const long long es = S.vec_off + src * R + rr;
+        double2 xv;
+        if (up.kind != 0 && active_rhs<R>(st, I.sys, rr, 0)) {
+            // the BiCGSTAB vector update this product's input needs, on the source row
+            // this thread alone reads: p = r + beta (p - omega v) or s = r - alpha v
+            const KState& k = st[I.sys * R + rr];
+            const double2 rv = to_d2(up.r[es]), vv = to_d2(up.v[es]);
+            double2 nv;
+            if (up.kind == 1) {
+                const double2 pv = to_d2(up.out[es]);
+                const double2 ov = cmul(k.omega, vv);
+                const double2 bt = cmul(k.beta, make_double2(pv.x - ov.x, pv.y - ov.y));
+                nv = make_double2(rv.x + bt.x, rv.y + bt.y);
+            } else {
+                const double2 av = cmul(k.alpha, vv);
+                nv = make_double2(rv.x - av.x, rv.y - av.y);
+            }
+            const VT q = from_d2<VT>(nv);
+            up.out[es] = q;
+            xv = to_d2(q);
+        } else {
+            xv = to_d2(x[es]);
+        }
+        const double2 z = cmul(t, xv);
         const double2 yu = make_double2(flipd(z.x, eneg), flipd(z.y, eneg));
         const double2 yw = make_double2(flipd(yu.x, sneg), flipd(yu.y, sneg));
         const long long o = S.vec_off + (long long)row * R + rr;
@@ -561,6 +593,145 @@ k_dense_gemv(int D, const double2* __restrict__ T, const double2* __restrict__ x
     }
 }
 
+// ------------------------------------------------------------ K4 scalars --
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+    const double den = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+__device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
+// Phases: 0 init (vector dots: |b|^2); 1 alpha = rho/<r0,v> (reduce dots);
+// 2 omega = <t,s>/|t|^2 (reduce dots); 3 end of iteration (vector dots |r|^2,
+// <r0,r>: convergence, restart test, beta); 4 restart done (reduce dots |r|^2).
+// One warp per (cluster, rhs): lanes stride over the item partials, a fixed
+// butterfly combines them (deterministic), lane 0 updates the scalars.
+template <int R>
+__device__ void scalar_step(const SysPlan* __restrict__ plan, KState* __restrict__ st, int phase,
+                            const double2* __restrict__ dots, double tol, int maxiter, int sidx, int rr, int lane) {
+    KState& k = st[sidx * R + rr];
+    if (phase != 0 && phase != 4 && (k.done || k.need_restart)) return;
+    if (phase == 4 && !k.need_restart) return;
+    const SysPlan pl = plan[sidx];
+    const bool vec = (phase == 0 || phase == 3);
+    const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
+    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+    for (int it = b0 + lane; it < b1; it += 32) {
+        const double2 a = __ldcg(dots + ((long long)it * R + rr) * 2 + 0);   // L2: other CTAs wrote them
+        const double2 c = __ldcg(dots + ((long long)it * R + rr) * 2 + 1);
+        d0.x += a.x; d0.y += a.y;
+        d1.x += c.x; d1.y += c.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
+        d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
+        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
+        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
+    }
+    if (lane != 0) return;
+    const double eps = 2.220446049250313e-16;
+    if (phase == 0) {
+        k.bsq = k.r0sq = k.rsq = d0.x;
+        k.tol2 = tol * tol * d0.x;
+        k.rho = k.alpha = k.omega = make_double2(1, 0);
+        k.iters = k.restarts = k.need_restart = 0;
+        k.maxiter = maxiter;
+        if (!isfinite(d0.x)) {   // a non-finite right-hand side: no comparison below may call it converged
+            k.done = 1;
+            k.status = GB_NAN;
+            return;
+        }
+        if (d0.x == 0.0 || !(k.rsq > k.tol2) || maxiter <= 0) {
+            k.done = 1;
+            k.status = GB_OK;
+        } else {
+            k.done = 0;
+            k.status = ST_RUNNING;
+            const double2 rho_old = k.rho;          // loop top of the first iteration
+            k.rho = make_double2(d0.x, 0.0);        // <r0, r> = |b|^2
+            k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
+        }
+        return;
+    }
+    if (phase == 4) {   // Eigen: r = b - A x; r0 = r; rho = r0_sqnorm = |r|^2; the first restart resets i
+        k.need_restart = 0;
+        k.rsq = k.r0sq = d0.x;
+        const double2 rho_old = k.rho;
+        k.rho = make_double2(d0.x, 0.0);
+        if (k.restarts++ == 0) k.iters = 0;
+        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
+        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
+        k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
+        if (!finite2(k.beta)) { k.done = 1; k.status = GB_BREAKDOWN; }
+        return;
+    }
+    if (phase == 1) {
+        k.alpha = cdiv(k.rho, d0);
+        if (!finite2(k.alpha)) { k.done = 1; k.status = (d0.x == 0 && d0.y == 0) ? GB_BREAKDOWN : GB_NAN; }
+    } else if (phase == 2) {
+        const double tt = d0.x;
+        k.omega = (tt > 0.0) ? make_double2(d1.x / tt, d1.y / tt) : make_double2(0, 0);
+        if (!finite2(k.omega)) { k.done = 1; k.status = GB_NAN; }
+    } else if (phase == 3) {
+        k.iters += 1;
+        k.rsq = d0.x;
+        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
+        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
+        if (k.iters >= k.maxiter) { k.done = 1; k.status = GB_NOT_CONVERGED; return; }
+        const double2 rho_old = k.rho;
+        k.rho = d1;   // <r0, r>
+        if (sqrt(k.rho.x * k.rho.x + k.rho.y * k.rho.y) < eps * eps * k.r0sq) {
+            if (k.restarts >= kMaxRestarts) { k.done = 1; k.status = GB_BREAKDOWN; return; }
+            k.rho = rho_old;   // phase 4 recomputes rho from the fresh residual
+            k.need_restart = 1;
+            return;
+        }
+        k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
+        if (!finite2(k.beta)) { k.done = 1; k.status = GB_NAN; }
+    }
+}
+
+template <int R>
+__global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ st, int phase,
+                         const double2* __restrict__ dots, double tol, int maxiter) {
+    const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (id >= nsys * R) return;
+    scalar_step<R>(plan, st, phase, dots, tol, maxiter, id / R, id % R, lane);
+}
+
+// Scalar update fused into the kernel that produces its partial dots: each CTA
+// of a cluster counts itself in after writing its partials; the last one (all of
+// the cluster's partials are then visible) runs scalar_step for every rhs with
+// its warp 0 and resets the counter for the next launch.  The partials are summed
+// in the same fixed order as by k_scalar.
+struct ScalarFuse {
+    KState* st = nullptr;   // null: no fused update
+    int* cnt = nullptr;     // [nsys] arrivals, zero between launches
+    int phase = 0;
+    double tol = 0;
+    int maxiter = 0;
+};
+
+// Called by warp 0 of a CTA of cluster sys after its partial dots are written.
+template <int R>
+__device__ void fused_scalar(const ScalarFuse& fz, const SysPlan* __restrict__ plan, const double2* __restrict__ dots,
+                             int sys, int nitems_sys, int lane) {
+    int last = 0;
+    if (lane == 0) {
+        __threadfence();
+        const int old = atomicAdd(fz.cnt + sys, 1);
+        last = (old == nitems_sys - 1);
+        if (last) {
+            fz.cnt[sys] = 0;
+            __threadfence();
+        }
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+#pragma unroll
+    for (int rr = 0; rr < R; rr++) scalar_step<R>(plan, fz.st, fz.phase, dots, fz.tol, fz.maxiter, sys, rr, lane);
+}
+
 // --------------------------------------------------------------- K3b reduce --
 // Per-lane sum of partials: plain sums for float2 / double2 partials, a
 // double-float sum for the double-float complex partials (re.h, im.h, re.l, im.l).
@@ -589,7 +760,7 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
          const SysPlan* __restrict__ plan, const long long* __restrict__ row_strip, const KState* __restrict__ st,
          int mask_mode, const OutT* __restrict__ CU, const OutT* __restrict__ CW, const double2* __restrict__ Tx_dense,
          const VT* __restrict__ x, VT* __restrict__ y, int mode, const VT* __restrict__ aux,
-         const double2* __restrict__ b128, double2* __restrict__ dots) {
+         const double2* __restrict__ b128, double2* __restrict__ dots, ScalarFuse fz) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
@@ -705,6 +876,10 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
             dots[((long long)it * R + rr) * 2 + 1] = d1[rr];
         }
     }
+    if (fz.st) {
+        const SysPlan pl = plan[I.sys];
+        fused_scalar<R>(fz, plan, dots, I.sys, pl.rend - pl.rbeg, lane);
+    }
 }
 
 // ------------------------------------------------------- K4 vector updates --
@@ -718,7 +893,7 @@ __global__ void __launch_bounds__(kVRows)
 k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
       int kind, const double2* __restrict__ b, VT* __restrict__ bx, VT* __restrict__ x, VT* __restrict__ r,
       VT* __restrict__ r0, VT* __restrict__ p, VT* __restrict__ v, VT* __restrict__ s, const VT* __restrict__ t,
-      double2* __restrict__ dots) {
+      double2* __restrict__ dots, const SysPlan* __restrict__ plan = nullptr, ScalarFuse fz = ScalarFuse()) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
@@ -794,106 +969,11 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
         }
         dots[((long long)it * R + rr) * 2 + which] = sm;
     }
-}
-
-// ------------------------------------------------------------ K4 scalars --
-__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-    const double den = b.x * b.x + b.y * b.y;
-    return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
-}
-__device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
-
-// Phases: 0 init (vector dots: |b|^2); 1 alpha = rho/<r0,v> (reduce dots);
-// 2 omega = <t,s>/|t|^2 (reduce dots); 3 end of iteration (vector dots |r|^2,
-// <r0,r>: convergence, restart test, beta); 4 restart done (reduce dots |r|^2).
-// One warp per (cluster, rhs): lanes stride over the item partials, a fixed
-// butterfly combines them (deterministic), lane 0 updates the scalars.
-template <int R>
-__global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ st, int phase,
-                         const double2* __restrict__ dots, double tol, int maxiter) {
-    const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (id >= nsys * R) return;
-    const int sidx = id / R, rr = id % R;
-    KState& k = st[id];
-    if (phase != 0 && phase != 4 && (k.done || k.need_restart)) return;
-    if (phase == 4 && !k.need_restart) return;
-    const SysPlan pl = plan[sidx];
-    const bool vec = (phase == 0 || phase == 3);
-    const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
-    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
-    for (int it = b0 + lane; it < b1; it += 32) {
-        const double2 a = dots[((long long)it * R + rr) * 2 + 0];
-        const double2 c = dots[((long long)it * R + rr) * 2 + 1];
-        d0.x += a.x; d0.y += a.y;
-        d1.x += c.x; d1.y += c.y;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
-        d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
-        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
-        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
-    }
-    if (lane != 0) return;
-    const double eps = 2.220446049250313e-16;
-    if (phase == 0) {
-        k.bsq = k.r0sq = k.rsq = d0.x;
-        k.tol2 = tol * tol * d0.x;
-        k.rho = k.alpha = k.omega = make_double2(1, 0);
-        k.iters = k.restarts = k.need_restart = 0;
-        k.maxiter = maxiter;
-        if (!isfinite(d0.x)) {   // a non-finite right-hand side: no comparison below may call it converged
-            k.done = 1;
-            k.status = GB_NAN;
-            return;
-        }
-        if (d0.x == 0.0 || !(k.rsq > k.tol2) || maxiter <= 0) {
-            k.done = 1;
-            k.status = GB_OK;
-        } else {
-            k.done = 0;
-            k.status = ST_RUNNING;
-            const double2 rho_old = k.rho;          // loop top of the first iteration
-            k.rho = make_double2(d0.x, 0.0);        // <r0, r> = |b|^2
-            k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
-        }
-        return;
-    }
-    if (phase == 4) {   // Eigen: r = b - A x; r0 = r; rho = r0_sqnorm = |r|^2; the first restart resets i
-        k.need_restart = 0;
-        k.rsq = k.r0sq = d0.x;
-        const double2 rho_old = k.rho;
-        k.rho = make_double2(d0.x, 0.0);
-        if (k.restarts++ == 0) k.iters = 0;
-        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
-        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
-        k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
-        if (!finite2(k.beta)) { k.done = 1; k.status = GB_BREAKDOWN; }
-        return;
-    }
-    if (phase == 1) {
-        k.alpha = cdiv(k.rho, d0);
-        if (!finite2(k.alpha)) { k.done = 1; k.status = (d0.x == 0 && d0.y == 0) ? GB_BREAKDOWN : GB_NAN; }
-    } else if (phase == 2) {
-        const double tt = d0.x;
-        k.omega = (tt > 0.0) ? make_double2(d1.x / tt, d1.y / tt) : make_double2(0, 0);
-        if (!finite2(k.omega)) { k.done = 1; k.status = GB_NAN; }
-    } else if (phase == 3) {
-        k.iters += 1;
-        k.rsq = d0.x;
-        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
-        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
-        if (k.iters >= k.maxiter) { k.done = 1; k.status = GB_NOT_CONVERGED; return; }
-        const double2 rho_old = k.rho;
-        k.rho = d1;   // <r0, r>
-        if (sqrt(k.rho.x * k.rho.x + k.rho.y * k.rho.y) < eps * eps * k.r0sq) {
-            if (k.restarts >= kMaxRestarts) { k.done = 1; k.status = GB_BREAKDOWN; return; }
-            k.rho = rho_old;   // phase 4 recomputes rho from the fresh residual
-            k.need_restart = 1;
-            return;
-        }
-        k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
-        if (!finite2(k.beta)) { k.done = 1; k.status = GB_NAN; }
+    if (fz.st && lr < 32) {
+        if (lr < R * 2) __threadfence();   // this lane's partial before the arrival count
+        __syncwarp();
+        const SysPlan pl = plan[I.sys];
+        fused_scalar<R>(fz, plan, dots, I.sys, pl.vend - pl.vbeg, lr);
     }
 }
 
@@ -1158,7 +1238,7 @@ WS ws_layout(const Plan& P, int prec, bool dense) {
     w.off_vec = take(vsz * (size_t)P.total_vec * 8);   // x r r0 p v s t b
     w.off_r128 = take((prec == GB_PREC_MIXED || prec == GB_PREC_MIXED_FP64RES) ? sizeof(double2) * (size_t)P.total_vec : 0);
     w.off_blob = take(sizeof(gb::SysDev) * P.nsys + sizeof(Strip) * P.nstrips + sizeof(Item) * (P.nv + P.nr) +
-                      sizeof(SysPlan) * P.nsys + sizeof(long long) * P.row_strip.size() + 256);
+                      sizeof(SysPlan) * P.nsys + sizeof(long long) * P.row_strip.size() + sizeof(int) * P.nsys + 256);
     w.total = o;
     return w;
 }
@@ -1171,6 +1251,7 @@ struct DevPlan {
     const SysPlan* sp;
     const long long* row_strip;
     int* err;   // set by a GEMV whose bounded wait on a copy expired
+    int* cnt;   // [nsys] arrival counters of the fused scalar updates (zero between launches)
 };
 
 int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t stream, DevPlan& D) {
@@ -1189,6 +1270,8 @@ int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t st
     size_t o_rs = put(P.row_strip.data(), sizeof(long long) * P.row_strip.size());
     const int zeros[4] = {0, 0, 0, 0};
     size_t o_err = put(zeros, sizeof(zeros));
+    const std::vector<int> counters(P.nsys, 0);
+    size_t o_cnt = put(counters.data(), sizeof(int) * P.nsys);
     unsigned char* dst = base + w.off_blob;
     void* dblob = nullptr;
     int slot = 0;
@@ -1204,6 +1287,7 @@ int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t st
     D.sp = reinterpret_cast<const SysPlan*>(dst + o_sp);
     D.row_strip = reinterpret_cast<const long long*>(dst + o_rs);
     D.err = reinterpret_cast<int*>(dst + o_err);
+    D.cnt = reinterpret_cast<int*>(dst + o_cnt);
     return GB_OK;
 }
 
@@ -1319,7 +1403,8 @@ int launch_df(const Plan& P, const DevPlan& D, const KState* st, int mask, const
 template <typename VT, int R>
 int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, const KState* st, int mask,
                  int pol, const void* mat_hi, const void* mat_lo, const double2* tvec, const VT* xin, VT* yout,
-                 int mode, const VT* aux, const double2* b128, double2* dots, cudaStream_t stream) {
+                 int mode, const VT* aux, const double2* b128, double2* dots, cudaStream_t stream,
+                 ScalarFuse fz = ScalarFuse(), YUpd<VT> up = YUpd<VT>()) {
     void* Yu = base + w.off_yu;
     void* Yw = base + w.off_yw;
     void* CU = base + w.off_cu;
@@ -1329,33 +1414,33 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     if (pol == 0) {
         gb::note_launch();
         k_yprep<0, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw));
+                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), up);
         if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
         k_reduce<double2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
             D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
-            reinterpret_cast<const double2*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+            reinterpret_cast<const double2*>(CW), nullptr, xin, yout, mode, aux, b128, dots, fz);
     } else if (pol == 1) {
         gb::note_launch();
         k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
+                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up);
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
         k_reduce<float2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
             D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
-            reinterpret_cast<const float2*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+            reinterpret_cast<const float2*>(CW), nullptr, xin, yout, mode, aux, b128, dots, fz);
     } else {
         gb::note_launch();
         k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw));
+                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up);
         if (P.nstrips) e = launch_df<R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
         k_reduce<float4, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
             D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float4*>(CU),
-            reinterpret_cast<const float4*>(CW), nullptr, xin, yout, mode, aux, b128, dots);
+            reinterpret_cast<const float4*>(CW), nullptr, xin, yout, mode, aux, b128, dots, fz);
     }
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
@@ -1450,8 +1535,17 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     const unsigned sblocks = (unsigned)((nsr * 32 + 127) / 128);
     const unsigned vb = (unsigned)P.nv;
 
+    auto fuse = [&](int phase) {
+        ScalarFuse f;
+        f.st = st;
+        f.cnt = D.cnt;
+        f.phase = phase;
+        f.tol = tol;
+        f.maxiter = maxiter;
+        return f;
+    };
     auto apply = [&](const VT* xin, VT* yout, int mode, const VT* aux, int mask, const double2* bb,
-                     cudaStream_t sm) -> int {
+                     cudaStream_t sm, ScalarFuse fz = ScalarFuse(), YUpd<VT> up = YUpd<VT>()) -> int {
         if (DENSE) {
             const long long grid = std::min<long long>(((long long)dense_D * 32 + 255) / 256, (long long)gb::sm_count() * 8);
             gb::note_launch();
@@ -1461,29 +1555,44 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             gb::note_launch();
             k_reduce<double2, VT, R, true><<<(unsigned)P.nr, kRWarps * 32, 0, sm>>>(
                 D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, nullptr, nullptr, Tx, xin, yout, mode, aux, bb,
-                dots);
+                dots, fz);
             GB_CUDA_TRY(cudaGetLastError());
             return GB_OK;
         }
-        return launch_apply<VT, R>(P, D, w, base, st, mask, pol, mat, nullptr, tvec, xin, yout, mode, aux, bb, dots, sm);
+        return launch_apply<VT, R>(P, D, w, base, st, mask, pol, mat, nullptr, tvec, xin, yout, mode, aux, bb, dots, sm,
+                                   fz, up);
     };
+    // One iteration: p-update + v = A p (+ alpha), s-update + t = A s (+ omega),
+    // x/r update (+ convergence, beta).  On the packed path the vector updates run
+    // inside the y-vector preparation of the product that reads them, and each
+    // scalar update inside the kernel that produces its dots (last CTA per cluster):
+    // 7 launches per iteration.  The dense path keeps the p- and s-update kernels.
     auto iteration = [&](cudaStream_t sm) -> int {
+        int e;
+        if (DENSE) {
+            gb::note_launch();
+            k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 1, nullptr, nullptr, x, r, r0, p, v, s, t,
+                                                dots);
+            e = apply(p, v, 1, r0, 0, nullptr, sm, fuse(1));
+            if (e) return e;
+            gb::note_launch();
+            k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 2, nullptr, nullptr, x, r, r0, p, v, s, t,
+                                                dots);
+            e = apply(s, t, 2, s, 0, nullptr, sm, fuse(2));
+            if (e) return e;
+        } else {
+            YUpd<VT> up1;
+            up1.kind = 1; up1.r = r; up1.v = v; up1.out = p;
+            e = apply(p, v, 1, r0, 0, nullptr, sm, fuse(1), up1);
+            if (e) return e;
+            YUpd<VT> up2;
+            up2.kind = 2; up2.r = r; up2.v = v; up2.out = s;
+            e = apply(s, t, 2, s, 0, nullptr, sm, fuse(2), up2);
+            if (e) return e;
+        }
         gb::note_launch();
-        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 1, nullptr, nullptr, x, r, r0, p, v, s, t, dots);
-        int e = apply(p, v, 1, r0, 0, nullptr, sm);
-        if (e) return e;
-        gb::note_launch();
-        k_scalar<R><<<sblocks, 128, 0, sm>>>(D.sp, P.nsys, st, 1, dots, tol, maxiter);
-        gb::note_launch();
-        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 2, nullptr, nullptr, x, r, r0, p, v, s, t, dots);
-        e = apply(s, t, 2, s, 0, nullptr, sm);
-        if (e) return e;
-        gb::note_launch();
-        k_scalar<R><<<sblocks, 128, 0, sm>>>(D.sp, P.nsys, st, 2, dots, tol, maxiter);
-        gb::note_launch();
-        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 3, nullptr, nullptr, x, r, r0, p, v, s, t, dots);
-        gb::note_launch();
-        k_scalar<R><<<sblocks, 128, 0, sm>>>(D.sp, P.nsys, st, 3, dots, tol, maxiter);
+        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 3, nullptr, nullptr, x, r, r0, p, v, s, t, dots,
+                                            D.sp, fuse(3));
         GB_CUDA_TRY(cudaGetLastError());
         return GB_OK;
     };
@@ -1491,10 +1600,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     // init: x = 0, r = r0 = b, scalars
     gb::note_launch();
     k_vec<VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, 0, b128, bvt ? bvt : bx, x, r, r0, p, v, s, t,
-                                            dots);
-    GB_CUDA_TRY(cudaGetLastError());
-    gb::note_launch();
-    k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 0, dots, tol, maxiter);
+                                            dots, D.sp, fuse(0));
     GB_CUDA_TRY(cudaGetLastError());
     const VT* bsrc_vt = bvt ? bvt : bx;
 
@@ -1763,6 +1869,8 @@ int upload_plan_pageable(const Plan& P, unsigned char* base, const WS& w, cudaSt
     size_t o_rs = put(P.row_strip.data(), sizeof(long long) * P.row_strip.size());
     const int zeros[4] = {0, 0, 0, 0};
     size_t o_err = put(zeros, sizeof(zeros));
+    const std::vector<int> counters(P.nsys, 0);
+    size_t o_cnt = put(counters.data(), sizeof(int) * P.nsys);
     unsigned char* dst = base + w.off_blob;
     // from pageable memory: returns once the blob has been taken, so it may go out of scope
     GB_CUDA_TRY(cudaMemcpyAsync(dst, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream));
@@ -1773,6 +1881,7 @@ int upload_plan_pageable(const Plan& P, unsigned char* base, const WS& w, cudaSt
     D.sp = reinterpret_cast<const SysPlan*>(dst + o_sp);
     D.row_strip = reinterpret_cast<const long long*>(dst + o_rs);
     D.err = reinterpret_cast<int*>(dst + o_err);
+    D.cnt = reinterpret_cast<int*>(dst + o_cnt);
     return GB_OK;
 }
 
