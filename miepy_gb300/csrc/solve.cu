@@ -56,7 +56,7 @@ namespace {
 
 constexpr int kVRows = 128;        // rows per vector work item (= threads per CTA)
 constexpr int kRRows = 32;         // rows per reduce work item
-constexpr int kRWarps = 8;         // warps per reduce CTA
+constexpr int kRWarps = 16;        // warps per reduce CTA
 constexpr int kGemvThreads = 128;  // 4 warps
 constexpr int kGemvWarps = kGemvThreads / 32;
 constexpr int kChunk = 4;          // iterations per host check
@@ -530,7 +530,10 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             }
             if (failed) break;
             // block done: column partial of block row j
-            OutT* cwp = CW + pl.cw_off + (sp.p0 + b) * (long long)B * RT;
+            // column partials by destination: block row j's partials from i < j are
+            // contiguous (index j(j-1)/2 + i), so the reduction streams them
+            const long long jb = j0 + b;
+            OutT* cwp = CW + pl.cw_off + (jb * (jb - 1) / 2 + sp.i) * (long long)B * RT;
 #pragma unroll
             for (int k = 0; k < CPL; k++)
 #pragma unroll
@@ -605,29 +608,8 @@ __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isf
 // <r0,r>: convergence, restart test, beta); 4 restart done (reduce dots |r|^2).
 // One warp per (cluster, rhs): lanes stride over the item partials, a fixed
 // butterfly combines them (deterministic), lane 0 updates the scalars.
-template <int R>
-__device__ void scalar_step(const SysPlan* __restrict__ plan, KState* __restrict__ st, int phase,
-                            const double2* __restrict__ dots, double tol, int maxiter, int sidx, int rr, int lane) {
-    KState& k = st[sidx * R + rr];
-    if (phase != 0 && phase != 4 && (k.done || k.need_restart)) return;
-    if (phase == 4 && !k.need_restart) return;
-    const SysPlan pl = plan[sidx];
-    const bool vec = (phase == 0 || phase == 3);
-    const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
-    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
-    for (int it = b0 + lane; it < b1; it += 32) {
-        const double2 a = __ldcg(dots + ((long long)it * R + rr) * 2 + 0);   // L2: other CTAs wrote them
-        const double2 c = __ldcg(dots + ((long long)it * R + rr) * 2 + 1);
-        d0.x += a.x; d0.y += a.y;
-        d1.x += c.x; d1.y += c.y;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
-        d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
-        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
-        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
-    }
-    if (lane != 0) return;
+// Scalar update of one (cluster, rhs) from its summed dots d0, d1 (one thread).
+__device__ void scalar_apply(KState& k, int phase, double2 d0, double2 d1, double tol, int maxiter) {
     const double eps = 2.220446049250313e-16;
     if (phase == 0) {
         k.bsq = k.r0sq = k.rsq = d0.x;
@@ -690,6 +672,37 @@ __device__ void scalar_step(const SysPlan* __restrict__ plan, KState* __restrict
     }
 }
 
+
+__device__ __forceinline__ bool scalar_skips(const KState& k, int phase) {
+    return (phase != 0 && phase != 4 && (k.done || k.need_restart)) || (phase == 4 && !k.need_restart);
+}
+
+// One warp per (cluster, rhs): lanes stride over the item partials, a fixed
+// butterfly combines them (deterministic), lane 0 updates the scalars.
+template <int R>
+__device__ void scalar_step(const SysPlan* __restrict__ plan, KState* __restrict__ st, int phase,
+                            const double2* __restrict__ dots, double tol, int maxiter, int sidx, int rr, int lane) {
+    KState& k = st[sidx * R + rr];
+    if (scalar_skips(k, phase)) return;
+    const SysPlan pl = plan[sidx];
+    const bool vec = (phase == 0 || phase == 3);
+    const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
+    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+    for (int it = b0 + lane; it < b1; it += 32) {
+        const double2 a = __ldcg(dots + ((long long)it * R + rr) * 2 + 0);
+        const double2 c = __ldcg(dots + ((long long)it * R + rr) * 2 + 1);
+        d0.x += a.x; d0.y += a.y;
+        d1.x += c.x; d1.y += c.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
+        d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
+        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
+        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
+    }
+    if (lane == 0) scalar_apply(k, phase, d0, d1, tol, maxiter);
+}
+
 template <int R>
 __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ st, int phase,
                          const double2* __restrict__ dots, double tol, int maxiter) {
@@ -712,24 +725,63 @@ struct ScalarFuse {
     int maxiter = 0;
 };
 
-// Called by warp 0 of a CTA of cluster sys after its partial dots are written.
-template <int R>
-__device__ void fused_scalar(const ScalarFuse& fz, const SysPlan* __restrict__ plan, const double2* __restrict__ dots,
-                             int sys, int nitems_sys, int lane) {
-    int last = 0;
-    if (lane == 0) {
+// Called by every thread of a CTA of cluster sys once its partial dots are
+// written and fenced.  The last CTA of the cluster sums the cluster's partials
+// with all its NT threads (strided per thread, then warp butterflies, then the
+// warps in order: a fixed order, deterministic) and updates the scalars.
+template <int R, int NT>
+__device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict__ plan,
+                                 const double2* __restrict__ dots, int sys, int nitems_sys) {
+    __shared__ int s_last;
+    __shared__ double2 s_red[NT / 32][R][2];
+    __syncthreads();
+    if (threadIdx.x == 0) {
         __threadfence();
         const int old = atomicAdd(fz.cnt + sys, 1);
-        last = (old == nitems_sys - 1);
-        if (last) {
+        s_last = (old == nitems_sys - 1);
+        if (s_last) {
             fz.cnt[sys] = 0;
             __threadfence();
         }
     }
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
+    __syncthreads();
+    if (!s_last) return;
+    const SysPlan pl = plan[sys];
+    const bool vec = (fz.phase == 0 || fz.phase == 3);
+    const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) scalar_step<R>(plan, fz.st, fz.phase, dots, fz.tol, fz.maxiter, sys, rr, lane);
+    for (int rr = 0; rr < R; rr++) {
+        double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+        for (int it = b0 + (int)threadIdx.x; it < b1; it += NT) {
+            const double2 a = __ldcg(dots + ((long long)it * R + rr) * 2 + 0);   // written by other CTAs
+            const double2 c = __ldcg(dots + ((long long)it * R + rr) * 2 + 1);
+            d0.x += a.x; d0.y += a.y;
+            d1.x += c.x; d1.y += c.y;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
+            d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
+            d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
+            d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
+        }
+        if (lane == 0) {
+            s_red[wid][rr][0] = d0;
+            s_red[wid][rr][1] = d1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < R) {
+        const int rr = threadIdx.x;
+        KState& k = fz.st[sys * R + rr];
+        if (scalar_skips(k, fz.phase)) return;
+        double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+        for (int w = 0; w < NT / 32; w++) {
+            d0.x += s_red[w][rr][0].x; d0.y += s_red[w][rr][0].y;
+            d1.x += s_red[w][rr][1].x; d1.y += s_red[w][rr][1].y;
+        }
+        scalar_apply(k, fz.phase, d0, d1, fz.tol, fz.maxiter);
+    }
 }
 
 // --------------------------------------------------------------- K3b reduce --
@@ -754,6 +806,107 @@ template <> struct RAcc<float4> {
 // y = x + T x (from the partials, or from a dense Tx), and per-item partial dots:
 //   mode 1: d0 = <r0, y>;  mode 2: d0 = |y|^2, d1 = <y, s>;
 //   mode 3: y := b - (x + T x), d0 = |y|^2  (residual).
+constexpr int kRBThreads = 384;   // threads of the block reduce (>= B*R for lmax <= 8, R <= 2)
+
+// K3b (packed path): one CTA per particle block k of a cluster.  Its rows' products
+// are the sum of the strip partials of block row k (contiguous in CU) and the
+// column partials of the blocks (i, k), i < k (contiguous in CW by destination).
+// The CTA's threads form G = kRBThreads / (B R) groups that split the terms; thread
+// (g, v) streams element v (= column * R + rhs) of its terms, so every term is one
+// coalesced B*R-element read.  The groups are combined in order (deterministic),
+// then thread (row, rhs) applies the sign/permutation of its row, adds the identity
+// term, stores y and contributes to the CTA's partial dot products (modes as k_reduce).
+template <typename OutT, typename VT, int R>
+__global__ void __launch_bounds__(kRBThreads)
+k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
+             const SysPlan* __restrict__ plan, const long long* __restrict__ row_strip, const KState* __restrict__ st,
+             int mask_mode, const OutT* __restrict__ CU, const OutT* __restrict__ CW, const VT* __restrict__ x,
+             VT* __restrict__ y, int mode, const VT* __restrict__ aux, const double2* __restrict__ b128,
+             double2* __restrict__ dots, ScalarFuse fz) {
+    const int it = blockIdx.x;
+    if (it >= nitems) return;
+    const Item I = items[it];
+    if (!any_active<R>(st, I.sys, mask_mode)) return;
+    const gb::SysDev S = sys[I.sys];
+    const SysPlan pl = plan[I.sys];
+    const int B = S.B, BR = B * R;
+    const int G = kRBThreads / BR;
+    const int tid = threadIdx.x, g = tid / BR, v = tid - g * BR;
+    const int k = I.r0 / B;   // particle (block row) of this item
+    __shared__ double2 partU[kRBThreads], partW[kRBThreads];
+    __shared__ double2 red[kRBThreads][2];
+    if (g < G) {
+        const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
+        const long long ns = s1 - s0;
+        const OutT* cu = CU + pl.cu_off + (s0 - pl.strip_base) * (long long)BR + v;
+        const OutT* cw = CW + pl.cw_off + ((long long)k * (k - 1) / 2) * BR + v;
+        RAcc<OutT> au, aw;
+        au.zero();
+        aw.zero();
+#pragma unroll 4
+        for (long long t = g; t < ns; t += G) au.add(cu[t * BR]);
+#pragma unroll 4
+        for (long long t = g; t < k; t += G) aw.add(cw[t * BR]);
+        partU[tid] = au.get();
+        partW[tid] = aw.get();
+    }
+    __syncthreads();
+    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+    int rr = 0;
+    if (tid < BR) {
+        const int r = tid / R;
+        rr = tid - r * R;
+        const int info = __ldg(S.rowinfo + r);
+        const int rho = info & ((1 << 29) - 1);
+        const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
+        double2 a = make_double2(0, 0), c = make_double2(0, 0);
+        for (int q = 0; q < G; q++) {
+            const double2 u = partU[q * BR + rho * R + rr], w = partW[q * BR + rho * R + rr];
+            a.x += u.x; a.y += u.y;
+            c.x += w.x; c.y += w.y;
+        }
+        a = make_double2(flipd(a.x, eneg), flipd(a.y, eneg));
+        c = make_double2(flipd(c.x, eneg ^ sneg), flipd(c.y, eneg ^ sneg));
+        const double2 tx = make_double2(a.x + c.x, a.y + c.y);
+        if (active_rhs<R>(st, I.sys, rr, mask_mode)) {
+            const long long e = S.vec_off + (long long)(I.r0 + r) * R + rr;
+            const double2 xv = to_d2(x[e]);
+            double2 yv = make_double2(xv.x + tx.x, xv.y + tx.y);
+            if (mode == 3) {
+                const double2 bv = b128 ? b128[e] : to_d2(aux[e]);
+                yv = make_double2(bv.x - yv.x, bv.y - yv.y);
+            }
+            const VT yo = from_d2<VT>(yv);
+            y[e] = yo;
+            const double2 yq = to_d2(yo);   // dots of the stored (rounded) vector
+            if (mode == 1) {
+                cfma_conj(d0, to_d2(aux[e]), yq);
+            } else if (mode == 2) {
+                d0.x += yq.x * yq.x + yq.y * yq.y;
+                cfma_conj(d1, yq, to_d2(aux[e]));
+            } else if (mode == 3) {
+                d0.x += yq.x * yq.x + yq.y * yq.y;
+            }
+        }
+    }
+    if (mode == 0) return;
+    red[tid][0] = d0;
+    red[tid][1] = d1;
+    __syncthreads();
+    if (tid < R) {   // per rhs, rows in order
+        double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
+        for (int q = tid; q < BR; q += R) {
+            s0.x += red[q][0].x; s0.y += red[q][0].y;
+            s1.x += red[q][1].x; s1.y += red[q][1].y;
+        }
+        dots[((long long)it * R + tid) * 2 + 0] = s0;
+        dots[((long long)it * R + tid) * 2 + 1] = s1;
+        __threadfence();
+    }
+    (void)rr;
+    if (fz.st) fused_scalar_cta<R, kRBThreads>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
+}
+
 template <typename OutT, typename VT, int R, bool DENSE>
 __global__ void __launch_bounds__(kRWarps * 32)
 k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
@@ -813,11 +966,10 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
         }
         __syncthreads();
     }
-    if (wid != 0) return;
     double2 d0[R], d1[R];
 #pragma unroll
     for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = make_double2(0, 0);
-    if (valid) {
+    if (valid && wid == 0) {
         double2 tx[R];
         if (DENSE) {
 #pragma unroll
@@ -863,22 +1015,25 @@ k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int
         }
     }
     if (mode == 0) return;
+    if (wid == 0) {
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) {
-        for (int o = 16; o > 0; o >>= 1) {
-            d0[rr].x += __shfl_xor_sync(0xffffffffu, d0[rr].x, o);
-            d0[rr].y += __shfl_xor_sync(0xffffffffu, d0[rr].y, o);
-            d1[rr].x += __shfl_xor_sync(0xffffffffu, d1[rr].x, o);
-            d1[rr].y += __shfl_xor_sync(0xffffffffu, d1[rr].y, o);
-        }
-        if (lane == 0) {
-            dots[((long long)it * R + rr) * 2 + 0] = d0[rr];
-            dots[((long long)it * R + rr) * 2 + 1] = d1[rr];
+        for (int rr = 0; rr < R; rr++) {
+            for (int o = 16; o > 0; o >>= 1) {
+                d0[rr].x += __shfl_xor_sync(0xffffffffu, d0[rr].x, o);
+                d0[rr].y += __shfl_xor_sync(0xffffffffu, d0[rr].y, o);
+                d1[rr].x += __shfl_xor_sync(0xffffffffu, d1[rr].x, o);
+                d1[rr].y += __shfl_xor_sync(0xffffffffu, d1[rr].y, o);
+            }
+            if (lane == 0) {
+                dots[((long long)it * R + rr) * 2 + 0] = d0[rr];
+                dots[((long long)it * R + rr) * 2 + 1] = d1[rr];
+                __threadfence();
+            }
         }
     }
     if (fz.st) {
         const SysPlan pl = plan[I.sys];
-        fused_scalar<R>(fz, plan, dots, I.sys, pl.rend - pl.rbeg, lane);
+        fused_scalar_cta<R, kRWarps * 32>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
     }
 }
 
@@ -969,11 +1124,10 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
         }
         dots[((long long)it * R + rr) * 2 + which] = sm;
     }
-    if (fz.st && lr < 32) {
-        if (lr < R * 2) __threadfence();   // this lane's partial before the arrival count
-        __syncwarp();
+    if (fz.st) {
+        if (lr < R * 2) __threadfence();   // this thread's partial before the arrival count
         const SysPlan pl = plan[I.sys];
-        fused_scalar<R>(fz, plan, dots, I.sys, pl.vend - pl.vbeg, lr);
+        fused_scalar_cta<R, kVRows>(fz, plan, dots, I.sys, pl.vend - pl.vbeg);
     }
 }
 
@@ -1180,7 +1334,7 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
         cw_off += d.P * d.B * R;
         cu_off += ((long long)P.strips.size() - pl.strip_base) * d.B * R;
         add_items(P.vitems, s, d.D, kVRows, pl.vbeg, pl.vend);
-        add_items(P.ritems, s, d.D, kRRows, pl.rbeg, pl.rend);
+        add_items(P.ritems, s, d.D, d.B, pl.rbeg, pl.rend);   // one item per particle block
         P.total_vec = std::max<long long>(P.total_vec, d.vec_off + (long long)d.D * R);
         P.max_B = std::max<long long>(P.max_B, d.B);
     }
@@ -1418,9 +1572,9 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
-        k_reduce<double2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+        k_reduce_blk<double2, VT, R><<<(unsigned)P.nr, kRBThreads, 0, stream>>>(
             D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
-            reinterpret_cast<const double2*>(CW), nullptr, xin, yout, mode, aux, b128, dots, fz);
+            reinterpret_cast<const double2*>(CW), xin, yout, mode, aux, b128, dots, fz);
     } else if (pol == 1) {
         gb::note_launch();
         k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
@@ -1428,9 +1582,9 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
-        k_reduce<float2, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+        k_reduce_blk<float2, VT, R><<<(unsigned)P.nr, kRBThreads, 0, stream>>>(
             D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
-            reinterpret_cast<const float2*>(CW), nullptr, xin, yout, mode, aux, b128, dots, fz);
+            reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz);
     } else {
         gb::note_launch();
         k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
@@ -1438,9 +1592,9 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         if (P.nstrips) e = launch_df<R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
-        k_reduce<float4, VT, R, false><<<(unsigned)P.nr, kRWarps * 32, 0, stream>>>(
+        k_reduce_blk<float4, VT, R><<<(unsigned)P.nr, kRBThreads, 0, stream>>>(
             D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float4*>(CU),
-            reinterpret_cast<const float4*>(CW), nullptr, xin, yout, mode, aux, b128, dots, fz);
+            reinterpret_cast<const float4*>(CW), xin, yout, mode, aux, b128, dots, fz);
     }
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
