@@ -228,6 +228,25 @@ int gb_near_field32(int N, int lmax, const double* pos, const double* radius, co
 int gb_beam_project(int N, int ncol, int G, const double* pos, const double* rhat, const double* w, double k,
                     double* out, int out_stride, void* stream);
 
+/* ------------------------------------------- cluster coefficients / far field --
+ * Cluster expansion about one origin: replaces cluster_coefficients,
+ * vsh/cluster_coefficients.py:14-53, with the incident-mode vsh_translation of
+ * cpp/src/vsh_translation.cpp:428-470.  pos [N,3] f64, p_scat [N,2,rmax(lmax)] c128
+ * (device); origin [3] f64 (host); p_cluster [2,rmax(lmax_cluster)] c128 (device).
+ * Scratch: gb_cluster_coefficients_workspace_size(N, lmax_cluster) bytes. */
+size_t gb_cluster_coefficients_workspace_size(int N, int lmax_cluster);
+int gb_cluster_coefficients(int N, int lmax, const double* pos, const double* p_scat, double k, const double* origin,
+                            int lmax_cluster, double* p_cluster, void* workspace, size_t ws_bytes, void* stream);
+
+/* Far-field E (or H) of the cluster in spherical components at points (R, theta,
+ * phi) about the origin: replaces E_angular / H_angular, sphere_cluster.py:393-426,
+ * through expand_E_far / expand_H_far, vsh/expansion.py:45-108.  radius, theta, phi
+ * [Npts] f64 (device); out [Npts][2] c128 (E_theta, E_phi); magnetic: swapped
+ * coefficients times hfac.  Scattered field only (no source). */
+int gb_far_field(int N, int lmax, const double* pos, const double* p_scat, double k, const double* origin, int Npts,
+                 const double* radius, const double* theta, const double* phi, int magnetic, double hfac_re,
+                 double hfac_im, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,10 @@ SIGNATURES = {
     "gb_solve_dense_workspace_size": (c_size_t, [c_int, c_int]),
     "gb_solve_dense": (c_int, [c_int, c_int, _P, _P, _P, c_double, c_int, _P, c_size_t, _P, _P, _P, _P]),
     "gb_beam_project": (c_int, [c_int, c_int, c_int, _P, _P, _P, c_double, _P, c_int, _P]),
+    "gb_cluster_coefficients_workspace_size": (c_size_t, [c_int, c_int]),
+    "gb_cluster_coefficients": (c_int, [c_int, c_int, _P, _P, c_double, _P, c_int, _P, _P, c_size_t, _P]),
+    "gb_far_field": (c_int, [c_int, c_int, _P, _P, c_double, _P, c_int, _P, _P, _P, c_int, c_double, c_double, _P,
+                             _P]),
     "gb_solve_dense_noalloc": (c_int, [c_int, c_int, _P, _P, _P, c_double, c_int, _P, _P, _P, _P]),
     "gb_apply_workspace_size": (c_size_t, [c_int, _P, c_int, c_int]),
     "gb_apply_batch": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_size_t, _P]),

@@ -191,6 +191,74 @@ class sphere_cluster:
             Ce += C.extinction
         return cross_sections(Cs, Ca, Ce)
 
+    # ------------------------------------------------- cluster coefficients --
+    def solve_cluster_coefficients(self, lmax=None):
+        """p_cluster [2, rmax(lmax)]: the particles' scattered fields re-expanded about
+        the origin (sphere_cluster.py:650-661, vsh/cluster_coefficients.py:14-53), on the GPU."""
+        lmax = self.lmax if lmax is None else int(lmax)
+        dev = self._batch.device
+        d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+        N = self.Nparticles
+        L = nat.lib()
+        ws = torch.empty(L.gb_cluster_coefficients_workspace_size(N, lmax), dtype=torch.uint8, device=dev)
+        out = torch.empty(2 * lmax_to_rmax(lmax), dtype=torch.complex128, device=dev)
+        pos = d(self.position, torch.float64)
+        ps = d(self.p_scat, torch.complex128)
+        origin = np.ascontiguousarray(np.asarray(self.origin, dtype=float))
+        nat.check(L.gb_cluster_coefficients(N, self.lmax, nat.ptr(pos), nat.ptr(ps),
+                                            float(np.real(self.material_data.k_b)), origin.ctypes.data, lmax,
+                                            nat.ptr(out), nat.ptr(ws), ws.numel(), current_stream(dev)),
+                  "cluster coefficients")
+        self.p_cluster = out.cpu().numpy().reshape(2, lmax_to_rmax(lmax))
+        return self.p_cluster
+
+    def cross_sections_per_multipole(self, lmax=None):
+        """Cluster cross-sections per multipole about the origin (sphere_cluster.py:428-440,
+        flux.cluster_cross_sections flux.py:35-56): each [2, lmax]."""
+        lmax = self.lmax if lmax is None else int(lmax)
+        pc = self.solve_cluster_coefficients(lmax)
+        k = float(np.real(self.material_data.k_b))
+        p0 = self.source.structure(np.array([self.origin], dtype=float), k, lmax)[0]
+        f = 4 * np.pi / k ** 2
+        Cs = np.zeros((2, lmax))
+        Ce = np.zeros((2, lmax))
+        for r in range(lmax_to_rmax(lmax)):
+            n = int(np.floor(np.sqrt(r + 1)))
+            Cs[:, n - 1] += f * np.abs(pc[:, r]) ** 2
+            Ce[:, n - 1] += f * np.real(np.conj(p0[:, r]) * pc[:, r])
+        return cross_sections(Cs, Ce - Cs, Ce)
+
+    def _angular(self, theta, phi, radius, source, magnetic):
+        if source:
+            raise NotImplementedError("source far fields (reflected sources) need substrate interfaces")
+        md = self.material_data
+        k = float(np.real(md.k_b))
+        if radius is None:
+            radius = 1e6 * 2 * np.pi / k
+        th, ph, R = np.broadcast_arrays(np.asarray(theta, float), np.asarray(phi, float), np.asarray(radius, float))
+        shape = th.shape
+        dev = self._batch.device
+        d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a).reshape(-1)).to(dev, dtype=dt)
+        pos = d(self.position, torch.float64)
+        ps = d(self.p_scat, torch.complex128)
+        Rt, Tt, Pt = d(R, torch.float64), d(th, torch.float64), d(ph, torch.float64)
+        out = torch.empty((th.size, 2), dtype=torch.complex128, device=dev)
+        hfac = -1j * np.sqrt(md.eps_b / md.mu_b) if magnetic else 1.0
+        origin = np.ascontiguousarray(np.asarray(self.origin, dtype=float))
+        nat.check(nat.lib().gb_far_field(self.Nparticles, self.lmax, nat.ptr(pos), nat.ptr(ps), k,
+                                         origin.ctypes.data, th.size, nat.ptr(Rt), nat.ptr(Tt), nat.ptr(Pt),
+                                         int(bool(magnetic)), float(np.real(hfac)), float(np.imag(hfac)),
+                                         nat.ptr(out), current_stream(dev)), "far field")
+        return out.cpu().numpy().T.reshape((2,) + shape)
+
+    def E_angular(self, theta, phi, radius=None, source=False):
+        """Far-field E (theta, phi components) of the particles (sphere_cluster.py:393-411)."""
+        return self._angular(theta, phi, radius, source, magnetic=False)
+
+    def H_angular(self, theta, phi, radius=None, source=False):
+        """Far-field H (theta, phi components) of the particles (sphere_cluster.py:413-426)."""
+        return self._angular(theta, phi, radius, source, magnetic=True)
+
     def _nosource(self):
         if self._F_nosrc is None:
             b = self._batch

@@ -25,6 +25,18 @@ struct Tables {
 };
 
 int get_tables(int lmax, cudaStream_t stream, const Tables** out);
+
+// Translation tables between orders Lc (outgoing about an origin) and Lin (about a
+// particle): every (n <= Lc, m, v <= Lin, u), tuple t = r(n, m) * rmax(Lin) + r(v, u).
+struct CrossTables {
+    int Lc = 0, Lin = 0, M = 0, Q = 0, PM = 0;
+    int4* nmvu = nullptr;
+    int2* qab = nullptr;
+    double* cA = nullptr;        // [M][Q]
+    double* cB = nullptr;        // [M][Q]
+    double* neg_ratio = nullptr; // [PM][PM]
+};
+int get_cross_tables(int Lc, int Lin, cudaStream_t stream, const CrossTables** out);
 int host_tuples(int L, std::vector<int4>& nmvu);
 
 int sm_count();

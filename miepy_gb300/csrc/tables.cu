@@ -24,7 +24,10 @@
 // the reference's placement rules (cpp/src/vsh_translation.cpp:211-232) for the
 // (i, j) block.
 
+#include <array>
+#include <map>
 #include <mutex>
+#include <algorithm>
 #include <vector>
 #include <cmath>
 #include <cstdio>
@@ -262,6 +265,68 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
         return gb_set_cuda_error(e, "building translation tables", __FILE__, __LINE__);
     }
     per[lmax] = T;
+    *out = T;
+    return GB_OK;
+}
+
+// Cross tables for translations between expansions of different orders (cluster
+// coefficients: outgoing order n <= Lc about the origin, incoming v <= Lin about a
+// particle), every (n, m, v, u) in mode order, t = r(n, m) * rmax(Lin) + r(v, u),
+// with the argument convention of vsh_translation (cpp/src/vsh_translation.cpp:
+// 428-470: the cache is evaluated at (n, -m, v, u)).  Same folded coefficients as
+// the pair tables; coefficient stride Q = max(Lc, Lin) + 1; the negative-order
+// Legendre ratio for orders p < Lc + Lin + 2.
+int get_cross_tables(int Lc, int Lin, cudaStream_t stream, const CrossTables** out) {
+    if (Lc < 1 || Lc > GB_LMAX_MAX || Lin < 1 || Lin > GB_LMAX_MAX)
+        return gb_set_error(GB_BAD_ARG, "cross table orders %d, %d outside 1..%d", Lc, Lin, GB_LMAX_MAX);
+    static std::mutex mu;
+    static std::map<std::array<int, 3>, CrossTables*> cache;
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    const std::array<int, 3> key{dev, Lc, Lin};
+    auto f = cache.find(key);
+    if (f != cache.end()) {
+        *out = f->second;
+        return GB_OK;
+    }
+    const int rc = lmax_to_rmax(Lc), ri = lmax_to_rmax(Lin), M = rc * ri, L = std::max(Lc, Lin), Q = L + 1;
+    const int PM = Lc + Lin + 2;
+    std::vector<int4> nmvu;
+    nmvu.reserve(M);
+    for (int n = 1; n <= Lc; n++)
+        for (int m = -n; m <= n; m++)
+            for (int v = 1; v <= Lin; v++)
+                for (int u = -v; u <= v; u++) nmvu.push_back(make_int4(n, m, v, u));
+    std::vector<double> negr((size_t)PM * PM, 0.0);
+    for (int p = 0; p < PM; p++)
+        for (int mu2 = 0; mu2 <= p; mu2++)
+            negr[(size_t)p * PM + mu2] = ((mu2 & 1) ? -1.0 : 1.0) * std::tgamma(p - mu2 + 1.0) / std::tgamma(p + mu2 + 1.0);
+    CrossTables* T = new CrossTables();
+    T->Lc = Lc;
+    T->Lin = Lin;
+    T->M = M;
+    T->Q = Q;
+    T->PM = PM;
+    cudaError_t e = cudaMalloc(&T->nmvu, sizeof(int4) * M);
+    if (e == cudaSuccess) e = cudaMalloc(&T->qab, sizeof(int2) * M);
+    if (e == cudaSuccess) e = cudaMalloc(&T->cA, sizeof(double) * M * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&T->cB, sizeof(double) * M * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&T->neg_ratio, sizeof(double) * PM * PM);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T->nmvu, nmvu.data(), sizeof(int4) * M, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T->neg_ratio, negr.data(), sizeof(double) * PM * PM, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) {
+        gb::note_launch();
+        k_tuple_table<<<(M + 127) / 128, 128, 0, stream>>>(L, M, T->nmvu, T->qab, T->cA, T->cB);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // host vectors go out of scope
+    if (e != cudaSuccess) {
+        cudaFree(T->nmvu); cudaFree(T->qab); cudaFree(T->cA); cudaFree(T->cB); cudaFree(T->neg_ratio);
+        delete T;
+        return gb_set_cuda_error(e, "building cross translation tables", __FILE__, __LINE__);
+    }
+    cache[key] = T;
     *out = T;
     return GB_OK;
 }

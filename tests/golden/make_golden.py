@@ -39,6 +39,17 @@ def cluster_record(miepy, name, cluster, store_matrix=False, field_pts=None):
     rec["force"] = c.force()
     rec["torque"] = c.torque()
     rec["force_nosource"] = c.force(source=False)
+    # cluster coefficients about the origin and far fields (the f2 row)
+    rec["p_cluster"] = miepy.cluster_coefficients(c.position, c.p_scat, md.k_b, origin=c.origin, lmax=c.lmax)
+    rec["p_cluster_lmax_plus1"] = miepy.cluster_coefficients(c.position, c.p_scat, md.k_b, origin=c.origin,
+                                                            lmax=min(c.lmax + 1, 8))
+    Cm = c.cross_sections_per_multipole()
+    rec["cluster_xs_per_multipole"] = np.array([np.asarray(v) for v in Cm], dtype=float)
+    th_far = np.linspace(0.1, np.pi - 0.1, 5)
+    ph_far = np.linspace(0.0, 2 * np.pi, 5)
+    rec["far_theta"], rec["far_phi"] = th_far, ph_far
+    rec["E_angular"] = c.E_angular(th_far, ph_far)
+    rec["H_angular"] = c.H_angular(th_far, ph_far)
     if store_matrix:
         rec["agg_tmatrix"] = miepy.interactions.sphere_aggregate_tmatrix(c.position, c.mie_scat, md.k_b)
     if field_pts is not None:
