@@ -91,7 +91,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "20"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -211,16 +211,22 @@ def run_gpu(args, rank, world):
     x = torch.randn(batches["mixed"].totals["vec"], dtype=torch.complex128, device=dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    def time_apply(b, prec, reps=20, gemv_only=False):
-        """Per-launch duration of the operator (or of its matrix pass alone) from
-        events around reps back-to-back launches on the stream."""
-        b.apply_repeat(x, prec, reps=3, gemv_only=gemv_only)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        b.apply_repeat(x, prec, reps=reps + 1, gemv_only=gemv_only)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1e3 / (reps + 1)
+    def time_apply(b, prec, reps=32, gemv_only=False):
+        """Per-launch duration of the operator (or of its matrix pass alone): events
+        around calls of k and k + reps back-to-back launches on the stream; the
+        difference over reps leaves out each call's fixed cost (host plan build and
+        the first full product), so it is the launches' own duration; the median of
+        five such differences."""
+        def span(n):
+            torch.cuda.synchronize()
+            e0.record(stream)
+            b.apply_repeat(x, prec, reps=n, gemv_only=gemv_only)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / 1e3
+        span(3)
+        k = 4
+        return float(np.median([(span(k + reps) - span(k)) / reps for _ in range(5)]))
 
     t_apply64 = time_apply(batches["mixed"], "fp32")
     t_gemv64 = time_apply(batches["mixed"], "fp32", gemv_only=True)

@@ -56,7 +56,6 @@ namespace {
 
 constexpr int kVRows = 128;        // rows per vector work item (= threads per CTA)
 constexpr int kRRows = 32;         // rows per reduce work item
-constexpr int kRWarps = 16;        // warps per reduce CTA
 constexpr int kGemvThreads = 128;  // 4 warps
 constexpr int kGemvWarps = kGemvThreads / 32;
 constexpr int kChunk = 4;          // iterations per host check
@@ -70,6 +69,47 @@ template <> __device__ __forceinline__ double2 from_d2<double2>(double2 v) { ret
 template <> __device__ __forceinline__ float2 from_d2<float2>(double2 v) {
     return make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
 }
+
+// Arithmetic of the vector kernels, their dot products and the BiCGSTAB scalar
+// step: FP32 for the FP32 solver (float2 vectors), FP64 otherwise.  GB300 issues an
+// FP64 warp instruction about once per 64 cycles per SM sub-partition, so the FP32
+// solver's small latency-bound kernels (reduce, vector update, scalar step) keep
+// off the FP64 pipe entirely.
+template <typename VT> struct Arith { using T = double; using C = double2; };
+template <> struct Arith<float2> { using T = float; using C = float2; };
+template <typename T> struct CplxT { using t = double2; };   // complex type of real type T
+template <> struct CplxT<float> { using t = float2; };
+
+template <typename C> __device__ __forceinline__ C to_c(float2 v);
+template <typename C> __device__ __forceinline__ C to_c(double2 v);
+template <> __device__ __forceinline__ float2 to_c<float2>(float2 v) { return v; }
+template <> __device__ __forceinline__ float2 to_c<float2>(double2 v) { return from_d2<float2>(v); }
+template <> __device__ __forceinline__ double2 to_c<double2>(double2 v) { return v; }
+template <typename VT> __device__ __forceinline__ VT from_c(float2 v);
+template <typename VT> __device__ __forceinline__ VT from_c(double2 v);
+template <> __device__ __forceinline__ float2 from_c<float2>(float2 v) { return v; }
+template <> __device__ __forceinline__ double2 from_c<double2>(double2 v) { return v; }
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return cmulf(a, b); }
+__device__ __forceinline__ void cfma_conj(float2& acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(-a.y, b.x, acc.y);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cflip(double2 a, unsigned neg) { return make_double2(flipd(a.x, neg), flipd(a.y, neg)); }
+__device__ __forceinline__ float2 cflip(float2 a, unsigned neg) { return make_float2(flipf(a.x, neg), flipf(a.y, neg)); }
+__device__ __forceinline__ double2 shfl_xor(double2 a, int o) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+__device__ __forceinline__ float2 shfl_xor(float2 a, int o) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+template <typename C> __device__ __forceinline__ C czero() { C z; z.x = 0; z.y = 0; return z; }
 
 // ----------------------------------------------------------- plan structs --
 struct Strip {          // GEMV work: blocks (i, j0 .. j0+nb-1) of cluster sys
@@ -89,11 +129,35 @@ struct SysPlan {
 };
 
 struct KState {         // per (cluster, rhs) BiCGSTAB scalars
-    double2 rho, alpha, omega, beta;
-    double r0sq, bsq, rsq, tol2;
+    double2 rho, alpha, omega, beta;   // FP64 solver
+    double r0sq, bsq, rsq, tol2;       // (bsq, rsq also mirrored from the FP32 solver, for the host)
+    float2 rho_f, alpha_f, omega_f, beta_f;   // FP32 solver
+    float r0sq_f, bsq_f, rsq_f, tol2_f;
     int iters, restarts, done, status;
     int need_restart, maxiter, pad0, pad1;
 };
+
+// The scalars of a KState in the solver's arithmetic T (read-only views for the
+// vector kernels' alpha, omega, beta).
+#define GB_KS_FIELD(name)                                                                            \
+    __device__ __forceinline__ auto& ks_##name(KState& k, double) { return k.name; }                  \
+    __device__ __forceinline__ auto& ks_##name(KState& k, float) { return k.name##_f; }
+#define GB_KS_CFIELD(name)                                                                           \
+    __device__ __forceinline__ const auto& ks_##name(const KState& k, double) { return k.name; }      \
+    __device__ __forceinline__ const auto& ks_##name(const KState& k, float) { return k.name##_f; }
+GB_KS_FIELD(rho)
+GB_KS_FIELD(alpha)
+GB_KS_FIELD(omega)
+GB_KS_FIELD(beta)
+GB_KS_FIELD(r0sq)
+GB_KS_FIELD(bsq)
+GB_KS_FIELD(rsq)
+GB_KS_FIELD(tol2)
+GB_KS_CFIELD(alpha)
+GB_KS_CFIELD(omega)
+GB_KS_CFIELD(beta)
+#undef GB_KS_FIELD
+#undef GB_KS_CFIELD
 
 enum { ST_RUNNING = -1 };
 
@@ -256,11 +320,12 @@ template <> struct YType<1> { using t = float4; };   // (re, re, im, im): broadc
 template <> struct YType<2> { using t = float4; };
 
 template <int YK> __device__ __forceinline__ typename YType<YK>::t make_y(double2 z);
+template <int YK> __device__ __forceinline__ typename YType<YK>::t make_y(float2 z);
 template <> __device__ __forceinline__ double2 make_y<0>(double2 z) { return z; }
-template <> __device__ __forceinline__ float4 make_y<1>(double2 z) {
-    const float re = __double2float_rn(z.x), im = __double2float_rn(z.y);
-    return make_float4(re, re, im, im);
-}
+template <> __device__ __forceinline__ double2 make_y<0>(float2 z) { return to_d2(z); }
+template <> __device__ __forceinline__ float4 make_y<1>(float2 z) { return make_float4(z.x, z.x, z.y, z.y); }
+template <> __device__ __forceinline__ float4 make_y<1>(double2 z) { return make_y<1>(from_d2<float2>(z)); }
+template <> __device__ __forceinline__ float4 make_y<2>(float2 z) { return make_float4(z.x, z.y, 0.f, 0.f); }
 template <> __device__ __forceinline__ float4 make_y<2>(double2 z) {
     const float hx = __double2float_rn(z.x), hy = __double2float_rn(z.y);
     return make_float4(hx, hy, __double2float_rn(z.x - (double)hx), __double2float_rn(z.y - (double)hy));
@@ -285,35 +350,34 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
     const int rho = info & ((1 << 29) - 1);
     const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
     const long long src = (long long)part * S.B + rho;
-    const double2 t = tvec[S.t_off + src];
+    using C = typename Arith<VT>::C;
+    using T = typename Arith<VT>::T;
+    const T tg{};
+    const C t = to_c<C>(tvec[S.t_off + src]);
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
         const long long es = S.vec_off + src * R + rr;
-        double2 xv;
+        C xv;
         if (up.kind != 0 && active_rhs<R>(st, I.sys, rr, 0)) {
             // the BiCGSTAB vector update this product's input needs, on the source row
             // this thread alone reads: p = r + beta (p - omega v) or s = r - alpha v
             const KState& k = st[I.sys * R + rr];
-            const double2 rv = to_d2(up.r[es]), vv = to_d2(up.v[es]);
-            double2 nv;
+            const C rv = to_c<C>(up.r[es]), vv = to_c<C>(up.v[es]);
+            C nv;
             if (up.kind == 1) {
-                const double2 pv = to_d2(up.out[es]);
-                const double2 ov = cmul(k.omega, vv);
-                const double2 bt = cmul(k.beta, make_double2(pv.x - ov.x, pv.y - ov.y));
-                nv = make_double2(rv.x + bt.x, rv.y + bt.y);
+                const C pv = to_c<C>(up.out[es]);
+                nv = cadd(rv, cmul(ks_beta(k, tg), csub(pv, cmul(ks_omega(k, tg), vv))));
             } else {
-                const double2 av = cmul(k.alpha, vv);
-                nv = make_double2(rv.x - av.x, rv.y - av.y);
+                nv = csub(rv, cmul(ks_alpha(k, tg), vv));
             }
-            const VT q = from_d2<VT>(nv);
+            const VT q = from_c<VT>(nv);
             up.out[es] = q;
-            xv = to_d2(q);
+            xv = to_c<C>(q);
         } else {
-            xv = to_d2(x[es]);
+            xv = to_c<C>(x[es]);
         }
-        const double2 z = cmul(t, xv);
-        const double2 yu = make_double2(flipd(z.x, eneg), flipd(z.y, eneg));
-        const double2 yw = make_double2(flipd(yu.x, sneg), flipd(yu.y, sneg));
+        const C yu = cflip(cmul(t, xv), eneg);
+        const C yw = cflip(yu, sneg);
         const long long o = S.vec_off + (long long)row * R + rr;
         Yu[o] = make_y<YK>(yu);
         Yw[o] = make_y<YK>(yw);
@@ -601,20 +665,45 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
     const double den = b.x * b.x + b.y * b.y;
     return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
 }
+__device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
+    const float den = b.x * b.x + b.y * b.y;
+    return make_float2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
 __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+__device__ __forceinline__ bool finite2(float2 a) { return isfinite(a.x) && isfinite(a.y); }
+__device__ __forceinline__ double tsqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float tsqrt(float v) { return sqrtf(v); }
+template <typename C> __device__ __forceinline__ C cmake(double re, double im) {
+    C z;
+    z.x = re;
+    z.y = im;
+    return z;
+}
 
 // Phases: 0 init (vector dots: |b|^2); 1 alpha = rho/<r0,v> (reduce dots);
 // 2 omega = <t,s>/|t|^2 (reduce dots); 3 end of iteration (vector dots |r|^2,
 // <r0,r>: convergence, restart test, beta); 4 restart done (reduce dots |r|^2).
-// One warp per (cluster, rhs): lanes stride over the item partials, a fixed
-// butterfly combines them (deterministic), lane 0 updates the scalars.
-// Scalar update of one (cluster, rhs) from its summed dots d0, d1 (one thread).
-__device__ void scalar_apply(KState& k, int phase, double2 d0, double2 d1, double tol, int maxiter) {
-    const double eps = 2.220446049250313e-16;
+// Scalar update of one (cluster, rhs) from its summed dots d0, d1 (one thread), in
+// the solver's arithmetic T; the FP32 solver mirrors bsq and rsq into the FP64
+// fields that the host reads.
+template <typename T>
+__device__ void scalar_apply_t(KState& k, int phase, typename CplxT<T>::t d0, typename CplxT<T>::t d1, double tol,
+                               int maxiter) {
+    using C = typename CplxT<T>::t;
+    const T tg{};
+    const T eps = (T)2.220446049250313e-16;
+    auto& rho = ks_rho(k, tg);
+    auto& alpha = ks_alpha(k, tg);
+    auto& omega = ks_omega(k, tg);
+    auto& beta = ks_beta(k, tg);
+    auto& r0sq = ks_r0sq(k, tg);
+    auto& bsq = ks_bsq(k, tg);
+    auto& rsq = ks_rsq(k, tg);
+    auto& tol2 = ks_tol2(k, tg);
     if (phase == 0) {
-        k.bsq = k.r0sq = k.rsq = d0.x;
-        k.tol2 = tol * tol * d0.x;
-        k.rho = k.alpha = k.omega = make_double2(1, 0);
+        bsq = r0sq = rsq = d0.x;
+        tol2 = (T)tol * (T)tol * d0.x;
+        rho = alpha = omega = cmake<C>(1, 0);
         k.iters = k.restarts = k.need_restart = 0;
         k.maxiter = maxiter;
         if (!isfinite(d0.x)) {   // a non-finite right-hand side: no comparison below may call it converged
@@ -622,101 +711,107 @@ __device__ void scalar_apply(KState& k, int phase, double2 d0, double2 d1, doubl
             k.status = GB_NAN;
             return;
         }
-        if (d0.x == 0.0 || !(k.rsq > k.tol2) || maxiter <= 0) {
+        if (d0.x == (T)0 || !(rsq > tol2) || maxiter <= 0) {
             k.done = 1;
             k.status = GB_OK;
         } else {
             k.done = 0;
             k.status = ST_RUNNING;
-            const double2 rho_old = k.rho;          // loop top of the first iteration
-            k.rho = make_double2(d0.x, 0.0);        // <r0, r> = |b|^2
-            k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
+            const C rho_old = rho;          // loop top of the first iteration
+            rho = cmake<C>(d0.x, 0.0);      // <r0, r> = |b|^2
+            beta = cmul(cdiv(rho, rho_old), cdiv(alpha, omega));
         }
         return;
     }
     if (phase == 4) {   // Eigen: r = b - A x; r0 = r; rho = r0_sqnorm = |r|^2; the first restart resets i
         k.need_restart = 0;
-        k.rsq = k.r0sq = d0.x;
-        const double2 rho_old = k.rho;
-        k.rho = make_double2(d0.x, 0.0);
+        rsq = r0sq = d0.x;
+        const C rho_old = rho;
+        rho = cmake<C>(d0.x, 0.0);
         if (k.restarts++ == 0) k.iters = 0;
-        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
-        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
-        k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
-        if (!finite2(k.beta)) { k.done = 1; k.status = GB_BREAKDOWN; }
+        if (!isfinite(rsq)) { k.done = 1; k.status = GB_NAN; return; }
+        if (!(rsq > tol2)) { k.done = 1; k.status = GB_OK; return; }
+        beta = cmul(cdiv(rho, rho_old), cdiv(alpha, omega));
+        if (!finite2(beta)) { k.done = 1; k.status = GB_BREAKDOWN; }
         return;
     }
     if (phase == 1) {
-        k.alpha = cdiv(k.rho, d0);
-        if (!finite2(k.alpha)) { k.done = 1; k.status = (d0.x == 0 && d0.y == 0) ? GB_BREAKDOWN : GB_NAN; }
+        alpha = cdiv(rho, d0);
+        if (!finite2(alpha)) { k.done = 1; k.status = (d0.x == 0 && d0.y == 0) ? GB_BREAKDOWN : GB_NAN; }
     } else if (phase == 2) {
-        const double tt = d0.x;
-        k.omega = (tt > 0.0) ? make_double2(d1.x / tt, d1.y / tt) : make_double2(0, 0);
-        if (!finite2(k.omega)) { k.done = 1; k.status = GB_NAN; }
+        const T tt = d0.x;
+        omega = (tt > (T)0) ? cmake<C>(d1.x / tt, d1.y / tt) : cmake<C>(0, 0);
+        if (!finite2(omega)) { k.done = 1; k.status = GB_NAN; }
     } else if (phase == 3) {
         k.iters += 1;
-        k.rsq = d0.x;
-        if (!isfinite(k.rsq)) { k.done = 1; k.status = GB_NAN; return; }
-        if (!(k.rsq > k.tol2)) { k.done = 1; k.status = GB_OK; return; }
+        rsq = d0.x;
+        if (!isfinite(rsq)) { k.done = 1; k.status = GB_NAN; return; }
+        if (!(rsq > tol2)) { k.done = 1; k.status = GB_OK; return; }
         if (k.iters >= k.maxiter) { k.done = 1; k.status = GB_NOT_CONVERGED; return; }
-        const double2 rho_old = k.rho;
-        k.rho = d1;   // <r0, r>
-        if (sqrt(k.rho.x * k.rho.x + k.rho.y * k.rho.y) < eps * eps * k.r0sq) {
+        const C rho_old = rho;
+        rho = d1;   // <r0, r>
+        if (tsqrt(rho.x * rho.x + rho.y * rho.y) < eps * eps * r0sq) {
             if (k.restarts >= kMaxRestarts) { k.done = 1; k.status = GB_BREAKDOWN; return; }
-            k.rho = rho_old;   // phase 4 recomputes rho from the fresh residual
+            rho = rho_old;   // phase 4 recomputes rho from the fresh residual
             k.need_restart = 1;
             return;
         }
-        k.beta = cmul(cdiv(k.rho, rho_old), cdiv(k.alpha, k.omega));
-        if (!finite2(k.beta)) { k.done = 1; k.status = GB_NAN; }
+        beta = cmul(cdiv(rho, rho_old), cdiv(alpha, omega));
+        if (!finite2(beta)) { k.done = 1; k.status = GB_NAN; }
     }
 }
-
+template <typename T, typename C>
+__device__ void scalar_apply(KState& k, int phase, C d0, C d1, double tol, int maxiter) {
+    scalar_apply_t<T>(k, phase, d0, d1, tol, maxiter);
+    if (std::is_same<T, float>::value) {
+        k.bsq = (double)k.bsq_f;
+        k.rsq = (double)k.rsq_f;
+    }
+}
 
 __device__ __forceinline__ bool scalar_skips(const KState& k, int phase) {
     return (phase != 0 && phase != 4 && (k.done || k.need_restart)) || (phase == 4 && !k.need_restart);
 }
 
+// Per-item partial dots: [item][rhs][2] complex values in the solver's arithmetic
+// (float2 for the FP32 solver, double2 otherwise) in the dots buffer.
 // One warp per (cluster, rhs): lanes stride over the item partials, a fixed
 // butterfly combines them (deterministic), lane 0 updates the scalars.
-template <int R>
+template <int R, typename T>
 __device__ void scalar_step(const SysPlan* __restrict__ plan, KState* __restrict__ st, int phase,
-                            const double2* __restrict__ dots, double tol, int maxiter, int sidx, int rr, int lane) {
+                            const double2* __restrict__ dots_raw, double tol, int maxiter, int sidx, int rr, int lane) {
+    using C = typename CplxT<T>::t;
+    const C* dots = reinterpret_cast<const C*>(dots_raw);
     KState& k = st[sidx * R + rr];
     if (scalar_skips(k, phase)) return;
     const SysPlan pl = plan[sidx];
     const bool vec = (phase == 0 || phase == 3);
     const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
-    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+    C d0 = czero<C>(), d1 = czero<C>();
     for (int it = b0 + lane; it < b1; it += 32) {
-        const double2 a = __ldcg(dots + ((long long)it * R + rr) * 2 + 0);
-        const double2 c = __ldcg(dots + ((long long)it * R + rr) * 2 + 1);
-        d0.x += a.x; d0.y += a.y;
-        d1.x += c.x; d1.y += c.y;
+        d0 = cadd(d0, __ldcg(dots + ((long long)it * R + rr) * 2 + 0));
+        d1 = cadd(d1, __ldcg(dots + ((long long)it * R + rr) * 2 + 1));
     }
     for (int o = 16; o > 0; o >>= 1) {
-        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
-        d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
-        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
-        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
+        d0 = cadd(d0, shfl_xor(d0, o));
+        d1 = cadd(d1, shfl_xor(d1, o));
     }
-    if (lane == 0) scalar_apply(k, phase, d0, d1, tol, maxiter);
+    if (lane == 0) scalar_apply<T>(k, phase, d0, d1, tol, maxiter);
 }
 
-template <int R>
+template <int R, typename T>
 __global__ void k_scalar(const SysPlan* __restrict__ plan, int nsys, KState* __restrict__ st, int phase,
                          const double2* __restrict__ dots, double tol, int maxiter) {
     const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (id >= nsys * R) return;
-    scalar_step<R>(plan, st, phase, dots, tol, maxiter, id / R, id % R, lane);
+    scalar_step<R, T>(plan, st, phase, dots, tol, maxiter, id / R, id % R, lane);
 }
 
 // Scalar update fused into the kernel that produces its partial dots: each CTA
 // of a cluster counts itself in after writing its partials; the last one (all of
-// the cluster's partials are then visible) runs scalar_step for every rhs with
-// its warp 0 and resets the counter for the next launch.  The partials are summed
-// in the same fixed order as by k_scalar.
+// the cluster's partials are then visible) runs the scalar update for every rhs
+// and resets the counter for the next launch.
 struct ScalarFuse {
     KState* st = nullptr;   // null: no fused update
     int* cnt = nullptr;     // [nsys] arrivals, zero between launches
@@ -729,11 +824,13 @@ struct ScalarFuse {
 // written and fenced.  The last CTA of the cluster sums the cluster's partials
 // with all its NT threads (strided per thread, then warp butterflies, then the
 // warps in order: a fixed order, deterministic) and updates the scalars.
-template <int R, int NT>
+template <int R, int NT, typename T>
 __device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict__ plan,
-                                 const double2* __restrict__ dots, int sys, int nitems_sys) {
+                                 const double2* __restrict__ dots_raw, int sys, int nitems_sys) {
+    using C = typename CplxT<T>::t;
+    const C* dots = reinterpret_cast<const C*>(dots_raw);
     __shared__ int s_last;
-    __shared__ double2 s_red[NT / 32][R][2];
+    __shared__ C s_red[NT / 32][R][2];
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -752,18 +849,14 @@ __device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
-        double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+        C d0 = czero<C>(), d1 = czero<C>();
         for (int it = b0 + (int)threadIdx.x; it < b1; it += NT) {
-            const double2 a = __ldcg(dots + ((long long)it * R + rr) * 2 + 0);   // written by other CTAs
-            const double2 c = __ldcg(dots + ((long long)it * R + rr) * 2 + 1);
-            d0.x += a.x; d0.y += a.y;
-            d1.x += c.x; d1.y += c.y;
+            d0 = cadd(d0, __ldcg(dots + ((long long)it * R + rr) * 2 + 0));   // written by other CTAs
+            d1 = cadd(d1, __ldcg(dots + ((long long)it * R + rr) * 2 + 1));
         }
         for (int o = 16; o > 0; o >>= 1) {
-            d0.x += __shfl_xor_sync(0xffffffffu, d0.x, o);
-            d0.y += __shfl_xor_sync(0xffffffffu, d0.y, o);
-            d1.x += __shfl_xor_sync(0xffffffffu, d1.x, o);
-            d1.y += __shfl_xor_sync(0xffffffffu, d1.y, o);
+            d0 = cadd(d0, shfl_xor(d0, o));
+            d1 = cadd(d1, shfl_xor(d1, o));
         }
         if (lane == 0) {
             s_red[wid][rr][0] = d0;
@@ -775,12 +868,12 @@ __device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict
         const int rr = threadIdx.x;
         KState& k = fz.st[sys * R + rr];
         if (scalar_skips(k, fz.phase)) return;
-        double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
+        C d0 = czero<C>(), d1 = czero<C>();
         for (int w = 0; w < NT / 32; w++) {
-            d0.x += s_red[w][rr][0].x; d0.y += s_red[w][rr][0].y;
-            d1.x += s_red[w][rr][1].x; d1.y += s_red[w][rr][1].y;
+            d0 = cadd(d0, s_red[w][rr][0]);
+            d1 = cadd(d1, s_red[w][rr][1]);
         }
-        scalar_apply(k, fz.phase, d0, d1, fz.tol, fz.maxiter);
+        scalar_apply<T>(k, fz.phase, d0, d1, fz.tol, fz.maxiter);
     }
 }
 
@@ -792,6 +885,10 @@ template <typename OutT> struct RAcc {
     __device__ void zero() { s.x = s.y = 0; }
     __device__ void add(const OutT& v) { s.x += v.x; s.y += v.y; }
     __device__ double2 get() const { return make_double2((double)s.x, (double)s.y); }
+    template <typename C> __device__ C as() const {   // in the arithmetic C of the consumer
+        if constexpr (std::is_same<C, OutT>::value) return s;
+        else return to_c<C>(get());
+    }
 };
 template <> struct RAcc<float4> {
     float rh, ih, rl, il;
@@ -801,6 +898,7 @@ template <> struct RAcc<float4> {
         df_add(ih, il, v.y, v.w);
     }
     __device__ double2 get() const { return make_double2((double)rh + (double)rl, (double)ih + (double)il); }
+    template <typename C> __device__ C as() const { return to_c<C>(get()); }
 };
 
 // y = x + T x (from the partials, or from a dense Tx), and per-item partial dots:
@@ -808,12 +906,52 @@ template <> struct RAcc<float4> {
 //   mode 3: y := b - (x + T x), d0 = |y|^2  (residual).
 constexpr int kRBThreads = 384;   // threads of the block reduce (>= B*R for lmax <= 8, R <= 2)
 
+// Partials are read as 16-byte words: two float2 elements, or one float4 / double2.
+template <typename OutT> struct PWord {
+    static constexpr int E = 1;
+    __device__ static void load(const OutT* p, OutT (&v)[1]) { v[0] = __ldg(p); }
+};
+template <> struct PWord<float2> {
+    static constexpr int E = 2;
+    __device__ static void load(const float2* p, float2 (&v)[2]) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        v[0] = make_float2(q.x, q.y);
+        v[1] = make_float2(q.z, q.w);
+    }
+};
+
+// a[e] += term t's word element e for t = t0, t0 + G, ... < n (terms stride elements
+// apart), in order; the loads of 8 terms are issued before their sums so that each
+// thread keeps 8 words in flight.
+template <typename OutT, int E>
+__device__ __forceinline__ void sum_terms(const OutT* __restrict__ p, long long t0, long long n, int G, long long stride,
+                                          RAcc<OutT> (&a)[E]) {
+    constexpr int U = 8;
+    long long t = t0;
+    for (; t + (U - 1) * (long long)G < n; t += U * (long long)G) {
+        OutT v[U][E];
+#pragma unroll
+        for (int u = 0; u < U; u++) PWord<OutT>::load(p + (t + u * (long long)G) * stride, v[u]);
+#pragma unroll
+        for (int u = 0; u < U; u++)
+#pragma unroll
+            for (int e = 0; e < E; e++) a[e].add(v[u][e]);
+    }
+    for (; t < n; t += G) {
+        OutT v[E];
+        PWord<OutT>::load(p + t * stride, v);
+#pragma unroll
+        for (int e = 0; e < E; e++) a[e].add(v[e]);
+    }
+}
+
 // K3b (packed path): one CTA per particle block k of a cluster.  Its rows' products
 // are the sum of the strip partials of block row k (contiguous in CU) and the
 // column partials of the blocks (i, k), i < k (contiguous in CW by destination).
-// The CTA's threads form G = kRBThreads / (B R) groups that split the terms; thread
-// (g, v) streams element v (= column * R + rhs) of its terms, so every term is one
-// coalesced B*R-element read.  The groups are combined in order (deterministic),
+// A term (B R elements, element = column * R + rhs) is W 16-byte words; the CTA's
+// threads form G = kRBThreads / W groups that split the terms, thread (g, w) streaming
+// word w of its terms, so every term is one coalesced read.  The groups are combined
+// in order (deterministic),
 // then thread (row, rhs) applies the sign/permutation of its row, adds the identity
 // term, stores y and contributes to the CTA's partial dot products (modes as k_reduce).
 template <typename OutT, typename VT, int R>
@@ -829,211 +967,147 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
     if (!any_active<R>(st, I.sys, mask_mode)) return;
     const gb::SysDev S = sys[I.sys];
     const SysPlan pl = plan[I.sys];
+    constexpr int E = PWord<OutT>::E;
     const int B = S.B, BR = B * R;
-    const int G = kRBThreads / BR;
-    const int tid = threadIdx.x, g = tid / BR, v = tid - g * BR;
+    const int W = BR / E;   // 16-byte words per term (B R is even)
+    const int G = kRBThreads / W;
+    const int tid = threadIdx.x, g = tid / W, w = tid - g * W;
     const int k = I.r0 / B;   // particle (block row) of this item
-    __shared__ double2 partU[kRBThreads], partW[kRBThreads];
-    __shared__ double2 red[kRBThreads][2];
+    using C = typename Arith<VT>::C;
+    using T = typename Arith<VT>::T;
+    __shared__ C partU[2 * kRBThreads], partW[2 * kRBThreads];
+    __shared__ C red[kRBThreads / 32][R][2];
     if (g < G) {
         const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
         const long long ns = s1 - s0;
-        const OutT* cu = CU + pl.cu_off + (s0 - pl.strip_base) * (long long)BR + v;
-        const OutT* cw = CW + pl.cw_off + ((long long)k * (k - 1) / 2) * BR + v;
-        RAcc<OutT> au, aw;
-        au.zero();
-        aw.zero();
-#pragma unroll 4
-        for (long long t = g; t < ns; t += G) au.add(cu[t * BR]);
-#pragma unroll 4
-        for (long long t = g; t < k; t += G) aw.add(cw[t * BR]);
-        partU[tid] = au.get();
-        partW[tid] = aw.get();
+        const OutT* cu = CU + pl.cu_off + (s0 - pl.strip_base) * (long long)BR + w * E;
+        const OutT* cw = CW + pl.cw_off + ((long long)k * (k - 1) / 2) * BR + w * E;
+        RAcc<OutT> au[E], aw[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            au[e].zero();
+            aw[e].zero();
+        }
+        sum_terms<OutT, E>(cu, g, ns, G, BR, au);
+        sum_terms<OutT, E>(cw, g, k, G, BR, aw);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            partU[g * BR + w * E + e] = au[e].template as<C>();
+            partW[g * BR + w * E + e] = aw[e].template as<C>();
+        }
     }
     __syncthreads();
-    double2 d0 = make_double2(0, 0), d1 = make_double2(0, 0);
-    int rr = 0;
+    C d0 = czero<C>(), d1 = czero<C>();
     if (tid < BR) {
-        const int r = tid / R;
-        rr = tid - r * R;
+        const int r = tid / R, rr = tid - r * R;
         const int info = __ldg(S.rowinfo + r);
         const int rho = info & ((1 << 29) - 1);
         const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
-        double2 a = make_double2(0, 0), c = make_double2(0, 0);
+        C a = czero<C>(), c = czero<C>();
         for (int q = 0; q < G; q++) {
-            const double2 u = partU[q * BR + rho * R + rr], w = partW[q * BR + rho * R + rr];
-            a.x += u.x; a.y += u.y;
-            c.x += w.x; c.y += w.y;
+            a = cadd(a, partU[q * BR + rho * R + rr]);
+            c = cadd(c, partW[q * BR + rho * R + rr]);
         }
-        a = make_double2(flipd(a.x, eneg), flipd(a.y, eneg));
-        c = make_double2(flipd(c.x, eneg ^ sneg), flipd(c.y, eneg ^ sneg));
-        const double2 tx = make_double2(a.x + c.x, a.y + c.y);
+        const C tx = cadd(cflip(a, eneg), cflip(c, eneg ^ sneg));
         if (active_rhs<R>(st, I.sys, rr, mask_mode)) {
             const long long e = S.vec_off + (long long)(I.r0 + r) * R + rr;
-            const double2 xv = to_d2(x[e]);
-            double2 yv = make_double2(xv.x + tx.x, xv.y + tx.y);
-            if (mode == 3) {
-                const double2 bv = b128 ? b128[e] : to_d2(aux[e]);
-                yv = make_double2(bv.x - yv.x, bv.y - yv.y);
-            }
-            const VT yo = from_d2<VT>(yv);
+            C yv = cadd(to_c<C>(x[e]), tx);
+            if (mode == 3) yv = csub(b128 ? to_c<C>(b128[e]) : to_c<C>(aux[e]), yv);
+            const VT yo = from_c<VT>(yv);
             y[e] = yo;
-            const double2 yq = to_d2(yo);   // dots of the stored (rounded) vector
+            const C yq = to_c<C>(yo);   // dots of the stored (rounded) vector
             if (mode == 1) {
-                cfma_conj(d0, to_d2(aux[e]), yq);
+                cfma_conj(d0, to_c<C>(aux[e]), yq);
             } else if (mode == 2) {
                 d0.x += yq.x * yq.x + yq.y * yq.y;
-                cfma_conj(d1, yq, to_d2(aux[e]));
+                cfma_conj(d1, yq, to_c<C>(aux[e]));
             } else if (mode == 3) {
                 d0.x += yq.x * yq.x + yq.y * yq.y;
             }
         }
     }
     if (mode == 0) return;
-    red[tid][0] = d0;
-    red[tid][1] = d1;
+    // CTA dots per rhs: rows of one rhs are R lanes apart, so butterflies over the
+    // lanes of equal rhs leave each warp's sums in lanes 0..R-1; the warps holding
+    // rows are then added in order (a fixed tree: deterministic)
+    const int lane = tid & 31, wid = tid >> 5, nw = (BR + 31) / 32;
+#pragma unroll
+    for (int o = 16; o >= R; o >>= 1) {
+        d0 = cadd(d0, shfl_xor(d0, o));
+        d1 = cadd(d1, shfl_xor(d1, o));
+    }
+    if (lane < R && wid < nw) {
+        red[wid][lane][0] = d0;
+        red[wid][lane][1] = d1;
+    }
     __syncthreads();
-    if (tid < R) {   // per rhs, rows in order
-        double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
-        for (int q = tid; q < BR; q += R) {
-            s0.x += red[q][0].x; s0.y += red[q][0].y;
-            s1.x += red[q][1].x; s1.y += red[q][1].y;
+    if (tid < R) {
+        C s0 = czero<C>(), s1 = czero<C>();
+        for (int q = 0; q < nw; q++) {
+            s0 = cadd(s0, red[q][tid][0]);
+            s1 = cadd(s1, red[q][tid][1]);
         }
-        dots[((long long)it * R + tid) * 2 + 0] = s0;
-        dots[((long long)it * R + tid) * 2 + 1] = s1;
+        C* dc = reinterpret_cast<C*>(dots);
+        dc[((long long)it * R + tid) * 2 + 0] = s0;
+        dc[((long long)it * R + tid) * 2 + 1] = s1;
         __threadfence();
     }
-    (void)rr;
-    if (fz.st) fused_scalar_cta<R, kRBThreads>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
+    if (fz.st) fused_scalar_cta<R, kRBThreads, T>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
 }
 
-template <typename OutT, typename VT, int R, bool DENSE>
-__global__ void __launch_bounds__(kRWarps * 32)
-k_reduce(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
-         const SysPlan* __restrict__ plan, const long long* __restrict__ row_strip, const KState* __restrict__ st,
-         int mask_mode, const OutT* __restrict__ CU, const OutT* __restrict__ CW, const double2* __restrict__ Tx_dense,
-         const VT* __restrict__ x, VT* __restrict__ y, int mode, const VT* __restrict__ aux,
-         const double2* __restrict__ b128, double2* __restrict__ dots, ScalarFuse fz) {
+// Dense path (FP64 vectors): y = x + T x for the 32 rows of one item (one warp),
+// with the partial dots of the modes of k_reduce_blk and the fused scalar update.
+template <int R>
+__global__ void __launch_bounds__(kRRows)
+k_reduce_dense(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
+               const SysPlan* __restrict__ plan, const KState* __restrict__ st, int mask_mode,
+               const double2* __restrict__ Tx, const double2* __restrict__ x, double2* __restrict__ y, int mode,
+               const double2* __restrict__ aux, const double2* __restrict__ b128, double2* __restrict__ dots,
+               ScalarFuse fz) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
     if (!any_active<R>(st, I.sys, mask_mode)) return;
     const gb::SysDev S = sys[I.sys];
-    __shared__ double2 pu[kRWarps][kRRows][R];
-    __shared__ double2 pw[kRWarps][kRRows][R];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const bool valid = lane < I.nr;
+    const int lane = threadIdx.x;
     const int row = I.r0 + lane;
-    const int B = S.B;
-    if (!DENSE) {
-        // partial sums kept in the partials' own precision (FP32 for the FP32 policy,
-        // double-float for the double-float one)
-        RAcc<OutT> su[R], sw[R];
-#pragma unroll
-        for (int rr = 0; rr < R; rr++) {
-            su[rr].zero();
-            sw[rr].zero();
-        }
-        if (valid) {
-            const int k = row / B, Rr = row % B;
-            const int info = __ldg(S.rowinfo + Rr);
-            const int rho = info & ((1 << 29) - 1);
-            const SysPlan pl = plan[I.sys];
-            const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
-            const long long nterm = (s1 - s0) + k;
-            for (long long t = wid; t < nterm; t += kRWarps) {
-                if (t < s1 - s0) {
-                    const OutT* src = CU + pl.cu_off + ((t + s0 - pl.strip_base) * B + rho) * R;
-#pragma unroll
-                    for (int rr = 0; rr < R; rr++) {
-                        su[rr].add(src[rr]);
-                    }
-                } else {
-                    const int i = (int)(t - (s1 - s0));
-                    const long long pr = pair_start(i, S.N) + (k - i - 1);
-                    const OutT* src = CW + pl.cw_off + (pr * B + rho) * R;
-#pragma unroll
-                    for (int rr = 0; rr < R; rr++) {
-                        sw[rr].add(src[rr]);
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int rr = 0; rr < R; rr++) {
-            pu[wid][lane][rr] = su[rr].get();
-            pw[wid][lane][rr] = sw[rr].get();
-        }
-        __syncthreads();
-    }
     double2 d0[R], d1[R];
 #pragma unroll
     for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = make_double2(0, 0);
-    if (valid && wid == 0) {
-        double2 tx[R];
-        if (DENSE) {
-#pragma unroll
-            for (int rr = 0; rr < R; rr++) tx[rr] = Tx_dense[(long long)row * R + rr];
-        } else {
-            const int info = __ldg(S.rowinfo + row % B);
-            const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
-#pragma unroll
-            for (int rr = 0; rr < R; rr++) {
-                double2 a = make_double2(0, 0), c = make_double2(0, 0);
-                for (int w = 0; w < kRWarps; w++) {
-                    a.x += pu[w][lane][rr].x;
-                    a.y += pu[w][lane][rr].y;
-                    c.x += pw[w][lane][rr].x;
-                    c.y += pw[w][lane][rr].y;
-                }
-                a = make_double2(flipd(a.x, eneg), flipd(a.y, eneg));
-                c = make_double2(flipd(c.x, eneg ^ sneg), flipd(c.y, eneg ^ sneg));
-                tx[rr] = make_double2(a.x + c.x, a.y + c.y);
-            }
-        }
+    if (lane < I.nr) {
         const long long vo = S.vec_off + (long long)row * R;
 #pragma unroll
         for (int rr = 0; rr < R; rr++) {
             if (!active_rhs<R>(st, I.sys, rr, mask_mode)) continue;
-            const double2 xv = to_d2(x[vo + rr]);
-            double2 yv = make_double2(xv.x + tx[rr].x, xv.y + tx[rr].y);
-            if (mode == 3) {
-                const double2 bv = b128 ? b128[vo + rr] : to_d2(aux[vo + rr]);
-                yv = make_double2(bv.x - yv.x, bv.y - yv.y);
-            }
-            const VT yo = from_d2<VT>(yv);
-            y[vo + rr] = yo;
-            const double2 yq = to_d2(yo);   // dots of the stored (rounded) vector
+            double2 yv = cadd(x[vo + rr], Tx[(long long)row * R + rr]);
+            if (mode == 3) yv = csub(b128 ? b128[vo + rr] : aux[vo + rr], yv);
+            y[vo + rr] = yv;
             if (mode == 1) {
-                cfma_conj(d0[rr], to_d2(aux[vo + rr]), yq);
+                cfma_conj(d0[rr], aux[vo + rr], yv);
             } else if (mode == 2) {
-                d0[rr].x += yq.x * yq.x + yq.y * yq.y;
-                cfma_conj(d1[rr], yq, to_d2(aux[vo + rr]));
+                d0[rr].x += yv.x * yv.x + yv.y * yv.y;
+                cfma_conj(d1[rr], yv, aux[vo + rr]);
             } else if (mode == 3) {
-                d0[rr].x += yq.x * yq.x + yq.y * yq.y;
+                d0[rr].x += yv.x * yv.x + yv.y * yv.y;
             }
         }
     }
     if (mode == 0) return;
-    if (wid == 0) {
 #pragma unroll
-        for (int rr = 0; rr < R; rr++) {
-            for (int o = 16; o > 0; o >>= 1) {
-                d0[rr].x += __shfl_xor_sync(0xffffffffu, d0[rr].x, o);
-                d0[rr].y += __shfl_xor_sync(0xffffffffu, d0[rr].y, o);
-                d1[rr].x += __shfl_xor_sync(0xffffffffu, d1[rr].x, o);
-                d1[rr].y += __shfl_xor_sync(0xffffffffu, d1[rr].y, o);
-            }
-            if (lane == 0) {
-                dots[((long long)it * R + rr) * 2 + 0] = d0[rr];
-                dots[((long long)it * R + rr) * 2 + 1] = d1[rr];
-                __threadfence();
-            }
+    for (int rr = 0; rr < R; rr++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            d0[rr] = cadd(d0[rr], shfl_xor(d0[rr], o));
+            d1[rr] = cadd(d1[rr], shfl_xor(d1[rr], o));
+        }
+        if (lane == 0) {
+            dots[((long long)it * R + rr) * 2 + 0] = d0[rr];
+            dots[((long long)it * R + rr) * 2 + 1] = d1[rr];
+            __threadfence();
         }
     }
     if (fz.st) {
         const SysPlan pl = plan[I.sys];
-        fused_scalar_cta<R, kRWarps * 32>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
+        fused_scalar_cta<R, kRRows, double>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
     }
 }
 
@@ -1055,11 +1129,14 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     const int mask = (kind == 0) ? -1 : (kind == 4 ? 1 : 0);
     if (!any_active<R>(st, I.sys, mask)) return;
     const gb::SysDev S = sys[I.sys];
-    __shared__ double2 red[kVRows / 32][R][2];
+    using C = typename Arith<VT>::C;
+    using T = typename Arith<VT>::T;
+    const T tg{};
+    __shared__ C red[kVRows / 32][R][2];
     const int lr = threadIdx.x;
-    double2 d0[R], d1[R];
+    C d0[R], d1[R];
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = make_double2(0, 0);
+    for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = czero<C>();
     if (lr < I.nr) {
         const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
 #pragma unroll
@@ -1068,30 +1145,27 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
             const long long e = vo + rr;
             const KState& k = st[I.sys * R + rr];
             if (kind == 0) {
-                const double2 bv = b ? b[e] : to_d2(bx[e]);
-                const VT bq = from_d2<VT>(bv);
-                const VT z = from_d2<VT>(make_double2(0, 0));
+                const VT bq = b ? from_d2<VT>(b[e]) : bx[e];
+                const VT z = from_c<VT>(czero<C>());
                 x[e] = z; p[e] = z; v[e] = z;
                 r[e] = bq; r0[e] = bq;
                 if (bx && b) bx[e] = bq;
-                const double2 bd = to_d2(bq);
+                const C bd = to_c<C>(bq);
                 d0[rr].x += bd.x * bd.x + bd.y * bd.y;
             } else if (kind == 1) {
-                const double2 rv = to_d2(r[e]), pv = to_d2(p[e]), vv = to_d2(v[e]);
-                const double2 ov = cmul(k.omega, vv);
-                const double2 bt = cmul(k.beta, make_double2(pv.x - ov.x, pv.y - ov.y));
-                p[e] = from_d2<VT>(make_double2(rv.x + bt.x, rv.y + bt.y));
+                const C rv = to_c<C>(r[e]), pv = to_c<C>(p[e]), vv = to_c<C>(v[e]);
+                const C bt = cmul(ks_beta(k, tg), csub(pv, cmul(ks_omega(k, tg), vv)));
+                p[e] = from_c<VT>(cadd(rv, bt));
             } else if (kind == 2) {
-                const double2 rv = to_d2(r[e]), vv = to_d2(v[e]);
-                const double2 av = cmul(k.alpha, vv);
-                s[e] = from_d2<VT>(make_double2(rv.x - av.x, rv.y - av.y));
+                const C rv = to_c<C>(r[e]), vv = to_c<C>(v[e]);
+                s[e] = from_c<VT>(csub(rv, cmul(ks_alpha(k, tg), vv)));
             } else if (kind == 3) {
-                const double2 pv = to_d2(p[e]), sv = to_d2(s[e]), tv = to_d2(t[e]), xv = to_d2(x[e]);
-                const double2 ap = cmul(k.alpha, pv), ws = cmul(k.omega, sv), wt = cmul(k.omega, tv);
-                x[e] = from_d2<VT>(make_double2(xv.x + ap.x + ws.x, xv.y + ap.y + ws.y));
-                const VT rq = from_d2<VT>(make_double2(sv.x - wt.x, sv.y - wt.y));
+                const C pv = to_c<C>(p[e]), sv = to_c<C>(s[e]), tv = to_c<C>(t[e]), xv = to_c<C>(x[e]);
+                const C ap = cmul(ks_alpha(k, tg), pv), ws = cmul(ks_omega(k, tg), sv), wt = cmul(ks_omega(k, tg), tv);
+                x[e] = from_c<VT>(cadd(cadd(xv, ap), ws));
+                const VT rq = from_c<VT>(csub(sv, wt));
                 r[e] = rq;
-                const double2 rd = to_d2(rq), r0v = to_d2(r0[e]);
+                const C rd = to_c<C>(rq), r0v = to_c<C>(r0[e]);
                 d0[rr].x += rd.x * rd.x + rd.y * rd.y;
                 cfma_conj(d1[rr], r0v, rd);
             } else if (kind == 4) {
@@ -1104,10 +1178,8 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
         for (int o = 16; o > 0; o >>= 1) {
-            d0[rr].x += __shfl_xor_sync(0xffffffffu, d0[rr].x, o);
-            d0[rr].y += __shfl_xor_sync(0xffffffffu, d0[rr].y, o);
-            d1[rr].x += __shfl_xor_sync(0xffffffffu, d1[rr].x, o);
-            d1[rr].y += __shfl_xor_sync(0xffffffffu, d1[rr].y, o);
+            d0[rr] = cadd(d0[rr], shfl_xor(d0[rr], o));
+            d1[rr] = cadd(d1[rr], shfl_xor(d1[rr], o));
         }
         if (lane == 0) {
             red[wid][rr][0] = d0[rr];
@@ -1117,17 +1189,14 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     __syncthreads();
     if (lr < R * 2) {
         const int rr = lr >> 1, which = lr & 1;
-        double2 sm = make_double2(0, 0);
-        for (int w = 0; w < kVRows / 32; w++) {
-            sm.x += red[w][rr][which].x;
-            sm.y += red[w][rr][which].y;
-        }
-        dots[((long long)it * R + rr) * 2 + which] = sm;
+        C sm = czero<C>();
+        for (int w = 0; w < kVRows / 32; w++) sm = cadd(sm, red[w][rr][which]);
+        reinterpret_cast<C*>(dots)[((long long)it * R + rr) * 2 + which] = sm;
     }
     if (fz.st) {
         if (lr < R * 2) __threadfence();   // this thread's partial before the arrival count
         const SysPlan pl = plan[I.sys];
-        fused_scalar_cta<R, kVRows>(fz, plan, dots, I.sys, pl.vend - pl.vbeg);
+        fused_scalar_cta<R, kVRows, T>(fz, plan, dots, I.sys, pl.vend - pl.vbeg);
     }
 }
 
@@ -1679,6 +1748,7 @@ template <typename VT, int R, bool DENSE>
 int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, int pol, const void* mat,
                  const double2* tvec, const double2* b128, VT* bvt, double tol, int maxiter, KState* st, int dense_D,
                  cudaStream_t stream, bool use_graph) {
+    static_assert(!DENSE || std::is_same<VT, double2>::value, "the dense path runs FP64 vectors");
     const size_t TV = (size_t)P.total_vec;
     VT* V = reinterpret_cast<VT*>(base + w.off_vec);
     VT *x = V, *r = V + TV, *r0 = V + 2 * TV, *p = V + 3 * TV, *v = V + 4 * TV, *s = V + 5 * TV, *t = V + 6 * TV,
@@ -1700,16 +1770,15 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     };
     auto apply = [&](const VT* xin, VT* yout, int mode, const VT* aux, int mask, const double2* bb,
                      cudaStream_t sm, ScalarFuse fz = ScalarFuse(), YUpd<VT> up = YUpd<VT>()) -> int {
-        if (DENSE) {
+        if constexpr (DENSE) {
             const long long grid = std::min<long long>(((long long)dense_D * 32 + 255) / 256, (long long)gb::sm_count() * 8);
             gb::note_launch();
             k_dense_gemv<R><<<(unsigned)std::max<long long>(grid, 1), 256, 0, sm>>>(
                 dense_D, reinterpret_cast<const double2*>(mat), reinterpret_cast<const double2*>(xin), Tx);
             GB_CUDA_TRY(cudaGetLastError());
             gb::note_launch();
-            k_reduce<double2, VT, R, true><<<(unsigned)P.nr, kRWarps * 32, 0, sm>>>(
-                D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, nullptr, nullptr, Tx, xin, yout, mode, aux, bb,
-                dots, fz);
+            k_reduce_dense<R><<<(unsigned)P.nr, kRRows, 0, sm>>>(D.sys, D.ritems, P.nr, D.sp, st, mask, Tx, xin, yout,
+                                                               mode, aux, bb, dots, fz);
             GB_CUDA_TRY(cudaGetLastError());
             return GB_OK;
         }
@@ -1850,7 +1919,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             k_vec<VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, 4, nullptr, nullptr, x, r, r0, p, v, s,
                                                     t, dots);
             gb::note_launch();
-            k_scalar<R><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 4, dots, tol, maxiter);
+            k_scalar<R, typename Arith<VT>::T><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 4, dots, tol, maxiter);
             GB_CUDA_TRY(cudaGetLastError());
             continue;
         }
