@@ -9,6 +9,8 @@ one class; every step is a call into the CUDA extension.
 
 from __future__ import annotations
 
+import threading
+
 import numpy as np
 import torch
 
@@ -48,6 +50,22 @@ def footprint_bytes(N, lmax, R=1, precision="fp64"):
     return mat + partials + vec + 4096
 
 
+_stage_local = threading.local()
+
+
+def _staging(nbytes):
+    """This thread's pinned staging buffer (grown as needed) and the event behind its
+    last host->device copy; waits for that copy before handing the buffer out again."""
+    st = getattr(_stage_local, "buf", None)
+    if st is not None:
+        st[1].synchronize()
+    if st is None or st[0].numel() < nbytes:
+        cap = max(nbytes, 1 << 20)
+        st = (torch.empty(cap, dtype=torch.uint8).pin_memory(), torch.cuda.Event())
+        _stage_local.buf = st
+    return st
+
+
 class ClusterBatch:
     """Independent clusters sharing launch sequences.
 
@@ -63,6 +81,34 @@ class ClusterBatch:
         self.device = require_cuda(device)
         self.R = int(R)
         self.precision = precision
+        self._set_layout(specs)
+        dev = self.device
+        t = self.totals
+        # inputs: one device allocation, filled by one host->device copy (see _upload)
+        self._parts = [("pos", np.float64, t["pos"]), ("mie_scat", np.complex128, t["mie"]),
+                       ("mie_int", np.complex128, t["mie"]), ("b", np.complex128, t["vec"])]
+        self._offs, nbytes = {}, 0
+        for name, dt, n in self._parts:
+            self._offs[name] = nbytes
+            nbytes += (np.dtype(dt).itemsize * max(n, 1) + 255) & ~255
+        self._inputs = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        tdt = {np.float64: torch.float64, np.complex128: torch.complex128}
+        self.pos, self.mie_scat, self.mie_int, self.b = (
+            self._inputs[self._offs[name]: self._offs[name] + np.dtype(dt).itemsize * max(n, 1)].view(tdt[dt])
+            for name, dt, n in self._parts)
+        self.h2d_bytes = 8 * t["pos"] + 16 * (2 * t["mie"] + t["vec"])
+        self.tvec = torch.empty(max(t["t"], 1), dtype=torch.complex128, device=dev)
+        self.x = torch.zeros(max(t["vec"], 1), dtype=torch.complex128, device=dev)
+        need = NEEDS[precision]
+        mat = max(t["mat"], 1)
+        self.mat128 = torch.empty(mat, dtype=torch.complex128, device=dev) if "c128" in need else None
+        self.mat64 = torch.empty(mat, dtype=torch.complex64, device=dev) if "hi" in need else None
+        self.mat64lo = torch.empty(mat, dtype=torch.complex64, device=dev) if "lo" in need else None
+        self._ws = None
+        self._host_out = None
+        self._upload(specs)
+
+    def _set_layout(self, specs):
         self.specs = specs
         self.nsys = len(specs)
         descs, mie_off, obs_off = [], [], []
@@ -90,31 +136,43 @@ class ClusterBatch:
         self.sys = nat.systems_array(descs)
         self.mie_off = np.asarray(mie_off, dtype=np.int64)
         self.obs_off = np.asarray(obs_off, dtype=np.int64)
-        dev = self.device
-        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-        self.pos = torch.empty(max(pos_off, 1), dtype=torch.float64, device=dev)
-        self.mie_scat = torch.empty(max(m_off, 1), dtype=torch.complex128, device=dev)
-        self.mie_int = torch.empty(max(m_off, 1), dtype=torch.complex128, device=dev)
-        self.b = torch.empty(max(vec_off, 1), dtype=torch.complex128, device=dev)
-        hpos = np.concatenate([np.asarray(s["position"], float).reshape(-1) for s in specs])
-        hmie = np.concatenate([np.asarray(s["mie_scat"], complex).reshape(-1) for s in specs])
-        hint = np.concatenate([np.asarray(s.get("mie_int", np.zeros_like(s["mie_scat"])), complex).reshape(-1)
-                               for s in specs])
-        hb = np.concatenate([np.asarray(s["p_src"], complex).reshape(-1) for s in specs])
-        self.pos.copy_(pin(hpos), non_blocking=True)
-        self.mie_scat.copy_(pin(hmie), non_blocking=True)
-        self.mie_int.copy_(pin(hint), non_blocking=True)
-        self.b.copy_(pin(hb), non_blocking=True)
-        self.h2d_bytes = hpos.nbytes + hmie.nbytes + hint.nbytes + hb.nbytes
-        self.tvec = torch.empty(max(t_off, 1), dtype=torch.complex128, device=dev)
-        self.x = torch.zeros(max(vec_off, 1), dtype=torch.complex128, device=dev)
-        need = NEEDS[precision]
-        self.mat128 = torch.empty(max(mat_off, 1), dtype=torch.complex128, device=dev) if "c128" in need else None
-        self.mat64 = torch.empty(max(mat_off, 1), dtype=torch.complex64, device=dev) if "hi" in need else None
-        self.mat64lo = torch.empty(max(mat_off, 1), dtype=torch.complex64, device=dev) if "lo" in need else None
-        self._ws = None
+
+    def _upload(self, specs):
+        """Host inputs of specs -> the device input buffer, through this thread's
+        pinned staging buffer, as one asynchronous copy on the current stream."""
+        stage, done = _staging(self._inputs.numel())
+        hv = stage.numpy()
+        for name, dt, n in self._parts:
+            dst = hv[self._offs[name]: self._offs[name] + np.dtype(dt).itemsize * n].view(dt)
+            o = 0
+            for sp in specs:
+                if name == "pos":
+                    a = np.asarray(sp["position"], float).reshape(-1)
+                elif name == "mie_scat":
+                    a = np.asarray(sp["mie_scat"]).reshape(-1)
+                elif name == "mie_int":
+                    a = np.asarray(sp.get("mie_int", np.zeros_like(sp["mie_scat"]))).reshape(-1)
+                else:
+                    a = np.asarray(sp["p_src"]).reshape(-1)
+                dst[o: o + a.size] = a
+                o += a.size
+        self._inputs.copy_(stage[: self._inputs.numel()], non_blocking=True)
+        done.record(torch.cuda.current_stream(self.device))
         self.status = self.iters = self.resid = None
         self.assembled = False
+
+    def load(self, specs):
+        """New clusters of the same shapes (per cluster N and lmax, same order) into
+        this batch's device buffers: positions, Mie coefficients, wavenumbers and
+        right-hand sides are uploaded; the matrices are rebuilt by the next assemble."""
+        old = [(l["N"], l["lmax"]) for l in self.layout]
+        new = [(np.asarray(s["position"]).reshape(-1, 3).shape[0], int(np.asarray(s["mie_scat"]).shape[-1]))
+               for s in specs]
+        if old != new:
+            raise ValueError("load() needs clusters of the batch's shapes (N, lmax per cluster)")
+        self._set_layout(specs)
+        self._upload(specs)
+        return self
 
     # ---------------------------------------------------------------- steps --
     def assemble(self):
@@ -214,6 +272,17 @@ class ClusterBatch:
         l = self.layout[s]
         xs = self.xs[: self.totals["obs"] * self.R * 6 * self.xs_L].view(-1, self.R, 3, 2 * self.xs_L)
         return xs[l["obs_off"]: l["obs_off"] + l["N"], :, :, : 2 * l["lmax"]].sum(dim=(0, 3))
+
+    def to_host(self):
+        """x, per-particle cross-sections, force and torque as numpy arrays, read back
+        with asynchronous copies into pinned buffers and a single synchronisation."""
+        srcs = {"x": self.x, "xs": self.xs, "F": self.F, "T": self.T}
+        if self._host_out is None or any(self._host_out[k].numel() != v.numel() for k, v in srcs.items()):
+            self._host_out = {k: torch.empty(v.numel(), dtype=v.dtype).pin_memory() for k, v in srcs.items()}
+        for k, v in srcs.items():
+            self._host_out[k].copy_(v, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        return {k: v.numpy().copy() for k, v in self._host_out.items()}
 
     # ------------------------------------------------------------- accessors --
     def cluster_view(self, s, t):

@@ -312,3 +312,39 @@ def test_full_size_random_cluster_residual():
     T = O.sphere_aggregate_tmatrix(pos, c.mie_scat.reshape(200, -1), c.material_data.k_b)
     r = O.gemv(T, c.p_inc.ravel()) + c.p_inc.ravel() - c.p_src.ravel()
     assert np.linalg.norm(r) / np.linalg.norm(c.p_src) < 1e-11
+
+
+# ------------------------------------------------- batch reuse and readback --
+def _spec(seed, N=12, lmax=3, R=2):
+    rng = np.random.default_rng(seed)
+    pos, rad = random_cluster(rng, N, 40 * nm, 80 * nm, 900 * nm)
+    md = gb.material_struct([gb.constant_material(index=1.6 + 0.05j)] * N, gb.constant_material(eps=1.0, mu=1.0),
+                            wavelength=(550 + 20 * seed) * nm)
+    ms, mi = gb.mie_coefficients(rad, md.eps, md.mu, md.eps_b, md.mu_b, md.k_b, lmax)
+    srcs = [gb.plane_wave.from_string("x"), gb.plane_wave.from_string("y")][:R]
+    p_src = np.stack([s.structure(pos, md.k_b, lmax) for s in srcs], axis=-1)
+    return dict(position=pos, mie_scat=ms, mie_int=mi, k=float(np.real(md.k_b)), p_src=p_src)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_load_reuses_batch_like_a_fresh_one(precision):
+    """A batch loaded with a new cluster of the same shape (new positions, Mie
+    coefficients, wavenumber and sources) gives exactly what a fresh batch gives;
+    to_host returns the same values as the device tensors."""
+    a, b = _spec(1), _spec(2)
+    reused = ClusterBatch([a], R=2, precision=precision)
+    for spec in (a, b):
+        reused.load([spec]) if spec is b else None
+        reused.assemble().solve(tol=1e-10, inner_tol=1e-4)
+        reused.epilogue(1.0)
+        out = reused.to_host()
+        fresh = ClusterBatch([spec], R=2, precision=precision).assemble()
+        fresh.solve(tol=1e-10, inner_tol=1e-4)
+        fresh.epilogue(1.0)
+        assert np.all(reused.status == 0) and np.all(fresh.status == 0)
+        np.testing.assert_array_equal(out["x"], fresh.x.cpu().numpy())
+        np.testing.assert_array_equal(out["xs"], fresh.xs.cpu().numpy())
+        np.testing.assert_array_equal(out["F"], fresh.F.cpu().numpy())
+        np.testing.assert_array_equal(out["T"], fresh.T.cpu().numpy())
+    with pytest.raises(ValueError):
+        reused.load([_spec(3, N=11)])
