@@ -111,6 +111,32 @@ __device__ __forceinline__ float2 shfl_xor(float2 a, int o) {
 }
 template <typename C> __device__ __forceinline__ C czero() { C z; z.x = 0; z.y = 0; return z; }
 
+// ---------------------------------------------- programmatic dependent launch --
+// The kernels of a BiCGSTAB iteration are launched with programmatic stream
+// serialisation: a kernel may start while its predecessor drains, runs its
+// prologue on plan data (constant during a solve), then waits for the predecessor
+// (griddepcontrol.wait: its grid complete, its memory visible) before any access to
+// data the predecessor produces or consumes.  Every CTA waits before it can exit,
+// so a grid's completion implies its predecessors' completion.  Without the launch
+// attribute the wait returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, Args... args) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // ----------------------------------------------------------- plan structs --
 struct Strip {          // GEMV work: blocks (i, j0 .. j0+nb-1) of cluster sys
     int sys, i, nb, pad;
@@ -338,13 +364,16 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
         int mask_mode, const double2* __restrict__ tvec, const VT* __restrict__ x, typename YType<YK>::t* __restrict__ Yu,
         typename YType<YK>::t* __restrict__ Yw, YUpd<VT> up) {
     const int it = blockIdx.x;
-    if (it >= nitems) return;
+    if (it >= nitems) {
+        pdl_wait();
+        return;
+    }
+    // prologue on plan data and the Mie vector (constant during a solve)
     const Item I = items[it];
-    if (!any_active<R>(st, I.sys, mask_mode)) return;
     const gb::SysDev S = sys[I.sys];
     const int lr = threadIdx.x;
-    if (lr >= I.nr) return;
-    const int row = I.r0 + lr;
+    const bool row_ok = lr < I.nr;
+    const int row = I.r0 + (row_ok ? lr : 0);
     const int part = row / S.B, Rr = row % S.B;
     const int info = __ldg(S.rowinfo + Rr);
     const int rho = info & ((1 << 29) - 1);
@@ -354,6 +383,9 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
     using T = typename Arith<VT>::T;
     const T tg{};
     const C t = to_c<C>(tvec[S.t_off + src]);
+    pdl_wait();
+    pdl_trigger();
+    if (!row_ok || !any_active<R>(st, I.sys, mask_mode)) return;
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
         const long long es = S.vec_off + src * R + rr;
@@ -483,6 +515,8 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     bool failed = false;
     int in_flight = 0;                    // chunks issued and not yet consumed
+    pdl_wait();                           // y vectors and scalars of the predecessors
+    pdl_trigger();
     for (long long w = sbeg + warp; w < send && !failed; w += nwarps) {
         const Strip sp = strips[w];
         bool act = false;
@@ -962,23 +996,28 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
              VT* __restrict__ y, int mode, const VT* __restrict__ aux, const double2* __restrict__ b128,
              double2* __restrict__ dots, ScalarFuse fz) {
     const int it = blockIdx.x;
-    if (it >= nitems) return;
-    const Item I = items[it];
-    if (!any_active<R>(st, I.sys, mask_mode)) return;
+    if (it >= nitems) {
+        pdl_wait();
+        return;
+    }
+    const Item I = items[it];   // prologue on plan data
     const gb::SysDev S = sys[I.sys];
     const SysPlan pl = plan[I.sys];
+    const int k = I.r0 / S.B;   // particle (block row) of this item
+    const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
+    pdl_wait();
+    pdl_trigger();
+    if (!any_active<R>(st, I.sys, mask_mode)) return;
     constexpr int E = PWord<OutT>::E;
     const int B = S.B, BR = B * R;
     const int W = BR / E;   // 16-byte words per term (B R is even)
     const int G = kRBThreads / W;
     const int tid = threadIdx.x, g = tid / W, w = tid - g * W;
-    const int k = I.r0 / B;   // particle (block row) of this item
     using C = typename Arith<VT>::C;
     using T = typename Arith<VT>::T;
     __shared__ C partU[2 * kRBThreads], partW[2 * kRBThreads];
     __shared__ C red[kRBThreads / 32][R][2];
     if (g < G) {
-        const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
         const long long ns = s1 - s0;
         const OutT* cu = CU + pl.cu_off + (s0 - pl.strip_base) * (long long)BR + w * E;
         const OutT* cw = CW + pl.cw_off + ((long long)k * (k - 1) / 2) * BR + w * E;
@@ -1124,11 +1163,16 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
       VT* __restrict__ r0, VT* __restrict__ p, VT* __restrict__ v, VT* __restrict__ s, const VT* __restrict__ t,
       double2* __restrict__ dots, const SysPlan* __restrict__ plan = nullptr, ScalarFuse fz = ScalarFuse()) {
     const int it = blockIdx.x;
-    if (it >= nitems) return;
-    const Item I = items[it];
+    if (it >= nitems) {
+        pdl_wait();
+        return;
+    }
+    const Item I = items[it];   // prologue on plan data
+    const gb::SysDev S = sys[I.sys];
+    pdl_wait();
+    pdl_trigger();
     const int mask = (kind == 0) ? -1 : (kind == 4 ? 1 : 0);
     if (!any_active<R>(st, I.sys, mask)) return;
-    const gb::SysDev S = sys[I.sys];
     using C = typename Arith<VT>::C;
     using T = typename Arith<VT>::T;
     const T tg{};
@@ -1574,11 +1618,10 @@ int launch_pgemv_group(const Plan& P, const DevPlan& D, const StripGroup& grp, c
         if (smem > 48 * 1024)                                                                                    \
             GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));      \
         gb::note_launch();                                                                                       \
-        kfn<<<(unsigned)grid, kGemvThreads, smem, stream>>>(                                                     \
-            D.sys, D.strips, grp.beg, grp.end, st, mask, mat_hi, mat_lo, reinterpret_cast<const YT*>(Yu),         \
-            reinterpret_cast<const YT*>(Yw), reinterpret_cast<OutT*>(CU), reinterpret_cast<OutT*>(CW), D.sp, rr0, \
-            Bmax, err);                                                                                          \
-        GB_CUDA_TRY(cudaGetLastError());                                                                         \
+        GB_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(kGemvThreads), smem, stream, D.sys, D.strips,    \
+                               grp.beg, grp.end, st, mask, mat_hi, mat_lo, reinterpret_cast<const YT*>(Yu),        \
+                               reinterpret_cast<const YT*>(Yw), reinterpret_cast<OutT*>(CU),                      \
+                               reinterpret_cast<OutT*>(CW), D.sp, rr0, Bmax, err));                               \
         return GB_OK;                                                                                            \
     }
     GB_PG(8, 1) GB_PG(8, 2) GB_PG(8, 4) GB_PG(16, 3) GB_PG(16, 5) GB_PG(32, 3) GB_PG(32, 4) GB_PG(32, 5)
@@ -1636,34 +1679,34 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     int e = GB_OK;
     if (pol == 0) {
         gb::note_launch();
-        k_yprep<0, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), up);
+        GB_CUDA_TRY(launch_pdl(k_yprep<0, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st, mask,
+                               tvec, xin, reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), up));
         if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
-        k_reduce_blk<double2, VT, R><<<(unsigned)P.nr, kRBThreads, 0, stream>>>(
-            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
-            reinterpret_cast<const double2*>(CW), xin, yout, mode, aux, b128, dots, fz);
+        GB_CUDA_TRY(launch_pdl(k_reduce_blk<double2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
+                               D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
+                               reinterpret_cast<const double2*>(CW), xin, yout, mode, aux, b128, dots, fz));
     } else if (pol == 1) {
         gb::note_launch();
-        k_yprep<1, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up);
+        GB_CUDA_TRY(launch_pdl(k_yprep<1, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st, mask,
+                               tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
-        k_reduce_blk<float2, VT, R><<<(unsigned)P.nr, kRBThreads, 0, stream>>>(
-            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
-            reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz);
+        GB_CUDA_TRY(launch_pdl(k_reduce_blk<float2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
+                               D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
+                               reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz));
     } else {
         gb::note_launch();
-        k_yprep<2, VT, R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, st, mask, tvec, xin,
-                                                     reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up);
+        GB_CUDA_TRY(launch_pdl(k_yprep<2, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st, mask,
+                               tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
         if (P.nstrips) e = launch_df<R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
-        k_reduce_blk<float4, VT, R><<<(unsigned)P.nr, kRBThreads, 0, stream>>>(
-            D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float4*>(CU),
-            reinterpret_cast<const float4*>(CW), xin, yout, mode, aux, b128, dots, fz);
+        GB_CUDA_TRY(launch_pdl(k_reduce_blk<float4, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
+                               D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float4*>(CU),
+                               reinterpret_cast<const float4*>(CW), xin, yout, mode, aux, b128, dots, fz));
     }
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
@@ -1814,8 +1857,8 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             if (e) return e;
         }
         gb::note_launch();
-        k_vec<VT, R><<<vb, kVRows, 0, sm>>>(D.sys, D.vitems, P.nv, st, 3, nullptr, nullptr, x, r, r0, p, v, s, t, dots,
-                                            D.sp, fuse(3));
+        GB_CUDA_TRY(launch_pdl(k_vec<VT, R>, dim3(vb), dim3(kVRows), 0, sm, D.sys, D.vitems, P.nv, st, 3, nullptr,
+                               nullptr, x, r, r0, p, v, s, t, dots, D.sp, fuse(3)));
         GB_CUDA_TRY(cudaGetLastError());
         return GB_OK;
     };
