@@ -695,18 +695,88 @@ k_dense_gemv(int D, const double2* __restrict__ T, const double2* __restrict__ x
 }
 
 // ------------------------------------------------------------ K4 scalars --
+// Partial dot products of the vector kernels.  The FP64 solver sums double2 values.
+// The FP32 solver sums double-float complex values: every product exact (FMA
+// error term), TwoSum accumulation, all on the FP32 pipe.  BiCGSTAB's inner
+// products cancel heavily as it converges (rho = <r0, r> falls far below
+// |r0| |r|), which a plain FP32 sum cannot follow on ill-conditioned clusters.
+// Stored per (item, rhs, which) in the 16-byte slots of the dots buffer: double2,
+// or float4 (re.h, im.h, re.l, im.l).
+__device__ __forceinline__ void df_acc_prod(float& h, float& l, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float s = h + p;
+    const float bb = s - h;
+    const float err = (h - (s - bb)) + (p - bb);
+    h = s;
+    l += err + e;
+}
+template <typename T> struct DotAcc;
+template <> struct DotAcc<double> {
+    double2 s;
+    __device__ void zero() { s = make_double2(0, 0); }
+    __device__ void fma_conj(double2 a, double2 b) { cfma_conj(s, a, b); }
+    __device__ void add_norm2(double2 y) { s.x += y.x * y.x + y.y * y.y; }
+    __device__ void add(const DotAcc& o) { s = cadd(s, o.s); }
+    __device__ DotAcc shuffled(int off) const {
+        DotAcc r;
+        r.s = shfl_xor(s, off);
+        return r;
+    }
+    __device__ void store(double2* p) const { *p = s; }
+    __device__ void load_cg(const double2* p) { s = __ldcg(p); }
+    __device__ double2 value() const { return s; }
+};
+template <> struct DotAcc<float> {
+    float2 h, l;
+    __device__ void zero() { h = l = make_float2(0.f, 0.f); }
+    __device__ void fma_conj(float2 a, float2 b) {   // += conj(a) b
+        df_acc_prod(h.x, l.x, a.x, b.x);
+        df_acc_prod(h.x, l.x, a.y, b.y);
+        df_acc_prod(h.y, l.y, a.x, b.y);
+        df_acc_prod(h.y, l.y, -a.y, b.x);
+    }
+    __device__ void add_norm2(float2 y) {
+        df_acc_prod(h.x, l.x, y.x, y.x);
+        df_acc_prod(h.x, l.x, y.y, y.y);
+    }
+    __device__ void add(const DotAcc& o) {
+        df_add(h.x, l.x, o.h.x, o.l.x);
+        df_add(h.y, l.y, o.h.y, o.l.y);
+    }
+    __device__ DotAcc shuffled(int off) const {
+        DotAcc r;
+        r.h = shfl_xor(h, off);
+        r.l = shfl_xor(l, off);
+        return r;
+    }
+    __device__ void store(double2* p) const { *reinterpret_cast<float4*>(p) = make_float4(h.x, h.y, l.x, l.y); }
+    __device__ void load_cg(const double2* p) {
+        const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+        h = make_float2(v.x, v.y);
+        l = make_float2(v.z, v.w);
+    }
+    __device__ float2 value() const { return make_float2(h.x + l.x, h.y + l.y); }
+};
+
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
     const double den = b.x * b.x + b.y * b.y;
     return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
 }
+// FP32 complex division by Smith's method: no square of b's components, so the
+// FP32 scalars of large right-hand sides (|b|^2 beyond ~1e19) do not overflow.
 __device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
-    const float den = b.x * b.x + b.y * b.y;
-    return make_float2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+    if (fabsf(b.x) >= fabsf(b.y)) {
+        const float r = b.y / b.x, d = b.x + b.y * r;
+        return make_float2((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+    }
+    const float r = b.x / b.y, d = b.y + b.x * r;
+    return make_float2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
 }
 __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 __device__ __forceinline__ bool finite2(float2 a) { return isfinite(a.x) && isfinite(a.y); }
-__device__ __forceinline__ double tsqrt(double v) { return sqrt(v); }
-__device__ __forceinline__ float tsqrt(float v) { return sqrtf(v); }
+__device__ __forceinline__ double cabs_t(double2 v) { return sqrt(v.x * v.x + v.y * v.y); }
+__device__ __forceinline__ float cabs_t(float2 v) { return hypotf(v.x, v.y); }   // no overflow of the squares
 template <typename C> __device__ __forceinline__ C cmake(double re, double im) {
     C z;
     z.x = re;
@@ -784,7 +854,7 @@ __device__ void scalar_apply_t(KState& k, int phase, typename CplxT<T>::t d0, ty
         if (k.iters >= k.maxiter) { k.done = 1; k.status = GB_NOT_CONVERGED; return; }
         const C rho_old = rho;
         rho = d1;   // <r0, r>
-        if (tsqrt(rho.x * rho.x + rho.y * rho.y) < eps * eps * r0sq) {
+        if (cabs_t(rho) < eps * eps * r0sq) {
             if (k.restarts >= kMaxRestarts) { k.done = 1; k.status = GB_BREAKDOWN; return; }
             rho = rho_old;   // phase 4 recomputes rho from the fresh residual
             k.need_restart = 1;
@@ -814,23 +884,26 @@ __device__ __forceinline__ bool scalar_skips(const KState& k, int phase) {
 template <int R, typename T>
 __device__ void scalar_step(const SysPlan* __restrict__ plan, KState* __restrict__ st, int phase,
                             const double2* __restrict__ dots_raw, double tol, int maxiter, int sidx, int rr, int lane) {
-    using C = typename CplxT<T>::t;
-    const C* dots = reinterpret_cast<const C*>(dots_raw);
+    const double2* dots = dots_raw;
     KState& k = st[sidx * R + rr];
     if (scalar_skips(k, phase)) return;
     const SysPlan pl = plan[sidx];
     const bool vec = (phase == 0 || phase == 3);
     const int b0 = vec ? pl.vbeg : pl.rbeg, b1 = vec ? pl.vend : pl.rend;
-    C d0 = czero<C>(), d1 = czero<C>();
+    DotAcc<T> d0, d1, t;
+    d0.zero();
+    d1.zero();
     for (int it = b0 + lane; it < b1; it += 32) {
-        d0 = cadd(d0, __ldcg(dots + ((long long)it * R + rr) * 2 + 0));
-        d1 = cadd(d1, __ldcg(dots + ((long long)it * R + rr) * 2 + 1));
+        t.load_cg(dots + ((long long)it * R + rr) * 2 + 0);
+        d0.add(t);
+        t.load_cg(dots + ((long long)it * R + rr) * 2 + 1);
+        d1.add(t);
     }
     for (int o = 16; o > 0; o >>= 1) {
-        d0 = cadd(d0, shfl_xor(d0, o));
-        d1 = cadd(d1, shfl_xor(d1, o));
+        d0.add(d0.shuffled(o));
+        d1.add(d1.shuffled(o));
     }
-    if (lane == 0) scalar_apply<T>(k, phase, d0, d1, tol, maxiter);
+    if (lane == 0) scalar_apply<T>(k, phase, d0.value(), d1.value(), tol, maxiter);
 }
 
 template <int R, typename T>
@@ -861,10 +934,9 @@ struct ScalarFuse {
 template <int R, int NT, typename T>
 __device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict__ plan,
                                  const double2* __restrict__ dots_raw, int sys, int nitems_sys) {
-    using C = typename CplxT<T>::t;
-    const C* dots = reinterpret_cast<const C*>(dots_raw);
+    const double2* dots = dots_raw;
     __shared__ int s_last;
-    __shared__ C s_red[NT / 32][R][2];
+    __shared__ DotAcc<T> s_red[NT / 32][R][2];
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -883,14 +955,18 @@ __device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
-        C d0 = czero<C>(), d1 = czero<C>();
+        DotAcc<T> d0, d1, t;
+        d0.zero();
+        d1.zero();
         for (int it = b0 + (int)threadIdx.x; it < b1; it += NT) {
-            d0 = cadd(d0, __ldcg(dots + ((long long)it * R + rr) * 2 + 0));   // written by other CTAs
-            d1 = cadd(d1, __ldcg(dots + ((long long)it * R + rr) * 2 + 1));
+            t.load_cg(dots + ((long long)it * R + rr) * 2 + 0);   // written by other CTAs
+            d0.add(t);
+            t.load_cg(dots + ((long long)it * R + rr) * 2 + 1);
+            d1.add(t);
         }
         for (int o = 16; o > 0; o >>= 1) {
-            d0 = cadd(d0, shfl_xor(d0, o));
-            d1 = cadd(d1, shfl_xor(d1, o));
+            d0.add(d0.shuffled(o));
+            d1.add(d1.shuffled(o));
         }
         if (lane == 0) {
             s_red[wid][rr][0] = d0;
@@ -902,12 +978,14 @@ __device__ void fused_scalar_cta(const ScalarFuse& fz, const SysPlan* __restrict
         const int rr = threadIdx.x;
         KState& k = fz.st[sys * R + rr];
         if (scalar_skips(k, fz.phase)) return;
-        C d0 = czero<C>(), d1 = czero<C>();
+        DotAcc<T> d0, d1;
+        d0.zero();
+        d1.zero();
         for (int w = 0; w < NT / 32; w++) {
-            d0 = cadd(d0, s_red[w][rr][0]);
-            d1 = cadd(d1, s_red[w][rr][1]);
+            d0.add(s_red[w][rr][0]);
+            d1.add(s_red[w][rr][1]);
         }
-        scalar_apply<T>(k, fz.phase, d0, d1, fz.tol, fz.maxiter);
+        scalar_apply<T>(k, fz.phase, d0.value(), d1.value(), fz.tol, fz.maxiter);
     }
 }
 
@@ -1016,7 +1094,7 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
     using C = typename Arith<VT>::C;
     using T = typename Arith<VT>::T;
     __shared__ C partU[2 * kRBThreads], partW[2 * kRBThreads];
-    __shared__ C red[kRBThreads / 32][R][2];
+    __shared__ DotAcc<T> red[kRBThreads / 32][R][2];
     if (g < G) {
         const long long ns = s1 - s0;
         const OutT* cu = CU + pl.cu_off + (s0 - pl.strip_base) * (long long)BR + w * E;
@@ -1036,7 +1114,9 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
         }
     }
     __syncthreads();
-    C d0 = czero<C>(), d1 = czero<C>();
+    DotAcc<T> d0, d1;
+    d0.zero();
+    d1.zero();
     if (tid < BR) {
         const int r = tid / R, rr = tid - r * R;
         const int info = __ldg(S.rowinfo + r);
@@ -1056,12 +1136,12 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
             y[e] = yo;
             const C yq = to_c<C>(yo);   // dots of the stored (rounded) vector
             if (mode == 1) {
-                cfma_conj(d0, to_c<C>(aux[e]), yq);
+                d0.fma_conj(to_c<C>(aux[e]), yq);
             } else if (mode == 2) {
-                d0.x += yq.x * yq.x + yq.y * yq.y;
-                cfma_conj(d1, yq, to_c<C>(aux[e]));
+                d0.add_norm2(yq);
+                d1.fma_conj(yq, to_c<C>(aux[e]));
             } else if (mode == 3) {
-                d0.x += yq.x * yq.x + yq.y * yq.y;
+                d0.add_norm2(yq);
             }
         }
     }
@@ -1072,8 +1152,8 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
     const int lane = tid & 31, wid = tid >> 5, nw = (BR + 31) / 32;
 #pragma unroll
     for (int o = 16; o >= R; o >>= 1) {
-        d0 = cadd(d0, shfl_xor(d0, o));
-        d1 = cadd(d1, shfl_xor(d1, o));
+        d0.add(d0.shuffled(o));
+        d1.add(d1.shuffled(o));
     }
     if (lane < R && wid < nw) {
         red[wid][lane][0] = d0;
@@ -1081,14 +1161,15 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
     }
     __syncthreads();
     if (tid < R) {
-        C s0 = czero<C>(), s1 = czero<C>();
+        DotAcc<T> s0, s1;
+        s0.zero();
+        s1.zero();
         for (int q = 0; q < nw; q++) {
-            s0 = cadd(s0, red[q][tid][0]);
-            s1 = cadd(s1, red[q][tid][1]);
+            s0.add(red[q][tid][0]);
+            s1.add(red[q][tid][1]);
         }
-        C* dc = reinterpret_cast<C*>(dots);
-        dc[((long long)it * R + tid) * 2 + 0] = s0;
-        dc[((long long)it * R + tid) * 2 + 1] = s1;
+        s0.store(dots + ((long long)it * R + tid) * 2 + 0);
+        s1.store(dots + ((long long)it * R + tid) * 2 + 1);
         __threadfence();
     }
     if (fz.st) fused_scalar_cta<R, kRBThreads, T>(fz, plan, dots, I.sys, pl.rend - pl.rbeg);
@@ -1176,11 +1257,14 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     using C = typename Arith<VT>::C;
     using T = typename Arith<VT>::T;
     const T tg{};
-    __shared__ C red[kVRows / 32][R][2];
+    __shared__ DotAcc<T> red[kVRows / 32][R][2];
     const int lr = threadIdx.x;
-    C d0[R], d1[R];
+    DotAcc<T> d0[R], d1[R];
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) d0[rr] = d1[rr] = czero<C>();
+    for (int rr = 0; rr < R; rr++) {
+        d0[rr].zero();
+        d1[rr].zero();
+    }
     if (lr < I.nr) {
         const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
 #pragma unroll
@@ -1194,8 +1278,7 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
                 x[e] = z; p[e] = z; v[e] = z;
                 r[e] = bq; r0[e] = bq;
                 if (bx && b) bx[e] = bq;
-                const C bd = to_c<C>(bq);
-                d0[rr].x += bd.x * bd.x + bd.y * bd.y;
+                d0[rr].add_norm2(to_c<C>(bq));
             } else if (kind == 1) {
                 const C rv = to_c<C>(r[e]), pv = to_c<C>(p[e]), vv = to_c<C>(v[e]);
                 const C bt = cmul(ks_beta(k, tg), csub(pv, cmul(ks_omega(k, tg), vv)));
@@ -1210,8 +1293,8 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
                 const VT rq = from_c<VT>(csub(sv, wt));
                 r[e] = rq;
                 const C rd = to_c<C>(rq), r0v = to_c<C>(r0[e]);
-                d0[rr].x += rd.x * rd.x + rd.y * rd.y;
-                cfma_conj(d1[rr], r0v, rd);
+                d0[rr].add_norm2(rd);
+                d1[rr].fma_conj(r0v, rd);
             } else if (kind == 4) {
                 r0[e] = r[e];
             }
@@ -1222,8 +1305,8 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
         for (int o = 16; o > 0; o >>= 1) {
-            d0[rr] = cadd(d0[rr], shfl_xor(d0[rr], o));
-            d1[rr] = cadd(d1[rr], shfl_xor(d1[rr], o));
+            d0[rr].add(d0[rr].shuffled(o));
+            d1[rr].add(d1[rr].shuffled(o));
         }
         if (lane == 0) {
             red[wid][rr][0] = d0[rr];
@@ -1233,9 +1316,10 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
     __syncthreads();
     if (lr < R * 2) {
         const int rr = lr >> 1, which = lr & 1;
-        C sm = czero<C>();
-        for (int w = 0; w < kVRows / 32; w++) sm = cadd(sm, red[w][rr][which]);
-        reinterpret_cast<C*>(dots)[((long long)it * R + rr) * 2 + which] = sm;
+        DotAcc<T> sm;
+        sm.zero();
+        for (int w = 0; w < kVRows / 32; w++) sm.add(red[w][rr][which]);
+        sm.store(dots + ((long long)it * R + rr) * 2 + which);
     }
     if (fz.st) {
         if (lr < R * 2) __threadfence();   // this thread's partial before the arrival count
@@ -1256,11 +1340,13 @@ __global__ void k_refine_axpy(const gb::SysDev* __restrict__ sys, const Item* __
     if (lr >= I.nr) return;
     const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
     for (int rr = 0; rr < R; rr++) {
-        if (ost[I.sys * R + rr].done) continue;
+        const KState& k = ost[I.sys * R + rr];
+        if (k.done) continue;
+        const double sc = sqrt(k.rsq);   // the inner solve ran on r / |r| (k_cast_f)
         const float2 dv = d[vo + rr];
         double2 xv = x128[vo + rr];
-        xv.x += (double)dv.x;
-        xv.y += (double)dv.y;
+        xv.x += sc * (double)dv.x;
+        xv.y += sc * (double)dv.y;
         x128[vo + rr] = xv;
     }
 }
@@ -1362,7 +1448,10 @@ __global__ void k_copy_out(const gb::SysDev* __restrict__ sys, const Item* __res
     for (int rr = 0; rr < R; rr++) dst[vo + rr] = to_d2(src[vo + rr]);
 }
 
-// dst (FP32) = src (FP64), zero for clusters the mask marks done
+// dst (FP32) = src (FP64), zero for clusters the mask marks done.  With the outer
+// (refinement) state as mask, src is the residual r and dst = r / |r|: each inner
+// FP32 solve sees a unit right-hand side, whatever the source amplitude, and
+// k_refine_axpy scales its correction back by |r|.
 __global__ void k_cast_f(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, int R,
                          const double2* __restrict__ src, float2* __restrict__ dst, const KState* __restrict__ mask) {
     const int it = blockIdx.x;
@@ -1375,7 +1464,8 @@ __global__ void k_cast_f(const gb::SysDev* __restrict__ sys, const Item* __restr
     for (int rr = 0; rr < R; rr++) {
         const double2 v = src[vo + rr];
         const bool off = mask && mask[I.sys * R + rr].done;
-        dst[vo + rr] = off ? make_float2(0.f, 0.f) : make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+        const double sc = mask ? 1.0 / sqrt(mask[I.sys * R + rr].rsq) : 1.0;
+        dst[vo + rr] = off ? make_float2(0.f, 0.f) : make_float2(__double2float_rn(v.x * sc), __double2float_rn(v.y * sc));
     }
 }
 

@@ -237,3 +237,21 @@ def test_nan_right_hand_side_reported_per_cluster(precision):
     b.solve(tol=1e-8)
     assert b.status[0] == nat.GB_OK
     assert b.status[1] == nat.GB_NAN
+
+
+@pytest.mark.gpu
+def test_ill_conditioned_lmax8_beam_request_converges():
+    """Request 16 of the serving stream (seed 4): N=40, lmax 8, Gaussian beam, a
+    system on which FP32 BiCGSTAB stalls unless its inner products are accumulated
+    beyond FP32 (they cancel as the residual falls).  Mixed must converge and give
+    C_ext within 1e-6 of FP64."""
+    rng = np.random.default_rng(4)
+    reqs = [SV.random_request(rng, rid=i) for i in range(17)]
+    r = reqs[16]
+    assert (len(r.radius), r.lmax) == (40, 8)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        with SV.SolveServer(precision=prec, tol=1e-8, max_waves=1, max_wave_requests=1) as srv:
+            out[prec] = srv.submit(r).result()
+    assert out["mixed"].status == 0 and out["fp64"].status == 0
+    assert abs(out["mixed"].C_ext - out["fp64"].C_ext) / abs(out["fp64"].C_ext) < 1e-6
