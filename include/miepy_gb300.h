@@ -80,6 +80,16 @@ int gb_tables_export(int lmax, int* nmvu, int* qab, double* cA, double* cB, int*
 int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* mie, double k,
                              double* out, void* stream);
 
+/* Reflection matrix of a planar interface at height z, in the reference layout:
+ * replaces reflection_matrix_nia, cpp/src/interactions.cpp:464-512.  Block (i, j)
+ * for every particle pair, the particle itself included: the outgoing translation
+ * from particle j to the mirror image of particle i, times -r (-1)^(m+n+a+1) and the
+ * Mie coefficient of particle j; r = r_re + i r_im is the normal-incidence
+ * reflection coefficient.  The reference subtracts it from the aggregate T-matrix
+ * (sphere_cluster.py:704-710).  pos [N,3] f64, mie [N,2,lmax] c128, out [D,D] c128. */
+int gb_reflection_matrix_dense(int N, int lmax, const double* pos, const double* mie, double k, double r_re,
+                               double r_im, double z, double* out, void* stream);
+
 /* Packed pair-block translation matrix of one cluster (see above).  Any
  * output may be NULL: out128 [P*B*B] c128; out64 [P*B*B] c64 = fl32(a);
  * out64lo [P*B*B] c64 = fl32(a - fl32(a)) (hi + lo carries ~48 bits). */

@@ -10,6 +10,7 @@ include/miepy_gb300.h.
 from . import backend, beams, materials as _materials_mod, sources, sweep
 from .beams import gaussian_beam
 from .cluster import cross_sections, solver, sphere_cluster
+from .interface import interface
 from .engine import ClusterBatch, footprint_bytes
 from .materials import (constant_material, dielectric, drude_material, function_material, material_struct,
                         materials)

@@ -102,6 +102,27 @@ def sphere_aggregate_tmatrix_jax(positions, mie, k):
     return DeviceAggregateTMatrix(positions, mie, k)
 
 
+def reflection_matrix_nia(positions, mie, k, reflected, z):
+    """positions [N,3], mie [N,2,lmax], k, reflection coefficient, interface height z ->
+    R [N,2,rmax,N,2,rmax] c128 (interactions.py:208-225 / interactions.cpp:464-512),
+    computed on the GPU by gb_reflection_matrix_dense."""
+    dev = require_cuda()
+    pos = np.ascontiguousarray(np.asarray(positions, dtype=float).reshape(-1, 3))
+    N = pos.shape[0]
+    mie = np.ascontiguousarray(np.asarray(mie, dtype=complex).reshape(N, -1))
+    lmax = mie.shape[1] // 2
+    rmax = lmax_to_rmax(lmax)
+    D = 2 * rmax * N
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_mie = torch.from_numpy(mie).to(dev)
+    out = torch.empty(D * D, dtype=torch.complex128, device=dev)
+    r = complex(reflected)
+    nat.check(nat.lib().gb_reflection_matrix_dense(N, lmax, nat.ptr(d_pos), nat.ptr(d_mie), float(np.real(k)), r.real,
+                                                   r.imag, float(z), nat.ptr(out), current_stream(dev)),
+              "reflection matrix")
+    return out.cpu().numpy().reshape(N, 2, rmax, N, 2, rmax)
+
+
 def solve_linear_system_jax(agg_tmatrix, p_src, method):
     """Solve p_inc = (I + T)^-1 p_src; returns numpy [N, 2, rmax]."""
     require_cuda()

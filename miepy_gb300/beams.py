@@ -148,6 +148,11 @@ class gaussian_beam:
         out._beam_inputs = (d_pos, d_rhat, d_w)
         return out
 
+    def reflect(self, interface, medium, wavelength):
+        """The reference reflects a beam by rotating its far field (beams.py:202-203,
+        323-360), which needs Wigner-D rotations (the ``spherical`` package)."""
+        raise NotImplementedError("reflected Gaussian beams need Wigner-D rotations; use a plane wave with interface=")
+
     def structure(self, position, k, lmax):
         """p_src [N, 2, rmax] (host numpy), computed on the GPU."""
         N = np.asarray(position, float).reshape(-1, 3).shape[0]

@@ -65,8 +65,6 @@ class sphere_cluster:
                  maxiter=None, device=None):
         if symmetry is not None:
             raise NotImplementedError("periodic symmetry is not on the GPU path yet")
-        if interface is not None:
-            raise NotImplementedError("substrate interfaces are not on the GPU path yet")
         self.position = np.asarray(np.atleast_2d(position), dtype=float)
         N = self.position.shape[0]
         self.radius = _atleast(radius, N, float)
@@ -135,12 +133,17 @@ class sphere_cluster:
         if wavelength is not None or source is not None:
             raise NotImplementedError("re-solving at a new wavelength/source: build a new cluster")
         self.p_src[...] = self.source.structure(self.position, self.material_data.k_b, self.lmax)
+        if self.interface is not None:   # sphere_cluster.py:683-685
+            reflected = self.source.reflect(self.interface, self.medium, self.wavelength)
+            self.p_src += reflected.structure(self.position, self.material_data.k_b, self.lmax)
         md = self.material_data
         spec = dict(position=self.position, mie_scat=self.mie_scat, mie_int=self.mie_int, k=float(np.real(md.k_b)),
                     p_src=self.p_src)
         prec = self.precision if self.interactions else "fp64"
         b = ClusterBatch([spec], R=1, precision=prec, device=self.device)
-        if self.interactions and self.Nparticles > 1:
+        if self.interactions and self.interface is not None:
+            self._solve_with_interface(b)
+        elif self.interactions and self.Nparticles > 1:
             b.assemble()
             b.solve(tol=self._tolerance(), maxiter=self.maxiter or DEFAULT_MAXITER,
                     inner_tol=min(1e-6, max(self._tolerance(), 1e-7)), max_refine=8)
@@ -165,6 +168,44 @@ class sphere_cluster:
         self._F = b.F[: self.Nparticles * 3].view(self.Nparticles, 3).cpu().numpy()
         self._T = b.T[: self.Nparticles * 3].view(self.Nparticles, 3).cpu().numpy()
         self._F_nosrc = self._T_nosrc = None
+
+    def _solve_with_interface(self, b):
+        """(I + T_agg - R) p_inc = p_src on the dense reference layout: the aggregate
+        T-matrix (gb_assemble_sphere_dense) minus the interface's reflection matrix
+        (gb_reflection_matrix_dense), as sphere_cluster.py:694-712; BiCGSTAB
+        (gb_solve_dense) or, for solver.exact, an LU solve."""
+        L = nat.lib()
+        dev, st = b.device, current_stream(b.device)
+        md = self.material_data
+        N, D = self.Nparticles, 2 * self.rmax * self.Nparticles
+        k = float(np.real(md.k_b))
+        nat.check(L.gb_expand_mie_batch(b.nsys, b.sys, b.mie_off.ctypes.data, nat.ptr(b.mie_scat), nat.ptr(b.tvec),
+                                        st), "expand mie")
+        T = torch.empty(D * D, dtype=torch.complex128, device=dev)
+        nat.check(L.gb_assemble_sphere_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k, nat.ptr(T), st),
+                  "dense assembly")
+        Rm = torch.empty_like(T)
+        r0 = complex(self.interface.reflection_coefficients(0, self.wavelength, self.medium)[0])
+        nat.check(L.gb_reflection_matrix_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k, r0.real, r0.imag,
+                                               float(self.interface.z), nat.ptr(Rm), st), "reflection matrix")
+        T -= Rm
+        del Rm
+        if _method_is_exact(self.method):
+            A = T.view(D, D) + torch.eye(D, dtype=torch.complex128, device=dev)
+            b.x.copy_(torch.linalg.solve(A, b.b[:D]))
+            self.solver_status, self.solver_iterations, self.solver_residual = 0, 0, 0.0
+            return
+        need = L.gb_solve_dense_workspace_size(D, 1)
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        status = np.zeros(1, np.int32)
+        iters = np.zeros(1, np.int32)
+        resid = np.zeros(1)
+        rc = L.gb_solve_dense(D, 1, nat.ptr(T), nat.ptr(b.b), nat.ptr(b.x), self._tolerance(),
+                              int(self.maxiter or DEFAULT_MAXITER), nat.ptr(ws), ws.numel(), status.ctypes.data,
+                              iters.ctypes.data, resid.ctypes.data, st)
+        if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN):
+            nat.check(rc, "dense solve")
+        self.solver_status, self.solver_iterations, self.solver_residual = int(status[0]), int(iters[0]), float(resid[0])
 
     def update_position(self, position):
         self.position = np.asarray(np.atleast_2d(position), dtype=float)
@@ -314,8 +355,11 @@ class sphere_cluster:
                 (z - self.position[i, 2]) ** 2 < self.radius[i] ** 2
         if source:
             k = md.k_b
-            S = self.source.H_field(x, y, z, k) * (md.eps_b / md.mu_b) ** 0.5 if magnetic else \
-                self.source.E_field(x, y, z, k)
+            srcs = [self.source]
+            if self.interface is not None:   # sphere_cluster.py:279-283, 355-361
+                srcs.append(self.source.reflect(self.interface, self.medium, self.wavelength))
+            S = sum(s.H_field(x, y, z, k) * (md.eps_b / md.mu_b) ** 0.5 if magnetic else s.E_field(x, y, z, k)
+                    for s in srcs)
             if use_int:
                 S = np.where(inside[None], 0.0, S)
             E = E + S

@@ -2,23 +2,23 @@
 // cpp/src/interactions.cpp:370-415, and vsh_translation_insert_pair (Mie overload),
 // cpp/src/vsh_translation.cpp:161-237).
 //
-// One CTA per particle pair (grid-stride over all pairs of all clusters of a
-// batch).  Per pair, in shared memory:
+// One CTA per group of PB particle pairs (grid-stride over the groups of all
+// clusters of a batch).  Per group, in shared memory:
 //   1. h_p(kr) by the upward j/y recurrence of spherical_hn_recursion
-//      (cpp/src/special.cpp:90-111), one thread; P_p^mu(cos theta) (no
+//      (cpp/src/special.cpp:90-111), one thread per pair; P_p^mu(cos theta) (no
 //      Condon-Shortley phase, GSL_SF_LEGENDRE_NONE convention), one thread per
-//      order mu; e^{i mu phi} by powering e^{i phi}, one thread per mu.  The angles
-//      enter only through cos/sin of theta and phi, taken directly from the
-//      separation vector: no acos/atan2/sincos of angles on the (slow) FP64 pipe;
-//   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p);
+//      (pair, mu); e^{i mu phi} by powering e^{i phi}.  The angles enter only
+//      through cos/sin of theta and phi, taken directly from the separation vector;
+//   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p) (FP64, or for the
+//      mixed path double-float on the FP32 pipe, with h_p from FP64);
+// then per pair, software-pipelined over the group:
 //   3. one thread per canonical tuple: A_t, B_t as real x complex FMA sums over
 //      the per-lmax coefficient table (tables.cu);
 //   4. coalesced block write: every entry of the B x B block looks up its tuple and
 //      sign in the element map.  Packed output writes the (i, j) block only, without
-//      Mie factors, in complex128 and/or complex64 (sign flips are bit operations,
-//      the complex64 copy is rounded once per tuple).  Dense output writes the (i, j)
-//      and (j, i) blocks of the reference's D x D matrix with the Mie factors of the
-//      column particle.
+//      Mie factors, in complex128 and/or complex64 hi / lo (sign flips are bit
+//      operations).  Dense output writes the (i, j) and (j, i) blocks of the
+//      reference's D x D matrix with the Mie factors of the column particle.
 
 #include <algorithm>
 #include <vector>
@@ -38,7 +38,7 @@ __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
 
 // Shared-memory layout of one CTA: the special functions of a group of PB pairs
 // (launch-wide strides PM = 2 Lmax + 2 orders, MU = 4 Lmax + 1 azimuthal orders),
-// then the tuple values of the pair being written.
+// then the tuple values of two pairs (the one being written and the next).
 struct AsmSmem {
     int PM, MU, M, PB;
     size_t off_geo, off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
@@ -57,9 +57,9 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_su
     s.off_e = take(sizeof(double2) * s.MU * PB);
     s.off_P = take(sizeof(double) * s.PM * s.PM * PB);
     s.off_G = take(16 * (size_t)s.PM * s.MU * PB);          // double2 (FP64 sums) or float4 (double-float)
-    s.off_T = take(fp64_sums ? sizeof(double2) * 2 * M : 0);
-    s.off_Tf = take(want64 ? sizeof(float2) * 2 * M : 0);
-    s.off_Tl = take(want64 ? sizeof(float2) * 2 * M : 0);
+    s.off_T = take(fp64_sums ? sizeof(double2) * 4 * M : 0);   // two buffers of (A, B) per tuple
+    s.off_Tf = take(want64 ? sizeof(float2) * 4 * M : 0);
+    s.off_Tl = take(want64 ? sizeof(float2) * 4 * M : 0);
     s.total = o;
     return s;
 }
@@ -100,6 +100,57 @@ __device__ __forceinline__ void df_rc_fma(float2& sh, float2& sl, float2 c, floa
     sl = __fadd2_rn(sl, __fadd2_rn(err, e));
 }
 
+// ------------------------------------------------------------ double-float --
+// Double-float (h + l, |l| <= ulp(h)/2) arithmetic on the FP32 pipe for the
+// special functions of the mixed path (GB300 issues an FP64 warp instruction about
+// once per 64 cycles per SM sub-partition).  Products by the FMA error term,
+// sums by TwoSum (Joldes, Muller, Popescu, ACM TOMS 44 (2017): DWTimesDW1 and
+// AccurateDWPlusDW), relative error a few 2^-48.
+struct DF { float h, l; };
+struct DFC { DF re, im; };
+__device__ __forceinline__ DF fast2sum(float a, float b) {
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF two_sum(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return DF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF df_of(double v) {   // FP64 -> double-float (2 conversions, 1 subtraction)
+    const float h = __double2float_rn(v);
+    return DF{h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    DF s = two_sum(a.h, b.h);
+    const DF t = two_sum(a.l, b.l);
+    s = fast2sum(s.h, s.l + t.h);
+    return fast2sum(s.h, s.l + t.l);
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return fast2sum(p, e);
+}
+__device__ __forceinline__ DF df_mulf(DF a, float b) {   // by a float (small integers are exact)
+    const float p = a.h * b;
+    float e = fmaf(a.h, b, -p);
+    e = fmaf(a.l, b, e);
+    return fast2sum(p, e);
+}
+__device__ __forceinline__ DF df_divf(DF a, float b) {   // by a float: the remainder of a rounded quotient is exact
+    const float q1 = a.h / b;
+    const float r = fmaf(-q1, b, a.h) + a.l;
+    return fast2sum(q1, r / b);
+}
+__device__ __forceinline__ DFC dfc_mul(DFC a, DFC b) {
+    return DFC{df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+__device__ __forceinline__ float4 dfc_pack(DFC z) { return make_float4(z.re.h, z.im.h, z.re.l, z.im.l); }
+__device__ __forceinline__ DFC dfc_unpack(float4 v) { return DFC{DF{v.x, v.z}, DF{v.y, v.w}}; }
+
 __device__ __forceinline__ int find_sys(const long long* base, int nsys, long long g) {
     int lo = 0, hi = nsys - 1;
     while (lo < hi) {
@@ -110,13 +161,24 @@ __device__ __forceinline__ int find_sys(const long long* base, int nsys, long lo
     return lo;
 }
 
+// Planar interface at height z with normal-incidence reflection coefficient r0
+// (the reflection matrix of interactions.cpp:464-512): pairs run over all (i, j),
+// the translation goes from particle j to the mirror image of particle i.
+struct Refl {
+    double z = 0;
+    double2 r0 = {0, 0};
+};
+
 // FP64_SUMS: tuple sums in FP64 (complex128 or dense output); otherwise in
 // double-float on the FP32 pipes, straight to the complex64 hi / lo outputs.
-template <bool DENSE, bool FP64_SUMS>
-__global__ void __launch_bounds__(kAsmThreads)
+// REFL: the dense reflection matrix instead of the aggregate T-matrix.
+template <bool DENSE, bool FP64_SUMS, bool REFL = false>
+__global__ void __launch_bounds__(kAsmThreads, 3)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
            int Lmax, int Mmax, int PB, const double* __restrict__ pos, const double2* __restrict__ mie,
-           double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld) {
+           double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
+           Refl refl = Refl()) {
+    static_assert(!REFL || (DENSE && FP64_SUMS), "the reflection matrix is a dense FP64 output");
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
@@ -137,7 +199,8 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         const int L = S.lmax, B = S.B, N = S.N;
         const int PM = 2 * L + 2, MU = 4 * L + 1;
         const long long p_first = (g - grp_base[s]) * (long long)PB;
-        const int np = (int)min((long long)PB, S.P - p_first);
+        const long long Ptot = REFL ? (long long)N * N : S.P;   // all ordered pairs for the reflection
+        const int np = (int)min((long long)PB, Ptot - p_first);
 
         // ---- phase 1a: one thread per pair: geometry, then h_p(kr) by the upward
         // j/y recurrence of spherical_hn_recursion (cpp/src/special.cpp:90-111).  The
@@ -145,10 +208,16 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // separation vector (the reference goes through acos/atan2 and back).
         if (tid < np) {
             int i, j;
-            pair_ij(p_first + tid, N, i, j);
+            if (REFL) {
+                i = (int)((p_first + tid) / N);
+                j = (int)((p_first + tid) % N);
+            } else {
+                pair_ij(p_first + tid, N, i, j);
+            }
             const double* pi_ = pos + S.pos_off + 3 * (long long)i;
             const double* pj_ = pos + S.pos_off + 3 * (long long)j;
-            const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
+            const double zi = REFL ? 2.0 * refl.z - pi_[2] : pi_[2];   // mirror image of particle i
+            const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = zi - pj_[2];
             const double rho2 = dx * dx + dy * dy;
             const double rad = sqrt(rho2 + dz * dz);
             const double inv_r = 1.0 / rad;
@@ -183,72 +252,134 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         }
         __syncthreads();
         // ---- phase 1b: P_q^mu(cos theta) (no Condon-Shortley phase), one thread per
-        // (pair, mu); e^{i mu phi} by binary powering, one thread per (pair, mu >= 0)
-        for (int it = tid; it < np * PM; it += kAsmThreads) {
-            const int pp = it / PM, mu = it % PM;
-            const double x = geo[8 * pp], u = geo[8 * pp + 1];
-            double* P = Pl + (size_t)PMs * PMs * pp;
-            double pmm = 1.0;
-            for (int kk = 1; kk <= mu; kk++) pmm *= (2 * kk - 1) * u;
-            P[mu * PMs + mu] = pmm;
-            if (mu + 1 < PM) {
-                double pa = pmm, pb = x * (2 * mu + 1) * pmm;
-                P[(mu + 1) * PMs + mu] = pb;
-                for (int q = mu + 2; q < PM; q++) {
-                    const double pc = ((2 * q - 1) * x * pb - (q + mu - 1) * pa) * c_inv_int[q - mu];
-                    P[q * PMs + mu] = pc;
-                    pa = pb;
-                    pb = pc;
+        // (pair, mu); e^{i mu phi} by binary powering, one thread per (pair, mu >= 0).
+        // The mixed path computes both in double-float on the FP32 pipe and turns
+        // h_q into double-float in place; the FP64 path keeps FP64.
+        if constexpr (FP64_SUMS) {
+            for (int it = tid; it < np * PM; it += kAsmThreads) {
+                const int pp = it / PM, mu = it % PM;
+                const double x = geo[8 * pp], u = geo[8 * pp + 1];
+                double* P = Pl + (size_t)PMs * PMs * pp;
+                double pmm = 1.0;
+                for (int kk = 1; kk <= mu; kk++) pmm *= (2 * kk - 1) * u;
+                P[mu * PMs + mu] = pmm;
+                if (mu + 1 < PM) {
+                    double pa = pmm, pb = x * (2 * mu + 1) * pmm;
+                    P[(mu + 1) * PMs + mu] = pb;
+                    for (int q = mu + 2; q < PM; q++) {
+                        const double pc = ((2 * q - 1) * x * pb - (q + mu - 1) * pa) * c_inv_int[q - mu];
+                        P[q * PMs + mu] = pc;
+                        pa = pb;
+                        pb = pc;
+                    }
                 }
             }
-        }
-        for (int it = tid; it < np * (2 * L + 1); it += kAsmThreads) {
-            const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
-            int e = mu;
-            double2 acc = make_double2(1.0, 0.0), base = make_double2(geo[8 * pp + 2], geo[8 * pp + 3]);
-            while (e) {
-                if (e & 1) acc = cmul(acc, base);
-                base = cmul(base, base);
-                e >>= 1;
+            for (int it = tid; it < np * (2 * L + 1); it += kAsmThreads) {
+                const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
+                int e = mu;
+                double2 acc = make_double2(1.0, 0.0), base = make_double2(geo[8 * pp + 2], geo[8 * pp + 3]);
+                while (e) {
+                    if (e & 1) acc = cmul(acc, base);
+                    base = cmul(base, base);
+                    e >>= 1;
+                }
+                eph[MUs * pp + 2 * L + mu] = acc;
+                eph[MUs * pp + 2 * L - mu] = make_double2(acc.x, -acc.y);
             }
-            eph[MUs * pp + 2 * L + mu] = acc;
-            eph[MUs * pp + 2 * L - mu] = make_double2(acc.x, -acc.y);
+        } else {
+            float2* P2 = reinterpret_cast<float2*>(Pl);      // same slots, (h, l)
+            float4* eph2 = reinterpret_cast<float4*>(eph);   // same slots, (re.h, im.h, re.l, im.l)
+            float4* hh2 = reinterpret_cast<float4*>(hh);
+            for (int it = tid; it < np * PM; it += kAsmThreads) {
+                const int pp = it / PM, mu = it % PM;
+                const DF x = df_of(geo[8 * pp]), u = df_of(geo[8 * pp + 1]);
+                float2* P = P2 + (size_t)PMs * PMs * pp;
+                DF pmm{1.f, 0.f};
+                for (int kk = 1; kk <= mu; kk++) pmm = df_mulf(df_mul(pmm, u), (float)(2 * kk - 1));
+                P[mu * PMs + mu] = make_float2(pmm.h, pmm.l);
+                if (mu + 1 < PM) {
+                    DF pa = pmm, pb = df_mulf(df_mul(x, pmm), (float)(2 * mu + 1));
+                    P[(mu + 1) * PMs + mu] = make_float2(pb.h, pb.l);
+                    for (int q = mu + 2; q < PM; q++) {
+                        const DF t = df_add(df_mulf(df_mul(x, pb), (float)(2 * q - 1)), df_neg(df_mulf(pa, (float)(q + mu - 1))));
+                        const DF pc = df_divf(t, (float)(q - mu));
+                        P[q * PMs + mu] = make_float2(pc.h, pc.l);
+                        pa = pb;
+                        pb = pc;
+                    }
+                }
+            }
+            for (int it = tid; it < np * (2 * L + 1); it += kAsmThreads) {
+                const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
+                int e = mu;
+                DFC acc{DF{1.f, 0.f}, DF{0.f, 0.f}}, base{df_of(geo[8 * pp + 2]), df_of(geo[8 * pp + 3])};
+                while (e) {
+                    if (e & 1) acc = dfc_mul(acc, base);
+                    base = dfc_mul(base, base);
+                    e >>= 1;
+                }
+                eph2[MUs * pp + 2 * L + mu] = dfc_pack(acc);
+                eph2[MUs * pp + 2 * L - mu] = dfc_pack(DFC{acc.re, df_neg(acc.im)});
+            }
+            for (int it = tid; it < np * PM; it += kAsmThreads) {   // each thread rewrites its own slot
+                const int pp = it / PM, q = it % PM;
+                const double2 hv = hh[PMs * pp + q];
+                hh2[PMs * pp + q] = dfc_pack(DFC{df_of(hv.x), df_of(hv.y)});
+            }
         }
         __syncthreads();
         // ---- phase 1c: G[p][mu] = P_p^mu h_p e^{i mu phi} (negative mu through the
-        // (-1)^mu (p-mu)!/(p+mu)! ratio), FP64 or split into double-float
+        // (-1)^mu (p-mu)!/(p+mu)! ratio), FP64, or double-float for the mixed path
+        // (the ratio as a double-float mantissa and an exact binary scaling)
         for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
             const int pp = it / (PM * MU), rem = it % (PM * MU);
             const int q = rem / MU, mi = rem % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
-            double2 gval = make_double2(0.0, 0.0);
-            if (am <= q) {
-                double P = Pl[(size_t)PMs * PMs * pp + q * PMs + am];
-                if (mu < 0) P *= S.neg_ratio[q * PM + am];
-                const double2 he = cmul(hh[PMs * pp + q], eph[MUs * pp + mi]);
-                gval = make_double2(P * he.x, P * he.y);
-            }
             const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
-            if (FP64_SUMS) {
+            if constexpr (FP64_SUMS) {
+                double2 gval = make_double2(0.0, 0.0);
+                if (am <= q) {
+                    double P = Pl[(size_t)PMs * PMs * pp + q * PMs + am];
+                    if (mu < 0) P *= S.neg_ratio[q * PM + am];
+                    const double2 he = cmul(hh[PMs * pp + q], eph[MUs * pp + mi]);
+                    gval = make_double2(P * he.x, P * he.y);
+                }
                 G64[gi] = gval;
             } else {
-                const float hx = __double2float_rn(gval.x), hy = __double2float_rn(gval.y);
-                G32[gi] = make_float4(hx, hy, __double2float_rn(gval.x - (double)hx),
-                                      __double2float_rn(gval.y - (double)hy));
+                float4 gval = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (am <= q) {
+                    const float2 pv = reinterpret_cast<const float2*>(Pl)[(size_t)PMs * PMs * pp + q * PMs + am];
+                    DF P{pv.x, pv.y};
+                    if (mu < 0) {
+                        const float4 r = S.neg_ratio2[q * PM + am];
+                        P = df_mul(P, DF{r.x, r.y});
+                        const int ex = (int)r.z;
+                        P = DF{ldexpf(P.h, ex), ldexpf(P.l, ex)};
+                    }
+                    const DFC he = dfc_mul(dfc_unpack(reinterpret_cast<const float4*>(hh)[PMs * pp + q]),
+                                           dfc_unpack(reinterpret_cast<const float4*>(eph)[MUs * pp + mi]));
+                    gval = dfc_pack(DFC{df_mul(P, he.re), df_mul(P, he.im)});
+                }
+                G32[gi] = gval;
             }
         }
         __syncthreads();
 
-        for (int pp = 0; pp < np; pp++) {
-            const long long p = p_first + pp;
+        // ---- phases 2 and 3, software-pipelined over the group's pairs: each thread
+        // writes pair pp's block (phase 3) and then forms the tuple values of pair
+        // pp + 1 (phase 2) into the other buffer, one barrier per pair.
+        const int Mb = lay.M;   // tuple-buffer stride (launch-wide)
+        auto tuples = [&](int pp, int buf) {
             const size_t gbase = (size_t)PMs * MUs * pp;
-            // ---- phase 2: translation coefficients of every canonical tuple
+            double2* tv = Tv + (size_t)buf * 2 * Mb;
+            float2* tf = Tf + (size_t)buf * 2 * Mb;
+            float2* tl = Tl + (size_t)buf * 2 * Mb;
             const int Q = L + 1;
             for (int t = tid; t < S.M; t += kAsmThreads) {
                 const int4 e = S.nmvu[t];
                 const int2 qq = S.qab[t];
                 const int mi = (e.w - e.y) + 2 * L;
                 const int nv = e.x + e.z;
-                if (FP64_SUMS) {
+                if constexpr (FP64_SUMS) {
                     const double* ca = S.cA + (size_t)t * Q;
                     const double* cb = S.cB + (size_t)t * Q;
                     double2 sa = make_double2(0.0, 0.0), sb = make_double2(0.0, 0.0);
@@ -265,37 +396,42 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                         sb.y = fma(c, gv.y, sb.y);
                     }
                     const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
-                    Tv[2 * t] = At;
-                    Tv[2 * t + 1] = Bt;
+                    tv[2 * t] = At;
+                    tv[2 * t + 1] = Bt;
                     if (!DENSE && want64) {
                         const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
                         const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
-                        Tf[2 * t] = ah;
-                        Tf[2 * t + 1] = bh;
-                        Tl[2 * t] = make_float2(__double2float_rn(At.x - (double)ah.x), __double2float_rn(At.y - (double)ah.y));
-                        Tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
+                        tf[2 * t] = ah;
+                        tf[2 * t + 1] = bh;
+                        tl[2 * t] = make_float2(__double2float_rn(At.x - (double)ah.x), __double2float_rn(At.y - (double)ah.y));
+                        tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
                     }
                 } else {
                     const float2* ca = S.cA2 + (size_t)t * Q;
                     const float2* cb = S.cB2 + (size_t)t * Q;
                     float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
-                    for (int q = 0; q <= qq.x; q++)
-                        df_rc_fma(ah, al, ca[q], G32[gbase + (size_t)(nv - 2 * q) * MUs + mi]);
-                    for (int q = 1; q <= qq.y; q++)
-                        df_rc_fma(bh, bl, cb[q], G32[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi]);
+                    // the A and B sums interleaved: two independent double-float chains
+                    const int qa = qq.x, qb = qq.y, qm = qa > qb ? qa : qb;
+                    for (int q = 0; q <= qm; q++) {
+                        if (q <= qa) df_rc_fma(ah, al, ca[q], G32[gbase + (size_t)(nv - 2 * q) * MUs + mi]);
+                        if (q >= 1 && q <= qb) df_rc_fma(bh, bl, cb[q], G32[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi]);
+                    }
                     // normalise (Fast2Sum): hi = fl(h + l), lo = l - (hi - h)
                     const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
                     const float2 a2 = __fadd2_rn(al, negf2(__fadd2_rn(a1, negf2(ah))));
                     const float2 b2 = __fadd2_rn(bl, negf2(__fadd2_rn(b1, negf2(bh))));
-                    Tf[2 * t] = mul_ipowf(a1, nv);
-                    Tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
-                    Tl[2 * t] = mul_ipowf(a2, nv);
-                    Tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
+                    tf[2 * t] = mul_ipowf(a1, nv);
+                    tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
+                    tl[2 * t] = mul_ipowf(a2, nv);
+                    tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
                 }
             }
-            __syncthreads();
-
-            // ---- phase 3: block write
+        };
+        auto write_block = [&](int pp, int buf) {
+            const long long p = p_first + pp;
+            const double2* tv = Tv + (size_t)buf * 2 * Mb;
+            const float2* tf = Tf + (size_t)buf * 2 * Mb;
+            const float2* tl = Tl + (size_t)buf * 2 * Mb;
             const int BB = B * B;
             if (!DENSE) {
                 const long long base = S.mat_off + p * (long long)BB;
@@ -303,17 +439,37 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
                     if (FP64_SUMS && out128) {
-                        const double2 v = Tv[code >> 1];
+                        const double2 v = tv[code >> 1];
                         out128[base + e] = make_double2(flipd(v.x, neg), flipd(v.y, neg));
                     }
                     if (out64) {
-                        const float2 v = Tf[code >> 1];
+                        const float2 v = tf[code >> 1];
                         out64[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
                     }
                     if (out64lo) {
-                        const float2 v = Tl[code >> 1];
+                        const float2 v = tl[code >> 1];
                         out64lo[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
                     }
+                }
+            } else if (REFL) {
+                // block (i, j) only: -r0 (-1)^(m+n+a+1) transfer mie(j, b, v)
+                const int i = (int)(p / N), j = (int)(p % N);
+                const double2* mj_ = mie + (long long)j * 2 * L;
+                const int rmx = B / 2;
+                for (int e = tid; e < BB; e += kAsmThreads) {
+                    const int R = e / B, C = e % B;
+                    const int code = __ldg(S.elem_map + e);
+                    const unsigned neg = code & 1;
+                    double2 v = tv[code >> 1];
+                    v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
+                    const int a = R / rmx, r = R - a * rmx;
+                    int n = 1;   // r = n(n+2) - n + m - 1 = n^2 + n + m - 1, |m| <= n: n = floor(sqrt(r + 1))
+                    while ((n + 1) * (n + 1) <= r + 1) n++;
+                    const int m = r + 1 - n * n - n;
+                    const double2 w = cmul(v, mj_[__ldg(S.miecol + C)]);
+                    const unsigned sgn = (unsigned)((m + n + a + 1) & 1) ^ 1u;   // -(-1)^(m+n+a+1)
+                    out128[((long long)i * B + R) * dense_ld + (long long)j * B + C] =
+                        cmul(make_double2(flipd(refl.r0.x, sgn), flipd(refl.r0.y, sgn)), w);
                 }
             } else {
                 int i, j;
@@ -324,7 +480,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     const int R = e / B, C = e % B;
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
-                    double2 v = Tv[code >> 1];
+                    double2 v = tv[code >> 1];
                     v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
                     const int col = __ldg(S.miecol + C);
                     const double2 vij = cmul(v, mj_[col]);
@@ -335,6 +491,12 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     out128[((long long)j * B + R) * dense_ld + (long long)i * B + C] = vji;
                 }
             }
+        };
+        tuples(0, 0);
+        __syncthreads();
+        for (int pp = 0; pp < np; pp++) {
+            write_block(pp, pp & 1);                        // reads buffer pp & 1
+            if (pp + 1 < np) tuples(pp + 1, (pp + 1) & 1);  // writes the other buffer
             __syncthreads();
         }
     }
@@ -398,6 +560,7 @@ int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector
         d.cB2 = T->cB2;
         d.elem_map = T->elem_map;
         d.neg_ratio = T->neg_ratio;
+        d.neg_ratio2 = T->neg_ratio2;
         d.rowinfo = T->rowinfo;
         d.miecol = T->miecol;
     }
@@ -470,7 +633,8 @@ int stage_release(int slot, cudaStream_t stream) {
 namespace {
 
 int launch_assemble(int nsys, const gb_system* sys, const double* pos, const double* mie, double* out128,
-                    float* out64, float* out64lo, long long dense_ld, bool dense, cudaStream_t stream) {
+                    float* out64, float* out64lo, long long dense_ld, bool dense, cudaStream_t stream,
+                    const Refl* refl = nullptr) {
     std::vector<gb::SysDev> sd;
     int st = gb::make_sysdev(nsys, sys, stream, sd);
     if (st) return st;
@@ -479,20 +643,23 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     for (int s = 0; s < nsys; s++) {
         Lmax = std::max(Lmax, sd[s].lmax);
         Mmax = std::max(Mmax, sd[s].M);
-        total_pairs += sd[s].P;
+        total_pairs += refl ? (long long)sd[s].N * sd[s].N : sd[s].P;
     }
     if (total_pairs == 0) return GB_OK;
     const bool fp64_sums = dense || out128 != nullptr;
     const bool want64 = (out64 != nullptr || out64lo != nullptr) && !dense;
-    // pairs per group: the largest power of two up to 32 whose special-function
-    // tables keep the CTA within ~100 KB of shared memory (at least one pair)
+    // pairs per group: the largest power of two up to 32 whose tables keep the CTA
+    // within ~72 KB of shared memory, so that three CTAs share an SM (at least one pair)
     int PB = 32;
-    while (PB > 1 && asm_layout(Lmax, Mmax, PB, fp64_sums, want64).total > 100 * 1024) PB >>= 1;
+    while (PB > 1 && asm_layout(Lmax, Mmax, PB, fp64_sums, want64).total > 72 * 1024) PB >>= 1;
     const AsmSmem lay = asm_layout(Lmax, Mmax, PB, fp64_sums, want64);
     const size_t smem = lay.total;
     if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
     std::vector<long long> gbase(nsys + 1, 0);
-    for (int s = 0; s < nsys; s++) gbase[s + 1] = gbase[s] + (sd[s].P + PB - 1) / PB;
+    for (int s = 0; s < nsys; s++) {
+        const long long np_s = refl ? (long long)sd[s].N * sd[s].N : sd[s].P;
+        gbase[s + 1] = gbase[s] + (np_s + PB - 1) / PB;
+    }
     const long long ngroups = gbase[nsys];
     // one staging upload: descriptors then group prefix sums
     std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * (nsys + 1));
@@ -504,7 +671,8 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     if (st) return st;
     const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
     const long long* dbase = reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys);
-    auto kfn = dense ? k_assemble<true, true> : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>);
+    auto kfn = refl ? k_assemble<true, true, true>
+                    : (dense ? k_assemble<true, true> : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>));
     GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
     int per_sm = 1;
     GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
@@ -514,7 +682,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
         dsys, nsys, dbase, ngroups, Lmax, Mmax, PB, pos, reinterpret_cast<const double2*>(mie),
         reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
-        dense_ld);
+        dense_ld, refl ? *refl : Refl());
     GB_CUDA_TRY(cudaGetLastError());
     return gb::stage_release(slot, stream);
 }
@@ -532,6 +700,19 @@ int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* m
     if (N == 1) return GB_OK;
     gb_system s{N, lmax, k, 0, 0, 0, 0};
     return launch_assemble(1, &s, pos, mie, out, nullptr, nullptr, D, true, (cudaStream_t)stream);
+}
+
+int gb_reflection_matrix_dense(int N, int lmax, const double* pos, const double* mie, double k, double r_re,
+                               double r_im, double z, double* out, void* stream) {
+    if (!pos || !mie || !out) return gb_set_error(GB_BAD_ARG, "null pointer");
+    if (N < 1 || lmax < 1 || lmax > GB_LMAX_MAX) return gb_set_error(GB_BAD_ARG, "N=%d lmax=%d invalid", N, lmax);
+    const long long D = 2LL * lmax_to_rmax(lmax) * N;
+    GB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double2) * D * D, (cudaStream_t)stream));
+    gb_system s{N, lmax, k, 0, 0, 0, 0};
+    Refl r;
+    r.z = z;
+    r.r0 = make_double2(r_re, r_im);
+    return launch_assemble(1, &s, pos, mie, out, nullptr, nullptr, D, true, (cudaStream_t)stream, &r);
 }
 
 int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,

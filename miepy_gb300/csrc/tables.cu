@@ -239,11 +239,22 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     if (e == cudaSuccess) e = cudaMalloc(&T->cB2, sizeof(float2) * M * Q);
     if (e == cudaSuccess) e = cudaMalloc(&T->elem_map, sizeof(int) * B * B);
     if (e == cudaSuccess) e = cudaMalloc(&T->neg_ratio, sizeof(double) * PM * PM);
+    if (e == cudaSuccess) e = cudaMalloc(&T->neg_ratio2, sizeof(float4) * PM * PM);
     if (e == cudaSuccess) e = cudaMalloc(&T->rowinfo, sizeof(int) * B);
     if (e == cudaSuccess) e = cudaMalloc(&T->miecol, sizeof(int) * B);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->nmvu, nmvu.data(), sizeof(int4) * M, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->elem_map, map.data(), sizeof(int) * B * B, cudaMemcpyHostToDevice, stream);
+    // double-float mantissa and binary exponent: the ratios reach 1/(2p)!, below the
+    // FP32 range, while ratio * P_p^mu stays moderate
+    std::vector<float4> negr2(negr.size());
+    for (size_t q = 0; q < negr.size(); q++) {
+        int ex = 0;
+        const double m = std::frexp(negr[q], &ex);
+        const float hi = (float)m;
+        negr2[q] = make_float4(hi, (float)(m - (double)hi), (float)ex, 0.f);
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->neg_ratio, negr.data(), sizeof(double) * PM * PM, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T->neg_ratio2, negr2.data(), sizeof(float4) * PM * PM, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->rowinfo, rowinfo.data(), sizeof(int) * B, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->miecol, miecol.data(), sizeof(int) * B, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) {
@@ -260,7 +271,7 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
         cudaFree(T->nmvu); cudaFree(T->qab); cudaFree(T->cA); cudaFree(T->cB); cudaFree(T->cA2); cudaFree(T->cB2);
-        cudaFree(T->elem_map); cudaFree(T->neg_ratio); cudaFree(T->rowinfo); cudaFree(T->miecol);
+        cudaFree(T->elem_map); cudaFree(T->neg_ratio); cudaFree(T->neg_ratio2); cudaFree(T->rowinfo); cudaFree(T->miecol);
         delete T;
         return gb_set_cuda_error(e, "building translation tables", __FILE__, __LINE__);
     }

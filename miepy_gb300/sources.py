@@ -36,6 +36,19 @@ class plane_wave:
     def __repr__(self):
         return f"plane_wave(polarization={self.polarization}, amplitude={self.amplitude}, theta={self.theta}, phi={self.phi})"
 
+    def reflect(self, interface, medium, wavelength):
+        """The plane wave reflected by a planar interface (sources/plane_waves.py:172-188):
+        direction theta -> pi - theta, Fresnel-weighted polarisation, phase referred to z."""
+        theta = np.pi - self.theta
+        k = 2 * np.pi * medium.index(wavelength) / wavelength
+        phase = self.phase - 2 * k * self.k_hat[2] * interface.z
+        r_parallel, r_perp = interface.reflection_coefficients(self.theta, wavelength, medium)
+        polarization = [r_parallel * self.polarization[0], r_perp * self.polarization[1]]
+        amplitude = np.linalg.norm(polarization) * self.amplitude
+        if amplitude == 0:
+            polarization = self.polarization
+        return plane_wave(polarization=polarization, theta=theta, phi=self.phi, amplitude=amplitude, phase=phase)
+
     @classmethod
     def from_string(cls, polarization, direction="z", amplitude=1, phase=0, standing=False):
         dirs = {"z": (0, 0), "+z": (0, 0), "-z": (np.pi, 0), "x": (np.pi / 2, 0), "+x": (np.pi / 2, 0),

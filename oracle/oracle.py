@@ -73,6 +73,7 @@ def _declare(L):
         "orc_vsh_translation": (None, [c_int, c_int, c_int, c_int, c_int, _D, _D, _D, c_double, c_int, _D]),
         "orc_vsh_cache_entry": (None, [c_int] * 4 + [_D, _I, _I, _D, _D]),
         "orc_sphere_aggregate_tmatrix": (None, [c_int, c_int, _D, _D, c_double, _D]),
+        "orc_reflection_matrix_nia": (None, [c_int, c_int, _D, _D, c_double, c_double, c_double, c_double, _D]),
         "orc_solve_linear_system": (c_int, [c_int, _D, _D, c_int, c_double, c_int, _D, _D]),
         "orc_bicgstab_plain": (c_int, [c_int, _D, _D, c_int, c_double, _D, _D]),
         "orc_gemv": (None, [c_int, _D, _D, _D]),
@@ -297,6 +298,22 @@ def sphere_aggregate_tmatrix(positions, mie, k):
     out = np.empty((D, D), dtype=np.complex128)
     lib().orc_sphere_aggregate_tmatrix(N, lmax, _dp(pos), _dp(mie.view(np.float64)), float(np.real(k)),
                                        _dp(out.view(np.float64)))
+    return out
+
+
+def reflection_matrix_nia(positions, mie, k, reflection, z):
+    """Reflection matrix of a planar interface at height z (cpp/src/interactions.cpp:464-512):
+    positions [N,3], mie [N, 2*lmax] (or [N,2,lmax]), reflection coefficient r0 ->
+    R [D, D] c128, subtracted from the aggregate T-matrix by the reference."""
+    pos = _f64(positions).reshape(-1, 3)
+    N = pos.shape[0]
+    mie = _c128(mie).reshape(N, -1)
+    lmax = mie.shape[1] // 2
+    D = 2 * lmax * (lmax + 2) * N
+    out = np.empty((D, D), dtype=np.complex128)
+    r = complex(reflection)
+    lib().orc_reflection_matrix_nia(N, lmax, _dp(pos), _dp(mie.view(np.float64)), float(np.real(k)), r.real, r.imag,
+                                    float(z), _dp(out.view(np.float64)))
     return out
 
 

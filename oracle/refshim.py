@@ -98,7 +98,7 @@ def build_cpp_module():
         "miepy.cpp.interactions", solver=solver, bicgstab=lambda A, b, maxiter, tolerance: O.bicgstab(A, b, maxiter, tolerance)[0],
         bicgstab_profiled=_bicgstab_profiled, bicgstab_preconditioned_profiled=_not_in_scope,
         sphere_aggregate_tmatrix=O.sphere_aggregate_tmatrix, particle_aggregate_tmatrix=_not_in_scope,
-        reflection_matrix_nia=_not_in_scope, solve_linear_system=_solve_linear_system,
+        reflection_matrix_nia=O.reflection_matrix_nia, solve_linear_system=_solve_linear_system,
     )
     forces = _module("miepy.cpp.forces", force=O.force, torque=O.torque, force_all=O.force_all,
                      torque_all=O.torque_all)

@@ -803,6 +803,46 @@ void orc_sphere_aggregate_tmatrix(int N, int lmax, const double* pos, const doub
     }
 }
 
+// interactions.reflection_matrix_nia: cpp/src/interactions.cpp:464-512.  Every
+// (i, j) block, i and j over all particles: the outgoing translation from particle
+// j to the mirror image of particle i in the plane z (its z replaced by 2 z - z_i),
+// times -reflection (-1)^(m+n+a+1) and the Mie coefficient of the column particle.
+// positions [N,3] f64, mie [N, 2*lmax] c128, out [D,D] c128.
+void orc_reflection_matrix_nia(int N, int lmax, const double* pos, const double* mie, double k, double r_re,
+                               double r_im, double z, double* out) {
+    const int rmax = lmax_to_rmax(lmax);
+    const int D = 2 * rmax * N;
+    cd* R = reinterpret_cast<cd*>(out);
+    const cd* M = reinterpret_cast<const cd*>(mie);
+    const cd refl(r_re, r_im);
+    for (long e = 0; e < long(D) * D; e++) R[e] = 0.0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < N; i++) {
+        const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2] - 2 * (pos[3 * i + 2] - z);
+        for (int j = 0; j < N; j++) {
+            const double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
+            double rad = std::sqrt(dx * dx + dy * dy + dz * dz);
+            double theta = std::acos(dz / rad);
+            double phi = std::atan2(dy, dx);
+            for (int n = 1; n <= lmax; n++)
+                for (int m = -n; m <= n; m++)
+                    for (int v = 1; v <= lmax; v++)
+                        for (int u = -v; u <= v; u++) {
+                            double tr[4];
+                            orc_vsh_translation(1, m, n, u, v, &rad, &theta, &phi, k, 0, tr);
+                            const cd transfer[2] = {cd(tr[0], tr[1]), cd(tr[2], tr[3])};
+                            for (int a = 0; a < 2; a++)
+                                for (int b = 0; b < 2; b++) {
+                                    const cd factor = -refl * double(sgnpow(m + n + a + 1));
+                                    const long idx = long(i) * 2 * rmax + a * rmax + n * (n + 2) - n + m - 1;
+                                    const long idy = long(j) * 2 * rmax + b * rmax + v * (v + 2) - v + u - 1;
+                                    R[idx * D + idy] = factor * transfer[(a + b) % 2] * M[long(j) * 2 * lmax + b * lmax + v - 1];
+                                }
+                        }
+        }
+    }
+}
+
 // interactions.solve_linear_system: cpp/src/interactions.cpp:347-368.
 // method 0 = bicgstab (Eigen, tol/maxiter), 1 = exact (partial-pivot LU).
 // T is the aggregate T-matrix WITHOUT the identity.  Returns iterations (bicgstab),

@@ -149,6 +149,43 @@ def main():
                                         wavelength=600 * nm, lmax=3, method=miepy.solver.exact),
                    store_matrix=True)
 
+    # a trimer above a planar interface (substrate row): reflected source, reflection
+    # matrix, solve, observables and fields with the reflected source
+    sub = miepy.interface(miepy.constant_material(index=1.7), z=-120 * nm)
+    c = miepy.sphere_cluster(position=[[0, 0, 0], [210 * nm, 40 * nm, 30 * nm], [-160 * nm, 90 * nm, 60 * nm]],
+                             radius=[70 * nm, 60 * nm, 80 * nm], material=diel, medium=miepy.materials.water(),
+                             source=miepy.sources.plane_wave([1, 0]), wavelength=600 * nm, lmax=3,
+                             interface=sub, method=miepy.solver.exact)
+    md = c.material_data
+    r0 = sub.reflection_coefficients(theta=0, wavelength=c.wavelength, medium=c.medium)[0]
+    C = c.cross_sections()
+    fx = np.array([0.0, 300 * nm, -250 * nm, 50 * nm])
+    fy = np.array([0.0, -100 * nm, 150 * nm, 400 * nm])
+    fz = np.array([-60 * nm, 200 * nm, -40 * nm, 120 * nm])
+    rec = dict(position=c.position, radius=c.radius, wavelength=np.float64(c.wavelength), lmax=np.int64(c.lmax),
+               eps=np.asarray(md.eps, complex), n=np.asarray(md.n, complex), eps_b=np.complex128(md.eps_b),
+               mu_b=np.complex128(md.mu_b), k_b=np.float64(np.real(md.k_b)), interface_z=np.float64(sub.z),
+               interface_index=np.complex128(1.7), r0=np.complex128(r0), mie_scat=c.mie_scat, mie_int=c.mie_int,
+               p_src=c.p_src, p_inc=c.p_inc, p_scat=c.p_scat, p_int=c.p_int,
+               cross_sections=np.array([C.scattering, C.absorption, C.extinction], dtype=float),
+               force=c.force(), torque=c.torque(),
+               reflection_matrix=miepy.interactions.reflection_matrix_nia(c.position, c.mie_scat, md.k_b, r0, sub.z),
+               field_x=fx, field_y=fy, field_z=fz, E_total=c.E_field(fx, fy, fz))
+    np.savez_compressed(os.path.join(HERE, "interface3_lmax3_exact.npz"), **rec)
+    print("wrote interface3_lmax3_exact")
+    # the reference's interface identity (moving particle and interface together),
+    # for a metallic sphere in water: both cross-section triples
+    wat = miepy.constant_material(index=1.33)
+    kw = dict(radius=75 * nm, material=miepy.constant_material(index=0.2 + 3.0j), medium=wat, lmax=2,
+              wavelength=600 * nm, source=miepy.sources.plane_wave([1, 0]), method=miepy.solver.exact)
+    c1 = miepy.sphere_cluster(position=[0, 0, -400 * nm], interface=miepy.interface(miepy.constant_material(index=1.7)),
+                              **kw)
+    c2 = miepy.sphere_cluster(position=[0, 0, 0],
+                              interface=miepy.interface(miepy.constant_material(index=1.7), z=400 * nm), **kw)
+    np.savez_compressed(os.path.join(HERE, "interface_identity.npz"), C1=np.array(c1.cross_sections()),
+                        C2=np.array(c2.cross_sections()))
+    print("wrote interface_identity")
+
     # special-function tables for the device recurrences
     from oracle import oracle as O
     z = np.linspace(-0.999, 0.999, 23)

@@ -37,6 +37,13 @@ PINNED = {
     "test_point_matching.py": 2,
     "test_coordinate_geometry.py": 2,
     "test_source_rotation.py": 1,
+    "test_interface.py": 2,
+}
+
+# Parametrisations that need the absent ``spherical`` package (Wigner-D rotation of
+# a reflected Gaussian beam), deselected by a -k expression on their ids.
+DESELECT = {
+    "test_interface.py": "not s10 and not source0",
 }
 
 pytestmark = pytest.mark.skipif(not reference_available(), reason="reference source tree not available")
@@ -48,6 +55,8 @@ def test_reference_suite_passes_on_oracle(fname):
     env = dict(os.environ, PYTHONPATH=ROOT + os.pathsep + os.environ.get("PYTHONPATH", ""))
     cmd = [sys.executable, "-m", "pytest", "-p", "no:cacheprovider", "-p", "oracle.pytest_refshim", "-q",
            "--rootdir", ROOT, ref_tests]
+    if fname in DESELECT:
+        cmd += ["-k", DESELECT[fname]]
     res = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=900)
     tail = res.stdout[-2000:] + res.stderr[-2000:]
     expected = PINNED[fname]
