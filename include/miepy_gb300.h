@@ -192,6 +192,32 @@ int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const int64_t* mie_
                       double eps_b, int source, double* p_scat, double* p_int, double* xs, double* force,
                       double* torque, void* stream);
 
+/* ---------------------------------------------------- general particles --
+ * Clusters of particles given by their T-matrices: the reference's
+ * particle_aggregate_tmatrix (cpp/src/interactions.cpp:416-462) with the T-matrix
+ * overload of vsh_translation_insert_pair (cpp/src/vsh_translation.cpp:53-159),
+ * whose block (i, j) is A_ij T_j, and cluster._solve_interactions
+ * (cluster.py:652-657).  The packed translation blocks A come from
+ * gb_assemble_batch (they do not depend on the particles); each particle's T-matrix
+ * [B][B] (B = 2 rmax, row-major, the reference's mode order) is applied to the
+ * vector before every matrix pass.  tmat128 / tmat64: complex128 / complex64
+ * T-matrices of all particles of all clusters, cluster s starting at complex
+ * offset tm_off[s]; GB_PREC_FP64 needs tmat128, GB_PREC_FP32 tmat64, the mixed
+ * methods both.  lmax <= 8.  Other arguments and results as gb_solve_batch (tvec
+ * is not used); the workspace is gb_solve_workspace_size's. */
+int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter,
+                           double inner_tol, int max_refine, const double* mat128, const float* mat64,
+                           const float* mat64lo, const double* tmat128, const float* tmat64, const int64_t* tm_off,
+                           const double* b, double* x, void* workspace, size_t ws_bytes, int* status, int* iters,
+                           double* resid, void* stream);
+
+/* Epilogue of T-matrix clusters: p_scat = T p_inc per particle (required output),
+ * then the cross-sections per (a, n), forces and torques of gb_epilogue_batch from
+ * p_scat, p_inc and p_src (flux.cpp:5-30, forces.cpp:7-171). */
+int gb_tmatrix_epilogue_batch(int nsys, const gb_system* sys, int R, const double* tmat128, const int64_t* tm_off,
+                              const int64_t* obs_off, const double* p_inc, const double* p_src, double eps_b,
+                              int source, double* p_scat, double* xs, double* force, double* torque, void* stream);
+
 /* Cross-sections of particles from given coefficients (replaces
  * flux.particle_cross_sections, cpp/src/flux.cpp:5-30, and the plugin function
  * particle_cross_sections_jax, backends/jax/flux.py:14-44): p_* [N,2,rmax] c128

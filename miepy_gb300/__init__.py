@@ -11,6 +11,7 @@ from . import backend, beams, materials as _materials_mod, sources, sweep
 from .beams import gaussian_beam
 from .cluster import cross_sections, solver, sphere_cluster
 from .interface import interface
+from .tmatrix_cluster import cluster, sphere, tmatrix_cluster, tmatrix_sphere
 from .engine import ClusterBatch, footprint_bytes
 from .materials import (constant_material, dielectric, drude_material, function_material, material_struct,
                         materials)

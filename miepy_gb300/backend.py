@@ -102,6 +102,32 @@ def sphere_aggregate_tmatrix_jax(positions, mie, k):
     return DeviceAggregateTMatrix(positions, mie, k)
 
 
+def particle_aggregate_tmatrix(positions, tmatrix, k):
+    """positions [N,3], tmatrix [N,2,rmax,2,rmax], k -> T_agg [N,2,rmax,N,2,rmax]
+    (interactions.cpp:416-462): the translation blocks A_ij from the GPU assembler
+    (unit Mie coefficients), then block (i, j) = A_ij T_j as one batched complex
+    GEMM (cuBLAS) over the column blocks."""
+    dev = require_cuda()
+    pos = np.ascontiguousarray(np.asarray(positions, dtype=float).reshape(-1, 3))
+    N = pos.shape[0]
+    T = np.asarray(tmatrix, dtype=complex).reshape(N, -1)
+    B = int(round(np.sqrt(T.shape[1])))
+    rmax = B // 2
+    lmax = rmax_to_lmax(rmax)
+    if N == 1:
+        return np.zeros((1, 2, rmax, 1, 2, rmax), dtype=complex)
+    D = B * N
+    d_pos = torch.from_numpy(pos).to(dev)
+    ones = torch.ones(N * 2 * lmax, dtype=torch.complex128, device=dev)
+    A = torch.empty(D * D, dtype=torch.complex128, device=dev)
+    nat.check(nat.lib().gb_assemble_sphere_dense(N, lmax, nat.ptr(d_pos), nat.ptr(ones), float(np.real(k)), nat.ptr(A),
+                                                 current_stream(dev)), "dense assembly")
+    Tj = torch.from_numpy(np.ascontiguousarray(T.reshape(N, B, B))).to(dev)
+    A4 = A.view(N, B, N, B).permute(2, 0, 1, 3).reshape(N, N * B, B)    # [j][(i, r)][c]
+    out = torch.bmm(A4, Tj)                                              # [j][(i, r)][col]
+    return out.reshape(N, N, B, B).permute(1, 2, 0, 3).reshape(N, 2, rmax, N, 2, rmax).cpu().numpy()
+
+
 def reflection_matrix_nia(positions, mie, k, reflected, z):
     """positions [N,3], mie [N,2,lmax], k, reflection coefficient, interface height z ->
     R [N,2,rmax,N,2,rmax] c128 (interactions.py:208-225 / interactions.cpp:464-512),

@@ -41,6 +41,7 @@ struct EpiArgs {
     double eps_b;
     double2* p_scat;
     double2* p_int;
+    const double2* pscat_in;    // given p_scat (general particles: T p_inc); null: t o p_inc
     double* xs;
     double* force;
     double* torque;
@@ -71,9 +72,11 @@ __global__ void __launch_bounds__(128) k_epilogue(EpiArgs a, long long total) {
     const double k = S.k;
     auto pin = [&](int e) { return a.p_inc[vb + (long long)e * R]; };
     auto psrc = [&](int e) { return a.p_src[vb + (long long)e * R]; };
-    auto pscat = [&](int e) { return cmul(pin(e), ms[__ldg(S.miecol + e)]); };
+    auto pscat = [&](int e) {
+        return a.pscat_in ? a.pscat_in[vb + (long long)e * R] : cmul(pin(e), ms[__ldg(S.miecol + e)]);
+    };
     // ---- p_scat, p_int (polarisation-swapped interior coefficients)
-    for (int e = lane; e < B; e += 32) {
+    for (int e = lane; e < B && !a.pscat_in; e += 32) {
         const double2 pi_ = pin(e);
         const int col = __ldg(S.miecol + e);   // a*L + n - 1
         if (a.p_scat) a.p_scat[vb + (long long)e * R] = cmul(pi_, ms[col]);
@@ -93,7 +96,7 @@ __global__ void __launch_bounds__(128) k_epilogue(EpiArgs a, long long total) {
             for (int m = -n; m <= n; m++) {
                 const int e = aa * rmax + n * n + n + m - 1;
                 const double2 pi_ = pin(e), pr = psrc(e);
-                const double2 ps = cmul(pi_, ms[aa * L + n - 1]);
+                const double2 ps = a.pscat_in ? pscat(e) : cmul(pi_, ms[aa * L + n - 1]);
                 cabs += f * ((pi_.x * ps.x + pi_.y * ps.y) - (ps.x * ps.x + ps.y * ps.y));
                 cext += f * (pr.x * ps.x + pr.y * ps.y);
             }
@@ -232,6 +235,102 @@ extern "C" int gb_epilogue_batch(int nsys, const gb_system* sys, int R, const in
     a.eps_b = eps_b;
     a.p_scat = reinterpret_cast<double2*>(p_scat);
     a.p_int = reinterpret_cast<double2*>(p_int);
+    a.xs = xs;
+    a.force = force;
+    a.torque = torque;
+    a.pscat_in = nullptr;
+    const long long total = base[nsys];
+    gb::note_launch();
+    k_epilogue<<<(unsigned)((total * 32 + 127) / 128), 128, 0, st_>>>(a, total);
+    GB_CUDA_TRY(cudaGetLastError());
+    return gb::stage_release(slot, st_);
+}
+
+// p_scat = T p_inc for clusters of general particles (cluster.py:652-657): one
+// thread per (cluster, row, rhs), B-term dot product with the particle's T-matrix row.
+namespace {
+__global__ void k_apply_tmat(const gb::SysDev* __restrict__ sys, const long long* __restrict__ base, int nsys, int R,
+                             const double2* __restrict__ p_inc, double2* __restrict__ p_scat, long long total) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        int s = 0, hi = nsys - 1;
+        while (s < hi) {
+            const int mid = (s + hi + 1) >> 1;
+            if (base[mid] <= g) s = mid;
+            else hi = mid - 1;
+        }
+        const gb::SysDev S = sys[s];
+        const long long loc = g - base[s];   // (row, rhs) within the cluster
+        const int rr = (int)(loc % R);
+        const long long row = loc / R;
+        const int B = S.B, part = (int)(row / B), e = (int)(row % B);
+        const double2* Tr = S.tmat128 + ((long long)part * B + e) * B;
+        const double2* xin = p_inc + S.vec_off + (long long)part * B * R + rr;
+        double2 acc = make_double2(0, 0);
+        for (int c = 0; c < B; c++) cfma(acc, __ldg(Tr + c), xin[(long long)c * R]);
+        p_scat[S.vec_off + row * R + rr] = acc;
+    }
+}
+}   // namespace
+
+extern "C" int gb_tmatrix_epilogue_batch(int nsys, const gb_system* sys, int R, const double* tmat128,
+                                         const int64_t* tm_off, const int64_t* obs_off, const double* p_inc,
+                                         const double* p_src, double eps_b, int source, double* p_scat, double* xs,
+                                         double* force, double* torque, void* stream) {
+    if (nsys < 1 || !sys || !tmat128 || !tm_off || !obs_off || !p_inc || !p_scat || R < 1)
+        return gb_set_error(GB_BAD_ARG, "bad epilogue arguments");
+    if ((xs || !source) && !p_src) return gb_set_error(GB_BAD_ARG, "p_src required");
+    cudaStream_t st_ = (cudaStream_t)stream;
+    std::vector<gb::SysDev> sd;
+    int st = gb::make_sysdev(nsys, sys, st_, sd);
+    if (st) return st;
+    std::vector<long long> rows(nsys + 1, 0), base(nsys + 1, 0), zeros(nsys, 0);
+    for (int s = 0; s < nsys; s++) {
+        sd[s].tmat128 = reinterpret_cast<const double2*>(tmat128) + tm_off[s];
+        rows[s + 1] = rows[s] + (long long)sd[s].D * R;
+        base[s + 1] = base[s] + (long long)sd[s].N * R;
+    }
+    std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * (4 * nsys + 2));
+    unsigned char* w = blob.data();
+    memcpy(w, sd.data(), sizeof(gb::SysDev) * nsys);
+    w += sizeof(gb::SysDev) * nsys;
+    memcpy(w, base.data(), sizeof(long long) * (nsys + 1));
+    w += sizeof(long long) * (nsys + 1);
+    memcpy(w, zeros.data(), sizeof(long long) * nsys);
+    w += sizeof(long long) * nsys;
+    memcpy(w, obs_off, sizeof(long long) * nsys);
+    w += sizeof(long long) * nsys;
+    memcpy(w, rows.data(), sizeof(long long) * (nsys + 1));
+    void* dblob = nullptr;
+    int slot = 0;
+    st = gb::stage_acquire(blob.data(), blob.size(), st_, &dblob, &slot);
+    if (st) return st;
+    unsigned char* d = static_cast<unsigned char*>(dblob);
+    const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(d);
+    const long long* dbase = reinterpret_cast<const long long*>(d + sizeof(gb::SysDev) * nsys);
+    const long long* drows = dbase + (nsys + 1) + 2 * nsys;
+    const long long total_rows = rows[nsys];
+    gb::note_launch();
+    k_apply_tmat<<<(unsigned)std::min<long long>((total_rows + 255) / 256, 65535), 256, 0, st_>>>(
+        dsys, drows, nsys, R, reinterpret_cast<const double2*>(p_inc), reinterpret_cast<double2*>(p_scat), total_rows);
+    GB_CUDA_TRY(cudaGetLastError());
+    EpiArgs a;
+    a.sys = dsys;
+    a.base = dbase;
+    a.mie_off = dbase + (nsys + 1);
+    a.obs_off = a.mie_off + nsys;
+    a.nsys = nsys;
+    a.R = R;
+    a.source = source;
+    a.xs_L = 0;
+    for (int s = 0; s < nsys; s++) a.xs_L = std::max(a.xs_L, sd[s].lmax);
+    a.mie_scat = nullptr;
+    a.mie_int = nullptr;
+    a.p_inc = reinterpret_cast<const double2*>(p_inc);
+    a.p_src = reinterpret_cast<const double2*>(p_src);
+    a.eps_b = eps_b;
+    a.p_scat = nullptr;
+    a.p_int = nullptr;
+    a.pscat_in = reinterpret_cast<const double2*>(p_scat);
     a.xs = xs;
     a.force = force;
     a.torque = torque;

@@ -71,6 +71,10 @@ struct SysDev {
     const float4* neg_ratio2;
     const int* rowinfo;
     const int* miecol;
+    // general particles: per-particle T-matrices [N][B][B] (row-major, mode order of
+    // the reference), complex128 and a complex64 copy; null for spheres (t vector)
+    const double2* tmat128 = nullptr;
+    const float2* tmat64 = nullptr;
 };
 
 // Pinned staging ring for per-call descriptor uploads (assemble.cu).

@@ -55,6 +55,7 @@
 namespace {
 
 constexpr int kVRows = 128;        // rows per vector work item (= threads per CTA)
+constexpr int kRBThreads = 384;    // threads of the block reduce and T-matrix y kernels (>= B*R for lmax <= 8, R <= 2)
 constexpr int kRRows = 32;         // rows per reduce work item
 constexpr int kGemvThreads = 128;  // 4 warps
 constexpr int kGemvWarps = kGemvThreads / 32;
@@ -411,6 +412,77 @@ k_yprep(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int 
         const C yu = cflip(cmul(t, xv), eneg);
         const C yw = cflip(yu, sneg);
         const long long o = S.vec_off + (long long)row * R + rr;
+        Yu[o] = make_y<YK>(yu);
+        Yw[o] = make_y<YK>(yw);
+    }
+}
+
+// y vectors of clusters of general particles (the T-matrix overload of the
+// reference's aggregate, vsh_translation.cpp:53-159: block (i, j) = A_ij T_j, so
+// (I + T_agg) x = x + A (T x) with the packed translation blocks A).  One CTA per
+// particle (an item of the reduce plan): it applies the BiCGSTAB vector update of
+// the particle's rows, keeps the updated vector in shared memory, then forms
+// z = eps(r) (T x)[rho(r)] for every row r with the particle's T-matrix: complex64
+// in FP32 arithmetic for the FP32 solver, complex128 in FP64 otherwise.
+template <int YK, typename VT, int R>
+__global__ void __launch_bounds__(kRBThreads)
+k_yprep_tmat(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
+             const KState* __restrict__ st, int mask_mode, const VT* __restrict__ x,
+             typename YType<YK>::t* __restrict__ Yu, typename YType<YK>::t* __restrict__ Yw, YUpd<VT> up) {
+    const int it = blockIdx.x;
+    if (it >= nitems) {
+        pdl_wait();
+        return;
+    }
+    const Item I = items[it];   // prologue on plan data
+    const gb::SysDev S = sys[I.sys];
+    using C = typename Arith<VT>::C;
+    using T = typename Arith<VT>::T;
+    const T tg{};
+    const int B = S.B, part = I.r0 / B, tid = threadIdx.x;
+    __shared__ C xs[kRBThreads];   // [B][R], B R <= kRBThreads
+    pdl_wait();
+    pdl_trigger();
+    if (!any_active<R>(st, I.sys, mask_mode)) return;   // the same for the whole CTA
+    if (tid < B * R) {
+        const int e = tid / R, rr = tid - e * R;
+        const long long es = S.vec_off + ((long long)part * B + e) * R + rr;
+        C xv;
+        if (up.kind != 0 && active_rhs<R>(st, I.sys, rr, 0)) {   // p = r + beta (p - omega v) or s = r - alpha v
+            const KState& k = st[I.sys * R + rr];
+            const C rv = to_c<C>(up.r[es]), vv = to_c<C>(up.v[es]);
+            C nv;
+            if (up.kind == 1) {
+                const C pv = to_c<C>(up.out[es]);
+                nv = cadd(rv, cmul(ks_beta(k, tg), csub(pv, cmul(ks_omega(k, tg), vv))));
+            } else {
+                nv = csub(rv, cmul(ks_alpha(k, tg), vv));
+            }
+            const VT q = from_c<VT>(nv);
+            up.out[es] = q;
+            xv = to_c<C>(q);
+        } else {
+            xv = to_c<C>(x[es]);
+        }
+        xs[tid] = xv;
+    }
+    __syncthreads();
+    if (tid < B * R) {
+        const int r = tid / R, rr = tid - r * R;
+        const int info = __ldg(S.rowinfo + r);
+        const int rho = info & ((1 << 29) - 1);
+        const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
+        C z = czero<C>();
+        if constexpr (std::is_same<C, float2>::value) {
+            const float2* Tr = S.tmat64 + ((long long)part * B + rho) * B;
+            for (int c = 0; c < B; c++) cfmaf(z, __ldg(Tr + c), xs[c * R + rr]);
+        } else {
+            const double2* Tr = S.tmat128 + ((long long)part * B + rho) * B;
+            for (int c = 0; c < B; c++) cfma(z, __ldg(Tr + c), xs[c * R + rr]);
+        }
+        const C yu = cflip(z, eneg);
+        const C yw = cflip(yu, sneg);
+        const long long o = S.vec_off + ((long long)part * B + r) * R + rr;
         Yu[o] = make_y<YK>(yu);
         Yw[o] = make_y<YK>(yw);
     }
@@ -1016,7 +1088,6 @@ template <> struct RAcc<float4> {
 // y = x + T x (from the partials, or from a dense Tx), and per-item partial dots:
 //   mode 1: d0 = <r0, y>;  mode 2: d0 = |y|^2, d1 = <y, s>;
 //   mode 3: y := b - (x + T x), d0 = |y|^2  (residual).
-constexpr int kRBThreads = 384;   // threads of the block reduce (>= B*R for lmax <= 8, R <= 2)
 
 // Partials are read as 16-byte words: two float2 elements, or one float4 / double2.
 template <typename OutT> struct PWord {
@@ -1478,6 +1549,7 @@ struct StripGroup {     // strips [beg, end) of clusters with block size B (one 
 struct Plan {
     int nsys = 0, R = 1, nv = 0, nr = 0;
     long long nstrips = 0, total_pairs = 0, total_vec = 0, max_B = 0, cw_elems = 0, cu_elems = 0;
+    bool tmat = false;   // general particles: y vectors from per-particle T-matrices (k_yprep_tmat)
     std::vector<StripGroup> groups;
     std::vector<gb::SysDev> sd;
     std::vector<Strip> strips;
@@ -1769,8 +1841,13 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     int e = GB_OK;
     if (pol == 0) {
         gb::note_launch();
-        GB_CUDA_TRY(launch_pdl(k_yprep<0, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st, mask,
-                               tvec, xin, reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), up));
+        if (P.tmat)
+            GB_CUDA_TRY(launch_pdl(k_yprep_tmat<0, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
+                                   D.ritems, P.nr, st, mask, xin, reinterpret_cast<double2*>(Yu),
+                                   reinterpret_cast<double2*>(Yw), up));
+        else
+            GB_CUDA_TRY(launch_pdl(k_yprep<0, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st,
+                                   mask, tvec, xin, reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), up));
         if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
@@ -1779,8 +1856,13 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
                                reinterpret_cast<const double2*>(CW), xin, yout, mode, aux, b128, dots, fz));
     } else if (pol == 1) {
         gb::note_launch();
-        GB_CUDA_TRY(launch_pdl(k_yprep<1, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st, mask,
-                               tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
+        if (P.tmat)
+            GB_CUDA_TRY(launch_pdl(k_yprep_tmat<1, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
+                                   D.ritems, P.nr, st, mask, xin, reinterpret_cast<float4*>(Yu),
+                                   reinterpret_cast<float4*>(Yw), up));
+        else
+            GB_CUDA_TRY(launch_pdl(k_yprep<1, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st,
+                                   mask, tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
         if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
         if (e) return e;
         gb::note_launch();
@@ -1789,8 +1871,13 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
                                reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz));
     } else {
         gb::note_launch();
-        GB_CUDA_TRY(launch_pdl(k_yprep<2, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st, mask,
-                               tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
+        if (P.tmat)
+            GB_CUDA_TRY(launch_pdl(k_yprep_tmat<2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
+                                   D.ritems, P.nr, st, mask, xin, reinterpret_cast<float4*>(Yu),
+                                   reinterpret_cast<float4*>(Yw), up));
+        else
+            GB_CUDA_TRY(launch_pdl(k_yprep<2, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st,
+                                   mask, tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
         if (P.nstrips) e = launch_df<R>(P, D, st, mask, mat_hi, mat_lo, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
@@ -1969,7 +2056,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         const void* a[12] = {base, mat, tvec, D.sys, D.strips, D.vitems, D.ritems, D.sp, st, nullptr, nullptr, nullptr};
         memcpy(key.a, a, sizeof(a));
         key.n[0] = P.nsys;
-        key.n[1] = R | (pol << 8) | ((DENSE ? 1 : 0) << 16) | ((long long)sizeof(VT) << 24);
+        key.n[1] = R | (pol << 8) | ((DENSE ? 1 : 0) << 16) | ((long long)sizeof(VT) << 24) | ((long long)P.tmat << 40);
         key.n[2] = P.nstrips;
         key.n[3] = P.nv | ((long long)P.nr << 32);
         memcpy(&key.n[4], &tol, sizeof(double));
@@ -2272,6 +2359,40 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
         return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
                              status, iters, resid, s);
     return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                         status, iters, resid, s);
+}
+
+int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter,
+                           double inner_tol, int max_refine, const double* mat128, const float* mat64,
+                           const float* mat64lo, const double* tmat128, const float* tmat64, const int64_t* tm_off,
+                           const double* b, double* x, void* workspace, size_t ws_bytes, int* status, int* iters,
+                           double* resid, void* stream) {
+    if (nsys < 1 || !sys || !tm_off || !b || !x || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
+    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
+    if (!prec_ok(prec, mat128, mat64, mat64lo))
+        return gb_set_error(GB_BAD_ARG, "precision %d is missing one of its matrices", prec);
+    const bool need128 = prec != GB_PREC_FP32, need64 = prec != GB_PREC_FP64;
+    if ((need128 && !tmat128) || (need64 && !tmat64))
+        return gb_set_error(GB_BAD_ARG, "precision %d needs the %s T-matrices", prec, need128 ? "complex128" : "complex64");
+    if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
+    cudaStream_t s = (cudaStream_t)stream;
+    Plan P;
+    int e = build_plan(nsys, sys, R, s, P);
+    if (e) return e;
+    for (int q = 0; q < nsys; q++) {
+        if (P.sd[q].B * R > kRBThreads) return gb_set_error(GB_UNSUPPORTED, "T-matrix clusters need lmax <= 8");
+        if (tmat128) P.sd[q].tmat128 = reinterpret_cast<const double2*>(tmat128) + tm_off[q];
+        if (tmat64) P.sd[q].tmat64 = reinterpret_cast<const float2*>(tmat64) + tm_off[q];
+    }
+    P.tmat = true;
+    WS w = ws_layout(P, prec, false);
+    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
+    unsigned char* base = static_cast<unsigned char*>(workspace);
+    if (inner_tol <= 0) inner_tol = 1e-6;
+    if (R == 1)
+        return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, nullptr, b, x, base, w,
+                             status, iters, resid, s);
+    return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, nullptr, b, x, base, w,
                          status, iters, resid, s);
 }
 

@@ -50,6 +50,17 @@ def footprint_bytes(N, lmax, R=1, precision="fp64"):
     return mat + partials + vec + 4096
 
 
+def _spec_lmax(spec, N):
+    """lmax of a cluster spec: from its Mie coefficients [N,2,lmax], or from its
+    T-matrices [N, B, B] / [N, 2, rmax, 2, rmax] (B = 2 lmax (lmax + 2))."""
+    if "mie_scat" in spec:
+        return int(np.asarray(spec["mie_scat"]).shape[-1])
+    T = np.asarray(spec["tmatrix"])
+    n = T.shape[0] if N is None else N
+    B = int(round(np.sqrt(T.size // n)))
+    return int(round(np.sqrt(1 + B // 2) - 1))
+
+
 _stage_local = threading.local()
 
 
@@ -106,6 +117,20 @@ class ClusterBatch:
         self.mat64lo = torch.empty(mat, dtype=torch.complex64, device=dev) if "lo" in need else None
         self._ws = None
         self._host_out = None
+        # general particles: per-particle T-matrices [N][B][B] instead of Mie coefficients
+        has_t = ["tmatrix" in sp for sp in specs]
+        if any(has_t) and not all(has_t):
+            raise ValueError("a batch holds either sphere clusters (mie_scat) or T-matrix clusters (tmatrix)")
+        self.tmatrix = all(has_t)
+        self.tmat128 = self.tmat64 = None
+        if self.tmatrix:
+            sizes = [l["N"] * (2 * l["rmax"]) ** 2 for l in self.layout]
+            self.tm_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+            n = int(sum(sizes))
+            if precision != "fp32":
+                self.tmat128 = torch.empty(n, dtype=torch.complex128, device=dev)
+            if precision != "fp64":
+                self.tmat64 = torch.empty(n, dtype=torch.complex64, device=dev)
         self._upload(specs)
 
     def _set_layout(self, specs):
@@ -117,7 +142,7 @@ class ClusterBatch:
         for s in specs:
             pos = np.asarray(s["position"], float).reshape(-1, 3)
             N = pos.shape[0]
-            lmax = int(np.asarray(s["mie_scat"]).shape[-1])
+            lmax = _spec_lmax(s, N)
             rmax = lmax_to_rmax(lmax)
             D = 2 * rmax * N
             el = matrix_elements(N, lmax)
@@ -142,6 +167,7 @@ class ClusterBatch:
         pinned staging buffer, as one asynchronous copy on the current stream."""
         stage, done = _staging(self._inputs.numel())
         hv = stage.numpy()
+        n_mie = lambda sp: 2 * np.asarray(sp["position"]).reshape(-1, 3).shape[0] * _spec_lmax(sp, None)
         for name, dt, n in self._parts:
             dst = hv[self._offs[name]: self._offs[name] + np.dtype(dt).itemsize * n].view(dt)
             o = 0
@@ -149,27 +175,35 @@ class ClusterBatch:
                 if name == "pos":
                     a = np.asarray(sp["position"], float).reshape(-1)
                 elif name == "mie_scat":
-                    a = np.asarray(sp["mie_scat"]).reshape(-1)
+                    a = np.asarray(sp["mie_scat"]).reshape(-1) if "mie_scat" in sp else np.zeros(n_mie(sp), complex)
                 elif name == "mie_int":
-                    a = np.asarray(sp.get("mie_int", np.zeros_like(sp["mie_scat"]))).reshape(-1)
+                    a = np.asarray(sp["mie_int"]).reshape(-1) if "mie_int" in sp else np.zeros(n_mie(sp), complex)
                 else:
                     a = np.asarray(sp["p_src"]).reshape(-1)
                 dst[o: o + a.size] = a
                 o += a.size
         self._inputs.copy_(stage[: self._inputs.numel()], non_blocking=True)
         done.record(torch.cuda.current_stream(self.device))
+        if self.tmatrix:   # per-particle T-matrices (a separate, larger upload)
+            host = np.concatenate([np.asarray(sp["tmatrix"], complex).reshape(-1) for sp in specs])
+            if self.tmat128 is not None:
+                self.tmat128.copy_(torch.from_numpy(np.ascontiguousarray(host)))
+            if self.tmat64 is not None:
+                self.tmat64.copy_(torch.from_numpy(np.ascontiguousarray(host.astype(np.complex64))))
         self.status = self.iters = self.resid = None
         self.assembled = False
 
     def load(self, specs):
         """New clusters of the same shapes (per cluster N and lmax, same order) into
         this batch's device buffers: positions, Mie coefficients, wavenumbers and
-        right-hand sides are uploaded; the matrices are rebuilt by the next assemble."""
+        right-hand sides (and T-matrices of general particles) are uploaded; the
+        matrices are rebuilt by the next assemble."""
         old = [(l["N"], l["lmax"]) for l in self.layout]
-        new = [(np.asarray(s["position"]).reshape(-1, 3).shape[0], int(np.asarray(s["mie_scat"]).shape[-1]))
-               for s in specs]
+        new = [(np.asarray(s["position"]).reshape(-1, 3).shape[0], _spec_lmax(s, None)) for s in specs]
         if old != new:
             raise ValueError("load() needs clusters of the batch's shapes (N, lmax per cluster)")
+        if any(("tmatrix" in s) != self.tmatrix for s in specs):
+            raise ValueError("load() needs clusters of the batch's kind (Mie coefficients or T-matrices)")
         self._set_layout(specs)
         self._upload(specs)
         return self
@@ -206,11 +240,19 @@ class ClusterBatch:
         status = np.zeros(n, dtype=np.int32)
         iters = np.zeros(n, dtype=np.int32)
         resid = np.zeros(n, dtype=np.float64)
-        rc = L.gb_solve_batch(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
-                              int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64), nat.ptr(self.mat64lo),
-                              nat.ptr(self.tvec),
-                              nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data,
-                              iters.ctypes.data, resid.ctypes.data, current_stream(self.device))
+        if self.tmatrix:
+            rc = L.gb_solve_batch_tmatrix(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
+                                          int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64),
+                                          nat.ptr(self.mat64lo), nat.ptr(self.tmat128), nat.ptr(self.tmat64),
+                                          self.tm_off.ctypes.data, nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws),
+                                          ws.numel(), status.ctypes.data, iters.ctypes.data, resid.ctypes.data,
+                                          current_stream(self.device))
+        else:
+            rc = L.gb_solve_batch(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
+                                  int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64), nat.ptr(self.mat64lo),
+                                  nat.ptr(self.tvec),
+                                  nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data,
+                                  iters.ctypes.data, resid.ctypes.data, current_stream(self.device))
         if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN) or (raise_on_fail and rc):
             nat.check(rc, "solve")
         self.status, self.iters, self.resid = status, iters, resid
@@ -259,11 +301,23 @@ class ClusterBatch:
         xs = alloc(max(n_obs * self.R * 6 * self.xs_L, 1), dtype=torch.float64, device=dev)
         F = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
         T = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
-        nat.check(L.gb_epilogue_batch(self.nsys, self.sys, self.R, self.mie_off.ctypes.data,
-                                      self.obs_off.ctypes.data, nat.ptr(self.mie_scat), nat.ptr(self.mie_int),
-                                      nat.ptr(self.x), nat.ptr(self.b), float(np.real(eps_b)), int(bool(source)),
-                                      nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
-                                      nat.ptr(T), current_stream(dev)), "epilogue")
+        if self.tmatrix:   # p_scat = T p_inc; no interior coefficients for general particles
+            if self.p_scat is None:
+                self.p_scat = torch.empty_like(self.x)
+            self.p_int = None
+            if self.tmat128 is None:
+                self.tmat128 = self.tmat64.to(torch.complex128)
+            nat.check(L.gb_tmatrix_epilogue_batch(self.nsys, self.sys, self.R, nat.ptr(self.tmat128),
+                                                  self.tm_off.ctypes.data, self.obs_off.ctypes.data, nat.ptr(self.x),
+                                                  nat.ptr(self.b), float(np.real(eps_b)), int(bool(source)),
+                                                  nat.ptr(self.p_scat), nat.ptr(xs), nat.ptr(F), nat.ptr(T),
+                                                  current_stream(dev)), "epilogue")
+        else:
+            nat.check(L.gb_epilogue_batch(self.nsys, self.sys, self.R, self.mie_off.ctypes.data,
+                                          self.obs_off.ctypes.data, nat.ptr(self.mie_scat), nat.ptr(self.mie_int),
+                                          nat.ptr(self.x), nat.ptr(self.b), float(np.real(eps_b)), int(bool(source)),
+                                          nat.ptr(self.p_scat), nat.ptr(self.p_int), nat.ptr(xs), nat.ptr(F),
+                                          nat.ptr(T), current_stream(dev)), "epilogue")
         self.xs, self.F, self.T = xs, F, T
         return self
 

@@ -1,0 +1,170 @@
+"""Clusters of general particles given by their T-matrices.
+
+Mirrors the solve of the reference's ``miepy.cluster`` (cluster.py:629-657): p_src
+from the source, (I + T_agg) p_inc = p_src with the aggregate of
+``particle_aggregate_tmatrix`` (interactions.cpp:417-462, block (i, j) = A_ij T_j),
+p_scat = T p_inc (cluster.py:657, ``einsum("naibj,nbj->nai")``), then cross-sections
+(flux.particle_cross_sections, cluster.py:407-421), forces and torques
+(cluster.py:472-510).  The particle T-matrices are the caller's ([N, 2, rmax, 2,
+rmax], the reference's layout): ``tmatrix_sphere`` for spheres, or T-matrices
+computed elsewhere (the reference's EBCM particle classes, core-shell Mie) for other
+particles.  On the GPU the packed translation blocks A are applied after each
+particle's T-matrix (``gb_solve_batch_tmatrix``); the dense aggregate is not formed.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .cluster import DEFAULT_MAXITER, DEFAULT_TOL, EXACT_TOL, _method_is_exact, cross_sections
+from .engine import ClusterBatch
+from .materials import constant_material
+from .mie import mie_coefficients
+from .modes import lmax_to_rmax
+
+
+def tmatrix_sphere(radius, wavelength, eps, eps_m, lmax, conducting=False):
+    """T-matrix [2, rmax, 2, rmax] of a sphere (tmatrix/common.py:6-28): a_n on the
+    electric and b_n on the magnetic diagonal, for every m of each n."""
+    n_m = np.sqrt(complex(eps_m))
+    k_b = 2 * np.pi * np.real(n_m) / wavelength
+    ms, _ = mie_coefficients(np.atleast_1d(radius), np.atleast_1d(complex(eps)), np.ones(1, complex),
+                             complex(eps_m), 1.0 + 0j, k_b, lmax, np.atleast_1d(conducting))
+    rmax = lmax_to_rmax(lmax)
+    T = np.zeros((2, rmax, 2, rmax), dtype=complex)
+    r = 0
+    for n in range(1, lmax + 1):
+        for _m in range(-n, n + 1):
+            T[0, r, 0, r] = ms[0, 0, n - 1]
+            T[1, r, 1, r] = ms[0, 1, n - 1]
+            r += 1
+    return T
+
+
+class sphere:
+    """A sphere particle for ``cluster`` (particles/sphere.py): position, radius,
+    material; its T-matrix from Mie theory."""
+
+    def __init__(self, position, radius, material):
+        self.position = np.asarray(position, dtype=float)
+        self.radius = float(radius)
+        self.material = material
+        self.tmatrix = None
+
+    def compute_tmatrix(self, lmax, wavelength, eps_m, **kwargs):
+        metal = getattr(self.material, "name", None) == "metal"
+        self.tmatrix = tmatrix_sphere(self.radius, wavelength, self.material.eps(wavelength), eps_m, lmax, metal)
+        return self.tmatrix
+
+
+class tmatrix_cluster:
+    """GMT solve for N particles given by T-matrices [N, 2, rmax, 2, rmax].
+
+    Keywords as the reference's cluster where they apply (source, wavelength, lmax,
+    medium, interactions, method), plus precision ("fp64" default, "mixed", "fp32"),
+    tol, maxiter and device.
+    """
+
+    def __init__(self, *, position, tmatrix, source, wavelength, lmax, medium=None, interactions=True, method=None,
+                 precision="fp64", tol=None, maxiter=None, device=None):
+        self.position = np.asarray(np.atleast_2d(position), dtype=float)
+        N = self.position.shape[0]
+        self.Nparticles = N
+        self.lmax = int(lmax)
+        self.rmax = lmax_to_rmax(self.lmax)
+        self.tmatrix = np.asarray(tmatrix, dtype=complex).reshape(N, 2, self.rmax, 2, self.rmax)
+        self.source = source
+        self.wavelength = wavelength
+        self.medium = medium if medium is not None else constant_material(eps=1.0, mu=1.0)
+        self.eps_b = complex(self.medium.eps(wavelength))
+        self.mu_b = complex(self.medium.mu(wavelength))
+        if self.eps_b.imag != 0 or self.mu_b.imag != 0:
+            raise ValueError("medium must be non-absorbing")
+        self.k_b = 2 * np.pi * np.real(np.sqrt(self.eps_b * self.mu_b)) / wavelength
+        self.interactions, self.method, self.precision = interactions, method, precision
+        self.tol, self.maxiter, self.device = tol, maxiter, device
+        self.solve()
+
+    def _tolerance(self):
+        if self.tol is not None:
+            return float(self.tol)
+        return EXACT_TOL if _method_is_exact(self.method) else DEFAULT_TOL
+
+    def solve(self):
+        N = self.Nparticles
+        self.p_src = np.asarray(self.source.structure(self.position, self.k_b, self.lmax), dtype=complex)
+        spec = dict(position=self.position, tmatrix=self.tmatrix, k=float(self.k_b), p_src=self.p_src)
+        prec = self.precision if self.interactions else "fp64"
+        b = ClusterBatch([spec], R=1, precision=prec, device=self.device)
+        if self.interactions and N > 1:
+            tol = self._tolerance()
+            b.assemble()
+            b.solve(tol=tol, maxiter=self.maxiter or DEFAULT_MAXITER, inner_tol=min(1e-6, max(tol, 1e-7)),
+                    max_refine=8)
+            self.solver_status, self.solver_iterations = int(b.status[0]), int(b.iters[0])
+            self.solver_residual = float(b.resid[0])
+        else:   # no interactions: p_inc = p_src (cluster.py:648-650)
+            b.x.copy_(b.b)
+            self.solver_status, self.solver_iterations, self.solver_residual = 0, 0, 0.0
+        b.epilogue(np.real(self.eps_b), source=True)
+        view = lambda t: b.cluster_view(0, t)[..., 0].cpu().numpy()
+        self.p_inc, self.p_scat = view(b.x), view(b.p_scat)
+        L = self.lmax
+        self._xs = b.xs[: N * 6 * L].view(N, 3, 2, L).cpu().numpy()
+        self._F = b.F[: N * 3].view(N, 3).cpu().numpy()
+        self._T = b.T[: N * 3].view(N, 3).cpu().numpy()
+        self._batch = b
+
+    def cross_sections_per_multipole_of_particle(self, i):
+        C = self._xs[i]
+        return cross_sections(C[0].copy(), C[1].copy(), C[2].copy())
+
+    def cross_sections_of_particle(self, i):
+        return cross_sections(*[float(np.sum(c)) for c in self._xs[i]])
+
+    def cross_sections(self):
+        return cross_sections(*[float(v) for v in self._xs.sum(axis=(0, 2, 3))])
+
+    def force(self):
+        return self._F.copy()
+
+    def torque(self):
+        return self._T.copy()
+
+    def force_on_particle(self, i):
+        return self._F[i].copy()
+
+    def torque_on_particle(self, i):
+        return self._T[i].copy()
+
+
+class cluster(tmatrix_cluster):
+    """The reference's ``miepy.cluster(particles=..., source, wavelength, lmax,
+    medium, interactions, method)`` (cluster.py:16-112): each particle gives its
+    position and ``compute_tmatrix(lmax, wavelength, eps_m)``; particles with equal
+    ``_dict_key`` share one computed T-matrix, as the reference caches them."""
+
+    def __init__(self, *, particles, source, wavelength, lmax, medium=None, origin=None, symmetry=None,
+                 interface=None, interactions=True, method=None, **kw):
+        if interface is not None:
+            raise NotImplementedError("interface with cluster not supported (as the reference)")
+        if symmetry is not None:
+            raise NotImplementedError("symmetries with cluster not supported (as the reference)")
+        self.particles = particles if isinstance(particles, list) else [particles]
+        medium = medium if medium is not None else constant_material(eps=1.0, mu=1.0)
+        eps_m = medium.eps(wavelength)
+        rmax = lmax_to_rmax(lmax)
+        T = np.empty((len(self.particles), 2, rmax, 2, rmax), dtype=complex)
+        cache = {}
+        for i, p in enumerate(self.particles):
+            key = p._dict_key(wavelength) if hasattr(p, "_dict_key") else None
+            if key is not None and key in cache:
+                T[i] = cache[key]
+                continue
+            T[i] = p.compute_tmatrix(lmax, wavelength, eps_m)
+            if key is not None:
+                cache[key] = T[i]
+        self.origin = np.zeros(3) if origin is None else np.asarray(origin, dtype=float)
+        super().__init__(position=[p.position for p in self.particles], tmatrix=T, source=source,
+                         wavelength=wavelength, lmax=lmax, medium=medium, interactions=interactions, method=method,
+                         **kw)

@@ -73,6 +73,7 @@ def _declare(L):
         "orc_vsh_translation": (None, [c_int, c_int, c_int, c_int, c_int, _D, _D, _D, c_double, c_int, _D]),
         "orc_vsh_cache_entry": (None, [c_int] * 4 + [_D, _I, _I, _D, _D]),
         "orc_sphere_aggregate_tmatrix": (None, [c_int, c_int, _D, _D, c_double, _D]),
+        "orc_particle_aggregate_tmatrix": (None, [c_int, c_int, _D, _D, c_double, _D]),
         "orc_reflection_matrix_nia": (None, [c_int, c_int, _D, _D, c_double, c_double, c_double, c_double, _D]),
         "orc_solve_linear_system": (c_int, [c_int, _D, _D, c_int, c_double, c_int, _D, _D]),
         "orc_bicgstab_plain": (c_int, [c_int, _D, _D, c_int, c_double, _D, _D]),
@@ -298,6 +299,21 @@ def sphere_aggregate_tmatrix(positions, mie, k):
     out = np.empty((D, D), dtype=np.complex128)
     lib().orc_sphere_aggregate_tmatrix(N, lmax, _dp(pos), _dp(mie.view(np.float64)), float(np.real(k)),
                                        _dp(out.view(np.float64)))
+    return out
+
+
+def particle_aggregate_tmatrix(positions, tmatrix, k):
+    """positions [N,3], tmatrix [N, 2*rmax, 2*rmax] (or [N,2,rmax,2,rmax]) -> T_agg [D, D]
+    c128 (cpp/src/interactions.cpp:416-462)."""
+    pos = _f64(positions).reshape(-1, 3)
+    N = pos.shape[0]
+    T = _c128(tmatrix).reshape(N, -1)
+    B = int(round(np.sqrt(T.shape[1])))
+    rmax = B // 2
+    D = B * N
+    out = np.empty((D, D), dtype=np.complex128)
+    lib().orc_particle_aggregate_tmatrix(N, rmax, _dp(pos), _dp(np.ascontiguousarray(T).view(np.float64)),
+                                         float(np.real(k)), _dp(out.view(np.float64)))
     return out
 
 

@@ -97,7 +97,7 @@ def build_cpp_module():
     interactions = _module(
         "miepy.cpp.interactions", solver=solver, bicgstab=lambda A, b, maxiter, tolerance: O.bicgstab(A, b, maxiter, tolerance)[0],
         bicgstab_profiled=_bicgstab_profiled, bicgstab_preconditioned_profiled=_not_in_scope,
-        sphere_aggregate_tmatrix=O.sphere_aggregate_tmatrix, particle_aggregate_tmatrix=_not_in_scope,
+        sphere_aggregate_tmatrix=O.sphere_aggregate_tmatrix, particle_aggregate_tmatrix=O.particle_aggregate_tmatrix,
         reflection_matrix_nia=O.reflection_matrix_nia, solve_linear_system=_solve_linear_system,
     )
     forces = _module("miepy.cpp.forces", force=O.force, torque=O.torque, force_all=O.force_all,

@@ -803,6 +803,45 @@ void orc_sphere_aggregate_tmatrix(int N, int lmax, const double* pos, const doub
     }
 }
 
+// interactions.particle_aggregate_tmatrix: cpp/src/interactions.cpp:416-462 with
+// vsh_translation_insert_pair (T-matrix overload), cpp/src/vsh_translation.cpp:53-159:
+// the translation blocks of the pair (the Mie overload's placements with unit Mie
+// coefficients), then agg(i, j) = A(i, j) T_j and agg(j, i) = A(j, i) T_i.
+// positions [N,3] f64, tmatrix [N, 2*rmax, 2*rmax] c128 (row-major), out [D,D] c128.
+void orc_particle_aggregate_tmatrix(int N, int rmax, const double* pos, const double* tmat, double k, double* out) {
+    const int lmax = int(std::lround(std::sqrt(1.0 + rmax) - 1.0));
+    const int B = 2 * rmax, D = B * N;
+    cd* agg = reinterpret_cast<cd*>(out);
+    const cd* T = reinterpret_cast<const cd*>(tmat);
+    for (long e = 0; e < long(D) * D; e++) agg[e] = 0.0;
+    if (N == 1) return;
+    std::vector<cd> A(size_t(D) * D, cd(0.0));
+    std::vector<cd> ones(size_t(N) * 2 * lmax, cd(1.0));
+    const int P = N * (N - 1) / 2;
+    std::vector<int> iv(P), jv(P);
+    int c = 0;
+    for (int i = 0; i < N; i++)
+        for (int j = i + 1; j < N; j++) { iv[c] = i; jv[c] = j; c++; }
+    TranslationCache C = make_cache(lmax);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int ij = 0; ij < P; ij++) {
+        const int i = iv[ij], j = jv[ij];
+        double dx = pos[3 * i] - pos[3 * j], dy = pos[3 * i + 1] - pos[3 * j + 1], dz = pos[3 * i + 2] - pos[3 * j + 2];
+        double rad = std::sqrt(dx * dx + dy * dy + dz * dz);
+        insert_pair(A.data(), D, ones.data(), lmax, i, j, rad, std::acos(dz / rad), std::atan2(dy, dx), k, C);
+        for (int r = 0; r < B; r++)
+            for (int col = 0; col < B; col++) {
+                cd sij = 0, sji = 0;
+                for (int q = 0; q < B; q++) {
+                    sij += A[size_t(i * B + r) * D + j * B + q] * T[(size_t(j) * B + q) * B + col];
+                    sji += A[size_t(j * B + r) * D + i * B + q] * T[(size_t(i) * B + q) * B + col];
+                }
+                agg[size_t(i * B + r) * D + j * B + col] = sij;
+                agg[size_t(j * B + r) * D + i * B + col] = sji;
+            }
+    }
+}
+
 // interactions.reflection_matrix_nia: cpp/src/interactions.cpp:464-512.  Every
 // (i, j) block, i and j over all particles: the outgoing translation from particle
 // j to the mirror image of particle i in the plane z (its z replaced by 2 z - z_i),

@@ -186,6 +186,46 @@ def main():
                         C2=np.array(c2.cross_sections()))
     print("wrote interface_identity")
 
+    # general particles (T-matrix row): the reference's miepy.cluster with a sphere, a
+    # core-shell particle and a particle whose T-matrix is a sphere's plus a dense
+    # random part (every block non-diagonal), solved exactly
+    rng = np.random.default_rng(20240611)
+    lm = 3
+    rm = lm * (lm + 2)
+    base = miepy.tmatrix.tmatrix_sphere(65 * nm, 600 * nm, 3.2 + 0.1j, 1.33 ** 2, lm)
+    T_dense = base + 0.15 * np.abs(base).max() * (rng.standard_normal((2, rm, 2, rm))
+                                                  + 1j * rng.standard_normal((2, rm, 2, rm))) / np.sqrt(2 * rm)
+
+    class fixed_tmatrix_particle(miepy.particles.particle_base.particle):
+        def __init__(self, position, tmatrix):
+            super().__init__(position, None, miepy.constant_material(index=1.8))
+            self._T = tmatrix
+
+        def compute_tmatrix(self, lmax, wavelength, eps_m, **kwargs):
+            self.tmatrix = self.tmatrix_fixed = self._T
+            return self._T
+
+        def _dict_key(self, wavelength):
+            return (fixed_tmatrix_particle, id(self))
+
+    parts = [miepy.sphere([0, 0, 0], 70 * nm, miepy.constant_material(index=1.9 + 0.05j)),
+             miepy.core_shell([220 * nm, 30 * nm, -40 * nm], 50 * nm, 20 * nm, miepy.constant_material(index=0.3 + 3j),
+                              miepy.constant_material(index=1.5)),
+             fixed_tmatrix_particle([-150 * nm, 120 * nm, 70 * nm], T_dense)]
+    c = miepy.cluster(particles=parts, source=miepy.sources.plane_wave([1, 1j]), wavelength=600 * nm, lmax=lm,
+                      medium=miepy.constant_material(index=1.33), method=miepy.solver.exact)
+    md = c.material_data
+    C = c.cross_sections()
+    per = np.array([[np.asarray(v) for v in c.cross_sections_per_multipole_of_particle(i)]
+                    for i in range(c.Nparticles)], dtype=float)
+    np.savez_compressed(os.path.join(HERE, "tmatrix3_lmax3_exact.npz"), position=c.position, tmatrix=c.tmatrix,
+                        wavelength=np.float64(c.wavelength), lmax=np.int64(lm), eps_b=np.complex128(md.eps_b),
+                        mu_b=np.complex128(md.mu_b), k_b=np.float64(np.real(md.k_b)), p_src=c.p_src, p_inc=c.p_inc,
+                        p_scat=c.p_scat, cross_sections=np.array([C.scattering, C.absorption, C.extinction]),
+                        cross_sections_per_multipole=per, force=c.force(), torque=c.torque(),
+                        agg_tmatrix=miepy.interactions.particle_aggregate_tmatrix(c.position, c.tmatrix, md.k_b))
+    print("wrote tmatrix3_lmax3_exact")
+
     # special-function tables for the device recurrences
     from oracle import oracle as O
     z = np.linspace(-0.999, 0.999, 23)
