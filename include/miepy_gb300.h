@@ -90,6 +90,17 @@ int gb_assemble_sphere_dense(int N, int lmax, const double* pos, const double* m
 int gb_reflection_matrix_dense(int N, int lmax, const double* pos, const double* mie, double k, double r_re,
                                double r_im, double z, double* out, void* stream);
 
+/* Aggregate T-matrix of a periodic cluster, in the reference layout: replaces
+ * sphere_aggregate_tmatrix_periodic, src/miepy/interactions.py:153-186.  The
+ * aggregate of gb_assemble_sphere_dense plus, for every ordered particle pair (i, j)
+ * (the particle itself included), the lattice sum over the cells c of
+ * e^{-i k khat.c} times the outgoing translation from pos_j + c to pos_i, times the
+ * Mie coefficient of particle j.  cells [ncell,3] f64 (device; the lattice vectors
+ * of miepy.symmetry's generators, the origin cell excluded), khat = (kx, ky, kz) the
+ * source's unit wave vector.  pos [N,3] f64, mie [N,2,lmax] c128, out [D,D] c128. */
+int gb_aggregate_periodic_dense(int N, int lmax, const double* pos, const double* mie, double k, const double* cells,
+                                int ncell, double kx, double ky, double kz, double* out, void* stream);
+
 /* Packed pair-block translation matrix of one cluster (see above).  Any
  * output may be NULL: out128 [P*B*B] c128; out64 [P*B*B] c64 = fl32(a);
  * out64lo [P*B*B] c64 = fl32(a - fl32(a)) (hi + lo carries ~48 bits). */

@@ -7,7 +7,7 @@ The compute path is the CUDA extension in csrc/, reached through the C ABI of
 include/miepy_gb300.h.
 """
 
-from . import backend, beams, materials as _materials_mod, sources, sweep
+from . import backend, beams, materials as _materials_mod, sources, sweep, symmetry
 from .beams import gaussian_beam
 from .cluster import cross_sections, solver, sphere_cluster
 from .interface import interface

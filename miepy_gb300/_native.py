@@ -46,6 +46,8 @@ SIGNATURES = {
     "gb_tables_export": (c_int, [c_int, _P, _P, _P, _P, _P]),
     "gb_assemble_sphere_dense": (c_int, [c_int, c_int, _P, _P, c_double, _P, _P]),
     "gb_reflection_matrix_dense": (c_int, [c_int, c_int, _P, _P, c_double, c_double, c_double, c_double, _P, _P]),
+    "gb_aggregate_periodic_dense": (c_int, [c_int, c_int, _P, _P, c_double, _P, c_int, c_double, c_double, c_double, _P,
+                                            _P]),
     "gb_assemble_sphere_packed": (c_int, [c_int, c_int, _P, c_double, _P, _P, _P, _P]),
     "gb_assemble_batch": (c_int, [c_int, _P, _P, _P, _P, _P, _P]),
     "gb_expand_mie_batch": (c_int, [c_int, _P, _P, _P, _P, _P]),

@@ -128,6 +128,37 @@ def particle_aggregate_tmatrix(positions, tmatrix, k):
     return out.reshape(N, N, B, B).permute(1, 2, 0, 3).reshape(N, 2, rmax, N, 2, rmax).cpu().numpy()
 
 
+def lattice_cells(symmetry, count=5000):
+    """The cell offsets [ncell, 3] a periodic symmetry sums over (interactions.py:168-169)."""
+    x, y, z = symmetry.generate(count)
+    return np.ascontiguousarray(np.array([x, y, z], dtype=float).T.reshape(-1, 3))
+
+
+def sphere_aggregate_tmatrix_periodic(positions, mie, k, symmetry, k_hat):
+    """positions [N,3], mie [N,2,lmax], k, a periodic symmetry, the source's unit wave
+    vector k_hat -> T_agg [N,2,rmax,N,2,rmax] (interactions.py:153-186): the aggregate
+    plus the lattice sums over symmetry.generate(5000), on the GPU
+    (gb_aggregate_periodic_dense)."""
+    dev = require_cuda()
+    pos = np.ascontiguousarray(np.asarray(positions, dtype=float).reshape(-1, 3))
+    N = pos.shape[0]
+    mie = np.asarray(mie, dtype=complex).reshape(N, 2, -1)
+    lmax = mie.shape[-1]
+    rmax = lmax_to_rmax(lmax)
+    D = 2 * rmax * N
+    cells = lattice_cells(symmetry)
+    kh = np.asarray(k_hat, dtype=float).reshape(3)
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_mie = torch.from_numpy(np.ascontiguousarray(mie)).to(dev)
+    d_cells = torch.from_numpy(cells).to(dev)
+    out = torch.empty(D * D, dtype=torch.complex128, device=dev)
+    nat.check(nat.lib().gb_aggregate_periodic_dense(N, lmax, nat.ptr(d_pos), nat.ptr(d_mie), float(np.real(k)),
+                                                    nat.ptr(d_cells), cells.shape[0], float(kh[0]), float(kh[1]),
+                                                    float(kh[2]), nat.ptr(out), current_stream(dev)),
+              "periodic aggregate")
+    return out.view(N, 2, rmax, N, 2, rmax).cpu().numpy()
+
+
 def reflection_matrix_nia(positions, mie, k, reflected, z):
     """positions [N,3], mie [N,2,lmax], k, reflection coefficient, interface height z ->
     R [N,2,rmax,N,2,rmax] c128 (interactions.py:208-225 / interactions.cpp:464-512),

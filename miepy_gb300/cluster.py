@@ -63,8 +63,6 @@ class sphere_cluster:
     def __init__(self, *, position, radius, material, source, wavelength, lmax, medium=None, origin=None,
                  symmetry=None, interface=None, interactions=True, method=None, precision="fp64", tol=None,
                  maxiter=None, device=None):
-        if symmetry is not None:
-            raise NotImplementedError("periodic symmetry is not on the GPU path yet")
         self.position = np.asarray(np.atleast_2d(position), dtype=float)
         N = self.position.shape[0]
         self.radius = _atleast(radius, N, float)
@@ -141,8 +139,8 @@ class sphere_cluster:
                     p_src=self.p_src)
         prec = self.precision if self.interactions else "fp64"
         b = ClusterBatch([spec], R=1, precision=prec, device=self.device)
-        if self.interactions and self.interface is not None:
-            self._solve_with_interface(b)
+        if self.interactions and (self.interface is not None or self.symmetry is not None):
+            self._solve_dense(b)
         elif self.interactions and self.Nparticles > 1:
             b.assemble()
             b.solve(tol=self._tolerance(), maxiter=self.maxiter or DEFAULT_MAXITER,
@@ -169,10 +167,12 @@ class sphere_cluster:
         self._T = b.T[: self.Nparticles * 3].view(self.Nparticles, 3).cpu().numpy()
         self._F_nosrc = self._T_nosrc = None
 
-    def _solve_with_interface(self, b):
-        """(I + T_agg - R) p_inc = p_src on the dense reference layout: the aggregate
-        T-matrix (gb_assemble_sphere_dense) minus the interface's reflection matrix
-        (gb_reflection_matrix_dense), as sphere_cluster.py:694-712; BiCGSTAB
+    def _solve_dense(self, b):
+        """(I + T_agg - R) p_inc = p_src on the dense reference layout, as
+        sphere_cluster.py:694-712: the aggregate T-matrix (gb_assemble_sphere_dense),
+        or with a periodic symmetry the aggregate plus its lattice sums
+        (gb_aggregate_periodic_dense), minus the interface's reflection matrix
+        (gb_reflection_matrix_dense) when there is one; BiCGSTAB
         (gb_solve_dense) or, for solver.exact, an LU solve."""
         L = nat.lib()
         dev, st = b.device, current_stream(b.device)
@@ -182,14 +182,25 @@ class sphere_cluster:
         nat.check(L.gb_expand_mie_batch(b.nsys, b.sys, b.mie_off.ctypes.data, nat.ptr(b.mie_scat), nat.ptr(b.tvec),
                                         st), "expand mie")
         T = torch.empty(D * D, dtype=torch.complex128, device=dev)
-        nat.check(L.gb_assemble_sphere_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k, nat.ptr(T), st),
-                  "dense assembly")
-        Rm = torch.empty_like(T)
-        r0 = complex(self.interface.reflection_coefficients(0, self.wavelength, self.medium)[0])
-        nat.check(L.gb_reflection_matrix_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k, r0.real, r0.imag,
-                                               float(self.interface.z), nat.ptr(Rm), st), "reflection matrix")
-        T -= Rm
-        del Rm
+        if self.symmetry is not None:   # sphere_cluster.py:699-702
+            from .backend import lattice_cells
+            cells = lattice_cells(self.symmetry)
+            kh = np.asarray(self.source.k_hat, dtype=float).reshape(3)
+            d_cells = torch.from_numpy(cells).to(dev)
+            nat.check(L.gb_aggregate_periodic_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k,
+                                                    nat.ptr(d_cells), cells.shape[0], float(kh[0]), float(kh[1]),
+                                                    float(kh[2]), nat.ptr(T), st), "periodic aggregate")
+        else:
+            nat.check(L.gb_assemble_sphere_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k, nat.ptr(T), st),
+                      "dense assembly")
+        if self.interface is not None:
+            Rm = torch.empty_like(T)
+            r0 = complex(self.interface.reflection_coefficients(0, self.wavelength, self.medium)[0])
+            nat.check(L.gb_reflection_matrix_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.mie_scat), k, r0.real,
+                                                   r0.imag, float(self.interface.z), nat.ptr(Rm), st),
+                      "reflection matrix")
+            T -= Rm
+            del Rm
         if _method_is_exact(self.method):
             A = T.view(D, D) + torch.eye(D, dtype=torch.complex128, device=dev)
             b.x.copy_(torch.linalg.solve(A, b.b[:D]))

@@ -169,16 +169,31 @@ struct Refl {
     double2 r0 = {0, 0};
 };
 
+// Periodic lattice (sphere_aggregate_tmatrix_periodic, interactions.py:153-186):
+// block (i, j) gains sum_c e^{-i k khat.c} A(pos_i - pos_j - c) mie_j over the
+// lattice cells c (cells [ncell][3], device).  Groups hold PB cells of one ordered
+// pair (gpp groups per pair); each group sums its phase-weighted tuple values in
+// shared memory and adds its block to the dense output with one atomic add per
+// entry.
+struct Latt {
+    const double* cells = nullptr;
+    int ncell = 0;
+    int gpp = 1;
+    double kx = 0, ky = 0, kz = 0;
+};
+
 // FP64_SUMS: tuple sums in FP64 (complex128 or dense output); otherwise in
 // double-float on the FP32 pipes, straight to the complex64 hi / lo outputs.
-// REFL: the dense reflection matrix instead of the aggregate T-matrix.
-template <bool DENSE, bool FP64_SUMS, bool REFL = false>
+// MODE 0: the aggregate T-matrix; 1: the dense reflection matrix (Refl); 2: the
+// lattice sums of a periodic cluster, added to a dense output (Latt).
+template <bool DENSE, bool FP64_SUMS, int MODE = 0>
 __global__ void __launch_bounds__(kAsmThreads, 3)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
            int Lmax, int Mmax, int PB, const double* __restrict__ pos, const double2* __restrict__ mie,
            double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
-           Refl refl = Refl()) {
-    static_assert(!REFL || (DENSE && FP64_SUMS), "the reflection matrix is a dense FP64 output");
+           Refl refl = Refl(), Latt latt = Latt()) {
+    constexpr bool REFL = MODE == 1, LATT = MODE == 2;
+    static_assert(MODE == 0 || (DENSE && FP64_SUMS), "reflection and lattice sums are dense FP64 outputs");
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
@@ -198,9 +213,19 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         const gb::SysDev S = sys[s];
         const int L = S.lmax, B = S.B, N = S.N;
         const int PM = 2 * L + 2, MU = 4 * L + 1;
-        const long long p_first = (g - grp_base[s]) * (long long)PB;
-        const long long Ptot = REFL ? (long long)N * N : S.P;   // all ordered pairs for the reflection
-        const int np = (int)min((long long)PB, Ptot - p_first);
+        const long long gl = g - grp_base[s];
+        const long long p_first = gl * (long long)PB;
+        long long lat_pair = 0;   // lattice: the ordered pair (i, j) = (lat_pair / N, lat_pair % N) ...
+        int lat_c0 = 0;           // ... and the group's first cell
+        int np;
+        if constexpr (LATT) {
+            lat_pair = gl / latt.gpp;
+            lat_c0 = (int)(gl - lat_pair * latt.gpp) * PB;
+            np = min(PB, latt.ncell - lat_c0);
+        } else {
+            const long long Ptot = REFL ? (long long)N * N : S.P;   // all ordered pairs for the reflection
+            np = (int)min((long long)PB, Ptot - p_first);
+        }
 
         // ---- phase 1a: one thread per pair: geometry, then h_p(kr) by the upward
         // j/y recurrence of spherical_hn_recursion (cpp/src/special.cpp:90-111).  The
@@ -208,7 +233,15 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // separation vector (the reference goes through acos/atan2 and back).
         if (tid < np) {
             int i, j;
-            if (REFL) {
+            double lx = 0.0, ly = 0.0, lz = 0.0;   // lattice: the cell that holds the image of particle j
+            if (LATT) {
+                i = (int)(lat_pair / N);
+                j = (int)(lat_pair % N);
+                const double* c = latt.cells + 3 * (long long)(lat_c0 + tid);
+                lx = c[0];
+                ly = c[1];
+                lz = c[2];
+            } else if (REFL) {
                 i = (int)((p_first + tid) / N);
                 j = (int)((p_first + tid) % N);
             } else {
@@ -217,7 +250,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             const double* pi_ = pos + S.pos_off + 3 * (long long)i;
             const double* pj_ = pos + S.pos_off + 3 * (long long)j;
             const double zi = REFL ? 2.0 * refl.z - pi_[2] : pi_[2];   // mirror image of particle i
-            const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = zi - pj_[2];
+            const double dx = pi_[0] - (pj_[0] + lx), dy = pi_[1] - (pj_[1] + ly), dz = zi - (pj_[2] + lz);
             const double rho2 = dx * dx + dy * dy;
             const double rad = sqrt(rho2 + dz * dz);
             const double inv_r = 1.0 / rad;
@@ -233,6 +266,12 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             ge[1] = rho * inv_r;                            // sin(theta) >= 0
             ge[2] = cphi;
             ge[3] = sphi;
+            if (LATT) {   // the Bloch phase e^{-i k khat.c} of the cell
+                double sp, cp;
+                sincos(-S.k * (latt.kx * lx + latt.ky * ly + latt.kz * lz), &sp, &cp);
+                ge[4] = cp;
+                ge[5] = sp;
+            }
             const double z = S.k * rad;
             const double inv_z = 1.0 / z;
             double sz, cz;
@@ -396,8 +435,20 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                         sb.y = fma(c, gv.y, sb.y);
                     }
                     const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
-                    tv[2 * t] = At;
-                    tv[2 * t + 1] = Bt;
+                    if constexpr (LATT) {   // this thread's running sums over the group's cells (buffer 0)
+                        const double2 ph = make_double2(geo[8 * pp + 4], geo[8 * pp + 5]);
+                        const double2 a = cmul(ph, At), b = cmul(ph, Bt);
+                        if (pp == 0) {
+                            Tv[2 * t] = a;
+                            Tv[2 * t + 1] = b;
+                        } else {
+                            Tv[2 * t] = make_double2(Tv[2 * t].x + a.x, Tv[2 * t].y + a.y);
+                            Tv[2 * t + 1] = make_double2(Tv[2 * t + 1].x + b.x, Tv[2 * t + 1].y + b.y);
+                        }
+                    } else {
+                        tv[2 * t] = At;
+                        tv[2 * t + 1] = Bt;
+                    }
                     if (!DENSE && want64) {
                         const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
                         const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
@@ -492,6 +543,27 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 }
             }
         };
+        if constexpr (LATT) {
+            // every thread sums its own tuples over the group's cells, then the group's
+            // share of block (i, j), times mie(j, b, v), is added to the dense output
+            for (int pp = 0; pp < np; pp++) tuples(pp, 0);
+            __syncthreads();
+            const int i = (int)(lat_pair / N), j = (int)(lat_pair % N);
+            const double2* mj_ = mie + (long long)j * 2 * L;
+            for (int e = tid; e < B * B; e += kAsmThreads) {
+                const int R = e / B, C = e % B;
+                const int code = __ldg(S.elem_map + e);
+                const unsigned neg = code & 1;
+                double2 v = Tv[code >> 1];
+                v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
+                const double2 w = cmul(v, mj_[__ldg(S.miecol + C)]);
+                double* o = reinterpret_cast<double*>(out128 + ((long long)i * B + R) * dense_ld + (long long)j * B + C);
+                atomicAdd(o, w.x);
+                atomicAdd(o + 1, w.y);
+            }
+            __syncthreads();   // the next group rewrites the tables and the sums
+            continue;
+        }
         tuples(0, 0);
         __syncthreads();
         for (int pp = 0; pp < np; pp++) {
@@ -634,7 +706,7 @@ namespace {
 
 int launch_assemble(int nsys, const gb_system* sys, const double* pos, const double* mie, double* out128,
                     float* out64, float* out64lo, long long dense_ld, bool dense, cudaStream_t stream,
-                    const Refl* refl = nullptr) {
+                    const Refl* refl = nullptr, const Latt* latt = nullptr) {
     std::vector<gb::SysDev> sd;
     int st = gb::make_sysdev(nsys, sys, stream, sd);
     if (st) return st;
@@ -643,7 +715,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     for (int s = 0; s < nsys; s++) {
         Lmax = std::max(Lmax, sd[s].lmax);
         Mmax = std::max(Mmax, sd[s].M);
-        total_pairs += refl ? (long long)sd[s].N * sd[s].N : sd[s].P;
+        total_pairs += (refl || latt) ? (long long)sd[s].N * sd[s].N : sd[s].P;
     }
     if (total_pairs == 0) return GB_OK;
     const bool fp64_sums = dense || out128 != nullptr;
@@ -655,10 +727,15 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     const AsmSmem lay = asm_layout(Lmax, Mmax, PB, fp64_sums, want64);
     const size_t smem = lay.total;
     if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
+    Latt lt = latt ? *latt : Latt();
+    if (latt) {
+        if (lt.ncell < 1) return GB_OK;
+        lt.gpp = (lt.ncell + PB - 1) / PB;
+    }
     std::vector<long long> gbase(nsys + 1, 0);
     for (int s = 0; s < nsys; s++) {
         const long long np_s = refl ? (long long)sd[s].N * sd[s].N : sd[s].P;
-        gbase[s + 1] = gbase[s] + (np_s + PB - 1) / PB;
+        gbase[s + 1] = gbase[s] + (latt ? (long long)sd[s].N * sd[s].N * lt.gpp : (np_s + PB - 1) / PB);
     }
     const long long ngroups = gbase[nsys];
     // one staging upload: descriptors then group prefix sums
@@ -671,8 +748,9 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     if (st) return st;
     const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
     const long long* dbase = reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys);
-    auto kfn = refl ? k_assemble<true, true, true>
-                    : (dense ? k_assemble<true, true> : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>));
+    auto kfn = latt ? k_assemble<true, true, 2>
+                    : refl ? k_assemble<true, true, 1>
+                           : (dense ? k_assemble<true, true> : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>));
     GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
     int per_sm = 1;
     GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
@@ -682,7 +760,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
     kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
         dsys, nsys, dbase, ngroups, Lmax, Mmax, PB, pos, reinterpret_cast<const double2*>(mie),
         reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
-        dense_ld, refl ? *refl : Refl());
+        dense_ld, refl ? *refl : Refl(), lt);
     GB_CUDA_TRY(cudaGetLastError());
     return gb::stage_release(slot, stream);
 }
@@ -713,6 +791,27 @@ int gb_reflection_matrix_dense(int N, int lmax, const double* pos, const double*
     r.z = z;
     r.r0 = make_double2(r_re, r_im);
     return launch_assemble(1, &s, pos, mie, out, nullptr, nullptr, D, true, (cudaStream_t)stream, &r);
+}
+
+int gb_aggregate_periodic_dense(int N, int lmax, const double* pos, const double* mie, double k, const double* cells,
+                                int ncell, double kx, double ky, double kz, double* out, void* stream) {
+    if (!pos || !mie || !out || (ncell > 0 && !cells)) return gb_set_error(GB_BAD_ARG, "null pointer");
+    if (N < 1 || lmax < 1 || lmax > GB_LMAX_MAX || ncell < 0)
+        return gb_set_error(GB_BAD_ARG, "N=%d lmax=%d ncell=%d invalid", N, lmax, ncell);
+    const long long D = 2LL * lmax_to_rmax(lmax) * N;
+    GB_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double2) * D * D, (cudaStream_t)stream));
+    gb_system s{N, lmax, k, 0, 0, 0, 0};
+    if (N > 1) {
+        const int e = launch_assemble(1, &s, pos, mie, out, nullptr, nullptr, D, true, (cudaStream_t)stream);
+        if (e) return e;
+    }
+    Latt lt;
+    lt.cells = cells;
+    lt.ncell = ncell;
+    lt.kx = kx;
+    lt.ky = ky;
+    lt.kz = kz;
+    return launch_assemble(1, &s, pos, mie, out, nullptr, nullptr, D, true, (cudaStream_t)stream, nullptr, &lt);
 }
 
 int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,

@@ -75,6 +75,7 @@ def _declare(L):
         "orc_sphere_aggregate_tmatrix": (None, [c_int, c_int, _D, _D, c_double, _D]),
         "orc_particle_aggregate_tmatrix": (None, [c_int, c_int, _D, _D, c_double, _D]),
         "orc_reflection_matrix_nia": (None, [c_int, c_int, _D, _D, c_double, c_double, c_double, c_double, _D]),
+        "orc_sphere_aggregate_tmatrix_periodic": (None, [c_int, c_int, _D, _D, c_double, c_int, _D, _D, _D]),
         "orc_solve_linear_system": (c_int, [c_int, _D, _D, c_int, c_double, c_int, _D, _D]),
         "orc_bicgstab_plain": (c_int, [c_int, _D, _D, c_int, c_double, _D, _D]),
         "orc_gemv": (None, [c_int, _D, _D, _D]),
@@ -330,6 +331,23 @@ def reflection_matrix_nia(positions, mie, k, reflection, z):
     r = complex(reflection)
     lib().orc_reflection_matrix_nia(N, lmax, _dp(pos), _dp(mie.view(np.float64)), float(np.real(k)), r.real, r.imag,
                                     float(z), _dp(out.view(np.float64)))
+    return out
+
+
+def sphere_aggregate_tmatrix_periodic(positions, mie, k, cells, k_hat):
+    """Aggregate T-matrix of a periodic cluster (src/miepy/interactions.py:153-186):
+    positions [N,3], mie [N,2,lmax], the lattice cells [ncell,3] (the symmetry's
+    generate(5000) in the reference), the source's unit wave vector k_hat -> [D, D] c128."""
+    pos = _f64(positions).reshape(-1, 3)
+    N = pos.shape[0]
+    mie = _c128(mie).reshape(N, -1)
+    lmax = mie.shape[1] // 2
+    D = 2 * lmax * (lmax + 2) * N
+    cells = _f64(cells).reshape(-1, 3)
+    out = np.empty((D, D), dtype=np.complex128)
+    lib().orc_sphere_aggregate_tmatrix_periodic(N, lmax, _dp(pos), _dp(mie.view(np.float64)), float(np.real(k)),
+                                                cells.shape[0], _dp(cells), _dp(_f64(k_hat).reshape(3)),
+                                                _dp(out.view(np.float64)))
     return out
 
 

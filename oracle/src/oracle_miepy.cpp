@@ -882,6 +882,55 @@ void orc_reflection_matrix_nia(int N, int lmax, const double* pos, const double*
     }
 }
 
+// interactions.sphere_aggregate_tmatrix_periodic: src/miepy/interactions.py:153-186.
+// The aggregate of orc_sphere_aggregate_tmatrix, then for every ordered pair (i, j)
+// and every mode pair the lattice sum over the cells c of the outgoing translation
+// (orc_vsh_translation) from pos_j + c to pos_i, times e^{-i k khat.c}, times
+// mie(j, b, v).  cells [ncell,3], khat [3].
+void orc_sphere_aggregate_tmatrix_periodic(int N, int lmax, const double* pos, const double* mie, double k, int ncell,
+                                           const double* cells, const double* khat, double* out) {
+    orc_sphere_aggregate_tmatrix(N, lmax, pos, mie, k, out);
+    if (ncell < 1) return;
+    const int rmax = lmax_to_rmax(lmax);
+    const int D = 2 * rmax * N;
+    cd* agg = reinterpret_cast<cd*>(out);
+    const cd* M = reinterpret_cast<const cd*>(mie);
+    std::vector<cd> phase(ncell);
+    for (int c = 0; c < ncell; c++)
+        phase[c] = std::exp(cd(0, -k * (khat[0] * cells[3 * c] + khat[1] * cells[3 * c + 1] + khat[2] * cells[3 * c + 2])));
+#pragma omp parallel for collapse(2) schedule(dynamic, 1)
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) {
+            std::vector<double> rad(ncell), theta(ncell), phi(ncell), tr(4 * size_t(ncell));
+            for (int c = 0; c < ncell; c++) {
+                const double dx = pos[3 * i] - (cells[3 * c] + pos[3 * j]);
+                const double dy = pos[3 * i + 1] - (cells[3 * c + 1] + pos[3 * j + 1]);
+                const double dz = pos[3 * i + 2] - (cells[3 * c + 2] + pos[3 * j + 2]);
+                rad[c] = std::sqrt(dx * dx + dy * dy + dz * dz);
+                theta[c] = std::acos(dz / rad[c]);
+                phi[c] = std::atan2(dy, dx);
+            }
+            for (int n = 1; n <= lmax; n++)
+                for (int m = -n; m <= n; m++)
+                    for (int v = 1; v <= lmax; v++)
+                        for (int u = -v; u <= v; u++) {
+                            orc_vsh_translation(ncell, m, n, u, v, rad.data(), theta.data(), phi.data(), k, 0, tr.data());
+                            cd sA = 0, sB = 0;
+                            for (int c = 0; c < ncell; c++) {
+                                sA += cd(tr[4 * c], tr[4 * c + 1]) * phase[c];
+                                sB += cd(tr[4 * c + 2], tr[4 * c + 3]) * phase[c];
+                            }
+                            const cd tsum[2] = {sA, sB};
+                            for (int a = 0; a < 2; a++)
+                                for (int b = 0; b < 2; b++) {
+                                    const long idx = long(i) * 2 * rmax + a * rmax + n * (n + 2) - n + m - 1;
+                                    const long idy = long(j) * 2 * rmax + b * rmax + v * (v + 2) - v + u - 1;
+                                    agg[idx * D + idy] += tsum[(a + b) % 2] * M[long(j) * 2 * lmax + b * lmax + v - 1];
+                                }
+                        }
+        }
+}
+
 // interactions.solve_linear_system: cpp/src/interactions.cpp:347-368.
 // method 0 = bicgstab (Eigen, tol/maxiter), 1 = exact (partial-pivot LU).
 // T is the aggregate T-matrix WITHOUT the identity.  Returns iterations (bicgstab),

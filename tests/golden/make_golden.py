@@ -226,6 +226,33 @@ def main():
                         agg_tmatrix=miepy.interactions.particle_aggregate_tmatrix(c.position, c.tmatrix, md.k_b))
     print("wrote tmatrix3_lmax3_exact")
 
+    # periodic clusters (lattice row): the reference's own lattice sums
+    # (interactions.sphere_aggregate_tmatrix_periodic over symmetry.generate(5000))
+    # and sphere_cluster(symmetry=...) solves: a dimer in a square lattice under an
+    # oblique plane wave, and one sphere in a chain along x
+    for name, sym, pos, rad, lm, src in [
+            ("periodic_square_dimer_lmax2", miepy.symmetry.square_lattice_2d(700 * nm),
+             [[-120 * nm, 20 * nm, 0], [130 * nm, -40 * nm, 30 * nm]], [70 * nm, 60 * nm], 2,
+             miepy.sources.plane_wave([1, 0.5j], theta=0.35, phi=0.6)),
+            ("periodic_chain_single_lmax3", miepy.symmetry.x_translation_1d(450 * nm), [[0, 0, 0]], [80 * nm], 3,
+             miepy.sources.plane_wave([0, 1], theta=0.5, phi=0.0))]:
+        c = miepy.sphere_cluster(position=pos, radius=rad, material=miepy.constant_material(index=1.8 + 0.02j),
+                                 medium=miepy.constant_material(index=1.33), source=src, wavelength=620 * nm, lmax=lm,
+                                 symmetry=sym, method=miepy.solver.exact)
+        md = c.material_data
+        xs_, ys_, zs_ = sym.generate(5000)
+        C = c.cross_sections()
+        agg = miepy.interactions.sphere_aggregate_tmatrix_periodic(c.position, c.mie_scat, md.k_b, sym,
+                                                                   src.k_hat)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), position=c.position, radius=c.radius,
+                            wavelength=np.float64(c.wavelength), lmax=np.int64(lm), k_b=np.float64(np.real(md.k_b)),
+                            eps=np.asarray(md.eps, complex), k_hat=np.asarray(src.k_hat, float),
+                            cells=np.array([xs_, ys_, zs_]).T, mie_scat=c.mie_scat, mie_int=c.mie_int, p_src=c.p_src,
+                            p_inc=c.p_inc, p_scat=c.p_scat, p_int=c.p_int, agg_tmatrix=agg,
+                            cross_sections=np.array([C.scattering, C.absorption, C.extinction]), force=c.force(),
+                            torque=c.torque())
+        print("wrote", name)
+
     # special-function tables for the device recurrences
     from oracle import oracle as O
     z = np.linspace(-0.999, 0.999, 23)
