@@ -38,7 +38,14 @@ def _is_exact(method):
 
 
 class DeviceAggregateTMatrix:
-    """Aggregate T-matrix of a sphere cluster held on the GPU in packed form."""
+    """Aggregate T-matrix of a sphere cluster held on the GPU in packed form.
+
+    The reference edits the aggregate in two places: sphere_cluster.py:704-710
+    subtracts the interface's reflection matrix (``agg -= R``) and
+    interactions.py:172-184 adds lattice sums entry by entry.  Arithmetic returns
+    the dense matrix as a host array; item access works on a dense host copy made
+    on first use, which solve_linear_system_jax then solves on the device.
+    """
 
     def __init__(self, positions, mie, k):
         self.positions = np.asarray(positions, dtype=float).reshape(-1, 3)
@@ -54,6 +61,7 @@ class DeviceAggregateTMatrix:
         self._batch = ClusterBatch([dict(position=self.positions, mie_scat=self.mie.reshape(self.N, 2, self.lmax),
                                          k=self.k, p_src=zeros)], R=1, precision="fp64")
         self._batch.assemble()
+        self._hold = [None]   # dense host copy (shared with reshaped views), once entries are read or edited
 
     @property
     def size(self):
@@ -80,14 +88,40 @@ class DeviceAggregateTMatrix:
                                                      nat.ptr(out), current_stream(dev)), "dense assembly")
         return out
 
+    @property
+    def _host(self):
+        return self._hold[0]
+
     def __array__(self, dtype=None, copy=None):
-        a = self.dense_device().cpu().numpy().reshape(self.shape)
+        if self._host is not None:
+            a = self._host.reshape(self.shape)
+        else:
+            a = self.dense_device().cpu().numpy().reshape(self.shape)
         return a.astype(dtype) if dtype is not None else a
 
-    def __sub__(self, other):
-        raise NotImplementedError("substrate reflection matrices are not on the GPU path yet")
+    def _entries(self):
+        if self._host is None:
+            self._hold[0] = self.dense_device().cpu().numpy()
+        return self._host.reshape(self.shape)
 
+    def __getitem__(self, key):
+        return self._entries()[key]
+
+    def __setitem__(self, key, value):
+        self._entries()[key] = value
+
+    def __sub__(self, other):
+        return np.asarray(self) - np.asarray(other)
+
+    def __add__(self, other):
+        return np.asarray(self) + np.asarray(other)
+
+    def __rsub__(self, other):
+        return np.asarray(other) - np.asarray(self)
+
+    __radd__ = __add__
     __isub__ = __sub__
+    __iadd__ = __add__
 
 
 def sphere_aggregate_tmatrix_jax(positions, mie, k):
@@ -186,7 +220,7 @@ def solve_linear_system_jax(agg_tmatrix, p_src, method):
     p_src = np.asarray(p_src, dtype=complex)
     N, rmax = p_src.shape[0], p_src.shape[-1]
     tol = EXACT_TOL if _is_exact(method) else BICGSTAB_TOL
-    if isinstance(agg_tmatrix, DeviceAggregateTMatrix):
+    if isinstance(agg_tmatrix, DeviceAggregateTMatrix) and agg_tmatrix._host is None:
         b = agg_tmatrix._batch
         b.b.copy_(torch.from_numpy(p_src.reshape(-1)).to(b.device))
         b.solve(tol=tol, maxiter=1000)

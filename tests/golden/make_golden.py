@@ -253,6 +253,21 @@ def main():
                             torque=c.torque())
         print("wrote", name)
 
+    # a periodic dimer above an interface: the lattice sums minus the reflection
+    # matrix (sphere_cluster.py:694-710 with both options)
+    sym = miepy.symmetry.square_lattice_2d(650 * nm)
+    sub = miepy.interface(miepy.constant_material(index=1.6), z=-150 * nm)
+    c = miepy.sphere_cluster(position=[[-100 * nm, 0, 0], [120 * nm, 30 * nm, 20 * nm]], radius=[70 * nm, 60 * nm],
+                             material=miepy.constant_material(index=2.0 + 0.05j),
+                             medium=miepy.constant_material(index=1.33), source=miepy.sources.plane_wave([1, 0]),
+                             wavelength=640 * nm, lmax=2, symmetry=sym, interface=sub, method=miepy.solver.exact)
+    C = c.cross_sections()
+    np.savez_compressed(os.path.join(HERE, "periodic_interface_dimer_lmax2.npz"), position=c.position,
+                        radius=c.radius, wavelength=np.float64(c.wavelength), p_src=c.p_src, p_inc=c.p_inc,
+                        p_scat=c.p_scat, cross_sections=np.array([C.scattering, C.absorption, C.extinction]),
+                        force=c.force(), torque=c.torque())
+    print("wrote periodic_interface_dimer_lmax2")
+
     # special-function tables for the device recurrences
     from oracle import oracle as O
     z = np.linspace(-0.999, 0.999, 23)

@@ -300,6 +300,28 @@ def test_plugin_backend_functions():
     assert np.all(np.asarray(one) == 0)
 
 
+def test_plugin_aggregate_edited_like_the_reference():
+    """The reference edits the plugin's aggregate: ``agg -= R`` for an interface
+    (sphere_cluster.py:704-710) and entry-wise ``agg[i, a, r, j, b, s] += ...`` for
+    lattice sums (interactions.py:172-184).  Both give the reference's solutions."""
+    from miepy_gb300 import backend
+    from oracle import oracle as O
+    g = G.load("interface3_lmax3_exact")
+    T = backend.sphere_aggregate_tmatrix_jax(g["position"], g["mie_scat"], g["k_b"])
+    T -= g["reflection_matrix"]
+    p = backend.solve_linear_system_jax(T, g["p_src"], gb.solver.exact)
+    assert rel(p, g["p_inc"]) < 1e-10
+    g = G.load("periodic_square_dimer_lmax2")
+    T = backend.sphere_aggregate_tmatrix_jax(g["position"], g["mie_scat"], g["k_b"])
+    lattice = g["agg_tmatrix"] - O.sphere_aggregate_tmatrix(g["position"], g["mie_scat"], g["k_b"]).reshape(T.shape)
+    for i in range(2):
+        for j in range(2):
+            T[i, :, :, j, :, :] += lattice[i, :, :, j, :, :]
+    assert rel(np.asarray(T), g["agg_tmatrix"]) < 1e-12
+    p = backend.solve_linear_system_jax(T, g["p_src"], gb.solver.exact)
+    assert rel(p, g["p_inc"]) < 1e-10
+
+
 def test_full_size_random_cluster_residual():
     """N = 200, lmax = 4 (D = 9600), two polarisations: the FP64 solution satisfies
     the oracle's own matrix equation (a size-independent check)."""

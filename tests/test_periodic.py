@@ -95,3 +95,21 @@ def test_periodic_sphere_cluster(name, method):
     np.testing.assert_allclose([C.scattering, C.absorption, C.extinction], g["cross_sections"], rtol=1e-9)
     assert rel(c.force(), g["force"]) < 1e-9
     assert rel(c.torque(), g["torque"]) < 1e-9
+
+
+@pytest.mark.gpu
+def test_periodic_cluster_above_an_interface():
+    """symmetry= and interface= together: the lattice sums minus the reflection
+    matrix (sphere_cluster.py:694-710), against the reference's own solve."""
+    import miepy_gb300 as gb
+    g = G.load("periodic_interface_dimer_lmax2")
+    c = gb.sphere_cluster(position=g["position"], radius=g["radius"], material=gb.constant_material(index=2.0 + 0.05j),
+                          medium=gb.constant_material(index=1.33), source=gb.plane_wave([1, 0]),
+                          wavelength=float(g["wavelength"]), lmax=2, symmetry=gb.symmetry.square_lattice_2d(650 * nm),
+                          interface=gb.interface(gb.constant_material(index=1.6), z=-150 * nm), method=gb.solver.exact)
+    assert rel(c.p_src, g["p_src"]) < 1e-12
+    assert rel(c.p_inc, g["p_inc"]) < 1e-10
+    C = c.cross_sections()
+    np.testing.assert_allclose([C.scattering, C.absorption, C.extinction], g["cross_sections"], rtol=1e-9)
+    assert rel(c.force(), g["force"]) < 1e-9
+    assert rel(c.torque(), g["torque"]) < 1e-9

@@ -201,3 +201,46 @@ def test_tmatrix_batch_load_reuses_like_a_fresh_one(precision):
     with pytest.raises(ValueError):
         reused.load([dict(position=b["position"], mie_scat=np.zeros((7, 2, 3), complex), k=b["k"],
                           p_src=b["p_src"])])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-11, 1e-9), ("mixed", 1e-11, 1e-8), ("fp32", 1e-5, 1e-3)])
+def test_tmatrix_batch_of_clusters_with_two_rhs(precision, tol, bound):
+    """Two clusters of different N and lmax in one batch, two right-hand sides each,
+    dense random T-matrices: against the oracle's dense aggregate and an LU solve."""
+    from miepy_gb300 import ClusterBatch, plane_wave
+    from oracle import oracle as O
+    rng = np.random.default_rng(9)
+    specs = []
+    for seed, N, lmax in [(31, 6, 3), (32, 9, 2)]:
+        pos, _, _, mie, k = random_cluster(seed, N=N, lmax=lmax)
+        rmax = lmax * (lmax + 2)
+        shape = (N, 2, rmax, 2, rmax)
+        T = sphere_tmatrices(mie) + 0.02 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+        p_src = np.stack([plane_wave([1, 0]).structure(pos, k, lmax), plane_wave([0, 1]).structure(pos, k, lmax)],
+                         axis=-1)
+        specs.append(dict(position=pos, tmatrix=T, k=k, p_src=p_src))
+    b = ClusterBatch(specs, R=2, precision=precision).assemble()
+    b.solve(tol=tol, inner_tol=1e-6)
+    b.epilogue(1.33 ** 2)
+    assert np.all(b.status == 0)
+    for q, sp in enumerate(specs):
+        A = O.particle_aggregate_tmatrix(sp["position"], sp["tmatrix"], sp["k"])
+        D = A.shape[0]
+        x_ref = np.linalg.solve(np.eye(D) + A, sp["p_src"].reshape(D, 2))
+        x = b.cluster_view(q, b.x).cpu().numpy().reshape(D, 2)
+        assert rel(x, x_ref) < bound
+        p_scat = np.einsum("naibj,nbjr->nair", sp["tmatrix"], x_ref.reshape(sp["p_src"].shape))
+        assert rel(b.cluster_view(q, b.p_scat).cpu().numpy(), p_scat) < bound
+
+
+@pytest.mark.gpu
+def test_cluster_without_interactions():
+    """interactions=False: p_inc = p_src and p_scat = T p_src (cluster.py:648-650)."""
+    import miepy_gb300 as gb
+    g = fixture()
+    parts = [fixed_particle(g["position"][i], g["tmatrix"][i]) for i in range(3)]
+    c = gb.cluster(particles=parts, source=gb.plane_wave([1, 1j]), wavelength=float(g["wavelength"]), lmax=3,
+                   medium=gb.constant_material(index=1.33), interactions=False)
+    assert rel(c.p_inc, g["p_src"]) < 1e-12
+    assert rel(c.p_scat, np.einsum("naibj,nbj->nai", g["tmatrix"], g["p_src"])) < 1e-12
