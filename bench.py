@@ -646,7 +646,8 @@ def main():
             cpu = dict(value=1.0 / info["seconds"], unit="solves/s", cores=info["cores"], kind="port",
                        sample="1 full solve of the workload (assembly + 2 BiCGSTAB solves + epilogue) on the oracle",
                        assembly_s=info["assembly_s"], iterations=info["iterations"])
-        line = dict(base, impl="gb300", dtype="c64 BiCGSTAB + double-float (c64 hi+lo) refinement residual",
+        line = dict(base, impl="gb300", dtype="c64 BiCGSTAB + double-float (c64 hi+lo) refinement residual, "
+                                             "c64 incremental residual once |r| <= 2.5e4 tol |b|",
                     gpu_launches=res.pop("gpu_launches_total"), cpu_baseline=cpu, **res)
         print(json.dumps(line))
     if world > 1:

@@ -61,6 +61,11 @@ constexpr int kGemvThreads = 128;  // 4 warps
 constexpr int kGemvWarps = kGemvThreads / 32;
 constexpr int kChunk = 4;          // iterations per host check
 constexpr int kMaxRestarts = 8;
+// Mixed refinement: once |r| <= kIncrTheta * tol * |b| for every running cluster,
+// the next residual is updated as r -= (I + T) d with the complex64 matrix (the
+// correction d is ~|r|, so the complex64 product's ~2e-6 relative error stays below
+// tol |b| / 20) instead of recomputed as b - (I + T) x in double-float.
+constexpr double kIncrTheta = 2.5e4;
 
 // ------------------------------------------------------------ type helpers --
 __device__ __forceinline__ double2 to_d2(double2 v) { return v; }
@@ -1402,7 +1407,8 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
 // ------------------------------------------------------ refinement helpers --
 template <int R>
 __global__ void k_refine_axpy(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems,
-                              const KState* __restrict__ ost, double2* __restrict__ x128, const float2* __restrict__ d) {
+                              const KState* __restrict__ ost, double2* __restrict__ x128, const float2* __restrict__ d,
+                              double2* __restrict__ dout) {
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const Item I = items[it];
@@ -1412,13 +1418,18 @@ __global__ void k_refine_axpy(const gb::SysDev* __restrict__ sys, const Item* __
     const long long vo = S.vec_off + (long long)(I.r0 + lr) * R;
     for (int rr = 0; rr < R; rr++) {
         const KState& k = ost[I.sys * R + rr];
-        if (k.done) continue;
+        if (k.done) {
+            if (dout) dout[vo + rr] = make_double2(0, 0);
+            continue;
+        }
         const double sc = sqrt(k.rsq);   // the inner solve ran on r / |r| (k_cast_f)
         const float2 dv = d[vo + rr];
+        const double2 dd = make_double2(sc * (double)dv.x, sc * (double)dv.y);
         double2 xv = x128[vo + rr];
-        xv.x += sc * (double)dv.x;
-        xv.y += sc * (double)dv.y;
+        xv.x += dd.x;
+        xv.y += dd.y;
         x128[vo + rr] = xv;
+        if (dout) dout[vo + rr] = dd;   // the correction, for an incremental residual update
     }
 }
 
@@ -1642,7 +1653,8 @@ void dense_plan(int D, int R, Plan& P) {
 }
 
 struct WS {
-    size_t off_state, off_ostate, off_dots, off_cu, off_cw, off_yu, off_yw, off_vec, off_tx, off_r128, off_blob, total;
+    size_t off_state, off_ostate, off_dots, off_cu, off_cw, off_yu, off_yw, off_vec, off_tx, off_r128, off_r128b,
+        off_d128, off_blob, total;
 };
 
 WS ws_layout(const Plan& P, int prec, bool dense) {
@@ -1666,6 +1678,9 @@ WS ws_layout(const Plan& P, int prec, bool dense) {
     }
     w.off_vec = take(vsz * (size_t)P.total_vec * 8);   // x r r0 p v s t b
     w.off_r128 = take((prec == GB_PREC_MIXED || prec == GB_PREC_MIXED_FP64RES) ? sizeof(double2) * (size_t)P.total_vec : 0);
+    // mixed: the second residual buffer and the correction of the incremental update
+    w.off_r128b = take(prec == GB_PREC_MIXED ? sizeof(double2) * (size_t)P.total_vec : 0);
+    w.off_d128 = take(prec == GB_PREC_MIXED ? sizeof(double2) * (size_t)P.total_vec : 0);
     w.off_blob = take(sizeof(gb::SysDev) * P.nsys + sizeof(Strip) * P.nstrips + sizeof(Item) * (P.nv + P.nr) +
                       sizeof(SysPlan) * P.nsys + sizeof(long long) * P.row_strip.size() + sizeof(int) * P.nsys + 256);
     w.total = o;
@@ -2047,11 +2062,9 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     GB_CUDA_TRY(cudaGetLastError());
     const VT* bsrc_vt = bvt ? bvt : bx;
 
-    // a chunk of iterations, captured once per argument set and replayed
-    cudaGraphExec_t exec = nullptr;
-    long long exec_kernels = 0;
-    GraphUse use;
-    if (use_graph) {
+    // chunks of nit iterations (kChunk, and single iterations for the tail of a
+    // solve), captured once per argument set and replayed
+    auto acquire = [&](int nit, GraphUse& use, cudaGraphExec_t& exec, long long& exec_kernels) -> int {
         GraphKey key{};
         const void* a[12] = {base, mat, tvec, D.sys, D.strips, D.vitems, D.ritems, D.sp, st, nullptr, nullptr, nullptr};
         memcpy(key.a, a, sizeof(a));
@@ -2064,6 +2077,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         key.n[6] = P.max_B;
         key.n[7] = P.total_vec;
         key.n[8] = groups_hash(P);
+        key.n[9] = nit;
         use.key = key;
         {
             std::lock_guard<std::mutex> lk(g_graphs.mu);
@@ -2074,50 +2088,85 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
                 f->second.inuse++;
                 f->second.last = ++g_graphs.clock;
                 use.held = true;
+                return GB_OK;
             }
         }
-        if (!exec) {
-            cudaStream_t cs = capture_stream();
-            GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-            gb::capture_begin();
-            int e = GB_OK;
-            for (int itn = 0; itn < kChunk && e == GB_OK; itn++) e = iteration(cs);
-            exec_kernels = gb::capture_end();
-            cudaGraph_t g = nullptr;
-            cudaError_t ce = cudaStreamEndCapture(cs, &g);
-            if (e) {
-                if (g) cudaGraphDestroy(g);
-                return e;
-            }
-            if (ce != cudaSuccess) return gb_set_cuda_error(ce, "capture of BiCGSTAB chunk", __FILE__, __LINE__);
-            ce = cudaGraphInstantiate(&exec, g, 0);
-            cudaGraphDestroy(g);
-            if (ce != cudaSuccess) return gb_set_cuda_error(ce, "instantiate BiCGSTAB graph", __FILE__, __LINE__);
-            std::lock_guard<std::mutex> lk(g_graphs.mu);
-            g_graphs.evict(255);   // bounded cache
-            auto f = g_graphs.map.find(key);
-            if (f != g_graphs.map.end()) {   // another thread built the same graph meanwhile
-                cudaGraphExecDestroy(exec);
-                exec = f->second.exec;
-                exec_kernels = f->second.kernels;
-                f->second.inuse++;
-                f->second.last = ++g_graphs.clock;
-            } else {
-                g_graphs.map[key] = GraphEntry{exec, exec_kernels, 1, ++g_graphs.clock};
-            }
-            use.held = true;
+        cudaStream_t cs = capture_stream();
+        GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        gb::capture_begin();
+        int e = GB_OK;
+        for (int itn = 0; itn < nit && e == GB_OK; itn++) e = iteration(cs);
+        exec_kernels = gb::capture_end();
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(cs, &g);
+        if (e) {
+            if (g) cudaGraphDestroy(g);
+            return e;
         }
+        if (ce != cudaSuccess) return gb_set_cuda_error(ce, "capture of BiCGSTAB chunk", __FILE__, __LINE__);
+        ce = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return gb_set_cuda_error(ce, "instantiate BiCGSTAB graph", __FILE__, __LINE__);
+        std::lock_guard<std::mutex> lk(g_graphs.mu);
+        g_graphs.evict(255);   // bounded cache
+        auto f = g_graphs.map.find(key);
+        if (f != g_graphs.map.end()) {   // another thread built the same graph meanwhile
+            cudaGraphExecDestroy(exec);
+            exec = f->second.exec;
+            exec_kernels = f->second.kernels;
+            f->second.inuse++;
+            f->second.last = ++g_graphs.clock;
+        } else {
+            g_graphs.map[key] = GraphEntry{exec, exec_kernels, 1, ++g_graphs.clock};
+        }
+        use.held = true;
+        return GB_OK;
+    };
+    cudaGraphExec_t exec = nullptr, exec1 = nullptr;
+    long long exec_kernels = 0, exec1_kernels = 0;
+    GraphUse use, use1;
+    if (use_graph) {
+        const int e = acquire(kChunk, use, exec, exec_kernels);
+        if (e) return e;
     }
-
+    // iterations still needed by the slowest running cluster, from its mean
+    // per-iteration residual reduction so far (kChunk when there is no estimate)
+    auto predict = [&](const std::vector<KState>& h) -> int {
+        int need = 1;
+        for (int q = 0; q < nsr; q++) {
+            const KState& k = h[q];
+            if (k.done) continue;
+            const bool f32 = std::is_same<VT, float2>::value;
+            const double rs = f32 ? (double)k.rsq_f : k.rsq, r0 = f32 ? (double)k.r0sq_f : k.r0sq;
+            const double t2 = tol * tol * (f32 ? (double)k.bsq_f : k.bsq);
+            if (k.restarts > 0 || k.iters < 1 || !(rs > 0) || !(r0 > rs) || !(t2 > 0)) return kChunk;
+            const double rate = std::log(rs / r0) / k.iters;   // log reduction of |r|^2 per iteration (< 0)
+            const double n = std::ceil(std::log(t2 / rs) / rate);
+            if (!(n < kChunk)) return kChunk;
+            need = std::max(need, (int)std::max(1.0, n));
+        }
+        return need;
+    };
     std::vector<KState> hst(nsr);
-    // every restart may reset the count once; bound the chunks accordingly
-    const long long max_chunks = ((long long)maxiter / kChunk + 2) * (kMaxRestarts + 2) + 16;
+    // every restart may reset the count once, and a chunk holds at least one
+    // iteration; bound the chunks accordingly
+    const long long max_chunks = ((long long)maxiter + 2) * (kMaxRestarts + 2) + 16;
+    int next = kChunk;   // iterations before the next host check
     for (long long chunk = 0; chunk < max_chunks; chunk++) {
-        if (exec) {
+        if (exec && next == kChunk) {
             GB_CUDA_TRY(cudaGraphLaunch(exec, stream));
             gb::note_launches(exec_kernels);
+        } else if (exec) {
+            if (!exec1) {
+                const int e = acquire(1, use1, exec1, exec1_kernels);
+                if (e) return e;
+            }
+            for (int itn = 0; itn < next; itn++) {
+                GB_CUDA_TRY(cudaGraphLaunch(exec1, stream));
+                gb::note_launches(exec1_kernels);
+            }
         } else {
-            for (int itn = 0; itn < kChunk; itn++) {
+            for (int itn = 0; itn < next; itn++) {
                 int e = iteration(stream);
                 if (e) return e;
             }
@@ -2141,9 +2190,11 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             gb::note_launch();
             k_scalar<R, typename Arith<VT>::T><<<sblocks, 128, 0, stream>>>(D.sp, P.nsys, st, 4, dots, tol, maxiter);
             GB_CUDA_TRY(cudaGetLastError());
+            next = kChunk;
             continue;
         }
         if (all_done) return GB_OK;
+        next = predict(hst);
     }
     return gb_set_error(GB_TIMEOUT, "BiCGSTAB driver exceeded its iteration bound");
 }
@@ -2210,9 +2261,13 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         return finish_status(h.data(), nsr, status, iters, resid);
     }
     // mixed: x = 0, r = b (FP64); repeat { FP32 BiCGSTAB on (I + T) d = r; x += d;
-    // r = b - (I + T) x in double-float (or FP64) }
+    // r = b - (I + T) x in double-float (or FP64), or r -= (I + T) d with the
+    // complex64 matrix once |r| is small enough (kIncrTheta) }
     double2* r128 = reinterpret_cast<double2*>(base + w.off_r128);
+    double2* r_nxt = prec == GB_PREC_MIXED ? reinterpret_cast<double2*>(base + w.off_r128b) : nullptr;
+    double2* d128 = prec == GB_PREC_MIXED ? reinterpret_cast<double2*>(base + w.off_d128) : nullptr;
     double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
+    bool incr = prec == GB_PREC_MIXED && kIncrTheta * tol >= 1.0;   // first pass: |r| = |b|
     gb::note_launch();
     k_outer_start<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, b2, x2, dots);
     gb::note_launch();
@@ -2227,9 +2282,13 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
                                            true);
         if (e) return e;
         gb::note_launch();
-        k_refine_axpy<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, ost, x2, V);
+        k_refine_axpy<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, ost, x2, V, incr ? d128 : nullptr);
         GB_CUDA_TRY(cudaGetLastError());
-        if (prec == GB_PREC_MIXED)
+        if (incr) {   // r_nxt = r - (d + T d), complex64 matrix, FP64 vectors
+            e = launch_apply<double2, R>(P, D, w, base, ost, -1, 1, mat64, nullptr, t2, d128, r_nxt, 3, nullptr, r128,
+                                         dots, stream);
+            std::swap(r128, r_nxt);
+        } else if (prec == GB_PREC_MIXED)
             e = launch_apply<double2, R>(P, D, w, base, ost, -1, 2, mat64, mat64lo, t2, x2, r128, 3, nullptr, b2, dots,
                                          stream);
         else
@@ -2244,6 +2303,11 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         bool all = true;
         for (int q = 0; q < nsr; q++) all &= (h[q].done != 0);
         if (all) break;
+        if (prec == GB_PREC_MIXED) {   // the next update may be incremental if every running |r| is small
+            incr = true;
+            for (int q = 0; q < nsr; q++)
+                if (!h[q].done && !(h[q].rsq <= kIncrTheta * kIncrTheta * h[q].tol2)) incr = false;
+        }
     }
     return finish_status(h.data(), nsr, status, iters, resid);
 }

@@ -176,6 +176,28 @@ def test_bicgstab_reference_tolerance_matches_reference_run(name):
     assert rel(x, g["p_inc"]) < 1e-8
 
 
+@pytest.mark.parametrize("tol,inner", [(1e-8, 1e-4), (1e-10, 1e-4), (1e-5, 1e-4), (1e-8, 1e-6)])
+def test_mixed_reported_residual_is_the_true_residual(tol, inner):
+    """The mixed solve's residual after its last refinement pass, updated
+    incrementally with the complex64 matrix once |r| <= 2.5e4 tol |b|, agrees with
+    b - (I + T) x recomputed in double-float, and is below tol."""
+    rng = np.random.default_rng(21)
+    pos, rad = random_cluster(rng, 60, 50 * nm, 100 * nm, 1400 * nm)
+    md = gb.material_struct([gb.constant_material(index=1.5 + 0.01j)] * 60, gb.constant_material(eps=1.0, mu=1.0),
+                            wavelength=600 * nm)
+    ms, mi = gb.mie_coefficients(rad, md.eps, md.mu, md.eps_b, md.mu_b, md.k_b, 4)
+    p_src = np.stack([gb.plane_wave.from_string(p).structure(pos, md.k_b, 4) for p in "xy"], axis=-1)
+    b = ClusterBatch([dict(position=pos, mie_scat=ms, mie_int=mi, k=float(np.real(md.k_b)), p_src=p_src)], R=2,
+                     precision="mixed").assemble()
+    b.solve(tol=tol, maxiter=1000, inner_tol=inner, max_refine=8)
+    assert np.all(b.status == 0)
+    r = (b.b - b.apply(b.x, "mixed")).view(-1, 2).cpu().numpy()
+    true = np.linalg.norm(r, axis=0) / np.linalg.norm(b.b.view(-1, 2).cpu().numpy(), axis=0)
+    reported = np.asarray(b.resid)
+    assert np.all(reported < tol) and np.all(true < tol)
+    assert np.all(np.abs(true - reported) <= 0.05 * tol)
+
+
 def test_mixed_precision_meets_fp64_within_1e6():
     rng = np.random.default_rng(11)
     N, lmax = 40, 4
