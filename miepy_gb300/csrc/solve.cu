@@ -532,18 +532,25 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
 }
 
 struct GemvLayout {
-    int chunk_cap, y_bytes, warp_bytes;
+    int chunk_cap, y_bytes, nys, warp_bytes;
 };
-// Per warp: S mbarriers | S y-vector slots (y_u of the blocks in flight) | y_w of
-// the strip's particle | S matrix stages (hi, then lo for double-float).
+// Per warp: S mbarriers | nys y-vector slots (y_u of the blocks in flight) | y_w of
+// the strip's particle | S matrix stages (hi, then lo for double-float).  The
+// producer runs S-1 chunks ahead of the consumer, so with cpb chunks per block the
+// y_u of at most 1 + ceil((S-1)/cpb) blocks are live: the first chunk of block
+// b + nys is issued only once every chunk of block b has been consumed.  (All
+// blocks of one launch have the block size Bmax.)
 __host__ __device__ inline GemvLayout gemv_layout(int Bmax, int rows_per_chunk, int RT, int S, int mat_bytes, bool df,
                                                   int y_bytes) {
     GemvLayout g;
     g.chunk_cap = ((rows_per_chunk * Bmax * mat_bytes) + 127) & ~127;
     g.y_bytes = (Bmax * RT * y_bytes + 127) & ~127;
+    const int cpb = (Bmax + rows_per_chunk - 1) / rows_per_chunk;
+    const int live = 1 + (S - 1 + cpb - 1) / cpb;
+    g.nys = live < S ? live : S;
     // + 256 B of padding: lanes whose columns lie past the block's end read (and
     // discard) up to LPR-1 elements beyond the last stage
-    g.warp_bytes = 128 + (S + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1) + 256;
+    g.warp_bytes = 128 + (g.nys + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1) + 256;
     return g;
 }
 
@@ -576,8 +583,8 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     unsigned char* wbase = gemv_smem + (size_t)wid * lay.warp_bytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(wbase);
     unsigned char* yring = wbase + 128;
-    YT* syw = reinterpret_cast<YT*>(yring + S * lay.y_bytes);
-    unsigned char* stages = yring + (S + 1) * lay.y_bytes;
+    YT* syw = reinterpret_cast<YT*>(yring + lay.nys * lay.y_bytes);
+    unsigned char* stages = yring + (lay.nys + 1) * lay.y_bytes;
     const unsigned stage_stride = lay.chunk_cap * (DF ? 2 : 1);
     const unsigned char* mh = reinterpret_cast<const unsigned char*>(mat_hi);
     const unsigned char* ml = reinterpret_cast<const unsigned char*>(mat_lo);
@@ -624,8 +631,8 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             tma_1d(dst, mstrip_h + src, bytes, bar);
             if (DF) tma_1d(dst + lay.chunk_cap, mstrip_l + src, bytes, bar);
             if (pc == 0)
-                tma_1d(yring + (size_t)(pb % S) * lay.y_bytes, Yu + vec_off + (long long)(j0 + pb) * B * RT, ybytes,
-                       bar);
+                tma_1d(yring + (size_t)(pb % lay.nys) * lay.y_bytes, Yu + vec_off + (long long)(j0 + pb) * B * RT,
+                       ybytes, bar);
             pstage = (pstage + 1 == S) ? 0 : pstage + 1;
             if (++pc == cpb) { pc = 0; ++pb; }
         };
@@ -650,7 +657,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             for (int k = 0; k < CPL; k++)
 #pragma unroll
                 for (int q = 0; q < RR; q++) Pol::zero(cw[k][q]);
-            const YT* syu = reinterpret_cast<const YT*>(yring + (size_t)(b % S) * lay.y_bytes);
+            const YT* syu = reinterpret_cast<const YT*>(yring + (size_t)(b % lay.nys) * lay.y_bytes);
             for (int c = 0; c < cpb; c++) {
                 if (issued < total) {   // into the stage freed by the previous chunk
                     if (lane == 0) issue();
@@ -1761,13 +1768,15 @@ Shape pick_shape(int Bmax) {
     return best;
 }
 
-// Steps per chunk for a shape: chunks of about 3 KB of matrix for the block size
-// the shape is made for (LPR*CPL columns), so that three stages and four y slots
-// per warp leave room for three 4-warp CTAs per SM.
+// Steps per chunk for a shape: chunks of about 6 KB of matrix for the block size
+// the shape is made for (LPR*CPL columns); with three stages and two y slots per
+// warp, two 4-warp CTAs share an SM.  (3 KB chunks with three CTAs per SM, and a
+// fourth stage, measured no faster for the complex64 pass and 7 % slower for the
+// compute-bound double-float pass, whose longer unrolled steps help.)
 constexpr int gemv_steps(int lpr, int cpl, int elem_bytes) {
-    return (3072 / ((32 / lpr) * lpr * cpl * elem_bytes)) < 1 ? 1
-           : (3072 / ((32 / lpr) * lpr * cpl * elem_bytes)) > 4 ? 4
-                                                                : 3072 / ((32 / lpr) * lpr * cpl * elem_bytes);
+    return (6144 / ((32 / lpr) * lpr * cpl * elem_bytes)) < 1 ? 1
+           : (6144 / ((32 / lpr) * lpr * cpl * elem_bytes)) > 8 ? 8
+                                                                : 6144 / ((32 / lpr) * lpr * cpl * elem_bytes);
 }
 
 template <class Pol, int RR, int RT>
