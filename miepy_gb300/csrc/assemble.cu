@@ -38,18 +38,20 @@ __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
 
 // Shared-memory layout of one CTA: the special functions of a group of PB pairs
 // (launch-wide strides PM = 2 Lmax + 2 orders, MU = 4 Lmax + 1 azimuthal orders),
-// then the tuple values of two pairs (the one being written and the next).
+// then the tuple values of NB pairs: two (the one being written and the next) where
+// they fit, one at large lmax, where two would cost occupancy.
 struct AsmSmem {
-    int PM, MU, M, PB;
+    int PM, MU, M, PB, NB;
     size_t off_geo, off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
 };
 
-__host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_sums, bool want64) {
+__host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_sums, bool want64, int NB) {
     AsmSmem s;
     s.PM = 2 * L + 2;
     s.MU = 4 * L + 1;
     s.M = M;
     s.PB = PB;
+    s.NB = NB;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 15) & ~size_t(15); return r; };
     s.off_geo = take(sizeof(double) * 8 * PB);
@@ -57,9 +59,9 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_su
     s.off_e = take(sizeof(double2) * s.MU * PB);
     s.off_P = take(sizeof(double) * s.PM * s.PM * PB);
     s.off_G = take(16 * (size_t)s.PM * s.MU * PB);          // double2 (FP64 sums) or float4 (double-float)
-    s.off_T = take(fp64_sums ? sizeof(double2) * 4 * M : 0);   // two buffers of (A, B) per tuple
-    s.off_Tf = take(want64 ? sizeof(float2) * 4 * M : 0);
-    s.off_Tl = take(want64 ? sizeof(float2) * 4 * M : 0);
+    s.off_T = take(fp64_sums ? sizeof(double2) * 2 * NB * M : 0);   // NB buffers of (A, B) per tuple
+    s.off_Tf = take(want64 ? sizeof(float2) * 2 * NB * M : 0);
+    s.off_Tl = take(want64 ? sizeof(float2) * 2 * NB * M : 0);
     s.total = o;
     return s;
 }
@@ -189,7 +191,7 @@ struct Latt {
 template <bool DENSE, bool FP64_SUMS, int MODE = 0>
 __global__ void __launch_bounds__(kAsmThreads, 3)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
-           int Lmax, int Mmax, int PB, const double* __restrict__ pos, const double2* __restrict__ mie,
+           int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
            double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
            Refl refl = Refl(), Latt latt = Latt()) {
     constexpr bool REFL = MODE == 1, LATT = MODE == 2;
@@ -197,7 +199,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
-    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE);
+    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE, NB);
     double* geo = reinterpret_cast<double*>(smem + lay.off_geo);        // [PB][8]
     double2* hh = reinterpret_cast<double2*>(smem + lay.off_h);         // [PB][PM]
     double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);        // [PB][MU]
@@ -567,8 +569,11 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         tuples(0, 0);
         __syncthreads();
         for (int pp = 0; pp < np; pp++) {
-            write_block(pp, pp & 1);                        // reads buffer pp & 1
-            if (pp + 1 < np) tuples(pp + 1, (pp + 1) & 1);  // writes the other buffer
+            write_block(pp, NB == 2 ? (pp & 1) : 0);   // reads buffer pp & 1 (or the one buffer)
+            if (pp + 1 < np) {
+                if (NB == 1) __syncthreads();   // one buffer: every read of it done before it is refilled
+                tuples(pp + 1, NB == 2 ? ((pp + 1) & 1) : 0);
+            }
             __syncthreads();
         }
     }
@@ -704,65 +709,83 @@ int stage_release(int slot, cudaStream_t stream) {
 
 namespace {
 
+// One launch per lmax of the batch (each with its own tuple layout and pairs per
+// group), so that small-lmax clusters of a ragged batch are not run with the
+// shared-memory strides of the largest one.
 int launch_assemble(int nsys, const gb_system* sys, const double* pos, const double* mie, double* out128,
                     float* out64, float* out64lo, long long dense_ld, bool dense, cudaStream_t stream,
                     const Refl* refl = nullptr, const Latt* latt = nullptr) {
-    std::vector<gb::SysDev> sd;
-    int st = gb::make_sysdev(nsys, sys, stream, sd);
+    std::vector<gb::SysDev> all;
+    int st = gb::make_sysdev(nsys, sys, stream, all);
     if (st) return st;
-    int Lmax = 1, Mmax = 0;
-    long long total_pairs = 0;
-    for (int s = 0; s < nsys; s++) {
-        Lmax = std::max(Lmax, sd[s].lmax);
-        Mmax = std::max(Mmax, sd[s].M);
-        total_pairs += (refl || latt) ? (long long)sd[s].N * sd[s].N : sd[s].P;
-    }
-    if (total_pairs == 0) return GB_OK;
     const bool fp64_sums = dense || out128 != nullptr;
     const bool want64 = (out64 != nullptr || out64lo != nullptr) && !dense;
-    // pairs per group: the largest power of two up to 32 whose tables keep the CTA
-    // within ~72 KB of shared memory, so that three CTAs share an SM (at least one pair)
-    int PB = 32;
-    while (PB > 1 && asm_layout(Lmax, Mmax, PB, fp64_sums, want64).total > 72 * 1024) PB >>= 1;
-    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, fp64_sums, want64);
-    const size_t smem = lay.total;
-    if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
-    Latt lt = latt ? *latt : Latt();
-    if (latt) {
-        if (lt.ncell < 1) return GB_OK;
-        lt.gpp = (lt.ncell + PB - 1) / PB;
+    std::vector<int> lmaxes;
+    for (const gb::SysDev& d : all)
+        if (std::find(lmaxes.begin(), lmaxes.end(), d.lmax) == lmaxes.end()) lmaxes.push_back(d.lmax);
+    std::sort(lmaxes.begin(), lmaxes.end());
+    for (int L : lmaxes) {
+        std::vector<gb::SysDev> sd;
+        for (const gb::SysDev& d : all)
+            if (d.lmax == L) sd.push_back(d);
+        const int ns = (int)sd.size();
+        int Mmax = 0;
+        long long total_pairs = 0;
+        for (const gb::SysDev& d : sd) {
+            Mmax = std::max(Mmax, d.M);
+            total_pairs += (refl || latt) ? (long long)d.N * d.N : d.P;
+        }
+        if (total_pairs == 0) continue;
+        // tuple buffers: two (pipelined pairs) when a one-pair group still fits ~72 KB,
+        // else one; pairs per group: the largest power of two up to 32 whose tables
+        // keep the CTA within ~72 KB of shared memory, so that three CTAs share an SM
+        const int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= 72 * 1024 ? 2 : 1;
+        int PB = 32;
+        while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > 72 * 1024) PB >>= 1;
+        const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB);
+        const size_t smem = lay.total;
+        if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
+        Latt lt = latt ? *latt : Latt();
+        if (latt) {
+            if (lt.ncell < 1) return GB_OK;
+            lt.gpp = (lt.ncell + PB - 1) / PB;
+        }
+        std::vector<long long> gbase(ns + 1, 0);
+        for (int s = 0; s < ns; s++) {
+            const long long np_s = refl ? (long long)sd[s].N * sd[s].N : sd[s].P;
+            gbase[s + 1] = gbase[s] + (latt ? (long long)sd[s].N * sd[s].N * lt.gpp : (np_s + PB - 1) / PB);
+        }
+        const long long ngroups = gbase[ns];
+        // one staging upload: descriptors then group prefix sums
+        std::vector<unsigned char> blob(sizeof(gb::SysDev) * ns + sizeof(long long) * (ns + 1));
+        memcpy(blob.data(), sd.data(), sizeof(gb::SysDev) * ns);
+        memcpy(blob.data() + sizeof(gb::SysDev) * ns, gbase.data(), sizeof(long long) * (ns + 1));
+        void* dblob = nullptr;
+        int slot = 0;
+        st = gb::stage_acquire(blob.data(), blob.size(), stream, &dblob, &slot);
+        if (st) return st;
+        const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
+        const long long* dbase =
+            reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * ns);
+        auto kfn = latt ? k_assemble<true, true, 2>
+                        : refl ? k_assemble<true, true, 1>
+                               : (dense ? k_assemble<true, true>
+                                        : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>));
+        GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
+        int per_sm = 1;
+        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
+        if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
+        const long long grid = std::min<long long>(ngroups, (long long)gb::sm_count() * per_sm);
+        gb::note_launch();
+        kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
+            dsys, ns, dbase, ngroups, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),
+            reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
+            dense_ld, refl ? *refl : Refl(), lt);
+        GB_CUDA_TRY(cudaGetLastError());
+        st = gb::stage_release(slot, stream);
+        if (st) return st;
     }
-    std::vector<long long> gbase(nsys + 1, 0);
-    for (int s = 0; s < nsys; s++) {
-        const long long np_s = refl ? (long long)sd[s].N * sd[s].N : sd[s].P;
-        gbase[s + 1] = gbase[s] + (latt ? (long long)sd[s].N * sd[s].N * lt.gpp : (np_s + PB - 1) / PB);
-    }
-    const long long ngroups = gbase[nsys];
-    // one staging upload: descriptors then group prefix sums
-    std::vector<unsigned char> blob(sizeof(gb::SysDev) * nsys + sizeof(long long) * (nsys + 1));
-    memcpy(blob.data(), sd.data(), sizeof(gb::SysDev) * nsys);
-    memcpy(blob.data() + sizeof(gb::SysDev) * nsys, gbase.data(), sizeof(long long) * (nsys + 1));
-    void* dblob = nullptr;
-    int slot = 0;
-    st = gb::stage_acquire(blob.data(), blob.size(), stream, &dblob, &slot);
-    if (st) return st;
-    const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
-    const long long* dbase = reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * nsys);
-    auto kfn = latt ? k_assemble<true, true, 2>
-                    : refl ? k_assemble<true, true, 1>
-                           : (dense ? k_assemble<true, true> : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>));
-    GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
-    int per_sm = 1;
-    GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
-    if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
-    const long long grid = std::min<long long>(ngroups, (long long)gb::sm_count() * per_sm);
-    gb::note_launch();
-    kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
-        dsys, nsys, dbase, ngroups, Lmax, Mmax, PB, pos, reinterpret_cast<const double2*>(mie),
-        reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
-        dense_ld, refl ? *refl : Refl(), lt);
-    GB_CUDA_TRY(cudaGetLastError());
-    return gb::stage_release(slot, stream);
+    return GB_OK;
 }
 
 }   // namespace
