@@ -109,7 +109,18 @@ class ClusterBatch:
             for name, dt, n in self._parts)
         self.h2d_bytes = 8 * t["pos"] + 16 * (2 * t["mie"] + t["vec"])
         self.tvec = torch.empty(max(t["t"], 1), dtype=torch.complex128, device=dev)
-        self.x = torch.zeros(max(t["vec"], 1), dtype=torch.complex128, device=dev)
+        # outputs in one float64 buffer: x, then per-particle xs, force and torque, so
+        # that to_host() reads them back with one copy
+        self.xs_L = max(l["lmax"] for l in self.layout)
+        nv2 = 2 * max(t["vec"], 1)
+        self._n_xs = max(t["obs"] * self.R * 6 * self.xs_L, 1)
+        self._n_f = max(t["obs"] * self.R * 3, 1)
+        self._out = torch.zeros(nv2 + self._n_xs + 2 * self._n_f, dtype=torch.float64, device=dev)
+        self.x = self._out[:nv2].view(torch.complex128)
+        self._xs_buf = self._out[nv2: nv2 + self._n_xs]
+        self._f_buf = self._out[nv2 + self._n_xs: nv2 + self._n_xs + self._n_f]
+        self._t_buf = self._out[nv2 + self._n_xs + self._n_f:]
+        self.xs = self.F = self.T = None
         need = NEEDS[precision]
         mat = max(t["mat"], 1)
         self.mat128 = torch.empty(mat, dtype=torch.complex128, device=dev) if "c128" in need else None
@@ -293,14 +304,12 @@ class ClusterBatch:
         L = nat.lib()
         dev = self.device
         n_obs = self.totals["obs"]
-        self.xs_L = max(l["lmax"] for l in self.layout)
         ragged = any(l["lmax"] != self.xs_L for l in self.layout)
         self.p_scat = torch.empty_like(self.x) if want_fields else None
         self.p_int = torch.empty_like(self.x) if want_fields else None
-        alloc = torch.zeros if ragged else torch.empty
-        xs = alloc(max(n_obs * self.R * 6 * self.xs_L, 1), dtype=torch.float64, device=dev)
-        F = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
-        T = torch.empty(max(n_obs * self.R * 3, 1), dtype=torch.float64, device=dev)
+        xs, F, T = self._xs_buf, self._f_buf, self._t_buf
+        if ragged:   # rows of clusters with a smaller lmax keep zeros past 2 lmax
+            xs.zero_()
         if self.tmatrix:   # p_scat = T p_inc; no interior coefficients for general particles
             if self.p_scat is None:
                 self.p_scat = torch.empty_like(self.x)
@@ -330,13 +339,15 @@ class ClusterBatch:
     def to_host(self):
         """x, per-particle cross-sections, force and torque as numpy arrays, read back
         with asynchronous copies into pinned buffers and a single synchronisation."""
-        srcs = {"x": self.x, "xs": self.xs, "F": self.F, "T": self.T}
-        if self._host_out is None or any(self._host_out[k].numel() != v.numel() for k, v in srcs.items()):
-            self._host_out = {k: torch.empty(v.numel(), dtype=v.dtype).pin_memory() for k, v in srcs.items()}
-        for k, v in srcs.items():
-            self._host_out[k].copy_(v, non_blocking=True)
+        if self._host_out is None or self._host_out.numel() != self._out.numel():
+            self._host_out = torch.empty(self._out.numel(), dtype=torch.float64).pin_memory()
+        self._host_out.copy_(self._out, non_blocking=True)
         torch.cuda.current_stream(self.device).synchronize()
-        return {k: v.numpy().copy() for k, v in self._host_out.items()}
+        h = self._host_out.numpy()
+        nv2 = 2 * self.x.numel()
+        n_xs, n_f = self._n_xs, self._n_f
+        return {"x": h[:nv2].view(np.complex128).copy(), "xs": h[nv2: nv2 + n_xs].copy(),
+                "F": h[nv2 + n_xs: nv2 + n_xs + n_f].copy(), "T": h[nv2 + n_xs + n_f:].copy()}
 
     # ------------------------------------------------------------- accessors --
     def cluster_view(self, s, t):
