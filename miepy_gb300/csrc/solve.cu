@@ -513,6 +513,21 @@ __device__ __forceinline__ void tma_1d(void* dst, const void* src, unsigned byte
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// The same copy with an L2 cache policy (the matrix stream is read once per pass and
+// marked evict-first, so that it does not push the GEMV's partials and the solver's
+// vectors out of L2 before the kernels that read them next).
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ void tma_1d_hint(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -599,6 +614,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     const long long nwarps = ((long long)gridDim.x * kGemvThreads) >> 5;
     bool failed = false;
     int in_flight = 0;                    // chunks issued and not yet consumed
+    const uint64_t stream_pol = l2_evict_first_policy();
     pdl_wait();                           // y vectors and scalars of the predecessors
     pdl_trigger();
     for (long long w = sbeg + warp; w < send && !failed; w += nwarps) {
@@ -628,8 +644,8 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
             unsigned char* dst = stages + (size_t)pstage * stage_stride;
             const long long src = (long long)pb * B * row_bytes + (long long)r0 * row_bytes;
             mbar_expect_tx(bar, bytes * (DF ? 2u : 1u) + (pc == 0 ? ybytes : 0u));
-            tma_1d(dst, mstrip_h + src, bytes, bar);
-            if (DF) tma_1d(dst + lay.chunk_cap, mstrip_l + src, bytes, bar);
+            tma_1d_hint(dst, mstrip_h + src, bytes, bar, stream_pol);
+            if (DF) tma_1d_hint(dst + lay.chunk_cap, mstrip_l + src, bytes, bar, stream_pol);
             if (pc == 0)
                 tma_1d(yring + (size_t)(pb % lay.nys) * lay.y_bytes, Yu + vec_off + (long long)(j0 + pb) * B * RT,
                        ybytes, bar);
