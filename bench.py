@@ -41,8 +41,8 @@ WORKLOAD = "random cluster N=200 lmax=4 R=2 (D=9600), n=1.5+0.01i, vacuum, 600 n
 # DRAM bytes (read + write) of one k_pgemv<Pol32> launch on this workload, from one
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); summary and command in
 # profiles/k_pgemv_pol32_cluster_n200_lmax4.txt
-GEMV_TRAFFIC_BYTES = 387_963_136
-GEMV_TRAFFIC_SOURCE = "ncu: dram__bytes_read.sum 367.71 MB + dram__bytes_write.sum 20.25 MB per launch"
+GEMV_TRAFFIC_BYTES = 375_720_448
+GEMV_TRAFFIC_SOURCE = "ncu: dram__bytes_read.sum 367.70 MB + dram__bytes_write.sum 8.02 MB per launch"
 
 
 # ---------------------------------------------------------------- workload --
