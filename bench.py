@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 NM = 1e-9
 TOL = 1e-8
+CONC_STREAMS = 2   # concurrent solve streams of the bench's serving-pattern figure
 INNER_TOL = 1e-4   # relative residual of each FP32 inner solve of the mixed method
 WORKLOAD = "random cluster N=200 lmax=4 R=2 (D=9600), n=1.5+0.01i, vacuum, 600 nm, seed 2"
 # DRAM bytes (read + write) of one k_pgemv<Pol32> launch on this workload, from one
@@ -266,16 +267,61 @@ def run_gpu(args, rank, world):
     e1.record(stream)
     torch.cuda.synchronize()
     t_e2e = e0.elapsed_time(e1) / 1e3
+
+    # ---- concurrent solves (the serving pattern): CONC_STREAMS host threads, each
+    # with its own batch on its own stream, args.steps solves each; one solve's
+    # latency-bound phases overlap another's matrix passes.  Device-timed: every
+    # stream waits on a start event and the main stream on every stream's end event.
+    conc = [batches["mixed"]] + [ClusterBatch([spec], R=R, precision="mixed", device=dev)
+                                 for _ in range(CONC_STREAMS - 1)]
+    conc_streams = [torch.cuda.Stream(dev) for _ in conc]
+    for b, st_ in zip(conc, conc_streams):
+        with torch.cuda.stream(st_):
+            for _ in range(args.warmup):
+                one_solve(b, "mixed")
+    torch.cuda.synchronize()
+    c_start, c_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ends = [torch.cuda.Event() for _ in conc]
+    per_conc = [None] * len(conc)
+
+    def conc_worker(i):
+        b, st_ = conc[i], conc_streams[i]
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        with torch.cuda.stream(st_):
+            st_.wait_event(c_start)
+            evs[0].record(st_)
+            for s_ in range(args.steps):
+                one_solve(b, "mixed")
+                evs[s_ + 1].record(st_)
+            ends[i].record(st_)
+        ends[i].synchronize()
+        per_conc[i] = [evs[j].elapsed_time(evs[j + 1]) for j in range(args.steps)]
+
+    n_c0 = L.gb_launch_count()
+    c_start.record(stream)
+    workers = [threading.Thread(target=conc_worker, args=(i,)) for i in range(len(conc))]
+    for th in workers:
+        th.start()
+    for th in workers:
+        th.join()
+    for ev in ends:
+        stream.wait_event(ev)
+    c_end.record(stream)
+    torch.cuda.synchronize()
+    t_conc = c_start.elapsed_time(c_end) / 1e3
+    launches_conc = L.gb_launch_count() - n_c0
+    per_c = np.concatenate([np.asarray(v) for v in per_conc])
+    conc_same = all(torch.equal(b.xs, conc[0].xs) and torch.equal(b.x, conc[0].x) for b in conc[1:])
     clocks_info = clocks.stop()
     h2d = bb.h2d_bytes
     d2h = sum(o.nbytes for o in out.values())
 
-    ts = np.array([t_mixed, t_fp64, t_e2e])
+    ts = np.array([t_mixed, t_fp64, t_e2e, t_conc])
     if world > 1:
         tt = torch.tensor(ts, device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         ts = tt.cpu().numpy()
-    t_mixed, t_fp64, t_e2e = ts
+    t_mixed, t_fp64, t_e2e, t_conc = ts
     res = dict(
         value=world * args.steps / t_mixed,
         ms_per_step=1e3 * t_mixed / args.steps,
@@ -285,6 +331,10 @@ def run_gpu(args, rank, world):
         cext_rel_err_mixed_vs_fp64=cext_err, iterations_fp64=iters_fp64, refinement_passes_mixed=iters_mixed,
         e2e=dict(value=world * e2e_steps / t_e2e, unit="solves/s", h2d_bytes_per_step=int(h2d),
                  d2h_bytes_per_step=int(d2h)),
+        concurrent=dict(streams=CONC_STREAMS, solves_per_s=world * CONC_STREAMS * args.steps / t_conc,
+                        p50_ms=float(np.percentile(per_c, 50)), p99_ms=float(np.percentile(per_c, 99)),
+                        results_identical_across_streams=bool(conc_same), gpu_launches=int(launches_conc),
+                        note="mixed solves of the same workload on concurrent streams, inputs resident"),
         roofline=dict(bound="hbm", achieved=mat_bytes_64 / t_gemv64 / 1e9, peak=peak, unit="GB/s",
                       frac=mat_bytes_64 / t_gemv64 / 1e9 / peak, traffic=GEMV_TRAFFIC_BYTES,
                       traffic_source=GEMV_TRAFFIC_SOURCE,
