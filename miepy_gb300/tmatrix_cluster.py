@@ -15,9 +15,11 @@ particle's T-matrix (``gb_solve_batch_tmatrix``); the dense aggregate is not for
 from __future__ import annotations
 
 import numpy as np
+import torch
 
+from . import _native as nat
 from .cluster import DEFAULT_MAXITER, DEFAULT_TOL, EXACT_TOL, _method_is_exact, cross_sections
-from .engine import ClusterBatch
+from .engine import ClusterBatch, current_stream
 from .materials import constant_material
 from .mie import mie_coefficients
 from .modes import lmax_to_rmax
@@ -51,6 +53,9 @@ class sphere:
         self.material = material
         self.tmatrix = None
 
+    def enclosed_radius(self):
+        return self.radius
+
     def compute_tmatrix(self, lmax, wavelength, eps_m, **kwargs):
         metal = getattr(self.material, "name", None) == "metal"
         self.tmatrix = tmatrix_sphere(self.radius, wavelength, self.material.eps(wavelength), eps_m, lmax, metal)
@@ -62,11 +67,12 @@ class tmatrix_cluster:
 
     Keywords as the reference's cluster where they apply (source, wavelength, lmax,
     medium, interactions, method), plus precision ("fp64" default, "mixed", "fp32"),
-    tol, maxiter and device.
+    tol, maxiter, device and enclosed_radius ([N], the radius of each particle's
+    circumscribing sphere, for the interior rule of the fields; none by default).
     """
 
     def __init__(self, *, position, tmatrix, source, wavelength, lmax, medium=None, interactions=True, method=None,
-                 precision="fp64", tol=None, maxiter=None, device=None):
+                 precision="fp64", tol=None, maxiter=None, device=None, enclosed_radius=None):
         self.position = np.asarray(np.atleast_2d(position), dtype=float)
         N = self.position.shape[0]
         self.Nparticles = N
@@ -83,6 +89,8 @@ class tmatrix_cluster:
         self.k_b = 2 * np.pi * np.real(np.sqrt(self.eps_b * self.mu_b)) / wavelength
         self.interactions, self.method, self.precision = interactions, method, precision
         self.tol, self.maxiter, self.device = tol, maxiter, device
+        self.enclosed = np.zeros(N) if enclosed_radius is None else np.broadcast_to(
+            np.asarray(enclosed_radius, dtype=float), (N,)).copy()
         self.solve()
 
     def _tolerance(self):
@@ -137,6 +145,55 @@ class tmatrix_cluster:
     def torque_on_particle(self, i):
         return self._T[i].copy()
 
+    # --------------------------------------------------------------- fields --
+    def _field(self, x1, x2, x3, interior, source, mask, far, spherical, magnetic):
+        """cluster.py:219-345: the outgoing expansions of every particle's p_scat
+        plus the source.  Inside a particle's enclosed radius the reference evaluates
+        its interior coefficients, which stay zero for general particles, so those
+        points read 0 (interior=True) or are masked (mask=True).  Evaluated by the
+        GPU near-field kernel (gb_near_field) with zero interior coefficients."""
+        if far or spherical:
+            raise NotImplementedError("far-field / spherical field evaluation is not on the GPU path")
+        x, y, z = np.broadcast_arrays(*(np.asarray(v, dtype=float) for v in (x1, x2, x3)))
+        shape = x.shape
+        pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+        dev = self._batch.device
+        N, L = self.Nparticles, self.lmax
+        d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+        ps = d(self.p_scat, torch.complex128)
+        zeros = torch.zeros_like(ps)
+        ones = torch.ones(N, dtype=torch.complex128, device=dev)
+        k_int = ones * self.k_b
+        hfac = -1j * np.sqrt(self.eps_b / self.mu_b) if magnetic else 1.0
+        use_int = bool(interior and not mask and np.any(self.enclosed > 0))
+        out = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
+        pos, rad, P = d(self.position, torch.float64), d(self.enclosed, torch.float64), d(pts, torch.float64)
+        nat.check(nat.lib().gb_near_field(N, L, nat.ptr(pos), nat.ptr(rad), nat.ptr(ps), nat.ptr(zeros),
+                                          float(self.k_b), nat.ptr(k_int), pts.shape[0], nat.ptr(P), int(use_int),
+                                          int(bool(magnetic)), float(np.real(hfac)), float(np.imag(hfac)),
+                                          nat.ptr(ones), nat.ptr(out), current_stream(dev)), "near field")
+        E = out.cpu().numpy().T.reshape((3,) + shape).copy()
+        inside = np.zeros(shape, dtype=bool)
+        for i in range(N):
+            inside |= ((x - self.position[i, 0]) ** 2 + (y - self.position[i, 1]) ** 2
+                       + (z - self.position[i, 2]) ** 2) < self.enclosed[i] ** 2
+        if source:
+            k = self.k_b
+            S = (self.source.H_field(x, y, z, k) * (self.eps_b / self.mu_b) ** 0.5 if magnetic
+                 else self.source.E_field(x, y, z, k))
+            if use_int:
+                S = np.where(inside[None], 0.0, S)
+            E = E + S
+        if mask:
+            E[:, inside] = 0
+        return E
+
+    def E_field(self, x1, x2, x3, interior=True, source=True, mask=False, far=False, spherical=False):
+        return self._field(x1, x2, x3, interior, source, mask, far, spherical, magnetic=False)
+
+    def H_field(self, x1, x2, x3, interior=True, source=True, mask=False, far=False, spherical=False):
+        return self._field(x1, x2, x3, interior, source, mask, far, spherical, magnetic=True)
+
 
 class cluster(tmatrix_cluster):
     """The reference's ``miepy.cluster(particles=..., source, wavelength, lmax,
@@ -165,6 +222,8 @@ class cluster(tmatrix_cluster):
             if key is not None:
                 cache[key] = T[i]
         self.origin = np.zeros(3) if origin is None else np.asarray(origin, dtype=float)
+        enclosed = [p.enclosed_radius() if hasattr(p, "enclosed_radius") else 0.0 for p in self.particles]
+        enclosed = [0.0 if e is None else float(e) for e in enclosed]
         super().__init__(position=[p.position for p in self.particles], tmatrix=T, source=source,
                          wavelength=wavelength, lmax=lmax, medium=medium, interactions=interactions, method=method,
-                         **kw)
+                         enclosed_radius=enclosed, **kw)

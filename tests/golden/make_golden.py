@@ -208,12 +208,20 @@ def main():
         def _dict_key(self, wavelength):
             return (fixed_tmatrix_particle, id(self))
 
+        def enclosed_radius(self):
+            return 75 * nm
+
     parts = [miepy.sphere([0, 0, 0], 70 * nm, miepy.constant_material(index=1.9 + 0.05j)),
              miepy.core_shell([220 * nm, 30 * nm, -40 * nm], 50 * nm, 20 * nm, miepy.constant_material(index=0.3 + 3j),
                               miepy.constant_material(index=1.5)),
              fixed_tmatrix_particle([-150 * nm, 120 * nm, 70 * nm], T_dense)]
     c = miepy.cluster(particles=parts, source=miepy.sources.plane_wave([1, 1j]), wavelength=600 * nm, lmax=lm,
                       medium=miepy.constant_material(index=1.33), method=miepy.solver.exact)
+    # field points: outside every particle, plus one inside the sphere and one inside
+    # the core-shell particle (interior rule)
+    fx = np.array([0.0, 300 * nm, -250 * nm, 50 * nm, 10 * nm, 225 * nm])
+    fy = np.array([0.0, -100 * nm, 150 * nm, 400 * nm, 5 * nm, 35 * nm])
+    fz = np.array([-200 * nm, 200 * nm, -40 * nm, 120 * nm, 0.0, -40 * nm])
     md = c.material_data
     C = c.cross_sections()
     per = np.array([[np.asarray(v) for v in c.cross_sections_per_multipole_of_particle(i)]
@@ -223,7 +231,10 @@ def main():
                         mu_b=np.complex128(md.mu_b), k_b=np.float64(np.real(md.k_b)), p_src=c.p_src, p_inc=c.p_inc,
                         p_scat=c.p_scat, cross_sections=np.array([C.scattering, C.absorption, C.extinction]),
                         cross_sections_per_multipole=per, force=c.force(), torque=c.torque(),
-                        agg_tmatrix=miepy.interactions.particle_aggregate_tmatrix(c.position, c.tmatrix, md.k_b))
+                        agg_tmatrix=miepy.interactions.particle_aggregate_tmatrix(c.position, c.tmatrix, md.k_b),
+                        field_x=fx, field_y=fy, field_z=fz, E_total=c.E_field(fx, fy, fz), H_total=c.H_field(fx, fy, fz),
+                        E_scat_only=c.E_field(fx, fy, fz, source=False, interior=False),
+                        E_masked=c.E_field(fx, fy, fz, mask=True))
     print("wrote tmatrix3_lmax3_exact")
 
     # periodic clusters (lattice row): the reference's own lattice sums

@@ -63,12 +63,16 @@ def random_cluster(seed, N=6, lmax=3):
 class fixed_particle:
     """A particle with a given T-matrix (what the reference's particle classes provide)."""
 
-    def __init__(self, position, tmatrix):
+    def __init__(self, position, tmatrix, enclosed=None):
         self.position = np.asarray(position, dtype=float)
         self._T = tmatrix
+        self._r = enclosed
 
     def compute_tmatrix(self, lmax, wavelength, eps_m, **kw):
         return self._T
+
+    def enclosed_radius(self):
+        return self._r
 
 
 # ------------------------------------------------------------------------ CPU --
@@ -118,7 +122,8 @@ def test_dense_particle_aggregate_on_gpu():
 def _reference_cluster(**kw):
     import miepy_gb300 as gb
     g = fixture()
-    parts = [fixed_particle(g["position"][i], g["tmatrix"][i]) for i in range(3)]
+    enclosed = [70 * nm, 70 * nm, 75 * nm]   # sphere, core + shell, the fixture's particle
+    parts = [fixed_particle(g["position"][i], g["tmatrix"][i], enclosed[i]) for i in range(3)]
     c = gb.cluster(particles=parts, source=gb.plane_wave([1, 1j]), wavelength=float(g["wavelength"]), lmax=3,
                    medium=gb.constant_material(index=1.33), method=gb.solver.exact, **kw)
     return g, c
@@ -137,6 +142,19 @@ def test_cluster_matches_reference_cluster():
     assert rel(per, g["cross_sections_per_multipole"]) < 1e-9
     assert rel(c.force(), g["force"]) < 1e-9
     assert rel(c.torque(), g["torque"]) < 1e-9
+
+
+@pytest.mark.gpu
+def test_cluster_fields_match_reference_cluster():
+    """E and H of the reference's cluster.E_field / H_field (cluster.py:219-345): the
+    outgoing expansions plus the source outside, zero inside a particle's enclosed
+    radius (interior=True or mask=True), 1e-9 of the largest field."""
+    g, c = _reference_cluster()
+    x, y, z = g["field_x"], g["field_y"], g["field_z"]
+    assert rel(c.E_field(x, y, z), g["E_total"]) < 1e-9
+    assert rel(c.H_field(x, y, z), g["H_total"]) < 1e-9
+    assert rel(c.E_field(x, y, z, source=False, interior=False), g["E_scat_only"]) < 1e-9
+    assert rel(c.E_field(x, y, z, mask=True), g["E_masked"]) < 1e-9
 
 
 @pytest.mark.gpu
