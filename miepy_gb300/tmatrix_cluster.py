@@ -14,11 +14,13 @@ particle's T-matrix (``gb_solve_batch_tmatrix``); the dense aggregate is not for
 
 from __future__ import annotations
 
+import types
+
 import numpy as np
 import torch
 
 from . import _native as nat
-from .cluster import DEFAULT_MAXITER, DEFAULT_TOL, EXACT_TOL, _method_is_exact, cross_sections
+from .cluster import DEFAULT_MAXITER, DEFAULT_TOL, EXACT_TOL, _method_is_exact, cross_sections, sphere_cluster
 from .engine import ClusterBatch, current_stream
 from .materials import constant_material
 from .mie import mie_coefficients
@@ -67,12 +69,29 @@ class tmatrix_cluster:
 
     Keywords as the reference's cluster where they apply (source, wavelength, lmax,
     medium, interactions, method), plus precision ("fp64" default, "mixed", "fp32"),
-    tol, maxiter, device and enclosed_radius ([N], the radius of each particle's
-    circumscribing sphere, for the interior rule of the fields; none by default).
+    tol, maxiter, device, origin (of the cluster coefficients, default 0) and
+    enclosed_radius ([N], the radius of each particle's circumscribing sphere, for
+    the interior rule of the fields; none by default).
     """
 
+    # cluster coefficients, per-multipole cluster cross-sections and far fields
+    # depend only on positions, p_scat, the source and the medium: the sphere
+    # cluster's GPU implementations (cluster.py:379-391, 616-627)
+    solve_cluster_coefficients = sphere_cluster.solve_cluster_coefficients
+    cross_sections_per_multipole = sphere_cluster.cross_sections_per_multipole
+    _angular = sphere_cluster._angular
+
+    def E_angular(self, theta, phi, radius=None, source=False):
+        """Far-field E (theta, phi components) of the particles (cluster.py:349-362:
+        the far expansions evaluated at radius, by default one wavelength 2 pi / k)."""
+        return self._angular(theta, phi, 2 * np.pi / self.k_b if radius is None else radius, source, magnetic=False)
+
+    def H_angular(self, theta, phi, radius=None, source=False):
+        """Far-field H (theta, phi components) of the particles (cluster.py:364-377)."""
+        return self._angular(theta, phi, 2 * np.pi / self.k_b if radius is None else radius, source, magnetic=True)
+
     def __init__(self, *, position, tmatrix, source, wavelength, lmax, medium=None, interactions=True, method=None,
-                 precision="fp64", tol=None, maxiter=None, device=None, enclosed_radius=None):
+                 precision="fp64", tol=None, maxiter=None, device=None, enclosed_radius=None, origin=None):
         self.position = np.asarray(np.atleast_2d(position), dtype=float)
         N = self.position.shape[0]
         self.Nparticles = N
@@ -87,6 +106,9 @@ class tmatrix_cluster:
         if self.eps_b.imag != 0 or self.mu_b.imag != 0:
             raise ValueError("medium must be non-absorbing")
         self.k_b = 2 * np.pi * np.real(np.sqrt(self.eps_b * self.mu_b)) / wavelength
+        self.material_data = types.SimpleNamespace(k_b=self.k_b, eps_b=self.eps_b, mu_b=self.mu_b)
+        self.origin = np.zeros(3) if origin is None else np.asarray(origin, dtype=float)
+        self.p_cluster = None
         self.interactions, self.method, self.precision = interactions, method, precision
         self.tol, self.maxiter, self.device = tol, maxiter, device
         self.enclosed = np.zeros(N) if enclosed_radius is None else np.broadcast_to(
@@ -221,9 +243,8 @@ class cluster(tmatrix_cluster):
             T[i] = p.compute_tmatrix(lmax, wavelength, eps_m)
             if key is not None:
                 cache[key] = T[i]
-        self.origin = np.zeros(3) if origin is None else np.asarray(origin, dtype=float)
         enclosed = [p.enclosed_radius() if hasattr(p, "enclosed_radius") else 0.0 for p in self.particles]
         enclosed = [0.0 if e is None else float(e) for e in enclosed]
         super().__init__(position=[p.position for p in self.particles], tmatrix=T, source=source,
                          wavelength=wavelength, lmax=lmax, medium=medium, interactions=interactions, method=method,
-                         enclosed_radius=enclosed, **kw)
+                         enclosed_radius=enclosed, origin=origin, **kw)

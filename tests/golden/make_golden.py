@@ -234,7 +234,12 @@ def main():
                         agg_tmatrix=miepy.interactions.particle_aggregate_tmatrix(c.position, c.tmatrix, md.k_b),
                         field_x=fx, field_y=fy, field_z=fz, E_total=c.E_field(fx, fy, fz), H_total=c.H_field(fx, fy, fz),
                         E_scat_only=c.E_field(fx, fy, fz, source=False, interior=False),
-                        E_masked=c.E_field(fx, fy, fz, mask=True))
+                        E_masked=c.E_field(fx, fy, fz, mask=True),
+                        p_cluster=miepy.cluster_coefficients(c.position, c.p_scat, md.k_b, origin=c.origin, lmax=lm),
+                        cluster_xs_per_multipole=np.array([np.asarray(v) for v in c.cross_sections_per_multipole()]),
+                        far_theta=np.linspace(0.1, np.pi - 0.1, 5), far_phi=np.linspace(0.0, 2 * np.pi, 5),
+                        E_angular=c.E_angular(np.linspace(0.1, np.pi - 0.1, 5), np.linspace(0.0, 2 * np.pi, 5)),
+                        H_angular=c.H_angular(np.linspace(0.1, np.pi - 0.1, 5), np.linspace(0.0, 2 * np.pi, 5)))
     print("wrote tmatrix3_lmax3_exact")
 
     # periodic clusters (lattice row): the reference's own lattice sums

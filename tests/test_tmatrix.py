@@ -158,6 +158,20 @@ def test_cluster_fields_match_reference_cluster():
 
 
 @pytest.mark.gpu
+def test_cluster_coefficients_and_far_field_match_reference_cluster():
+    """p_cluster (vsh/cluster_coefficients.py:14-53), the cluster cross-sections per
+    multipole (cluster.py:379-391) and E/H_angular (cluster.py:349-377) of the
+    reference's cluster: 1e-10 for the coefficients, 1e-8 for the far fields."""
+    g, c = _reference_cluster()
+    assert rel(c.solve_cluster_coefficients(), g["p_cluster"]) < 1e-10
+    Cm = np.array([np.asarray(v) for v in c.cross_sections_per_multipole()])
+    assert rel(Cm, g["cluster_xs_per_multipole"]) < 1e-9
+    th, ph = g["far_theta"], g["far_phi"]
+    assert rel(c.E_angular(th, ph), g["E_angular"]) < 1e-8
+    assert rel(c.H_angular(th, ph), g["H_angular"]) < 1e-8
+
+
+@pytest.mark.gpu
 def test_cluster_mixed_precision_extinction():
     g, c = _reference_cluster(precision="mixed", tol=1e-10)
     assert c.solver_status == 0
