@@ -51,7 +51,9 @@ extern "C" {
 /* precision of a solve */
 #define GB_PREC_FP64 0           /* complex128 matrix, complex128 Krylov vectors, FP64 arithmetic */
 #define GB_PREC_MIXED 1          /* complex64 BiCGSTAB on the hi matrix; refinement residuals with the
-                                    double-float (hi + lo) matrix, ~1e-14 relative accuracy, FP32 pipes */
+                                    double-float (hi + lo) matrix, ~1e-14 relative accuracy, FP32 pipes;
+                                    once |r| <= 2.5e4 tol |b| the residual is updated as r -= (I+T) d
+                                    with the complex64 matrix */
 #define GB_PREC_FP32 2           /* complex64 matrix + complex64 BiCGSTAB, no refinement */
 #define GB_PREC_MIXED_FP64RES 3  /* as MIXED, refinement residuals in FP64 arithmetic on the complex128 matrix */
 
@@ -138,7 +140,10 @@ int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, 
  * prec: GB_PREC_FP64 uses mat128; GB_PREC_FP32 uses mat64; GB_PREC_MIXED runs
  * FP32 BiCGSTAB on mat64 to inner_tol and refines x with residuals computed
  * from mat64 + mat64lo until |b - (I+T)x| <= tol |b| (at most max_refine
- * refinement passes); GB_PREC_MIXED_FP64RES takes its residuals from mat128.
+ * refinement passes; once every running cluster has |r| <= 2.5e4 tol |b|, the
+ * next residual is updated from the correction d with mat64, whose ~2e-6
+ * relative product error then stays below tol |b| / 20);
+ * GB_PREC_MIXED_FP64RES takes its residuals from mat128.
  * status/iters/resid: host arrays of nsys*R entries (may be NULL); iters are
  * BiCGSTAB iterations (FP64/FP32) or refinement passes (mixed). */
 size_t gb_solve_workspace_size(int nsys, const gb_system* sys, int R, int prec);
