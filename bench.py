@@ -166,6 +166,8 @@ def run_gpu(args, rank, world):
 
     # ---- resident inputs
     batches = {p: ClusterBatch([spec], R=R, precision=p, device=dev) for p in ("mixed", "fp64")}
+    # measured GEMV lane shapes (gb_autotune_gemv) before any solve captures its graphs
+    gemv_shapes = {p: {str(B): list(v) for B, v in b.autotune().items()} for p, b in batches.items()}
     for p, b in batches.items():
         for _ in range(args.warmup):
             one_solve(b, p)
@@ -331,6 +333,7 @@ def run_gpu(args, rank, world):
         cext_rel_err_mixed_vs_fp64=cext_err, iterations_fp64=iters_fp64, refinement_passes_mixed=iters_mixed,
         e2e=dict(value=world * e2e_steps / t_e2e, unit="solves/s", h2d_bytes_per_step=int(h2d),
                  d2h_bytes_per_step=int(d2h)),
+        gemv_shapes=gemv_shapes,
         concurrent=dict(streams=CONC_STREAMS, solves_per_s=world * CONC_STREAMS * args.steps / t_conc,
                         p50_ms=float(np.percentile(per_c, 50)), p99_ms=float(np.percentile(per_c, 99)),
                         results_identical_across_streams=bool(conc_same), gpu_launches=int(launches_conc),
@@ -406,8 +409,11 @@ def run_sweep(args, rank=0, world=1):
     stream = torch.cuda.current_stream()
     L = nat_lib()
 
+    shapes = {}
+
     def timed(precision, steps, warmup):
         b = ClusterBatch(specs, R=1, precision=precision, device=dev)
+        shapes[precision] = {str(B): list(v) for B, v in b.autotune().items()}   # measured GEMV lane shapes
         for _ in range(warmup):
             b.assemble(); b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8); b.epilogue(1.0)
         torch.cuda.synchronize()
@@ -449,7 +455,7 @@ def run_sweep(args, rank=0, world=1):
                 p50_ms=float(np.percentile(m["per"], 50)), p99_ms=float(np.percentile(m["per"], 99)),
                 fp64_solves_per_s=W / d["t"], cext_rel_err_mixed_vs_fp64=err,
                 all_converged=bool(np.all(m["status"] == 0) and np.all(d["status"] == 0)),
-                lmax_histogram={int(l): int(np.sum(lm == l)) for l in np.unique(lm)},
+                lmax_histogram={int(l): int(np.sum(lm == l)) for l in np.unique(lm)}, gemv_shapes=shapes,
                 resident_matrix_gb=m["mat_bytes"] / 1e9, gpu_launches=int(m["launches"]),
                 phases_mixed=m["phases"], phases_fp64=d["phases"], clocks=clocks_info)
 

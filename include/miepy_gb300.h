@@ -181,6 +181,23 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
                    const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
                    size_t ws_bytes, void* stream);
 
+/* GEMV tile-shape autotuner (no counterpart in the reference, whose matvec is an
+ * Eigen/OpenMP row-block product, cpp/src/interactions.cpp:27-92).  For every
+ * block-size group of the batch, times each lane shape covering the block on the
+ * batch's own plan and matrix (reps passes per shape, CUDA events on stream) and
+ * keeps the fastest for that block size, precision class (GB_PREC_FP64: the
+ * complex128 pass; any other: the complex64 pass) and R, in a process-wide table
+ * that later solves use.  x [total_vec * R] is any vector (it feeds the y vectors),
+ * y receives one product; the workspace is gb_apply_workspace_size's for
+ * GB_PREC_FP64 or GB_PREC_FP32.  Call it outside stream capture. */
+int gb_autotune_gemv(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                     const double* tvec, const double* x, double* y, void* workspace, size_t ws_bytes, int reps,
+                     void* stream);
+
+/* The lane shape (lanes per matrix row, columns per lane) the GEMV uses for block
+ * size B, precision class and R: the autotuned one, else the model's. */
+int gb_gemv_shape(int B, int prec, int R, int* lanes_per_row, int* cols_per_lane);
+
 /* The operator product of gb_apply_batch launched reps times back to back on
  * one prepared plan (no host work between launches), for kernel timing with
  * events on the stream.  gemv_only != 0 repeats only the matrix pass (the

@@ -65,6 +65,8 @@ SIGNATURES = {
     "gb_apply_workspace_size": (c_size_t, [c_int, _P, c_int, c_int]),
     "gb_apply_batch": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_size_t, _P]),
     "gb_apply_repeat": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_size_t, c_int, c_int, _P]),
+    "gb_autotune_gemv": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, c_size_t, c_int, _P]),
+    "gb_gemv_shape": (c_int, [c_int, c_int, c_int, _P, _P]),
     "gb_epilogue_batch": (c_int, [c_int, _P, c_int, _P, _P, _P, _P, _P, _P, c_double, c_int, _P, _P, _P, _P, _P,
                                   _P]),
     "gb_solve_batch_tmatrix": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P,

@@ -42,7 +42,9 @@
 // with r = b - A x when |rho| < eps^2 |r0|^2, stop when |r|^2 <= tol^2 |b|^2.
 
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <map>
 #include <cstring>
 #include <mutex>
 #include <type_traits>
@@ -236,6 +238,7 @@ __device__ __forceinline__ void df_add(float& h, float& l, float h2, float l2) {
 }
 
 struct Pol64 {                 // complex128 matrix, FP64 FMAs
+    static constexpr int ID = 0;
     static constexpr int MB = 16;
     static constexpr bool DF = false;
     using YT = double2;
@@ -256,6 +259,7 @@ struct Pol64 {                 // complex128 matrix, FP64 FMAs
 };
 
 struct Pol32 {                 // complex64 matrix, packed FP32 FMAs
+    static constexpr int ID = 1;
     static constexpr int MB = 8;
     static constexpr bool DF = false;
     using YT = float4;         // (re, re, im, im)
@@ -285,6 +289,7 @@ struct Pol32 {                 // complex64 matrix, packed FP32 FMAs
 // a double-float complex float4 (re.h, im.h, re.l, im.l), about 1e-14 relative.
 struct DFAcc { float2 ha, la, hb, lb; };
 struct PolDF {
+    static constexpr int ID = 2;
     static constexpr int MB = 8;
     static constexpr bool DF = true;
     using YT = float4;
@@ -563,8 +568,8 @@ __host__ __device__ inline GemvLayout gemv_layout(int Bmax, int rows_per_chunk, 
     const int cpb = (Bmax + rows_per_chunk - 1) / rows_per_chunk;
     const int live = 1 + (S - 1 + cpb - 1) / cpb;
     g.nys = live < S ? live : S;
-    // + 256 B of padding: lanes whose columns lie past the block's end read (and
-    // discard) up to LPR-1 elements beyond the last stage
+    // + 256 B of padding (kGemvPad): lanes whose columns lie past the block's end
+    // read (and discard) the elements after the last stage (shape_fits bounds it)
     g.warp_bytes = 128 + (g.nys + 1) * g.y_bytes + S * g.chunk_cap * (df ? 2 : 1) + 256;
     return g;
 }
@@ -1772,16 +1777,38 @@ struct Shape { int lpr, cpl; };
 
 // Lanes per row and columns per lane for a block size: the fewest idle lanes
 // (LPR*CPL >= Bmax), ties to more columns per lane.
+constexpr Shape kShapes[] = {{8, 1}, {8, 2}, {8, 4}, {16, 3}, {16, 5}, {32, 3}, {32, 4}, {32, 5}};
+
 Shape pick_shape(int Bmax) {
-    static const Shape cands[] = {{8, 1}, {8, 2}, {8, 4}, {16, 3}, {16, 5}, {32, 3}, {32, 4}, {32, 5}};
     Shape best{0, 0};
     double beff = -1;
-    for (const Shape& c : cands) {
+    for (const Shape& c : kShapes) {
         if (c.lpr * c.cpl < Bmax) continue;
         const double eff = double(Bmax) / (c.lpr * c.cpl);
         if (eff > beff + 1e-9 || (std::fabs(eff - beff) < 1e-9 && c.cpl > best.cpl)) { beff = eff; best = c; }
     }
     return best;
+}
+
+// A lane reads columns up to LPR*CPL - 1 of every row; past a block's last column
+// those reads land in the next row, the next stage or, after a warp's last stage,
+// the kGemvPad bytes of padding that gemv_layout adds.  A shape may overshoot the
+// block by no more than that padding (the model's shapes overshoot by at most
+// 10 elements of 16 B).
+constexpr int kGemvPad = 256;
+inline bool shape_fits(const Shape& c, int B, int elem_bytes) {
+    return c.lpr * c.cpl >= B && (c.lpr * c.cpl - B) * elem_bytes <= kGemvPad;
+}
+
+// Shapes measured by gb_autotune_gemv, per (block size, policy, RR, RT); the model
+// above where none was measured.
+std::mutex g_tune_mu;
+std::map<std::array<int, 4>, Shape> g_tuned;
+
+Shape tuned_shape(int B, int pol, int RR, int RT) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto f = g_tuned.find({B, pol, RR, RT});
+    return f != g_tuned.end() ? f->second : pick_shape(B);
 }
 
 // Steps per chunk for a shape: chunks of about 6 KB of matrix for the block size
@@ -1798,13 +1825,18 @@ constexpr int gemv_steps(int lpr, int cpl, int elem_bytes) {
 template <class Pol, int RR, int RT>
 int launch_pgemv_group(const Plan& P, const DevPlan& D, const StripGroup& grp, const KState* st, int mask,
                        const void* mat_hi, const void* mat_lo, const void* Yu, const void* Yw, void* CU, void* CW,
-                       int rr0, int* err, cudaStream_t stream) {
+                       int rr0, int* err, cudaStream_t stream, const Shape* force = nullptr) {
     using YT = typename Pol::YT;
     using OutT = typename Pol::OutT;
     constexpr int S = 3;   // stages per warp: one being read, two in flight
     const int Bmax = grp.B;
-    const Shape sh = pick_shape(Bmax);
+    // the double-float pass keeps the model's shape: launch_df splits the right-hand
+    // sides by that shape's width
+    const Shape sh = force ? *force : (Pol::DF ? pick_shape(Bmax) : tuned_shape(Bmax, Pol::ID, RR, RT));
     if (sh.lpr == 0) return gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", Bmax);
+    if (!shape_fits(sh, Bmax, Pol::MB))
+        return gb_set_error(GB_UNSUPPORTED, "GEMV shape %dx%d overruns the %d-column block's padding", sh.lpr, sh.cpl,
+                            Bmax);
     const int rpw = 32 / sh.lpr;
     const int G = gemv_steps(sh.lpr, sh.cpl, Pol::MB * (Pol::DF ? 2 : 1));
     const GemvLayout g = gemv_layout(Bmax, G * rpw, RT, S, Pol::MB, Pol::DF, sizeof(YT));
@@ -2483,6 +2515,95 @@ int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, doub
                              status, iters, resid, s);
     return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, nullptr, b, x, base, w,
                          status, iters, resid, s);
+}
+
+// Measured GEMV shapes: for every block-size group of the batch, each lane shape
+// that covers the block (LPR * CPL >= B) runs reps matrix passes on the batch's own
+// plan and matrices, timed with events; the fastest is kept for that (block size,
+// policy, R) in a process-wide table that later launches read.  Run outside stream
+// capture (the graphs of a solve keep the shapes they were captured with).
+int gb_autotune_gemv(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                     const double* tvec, const double* x, double* y, void* workspace, size_t ws_bytes, int reps,
+                     void* stream) {
+    if (nsys < 1 || !sys || !tvec || !x || !y || !workspace || reps < 1) return gb_set_error(GB_BAD_ARG, "bad argument");
+    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
+    const bool f64 = prec == GB_PREC_FP64;
+    if ((f64 && !mat128) || (!f64 && !mat64)) return gb_set_error(GB_BAD_ARG, "matrix missing for precision %d", prec);
+    const int aprec = f64 ? GB_PREC_FP64 : GB_PREC_FP32;
+    cudaStream_t s = (cudaStream_t)stream;
+    Plan P;
+    int e = build_plan(nsys, sys, R, s, P);
+    if (e) return e;
+    WS w = ws_layout(P, aprec, false);
+    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
+    unsigned char* base = static_cast<unsigned char*>(workspace);
+    DevPlan D;
+    e = upload_plan(P, base, w, s, D);
+    if (e) return e;
+    KState* st = reinterpret_cast<KState*>(base + w.off_state);
+    double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
+    const int pol = f64 ? 0 : 1;
+    const void* hi = f64 ? (const void*)mat128 : (const void*)mat64;
+    // one product prepares the y vectors the passes read
+    e = R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, nullptr, reinterpret_cast<const double2*>(tvec),
+                                          reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), 0,
+                                          nullptr, nullptr, dots, s)
+               : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, nullptr, reinterpret_cast<const double2*>(tvec),
+                                          reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y), 0,
+                                          nullptr, nullptr, dots, s);
+    if (e) return e;
+    void* Yu = base + w.off_yu;
+    void* Yw = base + w.off_yw;
+    void* CU = base + w.off_cu;
+    void* CW = base + w.off_cw;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    GB_CUDA_TRY(cudaEventCreate(&e0));
+    GB_CUDA_TRY(cudaEventCreate(&e1));
+    auto pass = [&](const StripGroup& grp, const Shape& c) -> int {
+        if (f64)
+            return R == 1 ? launch_pgemv_group<Pol64, 1, 1>(P, D, grp, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s, &c)
+                          : launch_pgemv_group<Pol64, 2, 2>(P, D, grp, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s, &c);
+        return R == 1 ? launch_pgemv_group<Pol32, 1, 1>(P, D, grp, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s, &c)
+                      : launch_pgemv_group<Pol32, 2, 2>(P, D, grp, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s, &c);
+    };
+    for (const StripGroup& grp : P.groups) {
+        if (grp.end == grp.beg) continue;
+        Shape best{0, 0};
+        float tbest = 0;
+        for (const Shape& c : kShapes) {
+            if (!shape_fits(c, grp.B, f64 ? Pol64::MB : Pol32::MB)) continue;
+            e = pass(grp, c);   // warm-up (also rejects a shape whose shared memory does not fit)
+            if (e == GB_UNSUPPORTED) continue;
+            if (e) break;
+            GB_CUDA_TRY(cudaEventRecord(e0, s));
+            for (int k = 0; k < reps && !e; k++) e = pass(grp, c);
+            if (e) break;
+            GB_CUDA_TRY(cudaEventRecord(e1, s));
+            GB_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0;
+            GB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (best.lpr == 0 || ms < tbest) { best = c; tbest = ms; }
+        }
+        if (e) break;
+        if (best.lpr) {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tuned[{grp.B, pol, R, R}] = best;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e) return e;
+    return check_device_error(D, s);
+}
+
+// The shape GEMV launches use for block size B, policy (0 complex128, 1 complex64)
+// and R right-hand sides: the measured one, or the model's.
+int gb_gemv_shape(int B, int prec, int R, int* lanes_per_row, int* cols_per_lane) {
+    if (!lanes_per_row || !cols_per_lane || B < 1) return gb_set_error(GB_BAD_ARG, "bad argument");
+    const Shape sh = tuned_shape(B, prec == GB_PREC_FP64 ? 0 : 1, R, R);
+    *lanes_per_row = sh.lpr;
+    *cols_per_lane = sh.cpl;
+    return sh.lpr ? GB_OK : gb_set_error(GB_UNSUPPORTED, "no GEMV shape for block size %d", B);
 }
 
 size_t gb_apply_workspace_size(int nsys, const gb_system* sys, int R, int prec) {

@@ -9,6 +9,7 @@ one class; every step is a call into the CUDA extension.
 
 from __future__ import annotations
 
+import ctypes
 import threading
 
 import numpy as np
@@ -296,6 +297,34 @@ class ClusterBatch:
                                     nat.ptr(self._ws), self._ws.numel(), int(reps), int(bool(gemv_only)),
                                     current_stream(self.device)), "apply_repeat")
         return y
+
+    def autotune(self, precision=None, reps=5):
+        """Measure the GEMV lane shapes of this batch's block sizes (gb_autotune_gemv)
+        for the matrix pass of precision (default: the batch's; "fp64" tunes the
+        complex128 pass, the others the complex64 one).  Returns {B: (lanes per row,
+        columns per lane)}.  Solves captured before keep their shapes."""
+        L = nat.lib()
+        prec = self.precision if precision is None else precision
+        code = PRECISIONS["fp64" if prec == "fp64" else "fp32"]
+        if code == PRECISIONS["fp64"] and self.mat128 is None or code != PRECISIONS["fp64"] and self.mat64 is None:
+            raise ValueError(f"this batch holds no matrix for {prec}")
+        need = L.gb_apply_workspace_size(self.nsys, self.sys, self.R, code)
+        ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        x = torch.zeros(max(self.totals["vec"], 1), dtype=torch.complex128, device=self.device)
+        y = torch.empty_like(x)
+        if self.totals["mat"] == 0:
+            return {}
+        if not self.assembled:
+            self.assemble()
+        nat.check(L.gb_autotune_gemv(self.nsys, self.sys, self.R, code, nat.ptr(self.mat128), nat.ptr(self.mat64),
+                                     nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y), nat.ptr(ws), ws.numel(), int(reps),
+                                     current_stream(self.device)), "autotune")
+        out = {}
+        for B in sorted({2 * l["rmax"] for l in self.layout if l["N"] > 1}):
+            lpr, cpl = ctypes.c_int(0), ctypes.c_int(0)
+            nat.check(L.gb_gemv_shape(B, code, self.R, ctypes.byref(lpr), ctypes.byref(cpl)), "gemv shape")
+            out[B] = (lpr.value, cpl.value)
+        return out
 
     def epilogue(self, eps_b, source=True, want_fields=True):
         """p_scat, p_int (device, [total_vec]) and per particle xs [N,R,3,2*Lx]
