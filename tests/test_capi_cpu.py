@@ -108,3 +108,18 @@ def test_no_cpu_fallback_when_cuda_missing():
     with pytest.raises(RuntimeError, match="CUDA"):
         gb.sphere_cluster(position=[[0, 0, 0], [3e-7, 0, 0]], radius=5e-8, material=gb.constant_material(index=1.5),
                           source=gb.plane_wave.from_string("x"), wavelength=6e-7, lmax=2)
+
+
+@pytest.mark.parametrize("lmax", range(1, 9))
+def test_model_gemv_shapes_stay_within_the_padding(lmax):
+    """The GEMV lane shape the launches use without autotuning covers the block, and
+    its column overshoot fits the 256 B of shared-memory padding after a warp's last
+    stage for complex128 (16 B) elements (host-side shape logic only, no GPU)."""
+    lib = _native.lib()
+    B = 2 * lmax * (lmax + 2)
+    for prec in (0, 2):   # GB_PREC_FP64 (complex128 pass), GB_PREC_FP32 (complex64 pass)
+        lpr, cpl = ctypes.c_int(0), ctypes.c_int(0)
+        assert lib.gb_gemv_shape(B, prec, 2, ctypes.byref(lpr), ctypes.byref(cpl)) == 0
+        cols = lpr.value * cpl.value
+        assert cols >= B
+        assert (cols - B) * 16 <= 256
