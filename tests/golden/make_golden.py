@@ -239,7 +239,10 @@ def main():
                         cluster_xs_per_multipole=np.array([np.asarray(v) for v in c.cross_sections_per_multipole()]),
                         far_theta=np.linspace(0.1, np.pi - 0.1, 5), far_phi=np.linspace(0.0, 2 * np.pi, 5),
                         E_angular=c.E_angular(np.linspace(0.1, np.pi - 0.1, 5), np.linspace(0.0, 2 * np.pi, 5)),
-                        H_angular=c.H_angular(np.linspace(0.1, np.pi - 0.1, 5), np.linspace(0.0, 2 * np.pi, 5)))
+                        H_angular=c.H_angular(np.linspace(0.1, np.pi - 0.1, 5), np.linspace(0.0, 2 * np.pi, 5)),
+                        T_sphere_metal=miepy.tmatrix.tmatrix_sphere(60 * nm, 600 * nm, -10 + 1j, 1.33 ** 2, lm,
+                                                                    conducting=True),
+                        T_sphere_lossy=miepy.tmatrix.tmatrix_sphere(90 * nm, 700 * nm, 4.0 + 0.8j, 1.0, lm))
     print("wrote tmatrix3_lmax3_exact")
 
     # periodic clusters (lattice row): the reference's own lattice sums

@@ -276,3 +276,14 @@ def test_cluster_without_interactions():
                    medium=gb.constant_material(index=1.33), interactions=False)
     assert rel(c.p_inc, g["p_src"]) < 1e-12
     assert rel(c.p_scat, np.einsum("naibj,nbj->nai", g["tmatrix"], g["p_src"])) < 1e-12
+
+
+def test_sphere_tmatrix_conducting_and_lossy_match_reference():
+    """tmatrix_sphere (tmatrix/common.py:6-28) for a perfect conductor and a lossy
+    dielectric in vacuum, against the reference's own T-matrices."""
+    import miepy_gb300 as gb
+    g = fixture()
+    T = gb.tmatrix_sphere(60 * nm, 600 * nm, -10 + 1j, 1.33 ** 2, 3, conducting=True)
+    assert rel(T, g["T_sphere_metal"]) < 1e-12
+    T = gb.tmatrix_sphere(90 * nm, 700 * nm, 4.0 + 0.8j, 1.0, 3)
+    assert rel(T, g["T_sphere_lossy"]) < 1e-12
