@@ -381,6 +381,49 @@ class sphere_cluster:
     def E_field(self, x1, x2, x3, interior=True, source=True, mask=False, far=False, spherical=False):
         return self._field(x1, x2, x3, interior, source, mask, far, spherical, magnetic=False)
 
+    def _field_from_particle(self, i, x, y, z, source, magnetic):
+        """sphere_cluster.py:150-200: particle i's outgoing expansion of p_scat plus its
+        regular (j_n, incident) expansion of p_inc (p_inc - p_src without the source),
+        about its own centre, at every point.  Two launches of the GPU near-field
+        kernel: exterior sums only, then the regular expansion alone (every point
+        counts as inside a sphere of unbounded radius, with k_b as its wavenumber)."""
+        x, y, z = np.broadcast_arrays(*(np.asarray(v, dtype=float) for v in (x, y, z)))
+        shape = x.shape
+        pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+        dev = self._batch.device
+        md = self.material_data
+        k = float(np.real(md.k_b))
+        d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+        pos = d(self.position[i: i + 1], torch.float64)
+        ps = d(self.p_scat[i: i + 1], torch.complex128)
+        p_reg = self.p_inc[i] - (0 if source else self.p_src[i])
+        pr = d(p_reg[None], torch.complex128)
+        zeros = torch.zeros_like(ps)
+        P = d(pts, torch.float64)
+        hfac = complex(-1j * np.sqrt(md.eps_b / md.mu_b)) if magnetic else 1.0 + 0j
+        k_reg = torch.full((1,), k, dtype=torch.complex128, device=dev)
+        h_reg = torch.full((1,), hfac, dtype=torch.complex128, device=dev)
+        big = torch.full((1,), 1e150, dtype=torch.float64, device=dev)
+        L = nat.lib()
+        outs = []
+        for interior, cs, ci, rad in ((0, ps, zeros, big), (1, zeros, pr, big)):
+            out = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
+            nat.check(L.gb_near_field(1, self.lmax, nat.ptr(pos), nat.ptr(rad), nat.ptr(cs), nat.ptr(ci), k,
+                                      nat.ptr(k_reg), pts.shape[0], nat.ptr(P), interior, int(bool(magnetic)),
+                                      float(hfac.real), float(hfac.imag), nat.ptr(h_reg), nat.ptr(out),
+                                      current_stream(dev)), "field from particle")
+            outs.append(out)
+        E = (outs[0] + outs[1]).cpu().numpy().T.reshape((3,) + shape)
+        return E
+
+    def E_field_from_particle(self, i, x, y, z, source=True):
+        """Electric field of particle i's expansions (sphere_cluster.py:150-173)."""
+        return self._field_from_particle(i, x, y, z, source, magnetic=False)
+
+    def H_field_from_particle(self, i, x, y, z, source=True):
+        """Magnetic field of particle i's expansions (sphere_cluster.py:175-200)."""
+        return self._field_from_particle(i, x, y, z, source, magnetic=True)
+
     def H_field(self, x1, x2, x3, interior=True, source=True, mask=False, far=False, spherical=False):
         return self._field(x1, x2, x3, interior, source, mask, far, spherical, magnetic=True)
 

@@ -92,6 +92,18 @@ def main():
     cluster_record(miepy, "dimer_lmax6_exact", miepy.sphere_cluster(**kw, method=miepy.solver.exact),
                    store_matrix=True, field_pts=pts)
     cluster_record(miepy, "dimer_lmax6_bicgstab", miepy.sphere_cluster(**kw))
+    # fields of one particle's expansions (sphere_cluster.py:150-200), at kr >= 10 from
+    # particle 0 (the regular expansion's upward recurrence stays accurate there);
+    # source=False last: the reference subtracts p_src from p_inc in place
+    c = miepy.sphere_cluster(**kw, method=miepy.solver.exact)
+    fx = np.array([700, -800, 100, 0.0, -500]) * nm
+    fy = np.array([0.0, 300, 900, -850, 600]) * nm
+    fz = np.array([200, -100, 50, 300, -400]) * nm
+    rec = dict(field_x=fx, field_y=fy, field_z=fz, E0=c.E_field_from_particle(0, fx, fy, fz),
+               H0=c.H_field_from_particle(0, fx, fy, fz), E1=c.E_field_from_particle(1, fx, fy, fz))
+    rec["E0_nosource"] = c.E_field_from_particle(0, fx, fy, fz, source=False)
+    np.savez_compressed(os.path.join(HERE, "dimer_lmax6_field_from_particle.npz"), **rec)
+    print("wrote dimer_lmax6_field_from_particle")
 
     # five Ag spheres, rhc, lmax 2 (the reference's multi-particle BiCGSTAB case)
     Ag = miepy.materials.Ag()

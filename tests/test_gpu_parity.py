@@ -264,6 +264,20 @@ def test_public_cluster_api_dimer():
         assert rel(Fi, g["force"][i]) < 1e-9
 
 
+def test_field_from_particle_matches_reference():
+    """E/H_field_from_particle (sphere_cluster.py:150-200) of the dimer at kr >= 9 from
+    the particle, with and without the source: 1e-9 of the largest field."""
+    g = G.load("dimer_lmax6_field_from_particle")
+    c = gb.sphere_cluster(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm,
+                          material=gb.constant_material(index=0.2 + 3.0j), source=gb.plane_wave.from_string("x"),
+                          wavelength=600 * nm, lmax=6, medium=gb.materials.water(), method=gb.solver.exact)
+    x, y, z = g["field_x"], g["field_y"], g["field_z"]
+    assert rel(c.E_field_from_particle(0, x, y, z), g["E0"]) < 1e-9
+    assert rel(c.H_field_from_particle(0, x, y, z), g["H0"]) < 1e-9
+    assert rel(c.E_field_from_particle(1, x, y, z), g["E1"]) < 1e-9
+    assert rel(c.E_field_from_particle(0, x, y, z, source=False), g["E0_nosource"]) < 1e-9
+
+
 def test_near_fields_match_reference():
     for name in ("dimer_lmax6_exact", "rand12_lmax3_exact"):
         g = G.load(name)
