@@ -165,8 +165,9 @@ int gb_solve_dense(int D, int R, const double* T, const double* b, double* x, do
  * The solve (same arguments and results as gb_solve_dense) runs in a fixed scratch
  * array of 1.25 MiB that the library carries in device memory; D * R may be at most
  * 8192, larger sizes return GB_OVER_BUDGET.  No cudaMalloc, cudaFree or pinned host
- * buffer is used.  The first call on each device looks up the array's address on
- * that device (make it before any stream capture begins).  All calls on a device
+ * buffer is used.  Every call looks up the array's address in the current device's
+ * context; the first call on a device may load the library's module there, so make
+ * it before any stream capture begins.  All calls on a device
  * share the one array and it keeps the previous call's contents: calls whose work
  * overlaps on the GPU (other streams, other host threads) race on it. */
 int gb_solve_dense_noalloc(int D, int R, const double* T, const double* b, double* x, double tol, int maxiter,
@@ -205,6 +206,16 @@ int gb_gemv_shape(int B, int prec, int R, int* lanes_per_row, int* cols_per_lane
 int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
                     const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
                     size_t ws_bytes, int reps, int gemv_only, void* stream);
+
+/* Wait limit of the GEMV's consumer waits on its matrix copies, in SM clock cycles
+ * (no counterpart in the reference, whose matvec has no asynchronous copies).  A
+ * wait that expires sets the launch's error flag and the call returns GB_TIMEOUT;
+ * the warp first drains its own copies in flight with the default limit.  cycles = 0
+ * makes every consumer wait expire at once (a test of that path); cycles < 0
+ * restores the default (4e8 cycles, about 0.2 s).  The limit is per device (the
+ * current one), read by every later launch, graph replays included.  previous, if
+ * not null, receives the limit before the call. */
+int gb_set_gemv_wait_limit(long long cycles, long long* previous);
 
 /* -------------------------------------------------------------- epilogue --
  * Per cluster and right-hand side, from p_inc [D][R] (c128), p_src [D][R],

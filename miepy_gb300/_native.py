@@ -67,6 +67,7 @@ SIGNATURES = {
     "gb_apply_repeat": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_size_t, c_int, c_int, _P]),
     "gb_autotune_gemv": (c_int, [c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, c_size_t, c_int, _P]),
     "gb_gemv_shape": (c_int, [c_int, c_int, c_int, _P, _P]),
+    "gb_set_gemv_wait_limit": (c_int, [ctypes.c_longlong, _P]),
     "gb_epilogue_batch": (c_int, [c_int, _P, c_int, _P, _P, _P, _P, _P, _P, c_double, c_int, _P, _P, _P, _P, _P,
                                   _P]),
     "gb_solve_batch_tmatrix": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P,

@@ -542,14 +542,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait: about 0.2 s of clock at most
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+// bounded wait: at most lim cycles of clock (about 0.2 s by default); lim <= 0
+// expires at once without waiting
+constexpr long long kWaitCycles = 400000000LL;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, long long lim = kWaitCycles) {
+    if (lim <= 0) return false;
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > 400000000LL) return false;
+        if (clock64() - t0 > lim) return false;
     return true;
 }
+
+}   // namespace
+
+// Limit of the GEMV's consumer waits (the waits for a matrix chunk to land), read by
+// every launch; gb_set_gemv_wait_limit changes it.  The waits that drain a warp's
+// copies in flight after a failure always use kWaitCycles, so that no bulk copy is
+// still landing in shared memory when its CTA exits.
+static __device__ long long g_gemv_wait_cycles = kWaitCycles;
+
+namespace {
 
 struct GemvLayout {
     int chunk_cap, y_bytes, nys, warp_bytes;
@@ -620,6 +633,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     bool failed = false;
     int in_flight = 0;                    // chunks issued and not yet consumed
     const uint64_t stream_pol = l2_evict_first_policy();
+    const long long wait_lim = g_gemv_wait_cycles;
     pdl_wait();                           // y vectors and scalars of the predecessors
     pdl_trigger();
     for (long long w = sbeg + warp; w < send && !failed; w += nwarps) {
@@ -685,7 +699,7 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
                     issued++;
                     in_flight++;
                 }
-                const bool ok = mbar_wait_bounded(bars + cstage, cphase);
+                const bool ok = mbar_wait_bounded(bars + cstage, cphase, wait_lim);
                 if (!__all_sync(0xffffffffu, ok)) {   // warp-uniform decision
                     if (lane == 0) atomicExch(err, 1);
                     failed = true;
@@ -2386,9 +2400,6 @@ bool prec_ok(int prec, const double* m128, const float* m64, const float* m64lo)
 // would synchronise the device) can still solve.  Enough for D * R <= 8192.
 constexpr size_t kNoAllocScratchBytes = 1280u * 1024u;
 constexpr long long kNoAllocMaxDR = 8192;
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices];
 
 }   // namespace
 
@@ -2396,21 +2407,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 
-// Device address of the scratch array on the current device, looked up once per
-// device (the lookup may load the library's module onto that device).
+// Device address of the scratch array in the current device's context.  Looked up
+// on every call (a host-side table lookup once the module is loaded; the first
+// call on a device may load the module there), so that an address never outlives
+// the context it belongs to (cudaDeviceReset, a context torn down and recreated).
 int noalloc_scratch(unsigned char** out) {
-    int dev = 0;
-    GB_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return gb_set_error(GB_UNSUPPORTED, "device %d is beyond the %d devices the scratch table covers", dev,
-                            kNoAllocMaxDevices);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_addr[dev] = p;
-    }
-    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    void* p = nullptr;
+    GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    *out = static_cast<unsigned char*>(p);
     return GB_OK;
 }
 
@@ -2710,6 +2714,15 @@ int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const doubl
         if (e) return e;
     }
     return check_device_error(D, s);
+}
+
+int gb_set_gemv_wait_limit(long long cycles, long long* previous) {
+    long long old = 0;
+    GB_CUDA_TRY(cudaMemcpyFromSymbol(&old, g_gemv_wait_cycles, sizeof(old)));
+    const long long v = cycles < 0 ? kWaitCycles : cycles;
+    GB_CUDA_TRY(cudaMemcpyToSymbol(g_gemv_wait_cycles, &v, sizeof(v)));
+    if (previous) *previous = old;
+    return GB_OK;
 }
 
 size_t gb_solve_dense_workspace_size(int D, int R) {

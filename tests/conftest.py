@@ -7,9 +7,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-# Reference source tree (read only; present in the build container, absent on GPU
-# hosts).  Tests that need it skip when it is missing.
-os.environ.setdefault("MIEPY_REFERENCE_SRC", "/root/reference/src")
+# The reference's Python layer, staged into the git-ignored baseline/_ref by
+# oracle/stage_reference.py (MIEPY_REFERENCE_SRC overrides it).  Tests that need it
+# skip when it is missing.
+_STAGED = os.path.join(ROOT, "baseline", "_ref", "src")
+if os.path.isdir(os.path.join(_STAGED, "miepy")):
+    os.environ.setdefault("MIEPY_REFERENCE_SRC", _STAGED)
 
 
 def pytest_configure(config):

@@ -203,9 +203,6 @@ def test_mixed_precision_meets_fp64_within_1e6():
     N, lmax = 40, 4
     pos, rad = random_cluster(rng, N, 50 * nm, 100 * nm, 1200 * nm)
     mat = gb.constant_material(index=1.5 + 0.01j)
-    specs = []
-    for pol in ("x", "y"):
-        pass
     c64 = gb.sphere_cluster(position=pos, radius=rad, material=mat, source=gb.plane_wave.from_string("x"),
                             wavelength=600 * nm, lmax=lmax, precision="mixed", tol=1e-10)
     c64r = gb.sphere_cluster(position=pos, radius=rad, material=mat, source=gb.plane_wave.from_string("x"),

@@ -1,10 +1,15 @@
-"""The no-allocation dense solve against the workspace dense solve.
+"""The no-allocation dense solve against the workspace dense solve and the reference.
 
 gb_solve_dense_noalloc runs the same FP64 BiCGSTAB as gb_solve_dense in a fixed
-device scratch array instead of a caller workspace.  Two calls in a row (of
-different sizes, so that the second meets the first one's leftovers in the shared
-array) must each agree with gb_solve_dense on the same input within the dense
-solve's bar: rtol 1e-10, atol 1e-14 of the largest coefficient.
+device scratch array instead of a caller workspace.  It is for callers that cannot
+allocate device memory (HBM reserved up front, or loops in which cudaMalloc/cudaFree
+would synchronise the device).  Two calls in a row (of different sizes, so that the
+second meets the first one's leftovers in the shared array) must each agree with
+gb_solve_dense on the same input and with the p_inc of the reference's exact solve
+in the golden fixture (right-hand side q is p_src (1 + 0.5i q), so its solution is
+p_inc (1 + 0.5i q)), within the dense solve's bar: rtol 1e-10, atol 1e-14 of the
+largest coefficient.  Repeated calls leave the device's free memory and the torch
+allocator's reservation unchanged.
 """
 
 import numpy as np
@@ -18,6 +23,7 @@ from tests import _golden as G
 pytestmark = pytest.mark.gpu
 
 EXACT_TOL = 1e-14
+CASES = (("dimer_lmax6_exact", 2), ("ag5_lmax2_exact", 1))   # a larger system with two right-hand sides, then a smaller
 
 
 def _dense_inputs(name, R):
@@ -25,8 +31,10 @@ def _dense_inputs(name, R):
     p_src = np.asarray(g["p_src"], dtype=complex)
     D = p_src.size
     T = np.ascontiguousarray(np.asarray(g["agg_tmatrix"], dtype=complex).reshape(D, D))
-    b = np.stack([p_src.reshape(-1) * (1.0 + 0.5j * q) for q in range(R)], axis=1)   # [D][R]
-    return D, T, np.ascontiguousarray(b)
+    scale = np.array([1.0 + 0.5j * q for q in range(R)])
+    b = p_src.reshape(-1, 1) * scale[None, :]                       # [D][R]
+    want = np.asarray(g["p_inc"], dtype=complex).reshape(-1, 1) * scale[None, :]
+    return D, T, np.ascontiguousarray(b), want
 
 
 def _solve_workspace(L, dev, D, R, T, b):
@@ -40,8 +48,7 @@ def _solve_workspace(L, dev, D, R, T, b):
     return x.cpu().numpy()
 
 
-def _solve_noalloc(L, dev, D, R, T, b):
-    x = torch.full_like(b, complex(np.nan, np.nan))
+def _noalloc_call(L, dev, D, R, T, b, x):
     status = np.zeros(R, np.int32)
     iters = np.zeros(R, np.int32)
     resid = np.zeros(R)
@@ -50,21 +57,43 @@ def _solve_noalloc(L, dev, D, R, T, b):
     assert rc in (nat.GB_OK, nat.GB_NOT_CONVERGED), nat.last_error()
     torch.cuda.synchronize(dev)
     assert np.all(iters > 0)
-    return x.cpu().numpy()
 
 
-def test_noalloc_dense_solve_matches_workspace_solve():
+def test_noalloc_dense_solve_matches_workspace_solve_and_reference():
     L = nat.lib()
     dev = torch.device("cuda:0")
     torch.cuda.set_device(dev)
-    # two calls in a row: a larger system with two right-hand sides, then a smaller one
-    for name, R in (("dimer_lmax6_exact", 2), ("ag5_lmax2_exact", 1)):
-        D, Tn, bn = _dense_inputs(name, R)
+    for name, R in CASES:
+        D, Tn, bn, want = _dense_inputs(name, R)
         T = torch.from_numpy(Tn).to(dev)
         b = torch.from_numpy(bn).to(dev)
         ref = _solve_workspace(L, dev, D, R, T, b)
-        got = _solve_noalloc(L, dev, D, R, T, b)
+        x = torch.full_like(b, complex(np.nan, np.nan))
+        _noalloc_call(L, dev, D, R, T, b, x)
+        got = x.cpu().numpy()
         np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-14 * np.max(np.abs(ref)))
+        np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-14 * np.max(np.abs(want)))
+
+
+def test_noalloc_calls_leave_device_memory_unchanged():
+    L = nat.lib()
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    bufs = []
+    for name, R in CASES:   # every input and output exists before the measured calls
+        D, Tn, bn, _ = _dense_inputs(name, R)
+        b = torch.from_numpy(bn).to(dev)
+        bufs.append((D, R, torch.from_numpy(Tn).to(dev), b, torch.empty_like(b)))
+    for D, R, T, b, x in bufs:   # warm-up: modules and kernels of both sizes loaded
+        _noalloc_call(L, dev, D, R, T, b, x)
+    free0, _ = torch.cuda.mem_get_info(dev)
+    reserved0 = torch.cuda.memory_reserved(dev)
+    for _ in range(2):
+        for D, R, T, b, x in bufs:
+            _noalloc_call(L, dev, D, R, T, b, x)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0, f"device free memory changed by {free0 - free1} B"
+    assert torch.cuda.memory_reserved(dev) == reserved0
 
 
 def test_noalloc_rejects_oversize():
