@@ -6,7 +6,9 @@ inputs and outputs of the sphere-cluster path as small ``.npz`` files.  The GPU
 parity tests compare the product against these fixtures without needing the
 reference tree at run time.
 
-Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py
+Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large]
+        (or with the reference staged by oracle/stage_reference.py:
+         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large])
 """
 
 import os
@@ -309,5 +311,106 @@ def main():
     print("wrote special_tables")
 
 
+def _observables(c):
+    """p coefficients, cross-sections (total and per particle per multipole), force
+    and torque of a solved reference cluster."""
+    C = c.cross_sections()
+    return dict(
+        p_src=c.p_src, p_inc=c.p_inc, p_scat=c.p_scat, p_int=c.p_int,
+        cross_sections=np.array([C.scattering, C.absorption, C.extinction], dtype=float),
+        cross_sections_per_multipole=np.array([[np.asarray(v) for v in c.cross_sections_per_multipole_of_particle(i)]
+                                               for i in range(c.Nparticles)], dtype=float),
+        force=c.force(), torque=c.torque())
+
+
+def _lapack_exact(miepy):
+    """Route the exact solve (method=solver.exact) of the oracle standing in for
+    miepy.cpp to LAPACK's partial-pivot LU (numpy.linalg.solve): the same algorithm
+    class as the reference's Eigen partialPivLu, multithreaded, so that systems of
+    D = 10^4 - 3 10^4 solve in seconds to minutes.  (I + T) is formed in place on
+    the reference's aggregate and restored afterwards."""
+    interactions = sys.modules["miepy.cpp.interactions"]
+    plain = interactions.solve_linear_system
+
+    def solve(agg, p_src, method=None, *a, **k):
+        if getattr(method, "name", method) != "exact":
+            return plain(agg, p_src, method, *a, **k)
+        D = p_src.size
+        A = agg.reshape(D, D)
+        A[np.diag_indices(D)] += 1.0
+        try:
+            return np.linalg.solve(A, p_src.reshape(D))
+        finally:
+            A[np.diag_indices(D)] -= 1.0
+
+    interactions.solve_linear_system = solve
+    return plain
+
+
+def large_main():
+    """Fixtures at the benchmark's own sizes (exact solves, LAPACK LU):
+
+    config2_n200_lmax4_exact  N = 200 spheres, radii U[50, 100] nm in a 2 um cube
+        (rejection sampling, seed 2: the benchmark's cluster), n = 1.5+0.01i, vacuum,
+        600 nm, lmax 4 (D = 9600); x- and y-polarised plane waves along +z;
+    sweep_n100_lmax7_400nm_exact  the wavelength sweep's cluster (N = 100 Drude
+        spheres, radii U[40, 80] nm, seed 3) at its first wavelength, 400 nm, where
+        the adaptive rule gives lmax 7 (D = 12600);
+    serve_n300_lmax6_exact  a serving-size request: N = 300 spheres, radii
+        U[50, 100] nm in a centred cube of side (N (0.5 um)^3)^(1/3) (rejection
+        sampling, seed 404), n = 1.9+0.05i, vacuum, 600 nm, lmax 6 (D = 28800),
+        x-polarised plane wave.
+    """
+    miepy = import_reference()
+    _lapack_exact(miepy)
+    exact = miepy.solver.exact
+
+    rng = np.random.default_rng(2)
+    pos, rad = random_positions(rng, 200, 50 * nm, 100 * nm, 2000 * nm)
+    diel = miepy.constant_material(index=1.5 + 0.01j)
+    rec = dict(position=pos, radius=rad, wavelength=np.float64(600 * nm), lmax=np.int64(4))
+    for pol in ("x", "y"):
+        c = miepy.sphere_cluster(position=pos, radius=rad, material=diel,
+                                 source=miepy.sources.plane_wave.from_string(polarization=pol),
+                                 wavelength=600 * nm, lmax=4, method=exact)
+        rec["k_b"] = np.float64(np.real(c.material_data.k_b))
+        rec["mie_scat"], rec["mie_int"] = c.mie_scat, c.mie_int
+        rec.update({f"{k}_{pol}": v for k, v in _observables(c).items()})
+    np.savez_compressed(os.path.join(HERE, "config2_n200_lmax4_exact.npz"), **rec)
+    print("wrote config2_n200_lmax4_exact")
+
+    def drude(wav):
+        w = 1239.84193e-9 / wav
+        return 9.0 - 9.0**2 / (w**2 + 1j * 0.07 * w)
+
+    rng = np.random.default_rng(3)
+    pos, rad = random_positions(rng, 100, 40 * nm, 80 * nm, 2000 * nm)
+    c = miepy.sphere_cluster(position=pos, radius=rad, material=miepy.function_material(drude),
+                             source=miepy.sources.plane_wave.from_string(polarization="x"),
+                             wavelength=400 * nm, lmax=7, method=exact)
+    rec = dict(position=pos, radius=rad, wavelength=np.float64(400 * nm), lmax=np.int64(7),
+               k_b=np.float64(np.real(c.material_data.k_b)), eps=np.asarray(c.material_data.eps, complex),
+               mie_scat=c.mie_scat, mie_int=c.mie_int, **_observables(c))
+    np.savez_compressed(os.path.join(HERE, "sweep_n100_lmax7_400nm_exact.npz"), **rec)
+    print("wrote sweep_n100_lmax7_400nm_exact")
+
+    rng = np.random.default_rng(404)
+    N = 300
+    side = (N * (500 * nm) ** 3) ** (1 / 3)
+    pos, rad = random_positions(rng, N, 50 * nm, 100 * nm, side)
+    pos = pos - side / 2
+    c = miepy.sphere_cluster(position=pos, radius=rad, material=miepy.constant_material(index=1.9 + 0.05j),
+                             source=miepy.sources.plane_wave.from_string(polarization="x"),
+                             wavelength=600 * nm, lmax=6, method=exact)
+    rec = dict(position=pos, radius=rad, wavelength=np.float64(600 * nm), lmax=np.int64(6),
+               k_b=np.float64(np.real(c.material_data.k_b)), mie_scat=c.mie_scat, mie_int=c.mie_int,
+               **_observables(c))
+    np.savez_compressed(os.path.join(HERE, "serve_n300_lmax6_exact.npz"), **rec)
+    print("wrote serve_n300_lmax6_exact")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "large":
+        large_main()
+    else:
+        main()

@@ -75,6 +75,38 @@ def test_plane_wave_structure_matches_reference():
         np.testing.assert_allclose(p, g["p_src"], rtol=1e-13, atol=1e-16)
 
 
+def test_benchmark_inputs_match_reference_at_full_size():
+    """The benchmark's cluster (seed 2), Mie coefficients and both plane waves are
+    the reference's (config2 fixture); the sweep's Drude cluster at 400 nm and the
+    serving-size request reproduce theirs too."""
+    import bench
+
+    g = G.load("config2_n200_lmax4_exact")
+    w = bench.workload_inputs()
+    np.testing.assert_allclose(w["position"], g["position"], rtol=1e-15, atol=0)   # the reference stores them to 1 ulp
+    np.testing.assert_allclose(w["radius"], g["radius"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(w["mie_scat"], g["mie_scat"], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(w["mie_int"], g["mie_int"], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(w["p_src"], np.stack([g["p_src_x"], g["p_src_y"]], axis=-1), rtol=1e-13, atol=1e-16)
+    from miepy_gb300 import sweep as SW
+    s = G.load("sweep_n100_lmax7_400nm_exact")
+    pos, rad = SW.drude_cluster(N=100, seed=3)
+    np.testing.assert_allclose(pos, s["position"], rtol=1e-15, atol=0)
+    eps = gb.drude_material(9.0, 9.0, 0.07).eps(400e-9)
+    np.testing.assert_allclose(eps, s["eps"][0], rtol=1e-14)
+    for name in ("sweep_n100_lmax7_400nm_exact", "serve_n300_lmax6_exact"):
+        h = G.load(name)
+        lmax = int(h["lmax"])
+        md = gb.material_struct([gb.constant_material(eps=complex(e)) for e in np.broadcast_to(
+            h["eps"] if "eps" in h else (1.9 + 0.05j) ** 2, h["radius"].shape)],
+            gb.constant_material(eps=1.0, mu=1.0), wavelength=float(h["wavelength"]))
+        ms, mi = gb.mie_coefficients(h["radius"], md.eps, md.mu, md.eps_b, md.mu_b, md.k_b, lmax)
+        np.testing.assert_allclose(ms, h["mie_scat"], rtol=1e-11, atol=1e-300)
+        np.testing.assert_allclose(mi, h["mie_int"], rtol=1e-11, atol=1e-300)
+        p = gb.plane_wave.from_string("x").structure(h["position"], md.k_b, lmax)
+        np.testing.assert_allclose(p, h["p_src"], rtol=1e-13, atol=1e-16)
+
+
 def test_pi_tau_limits_and_interior_values():
     from oracle import oracle as O
     th = np.array([0.0, 0.3, 1.1, 2.0, np.pi])
