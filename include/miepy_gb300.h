@@ -145,12 +145,41 @@ int gb_expand_mie_batch(int nsys, const gb_system* sys, const int64_t* mie_off, 
  * relative product error then stays below tol |b| / 20);
  * GB_PREC_MIXED_FP64RES takes its residuals from mat128.
  * status/iters/resid: host arrays of nsys*R entries (may be NULL); iters are
- * BiCGSTAB iterations (FP64/FP32) or refinement passes (mixed). */
+ * BiCGSTAB iterations (FP64/FP32) or refinement passes (mixed).
+ * R is 1, 2, 4 or 8, with B * R <= 384 for every cluster (B = 2 lmax (lmax + 2));
+ * with R = 4 or 8 the CUDA-core matrix passes run once per pair of right-hand
+ * sides. */
 size_t gb_solve_workspace_size(int nsys, const gb_system* sys, int R, int prec);
 int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
                    int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
                    const double* tvec, const double* b, double* x, void* workspace, size_t ws_bytes, int* status,
                    int* iters, double* resid, void* stream);
+
+/* Multi-RHS blocks on the tensor cores (no counterpart in the reference, whose
+ * solve_linear_system, cpp/src/interactions.cpp:347-368, takes one right-hand side
+ * per call and multiplies with an Eigen/OpenMP GEMV, :70-92).  For R = 4 or 8
+ * right-hand sides (polarisations x incidence directions or sources) of clusters
+ * with lmax <= 5, the matrix passes of the FP32 solves (GB_PREC_FP32, and the inner
+ * solves of GB_PREC_MIXED) run as tcgen05 split-BF16x3 GEMMs with FP32
+ * accumulation on mat_tc, the bf16 hi/lo tiles of mat64 made by
+ * gb_tc_matrix_build: one pass serves all R right-hand sides.  The product is
+ * about 5e-6 accurate relative to its largest term (complex64 arithmetic: 4e-7);
+ * the mixed method's refinement residuals stay on the CUDA-core passes, so its
+ * result meets tol as with gb_solve_batch.  The workspace is gb_solve_workspace_size's.
+ * mat_tc = NULL gives gb_solve_batch. */
+int gb_solve_batch_tc(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+                      int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
+                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
+                      size_t ws_bytes, int* status, int* iters, double* resid, void* stream);
+
+/* Bytes of the bf16 tile arena for a batch: per pair block 2 planes of Bp x Kp bf16
+ * (Bp = B rounded up to 8, Kp = 2B rounded up to 16), clusters in batch order. */
+size_t gb_tc_matrix_bytes(int nsys, const gb_system* sys);
+/* mat_tc = the bf16 hi/lo tiles of the packed complex64 matrix mat64 (hi = bf16(a),
+ * lo = bf16(a - hi) per real component), in the core-matrix layout the tensor-core
+ * pass streams into shared memory; one launch, to be repeated after every
+ * assembly.  Both pointers 16-byte aligned. */
+int gb_tc_matrix_build(int nsys, const gb_system* sys, const float* mat64, void* mat_tc, void* stream);
 
 /* Dense solve of (I + T) x = b for a caller-supplied dense aggregate matrix
  * T [D,D] c128 (the plugin path, where the caller already holds T).  BiCGSTAB as
@@ -206,6 +235,12 @@ int gb_gemv_shape(int B, int prec, int R, int* lanes_per_row, int* cols_per_lane
 int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
                     const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
                     size_t ws_bytes, int reps, int gemv_only, void* stream);
+
+/* gb_apply_repeat with the tensor-core pass (R = 4 or 8): y = (I + T) x from the
+ * bf16 tiles mat_tc, x rounded to complex64, y widened to FP64; reps = 1 is one
+ * product.  The workspace is gb_apply_workspace_size's for GB_PREC_FP32. */
+int gb_apply_repeat_tc(int nsys, const gb_system* sys, int R, const void* mat_tc, const double* tvec, const double* x,
+                       double* y, void* workspace, size_t ws_bytes, int reps, int gemv_only, void* stream);
 
 /* Wait limit of the GEMV's consumer waits on its matrix copies, in SM clock cycles
  * (no counterpart in the reference, whose matvec has no asynchronous copies).  A

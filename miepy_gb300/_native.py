@@ -54,6 +54,11 @@ SIGNATURES = {
     "gb_solve_workspace_size": (c_size_t, [c_int, _P, c_int, c_int]),
     "gb_solve_batch": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P, _P,
                                _P, c_size_t, _P, _P, _P, _P]),
+    "gb_solve_batch_tc": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P, _P,
+                                  _P, _P, c_size_t, _P, _P, _P, _P]),
+    "gb_tc_matrix_bytes": (c_size_t, [c_int, _P]),
+    "gb_tc_matrix_build": (c_int, [c_int, _P, _P, _P, _P]),
+    "gb_apply_repeat_tc": (c_int, [c_int, _P, c_int, _P, _P, _P, _P, _P, c_size_t, c_int, c_int, _P]),
     "gb_solve_dense_workspace_size": (c_size_t, [c_int, c_int]),
     "gb_solve_dense": (c_int, [c_int, c_int, _P, _P, _P, c_double, c_int, _P, c_size_t, _P, _P, _P, _P]),
     "gb_beam_project": (c_int, [c_int, c_int, c_int, _P, _P, _P, c_double, _P, c_int, _P]),

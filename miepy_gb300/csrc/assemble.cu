@@ -608,6 +608,7 @@ int sm_count() {
 
 int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector<SysDev>& out) {
     out.resize(nsys);
+    long long tc_off = 0;
     for (int s = 0; s < nsys; s++) {
         const gb_system& a = sys[s];
         if (a.N < 1 || a.lmax < 1 || a.lmax > GB_LMAX_MAX)
@@ -640,6 +641,8 @@ int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector
         d.neg_ratio2 = T->neg_ratio2;
         d.rowinfo = T->rowinfo;
         d.miecol = T->miecol;
+        d.tc_off = tc_off;
+        tc_off += d.P * tc_block_bytes(d.B);
     }
     return GB_OK;
 }

@@ -75,7 +75,21 @@ struct SysDev {
     // the reference), complex128 and a complex64 copy; null for spheres (t vector)
     const double2* tmat128 = nullptr;
     const float2* tmat64 = nullptr;
+    // byte offset of this cluster's blocks in the bf16 tile arena of the tensor-core
+    // matrix pass (tc_block_bytes(B) per pair, clusters in batch order)
+    long long tc_off = 0;
 };
+
+// bf16 tiles of one B x B complex64 block for the tensor-core matrix pass: the hi
+// and lo planes (hi = bf16(a), lo = bf16(a - hi), per real component), each
+// Bp x Kp bf16 (Bp = B rounded up to 8 rows, Kp = 2B real columns rounded up to 16)
+// in the K-major core-matrix layout of tcgen05 operands: element (m, k) at
+// (m / 8) * (Kp * 16) + (k / 8) * 128 + (m % 8) * 16 + (k % 8) * 2 bytes; padding
+// rows and columns hold zeros.
+__host__ __device__ inline int tc_rows(int B) { return (B + 7) & ~7; }
+__host__ __device__ inline int tc_cols(int B) { return (2 * B + 15) & ~15; }
+__host__ __device__ inline long long tc_plane_bytes(int B) { return 2LL * tc_rows(B) * tc_cols(B); }
+__host__ __device__ inline long long tc_block_bytes(int B) { return 2 * tc_plane_bytes(B); }
 
 // Pinned staging ring for per-call descriptor uploads (assemble.cu).
 int stage_acquire(const void* src, size_t bytes, cudaStream_t stream, void** dev_out, int* slot_out);

@@ -53,6 +53,7 @@
 
 #include "gb_common.cuh"
 #include "gb_internal.h"
+#include "solve_plan.cuh"
 
 namespace {
 
@@ -146,30 +147,12 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
 }
 
 // ----------------------------------------------------------- plan structs --
-struct Strip {          // GEMV work: blocks (i, j0 .. j0+nb-1) of cluster sys
-    int sys, i, nb, pad;
-    long long p0;       // first pair index (cluster-local)
-};
-struct Item {           // rows [r0, r0+nr) of cluster sys
-    int sys, r0, nr, pad;
-};
-struct SysPlan {
-    long long strip_row_base;   // index into row_strip (first block row of this cluster)
-    long long strip_base;       // global index of the first strip of this cluster
-    long long cw_off;           // element offset of this cluster's per-pair column partials
-    long long cu_off;           // element offset of this cluster's per-strip row partials
-    int vbeg, vend;             // vector items
-    int rbeg, rend;             // reduce items
-};
-
-struct KState {         // per (cluster, rhs) BiCGSTAB scalars
-    double2 rho, alpha, omega, beta;   // FP64 solver
-    double r0sq, bsq, rsq, tol2;       // (bsq, rsq also mirrored from the FP32 solver, for the host)
-    float2 rho_f, alpha_f, omega_f, beta_f;   // FP32 solver
-    float r0sq_f, bsq_f, rsq_f, tol2_f;
-    int iters, restarts, done, status;
-    int need_restart, maxiter, pad0, pad1;
-};
+using gb::Strip;
+using gb::Item;
+using gb::SysPlan;
+using gb::KState;
+using gb::active_rhs;
+using gb::any_active;
 
 // The scalars of a KState in the solver's arithmetic T (read-only views for the
 // vector kernels' alpha, omega, beta).
@@ -194,21 +177,6 @@ GB_KS_CFIELD(beta)
 #undef GB_KS_CFIELD
 
 enum { ST_RUNNING = -1 };
-
-// mask_mode: -1 all, 0 running clusters, 1 restarting clusters
-template <int R>
-__device__ __forceinline__ bool active_rhs(const KState* st, int sys, int rr, int mask_mode) {
-    if (mask_mode < 0) return true;
-    const KState& k = st[sys * R + rr];
-    return (mask_mode == 0) ? (!k.done && !k.need_restart) : (k.need_restart != 0);
-}
-template <int R>
-__device__ __forceinline__ bool any_active(const KState* st, int sys, int mask_mode) {
-    bool a = false;
-#pragma unroll
-    for (int rr = 0; rr < R; rr++) a |= active_rhs<R>(st, sys, rr, mask_mode);
-    return a;
-}
 
 // --------------------------------------------------------------- policies --
 // Arithmetic of the GEMV.  A lane multiplies one matrix element m by the y
@@ -355,6 +323,7 @@ template <int YK> struct YType;
 template <> struct YType<0> { using t = double2; };
 template <> struct YType<1> { using t = float4; };   // (re, re, im, im): broadcast pairs for f32x2 FMAs
 template <> struct YType<2> { using t = float4; };
+template <> struct YType<3> { using t = float2; };   // (re, im): the tensor-core pass builds its own operands
 
 template <int YK> __device__ __forceinline__ typename YType<YK>::t make_y(double2 z);
 template <int YK> __device__ __forceinline__ typename YType<YK>::t make_y(float2 z);
@@ -363,6 +332,8 @@ template <> __device__ __forceinline__ double2 make_y<0>(float2 z) { return to_d
 template <> __device__ __forceinline__ float4 make_y<1>(float2 z) { return make_float4(z.x, z.x, z.y, z.y); }
 template <> __device__ __forceinline__ float4 make_y<1>(double2 z) { return make_y<1>(from_d2<float2>(z)); }
 template <> __device__ __forceinline__ float4 make_y<2>(float2 z) { return make_float4(z.x, z.y, 0.f, 0.f); }
+template <> __device__ __forceinline__ float2 make_y<3>(float2 z) { return z; }
+template <> __device__ __forceinline__ float2 make_y<3>(double2 z) { return from_d2<float2>(z); }
 template <> __device__ __forceinline__ float4 make_y<2>(double2 z) {
     const float hx = __double2float_rn(z.x), hy = __double2float_rn(z.y);
     return make_float4(hx, hy, __double2float_rn(z.x - (double)hx), __double2float_rn(z.y - (double)hy));
@@ -633,7 +604,8 @@ k_pgemv(const gb::SysDev* __restrict__ sys, const Strip* __restrict__ strips, lo
     bool failed = false;
     int in_flight = 0;                    // chunks issued and not yet consumed
     const uint64_t stream_pol = l2_evict_first_policy();
-    const long long wait_lim = g_gemv_wait_cycles;
+    // a volatile read: only the host writes the limit, which the compiler cannot see
+    const long long wait_lim = *reinterpret_cast<volatile long long*>(&g_gemv_wait_cycles);
     pdl_wait();                           // y vectors and scalars of the predecessors
     pdl_trigger();
     for (long long w = sbeg + warp; w < send && !failed; w += nwarps) {
@@ -1623,7 +1595,13 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
     int st = gb::make_sysdev(nsys, sys, stream, P.sd);
     if (st) return st;
     long long pairs = 0;
-    for (auto& d : P.sd) pairs += d.P;
+    for (auto& d : P.sd) {
+        pairs += d.P;
+        // the block reduce holds one particle block's B x R terms, a thread each
+        if (d.B * R > kRBThreads)
+            return gb_set_error(GB_UNSUPPORTED, "R = %d right-hand sides need block size B <= %d (lmax %d gives %d)", R,
+                                kRBThreads / R, d.lmax, d.B);
+    }
     P.total_pairs = pairs;
     const long long warps = (long long)gb::sm_count() * 32;
     const long long J = std::max<long long>(1, std::min<long long>(8, pairs / std::max<long long>(1, 2 * warps)));
@@ -1895,16 +1873,42 @@ int launch_pgemv(const Plan& P, const DevPlan& D, const KState* st, int mask, co
     return GB_OK;
 }
 
-// Double-float pass for R right-hand sides: one launch for both, or one per
+// CUDA-core pass for R right-hand sides: one launch for R <= 2; for R = 4 or 8 one
+// launch per pair of right-hand sides (the accumulators of more would not stay in
+// registers), each a full matrix pass.
+template <class Pol, int R>
+int launch_pgemv_all(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* mat_hi,
+                     const void* Yu, const void* Yw, void* CU, void* CW, cudaStream_t stream) {
+    if constexpr (R <= 2) {
+        return launch_pgemv<Pol, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
+    } else {
+        for (int rr = 0; rr < R; rr += 2) {
+            const int e = launch_pgemv<Pol, 2, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, rr, D.err, stream);
+            if (e) return e;
+        }
+        return GB_OK;
+    }
+}
+
+// Double-float pass for R right-hand sides: one launch for both of R = 2, or one per
 // right-hand side where the wide shapes (5 columns per lane) would not keep two
-// sets of double-float accumulators in registers.
+// sets of double-float accumulators in registers, and one per pair or per
+// right-hand side for R = 4 or 8.
 template <int R>
 int launch_df(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* hi, const void* lo,
               const void* Yu, const void* Yw, void* CU, void* CW, cudaStream_t stream) {
     bool wide = false;
     for (const StripGroup& grp : P.groups) wide |= pick_shape(grp.B).cpl >= 5;
-    if (R == 1 || !wide)
-        return launch_pgemv<PolDF, R, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
+    if constexpr (R <= 2) {
+        if (R == 1 || !wide)
+            return launch_pgemv<PolDF, R, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
+    } else if (!wide) {
+        for (int rr = 0; rr < R; rr += 2) {
+            const int e = launch_pgemv<PolDF, 2, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
+            if (e) return e;
+        }
+        return GB_OK;
+    }
     for (int rr = 0; rr < R; rr++) {
         const int e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
         if (e) return e;
@@ -1912,8 +1916,21 @@ int launch_df(const Plan& P, const DevPlan& D, const KState* st, int mask, const
     return GB_OK;
 }
 
+// Tensor-core pass (gemv_tc.cu): one launch per block-size group.
+int launch_pgemv_tcore(const Plan& P, const DevPlan& D, int R, const KState* st, int mask, const void* mat_tc,
+                       const void* Yu, const void* Yw, void* CU, void* CW, cudaStream_t stream) {
+    for (const StripGroup& grp : P.groups) {
+        if (grp.end == grp.beg) continue;
+        const int e = gb::launch_pgemv_tc(R, D.sys, D.strips, grp.beg, grp.end, st, mask, mat_tc, Yu, Yw, CU, CW, D.sp,
+                                          grp.B, D.err, stream);
+        if (e) return e;
+    }
+    return GB_OK;
+}
+
 // One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
-// packed matrices with arithmetic policy pol: 0 Pol64, 1 Pol32, 2 PolDF.
+// packed matrices with arithmetic policy pol: 0 Pol64, 1 Pol32, 2 PolDF, 3 the
+// tensor-core pass (mat_hi = the bf16 tiles).
 template <typename VT, int R>
 int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, const KState* st, int mask,
                  int pol, const void* mat_hi, const void* mat_lo, const double2* tvec, const VT* xin, VT* yout,
@@ -1934,7 +1951,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         else
             GB_CUDA_TRY(launch_pdl(k_yprep<0, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st,
                                    mask, tvec, xin, reinterpret_cast<double2*>(Yu), reinterpret_cast<double2*>(Yw), up));
-        if (P.nstrips) e = launch_pgemv<Pol64, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
+        if (P.nstrips) e = launch_pgemv_all<Pol64, R>(P, D, st, mask, mat_hi, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
         GB_CUDA_TRY(launch_pdl(k_reduce_blk<double2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
@@ -1949,12 +1966,28 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         else
             GB_CUDA_TRY(launch_pdl(k_yprep<1, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st,
                                    mask, tvec, xin, reinterpret_cast<float4*>(Yu), reinterpret_cast<float4*>(Yw), up));
-        if (P.nstrips) e = launch_pgemv<Pol32, R, R>(P, D, st, mask, mat_hi, nullptr, Yu, Yw, CU, CW, 0, D.err, stream);
+        if (P.nstrips) e = launch_pgemv_all<Pol32, R>(P, D, st, mask, mat_hi, Yu, Yw, CU, CW, stream);
         if (e) return e;
         gb::note_launch();
         GB_CUDA_TRY(launch_pdl(k_reduce_blk<float2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
                                D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
                                reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz));
+    } else if (pol == 3) {   // tensor-core pass on the bf16 tiles (mat_hi): float2 y vectors and partials
+        if constexpr (R == 4 || R == 8) {
+            if (P.tmat) return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass serves sphere clusters");
+            gb::note_launch();
+            GB_CUDA_TRY(launch_pdl(k_yprep<3, VT, R>, dim3(vb), dim3(kVRows), 0, stream, D.sys, D.vitems, P.nv, st,
+                                   mask, tvec, xin, reinterpret_cast<float2*>(Yu), reinterpret_cast<float2*>(Yw), up));
+            if (P.nstrips) e = launch_pgemv_tcore(P, D, R, st, mask, mat_hi, Yu, Yw, CU, CW, stream);
+            if (e) return e;
+            gb::note_launch();
+            GB_CUDA_TRY(launch_pdl(k_reduce_blk<float2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream,
+                                   D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask,
+                                   reinterpret_cast<const float2*>(CU), reinterpret_cast<const float2*>(CW), xin, yout,
+                                   mode, aux, b128, dots, fz));
+        } else {
+            return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass needs R = 4 or 8 (got %d)", R);
+        }
     } else {
         gb::note_launch();
         if (P.tmat)
@@ -2291,11 +2324,16 @@ int read_state(const DevPlan& D, const KState* dev, int nsr, std::vector<KState>
     return GB_OK;
 }
 
+// mat_tc (optional, R = 4 or 8): the bf16 tiles of the tensor-core pass, used for
+// the products of the FP32 solves (the FP32 method, and the inner solves of the
+// mixed method); the refinement residuals keep the CUDA-core passes.
 template <int R>
 int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_tol, int max_refine,
                const double* mat128, const float* mat64, const float* mat64lo, const double* tvec, const double* b,
                double* x, unsigned char* base, const WS& w, int* status, int* iters, double* resid,
-               cudaStream_t stream) {
+               cudaStream_t stream, const void* mat_tc = nullptr) {
+    const int pol32 = mat_tc ? 3 : 1;
+    const void* m32 = mat_tc ? mat_tc : static_cast<const void*>(mat64);
     DevPlan D;
     int e = upload_plan(P, base, w, stream, D);
     if (e) return e;
@@ -2322,7 +2360,8 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
     float2* V = reinterpret_cast<float2*>(base + w.off_vec);
     float2* bx = V + 7 * TV;
     if (prec == GB_PREC_FP32) {
-        e = run_bicgstab<float2, R, false>(P, D, w, base, 1, mat64, t2, b2, nullptr, tol, maxiter, st, 0, stream, true);
+        e = run_bicgstab<float2, R, false>(P, D, w, base, pol32, m32, t2, b2, nullptr, tol, maxiter, st, 0, stream,
+                                           true);
         if (e) return e;
         gb::note_launch();
         k_copy_out<float2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, V, x2);
@@ -2349,8 +2388,8 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         gb::note_launch();
         k_cast_f<<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, r128, bx, ost);
         GB_CUDA_TRY(cudaGetLastError());
-        e = run_bicgstab<float2, R, false>(P, D, w, base, 1, mat64, t2, nullptr, bx, inner_tol, maxiter, st, 0, stream,
-                                           true);
+        e = run_bicgstab<float2, R, false>(P, D, w, base, pol32, m32, t2, nullptr, bx, inner_tol, maxiter, st, 0,
+                                           stream, true);
         if (e) return e;
         gb::note_launch();
         k_refine_axpy<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, ost, x2, V, incr ? d128 : nullptr);
@@ -2453,6 +2492,87 @@ int upload_plan_pageable(const Plan& P, unsigned char* base, const WS& w, cudaSt
     return GB_OK;
 }
 
+// y = (I + T) x for FP64 vectors x, y.  prec: GB_PREC_FP64 (complex128 pass),
+// GB_PREC_MIXED (double-float pass), GB_PREC_FP32 (complex64 pass, or the
+// tensor-core pass when mat_tc is given, on a rounded copy of x, widened to FP64).
+// repeat 0: one product; 1: reps products back to back; 2: one product, then the
+// matrix pass alone reps - 1 more times (kernel timing).
+template <int R>
+int apply_impl(const Plan& P, int prec, const double* mat128, const float* mat64, const float* mat64lo,
+               const void* mat_tc, const double* tvec, const double* x, double* y, unsigned char* base, const WS& w,
+               int reps, int repeat, cudaStream_t s) {
+    DevPlan D;
+    int e = upload_plan(P, base, w, s, D);
+    if (e) return e;
+    KState* st = reinterpret_cast<KState*>(base + w.off_state);
+    const double2* x2 = reinterpret_cast<const double2*>(x);
+    double2* y2 = reinterpret_cast<double2*>(y);
+    double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
+    const double2* t2 = reinterpret_cast<const double2*>(tvec);
+    const unsigned vb = (unsigned)P.nv;
+    const int pol = mat_tc ? 3 : (prec == GB_PREC_FP64 ? 0 : (prec == GB_PREC_MIXED ? 2 : 1));
+    const void* hi = pol == 3 ? mat_tc : (pol == 0 ? (const void*)mat128 : (const void*)mat64);
+    const void* lo = pol == 2 ? (const void*)mat64lo : nullptr;
+    void* Yu = base + w.off_yu;
+    void* Yw = base + w.off_yw;
+    void* CU = base + w.off_cu;
+    void* CW = base + w.off_cw;
+    auto pass = [&]() -> int {   // the matrix pass alone, on the y vectors of the first product
+        switch (pol) {
+            case 0: return launch_pgemv_all<Pol64, R>(P, D, st, -1, hi, Yu, Yw, CU, CW, s);
+            case 1: return launch_pgemv_all<Pol32, R>(P, D, st, -1, hi, Yu, Yw, CU, CW, s);
+            case 2: return launch_df<R>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, s);
+            default: return launch_pgemv_tcore(P, D, R, st, -1, hi, Yu, Yw, CU, CW, s);
+        }
+    };
+    const int n = repeat == 0 ? 1 : reps;
+    if (pol == 0 || pol == 2) {
+        for (int k = 0; k < n; k++) {
+            e = (k > 0 && repeat == 2) ? pass()
+                                       : launch_apply<double2, R>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0,
+                                                                  nullptr, nullptr, dots, s);
+            if (e) return e;
+        }
+        return check_device_error(D, s);
+    }
+    // FP32 product on a rounded copy of x, widened to FP64
+    const size_t TV = (size_t)P.total_vec;
+    float2* V = reinterpret_cast<float2*>(base + w.off_vec);
+    float2 *xf = V, *yf = V + TV;
+    gb::note_launch();
+    k_cast_f<<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, x2, xf, nullptr);
+    GB_CUDA_TRY(cudaGetLastError());
+    for (int k = 0; k < n; k++) {
+        e = (k > 0 && repeat == 2) ? pass()
+                                   : launch_apply<float2, R>(P, D, w, base, st, -1, pol, hi, nullptr, t2, xf, yf, 0,
+                                                             nullptr, nullptr, dots, s);
+        if (e) return e;
+    }
+    gb::note_launch();
+    k_copy_out<float2><<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, yf, y2);
+    GB_CUDA_TRY(cudaGetLastError());
+    return check_device_error(D, s);
+}
+
+int apply_entry(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                const float* mat64lo, const void* mat_tc, const double* tvec, const double* x, double* y,
+                void* workspace, size_t ws_bytes, int reps, int repeat, cudaStream_t s) {
+    if (R != 1 && R != 2 && R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "R must be 1, 2, 4 or 8 (got %d)", R);
+    if (prec == GB_PREC_MIXED_FP64RES) prec = GB_PREC_FP64;
+    Plan P;
+    int e = build_plan(nsys, sys, R, s, P);
+    if (e) return e;
+    WS w = ws_layout(P, prec, false);
+    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
+    unsigned char* base = static_cast<unsigned char*>(workspace);
+    switch (R) {
+        case 1: return apply_impl<1>(P, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, base, w, reps, repeat, s);
+        case 2: return apply_impl<2>(P, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, base, w, reps, repeat, s);
+        case 4: return apply_impl<4>(P, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, base, w, reps, repeat, s);
+        default: return apply_impl<8>(P, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, base, w, reps, repeat, s);
+    }
+}
+
 }   // namespace
 
 extern "C" {
@@ -2467,10 +2587,20 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
                    int max_refine, const double* mat128, const float* mat64, const float* mat64lo, const double* tvec,
                    const double* b, double* x, void* workspace, size_t ws_bytes, int* status, int* iters,
                    double* resid, void* stream) {
+    return gb_solve_batch_tc(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, nullptr,
+                             tvec, b, x, workspace, ws_bytes, status, iters, resid, stream);
+}
+
+int gb_solve_batch_tc(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+                      int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
+                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
+                      size_t ws_bytes, int* status, int* iters, double* resid, void* stream) {
     if (nsys < 1 || !sys || !tvec || !b || !x || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
-    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
+    if (R != 1 && R != 2 && R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "R must be 1, 2, 4 or 8 (got %d)", R);
     if (!prec_ok(prec, mat128, mat64, mat64lo))
         return gb_set_error(GB_BAD_ARG, "precision %d is missing one of its matrices", prec);
+    if (mat_tc && (R < 4 || (prec != GB_PREC_FP32 && prec != GB_PREC_MIXED)))
+        return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass serves the FP32 and mixed methods with R = 4 or 8");
     if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
     cudaStream_t s = (cudaStream_t)stream;
     Plan P;
@@ -2480,11 +2610,20 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
     if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
     unsigned char* base = static_cast<unsigned char*>(workspace);
     if (inner_tol <= 0) inner_tol = 1e-6;
-    if (R == 1)
-        return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
-                             status, iters, resid, s);
-    return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
-                         status, iters, resid, s);
+    switch (R) {
+        case 1:
+            return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
+                                 w, status, iters, resid, s);
+        case 2:
+            return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
+                                 w, status, iters, resid, s);
+        case 4:
+            return solve_impl<4>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
+                                 w, status, iters, resid, s, mat_tc);
+        default:
+            return solve_impl<8>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
+                                 w, status, iters, resid, s, mat_tc);
+    }
 }
 
 int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter,
@@ -2618,102 +2757,27 @@ int gb_apply_batch(int nsys, const gb_system* sys, int R, int prec, const double
                    const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
                    size_t ws_bytes, void* stream) {
     if (nsys < 1 || !sys || !tvec || !x || !y || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
-    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
     if (!prec_ok(prec, mat128, mat64, mat64lo)) return gb_set_error(GB_BAD_ARG, "matrix missing for precision %d", prec);
-    cudaStream_t s = (cudaStream_t)stream;
-    Plan P;
-    int e = build_plan(nsys, sys, R, s, P);
-    if (e) return e;
-    WS w = ws_layout(P, prec, false);
-    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
-    unsigned char* base = static_cast<unsigned char*>(workspace);
-    DevPlan D;
-    e = upload_plan(P, base, w, s, D);
-    if (e) return e;
-    KState* st = reinterpret_cast<KState*>(base + w.off_state);
-    const double2* x2 = reinterpret_cast<const double2*>(x);
-    double2* y2 = reinterpret_cast<double2*>(y);
-    double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
-    const double2* t2 = reinterpret_cast<const double2*>(tvec);
-    const unsigned vb = (unsigned)P.nv;
-    auto ap = [&](int pol, const void* hi, const void* lo) {
-        return R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr,
-                                                 dots, s)
-                      : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr,
-                                                 dots, s);
-    };
-    if (prec == GB_PREC_FP64 || prec == GB_PREC_MIXED) {
-        e = prec == GB_PREC_FP64 ? ap(0, mat128, nullptr) : ap(2, mat64, mat64lo);
-        if (e) return e;
-        return check_device_error(D, s);
-    }
-    // FP32 product on a rounded copy of x, widened to FP64
-    const size_t TV = (size_t)P.total_vec;
-    float2* V = reinterpret_cast<float2*>(base + w.off_vec);
-    float2 *xf = V, *yf = V + TV;
-    gb::note_launch();
-    k_cast_f<<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, x2, xf, nullptr);
-    if (R == 1)
-        e = launch_apply<float2, 1>(P, D, w, base, st, -1, 1, mat64, nullptr, t2, xf, yf, 0, nullptr, nullptr, dots, s);
-    else
-        e = launch_apply<float2, 2>(P, D, w, base, st, -1, 1, mat64, nullptr, t2, xf, yf, 0, nullptr, nullptr, dots, s);
-    if (e) return e;
-    gb::note_launch();
-    k_copy_out<float2><<<vb, kVRows, 0, s>>>(D.sys, D.vitems, P.nv, R, yf, y2);
-    GB_CUDA_TRY(cudaGetLastError());
-    return check_device_error(D, s);
+    return apply_entry(nsys, sys, R, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, workspace, ws_bytes, 1, 0,
+                       (cudaStream_t)stream);
 }
 
 int gb_apply_repeat(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
                     const float* mat64lo, const double* tvec, const double* x, double* y, void* workspace,
                     size_t ws_bytes, int reps, int gemv_only, void* stream) {
     if (nsys < 1 || !sys || !tvec || !x || !y || !workspace || reps < 1) return gb_set_error(GB_BAD_ARG, "bad argument");
-    if (R != 1 && R != 2) return gb_set_error(GB_UNSUPPORTED, "R must be 1 or 2 (got %d)", R);
     if (!prec_ok(prec, mat128, mat64, mat64lo)) return gb_set_error(GB_BAD_ARG, "matrix missing for precision %d", prec);
-    if (prec == GB_PREC_MIXED_FP64RES) prec = GB_PREC_FP64;
-    cudaStream_t s = (cudaStream_t)stream;
-    Plan P;
-    int e = build_plan(nsys, sys, R, s, P);
-    if (e) return e;
-    WS w = ws_layout(P, prec, false);
-    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
-    unsigned char* base = static_cast<unsigned char*>(workspace);
-    DevPlan D;
-    e = upload_plan(P, base, w, s, D);
-    if (e) return e;
-    KState* st = reinterpret_cast<KState*>(base + w.off_state);
-    const double2* x2 = reinterpret_cast<const double2*>(x);
-    double2* y2 = reinterpret_cast<double2*>(y);
-    double2* dots = reinterpret_cast<double2*>(base + w.off_dots);
-    const double2* t2 = reinterpret_cast<const double2*>(tvec);
-    const int pol = prec == GB_PREC_FP64 ? 0 : (prec == GB_PREC_MIXED ? 2 : 1);
-    const void* hi = pol == 0 ? (const void*)mat128 : (const void*)mat64;
-    const void* lo = pol == 2 ? (const void*)mat64lo : nullptr;
-    // the first product prepares the y vectors; gemv_only repeats the matrix pass alone
-    e = R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s)
-               : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s);
-    if (e) return e;
-    void* Yu = base + w.off_yu;
-    void* Yw = base + w.off_yw;
-    void* CU = base + w.off_cu;
-    void* CW = base + w.off_cw;
-    for (int k = 1; k < reps; k++) {
-        if (!gemv_only) {
-            e = R == 1 ? launch_apply<double2, 1>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s)
-                       : launch_apply<double2, 2>(P, D, w, base, st, -1, pol, hi, lo, t2, x2, y2, 0, nullptr, nullptr, dots, s);
-        } else if (pol == 0) {
-            e = R == 1 ? launch_pgemv<Pol64, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s)
-                       : launch_pgemv<Pol64, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s);
-        } else if (pol == 1) {
-            e = R == 1 ? launch_pgemv<Pol32, 1, 1>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s)
-                       : launch_pgemv<Pol32, 2, 2>(P, D, st, -1, hi, nullptr, Yu, Yw, CU, CW, 0, D.err, s);
-        } else {
-            e = R == 1 ? launch_df<1>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, s)
-                       : launch_df<2>(P, D, st, -1, hi, lo, Yu, Yw, CU, CW, s);
-        }
-        if (e) return e;
-    }
-    return check_device_error(D, s);
+    return apply_entry(nsys, sys, R, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, workspace, ws_bytes, reps,
+                       gemv_only ? 2 : 1, (cudaStream_t)stream);
+}
+
+int gb_apply_repeat_tc(int nsys, const gb_system* sys, int R, const void* mat_tc, const double* tvec, const double* x,
+                       double* y, void* workspace, size_t ws_bytes, int reps, int gemv_only, void* stream) {
+    if (nsys < 1 || !sys || !mat_tc || !tvec || !x || !y || !workspace || reps < 1)
+        return gb_set_error(GB_BAD_ARG, "bad argument");
+    if (R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass needs R = 4 or 8 (got %d)", R);
+    return apply_entry(nsys, sys, R, GB_PREC_FP32, nullptr, nullptr, nullptr, mat_tc, tvec, x, y, workspace, ws_bytes,
+                       reps, gemv_only ? 2 : 1, (cudaStream_t)stream);
 }
 
 int gb_set_gemv_wait_limit(long long cycles, long long* previous) {

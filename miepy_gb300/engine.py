@@ -87,9 +87,11 @@ class ClusterBatch:
         optional mie_int [N,2,lmax], eps_b float.
     """
 
-    def __init__(self, specs, R=1, precision="fp64", device=None):
+    def __init__(self, specs, R=1, precision="fp64", device=None, tensor=False):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {list(PRECISIONS)}")
+        if tensor and (int(R) not in (4, 8) or precision not in ("fp32", "mixed")):
+            raise ValueError("tensor=True serves R = 4 or 8 right-hand sides with precision 'fp32' or 'mixed'")
         self.device = require_cuda(device)
         self.R = int(R)
         self.precision = precision
@@ -127,6 +129,12 @@ class ClusterBatch:
         self.mat128 = torch.empty(mat, dtype=torch.complex128, device=dev) if "c128" in need else None
         self.mat64 = torch.empty(mat, dtype=torch.complex64, device=dev) if "hi" in need else None
         self.mat64lo = torch.empty(mat, dtype=torch.complex64, device=dev) if "lo" in need else None
+        # bf16 hi/lo tiles of the complex64 matrix for the tensor-core pass of the FP32
+        # solves (R = 4 or 8), rebuilt by every assemble
+        self.mat_tc = None
+        if tensor:
+            nb = nat.lib().gb_tc_matrix_bytes(self.nsys, self.sys)
+            self.mat_tc = torch.empty(max(int(nb), 16), dtype=torch.uint8, device=dev)
         self._ws = None
         self._host_out = None
         # general particles: per-particle T-matrices [N][B][B] instead of Mie coefficients
@@ -229,6 +237,9 @@ class ClusterBatch:
         if self.totals["mat"] > 0:
             nat.check(L.gb_assemble_batch(self.nsys, self.sys, nat.ptr(self.pos), nat.ptr(self.mat128),
                                           nat.ptr(self.mat64), nat.ptr(self.mat64lo), st), "assemble")
+            if self.mat_tc is not None:
+                nat.check(L.gb_tc_matrix_build(self.nsys, self.sys, nat.ptr(self.mat64), nat.ptr(self.mat_tc), st),
+                          "tensor-core tiles")
         self.assembled = True
         return self
 
@@ -260,11 +271,12 @@ class ClusterBatch:
                                           ws.numel(), status.ctypes.data, iters.ctypes.data, resid.ctypes.data,
                                           current_stream(self.device))
         else:
-            rc = L.gb_solve_batch(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
-                                  int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64), nat.ptr(self.mat64lo),
-                                  nat.ptr(self.tvec),
-                                  nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data,
-                                  iters.ctypes.data, resid.ctypes.data, current_stream(self.device))
+            tc = self.mat_tc if precision in ("fp32", "mixed") else None
+            rc = L.gb_solve_batch_tc(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
+                                     int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64),
+                                     nat.ptr(self.mat64lo), nat.ptr(tc), nat.ptr(self.tvec), nat.ptr(self.b),
+                                     nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data, iters.ctypes.data,
+                                     resid.ctypes.data, current_stream(self.device))
         if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN) or (raise_on_fail and rc):
             nat.check(rc, "solve")
         self.status, self.iters, self.resid = status, iters, resid
@@ -282,6 +294,21 @@ class ClusterBatch:
         nat.check(L.gb_apply_batch(self.nsys, self.sys, self.R, code, nat.ptr(self.mat128), nat.ptr(self.mat64),
                                    nat.ptr(self.mat64lo), nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y), nat.ptr(ws),
                                    ws.numel(), current_stream(self.device)), "apply")
+        return y
+
+    def apply_tc(self, x, reps=1, gemv_only=False):
+        """y = (I + T) x with the tensor-core pass (x: device complex128 [total_vec],
+        rounded to complex64; needs tensor=True); reps > 1 launches it back to back."""
+        if self.mat_tc is None:
+            raise ValueError("this batch was made without tensor=True")
+        L = nat.lib()
+        need = L.gb_apply_workspace_size(self.nsys, self.sys, self.R, nat.PREC_FP32)
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        y = torch.empty_like(x)
+        nat.check(L.gb_apply_repeat_tc(self.nsys, self.sys, self.R, nat.ptr(self.mat_tc), nat.ptr(self.tvec),
+                                       nat.ptr(x), nat.ptr(y), nat.ptr(self._ws), self._ws.numel(), int(reps),
+                                       int(bool(gemv_only)), current_stream(self.device)), "apply (tensor cores)")
         return y
 
     def apply_repeat(self, x, precision="fp32", reps=10, gemv_only=False):

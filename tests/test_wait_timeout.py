@@ -6,7 +6,8 @@ every consumer wait expire at once: each warp then sets the launch's error flag,
 drains its own copies in flight with the default limit, and returns, and the call
 reports GB_TIMEOUT.  With the default limit restored, the same batch gives the
 oracle's product (complex64 bar 2e-6) and converges in a solve: the context stays
-usable after the timeout.
+usable after the timeout (12-sphere cluster of the golden fixtures, two
+right-hand sides).
 """
 
 import ctypes
@@ -18,28 +19,20 @@ import torch
 from miepy_gb300 import _native as nat
 from miepy_gb300.engine import ClusterBatch
 from oracle import oracle as O
+from tests import _golden as G
 
 pytestmark = pytest.mark.gpu
 
-nm = 1e-9
-
-
-def _batch(rng, N=12, lmax=3):
-    pos = np.stack([np.arange(N) * 260 * nm, rng.uniform(-40, 40, N) * nm, np.zeros(N)], axis=1)
-    mie = (rng.normal(size=(N, 2, lmax)) + 1j * rng.normal(size=(N, 2, lmax))) * 0.2
-    k = 2 * np.pi / (600 * nm)
-    rmax = lmax * (lmax + 2)
-    x = rng.normal(size=(N, 2, rmax, 2)) + 1j * rng.normal(size=(N, 2, rmax, 2))
-    return pos, mie, k, x
 
 
 def test_expired_gemv_wait_reports_timeout_and_context_recovers():
     L = nat.lib()
-    rng = np.random.default_rng(3)
-    pos, mie, k, x = _batch(rng)
+    g = G.load("rand12_lmax3_exact")   # 12 spheres, lmax 3: a physical cluster from the reference
+    pos, mie, k = g["position"], g["mie_scat"], float(g["k_b"])
     N = pos.shape[0]
-    b = ClusterBatch([dict(position=pos, mie_scat=mie, k=k, p_src=x)], R=2, precision="mixed").assemble()
-    xd = torch.from_numpy(x.reshape(-1)).to(b.device)
+    p_src = np.stack([g["p_src"], g["p_src"] * (1 - 0.5j)], axis=-1)
+    b = ClusterBatch([dict(position=pos, mie_scat=mie, k=k, p_src=p_src)], R=2, precision="mixed").assemble()
+    xd = b.b.clone()
     prev = ctypes.c_longlong(0)
     nat.check(L.gb_set_gemv_wait_limit(0, ctypes.byref(prev)))
     try:
@@ -53,13 +46,16 @@ def test_expired_gemv_wait_reports_timeout_and_context_recovers():
     cur = ctypes.c_longlong(0)
     nat.check(L.gb_set_gemv_wait_limit(-1, ctypes.byref(cur)))
     assert cur.value == prev.value
-    # the context is usable: the same product now matches the oracle, and a solve converges
+    # the context is usable: the same product now matches the oracle, and a solve
+    # reaches the reference's exact solution
     T = O.sphere_aggregate_tmatrix(pos, mie.reshape(N, -1), k)
     D = T.shape[0]
-    xs = x.reshape(D, 2)
+    xs = p_src.reshape(D, 2)
     ref = np.stack([O.gemv(T, xs[:, r]) + xs[:, r] for r in range(2)], axis=1)
     y = b.apply(xd, "fp32").cpu().numpy().reshape(D, 2)
     assert np.max(np.abs(y - ref)) / np.max(np.abs(ref)) < 2e-6
-    b.solve(tol=1e-8, maxiter=500)
+    b.solve(tol=1e-10, maxiter=1000)
     assert np.all(np.asarray(b.status) == 0)
-    torch.cuda.synchronize()
+    x = b.cluster_view(0, b.x).cpu().numpy()
+    want = np.stack([g["p_inc"], g["p_inc"] * (1 - 0.5j)], axis=-1)
+    assert np.max(np.abs(x - want)) / np.max(np.abs(want)) < 1e-8
