@@ -208,6 +208,8 @@ def run_gpu(args, rank, world):
     cext_err = float(np.max(np.abs(ce_m - ce_d) / np.abs(ce_d)))
     iters_fp64 = batches["fp64"].iters.tolist()
     iters_mixed = batches["mixed"].iters.tolist()
+    ref_err = dict(mixed=errors_vs_reference(batches["mixed"], N, lmax, R),
+                   fp64=errors_vs_reference(batches["fp64"], N, lmax, R))
 
     # ---- dominant kernel: one packed-operator product (c64, as in the mixed inner solve),
     # and the double-float / FP64 products for reference
@@ -352,13 +354,130 @@ def run_gpu(args, rank, world):
             c128_fp64=dict(ms=1e3 * t_apply128, matrix_gbs=mat_bytes_128 / t_apply128 / 1e9)),
         gpu_launches_total=int(launches),
         clocks=clocks_info,
+        errors_vs_reference=ref_err,
     )
+    if not args.no_multi_rhs:
+        res["multi_rhs"] = run_multi_rhs(args, W, dev, peak)
     return res
 
 
+def errors_vs_reference(batch, N, lmax, R):
+    """Relative errors of a solved config-2 batch (x and y plane waves) against the
+    reference's exact solve of the same cluster (tests/golden/config2_n200_lmax4_exact,
+    made by the reference's own sphere_cluster): p_inc, total cross-sections, forces
+    and torques."""
+    path = os.path.join(ROOT, "tests", "golden", "config2_n200_lmax4_exact.npz")
+    if not os.path.exists(path):
+        return None
+    g = np.load(path)
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    x = batch.cluster_view(0, batch.x).cpu().numpy()
+    xs = batch.xs[: N * R * 6 * lmax].view(N, R, 3, 2, lmax).sum(dim=(0, 3, 4)).cpu().numpy()
+    F = batch.F[: N * R * 3].view(N, R, 3).cpu().numpy()
+    T = batch.T[: N * R * 3].view(N, R, 3).cpu().numpy()
+    out = {}
+    for q, pol in enumerate(("x", "y")):
+        C = g[f"cross_sections_{pol}"]
+        out[pol] = dict(p_inc=rel(x[..., q], g[f"p_inc_{pol}"]),
+                        C_sca=float(abs(xs[q, 0] - C[0]) / abs(C[0])), C_abs=float(abs(xs[q, 1] - C[1]) / abs(C[1])),
+                        C_ext=float(abs(xs[q, 2] - C[2]) / abs(C[2])), force=rel(F[:, q], g[f"force_{pol}"]),
+                        torque=rel(T[:, q], g[f"torque_{pol}"]))
+    return out
+
+
+def run_multi_rhs(args, W, dev, peak):
+    """Eight sources on the headline cluster (x and y polarisation at four incidence
+    directions): R = 8 right-hand sides share every matrix pass.  The FP32 inner
+    solves run their products either as one tcgen05 split-BF16x3 pass over the bf16
+    tiles (tensor=True) or as four CUDA-core complex64 passes (one per pair of
+    right-hand sides).  Reports both passes against the HBM roofline and both mixed
+    solves (tolerance 1e-8), with their C_ext error against an FP64 solve."""
+    import torch
+
+    import miepy_gb300 as gb
+    from miepy_gb300.engine import ClusterBatch
+    R = 8
+    srcs = []
+    for d in range(R // 2):
+        th, ph = 0.35 * d, 0.8 * d
+        srcs += [gb.plane_wave(polarization=[1, 0], theta=th, phi=ph), gb.plane_wave(polarization=[0, 1], theta=th, phi=ph)]
+    pos = W["position"]
+    N, lmax = pos.shape[0], W["lmax"]
+    p_src = np.stack([s_.structure(pos, W["k"], lmax) for s_ in srcs], axis=-1)
+    spec = dict(position=pos, mie_scat=W["mie_scat"], mie_int=W["mie_int"], k=W["k"], p_src=p_src)
+    stream = torch.cuda.current_stream()
+    bt = ClusterBatch([spec], R=R, precision="mixed", device=dev, tensor=True)
+    bc = ClusterBatch([spec], R=R, precision="mixed", device=dev)
+    b64 = ClusterBatch([spec], R=R, precision="fp64", device=dev)
+
+    def solve(b, prec="mixed"):
+        b.assemble()
+        b.solve(tol=TOL, maxiter=1000, inner_tol=INNER_TOL, max_refine=8, precision=prec)
+        b.epilogue(W["eps_b"])
+
+    for _ in range(max(1, args.warmup)):
+        solve(bt)
+        solve(bc)
+    solve(b64, "fp64")
+    torch.cuda.synchronize()
+    steps = max(3, args.steps // 2)
+
+    def timed(b):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        for _ in range(steps):
+            solve(b)
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]) / 1e3 / steps
+
+    t_tc, t_cc = timed(bt), timed(bc)
+    x = torch.randn(bt.totals["vec"], dtype=torch.complex128, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def span(fn, n):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn(n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    def per_pass(fn, reps=24):
+        span(fn, 3)
+        return float(np.median([(span(fn, 4 + reps) - span(fn, 4)) / reps for _ in range(5)]))
+
+    t_pass_tc = per_pass(lambda n: bt.apply_tc(x, reps=n, gemv_only=True))
+    t_pass_cc = per_pass(lambda n: bt.apply_repeat(x, "fp32", reps=n, gemv_only=True))
+    cext = lambda b: b.xs[: N * R * 6 * lmax].view(N, R, 3, 2, lmax).sum(dim=(0, 3, 4))[:, 2].cpu().numpy()
+    c64 = cext(b64)
+    err = lambda b: float(np.max(np.abs(cext(b) - c64) / np.abs(c64)))
+    P = N * (N - 1) // 2
+    B = 2 * lmax * (lmax + 2)
+    tile_bytes = P * 2 * (((B + 7) // 8) * 8) * (((2 * B + 15) // 16) * 16) * 2
+    mat64 = P * B * B * 8
+    return dict(
+        workload=f"{WORKLOAD.split(' R=2')[0]}, R=8 (x/y polarisation at 4 incidence directions)",
+        tensor_core=dict(solves_per_s=1.0 / t_tc, source_solves_per_s=R / t_tc, ms_per_step=1e3 * t_tc,
+                         cext_rel_err_vs_fp64=err(bt), pass_ms=1e3 * t_pass_tc,
+                         roofline=dict(bound="hbm", kernel="k_pgemv_tc<8> (tcgen05 split-BF16x3, one pass for R=8)",
+                                       algorithmic_bytes_per_launch=int(tile_bytes),
+                                       achieved=tile_bytes / t_pass_tc / 1e9, peak=peak, unit="GB/s",
+                                       frac=tile_bytes / t_pass_tc / 1e9 / peak)),
+        cuda_core=dict(solves_per_s=1.0 / t_cc, source_solves_per_s=R / t_cc, ms_per_step=1e3 * t_cc,
+                       cext_rel_err_vs_fp64=err(bc), pass_ms=1e3 * t_pass_cc,
+                       note="k_pgemv<Pol32> once per pair of right-hand sides: 4 matrix passes per product",
+                       matrix_gbs_per_product=mat64 / t_pass_cc / 1e9),
+        tensor_over_cuda_core=dict(pass_speedup=t_pass_cc / t_pass_tc, solve_speedup=t_cc / t_tc))
+
+
 # ---------------------------------------------------------- CPU baseline --
-def run_cpu_sample(threads=None):
-    """One full cluster solve on the host cores with the oracle (OpenMP)."""
+def run_cpu_sample(threads=None, gemv_reps=0):
+    """One full cluster solve on the host cores with the oracle (OpenMP): assembly,
+    BiCGSTAB for both polarisations, cross-sections, forces and torques.  With
+    gemv_reps > 0 it also times that many matrix-vector products of the assembled
+    matrix alone (the solve's bound: 16 D^2 bytes each)."""
     from oracle import oracle as O
     W = workload_inputs()
     if threads:
@@ -381,7 +500,18 @@ def run_cpu_sample(threads=None):
         O.force_all(ps, x, W["k"], W["eps_b"])
         O.torque_all(ps, x, W["k"], W["eps_b"])
     total = time.perf_counter() - t0
-    return dict(seconds=total, assembly_s=t_asm, cores=n_thr, iterations=its)
+    out = dict(seconds=total, assembly_s=t_asm, cores=n_thr, iterations=its)
+    if gemv_reps:
+        D = T.shape[0]
+        v = W["p_src"][..., 0].ravel()
+        O.gemv(T, v)
+        t1 = time.perf_counter()
+        for _ in range(gemv_reps):
+            O.gemv(T, v)
+        dt = (time.perf_counter() - t1) / gemv_reps
+        out["gemv_ms"] = 1e3 * dt
+        out["gemv_gbs"] = 16.0 * D * D / dt / 1e9
+    return out
 
 
 # ------------------------------------------------------ wavelength sweep --
@@ -466,21 +596,24 @@ SERVE_WORKLOAD = ("serving stream: seeded requests (seed 4), N log-uniform 2-500
                   "Gaussian beam (waist 1 um) 50/50; Poisson arrivals")
 
 
-def run_serve(args):
-    """Throughput at saturation (all requests queued at once) and latency at a
-    Poisson arrival rate of half that throughput, mixed precision; FP64 throughput
-    on the same requests."""
+def run_serve(args, nreq=None):
+    """The serving stream (seed 4): throughput at saturation (all requests queued at
+    once) in mixed precision and in FP64 over the same full stream; then Poisson
+    arrivals at half the mixed saturation rate, with each request's latency, its
+    latency alone on an idle server, and their ratio (the slowdown the mix causes);
+    every Poisson result is checked against its alone result."""
     import torch
     from miepy_gb300 import server as SV
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(4)
-    nreq = max(8, args.requests)
+    nreq = max(8, nreq or args.requests)
     reqs = [SV.random_request(rng, rid=i) for i in range(nreq)]
     L = nat_lib()
+    kw = dict(tol=TOL, max_waves=3, max_wave_requests=16)
 
     def saturate(precision, rs):
-        with SV.SolveServer(precision=precision, tol=TOL, max_waves=3, max_wave_requests=16) as srv:
+        with SV.SolveServer(precision=precision, **kw) as srv:
             t0 = time.perf_counter()
             futs = [srv.submit(r) for r in rs]
             out = [f.result() for f in futs]
@@ -497,9 +630,10 @@ def run_serve(args):
     n0 = L.gb_launch_count()
     t_sat, res_sat, st_sat = saturate("mixed", reqs)
     launches = L.gb_launch_count() - n0
+    t_64, res_64, _ = saturate("fp64", reqs)
     rate = 0.5 * nreq / t_sat
     arr = np.cumsum(np.random.default_rng(44).exponential(1.0 / rate, size=nreq))
-    with SV.SolveServer(precision="mixed", tol=TOL, max_waves=3, max_wave_requests=16) as srv:
+    with SV.SolveServer(precision="mixed", **kw) as srv:
         t0 = time.perf_counter()
         futs = []
         for r, ta in zip(reqs, arr):
@@ -510,26 +644,30 @@ def run_serve(args):
         res_poi = [f.result() for f in futs]
         t_poi = time.perf_counter() - t0
         st_poi = dict(srv.stats)
-    n64 = min(nreq, max(8, args.requests // 2))
-    t_64, res_64, _ = saturate("fp64", reqs[:n64])
-    t_m64, res_m64, _ = saturate("mixed", reqs[:n64])
+    with SV.SolveServer(precision="mixed", **kw) as srv:   # each request alone on an idle server
+        res_alone = [srv.submit(r).result() for r in reqs]
     clocks_info = clocks.stop()
     lat = np.array([r.latency for r in res_poi]) * 1e3
+    alone = np.array([r.latency for r in res_alone]) * 1e3
+    slow = lat / alone
     lat_sat = np.array([r.latency for r in res_sat]) * 1e3
-    err = max(abs(a.C_ext - b.C_ext) / abs(b.C_ext) for a, b in zip(res_m64, res_64))
+    err = max(abs(a.C_ext - b.C_ext) / abs(b.C_ext) for a, b in zip(res_sat, res_64))
+    err_alone = max(abs(a.C_ext - b.C_ext) / abs(b.C_ext) for a, b in zip(res_poi, res_alone))
     sizes = [(len(np.asarray(r.radius)), r.lmax) for r in reqs]
+    pct = lambda a, q: float(np.percentile(a, q))
     return dict(value=nreq / t_sat, ms_per_step=1e3 * t_sat / nreq,
-                p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
-                poisson=dict(rate_per_s=rate, achieved_solves_per_s=nreq / t_poi, p50_ms=float(np.percentile(lat, 50)),
-                             p99_ms=float(np.percentile(lat, 99)), waves=st_poi["waves"],
-                             max_concurrent_waves=st_poi["max_concurrent_waves"]),
-                saturation=dict(solves_per_s=nreq / t_sat, p50_ms=float(np.percentile(lat_sat, 50)),
-                                p99_ms=float(np.percentile(lat_sat, 99)), waves=st_sat["waves"],
-                                max_concurrent_waves=st_sat["max_concurrent_waves"],
+                p50_ms=pct(lat, 50), p99_ms=pct(lat, 99),
+                poisson=dict(rate_per_s=rate, achieved_solves_per_s=nreq / t_poi, p50_ms=pct(lat, 50),
+                             p99_ms=pct(lat, 99), alone_p50_ms=pct(alone, 50), alone_p99_ms=pct(alone, 99),
+                             slowdown_p50=pct(slow, 50), slowdown_p99=pct(slow, 99), waves=st_poi["waves"],
+                             max_concurrent_waves=st_poi["max_concurrent_waves"],
+                             cext_rel_err_vs_alone=float(err_alone)),
+                saturation=dict(solves_per_s=nreq / t_sat, p50_ms=pct(lat_sat, 50), p99_ms=pct(lat_sat, 99),
+                                waves=st_sat["waves"], max_concurrent_waves=st_sat["max_concurrent_waves"],
                                 peak_hbm_gb=st_sat["peak_bytes"] / 1e9),
-                fp64_solves_per_s=n64 / t_64, mixed_solves_per_s_same_subset=n64 / t_m64,
+                fp64_solves_per_s=nreq / t_64, mixed_over_fp64=t_64 / t_sat,
                 cext_rel_err_mixed_vs_fp64=float(err),
-                all_converged=bool(all(r.status == 0 for r in res_sat + res_poi + res_64)),
+                all_converged=bool(all(r.status == 0 for r in res_sat + res_poi + res_64 + res_alone)),
                 requests=nreq, largest_request=dict(N=int(max(sizes)[0]), lmax=int(max(s[1] for s in sizes))),
                 gpu_launches=int(launches), clocks=clocks_info)
 
@@ -624,6 +762,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="leave the serving stream out of the headline run")
+    ap.add_argument("--no-multi-rhs", action="store_true", help="leave the R=8 tensor-core leg out of the headline run")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -636,23 +776,32 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        steps = max(1, min(args.steps, 2))
         from oracle import oracle as O
         O.build()
-        for _ in range(min(args.warmup, 1)):
-            pass
+        cores = len(os.sched_getaffinity(0))
+        for _ in range(args.warmup):
+            run_cpu_sample(threads=cores)
         times, info = [], None
-        for _ in range(steps):
-            info = run_cpu_sample(threads=len(os.sched_getaffinity(0)))
+        for k in range(args.steps):
+            info = run_cpu_sample(threads=cores, gemv_reps=3 if k == 0 else 0)
+            if k == 0:
+                gemv = dict(ms=info["gemv_ms"], gbs=info["gemv_gbs"])
             times.append(info["seconds"])
-        v = steps / sum(times)
-        line = dict(base, impl="reference", value=v, ms_per_step=1e3 * sum(times) / steps, dtype="c128",
+        one = run_cpu_sample(threads=1, gemv_reps=1)   # one single-thread solve beside the all-core ones
+        O.set_num_threads(cores)
+        v = args.steps / sum(times)
+        line = dict(base, impl="reference", value=v, ms_per_step=1e3 * sum(times) / args.steps, dtype="c128",
                     cpu_baseline=dict(value=v, unit="solves/s", cores=info["cores"], kind="port",
-                                      sample=f"{steps} full solve(s) of the workload (oracle restatement of the "
-                                             "reference's OpenMP C++ path)"),
+                                      sample=f"{args.steps} full solves of the workload after {args.warmup} warm-up "
+                                             "solves (oracle restatement of the reference's OpenMP C++ path: "
+                                             "assembly, BiCGSTAB for both polarisations, cross-sections, forces, "
+                                             "torques)",
+                                      gemv_ms=gemv["ms"], gemv_gbs=gemv["gbs"],
+                                      single_thread=dict(value=1.0 / one["seconds"], unit="solves/s", cores=1,
+                                                         gemv_gbs=one["gemv_gbs"])),
                     e2e=dict(value=v, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
-                    iterations=info["iterations"])
-        line["steps"] = steps
+                    iterations=info["iterations"], p50_ms=1e3 * float(np.percentile(times, 50)),
+                    p99_ms=1e3 * float(np.percentile(times, 99)))
         print(json.dumps(line))
         return
 
@@ -698,13 +847,21 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:
-            info = run_cpu_sample(threads=len(os.sched_getaffinity(0)))
+            info = run_cpu_sample(threads=len(os.sched_getaffinity(0)), gemv_reps=3)
             cpu = dict(value=1.0 / info["seconds"], unit="solves/s", cores=info["cores"], kind="port",
                        sample="1 full solve of the workload (assembly + 2 BiCGSTAB solves + epilogue) on the oracle",
-                       assembly_s=info["assembly_s"], iterations=info["iterations"])
+                       assembly_s=info["assembly_s"], iterations=info["iterations"], gemv_gbs=info["gemv_gbs"])
+        serving = None
+        if world == 1 and not args.no_serving:
+            sv = run_serve(args)
+            serving = dict(workload=SERVE_WORKLOAD, requests=sv["requests"],
+                           mixed_solves_per_s=sv["saturation"]["solves_per_s"],
+                           fp64_solves_per_s=sv["fp64_solves_per_s"], mixed_over_fp64=sv["mixed_over_fp64"],
+                           cext_rel_err_mixed_vs_fp64=sv["cext_rel_err_mixed_vs_fp64"], poisson=sv["poisson"],
+                           all_converged=sv["all_converged"], largest_request=sv["largest_request"])
         line = dict(base, impl="gb300", dtype="c64 BiCGSTAB + double-float (c64 hi+lo) refinement residual, "
                                              "c64 incremental residual once |r| <= 2.5e4 tol |b|",
-                    gpu_launches=res.pop("gpu_launches_total"), cpu_baseline=cpu, **res)
+                    gpu_launches=res.pop("gpu_launches_total"), cpu_baseline=cpu, serving=serving, **res)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

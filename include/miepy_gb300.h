@@ -290,6 +290,18 @@ int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, doub
                            const double* b, double* x, void* workspace, size_t ws_bytes, int* status, int* iters,
                            double* resid, void* stream);
 
+/* Dense aggregate T-matrix of N general particles in the reference layout (replaces
+ * particle_aggregate_tmatrix, cpp/src/interactions.cpp:417-462, with the T-matrix
+ * overload of vsh_translation_insert_pair, cpp/src/vsh_translation.cpp:53-159):
+ * block (i, j) = A_ij T_j for i != j, zero for i = j, with A_ij the translation
+ * blocks of gb_assemble_sphere_dense at unit Mie coefficients.  pos [N,3] f64,
+ * tmat [N][B][B] c128 (B = 2 rmax: each particle's [2, rmax, 2, rmax] T-matrix
+ * row-major), out [D,D] c128; the workspace (gb_particle_aggregate_workspace_size
+ * bytes) holds A and the unit coefficients. */
+size_t gb_particle_aggregate_workspace_size(int N, int lmax);
+int gb_particle_aggregate_dense(int N, int lmax, const double* pos, const double* tmat, double k, void* workspace,
+                                size_t ws_bytes, double* out, void* stream);
+
 /* Epilogue of T-matrix clusters: p_scat = T p_inc per particle (required output),
  * then the cross-sections per (a, n), forces and torques of gb_epilogue_batch from
  * p_scat, p_inc and p_src (flux.cpp:5-30, forces.cpp:7-171). */

@@ -80,6 +80,8 @@ SIGNATURES = {
     "gb_tmatrix_epilogue_batch": (c_int, [c_int, _P, c_int, _P, _P, _P, _P, _P, c_double, c_int, _P, _P, _P, _P,
                                           _P]),
     "gb_particle_cross_sections": (c_int, [c_int, c_int, _P, _P, _P, c_double, _P, _P]),
+    "gb_particle_aggregate_workspace_size": (c_size_t, [c_int, c_int]),
+    "gb_particle_aggregate_dense": (c_int, [c_int, c_int, _P, _P, c_double, _P, c_size_t, _P, _P]),
     "gb_near_field": (c_int, [c_int, c_int, _P, _P, _P, _P, c_double, _P, c_int, _P, c_int, c_int, c_double, c_double,
                               _P, _P, _P]),
     "gb_near_field32": (c_int, [c_int, c_int, _P, _P, _P, _P, c_double, _P, c_int, _P, c_int, c_int, c_double,

@@ -139,8 +139,8 @@ def sphere_aggregate_tmatrix_jax(positions, mie, k):
 def particle_aggregate_tmatrix(positions, tmatrix, k):
     """positions [N,3], tmatrix [N,2,rmax,2,rmax], k -> T_agg [N,2,rmax,N,2,rmax]
     (interactions.cpp:416-462): the translation blocks A_ij from the GPU assembler
-    (unit Mie coefficients), then block (i, j) = A_ij T_j as one batched complex
-    GEMM (cuBLAS) over the column blocks."""
+    (unit Mie coefficients), then block (i, j) = A_ij T_j by the library's batched
+    complex128 block product (gb_particle_aggregate_dense)."""
     dev = require_cuda()
     pos = np.ascontiguousarray(np.asarray(positions, dtype=float).reshape(-1, 3))
     N = pos.shape[0]
@@ -151,15 +151,14 @@ def particle_aggregate_tmatrix(positions, tmatrix, k):
     if N == 1:
         return np.zeros((1, 2, rmax, 1, 2, rmax), dtype=complex)
     D = B * N
+    L = nat.lib()
     d_pos = torch.from_numpy(pos).to(dev)
-    ones = torch.ones(N * 2 * lmax, dtype=torch.complex128, device=dev)
-    A = torch.empty(D * D, dtype=torch.complex128, device=dev)
-    nat.check(nat.lib().gb_assemble_sphere_dense(N, lmax, nat.ptr(d_pos), nat.ptr(ones), float(np.real(k)), nat.ptr(A),
-                                                 current_stream(dev)), "dense assembly")
     Tj = torch.from_numpy(np.ascontiguousarray(T.reshape(N, B, B))).to(dev)
-    A4 = A.view(N, B, N, B).permute(2, 0, 1, 3).reshape(N, N * B, B)    # [j][(i, r)][c]
-    out = torch.bmm(A4, Tj)                                              # [j][(i, r)][col]
-    return out.reshape(N, N, B, B).permute(1, 2, 0, 3).reshape(N, 2, rmax, N, 2, rmax).cpu().numpy()
+    ws = torch.empty(L.gb_particle_aggregate_workspace_size(N, lmax), dtype=torch.uint8, device=dev)
+    out = torch.empty(D * D, dtype=torch.complex128, device=dev)
+    nat.check(L.gb_particle_aggregate_dense(N, lmax, nat.ptr(d_pos), nat.ptr(Tj), float(np.real(k)), nat.ptr(ws),
+                                            ws.numel(), nat.ptr(out), current_stream(dev)), "particle aggregate")
+    return out.view(N, 2, rmax, N, 2, rmax).cpu().numpy()
 
 
 def lattice_cells(symmetry, count=5000):

@@ -11,6 +11,7 @@ assembly and solve, and all observables come from the fused epilogue kernel.
 from __future__ import annotations
 
 import enum
+import warnings
 from collections import namedtuple
 
 import numpy as np
@@ -172,9 +173,14 @@ class sphere_cluster:
         sphere_cluster.py:694-712: the aggregate T-matrix (gb_assemble_sphere_dense),
         or with a periodic symmetry the aggregate plus its lattice sums
         (gb_aggregate_periodic_dense), minus the interface's reflection matrix
-        (gb_reflection_matrix_dense) when there is one; BiCGSTAB
-        (gb_solve_dense) or, for solver.exact, an LU solve."""
+        (gb_reflection_matrix_dense) when there is one; BiCGSTAB (gb_solve_dense),
+        run to 1e-14 for solver.exact.  These operators are not symmetric in their
+        pair blocks, so they are solved in FP64 whatever `precision` says (with a
+        warning when it says otherwise)."""
         L = nat.lib()
+        if self.precision != "fp64":
+            warnings.warn(f"precision={self.precision!r} does not apply to clusters with an interface or a periodic "
+                          "symmetry: their dense operator is solved in FP64", stacklevel=3)
         dev, st = b.device, current_stream(b.device)
         md = self.material_data
         N, D = self.Nparticles, 2 * self.rmax * self.Nparticles
@@ -201,11 +207,7 @@ class sphere_cluster:
                       "reflection matrix")
             T -= Rm
             del Rm
-        if _method_is_exact(self.method):
-            A = T.view(D, D) + torch.eye(D, dtype=torch.complex128, device=dev)
-            b.x.copy_(torch.linalg.solve(A, b.b[:D]))
-            self.solver_status, self.solver_iterations, self.solver_residual = 0, 0, 0.0
-            return
+        # solver.exact is the same BiCGSTAB run to 1e-14 (_tolerance), as the plugin's exact branch
         need = L.gb_solve_dense_workspace_size(D, 1)
         ws = torch.empty(need, dtype=torch.uint8, device=dev)
         status = np.zeros(1, np.int32)

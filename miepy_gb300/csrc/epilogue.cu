@@ -376,3 +376,107 @@ extern "C" int gb_particle_cross_sections(int N, int lmax, const double* p_scat,
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }
+
+// --------------------------------------------- general-particle aggregate --
+// The dense aggregate of clusters of general particles (particle_aggregate_tmatrix,
+// cpp/src/interactions.cpp:417-462, with the T-matrix overload of
+// vsh_translation_insert_pair, cpp/src/vsh_translation.cpp:53-159): block (i, j)
+// is A_ij T_j for i != j, zero for i = j, where A is the translation matrix with
+// unit Mie coefficients (the sphere assembler's dense output) and T_j the particle's
+// B x B T-matrix.  A batched complex128 block product on the FP64 pipe: one CTA per
+// (i, j, 32 x 32 output tile), K staged through shared memory in steps of 16, each
+// thread 2 x 2 outputs.
+namespace {
+constexpr int kBT = 32, kBK = 16;
+
+__global__ void k_unit_mie(double2* __restrict__ u, long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        u[e] = make_double2(1.0, 0.0);
+}
+
+__global__ void __launch_bounds__(256)
+k_block_tmat_product(int N, int B, const double2* __restrict__ A, const double2* __restrict__ T,
+                     double2* __restrict__ out) {
+    const int tiles = (B + kBT - 1) / kBT;
+    const int tr = blockIdx.x / tiles, tc = blockIdx.x - tr * tiles;
+    const int j = blockIdx.y, i = blockIdx.z;
+    const long long D = (long long)N * B;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const int r0 = tr * kBT + 2 * ty, c0 = tc * kBT + 2 * tx;
+    double2* ob = out + (long long)i * B * D + (long long)j * B;
+    if (i == j) {   // diagonal blocks stay zero
+#pragma unroll
+        for (int a = 0; a < 2; a++)
+#pragma unroll
+            for (int b = 0; b < 2; b++)
+                if (r0 + a < B && c0 + b < B) ob[(long long)(r0 + a) * D + c0 + b] = make_double2(0, 0);
+        return;
+    }
+    __shared__ double2 As[kBT][kBK + 1], Ts[kBK][kBT + 1];
+    const double2* ab = A + (long long)i * B * D + (long long)j * B;
+    const double2* tb = T + (long long)j * B * B;
+    double2 acc[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) acc[a][b] = make_double2(0, 0);
+    for (int k0 = 0; k0 < B; k0 += kBK) {
+        for (int e = tid; e < kBT * kBK; e += 256) {
+            const int rr = e / kBK, kk = e - rr * kBK;   // A tile: rows of block i, columns k0..
+            const int r = tr * kBT + rr, k = k0 + kk;
+            As[rr][kk] = (r < B && k < B) ? __ldg(ab + (long long)r * D + k) : make_double2(0, 0);
+            const int kr = e / kBT, cc = e - kr * kBT;   // T tile: rows k0.., columns of the output tile
+            const int kt = k0 + kr, c = tc * kBT + cc;
+            Ts[kr][cc] = (kt < B && c < B) ? __ldg(tb + (long long)kt * B + c) : make_double2(0, 0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kBK; kk++) {
+            const double2 a0 = As[2 * ty][kk], a1 = As[2 * ty + 1][kk];
+            const double2 t0 = Ts[kk][2 * tx], t1 = Ts[kk][2 * tx + 1];
+            cfma(acc[0][0], a0, t0);
+            cfma(acc[0][1], a0, t1);
+            cfma(acc[1][0], a1, t0);
+            cfma(acc[1][1], a1, t1);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+            if (r0 + a < B && c0 + b < B) ob[(long long)(r0 + a) * D + c0 + b] = acc[a][b];
+}
+}   // namespace
+
+extern "C" size_t gb_particle_aggregate_workspace_size(int N, int lmax) {
+    if (N < 1 || lmax < 1 || lmax > GB_LMAX_MAX) return 0;
+    const long long D = 2LL * lmax_to_rmax(lmax) * N;
+    return sizeof(double2) * (size_t)(D * D + 2LL * N * lmax);
+}
+
+extern "C" int gb_particle_aggregate_dense(int N, int lmax, const double* pos, const double* tmat, double k,
+                                           void* workspace, size_t ws_bytes, double* out, void* stream) {
+    if (!pos || !tmat || !workspace || !out) return gb_set_error(GB_BAD_ARG, "null pointer");
+    if (N < 1 || lmax < 1 || lmax > GB_LMAX_MAX) return gb_set_error(GB_BAD_ARG, "N=%d lmax=%d invalid", N, lmax);
+    if (N > 65535) return gb_set_error(GB_UNSUPPORTED, "more than 65535 particles");
+    const size_t need = gb_particle_aggregate_workspace_size(N, lmax);
+    if (ws_bytes < need) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, need);
+    cudaStream_t st = (cudaStream_t)stream;
+    const int B = 2 * lmax_to_rmax(lmax);
+    const long long D = (long long)B * N;
+    double2* A = static_cast<double2*>(workspace);
+    double2* unit = A + D * D;
+    gb::note_launch();
+    k_unit_mie<<<(unsigned)((2LL * N * lmax + 255) / 256), 256, 0, st>>>(unit, 2LL * N * lmax);
+    GB_CUDA_TRY(cudaGetLastError());
+    const int e = gb_assemble_sphere_dense(N, lmax, pos, reinterpret_cast<const double*>(unit), k,
+                                           reinterpret_cast<double*>(A), stream);
+    if (e) return e;
+    const int tiles = (B + kBT - 1) / kBT;
+    gb::note_launch();
+    k_block_tmat_product<<<dim3((unsigned)(tiles * tiles), (unsigned)N, (unsigned)N), 256, 0, st>>>(
+        N, B, A, reinterpret_cast<const double2*>(tmat), reinterpret_cast<double2*>(out));
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}

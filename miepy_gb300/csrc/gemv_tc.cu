@@ -385,8 +385,10 @@ k_pgemv_tc(const gb::SysDev* __restrict__ sys, const gb::Strip* __restrict__ str
         const gb::SysDev& Sd = sys[sp.sys];
         const int s = (int)(g % S), x = (int)(g & 1);
         unsigned char* stg = stages + (size_t)s * L.stage;
-        if (cb == 0)   // y_w of the strip's particle i
+        if (cb == 0) {   // y_w of the strip's particle i (the previous build read the old one before its barrier)
             for (int e = tid; e < B * R; e += kTcThreads) syw[e] = Yw[Sd.vec_off + (long long)sp.i * B * R + e];
+            __syncthreads();   // the build below reads other threads' entries
+        }
         bool ok = false;
         if (!*sabort) {
             ok = bar_wait(full + s, (unsigned)((g / S) & 1));

@@ -1,9 +1,9 @@
 """Continuous-batching solve server for sphere-cluster requests on one GPU.
 
 Requests (a cluster, a wavelength, an lmax and a source) arrive at any time.  A
-dispatcher thread admits waiting requests in arrival order against an HBM budget
-(the footprint of each request's matrices, vectors and solver scratch) and a number
-of wave slots.  Everything admitted together forms a wave: one ragged ClusterBatch
+dispatcher thread admits waiting requests against an HBM budget (the footprint of
+each request's matrices, vectors and solver scratch) and a number of wave slots,
+by size class and in arrival order within a class (SolveServer, _take_wave).  Everything admitted together forms a wave: one ragged ClusterBatch
 that is assembled, solved (all clusters advance through the same masked kernels;
 finished ones drop out) and reduced to observables in one sequence of launches on
 the wave's own CUDA stream.  Up to ``max_waves`` waves are on the GPU at once, so
@@ -115,12 +115,21 @@ class SolveServer:
     a ClusterResult."""
 
     def __init__(self, hbm_budget=None, max_waves=3, max_wave_requests=64, precision="mixed", tol=1e-8,
-                 inner_tol=1e-4, maxiter=1000, device=None, max_retries=2, fault_hook=None, metrics_path=None):
+                 inner_tol=1e-4, maxiter=1000, device=None, max_retries=2, fault_hook=None, metrics_path=None,
+                 small_bytes=1 << 30, cost_spread=16.0, max_wait_s=0.5):
         """max_retries: times a request whose wave failed (an exception on the host,
         e.g. an allocation failure) is re-admitted before its Future gets the error.
         fault_hook(wave_id, requests): called at the start of every wave; an exception
         it raises fails that wave (fault injection for tests).  metrics_path: JSONL
-        file receiving one line per finished request."""
+        file receiving one line per finished request.
+
+        Admission (see _take_wave): requests of footprint <= small_bytes are small,
+        the others large; a wave holds one class, and requests whose footprints lie
+        within a factor cost_spread of its first request's, so that no request waits
+        on a much larger one in its own wave; large waves hold at most max_waves - 1
+        slots, so small requests always find one.  Within a class, requests that do
+        not fit the free budget are passed over by later ones, except the class's
+        oldest once it has waited max_wait_s: then nothing passes it."""
         self.max_retries = int(max_retries)
         self.fault_hook = fault_hook
         self.metrics_path = metrics_path
@@ -131,10 +140,12 @@ class SolveServer:
         self.max_wave_requests = int(max_wave_requests)
         self.precision = precision
         self.tol, self.inner_tol, self.maxiter = float(tol), float(inner_tol), int(maxiter)
+        self.small_bytes, self.cost_spread, self.max_wait_s = int(small_bytes), float(cost_spread), float(max_wait_s)
         self._pending = collections.deque()
         self._cv = threading.Condition()
         self._in_use = 0
         self._waves_running = 0
+        self._large_running = 0
         self._wave_counter = 0
         self._closing = False
         self._free_streams = list(range(self.max_waves))
@@ -187,33 +198,65 @@ class SolveServer:
 
     # ------------------------------------------------------------ dispatch --
     def _take_wave(self):
-        """Requests for the next wave (arrival order, within the free budget and
-        the same medium); caller holds the lock."""
-        wave, used = [], 0
-        free = self.budget - self._in_use
-        while self._pending and len(wave) < self.max_wave_requests:
-            req, fut, t0, tries = self._pending[0]
+        """Requests for the next wave and their class (0 small, 1 large); caller
+        holds the lock.  The class whose oldest request is older goes first (large
+        only while it holds fewer than max_waves - 1 running waves).  Its requests
+        are taken in arrival order while they fit the free budget, share the first
+        one's medium and lie within cost_spread of its footprint; one that does not
+        fit is passed over, unless it is the class's oldest and has waited
+        max_wait_s."""
+        live = []
+        for item in self._pending:
+            req, fut, t0, tries = item
             if fut.cancelled():
-                self._pending.popleft()
                 self.stats["cancelled"] += 1
                 continue
             need = request_footprint(req, self.precision)
             if need > self.budget:
-                self._pending.popleft()
                 self.stats["rejected"] += 1
                 fut.set_exception(OverBudget(f"request {req.rid} needs {need} B, budget {self.budget} B"))
                 continue
-            if wave and req.medium_index != wave[0][0].medium_index:
-                break
-            if used + need > free:
-                break
-            self._pending.popleft()
-            if not fut.running() and not fut.set_running_or_notify_cancel():   # cancelled meanwhile
-                self.stats["cancelled"] += 1
+            live.append((item, need, 0 if need <= self.small_bytes else 1))
+        self._pending = collections.deque(item for item, _, _ in live)
+        free = self.budget - self._in_use
+        now = time.perf_counter()
+        oldest = {}
+        for item, need, cls in live:
+            oldest.setdefault(cls, item[2])
+        for cls in sorted(oldest, key=oldest.get):
+            if cls == 1 and self.max_waves >= 2 and self._large_running >= self.max_waves - 1:
                 continue
-            wave.append((req, fut, t0, need, tries))
-            used += need
-        return wave, used
+            wave, used, taken, anchor = [], 0, set(), None
+            first = True
+            for item, need, c in live:
+                if c != cls:
+                    continue
+                req, fut, t0, tries = item
+                head, first = first, False
+                if wave and req.medium_index != wave[0][0].medium_index:
+                    continue
+                if anchor is not None and not (anchor / self.cost_spread <= need <= anchor * self.cost_spread):
+                    continue
+                if used + need > free:
+                    if head and now - t0 > self.max_wait_s:
+                        break   # the class's oldest has waited long enough: nothing passes it
+                    continue
+                if not fut.running() and not fut.set_running_or_notify_cancel():   # cancelled meanwhile
+                    self.stats["cancelled"] += 1
+                    taken.add(id(item))
+                    continue
+                wave.append((req, fut, t0, need, tries))
+                taken.add(id(item))
+                used += need
+                if anchor is None:
+                    anchor = need
+                if len(wave) >= self.max_wave_requests:
+                    break
+            if taken:
+                self._pending = collections.deque(it for it in self._pending if id(it) not in taken)
+            if wave:
+                return wave, used, cls
+        return [], 0, None
 
     def _dispatch(self):
         while True:
@@ -222,12 +265,13 @@ class SolveServer:
                     if self._closing and not self._pending:
                         return
                     if self._pending and self._free_streams:
-                        wave, used = self._take_wave()
+                        wave, used, cls = self._take_wave()
                         if wave:
                             break
-                    self._cv.wait(timeout=0.5)
+                    self._cv.wait(timeout=0.05)
                 self._in_use += used
                 self._waves_running += 1
+                self._large_running += cls
                 self.stats["peak_bytes"] = max(self.stats["peak_bytes"], self._in_use)
                 self.stats["max_concurrent_waves"] = max(self.stats["max_concurrent_waves"], self._waves_running)
                 self.stats["admitted"] += len(wave)
@@ -235,9 +279,9 @@ class SolveServer:
                 sidx = self._free_streams.pop()
                 wid = self._wave_counter
                 self._wave_counter += 1
-            self._pool.submit(self._run_wave, wave, used, sidx, wid)
+            self._pool.submit(self._run_wave, wave, used, sidx, wid, cls)
 
-    def _run_wave(self, wave, used, sidx, wid):
+    def _run_wave(self, wave, used, sidx, wid, cls=0):
         t_admit = time.perf_counter()
         requeue = []
         try:
@@ -264,6 +308,7 @@ class SolveServer:
             with self._cv:
                 self._in_use -= used
                 self._waves_running -= 1
+                self._large_running -= cls
                 self._free_streams.append(sidx)
                 if requeue:
                     self.stats["failed_waves"] += 1

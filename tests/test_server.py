@@ -22,11 +22,14 @@ import pytest
 from miepy_gb300 import server as SV
 
 
-def _bare_server(budget, max_wave_requests=8, precision="mixed"):
+def _bare_server(budget, max_wave_requests=8, precision="mixed", small_bytes=1 << 62, cost_spread=float("inf"),
+                 max_wait_s=0.5, max_waves=3):
     s = object.__new__(SV.SolveServer)
     s.budget = budget
     s.max_wave_requests = max_wave_requests
     s.precision = precision
+    s.small_bytes, s.cost_spread, s.max_wait_s, s.max_waves = small_bytes, cost_spread, max_wait_s, max_waves
+    s._large_running = 0
     s._pending = collections.deque()
     s._in_use = 0
     s.stats = dict(admitted=0, completed=0, rejected=0, waves=0, peak_bytes=0, max_concurrent_waves=0,
@@ -48,7 +51,7 @@ def test_admission_fifo_budget_and_rejection():
         f = cf.Future()
         futs.append(f)
         s._pending.append((r, f, 0.0, 0))
-    wave, used = s._take_wave()
+    wave, used, _ = s._take_wave()
     assert [w[0].rid for w in wave] == [0, 1, 3]       # request 2 exceeds the whole budget ...
     assert used == need[0] + need[1] + need[3]
     assert isinstance(futs[2].exception(timeout=0), SV.OverBudget)  # ... and is rejected
@@ -57,10 +60,10 @@ def test_admission_fifo_budget_and_rejection():
     s2 = _bare_server(budget=need[0] + need[1])
     for r in (reqs[0], reqs[1], reqs[3]):
         s2._pending.append((r, cf.Future(), 0.0, 0))
-    wave, used = s2._take_wave()
+    wave, used, _ = s2._take_wave()
     assert [w[0].rid for w in wave] == [0, 1]          # request 3 waits: the budget is used up
     s2._in_use = used - need[0]                         # request 0's wave finished
-    wave, used = s2._take_wave()
+    wave, used, _ = s2._take_wave()
     assert [w[0].rid for w in wave] == [3]
 
 
@@ -70,16 +73,60 @@ def test_admission_waits_for_memory_and_splits_media():
     s = _bare_server(budget=int(1.5 * na))
     for r in (a, b):
         s._pending.append((r, cf.Future(), 0.0, 0))
-    wave, used = s._take_wave()
+    wave, used, _ = s._take_wave()
     assert [w[0].rid for w in wave] == [0]
     s._in_use = used
-    wave, _ = s._take_wave()
+    wave, _, _ = s._take_wave()
     assert wave == []                                   # request 1 waits for request 0's memory
     s2 = _bare_server(budget=10 * na)
     for r in (_req(10, 3, 0, 1.0), _req(10, 3, 1, 1.33), _req(10, 3, 2, 1.0)):
         s2._pending.append((r, cf.Future(), 0.0, 0))
-    wave, _ = s2._take_wave()
-    assert [w[0].rid for w in wave] == [0]              # one medium per wave
+    wave, _, _ = s2._take_wave()
+    assert [w[0].rid for w in wave] == [0, 2]           # one medium per wave ...
+    wave, _, _ = s2._take_wave()
+    assert [w[0].rid for w in wave] == [1]              # ... the other one next
+
+
+def test_admission_size_classes_spread_and_age_bound():
+    small, large = _req(10, 3, 0), _req(300, 6, 1)
+    ns, nl = SV.request_footprint(small, "mixed"), SV.request_footprint(large, "mixed")
+    # classes: a large request (older) and small ones never share a wave
+    s = _bare_server(budget=10 * nl, small_bytes=(ns + nl) // 2)
+    for r, t in ((large, 0.0), (small, 1.0), (_req(12, 3, 2), 2.0)):
+        s._pending.append((r, cf.Future(), t, 0))
+    wave, _, cls = s._take_wave()
+    assert [w[0].rid for w in wave] == [1] and cls == 1
+    wave, _, cls = s._take_wave()
+    assert [w[0].rid for w in wave] == [0, 2] and cls == 0
+    # large waves keep a slot free for small ones: with max_waves - 1 large waves running,
+    # a later small request goes first
+    s = _bare_server(budget=10 * nl, small_bytes=(ns + nl) // 2, max_waves=3)
+    s._large_running = 2
+    for r, t in ((large, 0.0), (small, 1.0)):
+        s._pending.append((r, cf.Future(), t, 0))
+    wave, _, cls = s._take_wave()
+    assert [w[0].rid for w in wave] == [0] and cls == 0
+    # cost spread: a request far smaller than the wave's first waits for its own wave
+    s = _bare_server(budget=10 * nl, cost_spread=4.0)
+    for r, t in ((large, 0.0), (small, 1.0), (_req(280, 6, 3), 2.0)):
+        s._pending.append((r, cf.Future(), t, 0))
+    wave, _, _ = s._take_wave()
+    assert [w[0].rid for w in wave] == [1, 3]
+    # skip-ahead: a request that does not fit is passed by a later one that does, until
+    # it has waited max_wait_s
+    now = SV.time.perf_counter()
+    s = _bare_server(budget=nl + ns, max_wait_s=0.5)
+    s._in_use = 2 * ns                                # free: nl - ns, too little for the large one
+    for r, t in ((large, now), (small, now + 0.001)):
+        s._pending.append((r, cf.Future(), t, 0))
+    wave, _, _ = s._take_wave()
+    assert [w[0].rid for w in wave] == [0]            # the small one passes the young large head
+    s = _bare_server(budget=nl + ns, max_wait_s=0.5)
+    s._in_use = 2 * ns                                # free: nl - ns, too little for the large one
+    for r, t in ((large, now - 1.0), (small, now)):
+        s._pending.append((r, cf.Future(), t, 0))
+    wave, _, _ = s._take_wave()
+    assert wave == []                                 # the old head keeps its place
 
 
 def test_request_generator():
