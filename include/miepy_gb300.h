@@ -344,6 +344,17 @@ int gb_near_field32(int N, int lmax, const double* pos, const double* radius, co
                     const double* p_int, double k, const double* k_int, int Npts, const double* pts, int interior,
                     int magnetic, double hfac_re, double hfac_im, const double* hfac_int, double* out, void* stream);
 
+/* Far-field form of the scattered field (replaces sphere_cluster.E_field /
+ * H_field with far=True, src/miepy/sphere_cluster.py:244-391, whose per-particle
+ * expand_E_far / expand_H_far are src/miepy/vsh/expansion.py:45-77,96-108): at each
+ * point the sum over particles of e^{ikr}/(kr) (-i)^n E_mn (tau, pi) terms of p_scat
+ * about the particle, no radial component and no interior expansions.  magnetic
+ * swaps the coefficients and multiplies by hfac (-i sqrt(eps_b / mu_b)).
+ * pos [N,3], p_scat [N,2,rmax] c128, pts [Npts,3] f64 (device), out [Npts][3] c128. */
+int gb_far_field_expansions(int N, int lmax, const double* pos, const double* p_scat, double k, int Npts,
+                            const double* pts, int magnetic, double hfac_re, double hfac_im, double* out,
+                            void* stream);
+
 /* ------------------------------------------------------------ beam source --
  * Beam expansion coefficients at N particles from the beam's far-field
  * projection: replaces integrate_phase, cpp/src/decomposition.cpp:29-66, as

@@ -86,6 +86,8 @@ SIGNATURES = {
                               _P, _P, _P]),
     "gb_near_field32": (c_int, [c_int, c_int, _P, _P, _P, _P, c_double, _P, c_int, _P, c_int, c_int, c_double,
                                 c_double, _P, _P, _P]),
+    "gb_far_field_expansions": (c_int, [c_int, c_int, _P, _P, c_double, c_int, _P, c_int, c_double, c_double, _P,
+                                        _P]),
 }
 
 

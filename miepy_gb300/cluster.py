@@ -53,6 +53,43 @@ def _method_is_exact(method):
     return name == "exact" or method == 1 or str(method).endswith("exact")
 
 
+def sph_points(x1, x2, x3, origin, spherical):
+    """The points as Cartesian arrays: (r, theta, phi) about origin when spherical
+    (coordinates.py:8-17), else (x, y, z) as given, broadcast to one shape."""
+    x1, x2, x3 = np.broadcast_arrays(*(np.asarray(v, dtype=float) for v in (x1, x2, x3)))
+    if not spherical:
+        return x1, x2, x3
+    o = np.asarray(origin, dtype=float)
+    return (o[0] + x1 * np.sin(x2) * np.cos(x3), o[1] + x1 * np.sin(x2) * np.sin(x3), o[2] + x1 * np.cos(x2))
+
+
+def vec_to_sph(F, theta, phi):
+    """Cartesian field components -> (r, theta, phi) components at the given angles
+    (vec_cart_to_sph, coordinates.py:71-89)."""
+    theta, phi = np.broadcast_arrays(np.asarray(theta, float), np.asarray(phi, float))
+    st, ct, sp, cp = np.sin(theta), np.cos(theta), np.sin(phi), np.cos(phi)
+    basis = [(st * cp, st * sp, ct), (ct * cp, ct * sp, -st), (-sp, cp, 0.0 * theta)]
+    return np.array([sum(b[c] * F[c] for c in range(3)) for b in basis])
+
+
+def far_expansions(dev, position, p_scat, k, pts, magnetic, hfac):
+    """Sum of every particle's outgoing expansion in its far-field form at pts
+    [P, 3] (gb_far_field_expansions): [P, 3] complex on the host."""
+    d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+    L = lmax_from_rmax(np.asarray(p_scat).shape[-1])
+    out = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
+    P = d(pts, torch.float64)
+    nat.check(nat.lib().gb_far_field_expansions(np.asarray(position).shape[0], L, nat.ptr(d(position, torch.float64)),
+                                                nat.ptr(d(p_scat, torch.complex128)), float(np.real(k)),
+                                                pts.shape[0], nat.ptr(P), int(bool(magnetic)), float(np.real(hfac)),
+                                                float(np.imag(hfac)), nat.ptr(out), current_stream(dev)), "far field")
+    return out.cpu().numpy()
+
+
+def lmax_from_rmax(rmax):
+    return int(round(np.sqrt(1 + rmax) - 1))
+
+
 class sphere_cluster:
     """Solve Generalized Mie Theory for an N-sphere cluster on the GPU.
 
@@ -336,10 +373,12 @@ class sphere_cluster:
 
     # --------------------------------------------------------------- fields --
     def _field(self, x1, x2, x3, interior, source, mask, far, spherical, magnetic):
-        if far or spherical:
-            raise NotImplementedError("far-field / spherical field evaluation is not on the GPU path yet")
-        x1, x2, x3 = (np.asarray(x, dtype=float) for x in (x1, x2, x3))
-        x, y, z = np.broadcast_arrays(x1, x2, x3)
+        """E or H at points (sphere_cluster.py:244-391).  spherical: the points are
+        (r, theta, phi) about the cluster origin and the field is returned in
+        spherical components there; far: every particle's outgoing expansion in its
+        far-field form (gb_far_field_expansions), the source's far field, and no
+        interior expansions or mask."""
+        x, y, z = sph_points(x1, x2, x3, self.origin, spherical)
         shape = x.shape
         pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
         dev = self._batch.device
@@ -347,20 +386,23 @@ class sphere_cluster:
         N, L = self.Nparticles, self.lmax
         d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
         pos = d(self.position, torch.float64)
-        rad = d(self.radius, torch.float64)
         ps = d(self.p_scat, torch.complex128)
-        pi_ = d(self.p_int, torch.complex128)
-        k_int = d(2 * np.pi * np.asarray(md.n, complex) / self.wavelength, torch.complex128)
         hfac = -1j * np.sqrt(md.eps_b / md.mu_b) if magnetic else 1.0
-        hint = d(-1j * np.sqrt(np.asarray(md.eps, complex) / np.asarray(md.mu, complex)), torch.complex128)
         P = d(pts, torch.float64)
         out = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
-        use_int = bool(interior and not mask)
-        nat.check(nat.lib().gb_near_field(N, L, nat.ptr(pos), nat.ptr(rad), nat.ptr(ps), nat.ptr(pi_),
-                                          float(np.real(md.k_b)), nat.ptr(k_int), pts.shape[0], nat.ptr(P),
-                                          int(use_int), int(bool(magnetic)), float(np.real(hfac)),
-                                          float(np.imag(hfac)), nat.ptr(hint), nat.ptr(out),
-                                          current_stream(dev)), "near field")
+        use_int = bool(interior and not mask and not far)
+        if far:
+            out = torch.from_numpy(far_expansions(dev, self.position, self.p_scat, md.k_b, pts, magnetic, hfac))
+        else:
+            rad = d(self.radius, torch.float64)
+            pi_ = d(self.p_int, torch.complex128)
+            k_int = d(2 * np.pi * np.asarray(md.n, complex) / self.wavelength, torch.complex128)
+            hint = d(-1j * np.sqrt(np.asarray(md.eps, complex) / np.asarray(md.mu, complex)), torch.complex128)
+            nat.check(nat.lib().gb_near_field(N, L, nat.ptr(pos), nat.ptr(rad), nat.ptr(ps), nat.ptr(pi_),
+                                              float(np.real(md.k_b)), nat.ptr(k_int), pts.shape[0], nat.ptr(P),
+                                              int(use_int), int(bool(magnetic)), float(np.real(hfac)),
+                                              float(np.imag(hfac)), nat.ptr(hint), nat.ptr(out),
+                                              current_stream(dev)), "near field")
         E = out.cpu().numpy().T.reshape((3,) + shape).copy()
         inside = np.zeros(shape, dtype=bool)
         for i in range(N):
@@ -371,13 +413,18 @@ class sphere_cluster:
             srcs = [self.source]
             if self.interface is not None:   # sphere_cluster.py:279-283, 355-361
                 srcs.append(self.source.reflect(self.interface, self.medium, self.wavelength))
-            S = sum(s.H_field(x, y, z, k) * (md.eps_b / md.mu_b) ** 0.5 if magnetic else s.E_field(x, y, z, k)
-                    for s in srcs)
+            if not all(hasattr(s, "E_field") for s in srcs):
+                raise NotImplementedError(f"{type(self.source).__name__} sources provide no field here; "
+                                          "use source=False")
+            S = sum(s.H_field(x, y, z, k, far=far) * (md.eps_b / md.mu_b) ** 0.5 if magnetic
+                    else s.E_field(x, y, z, k, far=far) for s in srcs)
             if use_int:
                 S = np.where(inside[None], 0.0, S)
             E = E + S
-        if mask:
+        if mask and not far:
             E[:, inside] = 0
+        if spherical:   # components along the points' own (r, theta, phi) directions
+            E = vec_to_sph(E, x2, x3)
         return E
 
     def E_field(self, x1, x2, x3, interior=True, source=True, mask=False, far=False, spherical=False):

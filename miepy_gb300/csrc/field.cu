@@ -54,14 +54,23 @@ __device__ double2 Emn(int m, int n) {
 // otherwise j_n of complex kr, factor -i.
 constexpr int kLF = 8;   // largest expansion order of the field kernel
 
+// far: the outgoing expansion's far-field form instead (expand_E_far,
+// vsh/expansion.py:45-77): no radial component, h_n(kr) -> (-i)^n e^{ikr} / (kr) with
+// E_theta = i f E_mn (-i)^n (c0 tau + c1 pi) e^{im phi},
+// E_phi = -f E_mn (-i)^n (c0 pi + c1 tau) e^{im phi}, f = e^{ikr} / (kr).
 __device__ void add_expansion(int L, const double2* __restrict__ c, int rmax, bool outgoing, double2 k, double rad,
                               double theta, double phi, bool swap, double2 pref, const double2* __restrict__ emn,
-                              const double* __restrict__ negf_tab, double2 E[3]) {
+                              const double* __restrict__ negf_tab, double2 E[3], bool far = false) {
     const int NP = L + 2;
     // radial functions z_n and derivatives for n = 0..L (the reference's recurrences)
     double2 z[kLF + 2], zp[kLF + 2];
     const double2 kr = make_double2(k.x * rad, k.y * rad);
-    if (outgoing) {
+    double2 ffar = make_double2(0, 0);
+    if (far) {
+        double s, co;
+        sincos(kr.x, &s, &co);
+        ffar = make_double2(co / kr.x, s / kr.x);
+    } else if (outgoing) {
         const double x = kr.x;
         double s, co;
         sincos(x, &s, &co);
@@ -93,7 +102,7 @@ __device__ void add_expansion(int L, const double2* __restrict__ c, int rmax, bo
     }
     // derivative z_n' = z_{n-1} - (n+1)/kr z_n, n >= 1
 #pragma unroll 1
-    for (int n = 1; n <= L; n++) {
+    for (int n = 1; n <= L && !far; n++) {
         double2 f = cdivd(make_double2((double)(n + 1), 0), kr);
         double2 a = cmul(f, z[n]);
         zp[n] = make_double2(z[n - 1].x - a.x, z[n - 1].y - a.y);
@@ -146,6 +155,21 @@ __device__ void add_expansion(int L, const double2* __restrict__ c, int rmax, bo
             double sm, cm;
             sincos((double)m * phi, &sm, &cm);
             const double2 eph = make_double2(cm, sm);
+            if (far) {
+                const double2 c0 = swap ? c[rmax + r] : c[r];
+                const double2 c1 = swap ? c[r] : c[rmax + r];
+                // i f E_mn (-i)^n e^{im phi}
+                const double2 mi_n = (n & 3) == 0 ? make_double2(1, 0)
+                                   : (n & 3) == 1 ? make_double2(0, -1)
+                                   : (n & 3) == 2 ? make_double2(-1, 0) : make_double2(0, 1);
+                const double2 w = cmul(cmul(make_double2(0, 1), ffar), cmul(cmul(emn[r], mi_n), eph));
+                const double2 a = make_double2(c0.x * tau_v + c1.x * pi_v, c0.y * tau_v + c1.y * pi_v);
+                const double2 b = make_double2(c0.x * pi_v + c1.x * tau_v, c0.y * pi_v + c1.y * tau_v);
+                const double2 t1 = cmul(w, a), t2 = cmul(make_double2(0, 1), cmul(w, b));
+                Es[1].x += t1.x; Es[1].y += t1.y;
+                Es[2].x += t2.x; Es[2].y += t2.y;
+                continue;
+            }
             const double2 H = z[n], Hp = zp[n];
             // N: (n(n+1) P H/kr e, (H + kr H') e/kr tau, i (H + kr H') e/kr pi)
             const double2 hk = cdivd(cmul(H, eph), kr);
@@ -182,7 +206,7 @@ __global__ void __launch_bounds__(kFieldThreads)
 k_field(int L, int N, const double* __restrict__ pos, const double* __restrict__ radius, const double2* __restrict__ p_scat,
         const double2* __restrict__ p_int, double k, const double2* __restrict__ k_int, int Npts,
         const double* __restrict__ pts, int interior, int magnetic, double2 hfac, const double2* __restrict__ hfac_int,
-        double2* __restrict__ out) {
+        double2* __restrict__ out, int far) {
     const int rmax = L * (L + 2);
     constexpr int kTile = 16;
     __shared__ double sp_pos[kTile][3];
@@ -230,7 +254,7 @@ k_field(int L, int N, const double* __restrict__ pos, const double* __restrict__
             const double theta = acos(dz / rad);
             const double phi = atan2(dy, dx);
             add_expansion(L, sp_c + q * 2 * rmax, rmax, true, make_double2(k, 0), rad, theta, phi, magnetic != 0,
-                          pref_out, emn, negf_tab, E);
+                          pref_out, emn, negf_tab, E, far != 0);
         }
     }
     if (!valid) return;
@@ -464,7 +488,27 @@ extern "C" int gb_near_field(int N, int lmax, const double* pos, const double* r
     if (lmax < 1 || lmax > kLF) return gb_set_error(GB_UNSUPPORTED, "near field supports lmax 1..%d (got %d)", kLF, lmax);
     gb::note_launch();
     k_field<<<grid, kFieldThreads, 0, s>>>(lmax, N, pos, radius, ps2, pi2, k, ki2, Npts, pts, interior, magnetic, hf,
-                                           hi2, o2);
+                                           hi2, o2, 0);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+// The far-field form of every particle's outgoing expansion, summed at the points
+// (sphere_cluster.E_field / H_field with far=True, sphere_cluster.py:244-391, with
+// expand_E_far / expand_H_far, vsh/expansion.py:45-77,96-108): no interior
+// expansions; H fields swap the coefficients and take the prefactor hfac.
+extern "C" int gb_far_field_expansions(int N, int lmax, const double* pos, const double* p_scat, double k, int Npts,
+                                       const double* pts, int magnetic, double hfac_re, double hfac_im, double* out,
+                                       void* stream) {
+    if (N < 1 || Npts < 0 || !pos || !p_scat || !pts || !out) return gb_set_error(GB_BAD_ARG, "bad field arguments");
+    if (lmax < 1 || lmax > kLF) return gb_set_error(GB_UNSUPPORTED, "far field supports lmax 1..%d (got %d)", kLF, lmax);
+    if (Npts == 0) return GB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned grid = (unsigned)((Npts + kFieldThreads - 1) / kFieldThreads);
+    gb::note_launch();
+    k_field<<<grid, kFieldThreads, 0, s>>>(lmax, N, pos, nullptr, reinterpret_cast<const double2*>(p_scat), nullptr, k,
+                                           nullptr, Npts, pts, 0, magnetic, make_double2(hfac_re, hfac_im), nullptr,
+                                           reinterpret_cast<double2*>(out), 1);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
 }

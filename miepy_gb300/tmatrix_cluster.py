@@ -20,7 +20,8 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .cluster import DEFAULT_MAXITER, DEFAULT_TOL, EXACT_TOL, _method_is_exact, cross_sections, sphere_cluster
+from .cluster import (DEFAULT_MAXITER, DEFAULT_TOL, EXACT_TOL, _method_is_exact, cross_sections, far_expansions,
+                      sph_points, sphere_cluster, vec_to_sph)
 from .engine import ClusterBatch, current_stream
 from .materials import constant_material
 from .mie import mie_coefficients
@@ -173,41 +174,47 @@ class tmatrix_cluster:
         plus the source.  Inside a particle's enclosed radius the reference evaluates
         its interior coefficients, which stay zero for general particles, so those
         points read 0 (interior=True) or are masked (mask=True).  Evaluated by the
-        GPU near-field kernel (gb_near_field) with zero interior coefficients."""
-        if far or spherical:
-            raise NotImplementedError("far-field / spherical field evaluation is not on the GPU path")
-        x, y, z = np.broadcast_arrays(*(np.asarray(v, dtype=float) for v in (x1, x2, x3)))
+        GPU near-field kernel (gb_near_field) with zero interior coefficients.
+        spherical and far as for sphere_cluster (points about the cluster origin;
+        far-field forms of the expansions, gb_far_field_expansions)."""
+        x, y, z = sph_points(x1, x2, x3, self.origin, spherical)
         shape = x.shape
         pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
         dev = self._batch.device
         N, L = self.Nparticles, self.lmax
-        d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
-        ps = d(self.p_scat, torch.complex128)
-        zeros = torch.zeros_like(ps)
-        ones = torch.ones(N, dtype=torch.complex128, device=dev)
-        k_int = ones * self.k_b
         hfac = -1j * np.sqrt(self.eps_b / self.mu_b) if magnetic else 1.0
-        use_int = bool(interior and not mask and np.any(self.enclosed > 0))
-        out = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
-        pos, rad, P = d(self.position, torch.float64), d(self.enclosed, torch.float64), d(pts, torch.float64)
-        nat.check(nat.lib().gb_near_field(N, L, nat.ptr(pos), nat.ptr(rad), nat.ptr(ps), nat.ptr(zeros),
-                                          float(self.k_b), nat.ptr(k_int), pts.shape[0], nat.ptr(P), int(use_int),
-                                          int(bool(magnetic)), float(np.real(hfac)), float(np.imag(hfac)),
-                                          nat.ptr(ones), nat.ptr(out), current_stream(dev)), "near field")
-        E = out.cpu().numpy().T.reshape((3,) + shape).copy()
+        use_int = bool(interior and not mask and not far and np.any(self.enclosed > 0))
+        if far:
+            out = far_expansions(dev, self.position, self.p_scat, self.k_b, pts, magnetic, hfac)
+        else:
+            d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+            ps = d(self.p_scat, torch.complex128)
+            zeros = torch.zeros_like(ps)
+            ones = torch.ones(N, dtype=torch.complex128, device=dev)
+            k_int = ones * self.k_b
+            o = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
+            pos, rad, P = d(self.position, torch.float64), d(self.enclosed, torch.float64), d(pts, torch.float64)
+            nat.check(nat.lib().gb_near_field(N, L, nat.ptr(pos), nat.ptr(rad), nat.ptr(ps), nat.ptr(zeros),
+                                              float(self.k_b), nat.ptr(k_int), pts.shape[0], nat.ptr(P), int(use_int),
+                                              int(bool(magnetic)), float(np.real(hfac)), float(np.imag(hfac)),
+                                              nat.ptr(ones), nat.ptr(o), current_stream(dev)), "near field")
+            out = o.cpu().numpy()
+        E = out.T.reshape((3,) + shape).copy()
         inside = np.zeros(shape, dtype=bool)
         for i in range(N):
             inside |= ((x - self.position[i, 0]) ** 2 + (y - self.position[i, 1]) ** 2
                        + (z - self.position[i, 2]) ** 2) < self.enclosed[i] ** 2
         if source:
             k = self.k_b
-            S = (self.source.H_field(x, y, z, k) * (self.eps_b / self.mu_b) ** 0.5 if magnetic
-                 else self.source.E_field(x, y, z, k))
+            S = (self.source.H_field(x, y, z, k, far=far) * (self.eps_b / self.mu_b) ** 0.5 if magnetic
+                 else self.source.E_field(x, y, z, k, far=far))
             if use_int:
                 S = np.where(inside[None], 0.0, S)
             E = E + S
-        if mask:
+        if mask and not far:
             E[:, inside] = 0
+        if spherical:
+            E = vec_to_sph(E, x2, x3)
         return E
 
     def E_field(self, x1, x2, x3, interior=True, source=True, mask=False, far=False, spherical=False):

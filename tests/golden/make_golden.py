@@ -6,9 +6,9 @@ inputs and outputs of the sphere-cluster path as small ``.npz`` files.  The GPU
 parity tests compare the product against these fixtures without needing the
 reference tree at run time.
 
-Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large]
+Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large | fields]
         (or with the reference staged by oracle/stage_reference.py:
-         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large])
+         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large | fields])
 """
 
 import os
@@ -409,8 +409,36 @@ def large_main():
     print("wrote serve_n300_lmax6_exact")
 
 
+def fields_main():
+    """Far-field and spherical-coordinate fields of the water dimer (lmax 6, exact
+    solve): E and H with far=True (Cartesian points 50 um away, and the same points
+    given as (r, theta, phi) with spherical=True) and near fields with
+    spherical=True at r = 400 nm about the origin."""
+    miepy = import_reference()
+    c = miepy.sphere_cluster(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm,
+                             material=miepy.constant_material(index=0.2 + 3.0j),
+                             source=miepy.sources.plane_wave.from_string(polarization="x"),
+                             wavelength=600 * nm, lmax=6, medium=miepy.materials.water(), method=miepy.solver.exact)
+    th = np.linspace(0.2, np.pi - 0.2, 5)
+    ph = np.linspace(0.1, 2 * np.pi - 0.3, 5)
+    r_far = np.full(5, 50e-6)
+    r_near = np.full(5, 400 * nm)
+    x, y, z = miepy.coordinates.sph_to_cart(r_far, th, ph)
+    rec = dict(theta=th, phi=ph, r_far=r_far, r_near=r_near, x_far=x, y_far=y, z_far=z,
+               E_far=c.E_field(x, y, z, far=True), H_far=c.H_field(x, y, z, far=True),
+               E_far_sph=c.E_field(r_far, th, ph, far=True, spherical=True),
+               H_far_sph=c.H_field(r_far, th, ph, far=True, spherical=True),
+               E_far_scat_sph=c.E_field(r_far, th, ph, far=True, spherical=True, source=False),
+               E_near_sph=c.E_field(r_near, th, ph, spherical=True),
+               H_near_sph=c.H_field(r_near, th, ph, spherical=True))
+    np.savez_compressed(os.path.join(HERE, "dimer_lmax6_far_spherical.npz"), **rec)
+    print("wrote dimer_lmax6_far_spherical")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "large":
         large_main()
+    elif len(sys.argv) > 1 and sys.argv[1] == "fields":
+        fields_main()
     else:
         main()

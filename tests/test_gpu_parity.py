@@ -433,3 +433,26 @@ def test_autotuned_gemv_shapes(precision):
     fresh.solve(tol=1e-10, inner_tol=1e-4)
     assert np.all(fresh.status == 0)
     assert rel(fresh.x.cpu().numpy(), ref) < 1e-8
+
+
+def test_far_and_spherical_fields_match_reference():
+    """E_field / H_field with far=True and/or spherical=True (sphere_cluster.py:244-391,
+    expand_E_far / expand_H_far, vsh/expansion.py:45-77,96-108) against the reference's
+    own values for the water dimer (fixture dimer_lmax6_far_spherical): 1e-9 of the
+    largest component."""
+    g = G.load("dimer_lmax6_far_spherical")
+    c = gb.sphere_cluster(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm,
+                          material=gb.constant_material(index=0.2 + 3.0j), source=gb.plane_wave.from_string("x"),
+                          wavelength=600 * nm, lmax=6, medium=gb.materials.water(), method=gb.solver.exact)
+    th, ph = g["theta"], g["phi"]
+    cases = [
+        (c.E_field(g["x_far"], g["y_far"], g["z_far"], far=True), g["E_far"]),
+        (c.H_field(g["x_far"], g["y_far"], g["z_far"], far=True), g["H_far"]),
+        (c.E_field(g["r_far"], th, ph, far=True, spherical=True), g["E_far_sph"]),
+        (c.H_field(g["r_far"], th, ph, far=True, spherical=True), g["H_far_sph"]),
+        (c.E_field(g["r_far"], th, ph, far=True, spherical=True, source=False), g["E_far_scat_sph"]),
+        (c.E_field(g["r_near"], th, ph, spherical=True), g["E_near_sph"]),
+        (c.H_field(g["r_near"], th, ph, spherical=True), g["H_near_sph"]),
+    ]
+    for got, want in cases:
+        assert rel(got, want) < 1e-9
