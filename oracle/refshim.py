@@ -5,8 +5,8 @@ TEST INFRASTRUCTURE ONLY, and only in a checkout that has the reference tree
 reference package ``miepy`` imports a compiled module ``miepy.cpp`` (pybind11
 over Eigen and GSL) that cannot be built without those libraries; this module
 registers the oracle (``oracle/oracle.py``) under that name with the same
-submodules and function names, plus small stand-ins for three optional third-
-party imports (``quaternion``, ``yaml``, ``matplotlib.colors``).  The reference's
+submodules and function names, plus small stand-ins for four optional third-
+party imports (``quaternion``, ``yaml``, ``matplotlib.colors``, ``spherical``).  The reference's
 Python files themselves run unmodified; the only run-time adjustment is the
 location of the material database, which the reference ships zipped.
 
@@ -149,6 +149,10 @@ class _Quat:
     def __hash__(self):
         return hash((float(np.sum(self.w)), float(np.sum(self.x)), float(np.sum(self.y)), float(np.sum(self.z))))
 
+    @property
+    def components(self):
+        return np.array([self.w, self.x, self.y, self.z])
+
 
 def _quaternion_module():
     m = types.ModuleType("quaternion")
@@ -178,6 +182,44 @@ def _quaternion_module():
     m.from_spherical_coords = from_spherical_coords
     m.as_rotation_matrix = as_rotation_matrix
     m.as_spherical_coords = as_spherical_coords
+    return m
+
+
+def _spherical_module():
+    """Stand-in for the ``spherical`` package's wigner_D(R, ell_min, ell_max), the
+    only function the reference takes from it (vsh/vsh_rotation.py:8-29).  For the
+    rotation R = Rz(alpha) Ry(beta) Rz(gamma) of quaternion components (w, x, y, z)
+    it returns, flattened [m', m] per ell, the complex conjugate of the standard
+    D-matrix exp(-i m' alpha) d^ell(beta) exp(-i m gamma), with
+    d^ell(beta) = exp(-i beta J_y) evaluated as a matrix exponential of the angular
+    momentum generator (J_y = (J+ - J-) / 2i on |ell, m>), so that the reference's
+    conj(D) (-1)^(m - m') is the standard rotation of its VSH coefficients."""
+    from scipy.linalg import expm
+
+    m = types.ModuleType("spherical")
+
+    def euler_zyz(q):
+        w, x, y, z = (float(np.ravel(c)[0]) for c in q)
+        beta = 2 * np.arctan2(np.hypot(x, y), np.hypot(w, z))
+        apc, amc = np.arctan2(z, w), np.arctan2(-x, y)
+        return apc + amc, beta, apc - amc
+
+    def d_small(ell, beta):
+        ms = np.arange(-ell, ell + 1, dtype=float)
+        jp = np.diag(np.sqrt(ell * (ell + 1) - ms[:-1] * (ms[:-1] + 1)), -1)   # <m+1|J+|m>
+        jy = (jp - jp.T) / 2j
+        return expm(-1j * beta * jy).real
+
+    def wigner_D(R, ell_min, ell_max):
+        alpha, beta, gamma = euler_zyz(R)
+        out = []
+        for ell in range(ell_min, ell_max + 1):
+            ms = np.arange(-ell, ell + 1)
+            D = np.exp(-1j * ms[:, None] * alpha) * d_small(ell, beta) * np.exp(-1j * ms[None, :] * gamma)
+            out.append(np.conj(D).ravel())
+        return np.concatenate(out)
+
+    m.wigner_D = wigner_D
     return m
 
 
@@ -242,7 +284,8 @@ def import_reference(ref_src: str | None = None):
     if "miepy" in sys.modules and getattr(sys.modules["miepy"], "_oracle_shim", False):
         return sys.modules["miepy"]
 
-    for name, factory in (("quaternion", _quaternion_module), ("yaml", _yaml_module)):
+    for name, factory in (("quaternion", _quaternion_module), ("yaml", _yaml_module),
+                          ("spherical", _spherical_module)):
         try:
             importlib.import_module(name)
         except ImportError:
