@@ -26,6 +26,7 @@ from scipy.special import erfc
 
 from . import _native as nat
 from .modes import lmax_to_rmax, mode_indices
+from .rotation import rotate_expansion_coefficients, rotation_matrix
 from .special import Emn, pi_func, tau_func
 from .sources import sph_basis_vectors
 
@@ -42,13 +43,52 @@ def _trapz_weights(x):
     return w
 
 
+# ------------------------------------------------------------ quaternions --
+# The unit quaternions the reference's beams use for directions (numpy-quaternion's
+# from_spherical_coords, product, inverse and as_spherical_coords), as (w, x, y, z)
+# arrays.
+def _q_from_sph(theta, phi):   # exp(phi k / 2) exp(theta j / 2): Rz(phi) Ry(theta)
+    theta, phi = np.broadcast_arrays(np.asarray(theta, float), np.asarray(phi, float))
+    return np.array([np.cos(phi / 2) * np.cos(theta / 2), -np.sin(phi / 2) * np.sin(theta / 2),
+                     np.cos(phi / 2) * np.sin(theta / 2), np.sin(phi / 2) * np.cos(theta / 2)])
+
+
+def _q_mul(a, b):
+    a1, b1, c1, d1 = a
+    a2, b2, c2, d2 = b
+    return np.array([a1 * a2 - b1 * b2 - c1 * c2 - d1 * d2, a1 * b2 + b1 * a2 + c1 * d2 - d1 * c2,
+                     a1 * c2 - b1 * d2 + c1 * a2 + d1 * b2, a1 * d2 + b1 * c2 - c1 * b2 + d1 * a2])
+
+
+def _q_inv(q):
+    return np.array([q[0], -q[1], -q[2], -q[3]]) / np.sum(np.asarray(q) ** 2, axis=0)
+
+
+def _q_to_sph(q):
+    w, x, y, z = q
+    return 2 * np.arctan2(np.sqrt(x ** 2 + y ** 2), np.sqrt(w ** 2 + z ** 2)), np.arctan2(z, w) + np.arctan2(-x, y)
+
+
+def rotate_sph(theta, phi, quat):
+    """Directions (theta, phi) rotated by quat (coordinates.py:157-170), with the
+    reference's correction of phi where theta = 0."""
+    theta, phi = np.broadcast_arrays(np.asarray(theta, float), np.asarray(phi, float))
+    tq = np.broadcast_to(np.asarray(quat, float).reshape((4,) + (1,) * theta.ndim), (4,) + theta.shape)
+    th_r, ph_r = _q_to_sph(_q_mul(tq, _q_from_sph(theta, phi)))
+    ph_r = np.array(ph_r, dtype=float)
+    ph_r[theta == 0] *= 2
+    return np.asarray(th_r, dtype=float), ph_r
+
+
 class gaussian_beam:
-    """Gaussian beam (sources/common.py:10-52) propagating along +z."""
+    """Gaussian beam (sources/common.py:10-52).  A beam at (theta, phi) is the +z beam
+    rotated by Rz(phi) Ry(theta) about its centre (sources/sources.py:164,
+    sources/beams.py:168-200): particle positions are taken into the beam's frame,
+    decomposed there on the GPU, and the coefficients rotated back (Wigner-D,
+    miepy_gb300.rotation)."""
 
     def __init__(self, width, polarization, power=1, theta_max=np.pi / 2, phase=0, center=None, theta=0, phi=0,
                  standing=False):
-        if theta != 0 or phi != 0:
-            raise NotImplementedError("rotated beams are not on the GPU path (propagation along +z only)")
         if standing:
             raise NotImplementedError("standing beams are not on the sphere-cluster path")
         self.width = width
@@ -149,12 +189,60 @@ class gaussian_beam:
         return out
 
     def reflect(self, interface, medium, wavelength):
-        """The reference reflects a beam by rotating its far field (beams.py:202-203,
-        323-360), which needs Wigner-D rotations (the ``spherical`` package)."""
-        raise NotImplementedError("reflected Gaussian beams need Wigner-D rotations; use a plane wave with interface=")
+        """The beam reflected by a planar interface (beams.py:202-203, 323-365)."""
+        return reflected_beam(self, interface, wavelength, medium)
+
+    @property
+    def rotated(self):
+        return self.theta != 0 or self.phi != 0
 
     def structure(self, position, k, lmax):
-        """p_src [N, 2, rmax] (host numpy), computed on the GPU."""
-        N = np.asarray(position, float).reshape(-1, 3).shape[0]
-        out = self.structure_device(position, k, lmax)
-        return out.cpu().numpy().reshape(N, 2, lmax_to_rmax(lmax))
+        """p_src [N, 2, rmax] (host numpy), computed on the GPU (and rotated on the
+        host for a beam at (theta, phi) != 0)."""
+        pos = np.asarray(position, float).reshape(-1, 3)
+        N = pos.shape[0]
+        if not self.rotated:
+            out = self.structure_device(pos, k, lmax)
+            return out.cpu().numpy().reshape(N, 2, lmax_to_rmax(lmax))
+        Rm = rotation_matrix(self.phi, self.theta)
+        # the beam frame: R^T (pos - center); structure_device subtracts the centre itself
+        pos_b = (pos - self.center) @ Rm + self.center
+        p = self.structure_device(pos_b, k, lmax).cpu().numpy().reshape(N, 2, lmax_to_rmax(lmax))
+        return rotate_expansion_coefficients(p, self.phi, self.theta)
+
+
+class reflected_beam(gaussian_beam):
+    """A Gaussian beam reflected by a planar interface (beams.py:323-365): the
+    incident beam's centre mirrored in the interface, direction pi - theta, and the
+    incident angular spectrum weighted by the Fresnel coefficients of each plane-wave
+    component, mapped through the two beam frames."""
+
+    def __init__(self, incident, interface, wavelength, medium):
+        center = np.array(incident.center, dtype=float)
+        center[2] += 2 * (interface.z - center[2])
+        gaussian_beam.__init__(self, width=incident.width, polarization=incident.polarization, power=incident.power,
+                               theta_max=incident.theta_max, phase=incident.phase, center=center,
+                               theta=np.pi - incident.theta, phi=incident.phi)
+        self.incident = incident
+        self.interface = interface
+        self.wavelength = wavelength
+        self.medium = medium
+
+    def angular_spectrum(self, theta, phi, k):
+        th, ph = rotate_sph(np.asarray(theta, float) - np.pi, phi, _q_from_sph(self.theta, self.phi))
+        th = np.where(th > np.pi / 2, np.pi - th, th)
+        r_par, r_perp = self.interface.reflection_coefficients(th, self.wavelength, self.medium)
+        th, ph = rotate_sph(th - np.pi, ph, _q_inv(_q_from_sph(self.incident.theta, self.incident.phi)))
+        U = self.incident.angular_spectrum(th, ph, k)
+        U[0] *= r_par
+        U[1] *= r_perp
+        return -U
+
+    def E0(self, k):
+        return self.incident.E0(k)
+
+    def theta_cutoff(self, k, cutoff=1e-6, tol=None):
+        return self.incident.theta_cutoff(k, cutoff, tol)
+
+    def reflect(self, interface, medium, wavelength):
+        raise NotImplementedError("a reflected beam is not reflected again")

@@ -6,9 +6,9 @@ inputs and outputs of the sphere-cluster path as small ``.npz`` files.  The GPU
 parity tests compare the product against these fixtures without needing the
 reference tree at run time.
 
-Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large | fields]
+Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large | fields | beams]
         (or with the reference staged by oracle/stage_reference.py:
-         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large | fields])
+         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large | fields | beams])
 """
 
 import os
@@ -409,6 +409,46 @@ def large_main():
     print("wrote serve_n300_lmax6_exact")
 
 
+def beams_main():
+    """Rotated and reflected Gaussian beams (the reference's rotation runs with the
+    harness's stand-in for the ``spherical`` package's Wigner-D matrices):
+    gauss_beam_rotated_lmax5  p_src of beams (waist 1 um, 600 nm, vacuum) at
+        (theta, phi) = (0.6, 0.9) centred off the origin, (pi, 0) and (1.2, -2.0)
+        with circular polarisation, at 7 positions, lmax 5;
+    interface_gauss3_lmax3_exact  the substrate trimer of interface3_lmax3_exact
+        driven by a Gaussian beam (waist 1 um): p_src with the reflected beam, p_inc,
+        cross-sections, forces and torques."""
+    miepy = import_reference()
+    k_v = 2 * np.pi / (600 * nm)
+    rng_b = np.random.default_rng(12)
+    bpos = rng_b.uniform(-600 * nm, 600 * nm, size=(7, 3))
+    specs = [dict(theta=0.6, phi=0.9, polarization=[1, 0], center=[50 * nm, -30 * nm, 20 * nm]),
+             dict(theta=np.pi, phi=0.0, polarization=[0, 1], center=[0, 0, 0]),
+             dict(theta=1.2, phi=-2.0, polarization=[1, 1j], center=[-40 * nm, 0, 70 * nm])]
+    rec = dict(position=bpos, k=np.float64(k_v), lmax=np.int64(5), width=np.float64(1000 * nm))
+    for q, sp in enumerate(specs):
+        b = miepy.sources.gaussian_beam(width=1000 * nm, polarization=sp["polarization"], theta=sp["theta"],
+                                        phi=sp["phi"], center=sp["center"])
+        rec[f"theta_{q}"], rec[f"phi_{q}"] = np.float64(sp["theta"]), np.float64(sp["phi"])
+        rec[f"polarization_{q}"] = np.asarray(sp["polarization"], complex)
+        rec[f"center_{q}"] = np.asarray(sp["center"], float)
+        rec[f"p_src_{q}"] = b.structure(bpos, k_v, 5)
+    np.savez_compressed(os.path.join(HERE, "gauss_beam_rotated_lmax5.npz"), **rec)
+    print("wrote gauss_beam_rotated_lmax5")
+    sub = miepy.interface(miepy.constant_material(index=1.7), z=-120 * nm)
+    c = miepy.sphere_cluster(position=[[0, 0, 0], [210 * nm, 40 * nm, 30 * nm], [-160 * nm, 90 * nm, 60 * nm]],
+                             radius=[70 * nm, 60 * nm, 80 * nm], material=miepy.constant_material(index=1.5 + 0.01j),
+                             medium=miepy.materials.water(),
+                             source=miepy.sources.gaussian_beam(width=1000 * nm, polarization=[1, 0]),
+                             wavelength=600 * nm, lmax=3, interface=sub, method=miepy.solver.exact)
+    C = c.cross_sections()
+    rec = dict(position=c.position, radius=c.radius, p_src=c.p_src, p_inc=c.p_inc, p_scat=c.p_scat,
+               cross_sections=np.array([C.scattering, C.absorption, C.extinction], dtype=float),
+               force=c.force(), torque=c.torque())
+    np.savez_compressed(os.path.join(HERE, "interface_gauss3_lmax3_exact.npz"), **rec)
+    print("wrote interface_gauss3_lmax3_exact")
+
+
 def fields_main():
     """Far-field and spherical-coordinate fields of the water dimer (lmax 6, exact
     solve): E and H with far=True (Cartesian points 50 um away, and the same points
@@ -440,5 +480,7 @@ if __name__ == "__main__":
         large_main()
     elif len(sys.argv) > 1 and sys.argv[1] == "fields":
         fields_main()
+    elif len(sys.argv) > 1 and sys.argv[1] == "beams":
+        beams_main()
     else:
         main()

@@ -14,9 +14,7 @@ import pytest
 from tests.conftest import ROOT, reference_available
 
 # Reference test files on the sphere-cluster path that the oracle must pass, with
-# the expected number of passing tests.  Tests that need libraries absent here
-# (``spherical`` for rotated beams; substrate reflection, which is outside the
-# path) are deselected by name.
+# the expected number of passing tests.
 PINNED = {
     "test_single_gmt.py": 3,
     "test_cluster.py": 2,
@@ -37,14 +35,14 @@ PINNED = {
     "test_point_matching.py": 2,
     "test_coordinate_geometry.py": 2,
     "test_source_rotation.py": 1,
-    "test_interface.py": 2,
+    "test_interface.py": 4,
+    "test_maxwells_equations.py": 14,
 }
 
-# Parametrisations that need the absent ``spherical`` package (Wigner-D rotation of
-# a reflected Gaussian beam), deselected by a -k expression on their ids.
-DESELECT = {
-    "test_interface.py": "not s10 and not source0",
-}
+# Parametrisations deselected by a -k expression on their ids (none at present: the
+# Gaussian-beam cases of test_interface.py, which rotate expansion coefficients, run
+# with the harness's stand-in for the ``spherical`` package).
+DESELECT = {}
 
 pytestmark = pytest.mark.skipif(not reference_available(), reason="reference source tree not available")
 
