@@ -44,7 +44,7 @@
 
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 160;   // 4 consumer warps + 1 producer warp
 constexpr int kTcStages = 3;
 constexpr long long kTcWaitCycles = 400000000LL;   // about 0.2 s of SM clock
 
@@ -122,23 +122,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* b) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(su32(b))
                  : "memory");
 }
-// 16 consecutive columns of the warp's 32 TMEM lanes (lane = accumulator row).  The
-// load and its wait are one statement, so no use of the registers can be scheduled
-// before they are written.
-__device__ __forceinline__ void tmem_ld16(unsigned taddr, float* v) {
-    unsigned r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];\n"
-        "tcgen05.wait::ld.sync.aligned;\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
 // Shared-memory matrix descriptor, K-major, no swizzle: core matrices of 8 rows x
 // 16 bytes; lbo = byte step between core matrices along K, sbo = along M (or N).
 __device__ __forceinline__ uint64_t smem_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
@@ -157,9 +140,18 @@ __device__ __forceinline__ unsigned bf2(float lo_half, float hi_half) {   // (fi
 __device__ __forceinline__ float bf_round(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
 
 // ------------------------------------------------------------ shared layout --
+// Header: S full barriers, 2 MMA barriers, the TMEM address, the abort flag, then S
+// job records; the row map at off_row; the two B-operand buffers; S stages, each
+// the block's two bf16 planes, its y_u (particle j) and y_w (particle i).
+struct TcJob {
+    long long cw;    // element offset of the block's column partials in CW
+    long long cu;    // element offset of the strip's row partials in CU (last block of a strip), else -1
+    int valid;       // 0: no more blocks for this CTA
+    int pad;
+};
 struct TcLayout {
     unsigned sbo, plane, tile, ybytes, stage, bbytes;
-    unsigned off_row, off_yw, off_b, off_stage, total;
+    unsigned off_jobs, off_row, off_b, off_stage, total;
 };
 __host__ __device__ inline TcLayout tc_layout(int B, int R) {
     TcLayout L;
@@ -168,11 +160,11 @@ __host__ __device__ inline TcLayout tc_layout(int B, int R) {
     L.plane = (unsigned)(Bp / 8) * L.sbo;
     L.tile = 2u * L.plane;
     L.ybytes = (unsigned)(B * R * 8);
-    L.stage = (L.tile + L.ybytes + 127u) & ~127u;
+    L.stage = (L.tile + 2u * L.ybytes + 127u) & ~127u;
     L.bbytes = (unsigned)(8 * R) * (unsigned)Kp * 2u;
-    L.off_row = 128;
-    L.off_yw = 1024;
-    L.off_b = L.off_yw + ((L.ybytes + 127u) & ~127u);
+    L.off_jobs = 128;   // after 2S + 2 barriers, the TMEM slot, the abort flag, the consumed count
+    L.off_row = 256;
+    L.off_b = 1024;
     L.off_stage = L.off_b + 2u * L.bbytes;
     unsigned end = L.off_stage + (unsigned)kTcStages * L.stage;
     // an M = 128 MMA reads 16 row groups of each plane: the lo plane of the last
@@ -230,6 +222,42 @@ k_tc_tiles(const gb::SysDev* __restrict__ sys, const float2* __restrict__ mat64,
 }
 
 // ------------------------------------------------------------- matrix pass --
+// NC consecutive TMEM columns (NC = 32 or 64) of the warp's 32 lanes, loaded in
+// x16 pieces and waited for once, in one statement.
+template <int NC> __device__ __forceinline__ void tmem_ld_cols(unsigned taddr, float* v);
+template <> __device__ __forceinline__ void tmem_ld_cols<32>(unsigned taddr, float* v) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%32];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%33];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr), "r"(taddr + 16u)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+template <> __device__ __forceinline__ void tmem_ld_cols<64>(unsigned taddr, float* v) {
+    tmem_ld_cols<32>(taddr, v);
+    tmem_ld_cols<32>(taddr + 32u, v + 32);
+}
+
+// The pass over strips [sbeg, send) of one block size B.  Warps 0-3 consume, warp 4
+// produces.  The producer (its lane 0) walks this CTA's strips (every gridDim.x-th,
+// skipping clusters with no active right-hand side); for each block it waits until
+// the block that last used the stage has finished its MMAs (the stage's empty
+// barrier, committed with them), writes the block's job record (its partials'
+// offsets) into the stage's slot and streams the block's bf16 planes, y_u of
+// particle j and y_w of particle i into the stage; after the last block it arrives
+// on the next stage's full barrier with an invalid job.  The consumers build each
+// block's B operand, meet at a named barrier, and thread 0 issues the MMAs,
+// committing them to the accumulator's barrier and the stage's empty barrier; then
+// every consumer reads the previous block's accumulator rows.  Each consumer keeps
+// the jobs of the block it builds and of the block it reads out in registers.
+constexpr int kTcConsumers = 128;   // warps 0-3
 template <int R>
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_pgemv_tc(const gb::SysDev* __restrict__ sys, const gb::Strip* __restrict__ strips, long long sbeg, long long send,
@@ -245,21 +273,27 @@ k_pgemv_tc(const gb::SysDev* __restrict__ sys, const gb::Strip* __restrict__ str
     const int Kp = gb::tc_cols(B);
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t* full = reinterpret_cast<uint64_t*>(sm);
-    uint64_t* mdone = full + S;
+    uint64_t* empty = full + S;
+    uint64_t* mdone = empty + S;
     unsigned* tslot = reinterpret_cast<unsigned*>(mdone + 2);
     volatile int* sabort = reinterpret_cast<volatile int*>(tslot + 1);
+    long long* sconsumed = reinterpret_cast<long long*>(tslot + 2);
+    TcJob* jobs = reinterpret_cast<TcJob*>(sm + L.off_jobs);
     int* srow = reinterpret_cast<int*>(sm + L.off_row);
-    float2* syw = reinterpret_cast<float2*>(sm + L.off_yw);
     unsigned char* bbuf = sm + L.off_b;
     unsigned char* stages = sm + L.off_stage;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long G = gridDim.x;
 
     if (tid == 0) {
-        for (int s = 0; s < S; s++) bar_init(full + s, 1);
+        for (int q = 0; q < S; q++) {
+            bar_init(full + q, 1);
+            bar_init(empty + q, 1);
+        }
         bar_init(mdone, 1);
         bar_init(mdone + 1, 1);
         *sabort = 0;
+        *sconsumed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     {   // both B-operand buffers start at zero: their K padding is never written again
@@ -280,183 +314,203 @@ k_pgemv_tc(const gb::SysDev* __restrict__ sys, const gb::Strip* __restrict__ str
     pdl_wait_tc();   // y vectors and solver state come from the preceding kernels
     pdl_trigger_tc();
 
-    auto active = [&](long long w) { return gb::any_active<R>(st, strips[w].sys, mask); };
-    auto seek = [&](long long w) {
-        while (w < send && !active(w)) w += G;
-        return w;
-    };
-    auto advance = [&](long long& w, int& b) {
-        if (++b >= strips[w].nb) {
-            b = 0;
-            w = seek(w + G);
-        }
-    };
-    const uint64_t pol = evict_first_policy();
-    auto issue = [&](long long w, int b, long long g) {   // thread 0: block b of strip w into stage g % S
-        const gb::Strip sp = strips[w];
-        const gb::SysDev& Sd = sys[sp.sys];
-        const int s = (int)(g % S);
-        unsigned char* dst = stages + (size_t)s * L.stage;
-        const int j = sp.i + 1 + (int)(sp.p0 - pair_start(sp.i, Sd.N)) + b;
-        bar_expect_tx(full + s, L.tile + L.ybytes);
-        bulk_copy_hint(dst, mat_tc + Sd.tc_off + (sp.p0 + b) * (long long)L.tile, L.tile, full + s, pol);
-        bulk_copy(dst + L.tile, Yu + Sd.vec_off + (long long)j * B * R, L.ybytes, full + s);
-    };
-
-    const long long first = seek(sbeg + blockIdx.x);
-    long long pw = first;   // producer cursor (thread 0)
-    int pb = 0;
-    long long issued = 0;
-    if (tid == 0)
-        while (issued < S && pw < send) {
-            issue(pw, pb, issued);
-            issued++;
-            advance(pw, pb);
-        }
-
-    // epilogue cursor: the block whose accumulator is read next
-    long long ew = first;
-    int eb = 0;
-    float u[2 * R];
-#pragma unroll
-    for (int q = 0; q < 2 * R; q++) u[q] = 0.f;
-    const int m = warp * 32 + lane;   // accumulator row (TMEM lane) of this thread
-    const bool warp_rows = warp * 32 < B;
-    int rho_m = 0;
-    unsigned eneg_m = 0;
-    if (m < B) {
-        rho_m = srow[m] & ((1 << 29) - 1);
-        eneg_m = (srow[m] >> 29) & 1;
-    }
-
-    // reads block e's accumulator: its column partials out, its row partial into u;
-    // at the strip's end the row partials out
-    auto epilogue = [&](long long e) -> bool {
-        const int x = (int)(e & 1);
-        bool ok = bar_wait(mdone + x, (unsigned)((e >> 1) & 1));
-        ok = __all_sync(0xffffffffu, ok);
-        tc_after_sync();
-        const gb::Strip sp = strips[ew];
-        const gb::SysDev& Sd = sys[sp.sys];
-        const gb::SysPlan& pl = plan[sp.sys];
-        if (ok && warp_rows) {
-            float v[N];
-#pragma unroll
-            for (int c = 0; c < N; c += 16)
-                tmem_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(x * N + c), v + c);
-            if (m < B) {
-                const int j = sp.i + 1 + (int)(sp.p0 - pair_start(sp.i, Sd.N)) + eb;
-                float2* cwp = CW + pl.cw_off + ((long long)j * (j - 1) / 2 + sp.i) * (long long)B * R +
-                              (long long)rho_m * R;
-#pragma unroll
-                for (int q = 0; q < R; q++) {
-                    u[2 * q] += v[2 * q] + v[4 * R + 2 * q];
-                    u[2 * q + 1] += v[2 * q + 1] + v[4 * R + 2 * q + 1];
-                    const float wr = v[2 * R + 2 * q] + v[6 * R + 2 * q];
-                    const float wi = v[2 * R + 2 * q + 1] + v[6 * R + 2 * q + 1];
-                    cwp[q] = make_float2(flipf(wr, eneg_m), flipf(wi, eneg_m));
+    if (warp == kTcConsumers / 32) {
+        // ------------------------------------------------------------ producer
+        long long k = 0;   // stages written (blocks and the final invalid job)
+        if (lane == 0) {
+            long long pw = sbeg + blockIdx.x;
+            int pb = 0;
+            const uint64_t pol = evict_first_policy();
+            auto seek = [&]() {
+                while (pw < send && !gb::any_active<R>(st, strips[pw].sys, mask)) pw += G;
+            };
+            seek();
+            for (;; k++) {
+                const int s = (int)(k % S);
+                if (k >= S && !bar_wait(empty + s, (unsigned)((k / S - 1) & 1))) {   // the stage's last MMAs
+                    *sabort = 1;
+                    atomicExch(err, 1);
+                    break;
+                }
+                if (*sabort) break;
+                if (pw >= send) {   // the end: an invalid job, with a plain arrive
+                    jobs[s].valid = 0;
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(su32(full + s)) : "memory");
+                    k++;
+                    break;
+                }
+                const gb::Strip sp = strips[pw];
+                const gb::SysDev& Sd = sys[sp.sys];
+                const gb::SysPlan& pl = plan[sp.sys];
+                const int j = sp.i + 1 + (int)(sp.p0 - pair_start(sp.i, Sd.N)) + pb;
+                TcJob J;
+                J.cw = pl.cw_off + ((long long)j * (j - 1) / 2 + sp.i) * (long long)B * R;
+                J.cu = (pb == sp.nb - 1) ? pl.cu_off + (pw - pl.strip_base) * (long long)B * R : -1;
+                J.valid = 1;
+                J.pad = 0;
+                jobs[s] = J;
+                unsigned char* dst = stages + (size_t)s * L.stage;
+                bar_expect_tx(full + s, L.tile + 2u * L.ybytes);   // arrive (release): the job record goes with it
+                bulk_copy_hint(dst, mat_tc + Sd.tc_off + (sp.p0 + pb) * (long long)L.tile, L.tile, full + s, pol);
+                bulk_copy(dst + L.tile, Yu + Sd.vec_off + (long long)j * B * R, L.ybytes, full + s);
+                bulk_copy(dst + L.tile + L.ybytes, Yw + Sd.vec_off + (long long)sp.i * B * R, L.ybytes, full + s);
+                if (++pb >= sp.nb) {
+                    pb = 0;
+                    pw += G;
+                    seek();
                 }
             }
         }
-        tc_before_sync();
-        if (!ok && lane == 0) {
-            *sabort = 1;
-            atomicExch(err, 1);
-        }
-        if (eb == sp.nb - 1) {   // the strip's row partial
-            if (ok && m < B) {
-                float2* cup = CU + pl.cu_off + (ew - pl.strip_base) * (long long)B * R + (long long)rho_m * R;
+        __syncthreads();   // every thread of the CTA meets here once the consumers are done
+        if (lane == 0)     // drain: every stage written and not consumed (bounded waits)
+            for (long long q = *sconsumed; q < k; q++) (void)bar_wait(full + (q % S), (unsigned)((q / S) & 1));
+    } else {
+        // ------------------------------------------------------------ consumers
+        float u[2 * R];
 #pragma unroll
-                for (int q = 0; q < R; q++) cup[q] = make_float2(flipf(u[2 * q], eneg_m), flipf(u[2 * q + 1], eneg_m));
+        for (int q = 0; q < 2 * R; q++) u[q] = 0.f;
+        const int m = warp * 32 + lane;   // accumulator row (TMEM lane) of this thread
+        const bool warp_rows = warp * 32 < B;
+        int rho_m = 0;
+        unsigned eneg_m = 0;
+        if (m < B) {
+            rho_m = srow[m] & ((1 << 29) - 1);
+            eneg_m = (srow[m] >> 29) & 1;
+        }
+        // block e's accumulator: its column partials out, its row partial into u; at the
+        // strip's end the row partials out
+        auto epilogue = [&](long long e, const TcJob& J) -> bool {
+            const int x = (int)(e & 1);
+            bool ok = bar_wait(mdone + x, (unsigned)((e >> 1) & 1));
+            ok = __all_sync(0xffffffffu, ok);
+            tc_after_sync();
+            if (ok && warp_rows) {
+                float v[N];
+                tmem_ld_cols<N>(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(x * N), v);
+                if (m < B) {
+                    float2 w[R];
+#pragma unroll
+                    for (int q = 0; q < R; q++) {
+                        u[2 * q] += v[2 * q] + v[4 * R + 2 * q];
+                        u[2 * q + 1] += v[2 * q + 1] + v[4 * R + 2 * q + 1];
+                        w[q] = make_float2(flipf(v[2 * R + 2 * q] + v[6 * R + 2 * q], eneg_m),
+                                           flipf(v[2 * R + 2 * q + 1] + v[6 * R + 2 * q + 1], eneg_m));
+                    }
+                    float4* cwp = reinterpret_cast<float4*>(CW + J.cw + (long long)rho_m * R);
+#pragma unroll
+                    for (int q = 0; q < R; q += 2) cwp[q / 2] = make_float4(w[q].x, w[q].y, w[q + 1].x, w[q + 1].y);
+                }
             }
-#pragma unroll
-            for (int q = 0; q < 2 * R; q++) u[q] = 0.f;
-        }
-        advance(ew, eb);
-        return ok;
-    };
-
-    long long cw = first;   // consumer cursor
-    int cb = 0;
-    long long g = 0;        // blocks whose MMAs were issued
-    bool aborted = false;
-    while (cw < send) {
-        const gb::Strip sp = strips[cw];
-        const gb::SysDev& Sd = sys[sp.sys];
-        const int s = (int)(g % S), x = (int)(g & 1);
-        unsigned char* stg = stages + (size_t)s * L.stage;
-        if (cb == 0) {   // y_w of the strip's particle i (the previous build read the old one before its barrier)
-            for (int e = tid; e < B * R; e += kTcThreads) syw[e] = Yw[Sd.vec_off + (long long)sp.i * B * R + e];
-            __syncthreads();   // the build below reads other threads' entries
-        }
-        bool ok = false;
-        if (!*sabort) {
-            ok = bar_wait(full + s, (unsigned)((g / S) & 1));
-            if (!ok) {
+            tc_before_sync();
+            if (!ok && lane == 0) {
                 *sabort = 1;
                 atomicExch(err, 1);
             }
-        }
-        // B operand of block g into buffer x (last read by the MMAs of block g - 2,
-        // which completed before this thread's epilogue of g - 2)
-        if (ok) {
-            const float2* yu = reinterpret_cast<const float2*>(stg + L.tile);
-            unsigned char* bb = bbuf + (size_t)x * L.bbytes;
-            for (int it = tid; it < B * R; it += kTcThreads) {
-                const int sc = it / R, q = it - sc * R;
-                const int info = srow[sc];
-                const int rs = info & ((1 << 29) - 1);
-                const unsigned en = (info >> 29) & 1;
-                const float2 zu = yu[rs * R + q], zw = syw[rs * R + q];
-                const float zr[2] = {flipf(zu.x, en), flipf(zw.x, en)};
-                const float zi[2] = {flipf(zu.y, en), flipf(zw.y, en)};
-                const unsigned col = (unsigned)(sc >> 2) * 128u + (unsigned)(sc & 3) * 4u;
+            if (J.cu >= 0) {   // the strip's row partial
+                if (ok && m < B) {
+                    float4* cup = reinterpret_cast<float4*>(CU + J.cu + (long long)rho_m * R);
 #pragma unroll
-                for (int h = 0; h < 2; h++) {   // h 0: U rows (z_j), 1: W rows (w_i)
-                    const float hr = bf_round(zr[h]), hi = bf_round(zi[h]);
-                    const float lr = zr[h] - hr, li = zi[h] - hi;
-                    const int n0 = h * 2 * R + 2 * q, n1 = n0 + 4 * R;   // hi rows, lo rows (n0 even)
-                    unsigned char* r0 = bb + (n0 >> 3) * L.sbo + col + (n0 & 7) * 16;
-                    unsigned char* r1 = bb + (n1 >> 3) * L.sbo + col + (n1 & 7) * 16;
-                    *reinterpret_cast<unsigned*>(r0) = bf2(hr, -hi);        // row n0:     re(A z)
-                    *reinterpret_cast<unsigned*>(r0 + 16) = bf2(hi, hr);    // row n0 + 1: im(A z)
-                    *reinterpret_cast<unsigned*>(r1) = bf2(lr, -li);
-                    *reinterpret_cast<unsigned*>(r1 + 16) = bf2(li, lr);
+                    for (int q = 0; q < R; q += 2)
+                        cup[q / 2] = make_float4(flipf(u[2 * q], eneg_m), flipf(u[2 * q + 1], eneg_m),
+                                                 flipf(u[2 * q + 2], eneg_m), flipf(u[2 * q + 3], eneg_m));
+                }
+#pragma unroll
+                for (int q = 0; q < 2 * R; q++) u[q] = 0.f;
+            }
+            return ok;
+        };
+
+        long long g = 0;   // blocks whose MMAs were issued
+        bool aborted = false;
+        TcJob prev;
+        prev.valid = 0;
+        while (true) {
+            const int s = (int)(g % S), x = (int)(g & 1);
+            unsigned char* stg = stages + (size_t)s * L.stage;
+            bool ok = false;
+            TcJob J;
+            J.valid = 0;
+            if (!*sabort) {
+                ok = bar_wait(full + s, (unsigned)((g / S) & 1));
+                if (!ok) {
+                    *sabort = 1;
+                    atomicExch(err, 1);
+                } else {
+                    J = jobs[s];
                 }
             }
+            // B operand of block g into buffer x (last read by the MMAs of block g - 2,
+            // which completed before this thread's epilogue of g - 2)
+            if (ok && J.valid) {
+                const float2* yu = reinterpret_cast<const float2*>(stg + L.tile);
+                const float2* yw = reinterpret_cast<const float2*>(stg + L.tile + L.ybytes);
+                unsigned char* bb = bbuf + (size_t)x * L.bbytes;
+                for (int it = tid; it < B * R; it += kTcConsumers) {
+                    const int sc = it / R, q = it - sc * R;
+                    const int info = srow[sc];
+                    const int rs = info & ((1 << 29) - 1);
+                    const unsigned en = (info >> 29) & 1;
+                    const float2 zu = yu[rs * R + q], zw = yw[rs * R + q];
+                    const float zr[2] = {flipf(zu.x, en), flipf(zw.x, en)};
+                    const float zi[2] = {flipf(zu.y, en), flipf(zw.y, en)};
+                    const unsigned col = (unsigned)(sc >> 2) * 128u + (unsigned)(sc & 3) * 4u;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {   // h 0: U rows (z_j), 1: W rows (w_i)
+                        const float hr = bf_round(zr[h]), hi = bf_round(zi[h]);
+                        const float lr = zr[h] - hr, li = zi[h] - hi;
+                        const int n0 = h * 2 * R + 2 * q, n1 = n0 + 4 * R;   // hi rows, lo rows (n0 even)
+                        unsigned char* r0 = bb + (n0 >> 3) * L.sbo + col + (n0 & 7) * 16;
+                        unsigned char* r1 = bb + (n1 >> 3) * L.sbo + col + (n1 & 7) * 16;
+                        *reinterpret_cast<unsigned*>(r0) = bf2(hr, -hi);        // row n0:     re(A z)
+                        *reinterpret_cast<unsigned*>(r0 + 16) = bf2(hi, hr);    // row n0 + 1: im(A z)
+                        *reinterpret_cast<unsigned*>(r1) = bf2(lr, -li);
+                        *reinterpret_cast<unsigned*>(r1 + 16) = bf2(li, lr);
+                    }
+                }
+            }
+            proxy_fence();   // generic writes of the B operand -> the tensor core's reads
+            tc_before_sync();
+            // the consumer warps' barrier, with the OR of every consumer's view of the
+            // abort flag (the producer may set it at any time): one decision for all
+            unsigned stop = (!ok || *sabort) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, %2, p;\n"
+                " selp.u32 %0, 1, 0, q;\n}\n"
+                : "=r"(stop)
+                : "r"(stop), "n"(kTcConsumers)
+                : "memory");
+            tc_after_sync();
+            if (stop) {
+                aborted = true;
+                break;
+            }
+            if (!J.valid) break;   // the same record for every consumer: the end of this CTA's blocks
+            if (tid == 0) {
+                const unsigned a_hi = su32(stg), a_lo = a_hi + L.plane, bsm = su32(bbuf + (size_t)x * L.bbytes);
+                const unsigned d = tmem + (unsigned)(x * N);
+                for (int ks = 0; ks < Kp / 16; ks++) {
+                    const uint64_t bd = smem_desc(bsm + ks * 256, 128, L.sbo);
+                    mma_bf16(d, smem_desc(a_hi + ks * 256, 128, L.sbo), bd, IDESC_FULL, ks > 0);
+                    mma_bf16(d, smem_desc(a_lo + ks * 256, 128, L.sbo), bd, IDESC_HALF, 1);
+                }
+                mma_commit(mdone + x);
+                mma_commit(empty + s);   // the stage is free once these MMAs have read it
+            }
+            g++;
+            if (g >= 2) epilogue(g - 2, prev);   // the previous block's accumulator out
+            prev = J;
         }
-        proxy_fence();   // generic writes of the B operand -> the tensor core's reads
+        if (!aborted && g >= 1 && !epilogue(g - 1, prev)) aborted = true;
+        if (tid == 0) {
+            *sconsumed = g;
+            if (aborted)   // bounded waits for the MMAs still in flight
+                for (long long e = (g >= 2 ? g - 2 : 0); e < g; e++)
+                    (void)bar_wait(mdone + (e & 1), (unsigned)((e >> 1) & 1));
+        }
         tc_before_sync();
         __syncthreads();
-        tc_after_sync();
-        if (*sabort) {
-            aborted = true;
-            break;
-        }
-        if (tid == 0) {
-            const unsigned a_hi = su32(stg), a_lo = a_hi + L.plane, bsm = su32(bbuf + (size_t)x * L.bbytes);
-            const unsigned d = tmem + (unsigned)(x * N);
-            for (int ks = 0; ks < Kp / 16; ks++) {
-                const uint64_t bd = smem_desc(bsm + ks * 256, 128, L.sbo);
-                mma_bf16(d, smem_desc(a_hi + ks * 256, 128, L.sbo), bd, IDESC_FULL, ks > 0);
-                mma_bf16(d, smem_desc(a_lo + ks * 256, 128, L.sbo), bd, IDESC_HALF, 1);
-            }
-            mma_commit(mdone + x);
-        }
-        g++;
-        advance(cw, cb);
-        // the previous block's accumulator out; its stage then takes the block S ahead
-        if (g >= 2 && epilogue(g - 2) && tid == 0 && pw < send) {
-            issue(pw, pb, issued);
-            issued++;
-            advance(pw, pb);
-        }
     }
-    if (!aborted && g >= 1 && !epilogue(g - 1)) aborted = true;
-    if (aborted && tid == 0) {   // bounded waits for the copies and MMAs still in flight
-        for (long long k = g; k < issued; k++) (void)bar_wait(full + (k % S), (unsigned)((k / S) & 1));
-        for (long long e = (g >= 2 ? g - 2 : 0); e < g; e++) (void)bar_wait(mdone + (e & 1), (unsigned)((e >> 1) & 1));
-    }
+    // every thread has passed the CTA barrier above (the producer then drained its copies)
     tc_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -482,9 +536,8 @@ int launch_pgemv_tc(int R, const SysDev* sys, const Strip* strips, long long sbe
         return gb_set_error(GB_UNSUPPORTED, "tensor-core pass: block size %d needs %u B of shared memory", B, L.total);
     const void* kfn = R == 4 ? reinterpret_cast<const void*>(k_pgemv_tc<4>) : reinterpret_cast<const void*>(k_pgemv_tc<8>);
     GB_CUDA_TRY(ensure_dynamic_smem(kfn, L.total));
-    int per_sm = 0;
-    GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kTcThreads, L.total));
-    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
+    // two CTAs per SM where their shared memory fits (228 KB per SM, 1 KB reserved per CTA)
+    const int per_sm = 2u * (L.total + 1024u) <= 228u * 1024u ? 2 : 1;
     const long long n = send - sbeg;
     const long long grid = n < (long long)sm_count() * per_sm ? n : (long long)sm_count() * per_sm;
     cudaLaunchConfig_t cfg = {};

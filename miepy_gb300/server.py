@@ -149,6 +149,7 @@ class SolveServer:
         self._wave_counter = 0
         self._closing = False
         self._free_streams = list(range(self.max_waves))
+        self._slot_class = {}
         self._streams = self._make_streams()
         # persistent workers: the native library keeps per-thread staging buffers
         # and capture streams, reused wave after wave
@@ -166,7 +167,12 @@ class SolveServer:
         return hbm_budget
 
     def _make_streams(self):
-        return [torch.cuda.Stream(device=self.device) for _ in range(self.max_waves)]
+        """Per wave slot a (normal, high-priority) pair of streams: waves of small
+        requests run on the high-priority one, so that their kernels are scheduled
+        ahead of a large wave's when both wait for SMs."""
+        lo, hi = torch.cuda.Stream.priority_range() if hasattr(torch.cuda.Stream, "priority_range") else (0, -1)
+        return [(torch.cuda.Stream(device=self.device, priority=lo),
+                 torch.cuda.Stream(device=self.device, priority=hi)) for _ in range(self.max_waves)]
 
     # --------------------------------------------------------------- client --
     def submit(self, req: ClusterRequest) -> cf.Future:
@@ -277,6 +283,7 @@ class SolveServer:
                 self.stats["admitted"] += len(wave)
                 self.stats["waves"] += 1
                 sidx = self._free_streams.pop()
+                self._slot_class[sidx] = cls
                 wid = self._wave_counter
                 self._wave_counter += 1
             self._pool.submit(self._run_wave, wave, used, sidx, wid, cls)
@@ -320,7 +327,8 @@ class SolveServer:
     def _execute(self, wave, sidx):
         """Solves one wave on its stream: one ragged ClusterBatch, assembled,
         solved and reduced; returns one ClusterResult per request."""
-        stream = self._streams[sidx]
+        normal, high = self._streams[sidx]
+        stream = high if self._slot_class.get(sidx, 1) == 0 else normal
         with torch.cuda.device(self.device), torch.cuda.stream(stream):
             specs = [request_spec(w[0]) for w in wave]
             b = ClusterBatch(specs, R=1, precision=self.precision, device=self.device)
