@@ -20,8 +20,7 @@ LIB = os.path.join(OUT, "libmiepy_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
-         "--split-compile=0"]   # the device code of one translation unit compiled on every core
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 
 
 def nvcc() -> str:

@@ -78,12 +78,14 @@ def far_expansions(dev, position, p_scat, k, pts, magnetic, hfac):
     d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
     L = lmax_from_rmax(np.asarray(p_scat).shape[-1])
     out = torch.empty((pts.shape[0], 3), dtype=torch.complex128, device=dev)
-    P = d(pts, torch.float64)
-    nat.check(nat.lib().gb_far_field_expansions(np.asarray(position).shape[0], L, nat.ptr(d(position, torch.float64)),
-                                                nat.ptr(d(p_scat, torch.complex128)), float(np.real(k)),
+    # every input stays referenced until the kernel has run
+    pos, ps, P = d(position, torch.float64), d(p_scat, torch.complex128), d(pts, torch.float64)
+    nat.check(nat.lib().gb_far_field_expansions(pos.shape[0], L, nat.ptr(pos), nat.ptr(ps), float(np.real(k)),
                                                 pts.shape[0], nat.ptr(P), int(bool(magnetic)), float(np.real(hfac)),
                                                 float(np.imag(hfac)), nat.ptr(out), current_stream(dev)), "far field")
-    return out.cpu().numpy()
+    res = out.cpu().numpy()
+    del pos, ps, P
+    return res
 
 
 def lmax_from_rmax(rmax):

@@ -2432,6 +2432,7 @@ bool prec_ok(int prec, const double* m128, const float* m64, const float* m64lo)
     }
 }
 
+#ifndef GB_SOLVE_MULTI_RHS   // (the R = 4 / 8 unit carries no scratch array)
 // ------------------------------------------- dense solve without allocation --
 // Scratch of gb_solve_dense_noalloc: a fixed device array that the library's module
 // brings with it, so that callers that must not allocate device memory (a server
@@ -2491,6 +2492,7 @@ int upload_plan_pageable(const Plan& P, unsigned char* base, const WS& w, cudaSt
     D.cnt = reinterpret_cast<int*>(dst + o_cnt);
     return GB_OK;
 }
+#endif
 
 // y = (I + T) x for FP64 vectors x, y.  prec: GB_PREC_FP64 (complex128 pass),
 // GB_PREC_MIXED (double-float pass), GB_PREC_FP32 (complex64 pass, or the
@@ -2558,6 +2560,11 @@ int apply_entry(int nsys, const gb_system* sys, int R, int prec, const double* m
                 const float* mat64lo, const void* mat_tc, const double* tvec, const double* x, double* y,
                 void* workspace, size_t ws_bytes, int reps, int repeat, cudaStream_t s) {
     if (R != 1 && R != 2 && R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "R must be 1, 2, 4 or 8 (got %d)", R);
+#ifndef GB_SOLVE_MULTI_RHS
+    if (R > 2)
+        return gb::apply_entry_multi(nsys, sys, R, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, workspace, ws_bytes,
+                                     reps, repeat, s);
+#endif
     if (prec == GB_PREC_MIXED_FP64RES) prec = GB_PREC_FP64;
     Plan P;
     int e = build_plan(nsys, sys, R, s, P);
@@ -2565,16 +2572,57 @@ int apply_entry(int nsys, const gb_system* sys, int R, int prec, const double* m
     WS w = ws_layout(P, prec, false);
     if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
     unsigned char* base = static_cast<unsigned char*>(workspace);
-    switch (R) {
-        case 1: return apply_impl<1>(P, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, base, w, reps, repeat, s);
-        case 2: return apply_impl<2>(P, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, base, w, reps, repeat, s);
-        case 4: return apply_impl<4>(P, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, base, w, reps, repeat, s);
-        default: return apply_impl<8>(P, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, base, w, reps, repeat, s);
-    }
+#ifndef GB_SOLVE_MULTI_RHS
+    if (R == 1) return apply_impl<1>(P, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, base, w, reps, repeat, s);
+    return apply_impl<2>(P, prec, mat128, mat64, mat64lo, nullptr, tvec, x, y, base, w, reps, repeat, s);
+#else
+    if (R == 4) return apply_impl<4>(P, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, base, w, reps, repeat, s);
+    return apply_impl<8>(P, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, base, w, reps, repeat, s);
+#endif
+}
+
+// Validation, plan and dispatch of a packed-operator solve (gb_solve_batch_tc).
+int solve_entry(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+                int max_refine, const double* mat128, const float* mat64, const float* mat64lo, const void* mat_tc,
+                const double* tvec, const double* b, double* x, void* workspace, size_t ws_bytes, int* status,
+                int* iters, double* resid, cudaStream_t s) {
+    if (nsys < 1 || !sys || !tvec || !b || !x || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
+    if (R != 1 && R != 2 && R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "R must be 1, 2, 4 or 8 (got %d)", R);
+    if (!prec_ok(prec, mat128, mat64, mat64lo))
+        return gb_set_error(GB_BAD_ARG, "precision %d is missing one of its matrices", prec);
+    if (mat_tc && (R < 4 || (prec != GB_PREC_FP32 && prec != GB_PREC_MIXED)))
+        return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass serves the FP32 and mixed methods with R = 4 or 8");
+    if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
+#ifndef GB_SOLVE_MULTI_RHS
+    if (R > 2)
+        return gb::solve_entry_multi(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo,
+                                     mat_tc, tvec, b, x, workspace, ws_bytes, status, iters, resid, s);
+#endif
+    Plan P;
+    int e = build_plan(nsys, sys, R, s, P);
+    if (e) return e;
+    WS w = ws_layout(P, prec, false);
+    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
+    unsigned char* base = static_cast<unsigned char*>(workspace);
+    if (inner_tol <= 0) inner_tol = 1e-6;
+#ifndef GB_SOLVE_MULTI_RHS
+    if (R == 1)
+        return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                             status, iters, resid, s);
+    return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                         status, iters, resid, s);
+#else
+    if (R == 4)
+        return solve_impl<4>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                             status, iters, resid, s, mat_tc);
+    return solve_impl<8>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
+                         status, iters, resid, s, mat_tc);
+#endif
 }
 
 }   // namespace
 
+#ifndef GB_SOLVE_MULTI_RHS
 extern "C" {
 
 size_t gb_solve_workspace_size(int nsys, const gb_system* sys, int R, int prec) {
@@ -2595,35 +2643,8 @@ int gb_solve_batch_tc(int nsys, const gb_system* sys, int R, int prec, double to
                       int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
                       const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
                       size_t ws_bytes, int* status, int* iters, double* resid, void* stream) {
-    if (nsys < 1 || !sys || !tvec || !b || !x || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
-    if (R != 1 && R != 2 && R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "R must be 1, 2, 4 or 8 (got %d)", R);
-    if (!prec_ok(prec, mat128, mat64, mat64lo))
-        return gb_set_error(GB_BAD_ARG, "precision %d is missing one of its matrices", prec);
-    if (mat_tc && (R < 4 || (prec != GB_PREC_FP32 && prec != GB_PREC_MIXED)))
-        return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass serves the FP32 and mixed methods with R = 4 or 8");
-    if (!(tol > 0) || maxiter < 1) return gb_set_error(GB_BAD_ARG, "tol must be > 0 and maxiter >= 1");
-    cudaStream_t s = (cudaStream_t)stream;
-    Plan P;
-    int e = build_plan(nsys, sys, R, s, P);
-    if (e) return e;
-    WS w = ws_layout(P, prec, false);
-    if (ws_bytes < w.total) return gb_set_error(GB_OVER_BUDGET, "workspace %zu B < required %zu B", ws_bytes, w.total);
-    unsigned char* base = static_cast<unsigned char*>(workspace);
-    if (inner_tol <= 0) inner_tol = 1e-6;
-    switch (R) {
-        case 1:
-            return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
-                                 w, status, iters, resid, s);
-        case 2:
-            return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
-                                 w, status, iters, resid, s);
-        case 4:
-            return solve_impl<4>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
-                                 w, status, iters, resid, s, mat_tc);
-        default:
-            return solve_impl<8>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base,
-                                 w, status, iters, resid, s, mat_tc);
-    }
+    return solve_entry(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, mat_tc, tvec,
+                       b, x, workspace, ws_bytes, status, iters, resid, (cudaStream_t)stream);
 }
 
 int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter,
@@ -2785,6 +2806,8 @@ int gb_set_gemv_wait_limit(long long cycles, long long* previous) {
     GB_CUDA_TRY(cudaMemcpyFromSymbol(&old, g_gemv_wait_cycles, sizeof(old)));
     const long long v = cycles < 0 ? kWaitCycles : cycles;
     GB_CUDA_TRY(cudaMemcpyToSymbol(g_gemv_wait_cycles, &v, sizeof(v)));
+    const int e = gb::set_wait_limit_multi(v);   // the copy of the R = 4 / 8 unit
+    if (e) return e;
     if (previous) *previous = old;
     return GB_OK;
 }
@@ -2871,3 +2894,29 @@ int gb_solve_dense_noalloc(int D, int R, const double* T, const double* b, doubl
 }
 
 }   // extern "C"
+#else   // GB_SOLVE_MULTI_RHS: the R = 4 and 8 instantiations, reached from the main unit
+
+namespace gb {
+
+int solve_entry_multi(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+                      int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
+                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
+                      size_t ws_bytes, int* status, int* iters, double* resid, cudaStream_t stream) {
+    return solve_entry(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, mat_tc, tvec,
+                       b, x, workspace, ws_bytes, status, iters, resid, stream);
+}
+
+int apply_entry_multi(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                      const float* mat64lo, const void* mat_tc, const double* tvec, const double* x, double* y,
+                      void* workspace, size_t ws_bytes, int reps, int repeat, cudaStream_t stream) {
+    return apply_entry(nsys, sys, R, prec, mat128, mat64, mat64lo, mat_tc, tvec, x, y, workspace, ws_bytes, reps,
+                       repeat, stream);
+}
+
+int set_wait_limit_multi(long long cycles) {
+    GB_CUDA_TRY(cudaMemcpyToSymbol(g_gemv_wait_cycles, &cycles, sizeof(cycles)));
+    return GB_OK;
+}
+
+}   // namespace gb
+#endif

@@ -57,4 +57,16 @@ int launch_pgemv_tc(int R, const SysDev* sys, const Strip* strips, long long sbe
                     int mask, const void* mat_tc, const void* Yu, const void* Yw, void* CU, void* CW,
                     const SysPlan* plan, int B, int* err, cudaStream_t stream);
 
+// The R = 4 and 8 solves, applies and wait limit, compiled in their own unit
+// (solve_multi.cu, which includes solve.cu with GB_SOLVE_MULTI_RHS defined) so that
+// the two halves of the solver compile in parallel.
+int solve_entry_multi(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+                      int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
+                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
+                      size_t ws_bytes, int* status, int* iters, double* resid, cudaStream_t stream);
+int apply_entry_multi(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
+                      const float* mat64lo, const void* mat_tc, const double* tvec, const double* x, double* y,
+                      void* workspace, size_t ws_bytes, int reps, int repeat, cudaStream_t stream);
+int set_wait_limit_multi(long long cycles);
+
 }   // namespace gb
