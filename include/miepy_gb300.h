@@ -155,9 +155,12 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
                    const double* tvec, const double* b, double* x, void* workspace, size_t ws_bytes, int* status,
                    int* iters, double* resid, void* stream);
 
-/* Multi-RHS blocks on the tensor cores (no counterpart in the reference, whose
- * solve_linear_system, cpp/src/interactions.cpp:347-368, takes one right-hand side
- * per call and multiplies with an Eigen/OpenMP GEMV, :70-92).  For R = 4 or 8
+/* gb_solve_batch with two options, each off when its pointer is NULL (both NULL
+ * gives gb_solve_batch).
+ *
+ * mat_tc: multi-RHS blocks on the tensor cores (no counterpart in the reference,
+ * whose solve_linear_system, cpp/src/interactions.cpp:347-368, takes one right-hand
+ * side per call and multiplies with an Eigen/OpenMP GEMV, :70-92).  For R = 4 or 8
  * right-hand sides (polarisations x incidence directions or sources) of clusters
  * with lmax <= 5, the matrix passes of the FP32 solves (GB_PREC_FP32, and the inner
  * solves of GB_PREC_MIXED) run as tcgen05 split-BF16x3 GEMMs with FP32
@@ -165,12 +168,44 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
  * gb_tc_matrix_build: one pass serves all R right-hand sides.  The product is
  * about 5e-6 accurate relative to its largest term (complex64 arithmetic: 4e-7);
  * the mixed method's refinement residuals stay on the CUDA-core passes, so its
- * result meets tol as with gb_solve_batch.  The workspace is gb_solve_workspace_size's.
- * mat_tc = NULL gives gb_solve_batch. */
-int gb_solve_batch_tc(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+ * result meets tol as with gb_solve_batch.
+ *
+ * pdiag: a diagonal right preconditioner M, complex128 [row] at each cluster's
+ * t_off like tvec (replaces solve_linear_system_preconditioned,
+ * cpp/src/interactions.cpp:321-345, with the sphere preconditioner of
+ * build_block_preconditioner_sphere, src/miepy/interactions.py:9-39: M =
+ * diag(1 / (1 + a_n)) of the Mie coefficients, 1 where |1 + a_n| < 1e-12; see
+ * gb_sphere_preconditioner).  Every BiCGSTAB of the solve is Eigen's
+ * right-preconditioned iteration (p^ = M p, v = (I + T) p^, x += alpha p^ + omega
+ * s^); the residual that decides convergence is the unpreconditioned one, so tol
+ * means the same as without M, and the mixed method's refinement residuals are the
+ * unpreconditioned b - (I + T) x.
+ *
+ * The workspace is gb_solve_workspace_size's. */
+int gb_solve_batch_ex(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
                       int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
-                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
-                      size_t ws_bytes, int* status, int* iters, double* resid, void* stream);
+                      const void* mat_tc, const double* pdiag, const double* tvec, const double* b, double* x,
+                      void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, void* stream);
+
+/* The sphere preconditioner of gb_solve_batch_ex: pdiag[e] = 1 / (1 + tvec[e]) over
+ * n entries of the Mie-factor arena (tvec from gb_expand_mie_batch), 1 where
+ * |1 + tvec[e]| < 1e-12 (build_block_preconditioner_sphere,
+ * src/miepy/interactions.py:9-39, whose blocks are diagonal: this is their
+ * diagonal, row by row). */
+int gb_sphere_preconditioner(long long n, const double* tvec, double* pdiag, void* stream);
+
+/* Block-diagonal right preconditioning of the dense solve (replaces
+ * solve_linear_system_preconditioned, cpp/src/interactions.cpp:321-345, with any
+ * M_inv_blocks, e.g. build_block_preconditioner_particle's inv(I + T_i),
+ * src/miepy/interactions.py:42-68).  Eigen's preconditioned BiCGSTAB on (I + T) is
+ * BiCGSTAB on (I + T) M for u, with x = M u and the same residuals; so
+ *   gb_dense_precondition_matrix: Tp = (I + T) M - I   (T, Tp [D][D] c128, Tp != T),
+ *   gb_solve_dense on Tp gives u,
+ *   gb_block_diag_apply: x = M u                      (u, x [D][R] c128, x != u),
+ * with Minv = M_inv_blocks [D][bs] c128 (block j in rows j bs .. j bs + bs - 1) and
+ * bs dividing D. */
+int gb_dense_precondition_matrix(int D, int bs, const double* T, const double* Minv, double* Tp, void* stream);
+int gb_block_diag_apply(int D, int R, int bs, const double* Minv, const double* u, double* x, void* stream);
 
 /* Bytes of the bf16 tile arena for a batch: per pair block 2 planes of Bp x Kp bf16
  * (Bp = B rounded up to 8, Kp = 2B rounded up to 16), clusters in batch order. */

@@ -54,8 +54,11 @@ SIGNATURES = {
     "gb_solve_workspace_size": (c_size_t, [c_int, _P, c_int, c_int]),
     "gb_solve_batch": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P, _P,
                                _P, c_size_t, _P, _P, _P, _P]),
-    "gb_solve_batch_tc": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P, _P,
-                                  _P, _P, c_size_t, _P, _P, _P, _P]),
+    "gb_solve_batch_ex": (c_int, [c_int, _P, c_int, c_int, c_double, c_int, c_double, c_int, _P, _P, _P, _P, _P, _P,
+                                  _P, _P, _P, c_size_t, _P, _P, _P, _P]),
+    "gb_sphere_preconditioner": (c_int, [ctypes.c_longlong, _P, _P, _P]),
+    "gb_dense_precondition_matrix": (c_int, [c_int, c_int, _P, _P, _P, _P]),
+    "gb_block_diag_apply": (c_int, [c_int, c_int, c_int, _P, _P, _P, _P]),
     "gb_tc_matrix_bytes": (c_size_t, [c_int, _P]),
     "gb_tc_matrix_build": (c_int, [c_int, _P, _P, _P, _P]),
     "gb_apply_repeat_tc": (c_int, [c_int, _P, c_int, _P, _P, _P, _P, _P, c_size_t, c_int, c_int, _P]),

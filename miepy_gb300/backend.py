@@ -213,34 +213,71 @@ def reflection_matrix_nia(positions, mie, k, reflected, z):
     return out.cpu().numpy().reshape(N, 2, rmax, N, 2, rmax)
 
 
-def solve_linear_system_jax(agg_tmatrix, p_src, method):
-    """Solve p_inc = (I + T)^-1 p_src; returns numpy [N, 2, rmax]."""
+def _block_diagonal(M_inv_blocks, block_size, D):
+    """The diagonal of M_inv_blocks [D, bs] when every block is diagonal, else None."""
+    M = np.asarray(M_inv_blocks, dtype=complex).reshape(D, block_size)
+    rows = np.arange(D)
+    diag = M[rows, rows % block_size]
+    off = M.copy()
+    off[rows, rows % block_size] = 0
+    return diag if not np.any(off) else None
+
+
+def solve_linear_system_jax(agg_tmatrix, p_src, method, M_inv_blocks=None, block_size=0):
+    """Solve p_inc = (I + T)^-1 p_src; returns numpy [N, 2, rmax].
+
+    M_inv_blocks / block_size (optional; the reference's CPU solve_linear_system
+    takes them, src/miepy/interactions.py:71-92, its GPU dispatch does not): a
+    block-diagonal right preconditioner [N * bs, bs] as built by
+    build_block_preconditioner_sphere / _particle (src/miepy/interactions.py:9-68).
+    A diagonal one (the sphere builder's) is folded into the packed solve; any other
+    runs the dense solve on (I + T) M."""
     require_cuda()
     p_src = np.asarray(p_src, dtype=complex)
     N, rmax = p_src.shape[0], p_src.shape[-1]
+    D = N * 2 * rmax
     tol = EXACT_TOL if _is_exact(method) else BICGSTAB_TOL
-    if isinstance(agg_tmatrix, DeviceAggregateTMatrix) and agg_tmatrix._host is None:
+    if M_inv_blocks is not None:
+        block_size = int(block_size)
+        if block_size < 1 or D % block_size or np.asarray(M_inv_blocks).size != D * block_size:
+            raise ValueError(f"M_inv_blocks must be [{D}, bs] with bs dividing {D}")
+    diag = _block_diagonal(M_inv_blocks, block_size, D) if M_inv_blocks is not None else None
+    if isinstance(agg_tmatrix, DeviceAggregateTMatrix) and agg_tmatrix._host is None and \
+            (M_inv_blocks is None or diag is not None):
         b = agg_tmatrix._batch
         b.b.copy_(torch.from_numpy(p_src.reshape(-1)).to(b.device))
-        b.solve(tol=tol, maxiter=1000)
+        pre = False
+        if diag is not None:   # rows of the packed solve are the reference's (i, a, r) order
+            pre = torch.from_numpy(np.ascontiguousarray(diag)).to(b.device)
+        b.solve(tol=tol, maxiter=1000, precondition=pre)
         return b.cluster_view(0, b.x)[..., 0].cpu().numpy()
     # a dense matrix supplied by the caller
-    D = N * 2 * rmax
     T = torch.as_tensor(np.ascontiguousarray(np.asarray(agg_tmatrix, dtype=complex).reshape(D, D)))
     dev = require_cuda()
     T = T.to(dev)
     bb = torch.from_numpy(np.ascontiguousarray(p_src.reshape(-1))).to(dev)
     x = torch.empty_like(bb)
     L = nat.lib()
+    st = current_stream(dev)
+    Minv = None
+    if M_inv_blocks is not None:
+        Minv = torch.from_numpy(np.ascontiguousarray(np.asarray(M_inv_blocks, dtype=complex).reshape(-1))).to(dev)
+        Tp = torch.empty_like(T)
+        nat.check(L.gb_dense_precondition_matrix(D, block_size, nat.ptr(T), nat.ptr(Minv), nat.ptr(Tp), st),
+                  "dense preconditioning")
+        T = Tp
     need = L.gb_solve_dense_workspace_size(D, 1)
     ws = torch.empty(need, dtype=torch.uint8, device=dev)
     status = np.zeros(1, np.int32)
     iters = np.zeros(1, np.int32)
     resid = np.zeros(1)
-    rc = L.gb_solve_dense(D, 1, nat.ptr(T), nat.ptr(bb), nat.ptr(x), tol, 1000, nat.ptr(ws), ws.numel(),
-                          status.ctypes.data, iters.ctypes.data, resid.ctypes.data, current_stream(dev))
+    u = torch.empty_like(bb) if Minv is not None else x
+    rc = L.gb_solve_dense(D, 1, nat.ptr(T), nat.ptr(bb), nat.ptr(u), tol, 1000, nat.ptr(ws), ws.numel(),
+                          status.ctypes.data, iters.ctypes.data, resid.ctypes.data, st)
     if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED):
         nat.check(rc, "dense solve")
+    if Minv is not None:
+        nat.check(L.gb_block_diag_apply(D, 1, block_size, nat.ptr(Minv), nat.ptr(u), nat.ptr(x), st), "x = M u")
     return x.cpu().numpy().reshape(N, 2, rmax)
 
 

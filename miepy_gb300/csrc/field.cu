@@ -86,18 +86,47 @@ __device__ void add_expansion(int L, const double2* __restrict__ c, int rmax, bo
             z[n] = make_double2(jn, yn);
         }
     } else {
+        // j_n of complex argument.  The upward recurrence (the reference's,
+        // cpp/src/special.cpp:20-45) multiplies its rounding errors by about
+        // |y_n / j_n| ~ ((2n-1)!!)^2 / |kr|^(2n+1) once n > |kr|, so it serves only
+        // |kr| >= NP; below that the values come from Miller's downward recurrence
+        // j_{n-1} = (2n+1)/kr j_n - j_{n+1}, started at n = NP + 24 from (j, j+1) =
+        // (1, 0) and normalised by j_0 = sin(kr)/kr or j_1 = j_0/kr - cos(kr)/kr,
+        // whichever is larger in modulus (they have no common zero).
         const double2 sz = csin(kr), cz = ccos(kr);
-        z[0] = cdivd(sz, kr);
-        if (NP > 1) {
-            double2 t = cdivd(z[0], kr);
-            double2 u = cdivd(cz, kr);
-            z[1] = make_double2(t.x - u.x, t.y - u.y);
-        }
+        const double2 e0 = cdivd(sz, kr);
+        const double2 t1 = cdivd(e0, kr), u1 = cdivd(cz, kr);
+        const double2 e1 = make_double2(t1.x - u1.x, t1.y - u1.y);
+        if (hypot(kr.x, kr.y) >= (double)NP) {
+            z[0] = e0;
+            if (NP > 1) z[1] = e1;
 #pragma unroll 1
-        for (int n = 2; n < NP; n++) {
-            double2 f = cdivd(make_double2(2.0 * n - 1, 0), kr);
-            double2 a = cmul(f, z[n - 1]);
-            z[n] = make_double2(a.x - z[n - 2].x, a.y - z[n - 2].y);
+            for (int n = 2; n < NP; n++) {
+                double2 f = cdivd(make_double2(2.0 * n - 1, 0), kr);
+                double2 a = cmul(f, z[n - 1]);
+                z[n] = make_double2(a.x - z[n - 2].x, a.y - z[n - 2].y);
+            }
+        } else {
+            double2 hi = make_double2(0.0, 0.0), cur = make_double2(1.0, 0.0);   // j_{n+1}, j_n (unscaled)
+#pragma unroll 1
+            for (int n = NP + 24; n >= 1; n--) {
+                const double2 f = cdivd(make_double2(2.0 * n + 1, 0), kr);
+                const double2 a = cmul(f, cur);
+                const double2 lo = make_double2(a.x - hi.x, a.y - hi.y);   // j_{n-1}
+                hi = cur;
+                cur = lo;
+                if (n - 1 < NP) z[n - 1] = lo;
+                if (fabs(cur.x) + fabs(cur.y) > 1e150) {   // keep the unnormalised values finite
+                    hi = make_double2(hi.x * 1e-150, hi.y * 1e-150);
+                    cur = make_double2(cur.x * 1e-150, cur.y * 1e-150);
+#pragma unroll 1
+                    for (int q = n - 1; q < NP; q++) z[q] = make_double2(z[q].x * 1e-150, z[q].y * 1e-150);
+                }
+            }
+            const bool use0 = !(NP > 1) || hypot(e0.x, e0.y) >= hypot(e1.x, e1.y);
+            const double2 s = use0 ? cdivd(e0, z[0]) : cdivd(e1, z[1]);
+#pragma unroll 1
+            for (int n = 0; n < NP; n++) z[n] = cmul(s, z[n]);
         }
     }
     // derivative z_n' = z_{n-1} - (n+1)/kr z_n, n >= 1

@@ -1162,7 +1162,7 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
              const SysPlan* __restrict__ plan, const long long* __restrict__ row_strip, const KState* __restrict__ st,
              int mask_mode, const OutT* __restrict__ CU, const OutT* __restrict__ CW, const VT* __restrict__ x,
              VT* __restrict__ y, int mode, const VT* __restrict__ aux, const double2* __restrict__ b128,
-             double2* __restrict__ dots, ScalarFuse fz) {
+             double2* __restrict__ dots, ScalarFuse fz, const double2* __restrict__ xscale) {
     const int it = blockIdx.x;
     if (it >= nitems) {
         pdl_wait();
@@ -1220,7 +1220,9 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
         const C tx = cadd(cflip(a, eneg), cflip(c, eneg ^ sneg));
         if (active_rhs<R>(st, I.sys, rr, mask_mode)) {
             const long long e = S.vec_off + (long long)(I.r0 + r) * R + rr;
-            C yv = cadd(to_c<C>(x[e]), tx);
+            C xe = to_c<C>(x[e]);
+            if (xscale) xe = cmul(xe, to_c<C>(xscale[S.t_off + I.r0 + r]));   // the identity's share of (I + T) D x
+            C yv = cadd(xe, tx);
             if (mode == 3) yv = csub(b128 ? to_c<C>(b128[e]) : to_c<C>(aux[e]), yv);
             const VT yo = from_c<VT>(yv);
             y[e] = yo;
@@ -1325,14 +1327,15 @@ k_reduce_dense(const gb::SysDev* __restrict__ sys, const Item* __restrict__ item
 // kind 0: init      x = 0, r = r0 = b, p = v = 0;     dots: |b|^2
 // kind 1: p-update  p = r + beta (p - omega v)
 // kind 2: s-update  s = r - alpha v
-// kind 3: x/r       x += alpha p + omega s; r = s - omega t;  dots: |r|^2, <r0, r>
+// kind 3: x/r       x += alpha p + omega s (times pdiag, when given); r = s - omega t;  dots: |r|^2, <r0, r>
 // kind 4: restart   r0 = r (r already b - A x)
 template <typename VT, int R>
 __global__ void __launch_bounds__(kVRows)
 k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int nitems, const KState* __restrict__ st,
       int kind, const double2* __restrict__ b, VT* __restrict__ bx, VT* __restrict__ x, VT* __restrict__ r,
       VT* __restrict__ r0, VT* __restrict__ p, VT* __restrict__ v, VT* __restrict__ s, const VT* __restrict__ t,
-      double2* __restrict__ dots, const SysPlan* __restrict__ plan = nullptr, ScalarFuse fz = ScalarFuse()) {
+      double2* __restrict__ dots, const SysPlan* __restrict__ plan = nullptr, ScalarFuse fz = ScalarFuse(),
+      const double2* __restrict__ pdiag = nullptr) {
     const int it = blockIdx.x;
     if (it >= nitems) {
         pdl_wait();
@@ -1379,7 +1382,9 @@ k_vec(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items, int ni
             } else if (kind == 3) {
                 const C pv = to_c<C>(p[e]), sv = to_c<C>(s[e]), tv = to_c<C>(t[e]), xv = to_c<C>(x[e]);
                 const C ap = cmul(ks_alpha(k, tg), pv), ws = cmul(ks_omega(k, tg), sv), wt = cmul(ks_omega(k, tg), tv);
-                x[e] = from_c<VT>(cadd(cadd(xv, ap), ws));
+                C dx = cadd(ap, ws);
+                if (pdiag) dx = cmul(dx, to_c<C>(pdiag[S.t_off + I.r0 + lr]));   // x += D (alpha p + omega s)
+                x[e] = from_c<VT>(cadd(xv, dx));
                 const VT rq = from_c<VT>(csub(sv, wt));
                 r[e] = rq;
                 const C rd = to_c<C>(rq), r0v = to_c<C>(r0[e]);
@@ -1573,7 +1578,7 @@ struct StripGroup {     // strips [beg, end) of clusters with block size B (one 
 
 struct Plan {
     int nsys = 0, R = 1, nv = 0, nr = 0;
-    long long nstrips = 0, total_pairs = 0, total_vec = 0, max_B = 0, cw_elems = 0, cu_elems = 0;
+    long long nstrips = 0, total_pairs = 0, total_vec = 0, total_t = 0, max_B = 0, cw_elems = 0, cu_elems = 0;
     bool tmat = false;   // general particles: y vectors from per-particle T-matrices (k_yprep_tmat)
     std::vector<StripGroup> groups;
     std::vector<gb::SysDev> sd;
@@ -1642,6 +1647,7 @@ int build_plan(int nsys, const gb_system* sys, int R, cudaStream_t stream, Plan&
         add_items(P.vitems, s, d.D, kVRows, pl.vbeg, pl.vend);
         add_items(P.ritems, s, d.D, d.B, pl.rbeg, pl.rend);   // one item per particle block
         P.total_vec = std::max<long long>(P.total_vec, d.vec_off + (long long)d.D * R);
+        P.total_t = std::max<long long>(P.total_t, d.t_off + (long long)d.D);
         P.max_B = std::max<long long>(P.max_B, d.B);
     }
     P.nstrips = (long long)P.strips.size();
@@ -1674,7 +1680,7 @@ void dense_plan(int D, int R, Plan& P) {
 
 struct WS {
     size_t off_state, off_ostate, off_dots, off_cu, off_cw, off_yu, off_yw, off_vec, off_tx, off_r128, off_r128b,
-        off_d128, off_blob, total;
+        off_d128, off_tp, off_blob, total;
 };
 
 WS ws_layout(const Plan& P, int prec, bool dense) {
@@ -1701,6 +1707,7 @@ WS ws_layout(const Plan& P, int prec, bool dense) {
     // mixed: the second residual buffer and the correction of the incremental update
     w.off_r128b = take(prec == GB_PREC_MIXED ? sizeof(double2) * (size_t)P.total_vec : 0);
     w.off_d128 = take(prec == GB_PREC_MIXED ? sizeof(double2) * (size_t)P.total_vec : 0);
+    w.off_tp = take(dense ? 0 : sizeof(double2) * (size_t)std::max<long long>(P.total_t, 1));   // t D (preconditioned)
     w.off_blob = take(sizeof(gb::SysDev) * P.nsys + sizeof(Strip) * P.nstrips + sizeof(Item) * (P.nv + P.nr) +
                       sizeof(SysPlan) * P.nsys + sizeof(long long) * P.row_strip.size() + sizeof(int) * P.nsys + 256);
     w.total = o;
@@ -1897,23 +1904,26 @@ int launch_pgemv_all(const Plan& P, const DevPlan& D, const KState* st, int mask
 template <int R>
 int launch_df(const Plan& P, const DevPlan& D, const KState* st, int mask, const void* hi, const void* lo,
               const void* Yu, const void* Yw, void* CU, void* CW, cudaStream_t stream) {
-    bool wide = false;
-    for (const StripGroup& grp : P.groups) wide |= pick_shape(grp.B).cpl >= 5;
-    if constexpr (R <= 2) {
-        if (R == 1 || !wide)
-            return launch_pgemv<PolDF, R, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
-    } else if (!wide) {
-        for (int rr = 0; rr < R; rr += 2) {
-            const int e = launch_pgemv<PolDF, 2, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
+    if constexpr (R == 1) {
+        return launch_pgemv<PolDF, 1, 1>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
+    } else {
+        bool wide = false;
+        for (const StripGroup& grp : P.groups) wide |= pick_shape(grp.B).cpl >= 5;
+        if (!wide) {
+            if constexpr (R == 2)
+                return launch_pgemv<PolDF, 2, 2>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, 0, D.err, stream);
+            for (int rr = 0; rr < R; rr += 2) {
+                const int e = launch_pgemv<PolDF, 2, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
+                if (e) return e;
+            }
+            return GB_OK;
+        }
+        for (int rr = 0; rr < R; rr++) {
+            const int e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
             if (e) return e;
         }
         return GB_OK;
     }
-    for (int rr = 0; rr < R; rr++) {
-        const int e = launch_pgemv<PolDF, 1, R>(P, D, st, mask, hi, lo, Yu, Yw, CU, CW, rr, D.err, stream);
-        if (e) return e;
-    }
-    return GB_OK;
 }
 
 // Tensor-core pass (gemv_tc.cu): one launch per block-size group.
@@ -1930,12 +1940,13 @@ int launch_pgemv_tcore(const Plan& P, const DevPlan& D, int R, const KState* st,
 
 // One product y = (I + T) x (mode 0), or the BiCGSTAB variants (modes 1-3), on the
 // packed matrices with arithmetic policy pol: 0 Pol64, 1 Pol32, 2 PolDF, 3 the
-// tensor-core pass (mat_hi = the bf16 tiles).
+// tensor-core pass (mat_hi = the bf16 tiles).  xscale (optional) scales the
+// identity's term per row: with tvec = t d and xscale = d the product is (I + T) D x.
 template <typename VT, int R>
 int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, const KState* st, int mask,
                  int pol, const void* mat_hi, const void* mat_lo, const double2* tvec, const VT* xin, VT* yout,
                  int mode, const VT* aux, const double2* b128, double2* dots, cudaStream_t stream,
-                 ScalarFuse fz = ScalarFuse(), YUpd<VT> up = YUpd<VT>()) {
+                 ScalarFuse fz = ScalarFuse(), YUpd<VT> up = YUpd<VT>(), const double2* xscale = nullptr) {
     void* Yu = base + w.off_yu;
     void* Yw = base + w.off_yw;
     void* CU = base + w.off_cu;
@@ -1956,7 +1967,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         gb::note_launch();
         GB_CUDA_TRY(launch_pdl(k_reduce_blk<double2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
                                D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const double2*>(CU),
-                               reinterpret_cast<const double2*>(CW), xin, yout, mode, aux, b128, dots, fz));
+                               reinterpret_cast<const double2*>(CW), xin, yout, mode, aux, b128, dots, fz, xscale));
     } else if (pol == 1) {
         gb::note_launch();
         if (P.tmat)
@@ -1971,7 +1982,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         gb::note_launch();
         GB_CUDA_TRY(launch_pdl(k_reduce_blk<float2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
                                D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float2*>(CU),
-                               reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz));
+                               reinterpret_cast<const float2*>(CW), xin, yout, mode, aux, b128, dots, fz, xscale));
     } else if (pol == 3) {   // tensor-core pass on the bf16 tiles (mat_hi): float2 y vectors and partials
         if constexpr (R == 4 || R == 8) {
             if (P.tmat) return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass serves sphere clusters");
@@ -1984,7 +1995,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             GB_CUDA_TRY(launch_pdl(k_reduce_blk<float2, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream,
                                    D.sys, D.ritems, P.nr, D.sp, D.row_strip, st, mask,
                                    reinterpret_cast<const float2*>(CU), reinterpret_cast<const float2*>(CW), xin, yout,
-                                   mode, aux, b128, dots, fz));
+                                   mode, aux, b128, dots, fz, xscale));
         } else {
             return gb_set_error(GB_UNSUPPORTED, "the tensor-core pass needs R = 4 or 8 (got %d)", R);
         }
@@ -2002,7 +2013,7 @@ int launch_apply(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         gb::note_launch();
         GB_CUDA_TRY(launch_pdl(k_reduce_blk<float4, VT, R>, dim3((unsigned)P.nr), dim3(kRBThreads), 0, stream, D.sys,
                                D.ritems, P.nr, D.sp, D.row_strip, st, mask, reinterpret_cast<const float4*>(CU),
-                               reinterpret_cast<const float4*>(CW), xin, yout, mode, aux, b128, dots, fz));
+                               reinterpret_cast<const float4*>(CW), xin, yout, mode, aux, b128, dots, fz, xscale));
     }
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
@@ -2083,10 +2094,15 @@ cudaStream_t capture_stream() {
 // Runs BiCGSTAB on vectors of type VT (double2 with pol 0 or dense, float2 with
 // pol 1) until every (cluster, rhs) is done.  The right-hand side is b128 (FP64) or,
 // when null, bvt.  The solution stays in the x vector of the workspace.
+// pdiag (packed path, optional): a diagonal right preconditioner D (one complex
+// factor per row, at t_off like tvec), and tvec_p = tvec * D: the iteration's
+// products are (I + T) D p = D p + A diag(t D) p, x is updated by D (alpha p + omega
+// s) (Eigen's BiCGSTAB with a preconditioner); restart residuals use (I + T) itself.
 template <typename VT, int R, bool DENSE>
 int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* base, int pol, const void* mat,
                  const double2* tvec, const double2* b128, VT* bvt, double tol, int maxiter, KState* st, int dense_D,
-                 cudaStream_t stream, bool use_graph) {
+                 cudaStream_t stream, bool use_graph, const double2* pdiag = nullptr,
+                 const double2* tvec_p = nullptr) {
     static_assert(!DENSE || std::is_same<VT, double2>::value, "the dense path runs FP64 vectors");
     const size_t TV = (size_t)P.total_vec;
     VT* V = reinterpret_cast<VT*>(base + w.off_vec);
@@ -2121,8 +2137,9 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
             GB_CUDA_TRY(cudaGetLastError());
             return GB_OK;
         }
-        return launch_apply<VT, R>(P, D, w, base, st, mask, pol, mat, nullptr, tvec, xin, yout, mode, aux, bb, dots, sm,
-                                   fz, up);
+        const bool pre = pdiag && mode != 3;   // the restart residual is b - (I + T) x
+        return launch_apply<VT, R>(P, D, w, base, st, mask, pol, mat, nullptr, pre ? tvec_p : tvec, xin, yout, mode,
+                                   aux, bb, dots, sm, fz, up, pre ? pdiag : nullptr);
     };
     // One iteration: p-update + v = A p (+ alpha), s-update + t = A s (+ omega),
     // x/r update (+ convergence, beta).  On the packed path the vector updates run
@@ -2154,7 +2171,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
         }
         gb::note_launch();
         GB_CUDA_TRY(launch_pdl(k_vec<VT, R>, dim3(vb), dim3(kVRows), 0, sm, D.sys, D.vitems, P.nv, st, 3, nullptr,
-                               nullptr, x, r, r0, p, v, s, t, dots, D.sp, fuse(3)));
+                               nullptr, x, r, r0, p, v, s, t, dots, D.sp, fuse(3), pdiag));
         GB_CUDA_TRY(cudaGetLastError());
         return GB_OK;
     };
@@ -2170,7 +2187,7 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
     // solve), captured once per argument set and replayed
     auto acquire = [&](int nit, GraphUse& use, cudaGraphExec_t& exec, long long& exec_kernels) -> int {
         GraphKey key{};
-        const void* a[12] = {base, mat, tvec, D.sys, D.strips, D.vitems, D.ritems, D.sp, st, nullptr, nullptr, nullptr};
+        const void* a[12] = {base, mat, tvec, D.sys, D.strips, D.vitems, D.ritems, D.sp, st, pdiag, tvec_p, nullptr};
         memcpy(key.a, a, sizeof(a));
         key.n[0] = P.nsys;
         key.n[1] = R | (pol << 8) | ((DENSE ? 1 : 0) << 16) | ((long long)sizeof(VT) << 24) | ((long long)P.tmat << 40);
@@ -2324,6 +2341,15 @@ int read_state(const DevPlan& D, const KState* dev, int nsr, std::vector<KState>
     return GB_OK;
 }
 
+// out[e] = t[e] d[e] over the Mie-factor arena (the preconditioned products' factors)
+__global__ void k_scale_t(const double2* __restrict__ t, const double2* __restrict__ d, double2* __restrict__ out,
+                          long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        out[e] = cmul(t[e], d[e]);
+}
+
+// pdiag (optional): the diagonal right preconditioner of run_bicgstab for every
+// BiCGSTAB of the solve (the mixed method's refinement residuals stay unpreconditioned).
 // mat_tc (optional, R = 4 or 8): the bf16 tiles of the tensor-core pass, used for
 // the products of the FP32 solves (the FP32 method, and the inner solves of the
 // mixed method); the refinement residuals keep the CUDA-core passes.
@@ -2331,12 +2357,21 @@ template <int R>
 int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_tol, int max_refine,
                const double* mat128, const float* mat64, const float* mat64lo, const double* tvec, const double* b,
                double* x, unsigned char* base, const WS& w, int* status, int* iters, double* resid,
-               cudaStream_t stream, const void* mat_tc = nullptr) {
+               cudaStream_t stream, const void* mat_tc = nullptr, const double* pdiag = nullptr) {
     const int pol32 = mat_tc ? 3 : 1;
     const void* m32 = mat_tc ? mat_tc : static_cast<const void*>(mat64);
     DevPlan D;
     int e = upload_plan(P, base, w, stream, D);
     if (e) return e;
+    const double2* pd = reinterpret_cast<const double2*>(pdiag);
+    double2* tp = nullptr;
+    if (pd) {
+        tp = reinterpret_cast<double2*>(base + w.off_tp);
+        gb::note_launch();
+        k_scale_t<<<(unsigned)std::min<long long>((P.total_t + 255) / 256, 4096), 256, 0, stream>>>(
+            reinterpret_cast<const double2*>(tvec), pd, tp, P.total_t);
+        GB_CUDA_TRY(cudaGetLastError());
+    }
     KState* st = reinterpret_cast<KState*>(base + w.off_state);
     KState* ost = reinterpret_cast<KState*>(base + w.off_ostate);
     const double2* t2 = reinterpret_cast<const double2*>(tvec);
@@ -2347,7 +2382,8 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
     const unsigned vb = (unsigned)P.nv;
     std::vector<KState> h;
     if (prec == GB_PREC_FP64) {
-        e = run_bicgstab<double2, R, false>(P, D, w, base, 0, mat128, t2, b2, nullptr, tol, maxiter, st, 0, stream, true);
+        e = run_bicgstab<double2, R, false>(P, D, w, base, 0, mat128, t2, b2, nullptr, tol, maxiter, st, 0, stream, true,
+                                            pd, tp);
         if (e) return e;
         gb::note_launch();
         k_copy_out<double2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R,
@@ -2361,7 +2397,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
     float2* bx = V + 7 * TV;
     if (prec == GB_PREC_FP32) {
         e = run_bicgstab<float2, R, false>(P, D, w, base, pol32, m32, t2, b2, nullptr, tol, maxiter, st, 0, stream,
-                                           true);
+                                           true, pd, tp);
         if (e) return e;
         gb::note_launch();
         k_copy_out<float2><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, V, x2);
@@ -2389,7 +2425,7 @@ int solve_impl(const Plan& P, int prec, double tol, int maxiter, double inner_to
         k_cast_f<<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, R, r128, bx, ost);
         GB_CUDA_TRY(cudaGetLastError());
         e = run_bicgstab<float2, R, false>(P, D, w, base, pol32, m32, t2, nullptr, bx, inner_tol, maxiter, st, 0,
-                                           stream, true);
+                                           stream, true, pd, tp);
         if (e) return e;
         gb::note_launch();
         k_refine_axpy<R><<<vb, kVRows, 0, stream>>>(D.sys, D.vitems, P.nv, ost, x2, V, incr ? d128 : nullptr);
@@ -2581,11 +2617,11 @@ int apply_entry(int nsys, const gb_system* sys, int R, int prec, const double* m
 #endif
 }
 
-// Validation, plan and dispatch of a packed-operator solve (gb_solve_batch_tc).
+// Validation, plan and dispatch of a packed-operator solve (gb_solve_batch_ex).
 int solve_entry(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
                 int max_refine, const double* mat128, const float* mat64, const float* mat64lo, const void* mat_tc,
-                const double* tvec, const double* b, double* x, void* workspace, size_t ws_bytes, int* status,
-                int* iters, double* resid, cudaStream_t s) {
+                const double* pdiag, const double* tvec, const double* b, double* x, void* workspace, size_t ws_bytes,
+                int* status, int* iters, double* resid, cudaStream_t s) {
     if (nsys < 1 || !sys || !tvec || !b || !x || !workspace) return gb_set_error(GB_BAD_ARG, "null argument");
     if (R != 1 && R != 2 && R != 4 && R != 8) return gb_set_error(GB_UNSUPPORTED, "R must be 1, 2, 4 or 8 (got %d)", R);
     if (!prec_ok(prec, mat128, mat64, mat64lo))
@@ -2596,7 +2632,7 @@ int solve_entry(int nsys, const gb_system* sys, int R, int prec, double tol, int
 #ifndef GB_SOLVE_MULTI_RHS
     if (R > 2)
         return gb::solve_entry_multi(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo,
-                                     mat_tc, tvec, b, x, workspace, ws_bytes, status, iters, resid, s);
+                                     mat_tc, pdiag, tvec, b, x, workspace, ws_bytes, status, iters, resid, s);
 #endif
     Plan P;
     int e = build_plan(nsys, sys, R, s, P);
@@ -2608,15 +2644,15 @@ int solve_entry(int nsys, const gb_system* sys, int R, int prec, double tol, int
 #ifndef GB_SOLVE_MULTI_RHS
     if (R == 1)
         return solve_impl<1>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
-                             status, iters, resid, s);
+                             status, iters, resid, s, nullptr, pdiag);
     return solve_impl<2>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
-                         status, iters, resid, s);
+                         status, iters, resid, s, nullptr, pdiag);
 #else
     if (R == 4)
         return solve_impl<4>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
-                             status, iters, resid, s, mat_tc);
+                             status, iters, resid, s, mat_tc, pdiag);
     return solve_impl<8>(P, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, tvec, b, x, base, w,
-                         status, iters, resid, s, mat_tc);
+                         status, iters, resid, s, mat_tc, pdiag);
 #endif
 }
 
@@ -2635,16 +2671,16 @@ int gb_solve_batch(int nsys, const gb_system* sys, int R, int prec, double tol, 
                    int max_refine, const double* mat128, const float* mat64, const float* mat64lo, const double* tvec,
                    const double* b, double* x, void* workspace, size_t ws_bytes, int* status, int* iters,
                    double* resid, void* stream) {
-    return gb_solve_batch_tc(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, nullptr,
-                             tvec, b, x, workspace, ws_bytes, status, iters, resid, stream);
+    return gb_solve_batch_ex(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, nullptr,
+                             nullptr, tvec, b, x, workspace, ws_bytes, status, iters, resid, stream);
 }
 
-int gb_solve_batch_tc(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
+int gb_solve_batch_ex(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
                       int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
-                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
-                      size_t ws_bytes, int* status, int* iters, double* resid, void* stream) {
-    return solve_entry(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, mat_tc, tvec,
-                       b, x, workspace, ws_bytes, status, iters, resid, (cudaStream_t)stream);
+                      const void* mat_tc, const double* pdiag, const double* tvec, const double* b, double* x,
+                      void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, void* stream) {
+    return solve_entry(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, mat_tc, pdiag,
+                       tvec, b, x, workspace, ws_bytes, status, iters, resid, (cudaStream_t)stream);
 }
 
 int gb_solve_batch_tmatrix(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter,
@@ -2900,10 +2936,10 @@ namespace gb {
 
 int solve_entry_multi(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
                       int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
-                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
-                      size_t ws_bytes, int* status, int* iters, double* resid, cudaStream_t stream) {
-    return solve_entry(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, mat_tc, tvec,
-                       b, x, workspace, ws_bytes, status, iters, resid, stream);
+                      const void* mat_tc, const double* pdiag, const double* tvec, const double* b, double* x,
+                      void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, cudaStream_t stream) {
+    return solve_entry(nsys, sys, R, prec, tol, maxiter, inner_tol, max_refine, mat128, mat64, mat64lo, mat_tc, pdiag,
+                       tvec, b, x, workspace, ws_bytes, status, iters, resid, stream);
 }
 
 int apply_entry_multi(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,

@@ -62,8 +62,8 @@ int launch_pgemv_tc(int R, const SysDev* sys, const Strip* strips, long long sbe
 // the two halves of the solver compile in parallel.
 int solve_entry_multi(int nsys, const gb_system* sys, int R, int prec, double tol, int maxiter, double inner_tol,
                       int max_refine, const double* mat128, const float* mat64, const float* mat64lo,
-                      const void* mat_tc, const double* tvec, const double* b, double* x, void* workspace,
-                      size_t ws_bytes, int* status, int* iters, double* resid, cudaStream_t stream);
+                      const void* mat_tc, const double* pdiag, const double* tvec, const double* b, double* x,
+                      void* workspace, size_t ws_bytes, int* status, int* iters, double* resid, cudaStream_t stream);
 int apply_entry_multi(int nsys, const gb_system* sys, int R, int prec, const double* mat128, const float* mat64,
                       const float* mat64lo, const void* mat_tc, const double* tvec, const double* x, double* y,
                       void* workspace, size_t ws_bytes, int reps, int repeat, cudaStream_t stream);

@@ -252,7 +252,14 @@ class ClusterBatch:
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
         return self._ws
 
-    def solve(self, tol=1e-5, maxiter=1000, inner_tol=1e-4, max_refine=8, precision=None, raise_on_fail=False):
+    def solve(self, tol=1e-5, maxiter=1000, inner_tol=1e-4, max_refine=8, precision=None, raise_on_fail=False,
+              precondition=False):
+        """Solve every cluster and right-hand side.  precondition=True runs the
+        BiCGSTAB iterations right-preconditioned by diag(1 / (1 + a_n)) of the Mie
+        coefficients (the reference's build_block_preconditioner_sphere,
+        src/miepy/interactions.py:9-39, inside solve_linear_system_preconditioned,
+        cpp/src/interactions.cpp:321-345); a device complex128 tensor gives the
+        diagonal itself (rows at the clusters' t offsets).  Sphere clusters only."""
         if not self.assembled:
             self.assemble()
         precision = precision or self.precision
@@ -264,6 +271,8 @@ class ClusterBatch:
         iters = np.zeros(n, dtype=np.int32)
         resid = np.zeros(n, dtype=np.float64)
         if self.tmatrix:
+            if precondition is not False and precondition is not None:
+                raise ValueError("precondition serves sphere clusters (the diagonal of the Mie coefficients)")
             rc = L.gb_solve_batch_tmatrix(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
                                           int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64),
                                           nat.ptr(self.mat64lo), nat.ptr(self.tmat128), nat.ptr(self.tmat64),
@@ -272,15 +281,31 @@ class ClusterBatch:
                                           current_stream(self.device))
         else:
             tc = self.mat_tc if precision in ("fp32", "mixed") else None
-            rc = L.gb_solve_batch_tc(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
+            if isinstance(precondition, torch.Tensor):
+                if precondition.dtype != torch.complex128 or precondition.numel() < self.totals["t"] or \
+                        precondition.device != self.x.device:
+                    raise ValueError("a given preconditioner is a device complex128 [rows] array at the t offsets")
+                pd = precondition
+            else:
+                pd = self._preconditioner() if precondition else None
+            rc = L.gb_solve_batch_ex(self.nsys, self.sys, self.R, code, float(tol), int(maxiter), float(inner_tol),
                                      int(max_refine), nat.ptr(self.mat128), nat.ptr(self.mat64),
-                                     nat.ptr(self.mat64lo), nat.ptr(tc), nat.ptr(self.tvec), nat.ptr(self.b),
-                                     nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data, iters.ctypes.data,
-                                     resid.ctypes.data, current_stream(self.device))
+                                     nat.ptr(self.mat64lo), nat.ptr(tc), nat.ptr(pd), nat.ptr(self.tvec),
+                                     nat.ptr(self.b), nat.ptr(self.x), nat.ptr(ws), ws.numel(), status.ctypes.data,
+                                     iters.ctypes.data, resid.ctypes.data, current_stream(self.device))
         if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN) or (raise_on_fail and rc):
             nat.check(rc, "solve")
         self.status, self.iters, self.resid = status, iters, resid
         return status
+
+    def _preconditioner(self):
+        """diag(1 / (1 + a_n)) per row at the clusters' t_off, from tvec (current
+        after every assemble)."""
+        if getattr(self, "pdiag", None) is None:
+            self.pdiag = torch.empty_like(self.tvec)
+        nat.check(nat.lib().gb_sphere_preconditioner(int(self.totals["t"]), nat.ptr(self.tvec), nat.ptr(self.pdiag),
+                                                      current_stream(self.device)), "sphere preconditioner")
+        return self.pdiag
 
     def apply(self, x, precision="fp64"):
         """y = (I + T) x on the packed matrices (x: device complex128 [total_vec]);

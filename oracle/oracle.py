@@ -78,6 +78,8 @@ def _declare(L):
         "orc_sphere_aggregate_tmatrix_periodic": (None, [c_int, c_int, _D, _D, c_double, c_int, _D, _D, _D]),
         "orc_solve_linear_system": (c_int, [c_int, _D, _D, c_int, c_double, c_int, _D, _D]),
         "orc_bicgstab_plain": (c_int, [c_int, _D, _D, c_int, c_double, _D, _D]),
+        "orc_solve_linear_system_precond": (c_int, [c_int, _D, _D, c_int, _D, c_int, c_double, c_int, _D, _D]),
+        "orc_bicgstab_precond": (c_int, [c_int, _D, _D, _D, c_int, c_int, c_double, _D, _D]),
         "orc_gemv": (None, [c_int, _D, _D, _D]),
         "orc_particle_cross_sections": (None, [c_int, _D, _D, _D, c_double, _D]),
         "orc_cluster_cross_sections": (None, [c_int, _D, _D, c_double, _D]),
@@ -380,6 +382,70 @@ def bicgstab(A, b, maxiter=1000, tolerance=1e-5):
     err = ctypes.c_double(0.0)
     it = lib().orc_bicgstab_plain(D, _dp(A.view(np.float64)), _dp(b.view(np.float64)), int(maxiter),
                                   float(tolerance), _dp(x.view(np.float64)), ctypes.byref(err))
+    return x, it, err.value
+
+
+def build_block_preconditioner_sphere(mie_scat, lmax):
+    """(M_inv_blocks [N*bs, bs], bs) with the diagonal 1 / (1 + a_n), 1 where
+    |1 + a_n| < 1e-12 (src/miepy/interactions.py:9-39)."""
+    mie = np.asarray(mie_scat, dtype=complex).reshape(-1, 2, lmax)
+    N = mie.shape[0]
+    rmax = lmax * (lmax + 2)
+    bs = 2 * rmax
+    M = np.zeros((N * bs, bs), dtype=complex)
+    ns = np.concatenate([np.full(2 * n + 1, n) for n in range(1, lmax + 1)])
+    for i in range(N):
+        for a in range(2):
+            for r in range(rmax):
+                val = 1.0 + mie[i, a, ns[r] - 1]
+                M[i * bs + a * rmax + r, a * rmax + r] = 1.0 if abs(val) < 1e-12 else 1.0 / val
+    return M, bs
+
+
+def build_block_preconditioner_particle(tmatrix):
+    """(M_inv_blocks, bs) with blocks inv(I + T_i), identity where singular
+    (src/miepy/interactions.py:42-68)."""
+    tm = np.asarray(tmatrix, dtype=complex)
+    N, bs = tm.shape[0], 2 * tm.shape[-1]
+    M = np.zeros((N * bs, bs), dtype=complex)
+    for i in range(N):
+        try:
+            M[i * bs:(i + 1) * bs] = np.linalg.inv(np.eye(bs) + tm[i].reshape(bs, bs))
+        except np.linalg.LinAlgError:
+            M[i * bs:(i + 1) * bs] = np.eye(bs)
+    return M, bs
+
+
+def solve_linear_system_precond(T, b, M_inv_blocks, block_size, method="bicgstab", tol=1e-5, maxiter=1000):
+    """(I + T) x = b with Eigen's BiCGSTAB right-preconditioned by M_inv_blocks.
+    Returns (x, iterations, relative residual)."""
+    T = _c128(T)
+    D = int(round(np.sqrt(T.size)))
+    b = _c128(b).reshape(D)
+    M = _c128(M_inv_blocks).reshape(D, block_size)
+    x = np.empty(D, dtype=np.complex128)
+    err = ctypes.c_double(0.0)
+    meth = 1 if (getattr(method, "name", method) == "exact" or method == 1) else 0
+    it = lib().orc_solve_linear_system_precond(D, _dp(T.view(np.float64)), _dp(b.view(np.float64)), meth,
+                                               _dp(M.view(np.float64)), int(block_size), float(tol), int(maxiter),
+                                               _dp(x.view(np.float64)), ctypes.byref(err))
+    if it < 0:
+        raise np.linalg.LinAlgError("singular interaction matrix")
+    return x, it, err.value
+
+
+def bicgstab_preconditioned(A, b, M_inv_blocks, block_size, maxiter=1000, tolerance=1e-5):
+    """The reference's bicgstab_preconditioned_profiled (x0 = b, absolute tolerance).
+    A includes the identity.  Returns (x, iters, residual)."""
+    A = _c128(A)
+    D = A.shape[0]
+    b = _c128(b).reshape(D)
+    M = _c128(M_inv_blocks).reshape(D, block_size)
+    x = np.empty(D, dtype=np.complex128)
+    err = ctypes.c_double(0.0)
+    it = lib().orc_bicgstab_precond(D, _dp(A.view(np.float64)), _dp(b.view(np.float64)), _dp(M.view(np.float64)),
+                                    int(block_size), int(maxiter), float(tolerance), _dp(x.view(np.float64)),
+                                    ctypes.byref(err))
     return x, it, err.value
 
 

@@ -506,10 +506,24 @@ double sqnorm(const std::vector<cd>& a) {
     return s;
 }
 
-// Eigen-style BiCGSTAB with identity preconditioner (called from
-// cpp/src/interactions.cpp:359-366): x0 = 0, stop when |r|^2 <= tol^2 |b|^2.
-int bicgstab_eigen(const cd* A, int D, const cd* b, cd* xout, double tol, int maxit, double* err_out) {
-    std::vector<cd> x(D, 0.0), r(b, b + D), r0(r), v(D, 0.0), p(D, 0.0), s(D), t(D);
+// y = M x for a block-diagonal M given as M_inv_blocks [D][bs]
+// (apply_block_preconditioner, cpp/src/interactions.cpp:211-228).
+void block_apply(const cd* M, int bs, int D, const std::vector<cd>& x, std::vector<cd>& y) {
+    for (int j0 = 0; j0 < D; j0 += bs)
+        for (int r = 0; r < bs; r++) {
+            cd acc = 0;
+            for (int k = 0; k < bs; k++) acc += M[size_t(j0 + r) * bs + k] * x[j0 + k];
+            y[j0 + r] = acc;
+        }
+}
+
+// Eigen-style BiCGSTAB (called from cpp/src/interactions.cpp:359-366 with the
+// identity preconditioner, and from :335-341 with the block-diagonal one, M given):
+// x0 = 0, stop when |r|^2 <= tol^2 |b|^2; with M the products are A (M p) and
+// A (M s) and x moves by alpha M p + omega M s.
+int bicgstab_eigen(const cd* A, int D, const cd* b, cd* xout, double tol, int maxit, double* err_out,
+                   const cd* M = nullptr, int bs = 0) {
+    std::vector<cd> x(D, 0.0), r(b, b + D), r0(r), v(D, 0.0), p(D, 0.0), s(D), t(D), y(D), z(D);
     double r0sq = sqnorm(r0), bsq = sqnorm(r);
     if (bsq == 0) {
         std::fill(xout, xout + D, cd(0));
@@ -532,14 +546,16 @@ int bicgstab_eigen(const cd* A, int D, const cd* b, cd* xout, double tol, int ma
         }
         cd beta = (rho / rho_old) * (alpha / w);
         for (int e = 0; e < D; e++) p[e] = r[e] + beta * (p[e] - w * v[e]);
-        gemv(A, D, p.data(), v.data());
+        if (M) block_apply(M, bs, D, p, y); else y = p;
+        gemv(A, D, y.data(), v.data());
         alpha = rho / dotc(r0, v);
         for (int e = 0; e < D; e++) s[e] = r[e] - alpha * v[e];
-        gemv(A, D, s.data(), t.data());
+        if (M) block_apply(M, bs, D, s, z); else z = s;
+        gemv(A, D, z.data(), t.data());
         double tmp = sqnorm(t);
         w = tmp > 0 ? dotc(t, s) / tmp : cd(0);
         for (int e = 0; e < D; e++) {
-            x[e] += alpha * p[e] + w * s[e];
+            x[e] += alpha * y[e] + w * z[e];
             r[e] = s[e] - w * t[e];
         }
         ++i;
@@ -970,6 +986,59 @@ int orc_solve_linear_system(int D, const double* T, const double* b, int method,
     }
     return bicgstab_eigen(A.data(), D, reinterpret_cast<const cd*>(b), reinterpret_cast<cd*>(x), tol, maxiter,
                           err_out);
+}
+
+// solve_linear_system_preconditioned: cpp/src/interactions.cpp:321-345 (the exact
+// branch ignores M).  Minv = M_inv_blocks [D][bs].
+int orc_solve_linear_system_precond(int D, const double* T, const double* b, int method, const double* Minv, int bs,
+                                    double tol, int maxiter, double* x, double* err_out) {
+    if (method == 1) return orc_solve_linear_system(D, T, b, method, tol, maxiter, x, err_out);
+    std::vector<cd> A(size_t(D) * D);
+    const cd* Tc = reinterpret_cast<const cd*>(T);
+#pragma omp parallel for schedule(static)
+    for (long e = 0; e < long(D) * D; e++) A[e] = Tc[e];
+    for (int i = 0; i < D; i++) A[size_t(i) * D + i] += 1.0;
+    return bicgstab_eigen(A.data(), D, reinterpret_cast<const cd*>(b), reinterpret_cast<cd*>(x), tol, maxiter,
+                          err_out, reinterpret_cast<const cd*>(Minv), bs);
+}
+
+// bicgstab_preconditioned_profiled (x0 = b, absolute |r| < tol):
+// cpp/src/interactions.cpp:230-290.  A includes the identity.
+int orc_bicgstab_precond(int D, const double* Aflat, const double* bflat, const double* Minv, int bs, int maxiter,
+                         double tol, double* xflat, double* err_out) {
+    const cd* A = reinterpret_cast<const cd*>(Aflat);
+    const cd* b = reinterpret_cast<const cd*>(bflat);
+    const cd* M = reinterpret_cast<const cd*>(Minv);
+    std::vector<cd> x(b, b + D), Ax(D), r(D);
+    gemv(A, D, x.data(), Ax.data());
+    for (int e = 0; e < D; e++) r[e] = b[e] - Ax[e];
+    double err = std::sqrt(sqnorm(r));
+    int it = 0;
+    if (err >= tol) {
+        std::vector<cd> rh(r), v(D, 0.0), p(D, 0.0), ph(D), vi(D), s(D), sh(D), t(D);
+        cd rho_prev = 1, alpha = 1, w_prev = 1;
+        it = 1;
+        while (true) {
+            cd rho = dotc(rh, r);
+            cd beta = (rho / rho_prev) * (alpha / w_prev);
+            for (int e = 0; e < D; e++) p[e] = r[e] + beta * (p[e] - w_prev * v[e]);
+            block_apply(M, bs, D, p, ph);
+            gemv(A, D, ph.data(), vi.data());
+            alpha = rho / dotc(rh, vi);
+            for (int e = 0; e < D; e++) s[e] = r[e] - alpha * vi[e];
+            block_apply(M, bs, D, s, sh);
+            gemv(A, D, sh.data(), t.data());
+            cd w = dotc(t, s) / dotc(t, t);
+            for (int e = 0; e < D; e++) { x[e] += alpha * ph[e] + w * sh[e]; r[e] = s[e] - w * t[e]; }
+            err = std::sqrt(sqnorm(r));
+            if (err < tol || it > maxiter) break;
+            rho_prev = rho; v = vi; w_prev = w;
+            it++;
+        }
+    }
+    if (err_out) *err_out = err;
+    std::memcpy(xflat, x.data(), sizeof(cd) * D);
+    return it;
 }
 
 // interactions.bicgstab (hand-written variant, x0 = b): cpp/src/interactions.cpp:98-150.

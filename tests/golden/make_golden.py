@@ -6,9 +6,11 @@ inputs and outputs of the sphere-cluster path as small ``.npz`` files.  The GPU
 parity tests compare the product against these fixtures without needing the
 reference tree at run time.
 
-Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large | fields | beams]
+Usage:  MIEPY_REFERENCE_SRC=/root/reference/src python tests/golden/make_golden.py [large | fields | beams | interior]
         (or with the reference staged by oracle/stage_reference.py:
-         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large | fields | beams])
+         MIEPY_REFERENCE_SRC=baseline/_ref/src python tests/golden/make_golden.py [large | fields | beams | interior])
+        MIEPY_REFERENCE_SRC=... python tests/golden/make_golden.py precond \
+            /root/reference/benchmarks/results/final_performance_branch.json
 """
 
 import os
@@ -475,8 +477,134 @@ def fields_main():
     print("wrote dimer_lmax6_far_spherical")
 
 
+def _mp_spherical_jn(n, z, derivative=False, dps=40):
+    """j_n(z) (or j_n'(z)) of complex z at dps digits (mpmath Bessel J of order
+    n + 1/2), rounded to complex128; arrays elementwise."""
+    import mpmath
+    mpmath.mp.dps = dps
+    zz = np.asarray(z, dtype=complex)
+    out = np.empty(zz.shape, dtype=complex)
+
+    def jn(order, w):
+        if order < 0:   # j_{-1}(w) = cos(w) / w
+            return mpmath.cos(w) / w
+        return mpmath.sqrt(mpmath.pi / (2 * w)) * mpmath.besselj(order + mpmath.mpf(1) / 2, w)
+
+    for idx, v in np.ndenumerate(zz):
+        w = mpmath.mpc(v.real, v.imag)
+        val = jn(n - 1, w) - (n + 1) / w * jn(n, w) if derivative else jn(n, w)
+        out[idx] = complex(val)
+    return out
+
+
+def interior_main():
+    """Interior fields against high-precision j_n:
+    interior_dimer_lmax6  the dimer of dimer_lmax6_exact (index 0.2 + 3i in water,
+        |k_int r| < 2.4), 40 points inside each sphere at 0.5 .. 74 nm from its
+        centre, and 8 outside;
+    interior_big_lmax8  two dielectric spheres (index 4 + 0.01i, radius 300 nm,
+        600 nm, vacuum, lmax 8, |k_int r| up to 12.6), 40 points inside each.
+    Each holds E and H from the reference as it is (j_n by the upward recurrence
+    of cpp/src/special.cpp:20-45, as restated by the oracle) and from the reference
+    with spherical_jn replaced by a 40-digit mpmath evaluation."""
+    miepy = import_reference()
+    rng = np.random.default_rng(31)
+
+    def points(centres, radius, per, r_lo):
+        out = []
+        for c in centres:
+            r = np.exp(rng.uniform(np.log(r_lo), np.log(0.99 * radius), per))
+            u = rng.normal(size=(per, 3))
+            u /= np.linalg.norm(u, axis=1)[:, None]
+            out.append(np.asarray(c)[None, :] + r[:, None] * u)
+        return np.concatenate(out)
+
+    cases = dict(
+        interior_dimer_lmax6=dict(position=[[-100 * nm, 0, 0], [100 * nm, 0, 0]], radius=75 * nm,
+                                  material=miepy.constant_material(index=0.2 + 3.0j), medium=miepy.materials.water(),
+                                  lmax=6, r_lo=0.5 * nm, outside=8),
+        interior_big_lmax8=dict(position=[[-350 * nm, 0, 0], [350 * nm, 0, 0]], radius=300 * nm,
+                                material=miepy.constant_material(index=4.0 + 0.01j), medium=None,
+                                lmax=8, r_lo=2 * nm, outside=0))
+    for name, cs in cases.items():
+        kw = dict(position=cs["position"], radius=cs["radius"], material=cs["material"],
+                  source=miepy.sources.plane_wave.from_string(polarization="x"), wavelength=600 * nm,
+                  lmax=cs["lmax"], method=miepy.solver.exact)
+        if cs["medium"] is not None:
+            kw["medium"] = cs["medium"]
+        c = miepy.sphere_cluster(**kw)
+        pts = points(cs["position"], cs["radius"], 40, cs["r_lo"])
+        if cs["outside"]:
+            pts = np.concatenate([pts, rng.uniform(-300 * nm, 300 * nm, size=(cs["outside"], 3)) + [0, 200 * nm, 0]])
+        x, y, z = pts.T
+        rec = dict(position=c.position, radius=c.radius, lmax=np.int64(cs["lmax"]), field_x=x, field_y=y, field_z=z,
+                   E_ref=c.E_field(x, y, z), H_ref=c.H_field(x, y, z))
+        saved = miepy.vsh.special.spherical_jn
+        miepy.vsh.special.spherical_jn = _mp_spherical_jn
+        try:
+            rec["E_mp"], rec["H_mp"] = c.E_field(x, y, z), c.H_field(x, y, z)
+        finally:
+            miepy.vsh.special.spherical_jn = saved
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)
+        print("wrote", name)
+
+
+def precond_main(results_json):
+    """Linear chains of silver spheres (radius 75 nm, 600 nm, rhc plane wave) of the
+    reference's solver benchmark (benchmarks/bench_solver.py:40-115), at the 15
+    (N, lmax, separation) points of its committed results file (passed as the
+    argument): positions, Mie coefficients, k and p_src from the reference, the
+    diagonal of its build_block_preconditioner_sphere, and the numbers the results
+    file holds for them (iterations, residuals, Frobenius norm of I + T, relative
+    difference of the two solutions) from its bicgstab_profiled and
+    bicgstab_preconditioned_profiled."""
+    import json
+    miepy = import_reference()
+    with open(results_json) as f:
+        data = json.load(f)
+    ents = []
+
+    def walk(o):
+        if isinstance(o, dict):
+            if "iterations_preconditioned" in o:
+                ents.append(o)
+            for v in o.values():
+                walk(v)
+        elif isinstance(o, list):
+            for v in o:
+                walk(v)
+
+    walk(data)
+    rec = dict(count=np.int64(len(ents)))
+    keys = ("iterations", "residual", "iterations_preconditioned", "residual_preconditioned", "frobenius_norm",
+            "solution_relative_diff")
+    for q, e in enumerate(ents):
+        N, lmax, sf = int(e["N"]), int(e["lmax"]), float(e["sep_factor"])
+        pos = np.zeros((N, 3))
+        pos[:, 0] = np.arange(N) * sf * 2 * 75 * nm
+        c = miepy.sphere_cluster(position=pos, radius=75 * nm, material=miepy.materials.Ag(),
+                                 source=miepy.sources.plane_wave.from_string(polarization="rhc"),
+                                 wavelength=600 * nm, lmax=lmax)
+        M, bs = miepy.interactions.build_block_preconditioner_sphere(c.mie_scat, lmax)
+        rows = np.arange(M.shape[0])
+        rec[f"N_{q}"], rec[f"lmax_{q}"], rec[f"sep_factor_{q}"] = np.int64(N), np.int64(lmax), np.float64(sf)
+        rec[f"position_{q}"] = c.position
+        rec[f"mie_scat_{q}"] = c.mie_scat
+        rec[f"k_b_{q}"] = np.float64(np.real(c.material_data.k_b))
+        rec[f"p_src_{q}"] = c.p_src
+        rec[f"pdiag_{q}"] = M[rows, rows % bs]
+        rec[f"expected_{q}"] = np.array([float(e[k]) for k in keys])
+    rec["expected_keys"] = np.array(keys)
+    np.savez_compressed(os.path.join(HERE, "precond_ag_chains.npz"), **rec)
+    print("wrote precond_ag_chains")
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] == "large":
+    if len(sys.argv) > 1 and sys.argv[1] == "interior":
+        interior_main()
+    elif len(sys.argv) > 2 and sys.argv[1] == "precond":
+        precond_main(sys.argv[2])
+    elif len(sys.argv) > 1 and sys.argv[1] == "large":
         large_main()
     elif len(sys.argv) > 1 and sys.argv[1] == "fields":
         fields_main()

@@ -308,13 +308,43 @@ def test_cluster_fields_match_reference():
     for p_ in c.position:
         inside |= (x - p_[0]) ** 2 + (y - p_[1]) ** 2 + (z - p_[2]) ** 2 < (75 * nm) ** 2
     E, H = c.E_field(x, y, z), c.H_field(x, y, z)
-    # outside the spheres: 1e-9.  Inside, the reference evaluates j_n(k_int r) of a
-    # complex argument by upward recurrence (cpp/src/special.cpp:19-45), which loses
-    # digits for |k r| < n; two evaluations of it agree to about 1e-4 there.
+    # outside the spheres: 1e-9 (interior points: test_interior_fields_high_precision)
     assert rel(E[:, ~inside], g["E_total"][:, ~inside]) < 1e-9
     assert rel(H[:, ~inside], g["H_total"][:, ~inside]) < 1e-9
-    assert rel(E[:, inside], g["E_total"][:, inside]) < 1e-4
-    assert rel(H[:, inside], g["H_total"][:, inside]) < 1e-4
+
+
+INTERIOR_CASES = {
+    "interior_dimer_lmax6": dict(radius=75 * nm, material=gb.constant_material(index=0.2 + 3.0j),
+                                 medium=gb.materials.water(), lmax=6),
+    "interior_big_lmax8": dict(radius=300 * nm, material=gb.constant_material(index=4.0 + 0.01j), medium=None,
+                               lmax=8),
+}
+
+
+@pytest.mark.parametrize("name", list(INTERIOR_CASES))
+def test_interior_fields_high_precision(name):
+    """Interior fields (j_n of complex k_int r) against the reference's field formula
+    evaluated with 40-digit j_n: 1e-9 of the largest field at every point.  Against
+    the reference as it is (upward recurrence, cpp/src/special.cpp:20-45): 1e-9 at
+    the points where the reference itself is within 1e-10 of the 40-digit value; at
+    the others (near the centres, |k_int r| < n) the reference's upward recurrence is
+    off by up to 30x the field (interior_dimer_lmax6) and 0.35x (interior_big_lmax8)."""
+    g = G.load(name)
+    cs = INTERIOR_CASES[name]
+    kw = dict(position=g["position"], radius=cs["radius"], material=cs["material"],
+              source=gb.plane_wave.from_string("x"), wavelength=600 * nm, lmax=cs["lmax"], method=gb.solver.exact)
+    if cs["medium"] is not None:
+        kw["medium"] = cs["medium"]
+    c = gb.sphere_cluster(**kw)
+    x, y, z = g["field_x"], g["field_y"], g["field_z"]
+    E, H = c.E_field(x, y, z), c.H_field(x, y, z)
+    assert rel(E, g["E_mp"]) < 1e-9
+    assert rel(H, g["H_mp"]) < 1e-9
+    for F, ref, mp in ((E, g["E_ref"], g["E_mp"]), (H, g["H_ref"], g["H_mp"])):
+        scale = np.abs(mp).max()
+        ok = np.abs(ref - mp).max(axis=0) <= 1e-10 * scale
+        assert ok.sum() >= 20
+        assert np.abs(F[:, ok] - ref[:, ok]).max() < 1e-9 * scale
 
 
 def test_plugin_backend_functions():
