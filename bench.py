@@ -233,6 +233,19 @@ def run_gpu(args, rank, world):
         k = 4
         return float(np.median([(span(k + reps) - span(k)) / reps for _ in range(5)]))
 
+    def time_assemble(b, reps=9):
+        """Device time of one assemble (Mie expansion + matrix assembly), median of reps."""
+        out_ = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record(stream)
+            b.assemble()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out_.append(e0.elapsed_time(e1) / 1e3)
+        return float(np.median(out_))
+
+    t_asm = {p: time_assemble(b) for p, b in batches.items()}
     t_apply64 = time_apply(batches["mixed"], "fp32")
     t_gemv64 = time_apply(batches["mixed"], "fp32", gemv_only=True)
     t_applydf = time_apply(batches["mixed"], "mixed")
@@ -352,6 +365,12 @@ def run_gpu(args, rank, world):
                           gemv_ms=1e3 * t_gemv64),
             double_float_hi_lo=dict(ms=1e3 * t_applydf, matrix_gbs=2 * mat_bytes_64 / t_applydf / 1e9),
             c128_fp64=dict(ms=1e3 * t_apply128, matrix_gbs=mat_bytes_128 / t_apply128 / 1e9)),
+        assembly=dict(
+            kernel="k_assemble (packed pair blocks; mixed writes complex64 hi + lo, FP64 complex128)",
+            mixed_ms=1e3 * t_asm["mixed"], fp64_ms=1e3 * t_asm["fp64"], bytes_written=int(mat_bytes_128),
+            write_floor_ms=1e3 * mat_bytes_128 / (peak * 1e9),
+            frac_of_floor_mixed=mat_bytes_128 / (peak * 1e9) / t_asm["mixed"],
+            frac_of_floor_fp64=mat_bytes_128 / (peak * 1e9) / t_asm["fp64"]),
         gpu_launches_total=int(launches),
         clocks=clocks_info,
         errors_vs_reference=ref_err,

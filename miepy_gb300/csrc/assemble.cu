@@ -29,7 +29,6 @@
 namespace {
 
 constexpr int kAsmThreads = 256;
-constexpr int kAsmWarps = kAsmThreads / 32;   // NB = kAsmWarps selects the warp-per-pair mode
 
 // 1/k for the Legendre recurrence (k = q - mu <= 2*lmax + 1)
 __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
@@ -410,15 +409,13 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // writes pair pp's block (phase 3) and then forms the tuple values of pair
         // pp + 1 (phase 2) into the other buffer, one barrier per pair.
         const int Mb = lay.M;   // tuple-buffer stride (launch-wide)
-        // tuples / write_block run over t0, t0 + ts, ...: the whole CTA (tid, kAsmThreads)
-        // or, in the warp-per-pair mode, one warp (lane, 32)
-        auto tuples = [&](int pp, int buf, int t0, int ts) {
+        auto tuples = [&](int pp, int buf) {
             const size_t gbase = (size_t)PMs * MUs * pp;
             double2* tv = Tv + (size_t)buf * 2 * Mb;
             float2* tf = Tf + (size_t)buf * 2 * Mb;
             float2* tl = Tl + (size_t)buf * 2 * Mb;
             const int Q = L + 1;
-            for (int t = t0; t < S.M; t += ts) {
+            for (int t = tid; t < S.M; t += kAsmThreads) {
                 const int4 e = S.nmvu[t];
                 const int2 qq = S.qab[t];
                 const int mi = (e.w - e.y) + 2 * L;
@@ -483,7 +480,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 }
             }
         };
-        auto write_block = [&](int pp, int buf, int t0, int ts) {
+        auto write_block = [&](int pp, int buf) {
             const long long p = p_first + pp;
             const double2* tv = Tv + (size_t)buf * 2 * Mb;
             const float2* tf = Tf + (size_t)buf * 2 * Mb;
@@ -491,7 +488,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             const int BB = B * B;
             if (!DENSE) {
                 const long long base = S.mat_off + p * (long long)BB;
-                for (int e = t0; e < BB; e += ts) {
+                for (int e = tid; e < BB; e += kAsmThreads) {
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
                     if (FP64_SUMS && out128) {
@@ -512,7 +509,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 const int i = (int)(p / N), j = (int)(p % N);
                 const double2* mj_ = mie + (long long)j * 2 * L;
                 const int rmx = B / 2;
-                for (int e = t0; e < BB; e += ts) {
+                for (int e = tid; e < BB; e += kAsmThreads) {
                     const int R = e / B, C = e % B;
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
@@ -532,7 +529,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 pair_ij(p, N, i, j);
                 const double2* mi_ = mie + (long long)i * 2 * L;
                 const double2* mj_ = mie + (long long)j * 2 * L;
-                for (int e = t0; e < BB; e += ts) {
+                for (int e = tid; e < BB; e += kAsmThreads) {
                     const int R = e / B, C = e % B;
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
@@ -551,7 +548,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         if constexpr (LATT) {
             // every thread sums its own tuples over the group's cells, then the group's
             // share of block (i, j), times mie(j, b, v), is added to the dense output
-            for (int pp = 0; pp < np; pp++) tuples(pp, 0, tid, kAsmThreads);
+            for (int pp = 0; pp < np; pp++) tuples(pp, 0);
             __syncthreads();
             const int i = (int)(lat_pair / N), j = (int)(lat_pair % N);
             const double2* mj_ = mie + (long long)j * 2 * L;
@@ -569,29 +566,13 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             __syncthreads();   // the next group rewrites the tables and the sums
             continue;
         }
-        if constexpr (!DENSE && MODE == 0) {
-            if (NB == kAsmWarps) {
-                // warp-per-pair mode (packed output, small lmax): warp w forms the tuple
-                // values of pairs w, w + 8, ... in its own buffer and writes their blocks;
-                // no CTA barrier until the group's tables are rebuilt
-                const int lane = tid & 31, warp = tid >> 5;
-                for (int pp = warp; pp < np; pp += kAsmWarps) {
-                    tuples(pp, warp, lane, 32);
-                    __syncwarp();
-                    write_block(pp, warp, lane, 32);
-                    __syncwarp();
-                }
-                __syncthreads();   // before the next group's phase 1 rewrites the tables
-                continue;
-            }
-        }
-        tuples(0, 0, tid, kAsmThreads);
+        tuples(0, 0);
         __syncthreads();
         for (int pp = 0; pp < np; pp++) {
-            write_block(pp, NB == 2 ? (pp & 1) : 0, tid, kAsmThreads);   // reads buffer pp & 1 (or the one buffer)
+            write_block(pp, NB == 2 ? (pp & 1) : 0);   // reads buffer pp & 1 (or the one buffer)
             if (pp + 1 < np) {
                 if (NB == 1) __syncthreads();   // one buffer: every read of it done before it is refilled
-                tuples(pp + 1, NB == 2 ? ((pp + 1) & 1) : 0, tid, kAsmThreads);
+                tuples(pp + 1, NB == 2 ? ((pp + 1) & 1) : 0);
             }
             __syncthreads();
         }
@@ -761,17 +742,9 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         // tuple buffers: two (pipelined pairs) when a one-pair group still fits ~72 KB,
         // else one; pairs per group: the largest power of two up to 32 whose tables
         // keep the CTA within ~72 KB of shared memory, so that three CTAs share an SM
-        // packed output where 8 tuple buffers and a group of 8 pairs fit ~110 KB (two CTAs
-        // per SM): warp-per-pair mode (NB = kAsmWarps, PB = 8)
-        const bool wpp = !dense && !refl && !latt &&
-                         asm_layout(L, Mmax, kAsmWarps, fp64_sums, want64, kAsmWarps).total <= 110 * 1024;
-        int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= 72 * 1024 ? 2 : 1;
+        const int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= 72 * 1024 ? 2 : 1;
         int PB = 32;
         while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > 72 * 1024) PB >>= 1;
-        if (wpp) {
-            NB = kAsmWarps;
-            PB = kAsmWarps;
-        }
         const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB);
         const size_t smem = lay.total;
         if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
