@@ -610,6 +610,7 @@ def run_sweep(args, rank=0, world=1):
 
 
 # --------------------------------------------------------- serving stream --
+SERVE_WAVES = 4           # waves on the GPU at once in the serving stream
 SERVE_WORKLOAD = ("serving stream: seeded requests (seed 4), N log-uniform 2-500, lmax uniform 2-8, index "
                   "U[1.3,2.5]+iU[0,0.1], radii 50-100 nm at constant density, 600 nm, vacuum, plane wave or "
                   "Gaussian beam (waist 1 um) 50/50; Poisson arrivals")
@@ -629,7 +630,7 @@ def run_serve(args, nreq=None):
     nreq = max(8, nreq or args.requests)
     reqs = [SV.random_request(rng, rid=i) for i in range(nreq)]
     L = nat_lib()
-    kw = dict(tol=TOL, max_waves=3, max_wave_requests=16)
+    kw = dict(tol=TOL, max_waves=SERVE_WAVES, max_wave_requests=16)
 
     def saturate(precision, rs):
         with SV.SolveServer(precision=precision, **kw) as srv:
@@ -640,9 +641,10 @@ def run_serve(args, nreq=None):
             stats = dict(srv.stats)
         return t, out, stats
 
-    # warm-up: tables of every lmax and the kernels (one small request per lmax)
-    warm = [SV.random_request(np.random.default_rng(100 + l), rid=-1, n_range=(4, 6), lmax_range=(l, l))
-            for l in range(2, 9)]
+    # warm-up: tables of every lmax, the kernels, and the Gaussian beam's far-field
+    # projection at every lmax (one small request per lmax and source kind)
+    warm = [SV.random_request(np.random.default_rng(100 + l), rid=-1, n_range=(4, 6), lmax_range=(l, l),
+                              source_kind=kind) for l in range(2, 9) for kind in ("plane", "gaussian")]
     for p in ("mixed", "fp64"):
         saturate(p, warm)
     clocks = ClockSampler(dev.index).start()

@@ -80,6 +80,15 @@ def rotate_sph(theta, phi, quat):
     return np.asarray(th_r, dtype=float), ph_r
 
 
+def _pinned_host(t):
+    """A device tensor as a numpy copy, read through a pinned buffer on the current
+    stream (one synchronisation of that stream only)."""
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t, non_blocking=True)
+    torch.cuda.current_stream(t.device).synchronize()
+    return h.numpy().copy()
+
+
 class gaussian_beam:
     """Gaussian beam (sources/common.py:10-52).  A beam at (theta, phi) is the +z beam
     rotated by Rz(phi) Ry(theta) about its centre (sources/sources.py:164,
@@ -175,9 +184,10 @@ class gaussian_beam:
         N = pos.shape[0]
         rmax = lmax_to_rmax(lmax)
         rhat, w = self.far_projection(k, lmax)
-        d_pos = torch.from_numpy(np.ascontiguousarray(pos)).to(dev)
-        d_rhat = torch.from_numpy(rhat).to(dev)
-        d_w = torch.from_numpy(w).to(dev)
+        # uploads from pinned copies (pageable uploads share the driver's staging path
+        # with other streams' copies and can wait behind their kernels)
+        d_pos, d_rhat, d_w = (torch.from_numpy(np.ascontiguousarray(a)).pin_memory().to(dev, non_blocking=True)
+                              for a in (pos, rhat, w))
         if out is None:
             out = torch.empty(N * 2 * rmax, dtype=torch.complex128, device=dev)
             out_stride = 1
@@ -203,11 +213,11 @@ class gaussian_beam:
         N = pos.shape[0]
         if not self.rotated:
             out = self.structure_device(pos, k, lmax)
-            return out.cpu().numpy().reshape(N, 2, lmax_to_rmax(lmax))
+            return _pinned_host(out).reshape(N, 2, lmax_to_rmax(lmax))
         Rm = rotation_matrix(self.phi, self.theta)
         # the beam frame: R^T (pos - center); structure_device subtracts the centre itself
         pos_b = (pos - self.center) @ Rm + self.center
-        p = self.structure_device(pos_b, k, lmax).cpu().numpy().reshape(N, 2, lmax_to_rmax(lmax))
+        p = _pinned_host(self.structure_device(pos_b, k, lmax)).reshape(N, 2, lmax_to_rmax(lmax))
         return rotate_expansion_coefficients(p, self.phi, self.theta)
 
 

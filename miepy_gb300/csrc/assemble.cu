@@ -650,7 +650,22 @@ int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector
 // Small per-call descriptor arrays travel through a ring of pinned host /
 // device staging slots (per host thread and device).  A slot is reused only
 // after the event recorded behind the kernels that read it has completed, so
-// calls stay asynchronous.
+// calls stay asynchronous.  Slots grow by doubling and never free a buffer while
+// the thread lives (cudaFree and cudaFreeHost wait for the whole device, which
+// would tie this thread to every other stream's work): outgrown buffers are
+// parked and released when the thread exits.
+struct Parked {
+    std::vector<void*> host, dev;
+    ~Parked() {
+        for (void* p : host) cudaFreeHost(p);
+        for (void* p : dev) cudaFree(p);
+    }
+};
+static Parked& parked() {
+    thread_local Parked p;
+    return p;
+}
+
 struct StageSlot {
     void* host = nullptr;
     void* dev = nullptr;
@@ -685,10 +700,12 @@ int stage_acquire(const void* src, size_t bytes, cudaStream_t stream, void** dev
     }
     if (!S.done) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming));
     if (S.cap < bytes) {
-        if (S.host) cudaFreeHost(S.host);
-        if (S.dev) cudaFree(S.dev);
+        size_t cap = std::max<size_t>(1 << 16, 2 * S.cap);
+        while (cap < bytes) cap *= 2;
+        if (S.host) parked().host.push_back(S.host);
+        if (S.dev) parked().dev.push_back(S.dev);
         S.host = S.dev = nullptr;
-        size_t cap = std::max<size_t>(bytes, 1 << 14);
+        S.cap = 0;
         GB_CUDA_TRY(cudaHostAlloc(&S.host, cap, cudaHostAllocDefault));
         GB_CUDA_TRY(cudaMalloc(&S.dev, cap));
         S.cap = cap;
@@ -698,6 +715,30 @@ int stage_acquire(const void* src, size_t bytes, cudaStream_t stream, void** dev
     *dev_out = S.dev;
     *slot_out = k;
     return GB_OK;
+}
+
+void* host_readback(size_t bytes) {
+    struct Buf {
+        void* p = nullptr;
+        size_t cap = 0;
+    };
+    thread_local Buf b[8];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    Buf& B = b[dev & 7];
+    if (B.cap < bytes) {
+        if (B.p) parked().host.push_back(B.p);
+        B.p = nullptr;
+        size_t cap = std::max<size_t>(1 << 16, 2 * B.cap);
+        while (cap < bytes) cap *= 2;
+        if (cudaHostAlloc(&B.p, cap, cudaHostAllocDefault) != cudaSuccess) {
+            B.p = nullptr;
+            B.cap = 0;
+            return nullptr;
+        }
+        B.cap = cap;
+    }
+    return B.p;
 }
 
 int stage_release(int slot, cudaStream_t stream) {

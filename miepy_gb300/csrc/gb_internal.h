@@ -95,6 +95,12 @@ __host__ __device__ inline long long tc_block_bytes(int B) { return 2 * tc_plane
 int stage_acquire(const void* src, size_t bytes, cudaStream_t stream, void** dev_out, int* slot_out);
 int stage_release(int slot, cudaStream_t stream);
 
+// This host thread's pinned buffer of at least bytes for device->host readbacks of
+// solver state (assemble.cu).  Valid until the thread's next call; a copy into it
+// waits only for its own stream, where one into pageable memory also holds the
+// driver's shared staging path until the stream's earlier work is done.
+void* host_readback(size_t bytes);
+
 int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector<SysDev>& out);
 
 }   // namespace gb

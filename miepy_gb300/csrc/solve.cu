@@ -1762,12 +1762,31 @@ int upload_plan(const Plan& P, unsigned char* base, const WS& w, cudaStream_t st
     return GB_OK;
 }
 
+// Readbacks of solver state go through the thread's pinned buffer, except while
+// the no-allocation solve runs on this thread (it must not allocate one).
+thread_local bool t_pageable_readback = false;
+struct PageableReadback {
+    bool prev;
+    PageableReadback() : prev(t_pageable_readback) { t_pageable_readback = true; }
+    ~PageableReadback() { t_pageable_readback = prev; }
+};
+
+int read_state(const DevPlan& D, const KState* dev, int nsr, std::vector<KState>& h, cudaStream_t stream);
+
 // Reads the GEMV error flag back (synchronises the stream).
 int check_device_error(const DevPlan& D, cudaStream_t stream) {
-    int h = 0;
-    GB_CUDA_TRY(cudaMemcpyAsync(&h, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    if (t_pageable_readback) {
+        int h = 0;
+        GB_CUDA_TRY(cudaMemcpyAsync(&h, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        GB_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (h) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
+        return GB_OK;
+    }
+    int* h = static_cast<int*>(gb::host_readback(sizeof(int)));
+    if (!h) return gb_set_error(GB_CUDA_ERROR, "no pinned readback buffer");
+    GB_CUDA_TRY(cudaMemcpyAsync(h, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GB_CUDA_TRY(cudaStreamSynchronize(stream));
-    if (h) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
+    if (*h) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
     return GB_OK;
 }
 
@@ -2292,11 +2311,10 @@ int run_bicgstab(const Plan& P, const DevPlan& D, const WS& w, unsigned char* ba
                 if (e) return e;
             }
         }
-        int herr = 0;
-        GB_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
-        GB_CUDA_TRY(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        GB_CUDA_TRY(cudaStreamSynchronize(stream));
-        if (herr) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
+        {
+            const int e = read_state(D, st, nsr, hst, stream);
+            if (e) return e;
+        }
         bool all_done = true, restart = false;
         for (int q = 0; q < nsr; q++) {
             if (!hst[q].done) all_done = false;
@@ -2331,13 +2349,27 @@ int finish_status(const KState* h, int nsr, int* status, int* iters, double* res
     return worst;
 }
 
+// The scalars of every (cluster, rhs) and the GEMV error flag, through this thread's
+// pinned readback buffer (synchronises the stream).
 int read_state(const DevPlan& D, const KState* dev, int nsr, std::vector<KState>& h, cudaStream_t stream) {
     h.resize(nsr);
-    int herr = 0;
-    GB_CUDA_TRY(cudaMemcpyAsync(h.data(), dev, sizeof(KState) * nsr, cudaMemcpyDeviceToHost, stream));
-    GB_CUDA_TRY(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    const size_t kb = sizeof(KState) * (size_t)nsr;
+    if (t_pageable_readback) {
+        int herr = 0;
+        GB_CUDA_TRY(cudaMemcpyAsync(h.data(), dev, kb, cudaMemcpyDeviceToHost, stream));
+        GB_CUDA_TRY(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        GB_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (herr) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
+        return GB_OK;
+    }
+    unsigned char* pin = static_cast<unsigned char*>(gb::host_readback(kb + 16));
+    if (!pin) return gb_set_error(GB_CUDA_ERROR, "no pinned readback buffer");
+    int* herr = reinterpret_cast<int*>(pin + kb);
+    GB_CUDA_TRY(cudaMemcpyAsync(pin, dev, kb, cudaMemcpyDeviceToHost, stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GB_CUDA_TRY(cudaStreamSynchronize(stream));
-    if (herr) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
+    if (*herr) return gb_set_error(GB_TIMEOUT, "a GEMV copy did not complete within its wait limit");
+    memcpy(h.data(), pin, kb);
     return GB_OK;
 }
 
@@ -2896,6 +2928,7 @@ int gb_solve_dense_noalloc(int D, int R, const double* T, const double* b, doubl
         return gb_set_error(GB_OVER_BUDGET, "D * R = %lld exceeds the no-allocation solve's limit of %lld",
                             (long long)D * R, kNoAllocMaxDR);
     cudaStream_t s = (cudaStream_t)stream;
+    const PageableReadback pageable;   // no pinned readback buffer either
     Plan P;
     dense_plan(D, R, P);
     WS w = ws_layout(P, GB_PREC_FP64, true);

@@ -150,6 +150,7 @@ class SolveServer:
         self._closing = False
         self._free_streams = list(range(self.max_waves))
         self._slot_class = {}
+        self._slot_cost = {}
         self._streams = self._make_streams()
         # persistent workers: the native library keeps per-thread staging buffers
         # and capture streams, reused wave after wave
@@ -167,12 +168,28 @@ class SolveServer:
         return hbm_budget
 
     def _make_streams(self):
-        """Per wave slot a (normal, high-priority) pair of streams: waves of small
-        requests run on the high-priority one, so that their kernels are scheduled
-        ahead of a large wave's when both wait for SMs."""
+        """Per wave slot one stream at every priority the device offers, lowest
+        first.  A wave runs on the stream whose priority matches its cost (see
+        _priority_level): when waves of different sizes wait for SMs, the CTAs of the
+        cheaper one are dispatched first, so a small request is not held behind a
+        large one's kernels."""
         lo, hi = torch.cuda.Stream.priority_range() if hasattr(torch.cuda.Stream, "priority_range") else (0, -1)
-        return [(torch.cuda.Stream(device=self.device, priority=lo),
-                 torch.cuda.Stream(device=self.device, priority=hi)) for _ in range(self.max_waves)]
+        step = -1 if hi < lo else 1
+        return [[torch.cuda.Stream(device=self.device, priority=p) for p in range(lo, hi + step, step)]
+                for _ in range(self.max_waves)]
+
+    @staticmethod
+    def _priority_level(cost, levels):
+        """Index into a slot's streams (0 = lowest priority) for a wave of cost bytes:
+        one level per factor of 8 in footprint, the highest at <= 64 MB."""
+        if levels <= 1:
+            return 0
+        k = 0
+        c = 64 << 20
+        while cost > c and k < levels - 1:
+            c *= 8
+            k += 1
+        return levels - 1 - k
 
     # --------------------------------------------------------------- client --
     def submit(self, req: ClusterRequest) -> cf.Future:
@@ -284,6 +301,7 @@ class SolveServer:
                 self.stats["waves"] += 1
                 sidx = self._free_streams.pop()
                 self._slot_class[sidx] = cls
+                self._slot_cost[sidx] = used
                 wid = self._wave_counter
                 self._wave_counter += 1
             self._pool.submit(self._run_wave, wave, used, sidx, wid, cls)
@@ -327,18 +345,22 @@ class SolveServer:
     def _execute(self, wave, sidx):
         """Solves one wave on its stream: one ragged ClusterBatch, assembled,
         solved and reduced; returns one ClusterResult per request."""
-        normal, high = self._streams[sidx]
-        stream = high if self._slot_class.get(sidx, 1) == 0 else normal
+        streams = self._streams[sidx]
+        stream = streams[self._priority_level(self._slot_cost.get(sidx, 1 << 62), len(streams))]
         with torch.cuda.device(self.device), torch.cuda.stream(stream):
             specs = [request_spec(w[0]) for w in wave]
             b = ClusterBatch(specs, R=1, precision=self.precision, device=self.device)
             b.assemble()
             b.solve(tol=self.tol, maxiter=self.maxiter, inner_tol=self.inner_tol, max_refine=8)
             b.epilogue(specs[0]["eps_b"])
-            xs = b.xs[: b.totals["obs"] * 6 * b.xs_L].view(-1, 3, 2 * b.xs_L).cpu().numpy()
-            F = b.F[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
-            T = b.T[: b.totals["obs"] * 3].view(-1, 3).cpu().numpy()
-            x = b.x.cpu().numpy()
+            # one pinned readback (a copy into pageable memory would share the driver's
+            # staging path with the other waves' copies and wait behind their kernels)
+            h = b.to_host()
+            nobs = b.totals["obs"]
+            xs = h["xs"][: nobs * 6 * b.xs_L].reshape(-1, 3, 2 * b.xs_L)
+            F = h["F"][: nobs * 3].reshape(-1, 3)
+            T = h["T"][: nobs * 3].reshape(-1, 3)
+            x = h["x"]
             status, iters = b.status.copy(), b.iters.copy()
             del b
         out = []
@@ -383,11 +405,12 @@ _BEAMS = {}                       # one beam object per waist: its far-field pro
 _BEAMS_LOCK = threading.Lock()
 
 def random_request(rng, rid=-1, n_range=(2, 500), lmax_range=(2, 8), wavelength=600e-9, beam_width=1e-6,
-                   rmin=50e-9, rmax=100e-9, cell=0.5e-6, max_tries=1_000_000):
+                   rmin=50e-9, rmax=100e-9, cell=0.5e-6, max_tries=1_000_000, source_kind=None):
     """One request of the serving workload: N log-uniform in n_range, lmax uniform,
     index U[1.3, 2.5] + i U[0, 0.1], radii U[rmin, rmax], centres in a cube of side
     (N cell^3)^(1/3) by rejection sampling; plane wave or Gaussian beam with equal
-    probability."""
+    probability (source_kind "plane" or "gaussian" fixes it; the draw is made
+    either way, so the rest of the stream is unchanged)."""
     from .beams import gaussian_beam
     N = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
     L = int(rng.integers(lmax_range[0], lmax_range[1] + 1))
@@ -406,7 +429,10 @@ def random_request(rng, rid=-1, n_range=(2, 500), lmax_range=(2, 8), wavelength=
             pos[n], rad[n] = c, r
             n += 1
     pos = pos - side / 2
-    if rng.uniform() < 0.5:
+    gauss = rng.uniform() < 0.5
+    if source_kind is not None:
+        gauss = source_kind == "gaussian"
+    if gauss:
         key = float(beam_width)
         with _BEAMS_LOCK:
             if key not in _BEAMS:

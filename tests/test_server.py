@@ -302,3 +302,23 @@ def test_ill_conditioned_lmax8_beam_request_converges():
             out[prec] = srv.submit(r).result()
     assert out["mixed"].status == 0 and out["fp64"].status == 0
     assert abs(out["mixed"].C_ext - out["fp64"].C_ext) / abs(out["fp64"].C_ext) < 1e-6
+
+
+def test_priority_level_by_wave_cost():
+    lv = SV.SolveServer._priority_level
+    # six levels (priorities 0 .. -5): the highest for <= 64 MB, one lower per factor 8
+    assert lv(1 << 20, 6) == 5 and lv(64 << 20, 6) == 5
+    assert lv((64 << 20) + 1, 6) == 4 and lv(512 << 20, 6) == 4
+    assert lv(4 << 30, 6) == 3 and lv(30 << 30, 6) == 2
+    assert lv(1 << 50, 6) == 0
+    assert lv(1 << 50, 1) == 0 and lv(1, 2) == 1
+
+
+def test_random_request_source_kind_keeps_the_stream():
+    a = [SV.random_request(np.random.default_rng(9), rid=i, n_range=(2, 6)) for i in range(3)]
+    g = [SV.random_request(np.random.default_rng(9), rid=i, n_range=(2, 6), source_kind="gaussian") for i in range(3)]
+    p = [SV.random_request(np.random.default_rng(9), rid=i, n_range=(2, 6), source_kind="plane") for i in range(3)]
+    for x, y, z in zip(a, g, p):
+        assert np.array_equal(x.position, y.position) and np.array_equal(x.position, z.position)
+        assert x.lmax == y.lmax == z.lmax and x.index == y.index
+        assert type(y.source).__name__ == "gaussian_beam" and type(z.source).__name__ == "plane_wave"
