@@ -188,8 +188,10 @@ struct Latt {
 // double-float on the FP32 pipes, straight to the complex64 hi / lo outputs.
 // MODE 0: the aggregate T-matrix; 1: the dense reflection matrix (Refl); 2: the
 // lattice sums of a periodic cluster, added to a dense output (Latt).
+// Occupancy: the double-float (mixed) path fits five CTAs per SM in 48 registers
+// without spills; the FP64 paths keep three (at five they spill).
 template <bool DENSE, bool FP64_SUMS, int MODE = 0>
-__global__ void __launch_bounds__(kAsmThreads, 3)
+__global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
            int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
            double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
@@ -780,12 +782,16 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
             total_pairs += (refl || latt) ? (long long)d.N * d.N : d.P;
         }
         if (total_pairs == 0) continue;
-        // tuple buffers: two (pipelined pairs) when a one-pair group still fits ~72 KB,
-        // else one; pairs per group: the largest power of two up to 32 whose tables
-        // keep the CTA within ~72 KB of shared memory, so that three CTAs share an SM
-        const int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= 72 * 1024 ? 2 : 1;
-        int PB = 32;
-        while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > 72 * 1024) PB >>= 1;
+        // tuple buffers: two (pipelined pairs) when a one-pair group still fits the
+        // CTA's shared-memory target, else one; pairs per group: the largest power of
+        // two up to the cap whose tables keep the CTA within the target.  Targets: ~72
+        // KB for the FP64 paths (three CTAs per SM), ~44 KB and at most 4 pairs for the
+        // double-float path (five CTAs per SM: measured 0.31 ms against 0.35 ms with
+        // three CTAs of 8 pairs at N = 200, lmax 4)
+        const size_t target = fp64_sums ? 72 * 1024 : 44 * 1024;
+        const int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= target ? 2 : 1;
+        int PB = fp64_sums ? 32 : 4;
+        while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > target) PB >>= 1;
         const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB);
         const size_t smem = lay.total;
         if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
@@ -819,7 +825,10 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         int per_sm = 1;
         GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
         if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
-        const long long grid = std::min<long long>(ngroups, (long long)gb::sm_count() * per_sm);
+        // one group per CTA (no persistent loop): CTAs retire every few microseconds, so
+        // kernels of higher-priority streams (other clusters' solves) are dispatched
+        // between them instead of waiting for the whole assembly
+        const long long grid = std::min<long long>(ngroups, 0x7fffffffLL);
         gb::note_launch();
         kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
             dsys, ns, dbase, ngroups, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),

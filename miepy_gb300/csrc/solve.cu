@@ -1861,8 +1861,10 @@ int launch_pgemv_group(const Plan& P, const DevPlan& D, const StripGroup& grp, c
     const size_t smem = (size_t)kGemvWarps * g.warp_bytes;
     if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "GEMV needs %zu B of shared memory", smem);
     const long long n = grp.end - grp.beg;
+    // one strip per warp (no persistent loop): CTAs retire after their strips, so
+    // kernels of higher-priority streams are dispatched between them
     const long long grid = std::max<long long>(1, std::min<long long>((n * 32 + kGemvThreads - 1) / kGemvThreads,
-                                                                      (long long)gb::sm_count() * 8));
+                                                                      0x7fffffffLL));
 #define GB_PG(LPRV, CPLV)                                                                                        \
     if (sh.lpr == LPRV && sh.cpl == CPLV) {                                                                      \
         constexpr int GV = gemv_steps(LPRV, CPLV, Pol::MB * (Pol::DF ? 2 : 1));                                  \
