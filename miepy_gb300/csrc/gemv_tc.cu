@@ -26,15 +26,19 @@
 // stored as the CUDA-core pass stores its column sums, C[rho(r)] = eps(r) (A z)[r],
 // so the block reduce that follows is shared.
 //
-// Pipeline per CTA (128 threads, persistent over strips): thread 0 streams each
-// block's two planes and its y_u by bulk copies (TMA) into a ring of 3 stages; all
-// threads build the block's B operand (bf16, core-matrix layout) in one of two
-// buffers; thread 0 issues the block's MMAs (M = 128: the block's rows, padding rows
-// read and discarded) into one of two TMEM accumulators and commits them to an
-// mbarrier; meanwhile every warp reads the previous block's accumulator rows
-// (tcgen05.ld), writes its column partials and keeps the strip's row sums.  Every
-// wait is bounded; a wait that expires sets the error flag, and the CTA waits (again
-// bounded) for its copies and MMAs in flight before it frees its TMEM and exits.
+// Pipeline per CTA (160 threads, two CTAs per SM, persistent over strips): a
+// producer warp walks the CTA's strips ahead of the others and, per block, writes a
+// job record and streams the block's two planes with its y_w (and the strip's y_u
+// with its first block) by bulk copies (TMA) into a ring of 3 stages, reusing a stage
+// once the MMAs that read it have committed to its empty barrier; the 4 consumer
+// warps build the block's B operand (bf16, core-matrix layout) in one of two buffers;
+// thread 0 issues the block's MMAs (M = 128: the block's rows, padding rows read and
+// discarded) into one of two TMEM accumulators and commits them to mbarriers;
+// meanwhile the consumer warps read the previous block's accumulator rows
+// (tcgen05.ld), write its column partials and keep the strip's row sums.  Every wait
+// is bounded; an expired wait sets the error flag, the consumers decide to stop
+// together through a reduction barrier, and the CTA waits (again bounded) for its
+// copies and MMAs in flight before it frees its TMEM and exits.
 
 #include <cuda_bf16.h>
 
