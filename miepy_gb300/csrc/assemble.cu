@@ -190,7 +190,12 @@ struct Latt {
 // lattice sums of a periodic cluster, added to a dense output (Latt).
 // Occupancy: the double-float (mixed) path fits five CTAs per SM in 48 registers
 // without spills; the FP64 paths keep three (at five they spill).
-template <bool DENSE, bool FP64_SUMS, int MODE = 0>
+// TS: tuple-stationary groups of the packed double-float path (lmax <= 4, one
+// tuple-value buffer per pair of the group, NB = PB): each thread loads its tuples'
+// indices and coefficients once and forms them for every pair of the group, then
+// every block of the group is written after one barrier, each element-map code read
+// once for all of them.
+template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false>
 __global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
            int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
@@ -198,6 +203,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
            Refl refl = Refl(), Latt latt = Latt()) {
     constexpr bool REFL = MODE == 1, LATT = MODE == 2;
     static_assert(MODE == 0 || (DENSE && FP64_SUMS), "reflection and lattice sums are dense FP64 outputs");
+    static_assert(!TS || (!DENSE && !FP64_SUMS && MODE == 0), "tuple-stationary groups serve the packed double-float path");
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
@@ -374,11 +380,11 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // ---- phase 1c: G[p][mu] = P_p^mu h_p e^{i mu phi} (negative mu through the
         // (-1)^mu (p-mu)!/(p+mu)! ratio), FP64, or double-float for the mixed path
         // (the ratio as a double-float mantissa and an exact binary scaling)
-        for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
-            const int pp = it / (PM * MU), rem = it % (PM * MU);
-            const int q = rem / MU, mi = rem % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
-            const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
-            if constexpr (FP64_SUMS) {
+        if constexpr (FP64_SUMS) {
+            for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
+                const int pp = it / (PM * MU), rem = it % (PM * MU);
+                const int q = rem / MU, mi = rem % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
+                const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
                 double2 gval = make_double2(0.0, 0.0);
                 if (am <= q) {
                     double P = Pl[(size_t)PMs * PMs * pp + q * PMs + am];
@@ -387,22 +393,36 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     gval = make_double2(P * he.x, P * he.y);
                 }
                 G64[gi] = gval;
-            } else {
-                float4 gval = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (am <= q) {
-                    const float2 pv = reinterpret_cast<const float2*>(Pl)[(size_t)PMs * PMs * pp + q * PMs + am];
-                    DF P{pv.x, pv.y};
-                    if (mu < 0) {
-                        const float4 r = S.neg_ratio2[q * PM + am];
-                        P = df_mul(P, DF{r.x, r.y});
-                        const int ex = (int)r.z;
-                        P = DF{ldexpf(P.h, ex), ldexpf(P.l, ex)};
+            }
+        } else {
+            // thread per (p, mu), looping over the group's pairs: the divisions and the
+            // negative-order ratio are per thread, not per entry (the group holds at
+            // most 4 pairs on this path)
+            for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
+                const int q = qm / MU, mi = qm - q * MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
+                float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (am <= q && mu < 0) r = S.neg_ratio2[q * PM + am];
+                for (int pp = 0; pp < np; pp++) {
+                    const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
+                    float4 gval = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (am <= q) {
+                        const float2 pv = reinterpret_cast<const float2*>(Pl)[(size_t)PMs * PMs * pp + q * PMs + am];
+                        DF P{pv.x, pv.y};
+                        if (mu < 0) {
+                            P = df_mul(P, DF{r.x, r.y});
+                            if (r.w != 0.f) {   // 2^e as a normal float: the scaling is one exact-rounded product
+                                P = DF{P.h * r.w, P.l * r.w};
+                            } else {
+                                const int ex = (int)r.z;
+                                P = DF{ldexpf(P.h, ex), ldexpf(P.l, ex)};
+                            }
+                        }
+                        const DFC he = dfc_mul(dfc_unpack(reinterpret_cast<const float4*>(hh)[PMs * pp + q]),
+                                               dfc_unpack(reinterpret_cast<const float4*>(eph)[MUs * pp + mi]));
+                        gval = dfc_pack(DFC{df_mul(P, he.re), df_mul(P, he.im)});
                     }
-                    const DFC he = dfc_mul(dfc_unpack(reinterpret_cast<const float4*>(hh)[PMs * pp + q]),
-                                           dfc_unpack(reinterpret_cast<const float4*>(eph)[MUs * pp + mi]));
-                    gval = dfc_pack(DFC{df_mul(P, he.re), df_mul(P, he.im)});
+                    G32[gi] = gval;
                 }
-                G32[gi] = gval;
             }
         }
         __syncthreads();
@@ -566,6 +586,61 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 atomicAdd(o + 1, w.y);
             }
             __syncthreads();   // the next group rewrites the tables and the sums
+            continue;
+        }
+        if constexpr (TS) {
+            constexpr int QX = 5;   // lmax <= 4: at most 5 terms per sum
+            for (int t = tid; t < S.M; t += kAsmThreads) {
+                const int4 e = S.nmvu[t];
+                const int2 qq = S.qab[t];
+                const int mi = (e.w - e.y) + 2 * L;
+                const int nv = e.x + e.z;
+                const float2* ca = S.cA2 + (size_t)t * (L + 1);
+                const float2* cb = S.cB2 + (size_t)t * (L + 1);
+                float2 cav[QX], cbv[QX];
+#pragma unroll
+                for (int q = 0; q < QX; q++) {
+                    cav[q] = q <= qq.x ? ca[q] : make_float2(0.f, 0.f);
+                    cbv[q] = (q >= 1 && q <= qq.y) ? cb[q] : make_float2(0.f, 0.f);
+                }
+                for (int pp = 0; pp < np; pp++) {
+                    const float4* gp = G32 + (size_t)PMs * MUs * pp + (size_t)nv * MUs + mi;
+                    float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
+#pragma unroll
+                    for (int q = 0; q < QX; q++) {
+                        if (q <= qq.x) df_rc_fma(ah, al, cav[q], gp[-2 * q * MUs]);
+                        if (q >= 1 && q <= qq.y) df_rc_fma(bh, bl, cbv[q], gp[(1 - 2 * q) * MUs]);
+                    }
+                    const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
+                    const float2 a2 = __fadd2_rn(al, negf2(__fadd2_rn(a1, negf2(ah))));
+                    const float2 b2 = __fadd2_rn(bl, negf2(__fadd2_rn(b1, negf2(bh))));
+                    float2* tf = Tf + (size_t)pp * 2 * Mb;
+                    float2* tl = Tl + (size_t)pp * 2 * Mb;
+                    tf[2 * t] = mul_ipowf(a1, nv);
+                    tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
+                    tl[2 * t] = mul_ipowf(a2, nv);
+                    tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
+                }
+            }
+            __syncthreads();
+            const int BB = B * B;
+            for (int el = tid; el < BB; el += kAsmThreads) {
+                const int code = __ldg(S.elem_map + el);
+                const unsigned neg = code & 1;
+                const int ti = code >> 1;
+                for (int pp = 0; pp < np; pp++) {
+                    const long long at = S.mat_off + (p_first + pp) * (long long)BB + el;
+                    if (out64) {
+                        const float2 v = Tf[(size_t)pp * 2 * Mb + ti];
+                        out64[at] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+                    }
+                    if (out64lo) {
+                        const float2 v = Tl[(size_t)pp * 2 * Mb + ti];
+                        out64lo[at] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
+                    }
+                }
+            }
+            __syncthreads();   // before the next group rewrites the tables and the buffers
             continue;
         }
         tuples(0, 0);
@@ -789,9 +864,20 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         // double-float path (five CTAs per SM: measured 0.31 ms against 0.35 ms with
         // three CTAs of 8 pairs at N = 200, lmax 4)
         const size_t target = fp64_sums ? 72 * 1024 : 44 * 1024;
-        const int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= target ? 2 : 1;
+        int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= target ? 2 : 1;
         int PB = fp64_sums ? 32 : 4;
         while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > target) PB >>= 1;
+        // tuple-stationary groups (packed double-float, lmax <= 4): one buffer per pair,
+        // the most pairs up to 4 that keep the target
+        bool ts = false;
+        if (!dense && !refl && !latt && !fp64_sums && L <= 4) {
+            int pb = 4;
+            while (pb > 1 && asm_layout(L, Mmax, pb, false, want64, pb).total > target) pb--;
+            if (pb >= 2) {
+                ts = true;
+                PB = NB = pb;
+            }
+        }
         const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB);
         const size_t smem = lay.total;
         if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
@@ -820,7 +906,9 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         auto kfn = latt ? k_assemble<true, true, 2>
                         : refl ? k_assemble<true, true, 1>
                                : (dense ? k_assemble<true, true>
-                                        : (fp64_sums ? k_assemble<false, true> : k_assemble<false, false>));
+                                        : (fp64_sums ? k_assemble<false, true>
+                                                     : (ts ? k_assemble<false, false, 0, true>
+                                                           : k_assemble<false, false>)));
         GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
         int per_sm = 1;
         GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));

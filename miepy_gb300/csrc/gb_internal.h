@@ -20,7 +20,7 @@ struct Tables {
     float2* cB2 = nullptr;     // [M][lmax+1] (hi, lo) split of cB
     int* elem_map = nullptr;   // [B*B] (tuple << 2) | (is_B << 1) | negate
     double* neg_ratio = nullptr;   // [(2L+2)^2] (-1)^mu (p-mu)!/(p+mu)!
-    float4* neg_ratio2 = nullptr;  // the same as (m.hi, m.lo, e, 0): ratio = (m.hi + m.lo) 2^e, m in [0.5, 1)
+    float4* neg_ratio2 = nullptr;  // the same as (m.hi, m.lo, e, s): ratio = (m.hi + m.lo) 2^e, m in [0.5, 1), s = 2^e if normal else 0
     int* rowinfo = nullptr;    // [B] rho(row) | eps_neg << 29 | sig_neg << 30
     int* miecol = nullptr;     // [B] a*lmax + n - 1
 };

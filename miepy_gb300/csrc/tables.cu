@@ -251,7 +251,9 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
         int ex = 0;
         const double m = std::frexp(negr[q], &ex);
         const float hi = (float)m;
-        negr2[q] = make_float4(hi, (float)(m - (double)hi), (float)ex, 0.f);
+        // .w: 2^e when it is a normal float (e >= -126), else 0 (the kernel then scales
+        // with ldexpf)
+        negr2[q] = make_float4(hi, (float)(m - (double)hi), (float)ex, ex >= -126 ? std::ldexp(1.0f, ex) : 0.f);
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->neg_ratio, negr.data(), sizeof(double) * PM * PM, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->neg_ratio2, negr2.data(), sizeof(float4) * PM * PM, cudaMemcpyHostToDevice, stream);
