@@ -83,21 +83,21 @@ __device__ __forceinline__ float2 mul_ipowf(float2 z, int k) {
     }
 }
 __device__ __forceinline__ float2 bcf(float v) { return make_float2(v, v); }
-__device__ __forceinline__ float2 negf2(float2 v) { return make_float2(-v.x, -v.y); }
 
-// (sh, sl) += (c.x + c.y) * (g.hi + g.lo): double-float real x complex
-// multiply-add on the FP32 pipes (packed f32x2): the hi*hi product is exact
-// (FMA error term), cross terms and the TwoSum error go to the low word.
-__device__ __forceinline__ void df_rc_fma(float2& sh, float2& sl, float2 c, float4 g) {
-    const float2 ah = bcf(c.x), al = bcf(c.y);
+// (sh, sl) += (ch + cl) * (g.hi + g.lo): double-float real x complex multiply-add
+// on the FP32 pipes (packed f32x2), with nch = -ch given.  pn = RN(-ch gh) is the
+// negated hi*hi product, fma(ch, gh, pn) its exact error; cross terms and the TwoSum
+// error of sh + p = sh - pn go to the low word.  Written with subtractions so that
+// no operand needs a sign flip.
+__device__ __forceinline__ void df_rc_fma(float2& sh, float2& sl, float ch, float nch, float cl, float4 g) {
     const float2 gh = make_float2(g.x, g.y), gl = make_float2(g.z, g.w);
-    const float2 p = __fmul2_rn(ah, gh);
-    float2 e = __ffma2_rn(ah, gh, negf2(p));
-    e = __ffma2_rn(ah, gl, e);
-    e = __ffma2_rn(al, gh, e);
-    const float2 t = __fadd2_rn(sh, p);
-    const float2 bb = __fadd2_rn(t, negf2(sh));
-    const float2 err = __fadd2_rn(__fadd2_rn(sh, negf2(__fadd2_rn(t, negf2(bb)))), __fadd2_rn(p, negf2(bb)));
+    const float2 pn = __fmul2_rn(bcf(nch), gh);
+    float2 e = __ffma2_rn(bcf(ch), gh, pn);
+    e = __ffma2_rn(bcf(ch), gl, e);
+    e = __ffma2_rn(bcf(cl), gh, e);
+    const float2 t = fsub2(sh, pn);
+    const float2 bb = fsub2(t, sh);
+    const float2 err = fsub2(fsub2(sh, fsub2(t, bb)), __fadd2_rn(pn, bb));   // (sh - (t - bb)) + (p - bb)
     sh = t;
     sl = __fadd2_rn(sl, __fadd2_rn(err, e));
 }
@@ -488,13 +488,19 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     // the A and B sums interleaved: two independent double-float chains
                     const int qa = qq.x, qb = qq.y, qm = qa > qb ? qa : qb;
                     for (int q = 0; q <= qm; q++) {
-                        if (q <= qa) df_rc_fma(ah, al, ca[q], G32[gbase + (size_t)(nv - 2 * q) * MUs + mi]);
-                        if (q >= 1 && q <= qb) df_rc_fma(bh, bl, cb[q], G32[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi]);
+                        if (q <= qa) {
+                            const float2 c = ca[q];
+                            df_rc_fma(ah, al, c.x, -c.x, c.y, G32[gbase + (size_t)(nv - 2 * q) * MUs + mi]);
+                        }
+                        if (q >= 1 && q <= qb) {
+                            const float2 c = cb[q];
+                            df_rc_fma(bh, bl, c.x, -c.x, c.y, G32[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi]);
+                        }
                     }
                     // normalise (Fast2Sum): hi = fl(h + l), lo = l - (hi - h)
                     const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
-                    const float2 a2 = __fadd2_rn(al, negf2(__fadd2_rn(a1, negf2(ah))));
-                    const float2 b2 = __fadd2_rn(bl, negf2(__fadd2_rn(b1, negf2(bh))));
+                    const float2 a2 = fsub2(al, fsub2(a1, ah));
+                    const float2 b2 = fsub2(bl, fsub2(b1, bh));
                     tf[2 * t] = mul_ipowf(a1, nv);
                     tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
                     tl[2 * t] = mul_ipowf(a2, nv);
@@ -598,22 +604,25 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 const float2* ca = S.cA2 + (size_t)t * (L + 1);
                 const float2* cb = S.cB2 + (size_t)t * (L + 1);
                 float2 cav[QX], cbv[QX];
+                float nca[QX], ncb[QX];   // negated hi words, once per tuple
 #pragma unroll
                 for (int q = 0; q < QX; q++) {
                     cav[q] = q <= qq.x ? ca[q] : make_float2(0.f, 0.f);
                     cbv[q] = (q >= 1 && q <= qq.y) ? cb[q] : make_float2(0.f, 0.f);
+                    nca[q] = -cav[q].x;
+                    ncb[q] = -cbv[q].x;
                 }
                 for (int pp = 0; pp < np; pp++) {
                     const float4* gp = G32 + (size_t)PMs * MUs * pp + (size_t)nv * MUs + mi;
                     float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
 #pragma unroll
                     for (int q = 0; q < QX; q++) {
-                        if (q <= qq.x) df_rc_fma(ah, al, cav[q], gp[-2 * q * MUs]);
-                        if (q >= 1 && q <= qq.y) df_rc_fma(bh, bl, cbv[q], gp[(1 - 2 * q) * MUs]);
+                        if (q <= qq.x) df_rc_fma(ah, al, cav[q].x, nca[q], cav[q].y, gp[-2 * q * MUs]);
+                        if (q >= 1 && q <= qq.y) df_rc_fma(bh, bl, cbv[q].x, ncb[q], cbv[q].y, gp[(1 - 2 * q) * MUs]);
                     }
                     const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
-                    const float2 a2 = __fadd2_rn(al, negf2(__fadd2_rn(a1, negf2(ah))));
-                    const float2 b2 = __fadd2_rn(bl, negf2(__fadd2_rn(b1, negf2(bh))));
+                    const float2 a2 = fsub2(al, fsub2(a1, ah));
+                    const float2 b2 = fsub2(bl, fsub2(b1, bh));
                     float2* tf = Tf + (size_t)pp * 2 * Mb;
                     float2* tl = Tl + (size_t)pp * 2 * Mb;
                     tf[2 * t] = mul_ipowf(a1, nv);

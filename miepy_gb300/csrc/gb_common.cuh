@@ -21,6 +21,17 @@ __host__ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 // acc += a * b
+// a - b on packed f32x2 (sub.rn.f32x2): the packed add takes no negated operand,
+// so a - b written as a + (-b) costs a sign flip per component on the integer pipe
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+    unsigned long long ra, rb, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    float2 d;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+    return d;
+}
 __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
     acc.x = fma(a.x, b.x, acc.x);
     acc.x = fma(-a.y, b.y, acc.x);

@@ -190,8 +190,8 @@ __device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y
 // (h, l) += p exactly (TwoSum on both components), error into l
 __device__ __forceinline__ void two_sum2(float2& h, float2& l, float2 p) {
     const float2 s = __fadd2_rn(h, p);
-    const float2 bb = __fadd2_rn(s, neg2(h));
-    const float2 err = __fadd2_rn(__fadd2_rn(h, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(p, neg2(bb)));
+    const float2 bb = fsub2(s, h);
+    const float2 err = __fadd2_rn(fsub2(h, fsub2(s, bb)), fsub2(p, bb));
     h = s;
     l = __fadd2_rn(l, err);
 }
@@ -277,13 +277,13 @@ struct PolDF {
         float2 p = __fmul2_rn(m.h, yr);
         float2 en = __ffma2_rn(m.nh, yr, p);                 // p - m y = -(rounding error)
         two_sum2(s.ha, s.la, p);
-        s.la = __fadd2_rn(s.la, neg2(en));
+        s.la = fsub2(s.la, en);
         s.la = __ffma2_rn(m.l, yr, s.la);
         s.la = __ffma2_rn(m.h, bc(y.z), s.la);
         p = __fmul2_rn(m.h, yi);
         en = __ffma2_rn(m.nh, yi, p);
         two_sum2(s.hb, s.lb, p);
-        s.lb = __fadd2_rn(s.lb, neg2(en));
+        s.lb = fsub2(s.lb, en);
         s.lb = __ffma2_rn(m.l, yi, s.lb);
         s.lb = __ffma2_rn(m.h, bc(y.w), s.lb);
     }
