@@ -774,9 +774,10 @@ def run_large(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="cluster", choices=["cluster", "sweep", "serve", "large"],
+    ap.add_argument("--config", default="cluster", choices=["cluster", "sweep", "serve", "large", "multi_rhs"],
                     help="cluster: the headline N=200 cluster; sweep: the 256-wavelength Drude sweep; "
-                         "serve: the request stream through the solve server")
+                         "serve: the request stream through the solve server; multi_rhs: the headline cluster "
+                         "with R = 8 right-hand sides, tensor-core and CUDA-core matrix passes")
     ap.add_argument("--requests", type=int, default=48, help="requests in the serving stream")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -836,6 +837,17 @@ def main():
                         config=dict(workload=LARGE_WORKLOAD, solve_tol=TOL, rhs=1), **res)
             print(json.dumps(line))
         return
+    if args.config == "multi_rhs":
+        if rank == 0:
+            dev = torch.device("cuda", 0)
+            torch.cuda.set_device(dev)
+            res = run_multi_rhs(args, workload_inputs(), dev, peaks()[0])
+            line = dict(base, metric="source solves/s (R = 8 right-hand sides per cluster solve)", unit="solves/s",
+                        impl="gb300", value=res["tensor_core"]["source_solves_per_s"],
+                        dtype="split-bf16x3 tensor-core FP32 inner solves + double-float refinement residual",
+                        cpu_baseline=None, config=dict(workload=res["workload"], solve_tol=TOL, rhs=8), **res)
+            print(json.dumps(line))
+        return
     if args.config == "serve":
         if rank == 0:
             res = run_serve(args)
@@ -843,7 +855,8 @@ def main():
                         unit="solves/s", impl="gb300", dtype="c64 BiCGSTAB + double-float refinement residual",
                         data="synthetic (seeded request stream)", cpu_baseline=None,
                         config=dict(workload=SERVE_WORKLOAD, solve_tol=TOL, rhs=1,
-                                    batching="continuous (waves admitted by HBM budget, 3 concurrent streams)"),
+                                    batching=f"continuous (waves admitted by HBM budget and size class, "
+                                             f"{SERVE_WAVES} concurrent waves, stream priority by wave cost)"),
                         **res)
             print(json.dumps(line))
         return
