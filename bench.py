@@ -167,7 +167,8 @@ def run_gpu(args, rank, world):
     # ---- resident inputs
     batches = {p: ClusterBatch([spec], R=R, precision=p, device=dev) for p in ("mixed", "fp64")}
     # measured GEMV lane shapes (gb_autotune_gemv) before any solve captures its graphs
-    gemv_shapes = {p: {str(B): list(v) for B, v in b.autotune().items()} for p, b in batches.items()}
+    gemv_shapes = {p: {str(B): list(v) for B, v in (b.gemv_shapes() if args.no_autotune else b.autotune()).items()}
+                   for p, b in batches.items()}
     for p, b in batches.items():
         for _ in range(args.warmup):
             one_solve(b, p)
@@ -786,6 +787,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="leave the serving stream out of the headline run")
     ap.add_argument("--no-multi-rhs", action="store_true", help="leave the R=8 tensor-core leg out of the headline run")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="GEMV lane shapes from the model instead of measured ones (for runs under a profiler, "
+                         "whose timings would mislead the tuner)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

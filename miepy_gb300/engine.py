@@ -371,6 +371,15 @@ class ClusterBatch:
         nat.check(L.gb_autotune_gemv(self.nsys, self.sys, self.R, code, nat.ptr(self.mat128), nat.ptr(self.mat64),
                                      nat.ptr(self.tvec), nat.ptr(x), nat.ptr(y), nat.ptr(ws), ws.numel(), int(reps),
                                      current_stream(self.device)), "autotune")
+        return self.gemv_shapes(prec)
+
+    def gemv_shapes(self, precision=None):
+        """{B: (lanes per row, columns per lane)}: the GEMV lane shapes the matrix pass of
+        precision launches with for this batch's block sizes (measured ones after
+        autotune, the model's otherwise)."""
+        L = nat.lib()
+        prec = self.precision if precision is None else precision
+        code = PRECISIONS["fp64" if prec == "fp64" else "fp32"]
         out = {}
         for B in sorted({2 * l["rmax"] for l in self.layout if l["N"] > 1}):
             lpr, cpl = ctypes.c_int(0), ctypes.c_int(0)
