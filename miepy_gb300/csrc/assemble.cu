@@ -190,11 +190,10 @@ struct Latt {
 // lattice sums of a periodic cluster, added to a dense output (Latt).
 // Occupancy: the double-float (mixed) path fits five CTAs per SM in 48 registers
 // without spills; the FP64 paths keep three (at five they spill).
-// TS: tuple-stationary groups of the packed double-float path (lmax <= 4, one
-// tuple-value buffer per pair of the group, NB = PB): each thread loads its tuples'
-// indices and coefficients once and forms them for every pair of the group, then
-// every block of the group is written after one barrier, each element-map code read
-// once for all of them.
+// TS: whole-group phases on the packed double-float path (lmax <= 4, one tuple-value
+// buffer per pair of the group, NB = PB): the group's (tuple, pair) sums are spread
+// evenly over the threads, then every block of the group is written after one
+// barrier, each element-map code read once for all of them.
 template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false>
 __global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
@@ -203,7 +202,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
            Refl refl = Refl(), Latt latt = Latt()) {
     constexpr bool REFL = MODE == 1, LATT = MODE == 2;
     static_assert(MODE == 0 || (DENSE && FP64_SUMS), "reflection and lattice sums are dense FP64 outputs");
-    static_assert(!TS || (!DENSE && !FP64_SUMS && MODE == 0), "tuple-stationary groups serve the packed double-float path");
+    static_assert(!TS || (!DENSE && !FP64_SUMS && MODE == 0), "whole-group phases serve the packed double-float path");
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
@@ -339,7 +338,13 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             float2* P2 = reinterpret_cast<float2*>(Pl);      // same slots, (h, l)
             float4* eph2 = reinterpret_cast<float4*>(eph);   // same slots, (re.h, im.h, re.l, im.l)
             float4* hh2 = reinterpret_cast<float4*>(hh);
-            for (int it = tid; it < np * PM; it += kAsmThreads) {
+            // the three loops below are independent: when they fit, they run at once on
+            // disjoint thread ranges (P from thread 0, e^{i mu phi} from o1, h from o2)
+            const int n1 = np * PM, n2 = np * (2 * L + 1);
+            const int o1 = (n1 + 31) & ~31, o2 = o1 + ((n2 + 31) & ~31);
+            const bool split = o2 + n1 <= kAsmThreads;
+            const int t1 = split ? tid - o1 : tid, t2 = split ? tid - o2 : tid;
+            for (int it = tid; it < np * PM && (!split || it < o1); it += kAsmThreads) {
                 const int pp = it / PM, mu = it % PM;
                 const DF x = df_of(geo[8 * pp]), u = df_of(geo[8 * pp + 1]);
                 float2* P = P2 + (size_t)PMs * PMs * pp;
@@ -358,7 +363,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     }
                 }
             }
-            for (int it = tid; it < np * (2 * L + 1); it += kAsmThreads) {
+            for (int it = t1; it >= 0 && it < n2; it += kAsmThreads) {
                 const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
                 int e = mu;
                 DFC acc{DF{1.f, 0.f}, DF{0.f, 0.f}}, base{df_of(geo[8 * pp + 2]), df_of(geo[8 * pp + 3])};
@@ -370,7 +375,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 eph2[MUs * pp + 2 * L + mu] = dfc_pack(acc);
                 eph2[MUs * pp + 2 * L - mu] = dfc_pack(DFC{acc.re, df_neg(acc.im)});
             }
-            for (int it = tid; it < np * PM; it += kAsmThreads) {   // each thread rewrites its own slot
+            for (int it = t2; it >= 0 && it < n1; it += kAsmThreads) {   // each thread rewrites its own slot
                 const int pp = it / PM, q = it % PM;
                 const double2 hv = hh[PMs * pp + q];
                 hh2[PMs * pp + q] = dfc_pack(DFC{df_of(hv.x), df_of(hv.y)});
@@ -595,41 +600,42 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             continue;
         }
         if constexpr (TS) {
-            constexpr int QX = 5;   // lmax <= 4: at most 5 terms per sum
-            for (int t = tid; t < S.M; t += kAsmThreads) {
+            // the group's (tuple, pair) sums spread evenly over the threads: item it is
+            // tuple it % M of pair it / M
+            const int M = S.M;
+            int t = tid, pp = 0;
+            while (t >= M) { t -= M; pp++; }
+            for (; pp < np;) {
                 const int4 e = S.nmvu[t];
                 const int2 qq = S.qab[t];
                 const int mi = (e.w - e.y) + 2 * L;
                 const int nv = e.x + e.z;
                 const float2* ca = S.cA2 + (size_t)t * (L + 1);
                 const float2* cb = S.cB2 + (size_t)t * (L + 1);
-                float2 cav[QX], cbv[QX];
-                float nca[QX], ncb[QX];   // negated hi words, once per tuple
+                const float4* gp = G32 + (size_t)PMs * MUs * pp + (size_t)nv * MUs + mi;
+                float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
 #pragma unroll
-                for (int q = 0; q < QX; q++) {
-                    cav[q] = q <= qq.x ? ca[q] : make_float2(0.f, 0.f);
-                    cbv[q] = (q >= 1 && q <= qq.y) ? cb[q] : make_float2(0.f, 0.f);
-                    nca[q] = -cav[q].x;
-                    ncb[q] = -cbv[q].x;
-                }
-                for (int pp = 0; pp < np; pp++) {
-                    const float4* gp = G32 + (size_t)PMs * MUs * pp + (size_t)nv * MUs + mi;
-                    float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
-#pragma unroll
-                    for (int q = 0; q < QX; q++) {
-                        if (q <= qq.x) df_rc_fma(ah, al, cav[q].x, nca[q], cav[q].y, gp[-2 * q * MUs]);
-                        if (q >= 1 && q <= qq.y) df_rc_fma(bh, bl, cbv[q].x, ncb[q], cbv[q].y, gp[(1 - 2 * q) * MUs]);
+                for (int q = 0; q < 5; q++) {   // lmax <= 4: at most 5 terms per sum
+                    if (q <= qq.x) {
+                        const float2 c = ca[q];
+                        df_rc_fma(ah, al, c.x, -c.x, c.y, gp[-2 * q * MUs]);
                     }
-                    const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
-                    const float2 a2 = fsub2(al, fsub2(a1, ah));
-                    const float2 b2 = fsub2(bl, fsub2(b1, bh));
-                    float2* tf = Tf + (size_t)pp * 2 * Mb;
-                    float2* tl = Tl + (size_t)pp * 2 * Mb;
-                    tf[2 * t] = mul_ipowf(a1, nv);
-                    tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
-                    tl[2 * t] = mul_ipowf(a2, nv);
-                    tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
+                    if (q >= 1 && q <= qq.y) {
+                        const float2 c = cb[q];
+                        df_rc_fma(bh, bl, c.x, -c.x, c.y, gp[(1 - 2 * q) * MUs]);
+                    }
                 }
+                const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
+                const float2 a2 = fsub2(al, fsub2(a1, ah));
+                const float2 b2 = fsub2(bl, fsub2(b1, bh));
+                float2* tf = Tf + (size_t)pp * 2 * Mb;
+                float2* tl = Tl + (size_t)pp * 2 * Mb;
+                tf[2 * t] = mul_ipowf(a1, nv);
+                tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
+                tl[2 * t] = mul_ipowf(a2, nv);
+                tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
+                t += kAsmThreads;
+                while (t >= M) { t -= M; pp++; }
             }
             __syncthreads();
             const int BB = B * B;
@@ -876,7 +882,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= target ? 2 : 1;
         int PB = fp64_sums ? 32 : 4;
         while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > target) PB >>= 1;
-        // tuple-stationary groups (packed double-float, lmax <= 4): one buffer per pair,
+        // whole-group phases (packed double-float, lmax <= 4): one buffer per pair,
         // the most pairs up to 4 that keep the target
         bool ts = false;
         if (!dense && !refl && !latt && !fp64_sums && L <= 4) {

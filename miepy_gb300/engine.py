@@ -224,7 +224,10 @@ class ClusterBatch:
             raise ValueError("load() needs clusters of the batch's shapes (N, lmax per cluster)")
         if any(("tmatrix" in s) != self.tmatrix for s in specs):
             raise ValueError("load() needs clusters of the batch's kind (Mie coefficients or T-matrices)")
-        self._set_layout(specs)
+        # same shapes, so the same offsets: only the wavenumbers of the descriptors change
+        self.specs = specs
+        for i, sp in enumerate(specs):
+            self.sys[i].k = float(np.real(sp["k"]))
         self._upload(specs)
         return self
 
@@ -395,8 +398,13 @@ class ClusterBatch:
         dev = self.device
         n_obs = self.totals["obs"]
         ragged = any(l["lmax"] != self.xs_L for l in self.layout)
-        self.p_scat = torch.empty_like(self.x) if want_fields else None
-        self.p_int = torch.empty_like(self.x) if want_fields else None
+        # the batch's own output buffers, rewritten by every epilogue
+        if want_fields:
+            if getattr(self, "_p_scat_buf", None) is None:
+                self._p_scat_buf, self._p_int_buf = torch.empty_like(self.x), torch.empty_like(self.x)
+            self.p_scat, self.p_int = self._p_scat_buf, self._p_int_buf
+        else:
+            self.p_scat = self.p_int = None
         xs, F, T = self._xs_buf, self._f_buf, self._t_buf
         if ragged:   # rows of clusters with a smaller lmax keep zeros past 2 lmax
             xs.zero_()
