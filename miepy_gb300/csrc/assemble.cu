@@ -54,10 +54,12 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_su
     s.NB = NB;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 15) & ~size_t(15); return r; };
-    s.off_geo = take(sizeof(double) * 8 * PB);
-    s.off_h = take(sizeof(double2) * s.PM * PB);
-    s.off_e = take(sizeof(double2) * s.MU * PB);
-    s.off_P = take(sizeof(double) * s.PM * s.PM * PB);
+    // the double-float path reads its G tables (k_asm_gtab) and needs no special functions
+    const size_t sf = fp64_sums ? 1 : 0;
+    s.off_geo = take(sf * sizeof(double) * 8 * PB);
+    s.off_h = take(sf * sizeof(double2) * s.PM * PB);
+    s.off_e = take(sf * sizeof(double2) * s.MU * PB);
+    s.off_P = take(sf * sizeof(double) * s.PM * s.PM * PB);
     s.off_G = take(16 * (size_t)s.PM * s.MU * PB);          // double2 (FP64 sums) or float4 (double-float)
     s.off_T = take(fp64_sums ? sizeof(double2) * 2 * NB * M : 0);   // NB buffers of (A, B) per tuple
     s.off_Tf = take(want64 ? sizeof(float2) * 2 * NB * M : 0);
@@ -197,7 +199,7 @@ struct Latt {
 template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false>
 __global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
-           int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
+           long long g_begin, int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
            double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
            Refl refl = Refl(), Latt latt = Latt()) {
     constexpr bool REFL = MODE == 1, LATT = MODE == 2;
@@ -217,7 +219,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
     float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
     float2* Tl = reinterpret_cast<float2*>(smem + lay.off_Tl);
     const int PMs = lay.PM, MUs = lay.MU;   // launch-wide strides
-    for (long long g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    for (long long g = g_begin + blockIdx.x; g < ngroups; g += gridDim.x) {   // groups [g_begin, ngroups)
         const int s = find_sys(grp_base, nsys, g);
         const gb::SysDev S = sys[s];
         const int L = S.lmax, B = S.B, N = S.N;
@@ -236,11 +238,12 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             np = (int)min((long long)PB, Ptot - p_first);
         }
 
-        // ---- phase 1a: one thread per pair: geometry, then h_p(kr) by the upward
+        // ---- phase 1a (FP64 paths; the double-float path reads the G tables of
+        // k_asm_gtab): one thread per pair: geometry, then h_p(kr) by the upward
         // j/y recurrence of spherical_hn_recursion (cpp/src/special.cpp:90-111).  The
         // angles enter only through cos/sin of theta and phi, straight from the
         // separation vector (the reference goes through acos/atan2 and back).
-        if (tid < np) {
+        if (FP64_SUMS && tid < np) {
             int i, j;
             double lx = 0.0, ly = 0.0, lz = 0.0;   // lattice: the cell that holds the image of particle j
             if (LATT) {
@@ -298,11 +301,10 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 h[q] = make_double2(jn, yn);
             }
         }
-        __syncthreads();
+        if constexpr (FP64_SUMS) __syncthreads();
         // ---- phase 1b: P_q^mu(cos theta) (no Condon-Shortley phase), one thread per
         // (pair, mu); e^{i mu phi} by binary powering, one thread per (pair, mu >= 0).
-        // The mixed path computes both in double-float on the FP32 pipe and turns
-        // h_q into double-float in place; the FP64 path keeps FP64.
+        // The double-float path instead loads the group's G tables.
         if constexpr (FP64_SUMS) {
             for (int it = tid; it < np * PM; it += kAsmThreads) {
                 const int pp = it / PM, mu = it % PM;
@@ -335,56 +337,27 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 eph[MUs * pp + 2 * L - mu] = make_double2(acc.x, -acc.y);
             }
         } else {
-            float2* P2 = reinterpret_cast<float2*>(Pl);      // same slots, (h, l)
-            float4* eph2 = reinterpret_cast<float4*>(eph);   // same slots, (re.h, im.h, re.l, im.l)
-            float4* hh2 = reinterpret_cast<float4*>(hh);
-            // the three loops below are independent: when they fit, they run at once on
-            // disjoint thread ranges (P from thread 0, e^{i mu phi} from o1, h from o2)
-            const int n1 = np * PM, n2 = np * (2 * L + 1);
-            const int o1 = (n1 + 31) & ~31, o2 = o1 + ((n2 + 31) & ~31);
-            const bool split = o2 + n1 <= kAsmThreads;
-            const int t1 = split ? tid - o1 : tid, t2 = split ? tid - o2 : tid;
-            for (int it = tid; it < np * PM && (!split || it < o1); it += kAsmThreads) {
-                const int pp = it / PM, mu = it % PM;
-                const DF x = df_of(geo[8 * pp]), u = df_of(geo[8 * pp + 1]);
-                float2* P = P2 + (size_t)PMs * PMs * pp;
-                DF pmm{1.f, 0.f};
-                for (int kk = 1; kk <= mu; kk++) pmm = df_mulf(df_mul(pmm, u), (float)(2 * kk - 1));
-                P[mu * PMs + mu] = make_float2(pmm.h, pmm.l);
-                if (mu + 1 < PM) {
-                    DF pa = pmm, pb = df_mulf(df_mul(x, pmm), (float)(2 * mu + 1));
-                    P[(mu + 1) * PMs + mu] = make_float2(pb.h, pb.l);
-                    for (int q = mu + 2; q < PM; q++) {
-                        const DF t = df_add(df_mulf(df_mul(x, pb), (float)(2 * q - 1)), df_neg(df_mulf(pa, (float)(q + mu - 1))));
-                        const DF pc = df_divf(t, (float)(q - mu));
-                        P[q * PMs + mu] = make_float2(pc.h, pc.l);
-                        pa = pb;
-                        pb = pc;
-                    }
+            // the group's G tables, written by k_asm_gtab at the start of each pair's
+            // own block in the output plane (entry p^2 + p + mu for |mu| <= p, as (re.hi,
+            // im.hi), (re.lo, im.lo)); zeros where |mu| > p.  Read through L2 (the
+            // kernel overwrites these words later, after the barrier that ends the sums).
+            const float2* gsrc = out64lo ? out64lo : out64;
+            const long long BBl = (long long)B * B;
+            for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
+                const int pp = it / (PM * MU), rem = it - pp * (PM * MU);
+                const int q = rem / MU, mi = rem - q * MU, mu = mi - 2 * L;
+                float4 gv = make_float4(0.f, 0.f, 0.f, 0.f);
+                if ((mu < 0 ? -mu : mu) <= q) {
+                    const float2* src = gsrc + S.mat_off + (p_first + pp) * BBl + 2 * (q * q + q + mu);
+                    const float2 a = __ldcg(src), b = __ldcg(src + 1);
+                    gv = make_float4(a.x, a.y, b.x, b.y);
                 }
-            }
-            for (int it = t1; it >= 0 && it < n2; it += kAsmThreads) {
-                const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
-                int e = mu;
-                DFC acc{DF{1.f, 0.f}, DF{0.f, 0.f}}, base{df_of(geo[8 * pp + 2]), df_of(geo[8 * pp + 3])};
-                while (e) {
-                    if (e & 1) acc = dfc_mul(acc, base);
-                    base = dfc_mul(base, base);
-                    e >>= 1;
-                }
-                eph2[MUs * pp + 2 * L + mu] = dfc_pack(acc);
-                eph2[MUs * pp + 2 * L - mu] = dfc_pack(DFC{acc.re, df_neg(acc.im)});
-            }
-            for (int it = t2; it >= 0 && it < n1; it += kAsmThreads) {   // each thread rewrites its own slot
-                const int pp = it / PM, q = it % PM;
-                const double2 hv = hh[PMs * pp + q];
-                hh2[PMs * pp + q] = dfc_pack(DFC{df_of(hv.x), df_of(hv.y)});
+                G32[(size_t)PMs * MUs * pp + (size_t)q * MUs + mi] = gv;
             }
         }
         __syncthreads();
-        // ---- phase 1c: G[p][mu] = P_p^mu h_p e^{i mu phi} (negative mu through the
-        // (-1)^mu (p-mu)!/(p+mu)! ratio), FP64, or double-float for the mixed path
-        // (the ratio as a double-float mantissa and an exact binary scaling)
+        // ---- phase 1c (FP64 paths): G[p][mu] = P_p^mu h_p e^{i mu phi} (negative mu
+        // through the (-1)^mu (p-mu)!/(p+mu)! ratio)
         if constexpr (FP64_SUMS) {
             for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
                 const int pp = it / (PM * MU), rem = it % (PM * MU);
@@ -399,38 +372,8 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 }
                 G64[gi] = gval;
             }
-        } else {
-            // thread per (p, mu), looping over the group's pairs: the divisions and the
-            // negative-order ratio are per thread, not per entry (the group holds at
-            // most 4 pairs on this path)
-            for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
-                const int q = qm / MU, mi = qm - q * MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
-                float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (am <= q && mu < 0) r = S.neg_ratio2[q * PM + am];
-                for (int pp = 0; pp < np; pp++) {
-                    const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
-                    float4 gval = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (am <= q) {
-                        const float2 pv = reinterpret_cast<const float2*>(Pl)[(size_t)PMs * PMs * pp + q * PMs + am];
-                        DF P{pv.x, pv.y};
-                        if (mu < 0) {
-                            P = df_mul(P, DF{r.x, r.y});
-                            if (r.w != 0.f) {   // 2^e as a normal float: the scaling is one exact-rounded product
-                                P = DF{P.h * r.w, P.l * r.w};
-                            } else {
-                                const int ex = (int)r.z;
-                                P = DF{ldexpf(P.h, ex), ldexpf(P.l, ex)};
-                            }
-                        }
-                        const DFC he = dfc_mul(dfc_unpack(reinterpret_cast<const float4*>(hh)[PMs * pp + q]),
-                                               dfc_unpack(reinterpret_cast<const float4*>(eph)[MUs * pp + mi]));
-                        gval = dfc_pack(DFC{df_mul(P, he.re), df_mul(P, he.im)});
-                    }
-                    G32[gi] = gval;
-                }
-            }
+            __syncthreads();
         }
-        __syncthreads();
 
         // ---- phases 2 and 3, software-pipelined over the group's pairs: each thread
         // writes pair pp's block (phase 3) and then forms the tuple values of pair
@@ -442,11 +385,22 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             float2* tf = Tf + (size_t)buf * 2 * Mb;
             float2* tl = Tl + (size_t)buf * 2 * Mb;
             const int Q = L + 1;
-            for (int t = tid; t < S.M; t += kAsmThreads) {
-                const int4 e = S.nmvu[t];
-                const int2 qq = S.qab[t];
-                const int mi = (e.w - e.y) + 2 * L;
-                const int nv = e.x + e.z;
+            for (int it = tid; it < S.M; it += kAsmThreads) {
+                int t, mi, nv;
+                int2 qq;
+                if constexpr (FP64_SUMS) {
+                    t = it;
+                    const int4 e = S.nmvu[t];
+                    qq = S.qab[t];
+                    mi = (e.w - e.y) + 2 * L;
+                    nv = e.x + e.z;
+                } else {   // sorted order: the lanes of a warp run sums of equal length
+                    const int4 f = S.tinfo[it];
+                    t = f.x;
+                    nv = f.y;
+                    mi = f.z + 2 * L;
+                    qq = make_int2(f.w & 255, f.w >> 8);
+                }
                 if constexpr (FP64_SUMS) {
                     const double* ca = S.cA + (size_t)t * Q;
                     const double* cb = S.cB + (size_t)t * Q;
@@ -487,8 +441,8 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                         tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
                     }
                 } else {
-                    const float2* ca = S.cA2 + (size_t)t * Q;
-                    const float2* cb = S.cB2 + (size_t)t * Q;
+                    const float2* ca = S.cA2s + (size_t)it * Q;
+                    const float2* cb = S.cB2s + (size_t)it * Q;
                     float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
                     // the A and B sums interleaved: two independent double-float chains
                     const int qa = qq.x, qb = qq.y, qm = qa > qb ? qa : qb;
@@ -602,25 +556,27 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         if constexpr (TS) {
             // the group's (tuple, pair) sums spread evenly over the threads: item it is
             // tuple it % M of pair it / M
+            // (tuples in the sorted order of S.tinfo: the lanes of a warp run sums of
+            // equal length)
             const int M = S.M;
-            int t = tid, pp = 0;
-            while (t >= M) { t -= M; pp++; }
+            int i = tid, pp = 0;
+            while (i >= M) { i -= M; pp++; }
             for (; pp < np;) {
-                const int4 e = S.nmvu[t];
-                const int2 qq = S.qab[t];
-                const int mi = (e.w - e.y) + 2 * L;
-                const int nv = e.x + e.z;
-                const float2* ca = S.cA2 + (size_t)t * (L + 1);
-                const float2* cb = S.cB2 + (size_t)t * (L + 1);
+                const int4 f = S.tinfo[i];
+                const int t = f.x, nv = f.y, mi = f.z + 2 * L, qa = f.w & 255, qb = f.w >> 8;
+                const int qm = qa > qb ? qa : qb;
+                const float2* ca = S.cA2s + (size_t)i * (L + 1);
+                const float2* cb = S.cB2s + (size_t)i * (L + 1);
                 const float4* gp = G32 + (size_t)PMs * MUs * pp + (size_t)nv * MUs + mi;
                 float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
 #pragma unroll
                 for (int q = 0; q < 5; q++) {   // lmax <= 4: at most 5 terms per sum
-                    if (q <= qq.x) {
+                    if (q > qm) break;
+                    if (q <= qa) {
                         const float2 c = ca[q];
                         df_rc_fma(ah, al, c.x, -c.x, c.y, gp[-2 * q * MUs]);
                     }
-                    if (q >= 1 && q <= qq.y) {
+                    if (q >= 1 && q <= qb) {
                         const float2 c = cb[q];
                         df_rc_fma(bh, bl, c.x, -c.x, c.y, gp[(1 - 2 * q) * MUs]);
                     }
@@ -634,11 +590,35 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
                 tl[2 * t] = mul_ipowf(a2, nv);
                 tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
-                t += kAsmThreads;
-                while (t >= M) { t -= M; pp++; }
+                i += kAsmThreads;
+                while (i >= M) { i -= M; pp++; }
             }
             __syncthreads();
-            const int BB = B * B;
+            const int BB = B * B;   // even: B = 2 rmax
+            if ((S.mat_off & 1) == 0 && ((reinterpret_cast<size_t>(out64) | reinterpret_cast<size_t>(out64lo)) & 15) == 0) {
+                // two elements per thread and 16-byte streaming stores (the blocks are
+                // read by the next kernels from HBM: more than L2 holds)
+                for (int e2 = tid; e2 < BB / 2; e2 += kAsmThreads) {
+                    const int2 code = __ldg(reinterpret_cast<const int2*>(S.elem_map) + e2);
+                    const unsigned n0 = code.x & 1, n1 = code.y & 1;
+                    const int t0 = code.x >> 1, t1 = code.y >> 1;
+                    for (int pp = 0; pp < np; pp++) {
+                        const long long at = S.mat_off + (p_first + pp) * (long long)BB + 2 * e2;
+                        if (out64) {
+                            const float2 a = Tf[(size_t)pp * 2 * Mb + t0], b = Tf[(size_t)pp * 2 * Mb + t1];
+                            __stcs(reinterpret_cast<float4*>(out64 + at),
+                                   make_float4(flipf(a.x, n0), flipf(a.y, n0), flipf(b.x, n1), flipf(b.y, n1)));
+                        }
+                        if (out64lo) {
+                            const float2 a = Tl[(size_t)pp * 2 * Mb + t0], b = Tl[(size_t)pp * 2 * Mb + t1];
+                            __stcs(reinterpret_cast<float4*>(out64lo + at),
+                                   make_float4(flipf(a.x, n0), flipf(a.y, n0), flipf(b.x, n1), flipf(b.y, n1)));
+                        }
+                    }
+                }
+                __syncthreads();   // before the next group rewrites the tables and the buffers
+                continue;
+            }
             for (int el = tid; el < BB; el += kAsmThreads) {
                 const int code = __ldg(S.elem_map + el);
                 const unsigned neg = code & 1;
@@ -668,6 +648,171 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             }
             __syncthreads();
         }
+    }
+}
+
+// Special functions of the packed double-float path, for PG pairs per CTA with the
+// lanes of every phase busy (the assembler's groups hold only a few pairs, so these
+// serial recurrences would leave most of its lanes idle):
+//   A. one thread per pair: geometry and h_p(kr) by the upward j/y recurrence of
+//      spherical_hn_recursion (cpp/src/special.cpp:90-111) in FP64, kept as
+//      double-float;
+//   B. one thread per (pair, mu): P_p^mu(cos theta) (no Condon-Shortley phase) and
+//      e^{i mu phi} by binary powering, in double-float on the FP32 pipe
+//      (Joldes-Muller-Popescu operations);
+//   C. one thread per table entry: G[p][mu] = P_p^mu h_p e^{i mu phi} for |mu| <= p
+//      (negative mu through the (-1)^mu (p-mu)!/(p+mu)! ratio, held as a
+//      double-float mantissa and an exact binary scaling).
+// The table of pair p goes to the start of the pair's own block in the output plane
+// (entry p^2 + p + mu as (re.hi, im.hi), (re.lo, im.lo): (2 lmax + 2)^2 entries fit in
+// the B^2 words of a block at every lmax); the assembler CTA of the pair reads it back
+// before it writes that block.
+constexpr int kGtabThreads = 256;
+
+struct GtabSmem {
+    size_t off_geo, off_h, off_P, off_e, total;
+};
+
+__host__ __device__ inline GtabSmem gtab_layout(int L, int PG) {
+    const int PM = 2 * L + 2, MU = 4 * L + 1;
+    GtabSmem s;
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 15) & ~size_t(15); return r; };
+    s.off_geo = take(sizeof(double) * 4 * PG);             // cos theta, sin theta, cos phi, sin phi
+    s.off_h = take(sizeof(float4) * PM * PG);              // h_p as double-float complex
+    s.off_P = take(sizeof(float2) * PM * PM * PG);         // P_p^mu [pair][p][mu] as double-float
+    s.off_e = take(sizeof(float4) * MU * PG);              // e^{i mu phi}, mu = -2L..2L
+    s.total = o;
+    return s;
+}
+
+__global__ void __launch_bounds__(kGtabThreads)
+k_asm_gtab(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
+           long long h_begin, int PG, const double* __restrict__ pos, float2* __restrict__ plane) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const long long g = h_begin + blockIdx.x;   // groups [h_begin, ngroups)
+    if (g >= ngroups) return;
+    const int tid = threadIdx.x;
+    const int s = find_sys(grp_base, nsys, g);
+    const gb::SysDev S = sys[s];
+    const int L = S.lmax, N = S.N, PM = 2 * L + 2, MU = 4 * L + 1;
+    const long long BB = (long long)S.B * S.B;
+    const long long p_first = (g - grp_base[s]) * (long long)PG;
+    const int np = (int)min((long long)PG, S.P - p_first);
+    const GtabSmem lay = gtab_layout(L, PG);
+    double* geo = reinterpret_cast<double*>(smem + lay.off_geo);
+    float4* hh = reinterpret_cast<float4*>(smem + lay.off_h);
+    float2* Pl = reinterpret_cast<float2*>(smem + lay.off_P);
+    float4* eph = reinterpret_cast<float4*>(smem + lay.off_e);
+
+    // ---- A: geometry (the angles enter only through cos/sin of theta and phi, taken
+    // from the separation vector) and h_p(kr), one thread per pair
+    if (tid < np) {
+        int i, j;
+        pair_ij(p_first + tid, N, i, j);
+        const double* pi_ = pos + S.pos_off + 3 * (long long)i;
+        const double* pj_ = pos + S.pos_off + 3 * (long long)j;
+        const double dx = pi_[0] - pj_[0], dy = pi_[1] - pj_[1], dz = pi_[2] - pj_[2];
+        const double rho2 = dx * dx + dy * dy;
+        const double rad = sqrt(rho2 + dz * dz);
+        const double inv_r = 1.0 / rad;
+        const double rho = sqrt(rho2);
+        double cphi = 1.0, sphi = 0.0;                  // phi = atan2(dy, dx) = 0 on the z axis
+        if (rho2 > 0.0) {
+            const double inv_rho = 1.0 / rho;
+            cphi = dx * inv_rho;
+            sphi = dy * inv_rho;
+        }
+        double* ge = geo + 4 * tid;
+        ge[0] = dz * inv_r;
+        ge[1] = rho * inv_r;
+        ge[2] = cphi;
+        ge[3] = sphi;
+        const double z = S.k * rad;
+        const double inv_z = 1.0 / z;
+        double sz, cz;
+        sincos(z, &sz, &cz);
+        double j0 = sz * inv_z, y0 = -cz * inv_z;
+        double j1 = j0 * inv_z + y0, y1 = y0 * inv_z - j0;
+        float4* h = hh + PM * tid;
+        h[0] = dfc_pack(DFC{df_of(j0), df_of(y0)});
+        h[1] = dfc_pack(DFC{df_of(j1), df_of(y1)});
+        for (int q = 2; q < PM; q++) {
+            const double f = (2 * q - 1) * inv_z;
+            const double jn = f * j1 - j0;
+            const double yn = f * y1 - y0;
+            j0 = j1; j1 = jn; y0 = y1; y1 = yn;
+            h[q] = dfc_pack(DFC{df_of(jn), df_of(yn)});
+        }
+    }
+    __syncthreads();
+    // ---- B: P_q^mu (threads from 0) and e^{i mu phi} (threads from o1, a warp
+    // boundary, so that no warp mixes the two recurrences)
+    {
+        const int n1 = np * PM, n2 = np * (2 * L + 1);
+        const int o1 = (n1 + 31) & ~31;
+        for (int it = tid; it < o1 + n2; it += kGtabThreads) {
+            if (it < n1) {
+                const int pp = it / PM, mu = it - pp * PM;
+                const DF x = df_of(geo[4 * pp]), u = df_of(geo[4 * pp + 1]);
+                float2* P = Pl + (size_t)PM * PM * pp;
+                DF pmm{1.f, 0.f};
+                for (int kk = 1; kk <= mu; kk++) pmm = df_mulf(df_mul(pmm, u), (float)(2 * kk - 1));
+                P[mu * PM + mu] = make_float2(pmm.h, pmm.l);
+                if (mu + 1 < PM) {
+                    DF pa = pmm, pb = df_mulf(df_mul(x, pmm), (float)(2 * mu + 1));
+                    P[(mu + 1) * PM + mu] = make_float2(pb.h, pb.l);
+                    for (int q = mu + 2; q < PM; q++) {
+                        const DF t = df_add(df_mulf(df_mul(x, pb), (float)(2 * q - 1)), df_neg(df_mulf(pa, (float)(q + mu - 1))));
+                        const DF pc = df_divf(t, (float)(q - mu));
+                        P[q * PM + mu] = make_float2(pc.h, pc.l);
+                        pa = pb;
+                        pb = pc;
+                    }
+                }
+            } else if (it >= o1) {
+                const int k = it - o1, pp = k / (2 * L + 1), mu = k - pp * (2 * L + 1);
+                int e = mu;
+                DFC acc{DF{1.f, 0.f}, DF{0.f, 0.f}}, base{df_of(geo[4 * pp + 2]), df_of(geo[4 * pp + 3])};
+                while (e) {
+                    if (e & 1) acc = dfc_mul(acc, base);
+                    base = dfc_mul(base, base);
+                    e >>= 1;
+                }
+                eph[MU * pp + 2 * L + mu] = dfc_pack(acc);
+                eph[MU * pp + 2 * L - mu] = dfc_pack(DFC{acc.re, df_neg(acc.im)});
+            }
+        }
+    }
+    __syncthreads();
+    // ---- C: the table entries, one thread per (pair, p, mu), |mu| <= p; orders
+    // |mu| > 2L (only at p = 2L + 1) occur in no tuple sum and are left out (e^{i mu
+    // phi} is held for |mu| <= 2L only)
+    const int PM2 = PM * PM;
+    for (int it = tid; it < np * PM2; it += kGtabThreads) {
+        const int pp = it / PM2, r = it - pp * PM2;
+        int q = (int)sqrtf((float)r);
+        if ((q + 1) * (q + 1) <= r) q++;
+        if (q * q > r) q--;
+        const int mu = r - q * q - q, am = mu < 0 ? -mu : mu;
+        if (am > 2 * L) continue;
+        const float2 pv = Pl[(size_t)PM2 * pp + q * PM + am];
+        DF P{pv.x, pv.y};
+        if (mu < 0) {
+            const float4 rr = S.neg_ratio2[q * PM + am];
+            P = df_mul(P, DF{rr.x, rr.y});
+            if (rr.w != 0.f) {   // 2^e as a normal float: the scaling is one exact-rounded product
+                P = DF{P.h * rr.w, P.l * rr.w};
+            } else {
+                const int ex = (int)rr.z;
+                P = DF{ldexpf(P.h, ex), ldexpf(P.l, ex)};
+            }
+        }
+        const DFC he = dfc_mul(dfc_unpack(hh[PM * pp + q]), dfc_unpack(eph[MU * pp + 2 * L + mu]));
+        const DFC G{df_mul(P, he.re), df_mul(P, he.im)};
+        float2* dst = plane + S.mat_off + (p_first + pp) * BB + 2 * r;
+        dst[0] = make_float2(G.re.h, G.im.h);
+        dst[1] = make_float2(G.re.l, G.im.l);
     }
 }
 
@@ -728,6 +873,9 @@ int make_sysdev(int nsys, const gb_system* sys, cudaStream_t stream, std::vector
         d.cB = T->cB;
         d.cA2 = T->cA2;
         d.cB2 = T->cB2;
+        d.tinfo = T->tinfo;
+        d.cA2s = T->cA2s;
+        d.cB2s = T->cB2s;
         d.elem_map = T->elem_map;
         d.neg_ratio = T->neg_ratio;
         d.neg_ratio2 = T->neg_ratio2;
@@ -907,10 +1055,18 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
             gbase[s + 1] = gbase[s] + (latt ? (long long)sd[s].N * sd[s].N * lt.gpp : (np_s + PB - 1) / PB);
         }
         const long long ngroups = gbase[ns];
-        // one staging upload: descriptors then group prefix sums
-        std::vector<unsigned char> blob(sizeof(gb::SysDev) * ns + sizeof(long long) * (ns + 1));
+        // the double-float path's G-table pass: PG pairs per CTA (the most, up to 32,
+        // whose special functions fit in 48 KB of shared memory)
+        int PG = 32;
+        while (PG > 1 && gtab_layout(L, PG).total > 48 * 1024) PG >>= 1;
+        std::vector<long long> gbase2(ns + 1, 0);
+        for (int s = 0; s < ns; s++) gbase2[s + 1] = gbase2[s] + (fp64_sums ? 0 : (sd[s].P + PG - 1) / PG);
+        // one staging upload: descriptors, then the group prefix sums of both passes
+        std::vector<unsigned char> blob(sizeof(gb::SysDev) * ns + 2 * sizeof(long long) * (ns + 1));
         memcpy(blob.data(), sd.data(), sizeof(gb::SysDev) * ns);
         memcpy(blob.data() + sizeof(gb::SysDev) * ns, gbase.data(), sizeof(long long) * (ns + 1));
+        memcpy(blob.data() + sizeof(gb::SysDev) * ns + sizeof(long long) * (ns + 1), gbase2.data(),
+               sizeof(long long) * (ns + 1));
         void* dblob = nullptr;
         int slot = 0;
         st = gb::stage_acquire(blob.data(), blob.size(), stream, &dblob, &slot);
@@ -918,6 +1074,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         const gb::SysDev* dsys = reinterpret_cast<const gb::SysDev*>(dblob);
         const long long* dbase =
             reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * ns);
+
         auto kfn = latt ? k_assemble<true, true, 2>
                         : refl ? k_assemble<true, true, 1>
                                : (dense ? k_assemble<true, true>
@@ -931,13 +1088,27 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         // one group per CTA (no persistent loop): CTAs retire every few microseconds, so
         // kernels of higher-priority streams (other clusters' solves) are dispatched
         // between them instead of waiting for the whole assembly
-        const long long grid = std::min<long long>(ngroups, 0x7fffffffLL);
-        gb::note_launch();
-        kfn<<<(unsigned)grid, kAsmThreads, smem, stream>>>(
-            dsys, ns, dbase, ngroups, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),
-            reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
-            dense_ld, refl ? *refl : Refl(), lt);
-        GB_CUDA_TRY(cudaGetLastError());
+        auto main_pass = [&](long long g0, long long g1) -> cudaError_t {
+            if (g1 <= g0) return cudaSuccess;
+            gb::note_launch();
+            kfn<<<(unsigned)std::min<long long>(g1 - g0, 0x7fffffffLL), kAsmThreads, smem, stream>>>(
+                dsys, ns, dbase, g1, g0, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),
+                reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64),
+                reinterpret_cast<float2*>(out64lo), dense_ld, refl ? *refl : Refl(), lt);
+            return cudaGetLastError();
+        };
+        if (!fp64_sums && gbase2[ns] > 0) {
+            // the G tables first (read back by the assembler CTA of each pair).  Running
+            // them in chunks on a second stream beside the assembler measured slower
+            // (0.232 ms with two chunks against 0.210 ms in one stream at N = 200, lmax 4).
+            const size_t gsm = gtab_layout(L, PG).total;
+            GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(k_asm_gtab), gsm));
+            gb::note_launch();
+            k_asm_gtab<<<(unsigned)std::min<long long>(gbase2[ns], 0x7fffffffLL), kGtabThreads, gsm, stream>>>(
+                dsys, ns, dbase + (ns + 1), gbase2[ns], 0, PG, pos, reinterpret_cast<float2*>(out64lo ? out64lo : out64));
+            GB_CUDA_TRY(cudaGetLastError());
+        }
+        GB_CUDA_TRY(main_pass(0, ngroups));
         st = gb::stage_release(slot, stream);
         if (st) return st;
     }

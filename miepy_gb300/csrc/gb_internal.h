@@ -18,6 +18,12 @@ struct Tables {
     double* cB = nullptr;      // [M][lmax+1]
     float2* cA2 = nullptr;     // [M][lmax+1] (hi, lo) split of cA
     float2* cB2 = nullptr;     // [M][lmax+1] (hi, lo) split of cB
+    // the tuples in order of (qmax_A, qmax_B) descending, so that the lanes of a warp
+    // run sums of equal length: (t, n + v, u - m, qmax_A | qmax_B << 8) and the (hi,
+    // lo) coefficients in that order
+    int4* tinfo = nullptr;     // [M]
+    float2* cA2s = nullptr;    // [M][lmax+1]
+    float2* cB2s = nullptr;    // [M][lmax+1]
     int* elem_map = nullptr;   // [B*B] (tuple << 2) | (is_B << 1) | negate
     double* neg_ratio = nullptr;   // [(2L+2)^2] (-1)^mu (p-mu)!/(p+mu)!
     float4* neg_ratio2 = nullptr;  // the same as (m.hi, m.lo, e, s): ratio = (m.hi + m.lo) 2^e, m in [0.5, 1), s = 2^e if normal else 0
@@ -66,6 +72,9 @@ struct SysDev {
     const double* cB;
     const float2* cA2;
     const float2* cB2;
+    const int4* tinfo;
+    const float2* cA2s;
+    const float2* cB2s;
     const int* elem_map;
     const double* neg_ratio;
     const float4* neg_ratio2;

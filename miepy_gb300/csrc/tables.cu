@@ -152,6 +152,16 @@ __global__ void k_split_coeffs(int n, const double* __restrict__ cA, const doubl
     cB2[e] = make_float2(bh, __double2float_rn(cB[e] - (double)bh));
 }
 
+// The coefficient tables in the sorted tuple order of tinfo.
+__global__ void k_perm_coeffs(int M, int Q, const int4* __restrict__ tinfo, const float2* __restrict__ cA2,
+                              const float2* __restrict__ cB2, float2* __restrict__ cA2s, float2* __restrict__ cB2s) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M * Q) return;
+    const int i = e / Q, q = e - i * Q, t = tinfo[i].x;
+    cA2s[e] = cA2[(size_t)t * Q + q];
+    cB2s[e] = cB2[(size_t)t * Q + q];
+}
+
 }   // namespace
 
 namespace gb {
@@ -225,6 +235,18 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
                 rowinfo[R] = rho | (eps_neg << 29) | (sig_neg << 30);
                 miecol[R] = a * L + n - 1;
             }
+    // sorted tuple order: the sum lengths of k_tuple_table, longest first
+    std::vector<int4> tinfo(M);
+    for (int t = 0; t < M; t++) {
+        const int n = nmvu[t].x, m = -nmvu[t].y, v = nmvu[t].z, u = nmvu[t].w;
+        const int qA = std::min(std::min(n, v), (n + v - std::abs(m + u)) / 2);
+        const int qB = std::min(std::min(n, v), (n + v + 1 - std::abs(m + u)) / 2);
+        tinfo[t] = make_int4(t, n + v, nmvu[t].w - nmvu[t].y, qA | (qB << 8));
+    }
+    std::stable_sort(tinfo.begin(), tinfo.end(), [](const int4& a, const int4& b) {
+        const int la = a.w & 255, lb = b.w & 255;
+        return la != lb ? la > lb : (a.w >> 8) > (b.w >> 8);
+    });
     Tables* T = new Tables();
     T->lmax = L;
     T->M = M;
@@ -237,6 +259,9 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     if (e == cudaSuccess) e = cudaMalloc(&T->cB, sizeof(double) * M * Q);
     if (e == cudaSuccess) e = cudaMalloc(&T->cA2, sizeof(float2) * M * Q);
     if (e == cudaSuccess) e = cudaMalloc(&T->cB2, sizeof(float2) * M * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&T->tinfo, sizeof(int4) * M);
+    if (e == cudaSuccess) e = cudaMalloc(&T->cA2s, sizeof(float2) * M * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&T->cB2s, sizeof(float2) * M * Q);
     if (e == cudaSuccess) e = cudaMalloc(&T->elem_map, sizeof(int) * B * B);
     if (e == cudaSuccess) e = cudaMalloc(&T->neg_ratio, sizeof(double) * PM * PM);
     if (e == cudaSuccess) e = cudaMalloc(&T->neg_ratio2, sizeof(float4) * PM * PM);
@@ -244,6 +269,7 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     if (e == cudaSuccess) e = cudaMalloc(&T->miecol, sizeof(int) * B);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->nmvu, nmvu.data(), sizeof(int4) * M, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(T->elem_map, map.data(), sizeof(int) * B * B, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T->tinfo, tinfo.data(), sizeof(int4) * M, cudaMemcpyHostToDevice, stream);
     // double-float mantissa and binary exponent: the ratios reach 1/(2p)!, below the
     // FP32 range, while ratio * P_p^mu stays moderate
     std::vector<float4> negr2(negr.size());
@@ -269,10 +295,16 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
         k_split_coeffs<<<(M * Q + 255) / 256, 256, 0, stream>>>(M * Q, T->cA, T->cB, T->cA2, T->cB2);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess) {
+        gb::note_launch();
+        k_perm_coeffs<<<(M * Q + 255) / 256, 256, 0, stream>>>(M, Q, T->tinfo, T->cA2, T->cB2, T->cA2s, T->cB2s);
+        e = cudaGetLastError();
+    }
     // the host vectors above go out of scope: make the copies complete first
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
         cudaFree(T->nmvu); cudaFree(T->qab); cudaFree(T->cA); cudaFree(T->cB); cudaFree(T->cA2); cudaFree(T->cB2);
+        cudaFree(T->tinfo); cudaFree(T->cA2s); cudaFree(T->cB2s);
         cudaFree(T->elem_map); cudaFree(T->neg_ratio); cudaFree(T->neg_ratio2); cudaFree(T->rowinfo); cudaFree(T->miecol);
         delete T;
         return gb_set_cuda_error(e, "building translation tables", __FILE__, __LINE__);

@@ -135,6 +135,32 @@ def test_packed_operator_matches_oracle_matvec(N, lmax, R):
     assert rel(ydf, ref) < 1e-12       # double-float hi + lo
 
 
+def test_double_float_planes_match_fp64_blocks():
+    """The mixed path's hi + lo planes (G tables from the special-function pass,
+    tuple sums in double-float) against the FP64 path's complex128 blocks, in one
+    ragged batch over lmax 1..8: 1e-12 relative to each block's largest entry."""
+    rng = np.random.default_rng(7)
+    shapes = [(5, 1), (7, 2), (12, 3), (30, 4), (9, 4), (9, 5), (5, 6), (4, 7), (4, 8)]
+    specs = []
+    for N, lmax in shapes:
+        pos, _ = random_cluster(rng, N, 40 * nm, 80 * nm, 1500 * nm)
+        rmax = lmax * (lmax + 2)
+        specs.append(dict(position=pos, mie_scat=np.ones((N, 2, lmax), complex), k=2 * np.pi / (rng.uniform(450, 900) * nm),
+                          p_src=np.ones((N, 2, rmax, 1), complex)))
+    b = ClusterBatch(specs, R=1, precision="fp64").assemble()
+    bm = ClusterBatch(specs, R=1, precision="mixed").assemble()
+    torch.cuda.synchronize()
+    m128 = b.mat128.cpu().numpy()
+    mdf = bm.mat64.cpu().numpy().astype(np.complex128) + bm.mat64lo.cpu().numpy().astype(np.complex128)
+    for lay, lay_m in zip(b.layout, bm.layout):
+        N, B = lay["N"], 2 * lay["rmax"]
+        P = N * (N - 1) // 2
+        ref = m128[lay["mat_off"]: lay["mat_off"] + P * B * B].reshape(P, B * B)
+        got = mdf[lay_m["mat_off"]: lay_m["mat_off"] + P * B * B].reshape(P, B * B)
+        err = np.max(np.abs(got - ref), axis=1) / np.max(np.abs(ref), axis=1)
+        assert err.max() < 1e-12, (N, lay["lmax"], err.max())
+
+
 # ------------------------------------------------------------------ solves --
 @pytest.mark.parametrize("name", G.EXACT_CASES)
 def test_fp64_solve_matches_exact_reference(name):
