@@ -678,7 +678,7 @@ __host__ __device__ inline GtabSmem gtab_layout(int L, int PG) {
     GtabSmem s;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 15) & ~size_t(15); return r; };
-    s.off_geo = take(sizeof(double) * 4 * PG);             // cos theta, sin theta, cos phi, sin phi
+    s.off_geo = take(sizeof(float2) * 4 * PG);             // cos theta, sin theta, cos phi, sin phi (double-float)
     s.off_h = take(sizeof(float4) * PM * PG);              // h_p as double-float complex
     s.off_P = take(sizeof(float2) * PM * PM * PG);         // P_p^mu [pair][p][mu] as double-float
     s.off_e = take(sizeof(float4) * MU * PG);              // e^{i mu phi}, mu = -2L..2L
@@ -700,7 +700,7 @@ k_asm_gtab(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
     const long long p_first = (g - grp_base[s]) * (long long)PG;
     const int np = (int)min((long long)PG, S.P - p_first);
     const GtabSmem lay = gtab_layout(L, PG);
-    double* geo = reinterpret_cast<double*>(smem + lay.off_geo);
+    float2* geo = reinterpret_cast<float2*>(smem + lay.off_geo);
     float4* hh = reinterpret_cast<float4*>(smem + lay.off_h);
     float2* Pl = reinterpret_cast<float2*>(smem + lay.off_P);
     float4* eph = reinterpret_cast<float4*>(smem + lay.off_e);
@@ -723,38 +723,46 @@ k_asm_gtab(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             cphi = dx * inv_rho;
             sphi = dy * inv_rho;
         }
-        double* ge = geo + 4 * tid;
-        ge[0] = dz * inv_r;
-        ge[1] = rho * inv_r;
-        ge[2] = cphi;
-        ge[3] = sphi;
+        float2* ge = geo + 4 * tid;   // converted once here, not in every (pair, mu) thread
+        const DF ct = df_of(dz * inv_r), st = df_of(rho * inv_r), cp = df_of(cphi), sp = df_of(sphi);
+        ge[0] = make_float2(ct.h, ct.l);
+        ge[1] = make_float2(st.h, st.l);
+        ge[2] = make_float2(cp.h, cp.l);
+        ge[3] = make_float2(sp.h, sp.l);
         const double z = S.k * rad;
         const double inv_z = 1.0 / z;
         double sz, cz;
         sincos(z, &sz, &cz);
         double j0 = sz * inv_z, y0 = -cz * inv_z;
         double j1 = j0 * inv_z + y0, y1 = y0 * inv_z - j0;
-        float4* h = hh + PM * tid;
-        h[0] = dfc_pack(DFC{df_of(j0), df_of(y0)});
-        h[1] = dfc_pack(DFC{df_of(j1), df_of(y1)});
+        // FP64 here; turned into double-float in place by the threads of phase B
+        double2* h = reinterpret_cast<double2*>(hh) + PM * tid;
+        h[0] = make_double2(j0, y0);
+        h[1] = make_double2(j1, y1);
         for (int q = 2; q < PM; q++) {
             const double f = (2 * q - 1) * inv_z;
             const double jn = f * j1 - j0;
             const double yn = f * y1 - y0;
             j0 = j1; j1 = jn; y0 = y1; y1 = yn;
-            h[q] = dfc_pack(DFC{df_of(jn), df_of(yn)});
+            h[q] = make_double2(jn, yn);
         }
     }
     __syncthreads();
-    // ---- B: P_q^mu (threads from 0) and e^{i mu phi} (threads from o1, a warp
-    // boundary, so that no warp mixes the two recurrences)
+    // ---- B: P_q^mu (threads from 0), e^{i mu phi} (threads from o1) and h_p into
+    // double-float (threads from o2; o1 and o2 on warp boundaries, so that no warp
+    // mixes two of the three)
     {
         const int n1 = np * PM, n2 = np * (2 * L + 1);
-        const int o1 = (n1 + 31) & ~31;
-        for (int it = tid; it < o1 + n2; it += kGtabThreads) {
+        const int o1 = (n1 + 31) & ~31, o2 = o1 + ((n2 + 31) & ~31);
+        for (int it = tid; it < o2 + n1; it += kGtabThreads) {
+            if (it >= o2) {   // each thread rewrites its own 16-byte slot
+                const double2 hv = reinterpret_cast<const double2*>(hh)[it - o2];
+                hh[it - o2] = dfc_pack(DFC{df_of(hv.x), df_of(hv.y)});
+                continue;
+            }
             if (it < n1) {
                 const int pp = it / PM, mu = it - pp * PM;
-                const DF x = df_of(geo[4 * pp]), u = df_of(geo[4 * pp + 1]);
+                const DF x{geo[4 * pp].x, geo[4 * pp].y}, u{geo[4 * pp + 1].x, geo[4 * pp + 1].y};
                 float2* P = Pl + (size_t)PM * PM * pp;
                 DF pmm{1.f, 0.f};
                 for (int kk = 1; kk <= mu; kk++) pmm = df_mulf(df_mul(pmm, u), (float)(2 * kk - 1));
@@ -770,10 +778,11 @@ k_asm_gtab(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                         pb = pc;
                     }
                 }
-            } else if (it >= o1) {
+            } else if (it >= o1 && it < o1 + n2) {
                 const int k = it - o1, pp = k / (2 * L + 1), mu = k - pp * (2 * L + 1);
                 int e = mu;
-                DFC acc{DF{1.f, 0.f}, DF{0.f, 0.f}}, base{df_of(geo[4 * pp + 2]), df_of(geo[4 * pp + 3])};
+                DFC acc{DF{1.f, 0.f}, DF{0.f, 0.f}}, base{DF{geo[4 * pp + 2].x, geo[4 * pp + 2].y},
+                                                          DF{geo[4 * pp + 3].x, geo[4 * pp + 3].y}};
                 while (e) {
                     if (e & 1) acc = dfc_mul(acc, base);
                     base = dfc_mul(base, base);
@@ -785,34 +794,47 @@ k_asm_gtab(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         }
     }
     __syncthreads();
-    // ---- C: the table entries, one thread per (pair, p, mu), |mu| <= p; orders
-    // |mu| > 2L (only at p = 2L + 1) occur in no tuple sum and are left out (e^{i mu
-    // phi} is held for |mu| <= 2L only)
-    const int PM2 = PM * PM;
-    for (int it = tid; it < np * PM2; it += kGtabThreads) {
-        const int pp = it / PM2, r = it - pp * PM2;
-        int q = (int)sqrtf((float)r);
-        if ((q + 1) * (q + 1) <= r) q++;
-        if (q * q > r) q--;
-        const int mu = r - q * q - q, am = mu < 0 ? -mu : mu;
-        if (am > 2 * L) continue;
-        const float2 pv = Pl[(size_t)PM2 * pp + q * PM + am];
-        DF P{pv.x, pv.y};
-        if (mu < 0) {
+    // ---- C: the table entries, one thread per (pair, p, |mu|) with |mu| <= min(p,
+    // 2L) (orders |mu| > 2L, only at p = 2L + 1, occur in no tuple sum; e^{i mu phi}
+    // is held for |mu| <= 2L): G(p, +-|mu|) from the four products of h_p and
+    // e^{i|mu|phi}, h e = (t1 - t2, t3 + t4) and h conj(e) = (t1 + t2, t4 - t3)
+    const int TRI = (2 * L + 1) * (2 * L + 2) / 2;   // entries with p <= 2L
+    const int NE = TRI + 2 * L + 1;                 // and p = 2L + 1, |mu| <= 2L
+    for (int it = tid; it < np * NE; it += kGtabThreads) {
+        const int pp = it / NE, r2 = it - pp * NE;
+        int q, am;
+        if (r2 < TRI) {
+            q = (int)((sqrtf(8.f * (float)r2 + 1.f) - 1.f) * 0.5f);
+            if ((q + 1) * (q + 2) / 2 <= r2) q++;
+            if (q * (q + 1) / 2 > r2) q--;
+            am = r2 - q * (q + 1) / 2;
+        } else {
+            q = 2 * L + 1;
+            am = r2 - TRI;
+        }
+        const float2 pv = Pl[(size_t)PM * PM * pp + q * PM + am];
+        const DF P{pv.x, pv.y};
+        const DFC h = dfc_unpack(hh[PM * pp + q]), e = dfc_unpack(eph[MU * pp + 2 * L + am]);
+        const DF t1 = df_mul(h.re, e.re), t2 = df_mul(h.im, e.im), t3 = df_mul(h.re, e.im), t4 = df_mul(h.im, e.re);
+        float2* dst = plane + S.mat_off + (p_first + pp) * BB + 2 * (q * q + q);
+        {
+            const DF gr = df_mul(P, df_add(t1, df_neg(t2))), gi = df_mul(P, df_add(t3, t4));
+            dst[2 * am] = make_float2(gr.h, gi.h);
+            dst[2 * am + 1] = make_float2(gr.l, gi.l);
+        }
+        if (am > 0) {   // mu = -|mu|: (-1)^mu (p-mu)!/(p+mu)! P_p^|mu| h_p e^{-i|mu|phi}
             const float4 rr = S.neg_ratio2[q * PM + am];
-            P = df_mul(P, DF{rr.x, rr.y});
+            DF Pn = df_mul(P, DF{rr.x, rr.y});
             if (rr.w != 0.f) {   // 2^e as a normal float: the scaling is one exact-rounded product
-                P = DF{P.h * rr.w, P.l * rr.w};
+                Pn = DF{Pn.h * rr.w, Pn.l * rr.w};
             } else {
                 const int ex = (int)rr.z;
-                P = DF{ldexpf(P.h, ex), ldexpf(P.l, ex)};
+                Pn = DF{ldexpf(Pn.h, ex), ldexpf(Pn.l, ex)};
             }
+            const DF gr = df_mul(Pn, df_add(t1, t2)), gi = df_mul(Pn, df_add(t4, df_neg(t3)));
+            dst[-2 * am] = make_float2(gr.h, gi.h);
+            dst[-2 * am + 1] = make_float2(gr.l, gi.l);
         }
-        const DFC he = dfc_mul(dfc_unpack(hh[PM * pp + q]), dfc_unpack(eph[MU * pp + 2 * L + mu]));
-        const DFC G{df_mul(P, he.re), df_mul(P, he.im)};
-        float2* dst = plane + S.mat_off + (p_first + pp) * BB + 2 * r;
-        dst[0] = make_float2(G.re.h, G.im.h);
-        dst[1] = make_float2(G.re.l, G.im.l);
     }
 }
 
