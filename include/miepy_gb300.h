@@ -105,7 +105,10 @@ int gb_aggregate_periodic_dense(int N, int lmax, const double* pos, const double
 
 /* Packed pair-block translation matrix of one cluster (see above).  Any
  * output may be NULL: out128 [P*B*B] c128; out64 [P*B*B] c64 = fl32(a);
- * out64lo [P*B*B] c64 = fl32(a - fl32(a)) (hi + lo carries ~48 bits). */
+ * out64lo [P*B*B] c64 = fl32(a - fl32(a)) (hi + lo carries ~48 bits).  Without
+ * out128 the complex64 outputs are built in double-float by two launches, and the
+ * first 2(2 lmax + 2)^2 words of each pair's block (in out64lo, else out64) hold
+ * that pair's special-function table until its block is written. */
 int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, double* out128, float* out64,
                               float* out64lo, void* stream);
 
@@ -122,8 +125,9 @@ typedef struct {
     int64_t t_off;      /* into the per-row Mie factor vector (complex128): first of D */
 } gb_system;
 
-/* Assemble the packed matrices of every cluster in the batch (one launch);
- * outputs as for gb_assemble_sphere_packed, any may be NULL. */
+/* Assemble the packed matrices of every cluster in the batch (one launch per
+ * lmax, preceded by the special-function launch without mat128); outputs as for
+ * gb_assemble_sphere_packed, any may be NULL. */
 int gb_assemble_batch(int nsys, const gb_system* sys, const double* pos, double* mat128, float* mat64,
                       float* mat64lo, void* stream);
 
