@@ -475,6 +475,26 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             const int BB = B * B;
             if (!DENSE) {
                 const long long base = S.mat_off + p * (long long)BB;
+                if (!FP64_SUMS && (base & 1) == 0 &&
+                    ((reinterpret_cast<size_t>(out64) | reinterpret_cast<size_t>(out64lo)) & 15) == 0) {
+                    // two elements per thread, 16-byte streaming stores (BB is even)
+                    for (int e2 = tid; e2 < BB / 2; e2 += kAsmThreads) {
+                        const int2 code = __ldg(reinterpret_cast<const int2*>(S.elem_map) + e2);
+                        const unsigned n0 = code.x & 1, n1 = code.y & 1;
+                        const int t0 = code.x >> 1, t1 = code.y >> 1;
+                        if (out64) {
+                            const float2 a = tf[t0], b = tf[t1];
+                            __stcs(reinterpret_cast<float4*>(out64 + base) + e2,
+                                   make_float4(flipf(a.x, n0), flipf(a.y, n0), flipf(b.x, n1), flipf(b.y, n1)));
+                        }
+                        if (out64lo) {
+                            const float2 a = tl[t0], b = tl[t1];
+                            __stcs(reinterpret_cast<float4*>(out64lo + base) + e2,
+                                   make_float4(flipf(a.x, n0), flipf(a.y, n0), flipf(b.x, n1), flipf(b.y, n1)));
+                        }
+                    }
+                    return;
+                }
                 for (int e = tid; e < BB; e += kAsmThreads) {
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
