@@ -161,6 +161,37 @@ def test_double_float_planes_match_fp64_blocks():
         assert err.max() < 1e-12, (N, lay["lmax"], err.max())
 
 
+def test_packed_assembly_at_odd_offsets():
+    """The packed double-float assembly through gb_assemble_batch with the clusters'
+    blocks at odd element offsets (8-byte aligned, so the block writes take the
+    one-element path) equals the same assembly at aligned offsets, bit for bit, at
+    lmax 4 (whole-group path) and lmax 6 (pair-by-pair path)."""
+    rng = np.random.default_rng(11)
+    L = nat.lib()
+    dev = torch.device("cuda", 0)
+    for N, lmax in [(7, 4), (5, 6)]:
+        pos, _ = random_cluster(rng, N, 40 * nm, 80 * nm, 1200 * nm)
+        B = 2 * lmax * (lmax + 2)
+        P = N * (N - 1) // 2
+        n = P * B * B
+        k = 2 * np.pi / (600 * nm)
+        dpos = torch.from_numpy(np.concatenate([pos.reshape(-1), pos.reshape(-1)])).to(dev)
+        outs = []
+        for base in (0, 1):
+            # two copies of the cluster: the second at mat_off = n + 2 + base
+            sysv = nat.systems_array([(N, lmax, k, 0, base, 0, 0), (N, lmax, k, 3 * N, n + 2 + base, 0, 0)])
+            hi = torch.full((2 * n + 4,), float("nan"), dtype=torch.complex64, device=dev)
+            lo = torch.full_like(hi, float("nan"))
+            nat.check(L.gb_assemble_batch(2, sysv, nat.ptr(dpos), None, nat.ptr(hi), nat.ptr(lo), current_stream(dev)))
+            torch.cuda.synchronize()
+            outs.append([(t[base: base + n].clone(), t[n + 2 + base: 2 * n + 2 + base].clone()) for t in (hi, lo)])
+        for plane in range(2):
+            for cl in range(2):
+                a, b = outs[0][plane][cl], outs[1][plane][cl]
+                assert torch.equal(a.view(torch.int64), b.view(torch.int64)), (N, lmax, plane, cl)
+        assert torch.equal(outs[0][0][0].view(torch.int64), outs[0][0][1].view(torch.int64))   # both copies alike
+
+
 # ------------------------------------------------------------------ solves --
 @pytest.mark.parametrize("name", G.EXACT_CASES)
 def test_fp64_solve_matches_exact_reference(name):
