@@ -9,9 +9,11 @@
 //      Condon-Shortley phase, GSL_SF_LEGENDRE_NONE convention), one thread per
 //      (pair, mu); e^{i mu phi} by powering e^{i phi}.  The angles enter only
 //      through cos/sin of theta and phi, taken directly from the separation vector;
-//   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p) (FP64, or for the
-//      mixed path double-float on the FP32 pipe, with h_p from FP64);
-// then per pair, software-pipelined over the group:
+//   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p), in FP64.
+// The packed double-float (mixed) path instead takes steps 1-2 from a separate pass,
+// k_asm_gtab (below), with 32 pairs per CTA, and loads the group's G tables;
+// then per pair, software-pipelined over the group (or, at lmax <= 4, for the whole
+// group at once):
 //   3. one thread per canonical tuple: A_t, B_t as real x complex FMA sums over
 //      the per-lmax coefficient table (tables.cu);
 //   4. coalesced block write: every entry of the B x B block looks up its tuple and
@@ -199,7 +201,7 @@ struct Latt {
 template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false>
 __global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
-           long long g_begin, int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
+           int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
            double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
            Refl refl = Refl(), Latt latt = Latt()) {
     constexpr bool REFL = MODE == 1, LATT = MODE == 2;
@@ -219,7 +221,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
     float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
     float2* Tl = reinterpret_cast<float2*>(smem + lay.off_Tl);
     const int PMs = lay.PM, MUs = lay.MU;   // launch-wide strides
-    for (long long g = g_begin + blockIdx.x; g < ngroups; g += gridDim.x) {   // groups [g_begin, ngroups)
+    for (long long g = blockIdx.x; g < ngroups; g += gridDim.x) {
         const int s = find_sys(grp_base, nsys, g);
         const gb::SysDev S = sys[s];
         const int L = S.lmax, B = S.B, N = S.N;
@@ -708,9 +710,9 @@ __host__ __device__ inline GtabSmem gtab_layout(int L, int PG) {
 
 __global__ void __launch_bounds__(kGtabThreads)
 k_asm_gtab(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
-           long long h_begin, int PG, const double* __restrict__ pos, float2* __restrict__ plane) {
+           int PG, const double* __restrict__ pos, float2* __restrict__ plane) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const long long g = h_begin + blockIdx.x;   // groups [h_begin, ngroups)
+    const long long g = blockIdx.x;
     if (g >= ngroups) return;
     const int tid = threadIdx.x;
     const int s = find_sys(grp_base, nsys, g);
@@ -1130,15 +1132,6 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         // one group per CTA (no persistent loop): CTAs retire every few microseconds, so
         // kernels of higher-priority streams (other clusters' solves) are dispatched
         // between them instead of waiting for the whole assembly
-        auto main_pass = [&](long long g0, long long g1) -> cudaError_t {
-            if (g1 <= g0) return cudaSuccess;
-            gb::note_launch();
-            kfn<<<(unsigned)std::min<long long>(g1 - g0, 0x7fffffffLL), kAsmThreads, smem, stream>>>(
-                dsys, ns, dbase, g1, g0, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),
-                reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64),
-                reinterpret_cast<float2*>(out64lo), dense_ld, refl ? *refl : Refl(), lt);
-            return cudaGetLastError();
-        };
         if (!fp64_sums && gbase2[ns] > 0) {
             // the G tables first (read back by the assembler CTA of each pair).  Running
             // them in chunks on a second stream beside the assembler measured slower
@@ -1147,10 +1140,15 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
             GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(k_asm_gtab), gsm));
             gb::note_launch();
             k_asm_gtab<<<(unsigned)std::min<long long>(gbase2[ns], 0x7fffffffLL), kGtabThreads, gsm, stream>>>(
-                dsys, ns, dbase + (ns + 1), gbase2[ns], 0, PG, pos, reinterpret_cast<float2*>(out64lo ? out64lo : out64));
+                dsys, ns, dbase + (ns + 1), gbase2[ns], PG, pos, reinterpret_cast<float2*>(out64lo ? out64lo : out64));
             GB_CUDA_TRY(cudaGetLastError());
         }
-        GB_CUDA_TRY(main_pass(0, ngroups));
+        gb::note_launch();
+        kfn<<<(unsigned)std::min<long long>(ngroups, 0x7fffffffLL), kAsmThreads, smem, stream>>>(
+            dsys, ns, dbase, ngroups, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),
+            reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
+            dense_ld, refl ? *refl : Refl(), lt);
+        GB_CUDA_TRY(cudaGetLastError());
         st = gb::stage_release(slot, stream);
         if (st) return st;
     }
