@@ -152,14 +152,17 @@ __global__ void k_split_coeffs(int n, const double* __restrict__ cA, const doubl
     cB2[e] = make_float2(bh, __double2float_rn(cB[e] - (double)bh));
 }
 
-// The coefficient tables in the sorted tuple order of tinfo.
-__global__ void k_perm_coeffs(int M, int Q, const int4* __restrict__ tinfo, const float2* __restrict__ cA2,
-                              const float2* __restrict__ cB2, float2* __restrict__ cA2s, float2* __restrict__ cB2s) {
+// The coefficient tables in the sorted tuple order of tinfo; the sum lengths of tinfo
+// are set from the device's own qab (the host's copy only orders the tuples).
+__global__ void k_perm_coeffs(int M, int Q, int* __restrict__ tinfo, const int2* __restrict__ qab,
+                              const float2* __restrict__ cA2, const float2* __restrict__ cB2,
+                              float2* __restrict__ cA2s, float2* __restrict__ cB2s) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= M * Q) return;
-    const int i = e / Q, q = e - i * Q, t = tinfo[i].x;
+    const int i = e / Q, q = e - i * Q, t = tinfo[4 * i];   // word 0 of the int4: the tuple
     cA2s[e] = cA2[(size_t)t * Q + q];
     cB2s[e] = cB2[(size_t)t * Q + q];
+    if (q == 0) tinfo[4 * i + 3] = qab[t].x | (qab[t].y << 8);   // word 3: the sum lengths
 }
 
 }   // namespace
@@ -297,7 +300,8 @@ int get_tables(int lmax, cudaStream_t stream, const Tables** out) {
     }
     if (e == cudaSuccess) {
         gb::note_launch();
-        k_perm_coeffs<<<(M * Q + 255) / 256, 256, 0, stream>>>(M, Q, T->tinfo, T->cA2, T->cB2, T->cA2s, T->cB2s);
+        k_perm_coeffs<<<(M * Q + 255) / 256, 256, 0, stream>>>(M, Q, reinterpret_cast<int*>(T->tinfo), T->qab, T->cA2,
+                                                                T->cB2, T->cA2s, T->cB2s);
         e = cudaGetLastError();
     }
     // the host vectors above go out of scope: make the copies complete first
