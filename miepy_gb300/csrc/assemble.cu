@@ -676,14 +676,15 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
 // Special functions of the packed double-float path, for PG pairs per CTA with the
 // lanes of every phase busy (the assembler's groups hold only a few pairs, so these
 // serial recurrences would leave most of its lanes idle):
-//   A. one thread per pair: geometry and h_p(kr) by the upward j/y recurrence of
-//      spherical_hn_recursion (cpp/src/special.cpp:90-111) in FP64, kept as
-//      double-float;
+//   A. one thread per pair: geometry (turned into double-float once) and h_p(kr) by
+//      the upward j/y recurrence of spherical_hn_recursion (cpp/src/special.cpp:
+//      90-111) in FP64;
 //   B. one thread per (pair, mu): P_p^mu(cos theta) (no Condon-Shortley phase) and
 //      e^{i mu phi} by binary powering, in double-float on the FP32 pipe
-//      (Joldes-Muller-Popescu operations);
-//   C. one thread per table entry: G[p][mu] = P_p^mu h_p e^{i mu phi} for |mu| <= p
-//      (negative mu through the (-1)^mu (p-mu)!/(p+mu)! ratio, held as a
+//      (Joldes-Muller-Popescu operations), and one per (pair, p) turning h_p into
+//      double-float, on disjoint warps;
+//   C. one thread per (pair, p, |mu|): G[p][+-mu] = P_p^|mu| h_p e^{+-i|mu|phi} for
+//      |mu| <= p (negative mu through the (-1)^mu (p-mu)!/(p+mu)! ratio, held as a
 //      double-float mantissa and an exact binary scaling).
 // The table of pair p goes to the start of the pair's own block in the output plane
 // (entry p^2 + p + mu as (re.hi, im.hi), (re.lo, im.lo): (2 lmax + 2)^2 entries fit in
