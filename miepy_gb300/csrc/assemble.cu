@@ -47,7 +47,8 @@ struct AsmSmem {
     size_t off_geo, off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
 };
 
-__host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_sums, bool want64, int NB) {
+__host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_sums, bool want64, int NB,
+                                               bool split = false) {
     AsmSmem s;
     s.PM = 2 * L + 2;
     s.MU = 4 * L + 1;
@@ -63,9 +64,10 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_su
     s.off_e = take(sf * sizeof(double2) * s.MU * PB);
     s.off_P = take(sf * sizeof(double) * s.PM * s.PM * PB);
     s.off_G = take(16 * (size_t)s.PM * s.MU * PB);          // double2 (FP64 sums) or float4 (double-float)
-    s.off_T = take(fp64_sums ? sizeof(double2) * 2 * NB * M : 0);   // NB buffers of (A, B) per tuple
-    s.off_Tf = take(want64 ? sizeof(float2) * 2 * NB * M : 0);
-    s.off_Tl = take(want64 ? sizeof(float2) * 2 * NB * M : 0);
+    const size_t kinds = split ? 1 : 2;   // (A, B) per tuple, or one of them at a time
+    s.off_T = take(fp64_sums ? sizeof(double2) * kinds * NB * M : 0);   // NB buffers of tuple values
+    s.off_Tf = take(want64 ? sizeof(float2) * kinds * NB * M : 0);
+    s.off_Tl = take(want64 ? sizeof(float2) * kinds * NB * M : 0);
     s.total = o;
     return s;
 }
@@ -198,7 +200,10 @@ struct Latt {
 // buffer per pair of the group, NB = PB): the group's (tuple, pair) sums are spread
 // evenly over the threads, then every block of the group is written after one
 // barrier, each element-map code read once for all of them.
-template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false>
+// SPLIT (MODE 0, one pair per group, one buffer): where one pair's A and B tuple
+// values do not fit in shared memory together (lmax 10), the A sums are formed and
+// their block elements written, then the B sums and theirs.
+template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false, bool SPLIT = false>
 __global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
            int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
@@ -207,10 +212,11 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
     constexpr bool REFL = MODE == 1, LATT = MODE == 2;
     static_assert(MODE == 0 || (DENSE && FP64_SUMS), "reflection and lattice sums are dense FP64 outputs");
     static_assert(!TS || (!DENSE && !FP64_SUMS && MODE == 0), "whole-group phases serve the packed double-float path");
+    static_assert(!SPLIT || (MODE == 0 && !TS), "split sums serve the pair-by-pair path of the aggregate");
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
-    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE, NB);
+    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE, NB, SPLIT);
     double* geo = reinterpret_cast<double*>(smem + lay.off_geo);        // [PB][8]
     double2* hh = reinterpret_cast<double2*>(smem + lay.off_h);         // [PB][PM]
     double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);        // [PB][MU]
@@ -381,11 +387,15 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // writes pair pp's block (phase 3) and then forms the tuple values of pair
         // pp + 1 (phase 2) into the other buffer, one barrier per pair.
         const int Mb = lay.M;   // tuple-buffer stride (launch-wide)
-        auto tuples = [&](int pp, int buf) {
+        constexpr int KINDS = SPLIT ? 1 : 2;
+        // slot of tuple t's value of kind k (0: A, 1: B); kind 2 below means both
+        auto slot = [](int t, int k) { return SPLIT ? t : 2 * t + k; };
+        auto tuples = [&](int pp, int buf, int kind) {
             const size_t gbase = (size_t)PMs * MUs * pp;
-            double2* tv = Tv + (size_t)buf * 2 * Mb;
-            float2* tf = Tf + (size_t)buf * 2 * Mb;
-            float2* tl = Tl + (size_t)buf * 2 * Mb;
+            double2* tv = Tv + (size_t)buf * KINDS * Mb;
+            float2* tf = Tf + (size_t)buf * KINDS * Mb;
+            float2* tl = Tl + (size_t)buf * KINDS * Mb;
+            const bool wantA = kind != 1, wantB = kind != 0;
             const int Q = L + 1;
             for (int it = tid; it < S.M; it += kAsmThreads) {
                 int t, mi, nv;
@@ -407,13 +417,13 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     const double* ca = S.cA + (size_t)t * Q;
                     const double* cb = S.cB + (size_t)t * Q;
                     double2 sa = make_double2(0.0, 0.0), sb = make_double2(0.0, 0.0);
-                    for (int q = 0; q <= qq.x; q++) {
+                    for (int q = 0; wantA && q <= qq.x; q++) {
                         const double c = ca[q];
                         const double2 gv = G64[gbase + (size_t)(nv - 2 * q) * MUs + mi];
                         sa.x = fma(c, gv.x, sa.x);
                         sa.y = fma(c, gv.y, sa.y);
                     }
-                    for (int q = 1; q <= qq.y; q++) {
+                    for (int q = 1; wantB && q <= qq.y; q++) {
                         const double c = cb[q];
                         const double2 gv = G64[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi];
                         sb.x = fma(c, gv.x, sb.x);
@@ -431,16 +441,22 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                             Tv[2 * t + 1] = make_double2(Tv[2 * t + 1].x + b.x, Tv[2 * t + 1].y + b.y);
                         }
                     } else {
-                        tv[2 * t] = At;
-                        tv[2 * t + 1] = Bt;
+                        if (wantA) tv[slot(t, 0)] = At;
+                        if (wantB) tv[slot(t, 1)] = Bt;
                     }
                     if (!DENSE && want64) {
                         const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
                         const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
-                        tf[2 * t] = ah;
-                        tf[2 * t + 1] = bh;
-                        tl[2 * t] = make_float2(__double2float_rn(At.x - (double)ah.x), __double2float_rn(At.y - (double)ah.y));
-                        tl[2 * t + 1] = make_float2(__double2float_rn(Bt.x - (double)bh.x), __double2float_rn(Bt.y - (double)bh.y));
+                        if (wantA) {
+                            tf[slot(t, 0)] = ah;
+                            tl[slot(t, 0)] = make_float2(__double2float_rn(At.x - (double)ah.x),
+                                                         __double2float_rn(At.y - (double)ah.y));
+                        }
+                        if (wantB) {
+                            tf[slot(t, 1)] = bh;
+                            tl[slot(t, 1)] = make_float2(__double2float_rn(Bt.x - (double)bh.x),
+                                                         __double2float_rn(Bt.y - (double)bh.y));
+                        }
                     }
                 } else {
                     const float2* ca = S.cA2s + (size_t)it * Q;
@@ -449,11 +465,11 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     // the A and B sums interleaved: two independent double-float chains
                     const int qa = qq.x, qb = qq.y, qm = qa > qb ? qa : qb;
                     for (int q = 0; q <= qm; q++) {
-                        if (q <= qa) {
+                        if (wantA && q <= qa) {
                             const float2 c = ca[q];
                             df_rc_fma(ah, al, c.x, -c.x, c.y, G32[gbase + (size_t)(nv - 2 * q) * MUs + mi]);
                         }
-                        if (q >= 1 && q <= qb) {
+                        if (wantB && q >= 1 && q <= qb) {
                             const float2 c = cb[q];
                             df_rc_fma(bh, bl, c.x, -c.x, c.y, G32[gbase + (size_t)(nv - 2 * q + 1) * MUs + mi]);
                         }
@@ -462,22 +478,30 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     const float2 a1 = __fadd2_rn(ah, al), b1 = __fadd2_rn(bh, bl);
                     const float2 a2 = fsub2(al, fsub2(a1, ah));
                     const float2 b2 = fsub2(bl, fsub2(b1, bh));
-                    tf[2 * t] = mul_ipowf(a1, nv);
-                    tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
-                    tl[2 * t] = mul_ipowf(a2, nv);
-                    tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
+                    if (wantA) {
+                        tf[slot(t, 0)] = mul_ipowf(a1, nv);
+                        tl[slot(t, 0)] = mul_ipowf(a2, nv);
+                    }
+                    if (wantB) {
+                        tf[slot(t, 1)] = mul_ipowf(b1, nv + 1);
+                        tl[slot(t, 1)] = mul_ipowf(b2, nv + 1);
+                    }
                 }
             }
         };
-        auto write_block = [&](int pp, int buf) {
+        // the block elements of kind `kind` (2: all); element code (t << 2) | (is_B << 1)
+        // | negate, its value at slot(t, is_B)
+        auto write_block = [&](int pp, int buf, int kind) {
             const long long p = p_first + pp;
-            const double2* tv = Tv + (size_t)buf * 2 * Mb;
-            const float2* tf = Tf + (size_t)buf * 2 * Mb;
-            const float2* tl = Tl + (size_t)buf * 2 * Mb;
+            const double2* tv = Tv + (size_t)buf * KINDS * Mb;
+            const float2* tf = Tf + (size_t)buf * KINDS * Mb;
+            const float2* tl = Tl + (size_t)buf * KINDS * Mb;
             const int BB = B * B;
+            auto at = [&](int code) { return slot(code >> 2, (code >> 1) & 1); };
+            auto skip = [&](int code) { return SPLIT && ((code >> 1) & 1) != kind; };
             if (!DENSE) {
                 const long long base = S.mat_off + p * (long long)BB;
-                if (!FP64_SUMS && (base & 1) == 0 &&
+                if (!SPLIT && !FP64_SUMS && (base & 1) == 0 &&
                     ((reinterpret_cast<size_t>(out64) | reinterpret_cast<size_t>(out64lo)) & 15) == 0) {
                     // two elements per thread, 16-byte streaming stores (BB is even)
                     for (int e2 = tid; e2 < BB / 2; e2 += kAsmThreads) {
@@ -499,17 +523,18 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 }
                 for (int e = tid; e < BB; e += kAsmThreads) {
                     const int code = __ldg(S.elem_map + e);
+                    if (skip(code)) continue;
                     const unsigned neg = code & 1;
                     if (FP64_SUMS && out128) {
-                        const double2 v = tv[code >> 1];
+                        const double2 v = tv[at(code)];
                         out128[base + e] = make_double2(flipd(v.x, neg), flipd(v.y, neg));
                     }
                     if (out64) {
-                        const float2 v = tf[code >> 1];
+                        const float2 v = tf[at(code)];
                         out64[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
                     }
                     if (out64lo) {
-                        const float2 v = tl[code >> 1];
+                        const float2 v = tl[at(code)];
                         out64lo[base + e] = make_float2(flipf(v.x, neg), flipf(v.y, neg));
                     }
                 }
@@ -541,8 +566,9 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 for (int e = tid; e < BB; e += kAsmThreads) {
                     const int R = e / B, C = e % B;
                     const int code = __ldg(S.elem_map + e);
+                    if (skip(code)) continue;
                     const unsigned neg = code & 1;
-                    double2 v = tv[code >> 1];
+                    double2 v = tv[at(code)];
                     v = make_double2(flipd(v.x, neg), flipd(v.y, neg));
                     const int col = __ldg(S.miecol + C);
                     const double2 vij = cmul(v, mj_[col]);
@@ -557,7 +583,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         if constexpr (LATT) {
             // every thread sums its own tuples over the group's cells, then the group's
             // share of block (i, j), times mie(j, b, v), is added to the dense output
-            for (int pp = 0; pp < np; pp++) tuples(pp, 0);
+            for (int pp = 0; pp < np; pp++) tuples(pp, 0, 2);
             __syncthreads();
             const int i = (int)(lat_pair / N), j = (int)(lat_pair % N);
             const double2* mj_ = mie + (long long)j * 2 * L;
@@ -660,13 +686,23 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             __syncthreads();   // before the next group rewrites the tables and the buffers
             continue;
         }
-        tuples(0, 0);
+        if constexpr (SPLIT) {   // one pair, one buffer: the A values and elements, then the B ones
+            for (int pp = 0; pp < np; pp++)
+                for (int kind = 0; kind < 2; kind++) {
+                    tuples(pp, 0, kind);
+                    __syncthreads();
+                    write_block(pp, 0, kind);
+                    __syncthreads();
+                }
+            continue;
+        }
+        tuples(0, 0, 2);
         __syncthreads();
         for (int pp = 0; pp < np; pp++) {
-            write_block(pp, NB == 2 ? (pp & 1) : 0);   // reads buffer pp & 1 (or the one buffer)
+            write_block(pp, NB == 2 ? (pp & 1) : 0, 2);   // reads buffer pp & 1 (or the one buffer)
             if (pp + 1 < np) {
                 if (NB == 1) __syncthreads();   // one buffer: every read of it done before it is refilled
-                tuples(pp + 1, NB == 2 ? ((pp + 1) & 1) : 0);
+                tuples(pp + 1, NB == 2 ? ((pp + 1) & 1) : 0, 2);
             }
             __syncthreads();
         }
@@ -1086,7 +1122,11 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
                 PB = NB = pb;
             }
         }
-        const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB);
+        // one pair's A and B tuple values together beyond a CTA's shared memory (lmax 10):
+        // the split kernel forms and writes them one kind at a time
+        const bool split = !ts && !refl && !latt && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > 227 * 1024;
+        if (split) PB = NB = 1;
+        const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB, split);
         const size_t smem = lay.total;
         if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
         Latt lt = latt ? *latt : Latt();
@@ -1122,10 +1162,13 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
 
         auto kfn = latt ? k_assemble<true, true, 2>
                         : refl ? k_assemble<true, true, 1>
-                               : (dense ? k_assemble<true, true>
-                                        : (fp64_sums ? k_assemble<false, true>
-                                                     : (ts ? k_assemble<false, false, 0, true>
-                                                           : k_assemble<false, false>)));
+                               : split ? (dense ? k_assemble<true, true, 0, false, true>
+                                                : (fp64_sums ? k_assemble<false, true, 0, false, true>
+                                                             : k_assemble<false, false, 0, false, true>))
+                                       : (dense ? k_assemble<true, true>
+                                                : (fp64_sums ? k_assemble<false, true>
+                                                             : (ts ? k_assemble<false, false, 0, true>
+                                                                   : k_assemble<false, false>)));
         GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
         int per_sm = 1;
         GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));

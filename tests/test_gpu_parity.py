@@ -46,7 +46,7 @@ def random_cluster(rng, N, rmin, rmax_, box):
 
 
 # ------------------------------------------------------------------ tables --
-@pytest.mark.parametrize("lmax", [1, 2, 4, 6, 8])
+@pytest.mark.parametrize("lmax", [1, 2, 4, 6, 8, 10])
 def test_translation_tables_match_oracle_cache(lmax):
     L = nat.lib()
     M = ctypes.c_int(0)
@@ -102,7 +102,7 @@ def test_dense_assembly_matches_reference(name):
     assert rel(T, ref) < 1e-12
 
 
-@pytest.mark.parametrize("N,lmax,seed", [(7, 3, 1), (4, 8, 2), (12, 1, 3), (9, 5, 4)])
+@pytest.mark.parametrize("N,lmax,seed", [(7, 3, 1), (4, 8, 2), (12, 1, 3), (9, 5, 4), (3, 9, 5), (3, 10, 6)])
 def test_dense_assembly_matches_oracle_random(N, lmax, seed):
     rng = np.random.default_rng(seed)
     pos, _ = random_cluster(rng, N, 50 * nm, 90 * nm, 1200 * nm)
@@ -110,7 +110,10 @@ def test_dense_assembly_matches_oracle_random(N, lmax, seed):
     k = 2 * np.pi / (600 * nm)
     T = dense_on_device(pos, mie, k, lmax)
     ref = O.sphere_aggregate_tmatrix(pos, mie.reshape(N, -1), k)
-    assert rel(T, ref) < 1e-12
+    # lmax 9 and 10: the Gaunt coefficients of orders up to 20 and the Hankel and
+    # Legendre recurrences to order 21 part between the two sides' methods by more
+    # than at lmax <= 8; held to the translation tables' own 1e-10
+    assert rel(T, ref) < (1e-12 if lmax <= 8 else 1e-10)
 
 
 @pytest.mark.parametrize("N,lmax,R", [(6, 3, 1), (5, 4, 2), (3, 8, 2), (25, 2, 1), (40, 3, 2)])
@@ -138,9 +141,10 @@ def test_packed_operator_matches_oracle_matvec(N, lmax, R):
 def test_double_float_planes_match_fp64_blocks():
     """The mixed path's hi + lo planes (G tables from the special-function pass,
     tuple sums in double-float) against the FP64 path's complex128 blocks, in one
-    ragged batch over lmax 1..8: 1e-12 relative to each block's largest entry."""
+    ragged batch over lmax 1..10 (at lmax 10 both paths form the A and B sums in two
+    passes): 1e-12 relative to each block's largest entry."""
     rng = np.random.default_rng(7)
-    shapes = [(5, 1), (7, 2), (12, 3), (30, 4), (9, 4), (9, 5), (5, 6), (4, 7), (4, 8)]
+    shapes = [(5, 1), (7, 2), (12, 3), (30, 4), (9, 4), (9, 5), (5, 6), (4, 7), (4, 8), (3, 9), (3, 10)]
     specs = []
     for N, lmax in shapes:
         pos, _ = random_cluster(rng, N, 40 * nm, 80 * nm, 1500 * nm)
