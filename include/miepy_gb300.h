@@ -117,9 +117,10 @@ int gb_assemble_sphere_packed(int N, int lmax, const double* pos, double k, doub
  * launch sequence.  Offsets are in elements of the respective device arrays. */
 typedef struct {
     int32_t N;          /* particles */
-    int32_t lmax;       /* expansion order, 1..10 (at 10 an assembly writing complex128 and
-                         * complex64 outputs in one call needs more than a CTA's 227 KB of
-                         * shared memory: GB_UNSUPPORTED) */
+    int32_t lmax;       /* expansion order: 1..10 for assembly (at 10 an assembly writing
+                         * complex128 and complex64 outputs in one call needs more than a
+                         * CTA's 227 KB of shared memory: GB_UNSUPPORTED), 1..8 for the
+                         * packed solvers (larger orders solve on the dense operator) */
     double k;           /* medium wavenumber */
     int64_t pos_off;    /* into pos (doubles): first of 3*N */
     int64_t mat_off;    /* into the packed matrices (complex elements): first of P*B*B */
