@@ -179,8 +179,8 @@ class sphere_cluster:
                     p_src=self.p_src)
         prec = self.precision if self.interactions else "fp64"
         b = ClusterBatch([spec], R=1, precision=prec, device=self.device)
-        if self.interactions and (self.interface is not None or self.symmetry is not None):
-            self._solve_dense(b)
+        if self.interactions and (self.interface is not None or self.symmetry is not None or self.lmax > 8):
+            self._solve_dense(b)   # (the packed solvers take lmax <= 8)
         elif self.interactions and self.Nparticles > 1:
             b.assemble()
             b.solve(tol=self._tolerance(), maxiter=self.maxiter or DEFAULT_MAXITER,
@@ -213,13 +213,14 @@ class sphere_cluster:
         or with a periodic symmetry the aggregate plus its lattice sums
         (gb_aggregate_periodic_dense), minus the interface's reflection matrix
         (gb_reflection_matrix_dense) when there is one; BiCGSTAB (gb_solve_dense),
-        run to 1e-14 for solver.exact.  These operators are not symmetric in their
-        pair blocks, so they are solved in FP64 whatever `precision` says (with a
-        warning when it says otherwise)."""
+        run to 1e-14 for solver.exact.  The interface and lattice operators are not
+        symmetric in their pair blocks, and the packed solvers take lmax <= 8, so these
+        are solved in FP64 whatever `precision` says (with a warning when it says
+        otherwise)."""
         L = nat.lib()
         if self.precision != "fp64":
-            warnings.warn(f"precision={self.precision!r} does not apply to clusters with an interface or a periodic "
-                          "symmetry: their dense operator is solved in FP64", stacklevel=3)
+            warnings.warn(f"precision={self.precision!r} does not apply to clusters with an interface, a periodic "
+                          "symmetry or lmax > 8: their dense operator is solved in FP64", stacklevel=3)
         dev, st = b.device, current_stream(b.device)
         md = self.material_data
         N, D = self.Nparticles, 2 * self.rmax * self.Nparticles

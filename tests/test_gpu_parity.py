@@ -196,6 +196,23 @@ def test_packed_assembly_at_odd_offsets():
         assert torch.equal(outs[0][0][0].view(torch.int64), outs[0][0][1].view(torch.int64))   # both copies alike
 
 
+def test_cluster_lmax9_on_the_dense_operator():
+    """A cluster of lmax 9 (beyond the packed solvers' lmax 8) through the public API
+    solves on the dense operator: p_inc against the oracle's exact solve (1e-10),
+    C_ext against the oracle's cross-sections (1e-9)."""
+    pos = np.array([[-110, 0, 0], [110, 0, 0], [0, 190, 40]], float) * nm
+    mat = gb.constant_material(index=1.6 + 0.05j)
+    c = gb.sphere_cluster(position=pos, radius=80 * nm, material=mat, source=gb.plane_wave.from_string("x"),
+                          wavelength=500 * nm, lmax=9, method=gb.solver.exact)
+    k = float(np.real(c.material_data.k_b))
+    T = O.sphere_aggregate_tmatrix(c.position, c.mie_scat.reshape(3, -1), k)
+    x = O.solve_linear_system(T, c.p_src.ravel(), "exact").reshape(c.p_inc.shape)
+    assert np.max(np.abs(c.p_inc - x)) / np.max(np.abs(x)) < 1e-10
+    per = [O.particle_cross_sections(c.p_scat[i], c.p_inc[i], c.p_src[i], k) for i in range(3)]
+    cext = sum(np.sum(p[2]) for p in per)
+    assert abs(c.cross_sections().extinction - cext) <= 1e-9 * abs(cext)
+
+
 # ------------------------------------------------------------------ solves --
 @pytest.mark.parametrize("name", G.EXACT_CASES)
 def test_fp64_solve_matches_exact_reference(name):
