@@ -1173,11 +1173,28 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
     const SysPlan pl = plan[I.sys];
     const int k = I.r0 / S.B;   // particle (block row) of this item
     const long long s0 = row_strip[pl.strip_row_base + k], s1 = row_strip[pl.strip_row_base + k + 1];
-    pdl_wait();
-    pdl_trigger();
-    if (!any_active<R>(st, I.sys, mask_mode)) return;
     constexpr int E = PWord<OutT>::E;
     const int B = S.B, BR = B * R;
+    // The combine's inputs (row map, x, aux, b, the identity's scale, the solver
+    // state) were written before the preceding matrix pass began, which waited for
+    // them: loaded ahead of the wait for that pass, while it still runs.  Only its
+    // partial sums need the wait.
+    const bool act = any_active<R>(st, I.sys, mask_mode);
+    int info_p = 0;
+    VT x_p{}, aux_p{};
+    double2 b_p = make_double2(0.0, 0.0), xs_p = make_double2(1.0, 0.0);
+    if (act && threadIdx.x < BR) {
+        const int r = threadIdx.x / R, rr = threadIdx.x - r * R;
+        const long long e = S.vec_off + (long long)(I.r0 + r) * R + rr;
+        info_p = __ldg(S.rowinfo + r);
+        x_p = x[e];
+        if (mode == 1 || mode == 2 || (mode == 3 && !b128)) aux_p = aux[e];
+        if (mode == 3 && b128) b_p = b128[e];
+        if (xscale) xs_p = xscale[S.t_off + I.r0 + r];
+    }
+    pdl_wait();
+    pdl_trigger();
+    if (!act) return;
     const int W = BR / E;   // 16-byte words per term (B R is even)
     const int G = kRBThreads / W;
     const int tid = threadIdx.x, g = tid / W, w = tid - g * W;
@@ -1209,7 +1226,7 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
     d1.zero();
     if (tid < BR) {
         const int r = tid / R, rr = tid - r * R;
-        const int info = __ldg(S.rowinfo + r);
+        const int info = info_p;
         const int rho = info & ((1 << 29) - 1);
         const unsigned eneg = (info >> 29) & 1, sneg = (info >> 30) & 1;
         C a = czero<C>(), c = czero<C>();
@@ -1220,18 +1237,18 @@ k_reduce_blk(const gb::SysDev* __restrict__ sys, const Item* __restrict__ items,
         const C tx = cadd(cflip(a, eneg), cflip(c, eneg ^ sneg));
         if (active_rhs<R>(st, I.sys, rr, mask_mode)) {
             const long long e = S.vec_off + (long long)(I.r0 + r) * R + rr;
-            C xe = to_c<C>(x[e]);
-            if (xscale) xe = cmul(xe, to_c<C>(xscale[S.t_off + I.r0 + r]));   // the identity's share of (I + T) D x
+            C xe = to_c<C>(x_p);
+            if (xscale) xe = cmul(xe, to_c<C>(xs_p));   // the identity's share of (I + T) D x
             C yv = cadd(xe, tx);
-            if (mode == 3) yv = csub(b128 ? to_c<C>(b128[e]) : to_c<C>(aux[e]), yv);
+            if (mode == 3) yv = csub(b128 ? to_c<C>(b_p) : to_c<C>(aux_p), yv);
             const VT yo = from_c<VT>(yv);
             y[e] = yo;
             const C yq = to_c<C>(yo);   // dots of the stored (rounded) vector
             if (mode == 1) {
-                d0.fma_conj(to_c<C>(aux[e]), yq);
+                d0.fma_conj(to_c<C>(aux_p), yq);
             } else if (mode == 2) {
                 d0.add_norm2(yq);
-                d1.fma_conj(yq, to_c<C>(aux[e]));
+                d1.fma_conj(yq, to_c<C>(aux_p));
             } else if (mode == 3) {
                 d0.add_norm2(yq);
             }
