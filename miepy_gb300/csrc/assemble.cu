@@ -430,20 +430,8 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                         sb.y = fma(c, gv.y, sb.y);
                     }
                     const double2 At = mul_ipow(sa, nv), Bt = mul_ipow(sb, nv + 1);
-                    if constexpr (LATT) {   // this thread's running sums over the group's cells (buffer 0)
-                        const double2 ph = make_double2(geo[8 * pp + 4], geo[8 * pp + 5]);
-                        const double2 a = cmul(ph, At), b = cmul(ph, Bt);
-                        if (pp == 0) {
-                            Tv[2 * t] = a;
-                            Tv[2 * t + 1] = b;
-                        } else {
-                            Tv[2 * t] = make_double2(Tv[2 * t].x + a.x, Tv[2 * t].y + a.y);
-                            Tv[2 * t + 1] = make_double2(Tv[2 * t + 1].x + b.x, Tv[2 * t + 1].y + b.y);
-                        }
-                    } else {
-                        if (wantA) tv[slot(t, 0)] = At;
-                        if (wantB) tv[slot(t, 1)] = Bt;
-                    }
+                    if (wantA) tv[slot(t, 0)] = At;
+                    if (wantB) tv[slot(t, 1)] = Bt;
                     if (!DENSE && want64) {
                         const float2 ah = make_float2(__double2float_rn(At.x), __double2float_rn(At.y));
                         const float2 bh = make_float2(__double2float_rn(Bt.x), __double2float_rn(Bt.y));
@@ -581,9 +569,24 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             }
         };
         if constexpr (LATT) {
-            // every thread sums its own tuples over the group's cells, then the group's
-            // share of block (i, j), times mie(j, b, v), is added to the dense output
-            for (int pp = 0; pp < np; pp++) tuples(pp, 0, 2);
+            // The tuple sums are linear in the G table: the group's cells are summed
+            // first, G = sum_c e^{-i k khat.c} G_c (into the first cell's table, each
+            // thread its own entries), and the tuple values formed once from it; then
+            // the group's share of block (i, j), times mie(j, b, v), is added to the
+            // dense output.
+            for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
+                const int q = qm / MU, mi = qm - q * MU;
+                double2 acc = make_double2(0.0, 0.0);
+                for (int pp = 0; pp < np; pp++) {
+                    const double2 ph = make_double2(geo[8 * pp + 4], geo[8 * pp + 5]);
+                    const double2 gv = cmul(ph, G64[(size_t)PMs * MUs * pp + (size_t)q * MUs + mi]);
+                    acc.x += gv.x;
+                    acc.y += gv.y;
+                }
+                G64[(size_t)q * MUs + mi] = acc;
+            }
+            __syncthreads();
+            tuples(0, 0, 2);
             __syncthreads();
             const int i = (int)(lat_pair / N), j = (int)(lat_pair % N);
             const double2* mj_ = mie + (long long)j * 2 * L;
