@@ -44,11 +44,11 @@ __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
 // they fit, one at large lmax, where two would cost occupancy.
 struct AsmSmem {
     int PM, MU, M, PB, NB;
-    size_t off_geo, off_h, off_P, off_e, off_G, off_T, off_Tf, off_Tl, total;
+    size_t off_geo, off_h, off_P, off_e, off_G, off_Gs, off_T, off_Tf, off_Tl, total;
 };
 
 __host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_sums, bool want64, int NB,
-                                               bool split = false) {
+                                               bool split = false, bool gsum = false) {
     AsmSmem s;
     s.PM = 2 * L + 2;
     s.MU = 4 * L + 1;
@@ -64,6 +64,7 @@ __host__ __device__ inline AsmSmem asm_layout(int L, int M, int PB, bool fp64_su
     s.off_e = take(sf * sizeof(double2) * s.MU * PB);
     s.off_P = take(sf * sizeof(double) * s.PM * s.PM * PB);
     s.off_G = take(16 * (size_t)s.PM * s.MU * PB);          // double2 (FP64 sums) or float4 (double-float)
+    s.off_Gs = take(gsum ? sizeof(double2) * s.PM * s.MU : 0);   // lattice sums: the group's running G sum
     const size_t kinds = split ? 1 : 2;   // (A, B) per tuple, or one of them at a time
     s.off_T = take(fp64_sums ? sizeof(double2) * kinds * NB * M : 0);   // NB buffers of tuple values
     s.off_Tf = take(want64 ? sizeof(float2) * kinds * NB * M : 0);
@@ -186,7 +187,8 @@ struct Refl {
 struct Latt {
     const double* cells = nullptr;
     int ncell = 0;
-    int gpp = 1;
+    int gpp = 1;   // groups per ordered pair, each over cpg consecutive cells in chunks of PB
+    int cpg = 1;
     double kx = 0, ky = 0, kz = 0;
 };
 
@@ -216,12 +218,13 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool want64 = out64 != nullptr || out64lo != nullptr;
-    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE, NB, SPLIT);
+    const AsmSmem lay = asm_layout(Lmax, Mmax, PB, FP64_SUMS, want64 && !DENSE, NB, SPLIT, LATT);
     double* geo = reinterpret_cast<double*>(smem + lay.off_geo);        // [PB][8]
     double2* hh = reinterpret_cast<double2*>(smem + lay.off_h);         // [PB][PM]
     double2* eph = reinterpret_cast<double2*>(smem + lay.off_e);        // [PB][MU]
     double* Pl = reinterpret_cast<double*>(smem + lay.off_P);           // [PB][PM][PM]
     double2* G64 = reinterpret_cast<double2*>(smem + lay.off_G);        // [PB][PM][MU]
+    double2* Gs = reinterpret_cast<double2*>(smem + lay.off_Gs);        // [PM][MU] (lattice sums)
     float4* G32 = reinterpret_cast<float4*>(smem + lay.off_G);
     double2* Tv = reinterpret_cast<double2*>(smem + lay.off_T);
     float2* Tf = reinterpret_cast<float2*>(smem + lay.off_Tf);
@@ -235,17 +238,23 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         const long long gl = g - grp_base[s];
         const long long p_first = gl * (long long)PB;
         long long lat_pair = 0;   // lattice: the ordered pair (i, j) = (lat_pair / N, lat_pair % N) ...
-        int lat_c0 = 0;           // ... and the group's first cell
+        int lat_c0 = 0;           // ... the first cell of the chunk ...
+        int lat_end = 0;          // ... and the end of the group's cells
         int np;
         if constexpr (LATT) {
             lat_pair = gl / latt.gpp;
-            lat_c0 = (int)(gl - lat_pair * latt.gpp) * PB;
-            np = min(PB, latt.ncell - lat_c0);
+            lat_c0 = (int)(gl - lat_pair * latt.gpp) * latt.cpg;
+            lat_end = min(lat_c0 + latt.cpg, latt.ncell);
+            np = min(PB, lat_end - lat_c0);
         } else {
             const long long Ptot = REFL ? (long long)N * N : S.P;   // all ordered pairs for the reflection
             np = (int)min((long long)PB, Ptot - p_first);
         }
 
+        // lattice sums: phases 1a-1c for every chunk of PB cells of the group, each
+        // chunk's phase-weighted G tables added to the running sum Gs; other modes run
+        // them once
+        for (bool first = true;; first = false) {
         // ---- phase 1a (FP64 paths; the double-float path reads the G tables of
         // k_asm_gtab): one thread per pair: geometry, then h_p(kr) by the upward
         // j/y recurrence of spherical_hn_recursion (cpp/src/special.cpp:90-111).  The
@@ -381,6 +390,29 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 G64[gi] = gval;
             }
             __syncthreads();
+        }
+        if constexpr (LATT) {
+            // the chunk's cells into the running sum, G = sum_c e^{-i k khat.c} G_c (the
+            // tuple sums are linear in G), each thread its own entries
+            for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
+                const int q = qm / MU, mi = qm - q * MU;
+                double2 acc = first ? make_double2(0.0, 0.0) : Gs[(size_t)q * MUs + mi];
+                for (int pp = 0; pp < np; pp++) {
+                    const double2 ph = make_double2(geo[8 * pp + 4], geo[8 * pp + 5]);
+                    const double2 gv = cmul(ph, G64[(size_t)PMs * MUs * pp + (size_t)q * MUs + mi]);
+                    acc.x += gv.x;
+                    acc.y += gv.y;
+                }
+                Gs[(size_t)q * MUs + mi] = acc;
+            }
+            __syncthreads();   // before the next chunk rewrites the cells' tables
+            lat_c0 += PB;
+            if (lat_c0 >= lat_end) break;
+            np = min(PB, lat_end - lat_c0);
+        } else {
+            (void)first;
+            break;
+        }
         }
 
         // ---- phases 2 and 3, software-pipelined over the group's pairs: each thread
@@ -569,21 +601,12 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             }
         };
         if constexpr (LATT) {
-            // The tuple sums are linear in the G table: the group's cells are summed
-            // first, G = sum_c e^{-i k khat.c} G_c (into the first cell's table, each
-            // thread its own entries), and the tuple values formed once from it; then
-            // the group's share of block (i, j), times mie(j, b, v), is added to the
-            // dense output.
+            // the tuple values once from the group's summed G table (into the first
+            // cell's slot), then the group's share of block (i, j), times mie(j, b, v),
+            // added to the dense output
             for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
                 const int q = qm / MU, mi = qm - q * MU;
-                double2 acc = make_double2(0.0, 0.0);
-                for (int pp = 0; pp < np; pp++) {
-                    const double2 ph = make_double2(geo[8 * pp + 4], geo[8 * pp + 5]);
-                    const double2 gv = cmul(ph, G64[(size_t)PMs * MUs * pp + (size_t)q * MUs + mi]);
-                    acc.x += gv.x;
-                    acc.y += gv.y;
-                }
-                G64[(size_t)q * MUs + mi] = acc;
+                G64[(size_t)q * MUs + mi] = Gs[(size_t)q * MUs + mi];
             }
             __syncthreads();
             tuples(0, 0, 2);
@@ -1129,13 +1152,22 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         // the split kernel forms and writes them one kind at a time
         const bool split = !ts && !refl && !latt && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > 227 * 1024;
         if (split) PB = NB = 1;
-        const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB, split);
+        const AsmSmem lay = asm_layout(L, Mmax, PB, fp64_sums, want64, NB, split, latt != nullptr);
         const size_t smem = lay.total;
         if (smem > 227 * 1024) return gb_set_error(GB_UNSUPPORTED, "assembler needs %zu B of shared memory", smem);
         Latt lt = latt ? *latt : Latt();
         if (latt) {
             if (lt.ncell < 1) return GB_OK;
-            lt.gpp = (lt.ncell + PB - 1) / PB;
+            // each group sums a range of whole chunks of PB cells (its tuple sums and
+            // block additions once per range); enough groups to fill the SMs about
+            // twice, at least one per ordered pair
+            long long pairs = 0;
+            for (const gb::SysDev& d : sd) pairs += (long long)d.N * d.N;
+            const long long chunks = (lt.ncell + PB - 1) / PB;
+            const long long want = 6LL * gb::sm_count();
+            const long long g = std::min<long long>(chunks, std::max<long long>(1, (want + pairs - 1) / pairs));
+            lt.cpg = (int)(((chunks + g - 1) / g) * PB);
+            lt.gpp = (lt.ncell + lt.cpg - 1) / lt.cpg;
         }
         std::vector<long long> gbase(ns + 1, 0);
         for (int s = 0; s < ns; s++) {
