@@ -243,7 +243,7 @@ def solve_linear_system_jax(agg_tmatrix, p_src, method, M_inv_blocks=None, block
             raise ValueError(f"M_inv_blocks must be [{D}, bs] with bs dividing {D}")
     diag = _block_diagonal(M_inv_blocks, block_size, D) if M_inv_blocks is not None else None
     if isinstance(agg_tmatrix, DeviceAggregateTMatrix) and agg_tmatrix._host is None and \
-            (M_inv_blocks is None or diag is not None):
+            (M_inv_blocks is None or diag is not None) and agg_tmatrix.lmax <= 8:   # the packed solvers' orders
         b = agg_tmatrix._batch
         b.b.copy_(torch.from_numpy(p_src.reshape(-1)).to(b.device))
         pre = False
@@ -251,10 +251,11 @@ def solve_linear_system_jax(agg_tmatrix, p_src, method, M_inv_blocks=None, block
             pre = torch.from_numpy(np.ascontiguousarray(diag)).to(b.device)
         b.solve(tol=tol, maxiter=1000, precondition=pre)
         return b.cluster_view(0, b.x)[..., 0].cpu().numpy()
-    # a dense matrix supplied by the caller
-    T = torch.as_tensor(np.ascontiguousarray(np.asarray(agg_tmatrix, dtype=complex).reshape(D, D)))
     dev = require_cuda()
-    T = T.to(dev)
+    if isinstance(agg_tmatrix, DeviceAggregateTMatrix) and agg_tmatrix._host is None:
+        T = agg_tmatrix.dense_device().reshape(D, D)   # assembled dense on the device
+    else:   # a dense matrix supplied by the caller
+        T = torch.as_tensor(np.ascontiguousarray(np.asarray(agg_tmatrix, dtype=complex).reshape(D, D))).to(dev)
     bb = torch.from_numpy(np.ascontiguousarray(p_src.reshape(-1))).to(dev)
     x = torch.empty_like(bb)
     L = nat.lib()

@@ -213,6 +213,29 @@ def test_cluster_lmax9_on_the_dense_operator():
     assert abs(c.cross_sections().extinction - cext) <= 1e-9 * abs(cext)
 
 
+def test_plugin_lmax9_solves_on_the_dense_operator():
+    """The plugin pair sphere_aggregate_tmatrix_jax -> solve_linear_system_jax at lmax 9
+    (beyond the packed solvers): the device aggregate is solved as a dense operator,
+    p_inc within 1e-10 of the oracle's exact solve."""
+    from miepy_gb300 import backend
+    rng = np.random.default_rng(21)
+    N, lmax = 3, 9
+    pos, rad = random_cluster(rng, N, 60 * nm, 90 * nm, 900 * nm)
+    # the spheres' own Mie coefficients (n = 1.6 + 0.05i in vacuum at 650 nm): their
+    # decay with order keeps (I + T) well conditioned, as for any physical cluster
+    md = gb.material_struct([gb.constant_material(index=1.6 + 0.05j)] * N, gb.constant_material(eps=1.0, mu=1.0),
+                            wavelength=650 * nm)
+    mie, _ = gb.mie_coefficients(rad, md.eps, md.mu, md.eps_b, md.mu_b, md.k_b, lmax)
+    k = float(np.real(md.k_b))
+    rmax = lmax * (lmax + 2)
+    p_src = rng.normal(size=(N, 2, rmax)) + 1j * rng.normal(size=(N, 2, rmax))
+    agg = backend.sphere_aggregate_tmatrix_jax(pos, mie, k)
+    x = backend.solve_linear_system_jax(agg, p_src, gb.solver.exact)
+    T = O.sphere_aggregate_tmatrix(pos, mie.reshape(N, -1), k)
+    ref = O.solve_linear_system(T, p_src.ravel(), "exact").reshape(N, 2, rmax)
+    assert rel(x, ref) < 1e-10
+
+
 # ------------------------------------------------------------------ solves --
 @pytest.mark.parametrize("name", G.EXACT_CASES)
 def test_fp64_solve_matches_exact_reference(name):
