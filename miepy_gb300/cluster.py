@@ -178,8 +178,9 @@ class sphere_cluster:
         spec = dict(position=self.position, mie_scat=self.mie_scat, mie_int=self.mie_int, k=float(np.real(md.k_b)),
                     p_src=self.p_src)
         prec = self.precision if self.interactions else "fp64"
-        b = ClusterBatch([spec], R=1, precision=prec, device=self.device)
-        if self.interactions and (self.interface is not None or self.symmetry is not None or self.lmax > 8):
+        dense = self.interactions and (self.interface is not None or self.symmetry is not None or self.lmax > 8)
+        b = ClusterBatch([spec], R=1, precision=prec, device=self.device, packed=not dense)
+        if dense:
             self._solve_dense(b)   # (the packed solvers take lmax <= 8)
         elif self.interactions and self.Nparticles > 1:
             b.assemble()

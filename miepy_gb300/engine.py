@@ -85,9 +85,12 @@ class ClusterBatch:
         position [N,3] float, mie_scat [N,2,lmax] complex, k float (medium wavenumber),
         p_src [N,2,rmax,R] complex (or [N,2,rmax] when R == 1),
         optional mie_int [N,2,lmax], eps_b float.
+    packed=False allocates no packed pair-block matrix: for a batch whose operator is
+    formed and solved densely (lmax > 8, an interface, a periodic symmetry), which
+    uses the batch only for its inputs, vectors and epilogue.
     """
 
-    def __init__(self, specs, R=1, precision="fp64", device=None, tensor=False):
+    def __init__(self, specs, R=1, precision="fp64", device=None, tensor=False, packed=True):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {list(PRECISIONS)}")
         if tensor and (int(R) not in (4, 8) or precision not in ("fp32", "mixed")):
@@ -124,7 +127,7 @@ class ClusterBatch:
         self._f_buf = self._out[nv2 + self._n_xs: nv2 + self._n_xs + self._n_f]
         self._t_buf = self._out[nv2 + self._n_xs + self._n_f:]
         self.xs = self.F = self.T = None
-        need = NEEDS[precision]
+        need = NEEDS[precision] if packed else ()
         mat = max(t["mat"], 1)
         self.mat128 = torch.empty(mat, dtype=torch.complex128, device=dev) if "c128" in need else None
         self.mat64 = torch.empty(mat, dtype=torch.complex64, device=dev) if "hi" in need else None

@@ -9,12 +9,15 @@ p_scat = T p_inc (cluster.py:657, ``einsum("naibj,nbj->nai")``), then cross-sect
 rmax], the reference's layout): ``tmatrix_sphere`` for spheres, or T-matrices
 computed elsewhere (the reference's EBCM particle classes, core-shell Mie) for other
 particles.  On the GPU the packed translation blocks A are applied after each
-particle's T-matrix (``gb_solve_batch_tmatrix``); the dense aggregate is not formed.
+particle's T-matrix (``gb_solve_batch_tmatrix``); the dense aggregate is formed only
+for lmax > 8, beyond the packed solvers' order limit (``gb_particle_aggregate_dense``
+then ``gb_solve_dense``).
 """
 
 from __future__ import annotations
 
 import types
+import warnings
 
 import numpy as np
 import torch
@@ -125,9 +128,12 @@ class tmatrix_cluster:
         N = self.Nparticles
         self.p_src = np.asarray(self.source.structure(self.position, self.k_b, self.lmax), dtype=complex)
         spec = dict(position=self.position, tmatrix=self.tmatrix, k=float(self.k_b), p_src=self.p_src)
-        prec = self.precision if self.interactions else "fp64"
-        b = ClusterBatch([spec], R=1, precision=prec, device=self.device)
-        if self.interactions and N > 1:
+        dense = self.interactions and N > 1 and self.lmax > 8   # the packed solvers take lmax <= 8
+        prec = self.precision if self.interactions and not dense else "fp64"
+        b = ClusterBatch([spec], R=1, precision=prec, device=self.device, packed=not dense)
+        if dense:
+            self._solve_dense(b)
+        elif self.interactions and N > 1:
             tol = self._tolerance()
             b.assemble()
             b.solve(tol=tol, maxiter=self.maxiter or DEFAULT_MAXITER, inner_tol=min(1e-6, max(tol, 1e-7)),
@@ -145,6 +151,36 @@ class tmatrix_cluster:
         self._F = b.F[: N * 3].view(N, 3).cpu().numpy()
         self._T = b.T[: N * 3].view(N, 3).cpu().numpy()
         self._batch = b
+
+    def _solve_dense(self, b):
+        """(I + T_agg) p_inc = p_src on the dense reference layout, as cluster.py:653-655
+        with interactions.cpp:416-462: the translation blocks times each particle's
+        T-matrix (gb_particle_aggregate_dense), then BiCGSTAB (gb_solve_dense) in FP64,
+        the route of lmax > 8 whatever `precision` says (with a warning when it says
+        otherwise)."""
+        if self.precision != "fp64":
+            warnings.warn(f"precision={self.precision!r} does not apply to T-matrix clusters of lmax > 8: their "
+                          "dense operator is solved in FP64", stacklevel=3)
+        L = nat.lib()
+        dev, st = b.device, current_stream(b.device)
+        N = self.Nparticles
+        D = 2 * self.rmax * N
+        ws = torch.empty(L.gb_particle_aggregate_workspace_size(N, self.lmax), dtype=torch.uint8, device=dev)
+        T = torch.empty(D * D, dtype=torch.complex128, device=dev)
+        nat.check(L.gb_particle_aggregate_dense(N, self.lmax, nat.ptr(b.pos), nat.ptr(b.tmat128), float(self.k_b),
+                                                nat.ptr(ws), ws.numel(), nat.ptr(T), st), "particle aggregate")
+        del ws
+        need = L.gb_solve_dense_workspace_size(D, 1)
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        status = np.zeros(1, np.int32)
+        iters = np.zeros(1, np.int32)
+        resid = np.zeros(1)
+        rc = L.gb_solve_dense(D, 1, nat.ptr(T), nat.ptr(b.b), nat.ptr(b.x), self._tolerance(),
+                              int(self.maxiter or DEFAULT_MAXITER), nat.ptr(ws), ws.numel(), status.ctypes.data,
+                              iters.ctypes.data, resid.ctypes.data, st)
+        if rc not in (nat.GB_OK, nat.GB_NOT_CONVERGED, nat.GB_BREAKDOWN, nat.GB_NAN):
+            nat.check(rc, "dense solve")
+        self.solver_status, self.solver_iterations, self.solver_residual = int(status[0]), int(iters[0]), float(resid[0])
 
     def cross_sections_per_multipole_of_particle(self, i):
         C = self._xs[i]

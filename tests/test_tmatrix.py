@@ -119,6 +119,38 @@ def test_dense_particle_aggregate_on_gpu():
     assert rel(A.reshape(432, 432), O.particle_aggregate_tmatrix(pos, T, k).reshape(432, 432)) < 1e-12
 
 
+@pytest.mark.gpu
+def test_tmatrix_cluster_lmax9_on_the_dense_operator():
+    """A cluster of general particles at lmax 9 (beyond the packed solvers' lmax 8)
+    solves on the dense aggregate: p_inc within 1e-10 of numpy's direct solve of the
+    oracle's aggregate, p_scat = T p_inc, and C_ext against the oracle's
+    cross-sections (1e-9).  The T-matrices are the spheres' with a cross-polarised
+    coupling of the dipole and quadrupole orders, so that they are not diagonal."""
+    import miepy_gb300 as gb
+    from oracle import oracle as O
+    N, lmax = 3, 9
+    rmax = lmax * (lmax + 2)
+    pos, radius, eps, mie, k = random_cluster(9, N=N, lmax=lmax)
+    rng = np.random.default_rng(4)
+    T = sphere_tmatrices(mie)
+    c8 = 0.01 * (rng.standard_normal((N, 8, 8)) + 1j * rng.standard_normal((N, 8, 8)))
+    T[:, 0, :8, 1, :8] += c8
+    T[:, 1, :8, 0, :8] += c8.transpose(0, 2, 1)
+    parts = [fixed_particle(pos[i], T[i], radius[i]) for i in range(N)]
+    with pytest.warns(UserWarning, match="lmax > 8"):
+        c = gb.cluster(particles=parts, source=gb.plane_wave([1, 1j]), wavelength=620 * nm, lmax=lmax,
+                       medium=gb.constant_material(index=1.33), method=gb.solver.exact, precision="mixed")
+    assert c.solver_status == 0
+    D = 2 * rmax * N
+    A = O.particle_aggregate_tmatrix(pos, T, k).reshape(D, D)
+    x = np.linalg.solve(np.eye(D) + A, c.p_src.reshape(-1)).reshape(N, 2, rmax)
+    assert rel(c.p_inc, x) < 1e-10
+    assert rel(c.p_scat, np.einsum("naibj,nbj->nai", T, x)) < 1e-10
+    per = [O.particle_cross_sections(c.p_scat[i], c.p_inc[i], c.p_src[i], k) for i in range(N)]
+    cext = sum(np.sum(p[2]) for p in per)
+    assert abs(c.cross_sections().extinction - cext) <= 1e-9 * abs(cext)
+
+
 def _reference_cluster(**kw):
     import miepy_gb300 as gb
     g = fixture()
