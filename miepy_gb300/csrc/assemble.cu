@@ -31,6 +31,7 @@
 namespace {
 
 constexpr int kAsmThreads = 256;
+constexpr int kAsmWideThreads = 512;
 
 // 1/k for the Legendre recurrence (k = q - mu <= 2*lmax + 1)
 __constant__ double c_inv_int[2 * GB_LMAX_MAX + 4] = {
@@ -205,8 +206,11 @@ struct Latt {
 // SPLIT (MODE 0, one pair per group, one buffer): where one pair's A and B tuple
 // values do not fit in shared memory together (lmax 10), the A sums are formed and
 // their block elements written, then the B sums and theirs.
-template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false, bool SPLIT = false>
-__global__ void __launch_bounds__(kAsmThreads, FP64_SUMS ? 3 : 5)
+// NT: threads per CTA.  The pair-by-pair double-float path runs 512 (kAsmWideThreads)
+// where its tuple buffers leave room for at most two CTAs per SM (lmax >= 8), so
+// that the SM keeps 32 warps instead of 16.
+template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false, bool SPLIT = false, int NT = kAsmThreads>
+__global__ void __launch_bounds__(NT, FP64_SUMS ? 3 : (NT > kAsmThreads ? 2 : 5))
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
            int Lmax, int Mmax, int PB, int NB, const double* __restrict__ pos, const double2* __restrict__ mie,
            double2* __restrict__ out128, float2* __restrict__ out64, float2* __restrict__ out64lo, long long dense_ld,
@@ -323,7 +327,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // (pair, mu); e^{i mu phi} by binary powering, one thread per (pair, mu >= 0).
         // The double-float path instead loads the group's G tables.
         if constexpr (FP64_SUMS) {
-            for (int it = tid; it < np * PM; it += kAsmThreads) {
+            for (int it = tid; it < np * PM; it += NT) {
                 const int pp = it / PM, mu = it % PM;
                 const double x = geo[8 * pp], u = geo[8 * pp + 1];
                 double* P = Pl + (size_t)PMs * PMs * pp;
@@ -341,7 +345,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     }
                 }
             }
-            for (int it = tid; it < np * (2 * L + 1); it += kAsmThreads) {
+            for (int it = tid; it < np * (2 * L + 1); it += NT) {
                 const int pp = it / (2 * L + 1), mu = it % (2 * L + 1);
                 int e = mu;
                 double2 acc = make_double2(1.0, 0.0), base = make_double2(geo[8 * pp + 2], geo[8 * pp + 3]);
@@ -360,7 +364,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             // kernel overwrites these words later, after the barrier that ends the sums).
             const float2* gsrc = out64lo ? out64lo : out64;
             const long long BBl = (long long)B * B;
-            for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
+            for (int it = tid; it < np * PM * MU; it += NT) {
                 const int pp = it / (PM * MU), rem = it - pp * (PM * MU);
                 const int q = rem / MU, mi = rem - q * MU, mu = mi - 2 * L;
                 float4 gv = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -376,7 +380,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         // ---- phase 1c (FP64 paths): G[p][mu] = P_p^mu h_p e^{i mu phi} (negative mu
         // through the (-1)^mu (p-mu)!/(p+mu)! ratio)
         if constexpr (FP64_SUMS) {
-            for (int it = tid; it < np * PM * MU; it += kAsmThreads) {
+            for (int it = tid; it < np * PM * MU; it += NT) {
                 const int pp = it / (PM * MU), rem = it % (PM * MU);
                 const int q = rem / MU, mi = rem % MU, mu = mi - 2 * L, am = mu < 0 ? -mu : mu;
                 const size_t gi = (size_t)PMs * MUs * pp + (size_t)q * MUs + mi;
@@ -394,7 +398,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
         if constexpr (LATT) {
             // the chunk's cells into the running sum, G = sum_c e^{-i k khat.c} G_c (the
             // tuple sums are linear in G), each thread its own entries
-            for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
+            for (int qm = tid; qm < PM * MU; qm += NT) {
                 const int q = qm / MU, mi = qm - q * MU;
                 double2 acc = first ? make_double2(0.0, 0.0) : Gs[(size_t)q * MUs + mi];
                 for (int pp = 0; pp < np; pp++) {
@@ -429,7 +433,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             float2* tl = Tl + (size_t)buf * KINDS * Mb;
             const bool wantA = kind != 1, wantB = kind != 0;
             const int Q = L + 1;
-            for (int it = tid; it < S.M; it += kAsmThreads) {
+            for (int it = tid; it < S.M; it += NT) {
                 int t, mi, nv;
                 int2 qq;
                 if constexpr (FP64_SUMS) {
@@ -524,7 +528,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 if (!SPLIT && !FP64_SUMS && (base & 1) == 0 &&
                     ((reinterpret_cast<size_t>(out64) | reinterpret_cast<size_t>(out64lo)) & 15) == 0) {
                     // two elements per thread, 16-byte streaming stores (BB is even)
-                    for (int e2 = tid; e2 < BB / 2; e2 += kAsmThreads) {
+                    for (int e2 = tid; e2 < BB / 2; e2 += NT) {
                         const int2 code = __ldg(reinterpret_cast<const int2*>(S.elem_map) + e2);
                         const unsigned n0 = code.x & 1, n1 = code.y & 1;
                         const int t0 = code.x >> 1, t1 = code.y >> 1;
@@ -541,7 +545,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                     }
                     return;
                 }
-                for (int e = tid; e < BB; e += kAsmThreads) {
+                for (int e = tid; e < BB; e += NT) {
                     const int code = __ldg(S.elem_map + e);
                     if (skip(code)) continue;
                     const unsigned neg = code & 1;
@@ -563,7 +567,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 const int i = (int)(p / N), j = (int)(p % N);
                 const double2* mj_ = mie + (long long)j * 2 * L;
                 const int rmx = B / 2;
-                for (int e = tid; e < BB; e += kAsmThreads) {
+                for (int e = tid; e < BB; e += NT) {
                     const int R = e / B, C = e % B;
                     const int code = __ldg(S.elem_map + e);
                     const unsigned neg = code & 1;
@@ -583,7 +587,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 pair_ij(p, N, i, j);
                 const double2* mi_ = mie + (long long)i * 2 * L;
                 const double2* mj_ = mie + (long long)j * 2 * L;
-                for (int e = tid; e < BB; e += kAsmThreads) {
+                for (int e = tid; e < BB; e += NT) {
                     const int R = e / B, C = e % B;
                     const int code = __ldg(S.elem_map + e);
                     if (skip(code)) continue;
@@ -604,7 +608,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             // the tuple values once from the group's summed G table (into the first
             // cell's slot), then the group's share of block (i, j), times mie(j, b, v),
             // added to the dense output
-            for (int qm = tid; qm < PM * MU; qm += kAsmThreads) {
+            for (int qm = tid; qm < PM * MU; qm += NT) {
                 const int q = qm / MU, mi = qm - q * MU;
                 G64[(size_t)q * MUs + mi] = Gs[(size_t)q * MUs + mi];
             }
@@ -613,7 +617,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             __syncthreads();
             const int i = (int)(lat_pair / N), j = (int)(lat_pair % N);
             const double2* mj_ = mie + (long long)j * 2 * L;
-            for (int e = tid; e < B * B; e += kAsmThreads) {
+            for (int e = tid; e < B * B; e += NT) {
                 const int R = e / B, C = e % B;
                 const int code = __ldg(S.elem_map + e);
                 const unsigned neg = code & 1;
@@ -664,7 +668,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 tf[2 * t + 1] = mul_ipowf(b1, nv + 1);
                 tl[2 * t] = mul_ipowf(a2, nv);
                 tl[2 * t + 1] = mul_ipowf(b2, nv + 1);
-                i += kAsmThreads;
+                i += NT;
                 while (i >= M) { i -= M; pp++; }
             }
             __syncthreads();
@@ -672,7 +676,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
             if ((S.mat_off & 1) == 0 && ((reinterpret_cast<size_t>(out64) | reinterpret_cast<size_t>(out64lo)) & 15) == 0) {
                 // two elements per thread and 16-byte streaming stores (the blocks are
                 // read by the next kernels from HBM: more than L2 holds)
-                for (int e2 = tid; e2 < BB / 2; e2 += kAsmThreads) {
+                for (int e2 = tid; e2 < BB / 2; e2 += NT) {
                     const int2 code = __ldg(reinterpret_cast<const int2*>(S.elem_map) + e2);
                     const unsigned n0 = code.x & 1, n1 = code.y & 1;
                     const int t0 = code.x >> 1, t1 = code.y >> 1;
@@ -693,7 +697,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 __syncthreads();   // before the next group rewrites the tables and the buffers
                 continue;
             }
-            for (int el = tid; el < BB; el += kAsmThreads) {
+            for (int el = tid; el < BB; el += NT) {
                 const int code = __ldg(S.elem_map + el);
                 const unsigned neg = code & 1;
                 const int ti = code >> 1;
@@ -1195,6 +1199,12 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         const long long* dbase =
             reinterpret_cast<const long long*>(static_cast<unsigned char*>(dblob) + sizeof(gb::SysDev) * ns);
 
+        // the pair-by-pair double-float path with room for at most two CTAs per SM
+        // (lmax >= 8) runs 512 threads per CTA (N = 200, lmax 8: 2.94 ms against 3.25
+        // ms; N = 60, lmax 9: 0.49 ms against 0.76 ms; more threads at lower lmax
+        // measured slower)
+        const bool wide = !fp64_sums && !ts && !split && !refl && !latt && smem > 227 * 1024 / 3;
+        const int nt = wide ? kAsmWideThreads : kAsmThreads;
         auto kfn = latt ? k_assemble<true, true, 2>
                         : refl ? k_assemble<true, true, 1>
                                : split ? (dense ? k_assemble<true, true, 0, false, true>
@@ -1203,10 +1213,12 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
                                        : (dense ? k_assemble<true, true>
                                                 : (fp64_sums ? k_assemble<false, true>
                                                              : (ts ? k_assemble<false, false, 0, true>
-                                                                   : k_assemble<false, false>)));
+                                                                   : (wide ? k_assemble<false, false, 0, false, false,
+                                                                                        kAsmWideThreads>
+                                                                           : k_assemble<false, false>))));
         GB_CUDA_TRY(gb::ensure_dynamic_smem(reinterpret_cast<const void*>(kfn), smem));
         int per_sm = 1;
-        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kAsmThreads, smem));
+        GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, nt, smem));
         if (per_sm < 1) return gb_set_error(GB_UNSUPPORTED, "assembler does not fit on an SM (smem %zu B)", smem);
         // one group per CTA (no persistent loop): CTAs retire every few microseconds, so
         // kernels of higher-priority streams (other clusters' solves) are dispatched
@@ -1223,7 +1235,7 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
             GB_CUDA_TRY(cudaGetLastError());
         }
         gb::note_launch();
-        kfn<<<(unsigned)std::min<long long>(ngroups, 0x7fffffffLL), kAsmThreads, smem, stream>>>(
+        kfn<<<(unsigned)std::min<long long>(ngroups, 0x7fffffffLL), nt, smem, stream>>>(
             dsys, ns, dbase, ngroups, L, Mmax, PB, NB, pos, reinterpret_cast<const double2*>(mie),
             reinterpret_cast<double2*>(out128), reinterpret_cast<float2*>(out64), reinterpret_cast<float2*>(out64lo),
             dense_ld, refl ? *refl : Refl(), lt);
