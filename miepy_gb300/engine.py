@@ -127,6 +127,7 @@ class ClusterBatch:
         self._f_buf = self._out[nv2 + self._n_xs: nv2 + self._n_xs + self._n_f]
         self._t_buf = self._out[nv2 + self._n_xs + self._n_f:]
         self.xs = self.F = self.T = None
+        self.packed = bool(packed)
         need = NEEDS[precision] if packed else ()
         mat = max(t["mat"], 1)
         self.mat128 = torch.empty(mat, dtype=torch.complex128, device=dev) if "c128" in need else None
@@ -236,6 +237,8 @@ class ClusterBatch:
 
     # ---------------------------------------------------------------- steps --
     def assemble(self):
+        if not self.packed:
+            raise ValueError("this batch was built with packed=False and holds no packed matrix to assemble")
         L = nat.lib()
         st = current_stream(self.device)
         nat.check(L.gb_expand_mie_batch(self.nsys, self.sys, self.mie_off.ctypes.data, nat.ptr(self.mie_scat),

@@ -141,6 +141,10 @@ def test_tmatrix_cluster_lmax9_on_the_dense_operator():
         c = gb.cluster(particles=parts, source=gb.plane_wave([1, 1j]), wavelength=620 * nm, lmax=lmax,
                        medium=gb.constant_material(index=1.33), method=gb.solver.exact, precision="mixed")
     assert c.solver_status == 0
+    b = c._batch   # the dense route allocates no packed matrix
+    assert not b.packed and b.mat128 is None and b.mat64 is None
+    with pytest.raises(ValueError, match="packed=False"):
+        b.assemble()
     D = 2 * rmax * N
     A = O.particle_aggregate_tmatrix(pos, T, k).reshape(D, D)
     x = np.linalg.solve(np.eye(D) + A, c.p_src.reshape(-1)).reshape(N, 2, rmax)
