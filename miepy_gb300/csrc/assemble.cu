@@ -12,7 +12,7 @@
 //   2. G[p][mu] = P_p^mu h_p e^{i mu phi} for all (p, |mu| <= p), in FP64.
 // The packed double-float (mixed) path instead takes steps 1-2 from a separate pass,
 // k_asm_gtab (below), with 32 pairs per CTA, and loads the group's G tables;
-// then per pair, software-pipelined over the group (or, at lmax <= 4, for the whole
+// then per pair, software-pipelined over the group (or, at lmax <= 5, for the whole
 // group at once):
 //   3. one thread per canonical tuple: A_t, B_t as real x complex FMA sums over
 //      the per-lmax coefficient table (tables.cu);
@@ -199,7 +199,7 @@ struct Latt {
 // lattice sums of a periodic cluster, added to a dense output (Latt).
 // Occupancy: the double-float (mixed) path fits five CTAs per SM in 48 registers
 // without spills; the FP64 paths keep three (at five they spill).
-// TS: whole-group phases on the packed double-float path (lmax <= 4, one tuple-value
+// TS: whole-group phases on the packed double-float path (lmax <= 5, one tuple-value
 // buffer per pair of the group, NB = PB): the group's (tuple, pair) sums are spread
 // evenly over the threads, then every block of the group is written after one
 // barrier, each element-map code read once for all of them.
@@ -648,7 +648,7 @@ k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __rest
                 const float4* gp = G32 + (size_t)PMs * MUs * pp + (size_t)nv * MUs + mi;
                 float2 ah = make_float2(0.f, 0.f), al = ah, bh = ah, bl = ah;
 #pragma unroll
-                for (int q = 0; q < 5; q++) {   // lmax <= 4: at most 5 terms per sum
+                for (int q = 0; q < 6; q++) {   // lmax <= 5: at most 6 terms per sum
                     if (q > qm) break;
                     if (q <= qa) {
                         const float2 c = ca[q];
@@ -1141,12 +1141,14 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         int NB = asm_layout(L, Mmax, 1, fp64_sums, want64, 2).total <= target ? 2 : 1;
         int PB = fp64_sums ? 32 : 4;
         while (PB > 1 && asm_layout(L, Mmax, PB, fp64_sums, want64, NB).total > target) PB >>= 1;
-        // whole-group phases (packed double-float, lmax <= 4): one buffer per pair,
-        // the most pairs up to 4 that keep the target
+        // whole-group phases (packed double-float, lmax <= 5): one buffer per pair,
+        // the most pairs up to 4 that keep the target (56 KB at lmax 5: two pairs, four
+        // CTAs per SM; N = 200 in 0.424 ms against 0.451 ms pair by pair)
         bool ts = false;
-        if (!dense && !refl && !latt && !fp64_sums && L <= 4) {
+        if (!dense && !refl && !latt && !fp64_sums && L <= 5) {
             int pb = 4;
-            while (pb > 1 && asm_layout(L, Mmax, pb, false, want64, pb).total > target) pb--;
+            const size_t ts_target = L == 5 ? 56 * 1024 : target;
+            while (pb > 1 && asm_layout(L, Mmax, pb, false, want64, pb).total > ts_target) pb--;
             if (pb >= 2) {
                 ts = true;
                 PB = NB = pb;

@@ -169,11 +169,12 @@ def test_packed_assembly_at_odd_offsets():
     """The packed double-float assembly through gb_assemble_batch with the clusters'
     blocks at odd element offsets (8-byte aligned, so the block writes take the
     one-element path) equals the same assembly at aligned offsets, bit for bit, at
-    lmax 4 (whole-group path) and lmax 6 (pair-by-pair path)."""
+    lmax 4 and 5 (whole-group path) and lmax 6 and 8 (pair-by-pair path; 512-thread
+    CTAs at lmax 8)."""
     rng = np.random.default_rng(11)
     L = nat.lib()
     dev = torch.device("cuda", 0)
-    for N, lmax in [(7, 4), (5, 6)]:
+    for N, lmax in [(7, 4), (6, 5), (5, 6), (4, 8)]:
         pos, _ = random_cluster(rng, N, 40 * nm, 80 * nm, 1200 * nm)
         B = 2 * lmax * (lmax + 2)
         P = N * (N - 1) // 2
