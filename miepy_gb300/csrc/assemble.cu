@@ -208,8 +208,8 @@ struct Latt {
 // their block elements written, then the B sums and theirs.
 // NT: threads per CTA.  The pair-by-pair double-float path runs 512 (kAsmWideThreads)
 // where its tuple buffers leave room for at most two CTAs per SM (lmax >= 8), so
-// that the SM keeps 32 warps instead of 16; the packed FP64 path likewise where one
-// CTA fits per SM (lmax >= 8: 16 warps instead of 8).
+// that the SM keeps 32 warps instead of 16; the packed FP64 and dense paths likewise
+// where one CTA fits per SM (lmax >= 8: 16 warps instead of 8).
 template <bool DENSE, bool FP64_SUMS, int MODE = 0, bool TS = false, bool SPLIT = false, int NT = kAsmThreads>
 __global__ void __launch_bounds__(NT, FP64_SUMS ? (NT > kAsmThreads ? 1 : 3) : (NT > kAsmThreads ? 2 : 5))
 k_assemble(const gb::SysDev* __restrict__ sys, int nsys, const long long* __restrict__ grp_base, long long ngroups,
@@ -1205,10 +1205,10 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
         // the pair-by-pair double-float path with room for at most two CTAs per SM
         // (lmax >= 8) runs 512 threads per CTA (N = 200, lmax 8: 2.94 ms against 3.25
         // ms; N = 60, lmax 9: 0.49 ms against 0.76 ms; more threads at lower lmax
-        // measured slower), and so does the packed FP64 path with room for one
-        // (lmax >= 8; N = 200, lmax 8: 8.37 ms against 9.93 ms; N = 60, lmax 9: 1.37 ms
-        // against 1.91 ms)
-        const bool wide = !split && !refl && !latt && !dense &&
+        // measured slower), and so do the packed FP64 and dense paths with room for
+        // one (lmax >= 8; packed N = 200, lmax 8: 8.37 ms against 9.93 ms; dense N = 60,
+        // lmax 9: 2.29 ms against 2.98 ms)
+        const bool wide = !split && !refl && !latt &&
                           (fp64_sums ? smem > 227 * 1024 / 2 : !ts && smem > 227 * 1024 / 3);
         const int nt = wide ? kAsmWideThreads : kAsmThreads;
         auto kfn = latt ? k_assemble<true, true, 2>
@@ -1216,7 +1216,8 @@ int launch_assemble(int nsys, const gb_system* sys, const double* pos, const dou
                                : split ? (dense ? k_assemble<true, true, 0, false, true>
                                                 : (fp64_sums ? k_assemble<false, true, 0, false, true>
                                                              : k_assemble<false, false, 0, false, true>))
-                                       : (dense ? k_assemble<true, true>
+                                       : (dense ? (wide ? k_assemble<true, true, 0, false, false, kAsmWideThreads>
+                                                        : k_assemble<true, true>)
                                                 : (fp64_sums ? (wide ? k_assemble<false, true, 0, false, false,
                                                                                   kAsmWideThreads>
                                                                      : k_assemble<false, true>)
